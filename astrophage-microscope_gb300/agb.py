@@ -1,0 +1,383 @@
+"""ctypes mirror of include/agb.h: the host-side interface of libagb.so.
+
+The structures are field-for-field copies of the C ABI; World wraps the
+engine's world handle with the reference's World operations
+(src/sim/world.cuh:183-243): create, spawn, import/export of the contract
+cell layout (contracts/cell_store_v1.h), step, per-stage calls and stats.
+Loading the library needs no GPU; every compute call does, and fails loudly
+(AgbError) when the CUDA engine cannot run.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libagb.so")
+
+ABI_VERSION = 1
+OK = 0
+STATUS_NAMES = ["Ok", "OutOfMemory", "CudaError", "InvalidArgument", "NotFound", "ParseError",
+                "ContractVersionMismatch", "CapacityExceeded", "FileIoError", "Unsupported",
+                "DeviceTimeout"]
+BC_DIRICHLET, BC_NEUMANN, BC_ROBIN = 0, 1, 2
+FIELD_T, FIELD_CO2, FIELD_N2, FIELD_IRR = 0, 1, 2, 3
+WALL_REFLECTING, WALL_PERIODIC, WALL_ABSORBING = 0, 1, 2
+GRAVITY_Y, GRAVITY_Z = 0, 1
+DIVIDE_CO2_QUOTA, DIVIDE_ENERGY = 0, 1
+PLACE_UNIFORM, PLACE_GAUSSIAN, PLACE_GRID, PLACE_DISC, PLACE_SLAB_X, PLACE_CLUSTERS = range(6)
+DIST_CONSTANT, DIST_UNIFORM, DIST_NORMAL, DIST_LOGNORMAL = range(4)
+STAGE_HASH, STAGE_THERMAL, STAGE_EMISSION, STAGE_MOTION = 0, 1, 2, 4
+STAGE_SLOW_FIELDS, STAGE_LIFECYCLE, STAGE_COMPACT, STAGE_CLOCK = 5, 6, 7, 8
+FLAG_OCCUPIED, FLAG_ALIVE, FLAG_AWAKE, FLAG_STUCK = 1, 2, 4, 8
+
+# Canon values the Python side needs (include/agb_canon.h).
+CELL_RADIUS = 5.0000000000000004e-06
+CELL_DIAMETER = 1.0000000000000001e-05
+CELL_ENERGY_MAX = 1500000.0
+DT_PHYSICS = 0.001
+AMBIENT_TEMP_DEFAULT = 293.14999999999998
+WATER_THERMAL_DIFFUSIVITY = 1.4325163582348751e-07
+CO2_DIFFUSIVITY_WATER = 1.92e-09
+N2_DIFFUSIVITY = 2.0e-9
+IRRADIANCE_NOMINAL_DIFFUSIVITY = 1.0e-9
+DEPOSIT_SCALE = (1.0e9, 1.0e15, 1.0e15, 1.0e18)
+CO2_MASS_PER_DIVISION = 2.0999999999999999e-14
+HASH_CELL_FACTOR = 2.2000000000000002
+
+
+class GridDesc(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
+                ("bc", C.c_int32 * 6), ("face_value", C.c_double * 6),
+                ("diffusivity", C.c_double), ("init", C.c_double), ("deposit_scale", C.c_double)]
+
+
+class Light(C.Structure):
+    _fields_ = [("dir_x", C.c_float), ("dir_y", C.c_float), ("dir_z", C.c_float),
+                ("irradiance", C.c_float), ("ambient", C.c_float), ("enabled", C.c_int32)]
+
+
+class WorldDesc(C.Structure):
+    _fields_ = [("abi_version", C.c_uint32),
+                ("chamber_w", C.c_double), ("chamber_h", C.c_double), ("chamber_d", C.c_double),
+                ("capacity", C.c_int32), ("seed", C.c_uint64),
+                ("boundary_x", C.c_int32), ("boundary_y", C.c_int32), ("gravity_axis", C.c_int32),
+                ("thermal_noise", C.c_uint8), ("contact_enabled", C.c_uint8),
+                ("adhesion_enabled", C.c_uint8), ("thermal_enabled", C.c_uint8),
+                ("emission_enabled", C.c_uint8), ("taxis_enabled", C.c_uint8),
+                ("occlusion_exact", C.c_uint8), ("compaction_enabled", C.c_uint8),
+                ("store_disposition", C.c_int32), ("ambient_temp", C.c_double),
+                ("grid", GridDesc * 4), ("hash_cell_size", C.c_double), ("light", Light),
+                ("physics_rate", C.c_double), ("biology_rate", C.c_double),
+                ("co2_mass_per_division", C.c_double),
+                ("division_predicate", C.c_int32), ("division_energy", C.c_double),
+                ("compaction_period", C.c_int32), ("trap_slot", C.c_int32),
+                ("trap_x", C.c_double), ("trap_y", C.c_double), ("trap_stiffness", C.c_double)]
+
+
+# The 25 arrays of contracts/cell_store_v1.h:42-75, in declaration order.
+CELL_FIELDS = [("id", np.uint64), ("flags", np.uint32), ("death_cause", np.uint8),
+               ("x", np.float64), ("y", np.float64), ("z", np.float64),
+               ("vx", np.float64), ("vy", np.float64), ("vz", np.float64),
+               ("energy", np.float64), ("temp_cell", np.float32), ("emit_power", np.float32),
+               ("dir_x", np.float32), ("dir_y", np.float32), ("dir_z", np.float32),
+               ("biomass", np.float64), ("co2_held", np.float64), ("age_s", np.float32),
+               ("rng_state", np.uint64), ("taxis_memory", np.float32), ("run_timer", np.float32),
+               ("t_local", np.float32), ("irradiance", np.float32), ("co2_local", np.float32),
+               ("n2_local", np.float32)]
+_CT = {np.uint64: C.c_uint64, np.uint32: C.c_uint32, np.uint8: C.c_uint8,
+       np.float64: C.c_double, np.float32: C.c_float}
+
+
+class Cells(C.Structure):
+    _fields_ = [(n, C.POINTER(_CT[t])) for n, t in CELL_FIELDS]
+
+
+class Spawn(C.Structure):
+    _fields_ = [("count", C.c_int32), ("placement", C.c_int32), ("charge_dist", C.c_int32),
+                ("awake", C.c_int32), ("place_x", C.c_double), ("place_y", C.c_double),
+                ("place_radius", C.c_double), ("charge_a", C.c_double), ("charge_b", C.c_double),
+                ("charge_max", C.c_double), ("clusters", C.c_int32), ("cluster_extent", C.c_double)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("tick", C.c_uint64), ("sim_time_s", C.c_double),
+                ("n_live", C.c_int32), ("n_dead", C.c_int32), ("n_dormant", C.c_int32),
+                ("n_awake", C.c_int32), ("n_taumoeba", C.c_int32),
+                ("mean_charge", C.c_double), ("total_energy_j", C.c_double),
+                ("mean_temp_cell_k", C.c_double), ("mean_temp_medium_k", C.c_double),
+                ("max_temp_medium_k", C.c_double), ("co2_total_kg", C.c_double),
+                ("n2_total_kg", C.c_double), ("mean_tau_tolerance", C.c_double),
+                ("divisions_this_window", C.c_int32), ("deaths_this_window", C.c_int32),
+                ("boil_events", C.c_int32), ("ignitions_this_window", C.c_int32),
+                ("physics_rate", C.c_double), ("biology_rate", C.c_double),
+                ("non_canon_run", C.c_uint8)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+def grid(n, nz, diffusivity, init, scale, bc, face_value=None):
+    g = GridDesc()
+    g.nx, g.ny, g.nz = n, n, nz
+    for f in range(6):
+        g.bc[f] = bc if isinstance(bc, int) else bc[f]
+        fv = init if face_value is None else face_value
+        g.face_value[f] = fv if not isinstance(fv, (list, tuple)) else fv[f]
+    g.diffusivity, g.init, g.deposit_scale = diffusivity, init, scale
+    return g
+
+
+def default_desc(capacity=25000, seed=20260802, co2_init=0.0):
+    """The reference world (src/sim/step.cu:9-78, src/sim/world.cuh:48-87):
+    4 mm x 4 mm x 60 um slab, 512^2 temperature (Robin at ambient), 256^2 CO2,
+    128^2 N2 and 512^2 irradiance grids, all depth-averaged (nz = 1).
+    Mirrors agb_world_desc_default() in the engine."""
+    d = WorldDesc()
+    d.abi_version = ABI_VERSION
+    d.chamber_w, d.chamber_h, d.chamber_d = 0.0040000000000000001, 0.0040000000000000001, 6.0000000000000002e-05
+    d.capacity, d.seed = capacity, seed
+    d.boundary_x = d.boundary_y = WALL_REFLECTING
+    d.gravity_axis = GRAVITY_Y
+    d.thermal_noise = d.contact_enabled = d.adhesion_enabled = 1
+    d.thermal_enabled = d.emission_enabled = d.taxis_enabled = d.occlusion_exact = 1
+    d.compaction_enabled = 0
+    d.store_disposition = 0
+    d.ambient_temp = AMBIENT_TEMP_DEFAULT
+    d.grid[FIELD_T] = grid(512, 1, WATER_THERMAL_DIFFUSIVITY, AMBIENT_TEMP_DEFAULT, DEPOSIT_SCALE[0], BC_ROBIN)
+    d.grid[FIELD_CO2] = grid(256, 1, CO2_DIFFUSIVITY_WATER, co2_init, DEPOSIT_SCALE[1], BC_NEUMANN)
+    d.grid[FIELD_N2] = grid(128, 1, N2_DIFFUSIVITY, 0.0, DEPOSIT_SCALE[2], BC_NEUMANN)
+    d.grid[FIELD_IRR] = grid(512, 1, IRRADIANCE_NOMINAL_DIFFUSIVITY, 0.0, DEPOSIT_SCALE[3], BC_NEUMANN)
+    d.hash_cell_size = HASH_CELL_FACTOR * CELL_DIAMETER
+    d.light = Light(1.0, 0.0, 0.0, 0.0, 0.0, 0)
+    d.physics_rate, d.biology_rate = 1.0, 1.0
+    d.co2_mass_per_division = CO2_MASS_PER_DIVISION
+    d.division_predicate, d.division_energy = DIVIDE_CO2_QUOTA, 0.0
+    d.compaction_period = 1
+    d.trap_slot, d.trap_x, d.trap_y, d.trap_stiffness = -1, 0.0, 0.0, 0.0
+    return d
+
+
+def spawn(count, placement=PLACE_UNIFORM, charge_dist=DIST_CONSTANT, awake=False,
+          place_x=0.0, place_y=0.0, place_radius=0.0, charge_a=0.0, charge_b=0.0,
+          charge_max=0.0, clusters=0, cluster_extent=0.0):
+    return Spawn(count, placement, charge_dist, int(bool(awake)), place_x, place_y, place_radius,
+                 charge_a, charge_b, charge_max, clusters, cluster_extent)
+
+
+class CellArrays:
+    """Host buffers in contract layout, one numpy array per SoA field."""
+
+    def __init__(self, n):
+        self.n = n
+        self.a = {name: np.zeros(max(n, 1), dtype=t) for name, t in CELL_FIELDS}
+
+    def struct(self):
+        c = Cells()
+        for name, t in CELL_FIELDS:
+            setattr(c, name, self.a[name].ctypes.data_as(C.POINTER(_CT[t])))
+        return c
+
+    def __getitem__(self, k):
+        return self.a[k][:self.n]
+
+    def copy(self):
+        o = CellArrays(self.n)
+        for k in self.a:
+            o.a[k][:] = self.a[k]
+        return o
+
+    @classmethod
+    def from_dict(cls, d):
+        n = len(d["id"])
+        o = cls(n)
+        for name, t in CELL_FIELDS:
+            o.a[name][:n] = np.asarray(d[name], dtype=t)
+        return o
+
+    def as_dict(self):
+        return {k: self.a[k][:self.n].copy() for k in self.a}
+
+
+class AgbError(RuntimeError):
+    pass
+
+
+def status_name(s):
+    return STATUS_NAMES[s] if 0 <= s < len(STATUS_NAMES) else "Unknown(%d)" % s
+
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load libagb.so (built by __graft_entry__.build()); raises if missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise AgbError("libagb.so not built at %s; run __graft_entry__.build()" % path)
+    lib = C.CDLL(path)
+    P, I32, U64 = C.c_void_p, C.c_int32, C.c_uint64
+    sigs = {
+        "agb_world_desc_default": (None, [C.POINTER(WorldDesc)]),
+        "agb_status_str": (C.c_char_p, [I32]),
+        "agb_last_error": (C.c_char_p, [P]),
+        "agb_device_info": (I32, [C.POINTER(I32), C.POINTER(I32), C.POINTER(I32)]),
+        "agb_world_create": (I32, [C.POINTER(WorldDesc), C.POINTER(P)]),
+        "agb_world_destroy": (None, [P]),
+        "agb_world_spawn": (I32, [P, C.POINTER(Spawn), P]),
+        "agb_world_import_cells": (I32, [P, C.POINTER(Cells), I32, U64, P]),
+        "agb_world_export_cells": (I32, [P, C.POINTER(Cells), I32, C.POINTER(I32), C.POINTER(U64), P]),
+        "agb_world_device_cells": (I32, [P, C.POINTER(Cells)]),
+        "agb_world_count": (I32, [P, C.POINTER(I32), P]),
+        "agb_world_import_field": (I32, [P, I32, P, P]),
+        "agb_world_export_field": (I32, [P, I32, P, P]),
+        "agb_world_export_deposit": (I32, [P, I32, P, P]),
+        "agb_world_step": (I32, [P, I32, P]),
+        "agb_world_step_graph": (I32, [P, I32, P]),
+        "agb_world_stage": (I32, [P, I32, P]),
+        "agb_world_diffuse": (I32, [P, I32, C.c_double, P]),
+        "agb_world_stats": (I32, [P, C.POINTER(Stats), P]),
+        "agb_world_stats_accum": (I32, [P, P]),
+        "agb_world_set_clock": (I32, [P, C.c_double, C.c_double]),
+        "agb_world_set_light": (I32, [P, C.POINTER(Light)]),
+        "agb_world_export_hash": (I32, [P, P, P, P, P, P, P]),
+        "agb_world_export_forces": (I32, [P, P, P, P, P]),
+        "agb_world_counters": (I32, [P, P, P]),
+    }
+    for name, (res, args) in sigs.items():
+        fn = getattr(lib, name)
+        fn.restype, fn.argtypes = res, args
+    _lib = lib
+    return lib
+
+
+def exported_symbols():
+    """Names declared in include/agb.h, for the symbol-export test."""
+    return ["agb_world_desc_default", "agb_status_str", "agb_last_error", "agb_device_info",
+            "agb_world_create", "agb_world_destroy", "agb_world_spawn", "agb_world_import_cells",
+            "agb_world_export_cells", "agb_world_device_cells", "agb_world_count",
+            "agb_world_import_field", "agb_world_export_field", "agb_world_export_deposit",
+            "agb_world_step", "agb_world_step_graph", "agb_world_stage", "agb_world_diffuse",
+            "agb_world_stats", "agb_world_stats_accum", "agb_world_set_clock",
+            "agb_world_set_light", "agb_world_export_hash", "agb_world_export_forces",
+            "agb_world_counters"]
+
+
+def field_shape(desc, f):
+    g = desc.grid[f]
+    return (g.nz, g.ny, g.nx)
+
+
+class World:
+    """One engine world (the reference's World) on the current CUDA device."""
+
+    def __init__(self, desc, lib=None):
+        self.lib = lib or load()
+        self.desc = desc
+        h = C.c_void_p()
+        self._check(self.lib.agb_world_create(C.byref(desc), C.byref(h)), "agb_world_create")
+        self.h = h
+
+    def _check(self, rc, what):
+        if rc != OK:
+            detail = ""
+            if getattr(self, "h", None):
+                msg = self.lib.agb_last_error(self.h)
+                detail = msg.decode() if msg else ""
+            raise AgbError("%s failed: %s %s" % (what, status_name(rc), detail))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.agb_world_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def spawn(self, p):
+        self._check(self.lib.agb_world_spawn(self.h, C.byref(p), None), "spawn")
+
+    def import_cells(self, cells, next_id):
+        s = cells.struct()
+        self._check(self.lib.agb_world_import_cells(self.h, C.byref(s), cells.n, next_id, None), "import_cells")
+
+    def export_cells(self):
+        n = self.count()
+        cells = CellArrays(n)
+        s = cells.struct()
+        cnt, nid = C.c_int32(), C.c_uint64()
+        self._check(self.lib.agb_world_export_cells(self.h, C.byref(s), n, C.byref(cnt), C.byref(nid), None),
+                    "export_cells")
+        return cells, nid.value
+
+    def count(self):
+        c = C.c_int32()
+        self._check(self.lib.agb_world_count(self.h, C.byref(c), None), "count")
+        return c.value
+
+    def import_field(self, f, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float32)
+        self._check(self.lib.agb_world_import_field(self.h, f, a.ctypes.data, None), "import_field")
+
+    def export_field(self, f):
+        out = np.zeros(field_shape(self.desc, f), dtype=np.float32)
+        self._check(self.lib.agb_world_export_field(self.h, f, out.ctypes.data, None), "export_field")
+        return out
+
+    def export_deposit(self, f):
+        out = np.zeros(field_shape(self.desc, f), dtype=np.uint64)
+        self._check(self.lib.agb_world_export_deposit(self.h, f, out.ctypes.data, None), "export_deposit")
+        return out
+
+    def step(self, ticks=1, graph=False):
+        fn = self.lib.agb_world_step_graph if graph else self.lib.agb_world_step
+        self._check(fn(self.h, ticks, None), "step")
+
+    def stage(self, s):
+        self._check(self.lib.agb_world_stage(self.h, s, None), "stage %d" % s)
+
+    def diffuse(self, f, dt):
+        self._check(self.lib.agb_world_diffuse(self.h, f, dt, None), "diffuse")
+
+    def stats(self):
+        s = Stats()
+        self._check(self.lib.agb_world_stats(self.h, C.byref(s), None), "stats")
+        return s
+
+    def stats_accum(self):
+        out = np.zeros(12, dtype=np.uint64)
+        self._check(self.lib.agb_world_stats_accum(self.h, out.ctypes.data), "stats_accum")
+        return out
+
+    def set_clock(self, physics, biology):
+        self._check(self.lib.agb_world_set_clock(self.h, physics, biology), "set_clock")
+
+    def export_hash(self):
+        dims = np.zeros(4, dtype=np.int32)
+        self._check(self.lib.agb_world_export_hash(self.h, dims.ctypes.data, None, None, None, None, None),
+                    "export_hash")
+        n = self.count()
+        ks = np.zeros(max(n, 1), np.uint32)
+        vs = np.zeros(max(n, 1), np.uint32)
+        bs = np.zeros(int(dims[3]), np.int32)
+        be = np.zeros(int(dims[3]), np.int32)
+        self._check(self.lib.agb_world_export_hash(self.h, dims.ctypes.data, ks.ctypes.data, vs.ctypes.data,
+                                                   bs.ctypes.data, be.ctypes.data, None), "export_hash")
+        return dims, ks[:n], vs[:n], bs, be
+
+    def export_forces(self):
+        n = self.count()
+        f = [np.zeros(max(n, 1), np.float32) for _ in range(3)]
+        self._check(self.lib.agb_world_export_forces(self.h, f[0].ctypes.data, f[1].ctypes.data,
+                                                     f[2].ctypes.data, None), "export_forces")
+        return [a[:n] for a in f]
+
+    def counters(self):
+        out = np.zeros(4, dtype=np.int64)
+        self._check(self.lib.agb_world_counters(self.h, out.ctypes.data, None), "counters")
+        return out

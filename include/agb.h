@@ -1,0 +1,271 @@
+/*
+ * include/agb.h -- C ABI of the GB300 per-tick physics engine (libagb.so).
+ *
+ * The engine is a drop-in for the simulator's src/sim + src/fields hot path:
+ * the spatial hash, thermal coupling + FTCS conduction, the shadowing sweep and
+ * feeding, contact forces + the exact Ornstein-Uhlenbeck integrator, CO2 uptake,
+ * death, division and stable compaction, and the fixed-point telemetry
+ * reduction. Plain C types only; every entry point returns an agb_status.
+ *
+ * Conventions
+ *   - Host buffers are caller-owned; device buffers are engine-owned and are
+ *     allocated once at agb_world_create (zero steady-state allocation, the
+ *     reference's T29 rule, tests/physics/test_perf.cu:28-74).
+ *   - All work is enqueued on the caller's stream; only the explicit export,
+ *     stats and count calls synchronise with the host. agb_world_step() never
+ *     waits on the device (the reference waits 2-3 times per tick,
+ *     src/sim/lifecycle.cu:250-252 and src/sim/cell_store.cu:428).
+ *   - One world handle per host thread.
+ *   - Status codes 0..9 are astro::Status (src/core/result.h:12-24) one-for-one.
+ */
+#ifndef AGB_H
+#define AGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AGB_ABI_VERSION 1u
+
+typedef int32_t agb_status;
+enum {
+    AGB_OK = 0,
+    AGB_OUT_OF_MEMORY = 1,
+    AGB_CUDA_ERROR = 2,
+    AGB_INVALID_ARGUMENT = 3,
+    AGB_NOT_FOUND = 4,
+    AGB_PARSE_ERROR = 5,
+    AGB_CONTRACT_VERSION_MISMATCH = 6,
+    AGB_CAPACITY_EXCEEDED = 7,
+    AGB_FILE_IO_ERROR = 8,
+    AGB_UNSUPPORTED = 9,
+    /* Not in astro::Status: a bounded device-side wait gave up. */
+    AGB_DEVICE_TIMEOUT = 10
+};
+
+/* Same object as cudaStream_t; NULL is the legacy default stream. */
+typedef struct CUstream_st* agb_stream;
+
+typedef struct agb_world agb_world;
+
+/* contracts/fields_v1.h:23-27 */
+enum { AGB_BC_DIRICHLET = 0, AGB_BC_NEUMANN = 1, AGB_BC_ROBIN = 2 };
+/* contracts/fields_v1.h:15-21 */
+enum { AGB_FIELD_TEMPERATURE = 0, AGB_FIELD_CO2 = 1, AGB_FIELD_N2 = 2, AGB_FIELD_IRRADIANCE = 3,
+       AGB_FIELD_COUNT = 4 };
+/* src/sim/integrator.cuh:227 Boundary, :175 GravityAxis */
+enum { AGB_WALL_REFLECTING = 0, AGB_WALL_PERIODIC = 1, AGB_WALL_ABSORBING = 2 };
+enum { AGB_GRAVITY_Y = 0, AGB_GRAVITY_Z = 1 };
+/* contracts/scenario_v3.h:35 StoreDisposition */
+enum { AGB_STORE_VOID = 0, AGB_STORE_FLASH = 1, AGB_STORE_RETAIN = 2 };
+/* Division predicate. CO2 quota is the reference (src/sim/lifecycle.cuh:33-36);
+ * the stored-energy threshold is an opt-in extension, not reference behaviour. */
+enum { AGB_DIVIDE_CO2_QUOTA = 0, AGB_DIVIDE_ENERGY = 1 };
+/* Face order of agb_grid_desc.bc / face_value. */
+enum { AGB_FACE_XMIN = 0, AGB_FACE_XMAX = 1, AGB_FACE_YMIN = 2, AGB_FACE_YMAX = 3,
+       AGB_FACE_ZMIN = 4, AGB_FACE_ZMAX = 5 };
+
+/*
+ * One scalar field on a regular grid (src/fields/grid.cuh:72-85 Grid2D,
+ * contracts/fields_v1.h:81-91 FieldView). The x spacing is dx = chamber_w / nx
+ * and y uses the same dx, as in the reference. nz == 1 is the reference's
+ * depth-averaged 2-D grid, bit for bit; nz > 1 is a 3-D grid with
+ * dz = chamber_d / nz, which must equal dx (isotropic 7-point stencil).
+ * nx == 0 disables the field (it is then never sampled, diffused or stored).
+ */
+typedef struct agb_grid_desc {
+    int32_t nx, ny, nz;
+    int32_t bc[6];            /* per face, AGB_FACE_* order; the reference uses one bc for all */
+    double face_value[6];     /* Dirichlet value / Robin reference temperature per face */
+    double diffusivity;       /* [m^2/s] */
+    double init;              /* uniform initial value (the reference fills with its ambient) */
+    double deposit_scale;     /* fixed-point scale of the deposit accumulator */
+} agb_grid_desc;
+
+/* contracts/fields_v1.h:106-111 LightSource + World::ambient_irradiance.
+ * The sweep runs along the dominant axis of dir (ties: x, then y, then z);
+ * the reference only has in-plane x/y light (src/sim/emission.cu:161-163). */
+typedef struct agb_light {
+    float dir_x, dir_y, dir_z;
+    float irradiance;         /* [W/m^2] at the illuminated boundary */
+    float ambient;            /* [W/m^2] isotropic ambient */
+    int32_t enabled;
+} agb_light;
+
+/* WorldDesc + MotionConfig + the World knobs the tick reads
+ * (src/sim/world.cuh:48-180). agb_world_desc_default() fills the reference's
+ * defaults (src/sim/step.cu:9-78, src/sim/world.cuh:48-87). */
+typedef struct agb_world_desc {
+    uint32_t abi_version;     /* AGB_ABI_VERSION */
+    double chamber_w, chamber_h, chamber_d;   /* [m], centred on the origin */
+    int32_t capacity;         /* cell slots */
+    uint64_t seed;
+    int32_t boundary_x, boundary_y, gravity_axis;
+    uint8_t thermal_noise, contact_enabled, adhesion_enabled, thermal_enabled;
+    uint8_t emission_enabled, taxis_enabled, occlusion_exact, compaction_enabled;
+    int32_t store_disposition;
+    double ambient_temp;      /* [K] */
+    agb_grid_desc grid[AGB_FIELD_COUNT];
+    double hash_cell_size;    /* [m]; the reference uses HASH_CELL_FACTOR * CELL_DIAMETER */
+    agb_light light;
+    double physics_rate, biology_rate;
+    double co2_mass_per_division;             /* [kg] World override, canon by default */
+    /* Extensions; the defaults reproduce the reference. */
+    int32_t division_predicate;               /* AGB_DIVIDE_* */
+    double division_energy;                   /* [J] threshold for AGB_DIVIDE_ENERGY */
+    int32_t compaction_period;                /* ticks between compaction checks; 1 = reference */
+    int32_t trap_slot;                        /* optical trap (World::trap_*); -1 = off */
+    double trap_x, trap_y, trap_stiffness;
+} agb_world_desc;
+
+/* Host view of the 25 SoA arrays of contracts/cell_store_v1.h:42-75, field for
+ * field. Any pointer may be NULL in export calls (that array is skipped). */
+typedef struct agb_cells {
+    uint64_t* id;
+    uint32_t* flags;
+    uint8_t* death_cause;
+    double *x, *y, *z;
+    double *vx, *vy, *vz;
+    double* energy;
+    float* temp_cell;
+    float* emit_power;
+    float *dir_x, *dir_y, *dir_z;
+    double* biomass;
+    double* co2_held;
+    float* age_s;
+    uint64_t* rng_state;
+    float* taxis_memory;
+    float* run_timer;
+    float* t_local;
+    float* irradiance;
+    float* co2_local;
+    float* n2_local;
+} agb_cells;
+
+/* src/sim/cell_store.cuh:15-28 SpawnParams. Placements 0-3 and distributions
+ * 0-2 are the reference's (src/sim/cell_store.cu:42-130); the rest generate the
+ * benchmark workloads and are extensions:
+ *   AGB_PLACE_SLAB_X   x uniform in place_x +- place_radius, y over the chamber,
+ *                      z as the reference (uniform through the depth);
+ *   AGB_PLACE_CLUSTERS a 3-D Gaussian mixture: `clusters` centres uniform in a
+ *                      cube of edge cluster_extent, sigma = place_radius;
+ *   AGB_DIST_LOGNORMAL charge = exp(ln(charge_a) + charge_b * N(0,1)).
+ * charge_max > 0 clips the charge from above after the reference's clamp to [0,1]. */
+enum { AGB_PLACE_UNIFORM = 0, AGB_PLACE_GAUSSIAN = 1, AGB_PLACE_GRID = 2, AGB_PLACE_DISC = 3,
+       AGB_PLACE_SLAB_X = 4, AGB_PLACE_CLUSTERS = 5 };
+enum { AGB_DIST_CONSTANT = 0, AGB_DIST_UNIFORM = 1, AGB_DIST_NORMAL = 2, AGB_DIST_LOGNORMAL = 3 };
+typedef struct agb_spawn {
+    int32_t count, placement, charge_dist, awake;
+    double place_x, place_y, place_radius;
+    double charge_a, charge_b;
+    double charge_max;
+    int32_t clusters;
+    double cluster_extent;
+} agb_spawn;
+
+/* contracts/telemetry_v1.h:17-39 Stats, same members in the same order. */
+typedef struct agb_stats {
+    uint64_t tick;
+    double sim_time_s;
+    int32_t n_live, n_dead, n_dormant, n_awake, n_taumoeba;
+    double mean_charge;
+    double total_energy_j;
+    double mean_temp_cell_k;
+    double mean_temp_medium_k;
+    double max_temp_medium_k;
+    double co2_total_kg;
+    double n2_total_kg;
+    double mean_tau_tolerance;
+    int32_t divisions_this_window;
+    int32_t deaths_this_window;
+    int32_t boil_events;
+    int32_t ignitions_this_window;
+    double physics_rate, biology_rate;
+    uint8_t non_canon_run;
+} agb_stats;
+
+/* Stages of world_step (src/sim/step.cu:109-184), for stage-level parity. */
+enum {
+    AGB_STAGE_HASH = 0,        /* hash_build, src/sim/hash.cu:106-133 */
+    AGB_STAGE_THERMAL = 1,     /* thermal_step, src/sim/thermal.cu:75-103 */
+    AGB_STAGE_EMISSION = 2,    /* emission_step, src/sim/emission.cu:119-177 */
+    AGB_STAGE_MOTION = 4,      /* motion_step, src/sim/integrator.cu:154-177 */
+    AGB_STAGE_SLOW_FIELDS = 5, /* CO2/N2 flush + diffuse, src/sim/step.cu:168-171 */
+    AGB_STAGE_LIFECYCLE = 6,   /* lifecycle_step, src/sim/lifecycle.cu:208-294 */
+    AGB_STAGE_COMPACT = 7,     /* cell_store_compact, src/sim/cell_store.cu:414-456 */
+    AGB_STAGE_CLOCK = 8        /* ++tick; sim_time += dt, src/sim/step.cu:182-183 */
+};
+
+/* Reference defaults: 4 mm x 4 mm x 60 um slab, 512^2 temperature (Robin),
+ * 256^2 CO2, 128^2 N2 and 512^2 irradiance grids (all nz = 1), canon hash. */
+void agb_world_desc_default(agb_world_desc* d);
+
+const char* agb_status_str(agb_status s);
+const char* agb_last_error(const agb_world* w);
+/* CUDA device the engine runs on and its compute capability (e.g. 103). */
+agb_status agb_device_info(int32_t* device, int32_t* sm_version, int32_t* sm_count);
+
+/* world_create / world_destroy (src/sim/world.cuh:222-223). */
+agb_status agb_world_create(const agb_world_desc* d, agb_world** out);
+void agb_world_destroy(agb_world* w);
+
+/* cell_store_spawn (src/sim/cell_store.cuh:73): appends p->count seeded cells. */
+agb_status agb_world_spawn(agb_world* w, const agb_spawn* p, agb_stream s);
+
+/* Replace the whole population with `count` cells in contract layout; next_id
+ * is the id the next daughter gets (CellStore::next_id). */
+agb_status agb_world_import_cells(agb_world* w, const agb_cells* src, int32_t count,
+                                  uint64_t next_id, agb_stream s);
+/* Copy up to max_count cells out; writes the live upper bound and next_id. Syncs. */
+agb_status agb_world_export_cells(agb_world* w, agb_cells* dst, int32_t max_count,
+                                  int32_t* count, uint64_t* next_id, agb_stream s);
+/* Device pointers of the SoA (the reference's CellStore::view); count via agb_world_count. */
+agb_status agb_world_device_cells(agb_world* w, agb_cells* dev);
+agb_status agb_world_count(agb_world* w, int32_t* count, agb_stream s);
+
+/* Field values, nx*ny*nz floats, x fastest (reference: [x + n*y]). */
+agb_status agb_world_import_field(agb_world* w, int32_t field, const float* src, agb_stream s);
+agb_status agb_world_export_field(agb_world* w, int32_t field, float* dst, agb_stream s);
+/* Raw fixed-point accumulator (irradiance: the occlusion stamp of the last emission stage). */
+agb_status agb_world_export_deposit(agb_world* w, int32_t field, uint64_t* dst, agb_stream s);
+
+/* world_step x ticks (src/sim/step.cu:109-184). No host synchronisation. */
+agb_status agb_world_step(agb_world* w, int32_t ticks, agb_stream s);
+/* Capture `ticks` ticks once as a CUDA graph and replay it on later calls with
+ * the same tick count: one launch per call. */
+agb_status agb_world_step_graph(agb_world* w, int32_t ticks, agb_stream s);
+/* One stage of the tick at the world's dt (AGB_STAGE_*). */
+agb_status agb_world_stage(agb_world* w, int32_t stage, agb_stream s);
+/* grid_diffuse on one field for dt (src/fields/diffuse.cu:159-186). */
+agb_status agb_world_diffuse(agb_world* w, int32_t field, double dt, agb_stream s);
+
+/* world_stats (src/sim/stats.cu:102-153): fixed-point reduction + window counters. Syncs. */
+agb_status agb_world_stats(agb_world* w, agb_stats* out, agb_stream s);
+/* The raw fixed-point sums of the last agb_world_stats, StatsAccum order
+ * (src/sim/world.cuh:39-45): energy, temp_cell, temp_medium, co2, n2, max_temp,
+ * tau_tolerance, n_alive, n_dead, n_awake, n_dormant, n_taumoeba. */
+agb_status agb_world_stats_accum(agb_world* w, uint64_t out[12]);
+
+/* world_set_clock with explicit rates (src/sim/step.cu:196-205, clamped). */
+agb_status agb_world_set_clock(agb_world* w, double physics_rate, double biology_rate);
+agb_status agb_world_set_light(agb_world* w, const agb_light* light);
+
+/* Hash state after the last hash stage: dims = {nx, ny, nz, bucket_count};
+ * keys/vals in sorted order (count entries); bucket_start/end dense
+ * (bucket_count entries, empty buckets 0/0 as in src/sim/hash.cu:110-113). Syncs. */
+agb_status agb_world_export_hash(agb_world* w, int32_t dims[4], uint32_t* keys_sorted,
+                                 uint32_t* vals_sorted, int32_t* bucket_start,
+                                 int32_t* bucket_end, agb_stream s);
+/* Net force per slot of the last motion stage (World::d_fx/fy/fz). Syncs. */
+agb_status agb_world_export_forces(agb_world* w, float* fx, float* fy, float* fz, agb_stream s);
+/* Device counters: {divisions_this_window, deaths_total, dead_slots_prev,
+ * device error word}. Syncs. */
+agb_status agb_world_counters(agb_world* w, int64_t out[4], agb_stream s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AGB_H */

@@ -1,0 +1,1333 @@
+/*
+ * oracle/oracle.c -- CPU oracle of the per-tick physics step (test infrastructure).
+ *
+ * A plain-C restatement of the reference's kernel bodies in the reference's own
+ * FP64 arithmetic; each function names the reference file:line it follows.
+ * Float expressions are written in the reference's evaluation order and the
+ * file is compiled with -ffp-contract=off, so FP32 field arithmetic matches the
+ * reference (and the CUDA engine, which uses explicitly rounded operations)
+ * bit for bit. Generalisations beyond the reference (3-D grids, per-face
+ * boundary conditions, a z light axis, the energy division predicate, the
+ * compaction period, the extra spawn distributions) are marked EXTENSION.
+ *
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline use it.
+ */
+#include "oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../include/agb_canon.h"
+
+/* ------------------------------------------------------------------------- */
+/* RNG: src/core/rng.cuh:23-117                                               */
+/* ------------------------------------------------------------------------- */
+typedef struct { uint64_t state, inc; } pcg32;
+
+static uint64_t splitmix64(uint64_t x) {                  /* rng.cuh:23-28 */
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+static uint32_t pcg32_next(pcg32* r) {                    /* rng.cuh:35-41 */
+    const uint64_t old = r->state;
+    r->state = old * 6364136223846793005ull + r->inc;
+    const uint32_t xs = (uint32_t)(((old >> 18) ^ old) >> 27);
+    const uint32_t rot = (uint32_t)(old >> 59);
+    return (xs >> rot) | (xs << ((0u - rot) & 31u));
+}
+
+static pcg32 pcg32_seed(uint64_t initstate, uint64_t initseq) {   /* rng.cuh:44-50 */
+    pcg32 r = {0ull, (initseq << 1u) | 1u};
+    pcg32_next(&r);
+    r.state += initstate;
+    pcg32_next(&r);
+    return r;
+}
+
+static uint64_t cell_stream_inc(uint64_t id) {            /* rng.cuh:54-56 */
+    return (splitmix64(id ^ 0xA5A5A5A5DEADBEEFull) << 1u) | 1u;
+}
+static pcg32 cell_rng(uint64_t state, uint64_t id) {      /* rng.cuh:58-60 */
+    pcg32 r = {state, cell_stream_inc(id)};
+    return r;
+}
+static uint64_t cell_rng_init(uint64_t seed, uint64_t id) {   /* rng.cuh:62-65 */
+    return pcg32_seed(seed ^ splitmix64(id), splitmix64(id + 1)).state;
+}
+static uint64_t pcg_split(uint64_t parent, uint64_t did) {    /* rng.cuh:69-71 */
+    return splitmix64(parent ^ splitmix64(did * 0x2545F4914F6CDD1Dull));
+}
+static double uniform01d(pcg32* r) {                      /* rng.cuh:80-84 */
+    const uint64_t hi = (uint64_t)pcg32_next(r) << 21;
+    const uint64_t lo = (uint64_t)pcg32_next(r) >> 11;
+    return (double)((hi ^ lo) & ((1ull << 53) - 1)) * (1.0 / 9007199254740992.0);
+}
+static double uniform_range(pcg32* r, double lo, double hi) {   /* rng.cuh:86-88 */
+    return lo + (hi - lo) * uniform01d(r);
+}
+static void gaussian_pair(pcg32* r, double* z0, double* z1) {   /* rng.cuh:92-101 */
+    double u1 = uniform01d(r);
+    if (u1 < 1.0e-300) u1 = 1.0e-300;
+    const double u2 = uniform01d(r);
+    const double mag = sqrt(-2.0 * log(u1));
+    const double ang = 6.283185307179586476925286766559 * u2;
+    *z0 = mag * cos(ang);
+    *z1 = mag * sin(ang);
+}
+static double gaussian(pcg32* r) { double a, b; gaussian_pair(r, &a, &b); return a; }
+
+void orc_pcg32_seed_draws(uint64_t s, uint64_t q, int32_t n, uint32_t* out) {
+    pcg32 r = pcg32_seed(s, q);
+    for (int32_t i = 0; i < n; ++i) out[i] = pcg32_next(&r);
+}
+uint64_t orc_cell_rng_init(uint64_t seed, uint64_t id) { return cell_rng_init(seed, id); }
+uint64_t orc_pcg_split(uint64_t p, uint64_t d) { return pcg_split(p, d); }
+
+/* ------------------------------------------------------------------------- */
+/* Small vector + fixed point: src/core/vec.cuh, src/core/fixed_atomic.cuh    */
+/* ------------------------------------------------------------------------- */
+typedef struct { double x, y, z; } vec3;
+static vec3 v3(double x, double y, double z) { vec3 r = {x, y, z}; return r; }
+static vec3 vsub(vec3 a, vec3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+static vec3 vscale(vec3 a, double s) { return v3(a.x * s, a.y * s, a.z * s); }
+static double vdot(vec3 a, vec3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static vec3 vnormalize(vec3 a) {                          /* vec.cuh:34-37 */
+    const double l = sqrt(vdot(a, a));
+    return l > 0.0 ? vscale(a, 1.0 / l) : v3(0.0, 0.0, 1.0);
+}
+
+static int64_t to_fixed(double v, double scale) { return (int64_t)llround(v * scale); } /* fixed_atomic.cuh:27-29 */
+static double from_fixed(uint64_t raw, double scale) { return (double)(int64_t)raw / scale; } /* :31-33 */
+
+static void deposit_add(uint64_t* acc, double value, double scale) {   /* fixed_atomic.cuh:38-40 */
+    const uint64_t v = (uint64_t)to_fixed(value, scale);
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+    *acc += v;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Grids: src/fields/grid.cuh, src/fields/diffuse.cu                          */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+    int enabled;
+    int32_t nx, ny, nz;
+    int64_t count;
+    double dx, dz, dz_eff, diffusivity, deposit_scale, robin;
+    float dxf, dzf, robinf;
+    int32_t bc[6];
+    float facef[6];
+    float* value;
+    float* scratch;
+    uint64_t* deposit;
+} grid;
+
+static int grid_init(grid* g, const agb_grid_desc* d, double chamber_w, double chamber_d) {
+    memset(g, 0, sizeof(*g));
+    if (d->nx <= 0) return 0;
+    if (d->nx <= 1 || d->ny <= 1 || d->nz < 1) return AGB_INVALID_ARGUMENT;   /* diffuse.cu:94 */
+    g->enabled = 1;
+    g->nx = d->nx; g->ny = d->ny; g->nz = d->nz;
+    g->count = (int64_t)d->nx * d->ny * d->nz;
+    g->dx = chamber_w / (double)d->nx;                     /* diffuse.cu:97 */
+    g->dz_eff = chamber_d / (double)d->nz;                 /* nz == 1: the full depth */
+    g->dz = d->nz > 1 ? g->dz_eff : 0.0;
+    if (d->nz > 1 && fabs(g->dz / g->dx - 1.0) > 1e-9) return AGB_UNSUPPORTED;
+    g->diffusivity = d->diffusivity;
+    g->deposit_scale = d->deposit_scale;
+    g->robin = g->dx * AGB_AIR_CONVECTION_H / AGB_WATER_CONDUCTIVITY;   /* diffuse.cu:102 */
+    g->dxf = (float)g->dx;                                  /* grid_view, diffuse.cu:198 */
+    g->dzf = (float)g->dz;
+    g->robinf = (float)g->robin;
+    for (int f = 0; f < 6; ++f) { g->bc[f] = d->bc[f]; g->facef[f] = (float)d->face_value[f]; }
+    g->value = (float*)malloc(sizeof(float) * g->count);
+    g->scratch = (float*)malloc(sizeof(float) * g->count);
+    g->deposit = (uint64_t*)calloc((size_t)g->count, sizeof(uint64_t));
+    if (!g->value || !g->scratch || !g->deposit) return AGB_OUT_OF_MEMORY;
+    const float fill = (float)d->init;                      /* grid_fill, diffuse.cu:128-134 */
+    for (int64_t i = 0; i < g->count; ++i) g->value[i] = g->scratch[i] = fill;
+    return 0;
+}
+
+static void grid_free(grid* g) { free(g->value); free(g->scratch); free(g->deposit); }
+
+/* grid_sample, grid.cuh:109-125 (bilinear); EXTENSION: trilinear for nz > 1
+ * as a z-lerp of two reference bilinears. */
+static float bilerp(const float* v, int32_t nx, int32_t ny, int32_t x0, int32_t y0, float tx, float ty) {
+    const int32_t x1 = x0 + 1, y1 = y0 + 1;
+    const int32_t xa = x0 < 0 ? 0 : (x0 >= nx ? nx - 1 : x0), xb = x1 < 0 ? 0 : (x1 >= nx ? nx - 1 : x1);
+    const int32_t ya = y0 < 0 ? 0 : (y0 >= ny ? ny - 1 : y0), yb = y1 < 0 ? 0 : (y1 >= ny ? ny - 1 : y1);
+    return (1.0f - tx) * (1.0f - ty) * v[ya * nx + xa] + tx * (1.0f - ty) * v[ya * nx + xb] +
+           (1.0f - tx) * ty * v[yb * nx + xa] + tx * ty * v[yb * nx + xb];
+}
+
+static float grid_sample(const grid* g, float x, float y, float z) {
+    const float hx = 0.5f * g->nx * g->dxf;
+    const float hy = 0.5f * g->ny * g->dxf;
+    const float gx = (x + hx) / g->dxf - 0.5f;
+    const float gy = (y + hy) / g->dxf - 0.5f;
+    const int32_t x0 = (int32_t)floorf(gx);
+    const int32_t y0 = (int32_t)floorf(gy);
+    const float tx = gx - (float)x0;
+    const float ty = gy - (float)y0;
+    if (g->nz == 1) return bilerp(g->value, g->nx, g->ny, x0, y0, tx, ty);
+    const float hz = 0.5f * g->nz * g->dzf;
+    const float gz = (z + hz) / g->dzf - 0.5f;
+    const int32_t z0 = (int32_t)floorf(gz);
+    const float tz = gz - (float)z0;
+    const int32_t za = z0 < 0 ? 0 : (z0 >= g->nz ? g->nz - 1 : z0);
+    const int32_t zb = z0 + 1 < 0 ? 0 : (z0 + 1 >= g->nz ? g->nz - 1 : z0 + 1);
+    const int64_t plane = (int64_t)g->nx * g->ny;
+    const float b0 = bilerp(g->value + za * plane, g->nx, g->ny, x0, y0, tx, ty);
+    const float b1 = bilerp(g->value + zb * plane, g->nx, g->ny, x0, y0, tx, ty);
+    return (1.0f - tz) * b0 + tz * b1;
+}
+
+/* grid_index_nearest, grid.cuh:134-141; EXTENSION: k from z for nz > 1. */
+static int64_t grid_nearest(const grid* g, float x, float y, float z) {
+    const float hx = 0.5f * g->nx * g->dxf;
+    const float hy = 0.5f * g->ny * g->dxf;
+    int32_t i = (int32_t)((x + hx) / g->dxf);
+    int32_t j = (int32_t)((y + hy) / g->dxf);
+    i = i < 0 ? 0 : (i >= g->nx ? g->nx - 1 : i);
+    j = j < 0 ? 0 : (j >= g->ny ? g->ny - 1 : j);
+    int32_t k = 0;
+    if (g->nz > 1) {
+        const float hz = 0.5f * g->nz * g->dzf;
+        k = (int32_t)((z + hz) / g->dzf);
+        k = k < 0 ? 0 : (k >= g->nz ? g->nz - 1 : k);
+    }
+    return (int64_t)i + (int64_t)g->nx * ((int64_t)j + (int64_t)g->ny * k);
+}
+
+/* flush_kernel, diffuse.cu:51-60 */
+static void grid_flush(grid* g) {
+    if (!g->enabled) return;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int64_t i = 0; i < g->count; ++i) {
+        const uint64_t raw = g->deposit[i];
+        if (raw != 0ull) {
+            g->value[i] += (float)from_fixed(raw, g->deposit_scale);
+            g->deposit[i] = 0ull;
+        }
+    }
+}
+
+/* diffuse_kernel's ghost, diffuse.cu:27-36, per face (EXTENSION: a bc per face). */
+static float ghost(const grid* g, int face, float c) {
+    if (g->bc[face] == AGB_BC_DIRICHLET) return g->facef[face];
+    if (g->bc[face] == AGB_BC_ROBIN) return c - g->robinf * (c - g->facef[face]);
+    return c;
+}
+
+/* diffuse_kernel, diffuse.cu:19-44: one explicit pass value -> scratch, then the
+ * ping-pong swap of grid_diffuse_substep (:153-155). EXTENSION: 7-point for nz > 1. */
+static void grid_pass(grid* g, float coeff) {
+    const int32_t nx = g->nx, ny = g->ny, nz = g->nz;
+    const int64_t plane = (int64_t)nx * ny;
+    const float* src = g->value;
+    float* dst = g->scratch;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) collapse(2)
+#endif
+    for (int32_t k = 0; k < nz; ++k)
+        for (int32_t j = 0; j < ny; ++j)
+            for (int32_t i = 0; i < nx; ++i) {
+                const int64_t idx = (int64_t)i + (int64_t)nx * j + plane * k;
+                const float c = src[idx];
+                const float l = (i > 0) ? src[idx - 1] : ghost(g, AGB_FACE_XMIN, c);
+                const float r = (i < nx - 1) ? src[idx + 1] : ghost(g, AGB_FACE_XMAX, c);
+                const float d = (j > 0) ? src[idx - nx] : ghost(g, AGB_FACE_YMIN, c);
+                const float u = (j < ny - 1) ? src[idx + nx] : ghost(g, AGB_FACE_YMAX, c);
+                if (nz == 1) {
+                    dst[idx] = c + coeff * (l + r + d + u - 4.0f * c);
+                } else {
+                    const float b = (k > 0) ? src[idx - plane] : ghost(g, AGB_FACE_ZMIN, c);
+                    const float f = (k < nz - 1) ? src[idx + plane] : ghost(g, AGB_FACE_ZMAX, c);
+                    dst[idx] = c + coeff * (l + r + d + u + b + f - 6.0f * c);
+                }
+            }
+    float* t = g->value; g->value = g->scratch; g->scratch = t;
+}
+
+/* substeps_for_dt, grid.cuh:51-53; 3-D uses the 1/6 bound (EXTENSION). */
+static int32_t grid_substeps(const grid* g, double dt) {
+    const double lim = g->nz > 1 ? 6.0 : 4.0;
+    return (int32_t)(dt / (g->dx * g->dx / (lim * g->diffusivity))) + 1;
+}
+static float grid_coeff(const grid* g, double dt_sub) {
+    return (float)(g->diffusivity * dt_sub / (g->dx * g->dx));     /* diffuse.cu:145,167 */
+}
+static int coeff_stable(const grid* g, float c) {
+    return g->nz > 1 ? (c <= (float)(1.0 / 6.0)) : (c <= 0.25f);   /* diffuse.cu:146,172 */
+}
+
+/* grid_diffuse, diffuse.cu:159-186 */
+static int grid_diffuse(grid* g, double dt) {
+    if (!g->enabled) return 0;
+    const int32_t steps = grid_substeps(g, dt);
+    if (steps <= 0) return 0;
+    const double dt_sub = dt / steps;
+    const float coeff = grid_coeff(g, dt_sub);
+    if (!coeff_stable(g, coeff)) return AGB_INVALID_ARGUMENT;
+    for (int32_t s = 0; s < steps; ++s) grid_pass(g, coeff);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* World                                                                      */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+    uint64_t* id; uint32_t* flags; uint8_t* death_cause;
+    double *x, *y, *z, *vx, *vy, *vz, *energy;
+    float *temp_cell, *emit_power, *dir_x, *dir_y, *dir_z;
+    double *biomass, *co2_held;
+    float* age_s;
+    uint64_t* rng_state;
+    float *taxis_memory, *run_timer, *t_local, *irradiance, *co2_local, *n2_local;
+} soa;
+
+struct orc_world {
+    agb_world_desc d;
+    soa c;
+    int32_t count, capacity;
+    uint64_t next_id;
+    grid g[AGB_FIELD_COUNT];
+    /* hash (src/sim/hash.cuh:25-48) */
+    int32_t hnx, hny, hnz, hbuckets;
+    double hcell;
+    float hcellf, hinv, hox, hoy, hoz;
+    uint32_t *keys, *vals, *keys_sorted, *vals_sorted, *tmp_k, *tmp_v;
+    int32_t *bstart, *bend;
+    double *fx, *fy, *fz;
+    uint64_t* co2_demand;
+    int32_t *scan_flags, *prefix, *compact_src;
+    void* scratch;
+    /* counters (World, src/sim/world.cuh:111-129) */
+    int32_t divisions_this_window, dead_slots_prev;
+    int64_t deaths_total, deaths_reported;
+    uint64_t tick;
+    double sim_time, physics_rate, biology_rate;
+    uint64_t accum[12];
+};
+
+static void soa_sizes(size_t sz[25]) {
+    const size_t s[25] = {8, 4, 1, 8, 8, 8, 8, 8, 8, 8, 4, 4, 4, 4, 4, 8, 8, 4, 8, 4, 4, 4, 4, 4, 4};
+    memcpy(sz, s, sizeof(s));
+}
+static void soa_ptrs(soa* c, void** p) {
+    void** q[25] = {(void**)&c->id, (void**)&c->flags, (void**)&c->death_cause, (void**)&c->x,
+                    (void**)&c->y, (void**)&c->z, (void**)&c->vx, (void**)&c->vy, (void**)&c->vz,
+                    (void**)&c->energy, (void**)&c->temp_cell, (void**)&c->emit_power,
+                    (void**)&c->dir_x, (void**)&c->dir_y, (void**)&c->dir_z, (void**)&c->biomass,
+                    (void**)&c->co2_held, (void**)&c->age_s, (void**)&c->rng_state,
+                    (void**)&c->taxis_memory, (void**)&c->run_timer, (void**)&c->t_local,
+                    (void**)&c->irradiance, (void**)&c->co2_local, (void**)&c->n2_local};
+    for (int k = 0; k < 25; ++k) p[k] = (void*)q[k];
+}
+static void host_ptrs(const agb_cells* h, void** p) {
+    void* q[25] = {h->id, h->flags, h->death_cause, h->x, h->y, h->z, h->vx, h->vy, h->vz,
+                   h->energy, h->temp_cell, h->emit_power, h->dir_x, h->dir_y, h->dir_z,
+                   h->biomass, h->co2_held, h->age_s, h->rng_state, h->taxis_memory,
+                   h->run_timer, h->t_local, h->irradiance, h->co2_local, h->n2_local};
+    memcpy(p, q, sizeof(q));
+}
+
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+    omp_set_num_threads(n > 0 ? n : 1);
+#else
+    (void)n;
+#endif
+}
+
+void orc_world_destroy(orc_world* w) {
+    if (!w) return;
+    void* p[25];
+    soa_ptrs(&w->c, p);
+    for (int k = 0; k < 25; ++k) free(*(void**)p[k]);
+    for (int f = 0; f < AGB_FIELD_COUNT; ++f) grid_free(&w->g[f]);
+    free(w->keys); free(w->vals); free(w->keys_sorted); free(w->vals_sorted);
+    free(w->tmp_k); free(w->tmp_v); free(w->bstart); free(w->bend);
+    free(w->fx); free(w->fy); free(w->fz); free(w->co2_demand);
+    free(w->scan_flags); free(w->prefix); free(w->compact_src); free(w->scratch);
+    free(w);
+}
+
+/* world_create (src/sim/step.cu:9-78) + hash_create (src/sim/hash.cu:46-80). */
+int orc_world_create(const agb_world_desc* d, orc_world** out) {
+    *out = NULL;
+    if (!d || d->abi_version != AGB_ABI_VERSION) return AGB_CONTRACT_VERSION_MISMATCH;
+    if (d->capacity <= 0 || d->capacity > AGB_MAX_CELLS) return AGB_INVALID_ARGUMENT;  /* cell_store.cu:140-141 */
+    orc_world* w = (orc_world*)calloc(1, sizeof(orc_world));
+    if (!w) return AGB_OUT_OF_MEMORY;
+    w->d = *d;
+    w->capacity = d->capacity;
+    w->next_id = 1;                                      /* cell_store.cuh:42 */
+    size_t sz[25];
+    soa_sizes(sz);
+    void* p[25];
+    soa_ptrs(&w->c, p);
+    for (int k = 0; k < 25; ++k) {
+        *(void**)p[k] = calloc((size_t)d->capacity, sz[k]);
+        if (!*(void**)p[k]) { orc_world_destroy(w); return AGB_OUT_OF_MEMORY; }
+    }
+    for (int f = 0; f < AGB_FIELD_COUNT; ++f) {
+        const int rc = grid_init(&w->g[f], &d->grid[f], d->chamber_w, d->chamber_d);
+        if (rc) { orc_world_destroy(w); return rc; }
+    }
+    const double cell = d->hash_cell_size > 0.0 ? d->hash_cell_size
+                                                : AGB_HASH_CELL_FACTOR * AGB_CELL_DIAMETER;
+    w->hcell = cell;
+    w->hnx = (int32_t)ceil(d->chamber_w / cell);          /* hash.cu:48-53 */
+    w->hny = (int32_t)ceil(d->chamber_h / cell);
+    w->hnz = (int32_t)ceil(d->chamber_d / cell);
+    if (w->hnx < 1) w->hnx = 1;
+    if (w->hny < 1) w->hny = 1;
+    if (w->hnz < 1) w->hnz = 1;
+    const double nb = (double)w->hnx * w->hny * w->hnz;
+    if (nb >= 2147483647.0) { orc_world_destroy(w); return AGB_INVALID_ARGUMENT; }
+    w->hbuckets = w->hnx * w->hny * w->hnz;
+    w->hcellf = (float)cell;                              /* hash_view, hash.cu:90-104 */
+    w->hinv = (float)(1.0 / cell);
+    w->hox = (float)(-0.5 * w->hnx * cell);
+    w->hoy = (float)(-0.5 * w->hny * cell);
+    w->hoz = (float)(-0.5 * w->hnz * cell);
+    const size_t n = (size_t)d->capacity;
+    w->keys = (uint32_t*)calloc(n, 4); w->vals = (uint32_t*)calloc(n, 4);
+    w->keys_sorted = (uint32_t*)calloc(n, 4); w->vals_sorted = (uint32_t*)calloc(n, 4);
+    w->tmp_k = (uint32_t*)calloc(n, 4); w->tmp_v = (uint32_t*)calloc(n, 4);
+    w->bstart = (int32_t*)calloc((size_t)w->hbuckets, 4);
+    w->bend = (int32_t*)calloc((size_t)w->hbuckets, 4);
+    w->fx = (double*)calloc(n, 8); w->fy = (double*)calloc(n, 8); w->fz = (double*)calloc(n, 8);
+    w->co2_demand = (uint64_t*)calloc(w->g[AGB_FIELD_CO2].enabled ? (size_t)w->g[AGB_FIELD_CO2].count : 1, 8);
+    w->scan_flags = (int32_t*)calloc(n, 4); w->prefix = (int32_t*)calloc(n, 4);
+    w->compact_src = (int32_t*)calloc(n, 4); w->scratch = calloc(n, 8);
+    if (!w->keys || !w->vals || !w->keys_sorted || !w->vals_sorted || !w->tmp_k || !w->tmp_v ||
+        !w->bstart || !w->bend || !w->fx || !w->fy || !w->fz || !w->co2_demand ||
+        !w->scan_flags || !w->prefix || !w->compact_src || !w->scratch) {
+        orc_world_destroy(w);
+        return AGB_OUT_OF_MEMORY;
+    }
+    w->physics_rate = d->physics_rate;
+    w->biology_rate = d->biology_rate;
+    *out = w;
+    return 0;
+}
+
+int orc_world_set_clock(orc_world* w, double p, double b) {   /* world_set_clock, step.cu:206-215 */
+    w->physics_rate = p < AGB_CLOCK_PHYSICS_MIN ? AGB_CLOCK_PHYSICS_MIN
+                    : (p > AGB_CLOCK_PHYSICS_MAX ? AGB_CLOCK_PHYSICS_MAX : p);
+    w->biology_rate = b < AGB_CLOCK_BIOLOGY_MIN ? AGB_CLOCK_BIOLOGY_MIN
+                    : (b > AGB_CLOCK_BIOLOGY_MAX ? AGB_CLOCK_BIOLOGY_MAX : b);
+    return 0;
+}
+
+int orc_world_import_cells(orc_world* w, const agb_cells* src, int32_t count, uint64_t next_id) {
+    if (count < 0 || count > w->capacity) return AGB_CAPACITY_EXCEEDED;
+    size_t sz[25]; void* p[25]; void* h[25];
+    soa_sizes(sz); soa_ptrs(&w->c, p); host_ptrs(src, h);
+    for (int k = 0; k < 25; ++k)
+        if (h[k]) memcpy(*(void**)p[k], h[k], sz[k] * (size_t)count);
+    w->count = count;
+    w->next_id = next_id;
+    return 0;
+}
+
+int orc_world_export_cells(orc_world* w, agb_cells* dst, int32_t max_count, int32_t* count,
+                           uint64_t* next_id) {
+    const int32_t n = w->count < max_count ? w->count : max_count;
+    size_t sz[25]; void* p[25]; void* h[25];
+    soa_sizes(sz); soa_ptrs(&w->c, p); host_ptrs(dst, h);
+    for (int k = 0; k < 25; ++k)
+        if (h[k] && n > 0) memcpy(h[k], *(void**)p[k], sz[k] * (size_t)n);
+    if (count) *count = w->count;
+    if (next_id) *next_id = w->next_id;
+    return 0;
+}
+
+int orc_world_import_field(orc_world* w, int32_t f, const float* src) {
+    if (f < 0 || f >= AGB_FIELD_COUNT || !w->g[f].enabled) return AGB_INVALID_ARGUMENT;
+    memcpy(w->g[f].value, src, sizeof(float) * (size_t)w->g[f].count);
+    return 0;
+}
+int orc_world_export_field(orc_world* w, int32_t f, float* dst) {
+    if (f < 0 || f >= AGB_FIELD_COUNT || !w->g[f].enabled) return AGB_INVALID_ARGUMENT;
+    memcpy(dst, w->g[f].value, sizeof(float) * (size_t)w->g[f].count);
+    return 0;
+}
+int orc_world_export_deposit(orc_world* w, int32_t f, uint64_t* dst) {
+    if (f < 0 || f >= AGB_FIELD_COUNT || !w->g[f].enabled) return AGB_INVALID_ARGUMENT;
+    memcpy(dst, w->g[f].deposit, sizeof(uint64_t) * (size_t)w->g[f].count);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Spawn: spawn_kernel, src/sim/cell_store.cu:42-130 (+ EXTENSION placements) */
+/* ------------------------------------------------------------------------- */
+static double clampd(double v, double lo, double hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+static double sample_charge(pcg32* r, const agb_spawn* p) {   /* cell_store.cu:33-40 */
+    switch (p->charge_dist) {
+        case AGB_DIST_UNIFORM: return uniform_range(r, p->charge_a, p->charge_b);
+        case AGB_DIST_NORMAL: return p->charge_a + p->charge_b * gaussian(r);
+        case AGB_DIST_LOGNORMAL: return exp(log(p->charge_a) + p->charge_b * gaussian(r));
+        default: return p->charge_a;
+    }
+}
+
+/* EXTENSION: the centre of cluster k, from its own stream keyed on (seed, k). */
+static vec3 cluster_centre(uint64_t seed, int32_t k, double extent) {
+    const uint64_t id = 0xC1A5C1A5ull + (uint64_t)k;
+    pcg32 r = cell_rng(cell_rng_init(seed ^ 0x5EEDC1A5ull, id), id);
+    const double h = 0.5 * extent;
+    const double x = uniform_range(&r, -h, h);
+    const double y = uniform_range(&r, -h, h);
+    const double z = uniform_range(&r, -h, h);
+    return v3(x, y, z);
+}
+
+int orc_world_spawn(orc_world* w, const agb_spawn* p) {
+    if (p->count <= 0) return 0;
+    if (w->count + p->count > w->capacity) return AGB_CAPACITY_EXCEEDED;   /* cell_store.cu:264-265 */
+    if (p->placement == AGB_PLACE_CLUSTERS && p->clusters <= 0) return AGB_INVALID_ARGUMENT;
+    const double cw = w->d.chamber_w, ch = w->d.chamber_h, cd = w->d.chamber_d;
+    const double a = AGB_CELL_RADIUS;
+    soa* v = &w->c;
+    for (int32_t i = 0; i < p->count; ++i) {
+        const int32_t slot = w->count + i;
+        const uint64_t id = w->next_id + (uint64_t)i;
+        const uint64_t state = cell_rng_init(w->d.seed, id);
+        pcg32 r = cell_rng(state, id);
+        double x = 0.0, y = 0.0, z = 0.0;
+        int z_done = 0;
+        switch (p->placement) {
+            case AGB_PLACE_GAUSSIAN: {
+                double gx, gy;
+                gaussian_pair(&r, &gx, &gy);
+                x = p->place_x + p->place_radius * gx;
+                y = p->place_y + p->place_radius * gy;
+                break;
+            }
+            case AGB_PLACE_DISC: {
+                const double rad = p->place_radius * sqrt(uniform01d(&r));
+                const double ang = uniform_range(&r, 0.0, AGB_TWO_PI);
+                x = p->place_x + rad * cos(ang);
+                y = p->place_y + rad * sin(ang);
+                break;
+            }
+            case AGB_PLACE_GRID: {
+                const int side = (int)ceil(sqrt((double)p->count));
+                const int gx = i % side, gy = i / side;
+                x = ((double)gx / side - 0.5) * cw * 0.98;
+                y = ((double)gy / side - 0.5) * ch * 0.98;
+                break;
+            }
+            case AGB_PLACE_SLAB_X:
+                x = uniform_range(&r, p->place_x - p->place_radius, p->place_x + p->place_radius);
+                y = uniform_range(&r, -0.5 * ch, 0.5 * ch);
+                break;
+            case AGB_PLACE_CLUSTERS: {
+                int32_t k = (int32_t)(uniform01d(&r) * (double)p->clusters);
+                if (k >= p->clusters) k = p->clusters - 1;
+                const vec3 c0 = cluster_centre(w->d.seed, k, p->cluster_extent);
+                double gx, gy, gz, gw;
+                gaussian_pair(&r, &gx, &gy);
+                gaussian_pair(&r, &gz, &gw);
+                x = c0.x + p->place_radius * gx;
+                y = c0.y + p->place_radius * gy;
+                z = clampd(c0.z + p->place_radius * gz, -0.5 * cd + a, 0.5 * cd - a);
+                z_done = 1;
+                break;
+            }
+            default:
+                x = uniform_range(&r, -0.5 * cw, 0.5 * cw);
+                y = uniform_range(&r, -0.5 * ch, 0.5 * ch);
+                break;
+        }
+        x = clampd(x, -0.5 * cw + a, 0.5 * cw - a);
+        y = clampd(y, -0.5 * ch + a, 0.5 * ch - a);
+        if (!z_done) z = uniform_range(&r, -0.5 * cd + a, 0.5 * cd - a);
+        double charge = clampd(sample_charge(&r, p), 0.0, 1.0);
+        if (p->charge_max > 0.0 && charge > p->charge_max) charge = p->charge_max;
+        v->id[slot] = id;
+        v->flags[slot] = AGB_FLAG_OCCUPIED | AGB_FLAG_ALIVE | (p->awake ? AGB_FLAG_AWAKE : 0u);
+        v->death_cause[slot] = AGB_DEATH_NONE;
+        v->x[slot] = x; v->y[slot] = y; v->z[slot] = z;
+        v->vx[slot] = 0.0; v->vy[slot] = 0.0; v->vz[slot] = 0.0;
+        v->energy[slot] = charge * AGB_CELL_ENERGY_MAX;
+        v->temp_cell[slot] = (float)(p->awake ? AGB_CELL_TEMP_SETPOINT : AGB_AMBIENT_TEMP_DEFAULT);
+        v->emit_power[slot] = 0.0f;
+        double dx, dy, dz, dd;                             /* gaussian3, rng.cuh:111-117 */
+        gaussian_pair(&r, &dx, &dy);
+        gaussian_pair(&r, &dz, &dd);
+        const vec3 dir = vnormalize(v3(dx, dy, dz));
+        v->dir_x[slot] = (float)dir.x; v->dir_y[slot] = (float)dir.y; v->dir_z[slot] = (float)dir.z;
+        v->biomass[slot] = AGB_CELL_MASS_DRY;
+        v->co2_held[slot] = 0.0;
+        v->age_s[slot] = 0.0f;
+        v->rng_state[slot] = r.state;
+        v->taxis_memory[slot] = 0.0f;
+        v->run_timer[slot] = 0.0f;
+        v->t_local[slot] = v->temp_cell[slot];
+        v->irradiance[slot] = 0.0f;
+        v->co2_local[slot] = 0.0f;
+        v->n2_local[slot] = 0.0f;
+    }
+    w->count += p->count;
+    w->next_id += (uint64_t)p->count;
+    return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Spatial hash: src/sim/hash.cuh:59-111, src/sim/hash.cu:15-38, 106-133      */
+/* ------------------------------------------------------------------------- */
+static int32_t clampi(int32_t v, int32_t lo, int32_t hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+static void hash_coords(const orc_world* w, double x, double y, double z, int32_t* gx, int32_t* gy,
+                        int32_t* gz) {                    /* hash.cuh:63-68 */
+    *gx = clampi((int32_t)((x - w->hox) * w->hinv), 0, w->hnx - 1);
+    *gy = clampi((int32_t)((y - w->hoy) * w->hinv), 0, w->hny - 1);
+    *gz = clampi((int32_t)((z - w->hoz) * w->hinv), 0, w->hnz - 1);
+}
+static uint32_t hash_index(const orc_world* w, int32_t gx, int32_t gy, int32_t gz) {
+    return (uint32_t)((gz * w->hny + gy) * w->hnx + gx);   /* hash.cuh:70-72 */
+}
+
+/* Stable LSD radix sort of (key, value) on the bits the bucket count needs;
+ * identical output to CUB's stable SortPairs over all 32 bits. */
+static void stable_sort_pairs(orc_world* w, int32_t n) {
+    uint32_t bits = 0;
+    while (bits < 32 && ((uint64_t)w->hbuckets >> bits) != 0) ++bits;
+    uint32_t *ik = w->keys, *iv = w->vals, *ok = w->keys_sorted, *ov = w->vals_sorted;
+    memcpy(ok, ik, 4 * (size_t)n); memcpy(ov, iv, 4 * (size_t)n);
+    uint32_t *ak = ok, *av = ov, *bk = w->tmp_k, *bv = w->tmp_v;
+    for (uint32_t shift = 0; shift < bits; shift += 8) {
+        size_t cnt[257];
+        memset(cnt, 0, sizeof(cnt));
+        for (int32_t i = 0; i < n; ++i) ++cnt[((ak[i] >> shift) & 255u) + 1];
+        for (int d = 0; d < 256; ++d) cnt[d + 1] += cnt[d];
+        for (int32_t i = 0; i < n; ++i) {
+            const size_t pos = cnt[(ak[i] >> shift) & 255u]++;
+            bk[pos] = ak[i]; bv[pos] = av[i];
+        }
+        uint32_t* t = ak; ak = bk; bk = t; t = av; av = bv; bv = t;
+    }
+    if (ak != ok) { memcpy(ok, ak, 4 * (size_t)n); memcpy(ov, av, 4 * (size_t)n); }
+}
+
+static int hash_build(orc_world* w) {
+    const int32_t n = w->count;
+    if (n <= 0) return 0;                                  /* hash.cu:107 */
+    memset(w->bstart, 0, 4 * (size_t)w->hbuckets);         /* hash.cu:110-113 */
+    memset(w->bend, 0, 4 * (size_t)w->hbuckets);
+    for (int32_t i = 0; i < n; ++i) {                      /* key_kernel, hash.cu:15-25 */
+        w->vals[i] = (uint32_t)i;
+        if (w->c.flags[i] & AGB_FLAG_OCCUPIED) {
+            int32_t gx, gy, gz;
+            hash_coords(w, w->c.x[i], w->c.y[i], w->c.z[i], &gx, &gy, &gz);
+            w->keys[i] = hash_index(w, gx, gy, gz);
+        } else {
+            w->keys[i] = (uint32_t)w->hbuckets;
+        }
+    }
+    stable_sort_pairs(w, n);                               /* hash.cu:125-126 */
+    for (int32_t i = 0; i < n; ++i) {                      /* range_kernel, hash.cu:29-38 */
+        const uint32_t k = w->keys_sorted[i];
+        if (k >= (uint32_t)w->hbuckets) continue;
+        if (i == 0 || w->keys_sorted[i - 1] != k) w->bstart[k] = i;
+        if (i == n - 1 || w->keys_sorted[i + 1] != k) w->bend[k] = i + 1;
+    }
+    return 0;
+}
+
+/* ASTRO_FOR_EACH_NEIGHBOUR, hash.cuh:88-111, as an explicit iterator. */
+typedef struct { int32_t gx, gy, gz, dz, dy, dx, k, e; } nbr_it;
+static void nbr_begin(const orc_world* w, nbr_it* it, double px, double py, double pz) {
+    hash_coords(w, px, py, pz, &it->gx, &it->gy, &it->gz);
+    it->dz = -1; it->dy = -1; it->dx = -2; it->k = 0; it->e = 0;
+}
+static int nbr_next(const orc_world* w, nbr_it* it, int32_t* j) {
+    for (;;) {
+        if (it->k < it->e) { *j = (int32_t)w->vals_sorted[it->k++]; return 1; }
+        if (++it->dx > 1) {
+            it->dx = -1;
+            if (++it->dy > 1) { it->dy = -1; if (++it->dz > 1) return 0; }
+        }
+        const int32_t cz = it->gz + it->dz, cy = it->gy + it->dy, cx = it->gx + it->dx;
+        if (cz < 0 || cz >= w->hnz || cy < 0 || cy >= w->hny || cx < 0 || cx >= w->hnx) continue;
+        const uint32_t b = hash_index(w, cx, cy, cz);
+        it->k = w->bstart[b];
+        it->e = w->bend[b];
+    }
+}
+
+int orc_world_export_hash(orc_world* w, int32_t dims[4], uint32_t* ks, uint32_t* vs, int32_t* bs,
+                          int32_t* be) {
+    dims[0] = w->hnx; dims[1] = w->hny; dims[2] = w->hnz; dims[3] = w->hbuckets;
+    if (ks) memcpy(ks, w->keys_sorted, 4 * (size_t)w->count);
+    if (vs) memcpy(vs, w->vals_sorted, 4 * (size_t)w->count);
+    if (bs) memcpy(bs, w->bstart, 4 * (size_t)w->hbuckets);
+    if (be) memcpy(be, w->bend, 4 * (size_t)w->hbuckets);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Thermal: src/sim/thermal.cu:19-103, src/sim/thermal.cuh:51-86              */
+/* ------------------------------------------------------------------------- */
+static void thermal_cells(orc_world* w, grid* T, double dt_sub, double cap, double cond) {
+    soa* v = &w->c;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int32_t i = 0; i < w->count; ++i) {               /* thermal_kernel, thermal.cu:19-71 */
+        const uint32_t flags = v->flags[i];
+        if (!(flags & AGB_FLAG_OCCUPIED)) continue;
+        const float xf = (float)v->x[i], yf = (float)v->y[i], zf = (float)v->z[i];
+        const int64_t idx = grid_nearest(T, xf, yf, zf);
+        const float t_grid = T->value[idx];
+        int awake = (flags & AGB_FLAG_AWAKE) != 0u;
+        if (!awake && (double)t_grid >= AGB_CELL_TEMP_SETPOINT) {   /* should_ignite */
+            awake = 1;
+            v->flags[i] = flags | AGB_FLAG_AWAKE;
+        }
+        const double t_cell = awake ? AGB_CELL_TEMP_SETPOINT : (double)t_grid;
+        v->temp_cell[i] = (float)t_cell;
+        if (!awake || !(flags & AGB_FLAG_ALIVE)) continue;
+        double e = 0.0;                                    /* lumped_exchange_energy, thermal.cuh:80-86 */
+        if (cap > 0.0 && cond > 0.0) {
+            const double relax = -expm1(-cond * dt_sub / cap);
+            e = cap * (t_cell - (double)t_grid) * relax;
+        }
+        double energy = v->energy[i] - e;
+        double moved = e;
+        if (energy < 0.0) { moved = v->energy[i]; energy = 0.0; }
+        else if (energy > AGB_CELL_ENERGY_MAX) { moved = v->energy[i] - AGB_CELL_ENERGY_MAX; energy = AGB_CELL_ENERGY_MAX; }
+        v->energy[i] = energy;
+        deposit_add(&T->deposit[idx], moved / cap, T->deposit_scale);
+        if (energy <= 0.0) {
+            v->flags[i] = v->flags[i] & ~AGB_FLAG_ALIVE;
+            v->death_cause[i] = AGB_DEATH_STARVED;
+            v->emit_power[i] = 0.0f;
+        }
+    }
+}
+
+static int thermal_step(orc_world* w, double dt) {       /* thermal_step, thermal.cu:75-103 */
+    grid* T = &w->g[AGB_FIELD_TEMPERATURE];
+    if (!T->enabled) return 0;
+    const int32_t substeps = grid_substeps(T, dt);
+    const double dt_sub = dt / substeps;
+    const double cap = AGB_WATER_DENSITY * AGB_WATER_SPECIFIC_HEAT * T->dx * T->dx * T->dz_eff;
+    const double cond = AGB_CONDUCTION_COEFF;
+    const float coeff = grid_coeff(T, dt_sub);
+    if (!coeff_stable(T, coeff)) return AGB_INVALID_ARGUMENT;
+    for (int32_t s = 0; s < substeps; ++s) {
+        if (w->count > 0 && w->d.thermal_enabled) {
+            thermal_cells(w, T, dt_sub, cap, cond);
+            grid_flush(T);
+        }
+        grid_pass(T, coeff);
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Emission: src/sim/emission.cu:17-177, src/sim/emission.cuh:19-53           */
+/* ------------------------------------------------------------------------- */
+static double disc_overlap_fraction(double p, double a) {   /* emission.cuh:19-25 */
+    if (p <= 0.0) return 1.0;
+    if (p >= 2.0 * a) return 0.0;
+    const double x = p / (2.0 * a);
+    return (2.0 / AGB_PI) * (acos(x) - x * sqrt(1.0 - x * x));
+}
+static double shadow_fraction(vec3 self, vec3 other, vec3 L) {   /* emission.cuh:30-37 */
+    const vec3 d = vsub(self, other);
+    const double along = vdot(d, L);
+    if (along <= 0.0) return 0.0;
+    const double perp2 = vdot(d, d) - along * along;
+    const double perp = perp2 > 0.0 ? sqrt(perp2) : 0.0;
+    return disc_overlap_fraction(perp, AGB_CELL_RADIUS);
+}
+static double column_transmittance(double area, double face) {   /* emission.cuh:43-47 */
+    if (face <= 0.0) return 1.0;
+    const double t = 1.0 - area / face;
+    return t > 0.0 ? t : 0.0;
+}
+
+/* Sweep axis: emission.cu:161-163 (x or y); EXTENSION: z when it dominates. */
+static int light_axis(vec3 d, int* sign) {
+    const double ax = fabs(d.x), ay = fabs(d.y), az = fabs(d.z);
+    int axis = (ax >= ay) ? 0 : 1;
+    if (az > ax && az > ay) axis = 2;
+    const double c = axis == 0 ? d.x : (axis == 1 ? d.y : d.z);
+    *sign = c >= 0.0 ? 1 : -1;
+    return axis;
+}
+
+static void emission_step(orc_world* w, double dt) {
+    grid* I = &w->g[AGB_FIELD_IRRADIANCE];
+    if (!I->enabled) return;
+    const agb_light* L = &w->d.light;
+    const float source = L->enabled ? L->irradiance : 0.0f;
+    const float ambient = L->ambient;
+    if (source <= 0.0f && ambient <= 0.0f) return;         /* emission.cu:150 */
+    const vec3 dir = vnormalize(v3(L->dir_x, L->dir_y, L->dir_z));
+    memset(I->deposit, 0, sizeof(uint64_t) * (size_t)I->count);   /* clear_kernel */
+    soa* v = &w->c;
+    if (w->count > 0 && source > 0.0f) {                   /* occlusion_stamp_kernel, :17-27 */
+        for (int32_t i = 0; i < w->count; ++i) {
+            const uint32_t f = v->flags[i];
+            if (!(f & AGB_FLAG_OCCUPIED)) continue;
+            const double area = (f & AGB_FLAG_ALIVE) ? AGB_CELL_CROSS_SECTION
+                                                     : AGB_CELL_CROSS_SECTION * (1.0 - AGB_CELL_ALBEDO_DEAD);
+            const int64_t idx = grid_nearest(I, (float)v->x[i], (float)v->y[i], (float)v->z[i]);
+            deposit_add(&I->deposit[idx], area, I->deposit_scale);
+        }
+    }
+    int sign;
+    const int axis = light_axis(dir, &sign);
+    /* Face of one voxel across the sweep: emission.cu:164 (dx * chamber depth). */
+    const double face = axis == 2 ? I->dx * I->dx : I->dx * I->dz_eff;
+    const int32_t nx = I->nx, ny = I->ny, nz = I->nz;
+    const int64_t plane = (int64_t)nx * ny;
+    const int32_t len = axis == 0 ? nx : (axis == 1 ? ny : nz);
+    const int64_t stride = axis == 0 ? 1 : (axis == 1 ? nx : plane);
+    const int64_t lines = I->count / len;
+    for (int64_t line = 0; line < lines; ++line) {         /* sweep_kernel, :37-53 */
+        int64_t base;
+        if (axis == 0) base = line * nx;
+        else if (axis == 1) base = (line % nx) + (line / nx) * plane;
+        else base = line;
+        double t = 1.0;
+        for (int32_t s = 0; s < len; ++s) {
+            const int32_t step = sign > 0 ? s : (len - 1 - s);
+            const int64_t idx = base + stride * step;
+            I->value[idx] = (float)(source * t) + ambient;
+            const double area = from_fixed(I->deposit[idx], I->deposit_scale);
+            t *= column_transmittance(area, face);
+        }
+    }
+    if (w->count <= 0) return;
+    const unsigned char exact = w->d.occlusion_exact;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 256)
+#endif
+    for (int32_t i = 0; i < w->count; ++i) {               /* feed_kernel, :81-115 */
+        const uint32_t f = v->flags[i];
+        if (!(f & AGB_FLAG_OCCUPIED) || !(f & AGB_FLAG_ALIVE)) continue;
+        const vec3 pos = v3(v->x[i], v->y[i], v->z[i]);
+        double directional = (double)grid_sample(I, (float)pos.x, (float)pos.y, (float)pos.z) - ambient;
+        if (directional < 0.0) directional = 0.0;
+        if (exact) {
+            double open = 1.0;
+            nbr_it it;
+            int32_t j;
+            nbr_begin(w, &it, pos.x, pos.y, pos.z);
+            while (nbr_next(w, &it, &j)) {
+                if (j != i && (v->flags[j] & AGB_FLAG_OCCUPIED) && (v->flags[j] & AGB_FLAG_ALIVE))
+                    open *= (1.0 - shadow_fraction(pos, v3(v->x[j], v->y[j], v->z[j]), dir));
+            }
+            directional *= open;
+        }
+        v->irradiance[i] = (float)directional;
+        const double gained = (directional * AGB_CELL_CROSS_SECTION + (double)ambient * AGB_CELL_SURFACE_AREA) * dt;
+        double e = v->energy[i] + gained;
+        if (e > AGB_CELL_ENERGY_MAX) e = AGB_CELL_ENERGY_MAX;
+        v->energy[i] = e;
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* Motion: src/sim/integrator.cu:20-177, src/sim/integrator.cuh:29-254        */
+/* ------------------------------------------------------------------------- */
+static double cell_mass(double biomass, double energy) {   /* integrator.cuh:42-44 */
+    return biomass + energy / (AGB_C_LIGHT * AGB_C_LIGHT);
+}
+static double drag_coefficient(double t) {                /* integrator.cuh:29-37 */
+    return 6.0 * AGB_PI * (AGB_VF_A * exp(AGB_VF_B / (t - AGB_VF_C))) * AGB_CELL_RADIUS;
+}
+static double ou_position_shape(double x) {               /* integrator.cuh:80-91 */
+    if (x < 1.0e-2) {
+        const double x3 = x * x * x;
+        return x3 * (2.0 / 3.0 + x * (-0.5 + x * (7.0 / 30.0 + x * (-1.0 / 12.0))));
+    }
+    const double e = exp(-x);
+    return 2.0 * x - 3.0 + 4.0 * e - e * e;
+}
+typedef struct { double e1, ome, inv_beta, s_rr, s_vv, s_rv; } ou_coef;
+static ou_coef ou_coefficients(double mass, double gamma, double T, double dt) {   /* :103-121 */
+    ou_coef c;
+    const double beta = gamma / mass;
+    const double x = beta * dt;
+    c.ome = -expm1(-x);
+    c.e1 = 1.0 - c.ome;
+    c.inv_beta = 1.0 / beta;
+    const double kTm = AGB_K_BOLTZ * T / mass;
+    const double var_vv = kTm * (-expm1(-2.0 * x));
+    const double var_rr = kTm * c.inv_beta * c.inv_beta * ou_position_shape(x);
+    c.s_vv = sqrt(var_vv > 0.0 ? var_vv : 0.0);
+    c.s_rr = sqrt(var_rr > 0.0 ? var_rr : 0.0);
+    c.s_rv = kTm * c.inv_beta * c.ome * c.ome;
+    return c;
+}
+static void ou_advance_axis(double* pos, double* vel, double force, double gamma, const ou_coef* c,
+                            double dt, int noise, double z1, double z2) {   /* :128-154 */
+    const double v_term = force / gamma;
+    const double dpos = v_term * dt + (*vel - v_term) * c->ome * c->inv_beta;
+    const double dvel = (v_term - *vel) * c->ome;
+    double npos = *pos + dpos;
+    double nvel = *vel + dvel;
+    if (noise && c->s_rr > 0.0) {
+        const double a = c->s_rv / c->s_rr;
+        const double b2 = c->s_vv * c->s_vv - a * a;
+        const double b = sqrt(b2 > 0.0 ? b2 : 0.0);
+        npos += c->s_rr * z1;
+        nvel += a * z1 + b * z2;
+    } else if (noise) {
+        nvel += c->s_vv * z2;
+    }
+    *pos = npos;
+    *vel = nvel;
+}
+static int apply_boundary_axis(double* p, double* v, double half, double radius, int mode) {   /* :233-254 */
+    const double lo = -half + radius;
+    const double hi = half - radius;
+    if (*p >= lo && *p <= hi) return 1;
+    if (mode == AGB_WALL_PERIODIC) {
+        const double span = 2.0 * half;
+        while (*p < -half) *p += span;
+        while (*p > half) *p -= span;
+        return 1;
+    }
+    if (mode == AGB_WALL_ABSORBING) return 0;
+    *p = (*p < lo) ? lo : hi;
+    *v = 0.0;
+    return 1;
+}
+
+static void motion_step(orc_world* w, double dt) {        /* motion_step, integrator.cu:154-177 */
+    soa* v = &w->c;
+    const int32_t n = w->count;
+    if (n <= 0) return;
+    const grid *T = &w->g[AGB_FIELD_TEMPERATURE], *C = &w->g[AGB_FIELD_CO2], *N = &w->g[AGB_FIELD_N2];
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int32_t i = 0; i < n; ++i) {                      /* field_sample_kernel, :20-30 */
+        if (!(v->flags[i] & AGB_FLAG_OCCUPIED)) continue;
+        const float x = (float)v->x[i], y = (float)v->y[i], z = (float)v->z[i];
+        if (T->enabled) v->t_local[i] = grid_sample(T, x, y, z);
+        if (C->enabled) v->co2_local[i] = grid_sample(C, x, y, z);
+        if (N->enabled) v->n2_local[i] = grid_sample(N, x, y, z);
+    }
+    const double kc = AGB_CONTACT_STIFFNESS / w->physics_rate;
+    const double kt = w->d.trap_stiffness / w->physics_rate;
+    const double two_a = AGB_CELL_DIAMETER;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 256)
+#endif
+    for (int32_t i = 0; i < n; ++i) {                      /* forces_kernel, :40-76 */
+        const uint32_t flags = v->flags[i];
+        if (!(flags & AGB_FLAG_OCCUPIED)) { w->fx[i] = w->fy[i] = w->fz[i] = 0.0; continue; }
+        const double mass = cell_mass(v->biomass[i], v->energy[i]);
+        const int alive = (flags & AGB_FLAG_ALIVE) != 0u;
+        const double emit = alive ? (double)v->emit_power[i] : 0.0;
+        vec3 F = v3(0.0, 0.0, 0.0);                        /* cell_force, integrator.cuh:179-188 */
+        const double wgt = -(mass - AGB_WATER_DENSITY * AGB_CELL_VOLUME) * AGB_G_ACCEL;
+        if (w->d.gravity_axis == AGB_GRAVITY_Y) F.y += wgt; else F.z += wgt;
+        const double thrust = emit / AGB_C_LIGHT;
+        if (thrust != 0.0) {
+            F.x -= (double)v->dir_x[i] * thrust;
+            F.y -= (double)v->dir_y[i] * thrust;
+            F.z -= (double)v->dir_z[i] * thrust;
+        }
+        if (w->d.contact_enabled) {
+            const vec3 pos = v3(v->x[i], v->y[i], v->z[i]);
+            nbr_it it;
+            int32_t j;
+            nbr_begin(w, &it, pos.x, pos.y, pos.z);
+            while (nbr_next(w, &it, &j)) {
+                if (j == i || !(v->flags[j] & AGB_FLAG_OCCUPIED)) continue;
+                const vec3 d = vsub(pos, v3(v->x[j], v->y[j], v->z[j]));   /* contact_force, :210-219 */
+                const double r2 = vdot(d, d);
+                if (r2 >= two_a * two_a || r2 <= 0.0) continue;
+                const double r = sqrt(r2);
+                const double overlap = two_a - r;
+                const double s = kc * overlap / r;
+                F.x += d.x * s; F.y += d.y * s; F.z += d.z * s;
+            }
+        }
+        if (i == w->d.trap_slot) {                          /* trap_force, :195-197 */
+            F.x += kt * (w->d.trap_x - v->x[i]);
+            F.y += kt * (w->d.trap_y - v->y[i]);
+            F.z += 0.0;
+        }
+        w->fx[i] = F.x; w->fy[i] = F.y; w->fz[i] = F.z;
+    }
+    const double a = AGB_CELL_RADIUS;
+    const double hw = 0.5 * w->d.chamber_w, hh = 0.5 * w->d.chamber_h, hd = 0.5 * w->d.chamber_d;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int32_t i = 0; i < n; ++i) {                      /* integrate_kernel, :79-150 */
+        const uint32_t flags = v->flags[i];
+        if (!(flags & AGB_FLAG_OCCUPIED)) continue;
+        const double t_local = (double)v->t_local[i];
+        const double mass = cell_mass(v->biomass[i], v->energy[i]);
+        const int awake = (flags & AGB_FLAG_AWAKE) != 0u;
+        const double t_drag = awake ? AGB_CELL_TEMP_SETPOINT : t_local;
+        double gamma = drag_coefficient(t_drag);
+        double px = v->x[i], py = v->y[i], pz = v->z[i];
+        double ux = v->vx[i], uy = v->vy[i], uz = v->vz[i];
+        if (flags & AGB_FLAG_STUCK) gamma *= AGB_WALL_STUCK_DRAG_MULT;
+        pcg32 rng = cell_rng(v->rng_state[i], v->id[i]);
+        const ou_coef c = ou_coefficients(mass, gamma, t_drag, dt);   /* integrate_cell, :158-169 */
+        double z1, z2, z3, z4, z5, z6;
+        gaussian_pair(&rng, &z1, &z2);
+        gaussian_pair(&rng, &z3, &z4);
+        gaussian_pair(&rng, &z5, &z6);
+        ou_advance_axis(&px, &ux, w->fx[i], gamma, &c, dt, w->d.thermal_noise, z1, z2);
+        ou_advance_axis(&py, &uy, w->fy[i], gamma, &c, dt, w->d.thermal_noise, z3, z4);
+        ou_advance_axis(&pz, &uz, w->fz[i], gamma, &c, dt, w->d.thermal_noise, z5, z6);
+        v->rng_state[i] = rng.state;
+        int kept = apply_boundary_axis(&px, &ux, hw, a, w->d.boundary_x);
+        kept = apply_boundary_axis(&py, &uy, hh, a, w->d.boundary_y) && kept;
+        const double z_before = pz;
+        apply_boundary_axis(&pz, &uz, hd, a, AGB_WALL_REFLECTING);
+        const int touched = (pz != z_before);
+        uint32_t nf = flags;
+        if (w->d.adhesion_enabled) {
+            if (touched && !(flags & AGB_FLAG_STUCK)) {
+                pcg32 ar = cell_rng(v->rng_state[i], v->id[i]);
+                const int sticks = uniform01d(&ar) < AGB_WALL_STICKINESS;
+                v->rng_state[i] = ar.state;
+                if (sticks) nf |= AGB_FLAG_STUCK;
+            } else if (flags & AGB_FLAG_STUCK) {
+                const double away = (pz < 0.0) ? w->fz[i] : -w->fz[i];
+                if (away > AGB_WALL_RELEASE_FORCE) nf &= ~AGB_FLAG_STUCK;
+            }
+        }
+        v->flags[i] = nf;
+        if (!kept) {
+            v->flags[i] = nf & ~AGB_FLAG_ALIVE;
+            v->death_cause[i] = AGB_DEATH_CULLED;
+            v->emit_power[i] = 0.0f;
+        }
+        v->x[i] = px; v->y[i] = py; v->z[i] = pz;
+        v->vx[i] = ux; v->vy[i] = uy; v->vz[i] = uz;
+        v->age_s[i] += (float)dt;
+    }
+}
+
+int orc_world_export_forces(orc_world* w, double* fx, double* fy, double* fz) {
+    const size_t b = sizeof(double) * (size_t)w->count;
+    memcpy(fx, w->fx, b); memcpy(fy, w->fy, b); memcpy(fz, w->fz, b);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Lifecycle: src/sim/lifecycle.cu:26-294, src/sim/lifecycle.cuh:24-99;       */
+/* compaction: src/sim/cell_store.cu:368-456                                  */
+/* ------------------------------------------------------------------------- */
+static double co2_uptake_rate(double c) {                 /* lifecycle.cuh:24-28 */
+    if (c <= 0.0) return 0.0;
+    return AGB_LIFE_CO2_UPTAKE_MAX * c / (c + AGB_LIFE_CO2_HALF_SATURATION);
+}
+static int ready_to_divide(const orc_world* w, int32_t i) {   /* lifecycle.cuh:33-36 (+ EXTENSION) */
+    if (w->d.division_predicate == AGB_DIVIDE_ENERGY) return w->c.energy[i] >= w->d.division_energy;
+    return w->c.co2_held[i] >= w->d.co2_mass_per_division;
+}
+static void division_axis(uint64_t did, double* ax, double* ay, double* az) {   /* lifecycle.cuh:87-99 */
+    const uint64_t h = splitmix64(splitmix64(did));
+    const double u = (double)(h >> 33) * (1.0 / 2147483648.0) - 1.0;
+    const double phi = (double)(h & 0xFFFFFFFFull) * (AGB_TWO_PI / 4294967296.0);
+    const double s = sqrt(u * u < 1.0 ? 1.0 - u * u : 0.0);
+    *ax = s * cos(phi);
+    *ay = s * sin(phi);
+    *az = u;
+}
+
+static void gather_all(orc_world* w, int32_t live) {      /* compact_field x 25, cell_store.cu:402-456 */
+    size_t sz[25]; void* p[25];
+    soa_sizes(sz); soa_ptrs(&w->c, p);
+    unsigned char* sc = (unsigned char*)w->scratch;
+    for (int k = 0; k < 25; ++k) {
+        unsigned char* arr = *(unsigned char**)p[k];
+        for (int32_t o = 0; o < live; ++o)
+            memcpy(sc + sz[k] * (size_t)o, arr + sz[k] * (size_t)w->compact_src[o], sz[k]);
+        memcpy(arr, sc, sz[k] * (size_t)live);
+    }
+}
+
+static int compact(orc_world* w) {                        /* cell_store_compact, cell_store.cu:414-456 */
+    const int32_t cnt = w->count;
+    if (cnt <= 0) return 0;
+    int32_t run = 0;
+    for (int32_t i = 0; i < cnt; ++i) {
+        const uint32_t f = w->c.flags[i];
+        const int32_t keep = ((f & AGB_FLAG_OCCUPIED) && (f & AGB_FLAG_ALIVE)) ? 1 : 0;
+        if (keep) w->compact_src[run] = i;
+        run += keep;
+    }
+    const int32_t live = run;
+    if (live >= cnt) return 0;
+    if (live > 0) gather_all(w, live);
+    w->count = live;
+    return 0;
+}
+
+static void lifecycle_step(orc_world* w, double dt) {    /* lifecycle_step, lifecycle.cu:208-294 */
+    soa* v = &w->c;
+    const int32_t n = w->count;
+    if (n <= 0) return;
+    const double dt_bio = dt * w->biology_rate;
+    grid* C = &w->g[AGB_FIELD_CO2];
+    if (C->enabled) {
+        const double gv = C->dx * C->dx * C->dz_eff;
+        memset(w->co2_demand, 0, sizeof(uint64_t) * (size_t)C->count);   /* clear_u64_kernel */
+        for (int32_t i = 0; i < n; ++i) {                  /* demand_kernel, :41-52 */
+            const uint32_t f = v->flags[i];
+            if (!(f & AGB_FLAG_OCCUPIED) || !(f & AGB_FLAG_ALIVE)) continue;
+            const int64_t idx = grid_nearest(C, (float)v->x[i], (float)v->y[i], (float)v->z[i]);
+            const double want = co2_uptake_rate((double)C->value[idx]) * dt_bio;
+            if (want <= 0.0) continue;
+            deposit_add(&w->co2_demand[idx], want / gv, C->deposit_scale);
+        }
+        for (int32_t i = 0; i < n; ++i) {                  /* uptake_kernel, :62-86 */
+            const uint32_t f = v->flags[i];
+            if (!(f & AGB_FLAG_OCCUPIED) || !(f & AGB_FLAG_ALIVE)) continue;
+            const int64_t idx = grid_nearest(C, (float)v->x[i], (float)v->y[i], (float)v->z[i]);
+            const double want = co2_uptake_rate((double)C->value[idx]) * dt_bio;
+            if (want <= 0.0) continue;
+            const double asked = from_fixed(w->co2_demand[idx], C->deposit_scale);
+            const double available = (double)C->value[idx];
+            double taken = want;
+            if (asked > available && asked > 0.0) taken = want * (available / asked);
+            if (taken <= 0.0) continue;
+            v->co2_held[i] += taken;
+            deposit_add(&C->deposit[idx], -taken / gv, C->deposit_scale);
+        }
+        grid_flush(C);                                     /* lifecycle.cu:235 */
+    }
+    for (int32_t i = 0; i < n; ++i) {                      /* death_kernel, :100-112 */
+        const uint32_t f = v->flags[i];
+        if (!(f & AGB_FLAG_OCCUPIED) || !(f & AGB_FLAG_ALIVE)) continue;
+        if (!((double)v->t_local[i] > AGB_CELL_LETHAL_TEMP)) continue;
+        v->flags[i] = f & ~AGB_FLAG_ALIVE;
+        v->death_cause[i] = AGB_DEATH_OVERHEATED;
+        v->emit_power[i] = 0.0f;
+        v->energy[i] = w->d.store_disposition == AGB_STORE_RETAIN ? v->energy[i] : 0.0;   /* corpse_energy */
+    }
+    int32_t births = 0, deads = 0;
+    for (int32_t i = 0; i < n; ++i) {                      /* mark_kernel, :119-135 */
+        const uint32_t f = v->flags[i];
+        const int occ = (f & AGB_FLAG_OCCUPIED) != 0u, alive = (f & AGB_FLAG_ALIVE) != 0u;
+        const int div = occ && alive && ready_to_divide(w, i);
+        w->scan_flags[i] = div;
+        births += div;
+        deads += (occ && !alive);
+    }
+    const int32_t new_deaths = deads - w->dead_slots_prev;
+    if (new_deaths > 0) w->deaths_total += new_deaths;
+    if (births > 0) {
+        int32_t run = 0;                                   /* ExclusiveSum, :269-270 */
+        for (int32_t i = 0; i < n; ++i) { w->prefix[i] = run; run += w->scan_flags[i]; }
+        const int32_t base = n;
+        if (base + births > w->capacity) births = w->capacity - base;
+        if (births > 0) {
+            const uint64_t first_id = w->next_id;
+            const double a = AGB_CELL_RADIUS;
+            const double hx = 0.5 * w->d.chamber_w - a, hy = 0.5 * w->d.chamber_h - a,
+                         hz = 0.5 * w->d.chamber_d - a;
+            for (int32_t i = 0; i < n; ++i) {              /* divide_kernel, :140-204 */
+                const uint32_t f = v->flags[i];
+                if (!(f & AGB_FLAG_OCCUPIED) || !(f & AGB_FLAG_ALIVE)) continue;
+                if (!ready_to_divide(w, i)) continue;
+                const int32_t slot = base + w->prefix[i];
+                if (slot >= w->capacity) continue;
+                const uint64_t did = first_id + (uint64_t)w->prefix[i];
+                const double half0 = 0.5 * (v->energy[i] - AGB_LIFE_DIVISION_ENERGY_COST);
+                const double half = half0 > 0.0 ? half0 : 0.0;
+                v->energy[i] = half;
+                v->energy[slot] = half;
+                v->co2_held[i] = 0.0;
+                v->co2_held[slot] = 0.0;
+                v->biomass[slot] = AGB_CELL_MASS_DRY;
+                double ax, ay, az;
+                division_axis(did, &ax, &ay, &az);
+                v->x[slot] = v->x[i] + a * ax; v->x[i] -= a * ax;
+                v->y[slot] = v->y[i] + a * ay; v->y[i] -= a * ay;
+                v->z[slot] = v->z[i] + a * az; v->z[i] -= a * az;
+                v->x[slot] = clampd(v->x[slot], -hx, hx);
+                v->y[slot] = clampd(v->y[slot], -hy, hy);
+                v->z[slot] = clampd(v->z[slot], -hz, hz);
+                v->x[i] = clampd(v->x[i], -hx, hx);
+                v->y[i] = clampd(v->y[i], -hy, hy);
+                v->z[i] = clampd(v->z[i], -hz, hz);
+                v->vx[slot] = v->vx[i]; v->vy[slot] = v->vy[i]; v->vz[slot] = v->vz[i];
+                v->id[slot] = did;
+                v->flags[slot] = v->flags[i];
+                v->death_cause[slot] = AGB_DEATH_NONE;
+                v->temp_cell[slot] = v->temp_cell[i];
+                v->emit_power[slot] = 0.0f;
+                v->dir_x[slot] = v->dir_x[i]; v->dir_y[slot] = v->dir_y[i]; v->dir_z[slot] = v->dir_z[i];
+                v->age_s[slot] = 0.0f;
+                v->rng_state[slot] = pcg_split(v->rng_state[i], did);
+                v->taxis_memory[slot] = 0.0f;
+                v->run_timer[slot] = 0.0f;
+                v->t_local[slot] = v->t_local[i];
+                v->irradiance[slot] = 0.0f;
+                v->co2_local[slot] = v->co2_local[i];
+                v->n2_local[slot] = v->n2_local[i];
+            }
+            w->divisions_this_window += births;
+            w->next_id += (uint64_t)births;
+            w->count += births;
+        }
+    }
+    /* Compaction (lifecycle.cu:289-293); EXTENSION: only on every compaction_period-th tick. */
+    const int32_t period = w->d.compaction_period > 0 ? w->d.compaction_period : 1;
+    int compacted = 0;
+    if (w->d.compaction_enabled && deads > 0 && ((w->tick + 1) % (uint64_t)period) == 0) {
+        compact(w);
+        compacted = 1;
+    }
+    w->dead_slots_prev = compacted ? 0 : deads;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Tick: world_step, src/sim/step.cu:109-184                                  */
+/* ------------------------------------------------------------------------- */
+static int slow_fields(orc_world* w, double dt) {         /* step.cu:168-171 */
+    grid_flush(&w->g[AGB_FIELD_CO2]);
+    grid_flush(&w->g[AGB_FIELD_N2]);
+    int rc = grid_diffuse(&w->g[AGB_FIELD_CO2], dt);
+    if (rc) return rc;
+    return grid_diffuse(&w->g[AGB_FIELD_N2], dt);
+}
+
+int orc_world_stage(orc_world* w, int32_t stage) {
+    const double dt = AGB_DT_PHYSICS * w->physics_rate;
+    switch (stage) {
+        case AGB_STAGE_HASH: return hash_build(w);
+        case AGB_STAGE_THERMAL: return thermal_step(w, dt);
+        case AGB_STAGE_EMISSION: emission_step(w, dt); return 0;
+        case AGB_STAGE_MOTION: motion_step(w, dt); return 0;
+        case AGB_STAGE_SLOW_FIELDS: return slow_fields(w, dt);
+        case AGB_STAGE_LIFECYCLE: lifecycle_step(w, dt); return 0;
+        case AGB_STAGE_COMPACT: return compact(w);
+        case AGB_STAGE_CLOCK: ++w->tick; w->sim_time += dt; return 0;
+    }
+    return AGB_INVALID_ARGUMENT;
+}
+
+int orc_world_step(orc_world* w, int32_t ticks) {
+    if (w->d.taxis_enabled) return AGB_UNSUPPORTED;
+    for (int32_t t = 0; t < ticks; ++t) {
+        const double dt = AGB_DT_PHYSICS * w->physics_rate;
+        int rc = hash_build(w);
+        if (!rc && w->d.thermal_enabled) rc = thermal_step(w, dt);
+        if (rc) return rc;
+        if (w->d.emission_enabled) emission_step(w, dt);
+        motion_step(w, dt);
+        rc = slow_fields(w, dt);
+        if (rc) return rc;
+        lifecycle_step(w, dt);
+        ++w->tick;
+        w->sim_time += dt;
+    }
+    return 0;
+}
+
+int orc_world_diffuse(orc_world* w, int32_t f, double dt) {
+    if (f < 0 || f >= AGB_FIELD_COUNT) return AGB_INVALID_ARGUMENT;
+    return grid_diffuse(&w->g[f], dt);
+}
+
+int orc_world_counters(orc_world* w, int64_t out[4]) {
+    out[0] = w->divisions_this_window;
+    out[1] = w->deaths_total;
+    out[2] = w->dead_slots_prev;
+    out[3] = 0;
+    return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Telemetry: src/sim/stats.cu:27-153                                         */
+/* ------------------------------------------------------------------------- */
+int orc_world_stats(orc_world* w, agb_stats* s) {
+    uint64_t energy = 0, temp_cell = 0, temp_medium = 0, co2 = 0, n2 = 0, max_temp = 0;
+    uint32_t n_alive = 0, n_dead = 0, n_awake = 0, n_dormant = 0;
+    const soa* v = &w->c;
+    for (int32_t i = 0; i < w->count; ++i) {               /* stats_cells_kernel, :27-43 */
+        const uint32_t f = v->flags[i];
+        if (!(f & AGB_FLAG_OCCUPIED)) continue;
+        const int alive = (f & AGB_FLAG_ALIVE) != 0u, awake = (f & AGB_FLAG_AWAKE) != 0u;
+        if (alive) ++n_alive; else ++n_dead;
+        if (awake) ++n_awake; else ++n_dormant;
+        energy += (uint64_t)to_fixed(v->energy[i], AGB_DEPOSIT_SCALE_STATS);
+        if (alive) temp_cell += (uint64_t)to_fixed((double)v->temp_cell[i], AGB_DEPOSIT_SCALE_STATS);
+    }
+    const grid *T = &w->g[AGB_FIELD_TEMPERATURE], *C = &w->g[AGB_FIELD_CO2], *N = &w->g[AGB_FIELD_N2];
+    if (T->enabled)                                        /* stats_field_kernel, :45-60 */
+        for (int64_t i = 0; i < T->count; ++i) {
+            const double t = (double)T->value[i];
+            temp_medium += (uint64_t)to_fixed(t, AGB_DEPOSIT_SCALE_STATS);
+            const uint64_t m = (uint64_t)to_fixed(t, AGB_DEPOSIT_SCALE_STATS);
+            if (m > max_temp) max_temp = m;
+        }
+    if (C->enabled)
+        for (int64_t i = 0; i < C->count; ++i) co2 += (uint64_t)to_fixed((double)C->value[i], AGB_STATS_SCALE_FIELD);
+    if (N->enabled)
+        for (int64_t i = 0; i < N->count; ++i) n2 += (uint64_t)to_fixed((double)N->value[i], AGB_STATS_SCALE_FIELD);
+    const uint64_t acc[12] = {energy, temp_cell, temp_medium, co2, n2, max_temp, 0,
+                              n_alive, n_dead, n_awake, n_dormant, 0};
+    memcpy(w->accum, acc, sizeof(acc));
+    memset(s, 0, sizeof(*s));                              /* world_stats, :102-153 */
+    s->tick = w->tick;
+    s->sim_time_s = w->sim_time;
+    s->physics_rate = w->physics_rate;
+    s->biology_rate = w->biology_rate;
+    s->n_live = (int32_t)n_alive;
+    s->n_dead = (int32_t)n_dead;
+    s->n_awake = (int32_t)n_awake;
+    s->n_dormant = (int32_t)n_dormant;
+    s->n_taumoeba = 0;
+    s->mean_tau_tolerance = 0.0;
+    s->total_energy_j = from_fixed(energy, AGB_DEPOSIT_SCALE_STATS);
+    s->mean_charge = (n_alive + n_dead) > 0u
+        ? s->total_energy_j / ((n_alive + n_dead) * AGB_CELL_ENERGY_MAX) : 0.0;
+    s->mean_temp_cell_k = n_alive > 0u ? from_fixed(temp_cell, AGB_DEPOSIT_SCALE_STATS) / n_alive : 0.0;
+    const double cells = T->enabled ? (double)T->count : 0.0;
+    s->mean_temp_medium_k = cells > 0.0 ? from_fixed(temp_medium, AGB_DEPOSIT_SCALE_STATS) / cells : 0.0;
+    s->max_temp_medium_k = from_fixed(max_temp, AGB_DEPOSIT_SCALE_STATS);
+    const double vc = C->enabled ? C->dx * C->dx * C->dz_eff : 0.0;
+    const double vn = N->enabled ? N->dx * N->dx * N->dz_eff : 0.0;
+    s->co2_total_kg = from_fixed(co2, AGB_STATS_SCALE_FIELD) * vc;
+    s->n2_total_kg = from_fixed(n2, AGB_STATS_SCALE_FIELD) * vn;
+    s->divisions_this_window = w->divisions_this_window;
+    s->deaths_this_window = (int32_t)(w->deaths_total - w->deaths_reported);
+    w->divisions_this_window = 0;
+    w->deaths_reported = w->deaths_total;
+    s->boil_events = s->max_temp_medium_k >= AGB_WATER_BOILING_POINT ? 1 : 0;
+    s->ignitions_this_window = 0;
+    s->non_canon_run = 0;
+    return 0;
+}
+
+int orc_world_stats_accum(orc_world* w, uint64_t out[12]) {
+    memcpy(out, w->accum, sizeof(w->accum));
+    return 0;
+}
