@@ -237,6 +237,7 @@ def load(path=LIB_PATH):
         "agb_world_step": (I32, [P, I32, P]),
         "agb_world_step_graph": (I32, [P, I32, P]),
         "agb_world_stage": (I32, [P, I32, P]),
+        "agb_world_graph_kernels": (I32, [P, C.POINTER(I32)]),
         "agb_world_diffuse": (I32, [P, I32, C.c_double, P]),
         "agb_world_stats": (I32, [P, C.POINTER(Stats), P]),
         "agb_world_stats_accum": (I32, [P, P]),
@@ -259,10 +260,16 @@ def exported_symbols():
             "agb_world_create", "agb_world_destroy", "agb_world_spawn", "agb_world_import_cells",
             "agb_world_export_cells", "agb_world_device_cells", "agb_world_count",
             "agb_world_import_field", "agb_world_export_field", "agb_world_export_deposit",
-            "agb_world_step", "agb_world_step_graph", "agb_world_stage", "agb_world_diffuse",
+            "agb_world_step", "agb_world_step_graph", "agb_world_graph_kernels", "agb_world_stage",
+            "agb_world_diffuse",
             "agb_world_stats", "agb_world_stats_accum", "agb_world_set_clock",
             "agb_world_set_light", "agb_world_export_hash", "agb_world_export_forces",
             "agb_world_counters"]
+
+
+def _st(stream):
+    """A cudaStream_t given as an int handle (e.g. torch.cuda.Stream.cuda_stream) or None."""
+    return None if stream is None else C.c_void_p(int(stream))
 
 
 def field_shape(desc, f):
@@ -299,25 +306,27 @@ class World:
         except Exception:
             pass
 
-    def spawn(self, p):
-        self._check(self.lib.agb_world_spawn(self.h, C.byref(p), None), "spawn")
+    def spawn(self, p, stream=None):
+        self._check(self.lib.agb_world_spawn(self.h, C.byref(p), _st(stream)), "spawn")
 
-    def import_cells(self, cells, next_id):
+    def import_cells(self, cells, next_id, stream=None):
         s = cells.struct()
-        self._check(self.lib.agb_world_import_cells(self.h, C.byref(s), cells.n, next_id, None), "import_cells")
+        self._check(self.lib.agb_world_import_cells(self.h, C.byref(s), cells.n, next_id, _st(stream)),
+                    "import_cells")
 
-    def export_cells(self):
-        n = self.count()
-        cells = CellArrays(n)
+    def export_cells(self, stream=None, into=None):
+        """Copy the population out; `into` reuses caller-owned (e.g. pinned) buffers."""
+        n = self.count(stream)
+        cells = into if (into is not None and into.n >= n) else CellArrays(n)
         s = cells.struct()
         cnt, nid = C.c_int32(), C.c_uint64()
-        self._check(self.lib.agb_world_export_cells(self.h, C.byref(s), n, C.byref(cnt), C.byref(nid), None),
-                    "export_cells")
+        self._check(self.lib.agb_world_export_cells(self.h, C.byref(s), n, C.byref(cnt), C.byref(nid),
+                                                    _st(stream)), "export_cells")
         return cells, nid.value
 
-    def count(self):
+    def count(self, stream=None):
         c = C.c_int32()
-        self._check(self.lib.agb_world_count(self.h, C.byref(c), None), "count")
+        self._check(self.lib.agb_world_count(self.h, C.byref(c), _st(stream)), "count")
         return c.value
 
     def import_field(self, f, arr):
@@ -334,15 +343,20 @@ class World:
         self._check(self.lib.agb_world_export_deposit(self.h, f, out.ctypes.data, None), "export_deposit")
         return out
 
-    def step(self, ticks=1, graph=False):
+    def step(self, ticks=1, graph=False, stream=None):
         fn = self.lib.agb_world_step_graph if graph else self.lib.agb_world_step
-        self._check(fn(self.h, ticks, None), "step")
+        self._check(fn(self.h, ticks, _st(stream)), "step")
 
     def stage(self, s):
         self._check(self.lib.agb_world_stage(self.h, s, None), "stage %d" % s)
 
-    def diffuse(self, f, dt):
-        self._check(self.lib.agb_world_diffuse(self.h, f, dt, None), "diffuse")
+    def graph_kernels(self):
+        k = C.c_int32()
+        self._check(self.lib.agb_world_graph_kernels(self.h, C.byref(k)), "graph_kernels")
+        return k.value
+
+    def diffuse(self, f, dt, stream=None):
+        self._check(self.lib.agb_world_diffuse(self.h, f, dt, _st(stream)), "diffuse")
 
     def stats(self):
         s = Stats()

@@ -1,0 +1,517 @@
+// k_cells.cu -- per-cell stages of the tick: thermal coupling
+// (src/sim/thermal.cu:19-103), occlusion stamp + transmittance sweep + feeding
+// (src/sim/emission.cu:17-177) and motion: field sample + forces + exact OU
+// integration (src/sim/integrator.cu:20-177).
+//
+// Forces and integration share one kernel here. The reference splits them
+// (ADR-018) because contact must read every neighbour's pre-step position; the
+// neighbour walk reads the hash's sorted snapshot, taken before any position
+// changes, so the fused kernel reads exactly what the split kernels read.
+#include <cuda_runtime.h>
+
+#include "cells.h"
+
+namespace agb {
+
+namespace {
+
+// ASTRO_FOR_EACH_NEIGHBOUR (src/sim/hash.cuh:88-111): buckets in z, y, x
+// order, entries in sorted order. The three x-adjacent buckets of a row are
+// consecutive keys, hence one contiguous run of the sorted arrays.
+template <class F>
+__device__ __forceinline__ void walk_neighbours(const HashDev& h, int32_t gx, int32_t gy, int32_t gz, F&& f) {
+    const int32_t xlo = gx > 0 ? gx - 1 : 0;
+    const int32_t nxr = (gx < h.nx - 1 ? gx + 1 : h.nx - 1) - xlo;
+    // All nine rows' bucket ranges are loaded before any entry is visited, so
+    // the 27 table reads overlap instead of serialising row by row.
+    int32_t lo[9], hi[9];
+#pragma unroll
+    for (int r = 0; r < 9; ++r) {
+        const int32_t cz = gz + r / 3 - 1, cy = gy + r % 3 - 1;
+        lo[r] = 0;
+        hi[r] = 0;
+        if (cz < 0 || cz >= h.nz || cy < 0 || cy >= h.ny) continue;
+        const int32_t b0 = (cz * h.ny + cy) * h.nx + xlo;
+        const int2 r0 = __ldg(&h.ranges[b0]);
+        const int2 r1 = nxr >= 1 ? __ldg(&h.ranges[b0 + 1]) : make_int2(0, 0);
+        const int2 r2 = nxr >= 2 ? __ldg(&h.ranges[b0 + 2]) : make_int2(0, 0);
+        int32_t l = 0, e = 0;
+        bool found = false;
+        if (r0.y > r0.x) { l = r0.x; e = r0.y; found = true; }
+        if (r1.y > r1.x) { if (!found) { l = r1.x; found = true; } e = r1.y; }
+        if (r2.y > r2.x) { if (!found) { l = r2.x; found = true; } e = r2.y; }
+        lo[r] = l;
+        hi[r] = e;
+    }
+#pragma unroll 1
+    for (int r = 0; r < 9; ++r)
+        for (int32_t k = lo[r]; k < hi[r]; ++k) f(k);
+}
+
+// ---------------------------------------------------------------------------
+// Thermal substep (thermal_kernel, src/sim/thermal.cu:19-71)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) thermal_kernel(DevState* S, Ctx c, TickParams p) {
+    const SoA v = S->cur;
+    const int32_t n = S->count;
+    const GridDev T = c.g[AGB_FIELD_TEMPERATURE];
+    AGB_FOR_CELLS(i, n) {
+        const uint32_t flags = v.flags[i];
+        if (!(flags & AGB_FLAG_OCCUPIED)) continue;
+        const int64_t idx = grid_nearest(T, d2f(v.x[i]), d2f(v.y[i]), d2f(v.z[i]));
+        const float t_grid = T.value[idx];
+        bool awake = (flags & AGB_FLAG_AWAKE) != 0u;
+        uint32_t nf = flags;
+        if (!awake && t_grid >= c.setpoint_up) {          // should_ignite, thermal.cuh:51-53
+            awake = true;
+            nf = flags | AGB_FLAG_AWAKE;
+            v.flags[i] = nf;
+        }
+        v.temp_cell[i] = awake ? c.setpoint_hi : t_grid;   // (float)cell_temperature
+        if (!awake || !(flags & AGB_FLAG_ALIVE)) continue;
+        // lumped_exchange_energy (thermal.cuh:80-86): C (T_cell - T_grid) relax,
+        // with T_cell - T_grid formed exactly from the setpoint's float pair.
+        const float dT = (c.setpoint_hi - t_grid) + c.setpoint_lo;
+        const float e = p.t_cap_relax * dT;
+        const double E = v.energy[i];
+        double En = E - f2d(e);
+        float amount = p.t_relax * dT;                    // moved / C when unclamped
+        if (dkey(En) < dkey(0.0)) {
+            amount = (float)(E / p.t_cap);
+            En = 0.0;
+        } else if (dkey(En) > dkey(AGB_CELL_ENERGY_MAX)) {
+            amount = (float)((E - AGB_CELL_ENERGY_MAX) / p.t_cap);
+            En = AGB_CELL_ENERGY_MAX;
+        }
+        v.energy[i] = En;
+        deposit_fixed(&T.deposit[idx], to_fixed_f(amount, (float)T.scale));
+        if (dkey(En) <= dkey(0.0)) {                     // starved
+            v.flags[i] = nf & ~AGB_FLAG_ALIVE;
+            v.death_cause[i] = AGB_DEATH_STARVED;
+            v.emit_power[i] = 0.0f;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Emission (src/sim/emission.cu:17-177)
+// ---------------------------------------------------------------------------
+__global__ void clear_stamps_kernel(DevState* S, Ctx c, const int32_t* __restrict__ stamp_idx) {
+    const int32_t n = S->n_stamps;
+    unsigned long long* dep = c.g[AGB_FIELD_IRRADIANCE].deposit;
+    AGB_FOR_CELLS(i, n) {
+        const int32_t idx = stamp_idx[i];
+        if (idx >= 0) dep[idx] = 0ull;
+    }
+}
+
+// occlusion_stamp_kernel (emission.cu:17-27). Also records each cell's voxel so
+// the next emission stage can clear exactly these voxels.
+__global__ void stamp_kernel(DevState* S, Ctx c, int32_t* stamp_idx) {
+    const SoA v = S->cur;
+    const int32_t n = S->count;
+    if (blockIdx.x == 0 && threadIdx.x == 0) S->n_stamps = n;
+    const GridDev I = c.g[AGB_FIELD_IRRADIANCE];
+    AGB_FOR_CELLS(i, n) {
+        const uint32_t f = v.flags[i];
+        int32_t rec = -1;
+        if (f & AGB_FLAG_OCCUPIED) {
+            const int64_t idx = grid_nearest(I, d2f(v.x[i]), d2f(v.y[i]), d2f(v.z[i]));
+            deposit_fixed(&I.deposit[idx], (f & AGB_FLAG_ALIVE) ? c.stamp_alive : c.stamp_dead);
+            rec = (int32_t)idx;
+        }
+        stamp_idx[i] = rec;
+    }
+}
+
+// sweep_kernel (emission.cu:37-53): one thread per line in sweep order. The
+// FP64 transmittance recurrence runs only at stamped voxels (an empty voxel's
+// factor is exactly 1), and the float output only changes there, so empty
+// voxels cost one load and one store.
+constexpr int SWEEP_PF = 8;
+
+__global__ void __launch_bounds__(128) sweep_kernel(Ctx c) {
+    const GridDev I = c.g[AGB_FIELD_IRRADIANCE];
+    const int32_t nx = I.nx, ny = I.ny;
+    const int64_t plane = (int64_t)nx * ny;
+    const int axis = c.light_axis;
+    const int32_t len = axis == 0 ? nx : (axis == 1 ? ny : I.nz);
+    const int64_t stride = axis == 0 ? 1 : (axis == 1 ? nx : plane);
+    const int64_t lines = I.count / len;
+    const double inv_scale_unused = 0.0;
+    (void)inv_scale_unused;
+    for (int64_t line = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; line < lines;
+         line += (int64_t)gridDim.x * blockDim.x) {
+        int64_t base;
+        if (axis == 0) base = line * nx;
+        else if (axis == 1) base = (line % nx) + (line / nx) * plane;
+        else base = line;
+        double t = 1.0;
+        float cur = fa(d2f((double)c.source * t), c.ambient_irr);
+        for (int32_t s0 = 0; s0 < len; s0 += SWEEP_PF) {
+            unsigned long long raw[SWEEP_PF];
+#pragma unroll
+            for (int u = 0; u < SWEEP_PF; ++u) {
+                const int32_t s = s0 + u;
+                const int32_t step = c.light_sign > 0 ? s : (len - 1 - s);
+                raw[u] = s < len ? __ldg(&I.deposit[base + stride * step]) : 0ull;
+            }
+#pragma unroll
+            for (int u = 0; u < SWEEP_PF; ++u) {
+                const int32_t s = s0 + u;
+                if (s >= len) break;
+                const int32_t step = c.light_sign > 0 ? s : (len - 1 - s);
+                I.value[base + stride * step] = cur;
+                if (raw[u] != 0ull) {
+                    const double area = (double)(long long)raw[u] / I.scale;   // from_fixed
+                    const double tr = 1.0 - area / c.face_area;                // column_transmittance
+                    t *= tr > 0.0 ? tr : 0.0;
+                    cur = fa(d2f((double)c.source * t), c.ambient_irr);
+                }
+            }
+        }
+    }
+}
+
+// x-axis sweep: rows are contiguous in memory, so one warp takes a row, 32
+// consecutive voxels per step (coalesced). Stamped voxels are rare; the FP64
+// recurrence walks them in sweep order, broadcasting each factor.
+__global__ void __launch_bounds__(256) sweep_rows_kernel(Ctx c) {
+    const GridDev I = c.g[AGB_FIELD_IRRADIANCE];
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int32_t len = I.nx;
+    const int64_t lines = I.count / len;
+    for (int64_t line = warp; line < lines; line += nwarps) {
+        const int64_t base = line * len;
+        double t = 1.0;
+        float cur = fa(d2f((double)c.source * t), c.ambient_irr);
+        for (int32_t s0 = 0; s0 < len; s0 += 32) {
+            const int32_t s = s0 + lane;
+            const bool in = s < len;
+            const int64_t idx = base + (c.light_sign > 0 ? s : (len - 1 - s));
+            const unsigned long long raw = in ? __ldg(&I.deposit[idx]) : 0ull;
+            unsigned mask = __ballot_sync(0xFFFFFFFFu, raw != 0ull);
+            float mine = cur;
+            if (mask) {
+                double f = 1.0;
+                if (raw != 0ull) {
+                    const double area = (double)(long long)raw / I.scale;
+                    const double tr = 1.0 - area / c.face_area;
+                    f = tr > 0.0 ? tr : 0.0;
+                }
+                while (mask) {
+                    const int b = __ffs(mask) - 1;
+                    mask &= mask - 1u;
+                    t *= __shfl_sync(0xFFFFFFFFu, f, b);
+                    cur = fa(d2f((double)c.source * t), c.ambient_irr);
+                    if (lane > b) mine = cur;
+                }
+            }
+            if (in) I.value[idx] = mine;
+        }
+    }
+}
+
+// disc_overlap_fraction / shadow_fraction in FP64 (emission.cuh:19-37): the
+// decision path for near-degenerate geometry, rounded operation by operation
+// as the reference writes it (no contraction: an FMA here would leave the
+// rounding error of dx*dx in perp2 and turn an exact total shadow into 1e-8).
+__device__ double shadow_fraction64(double dx, double dy, double dz, const Ctx& c) {
+    const double along = __dadd_rn(__dadd_rn(__dmul_rn(dx, c.ldx), __dmul_rn(dy, c.ldy)), __dmul_rn(dz, c.ldz));
+    if (along <= 0.0) return 0.0;
+    const double len2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    const double perp2 = __dsub_rn(len2, __dmul_rn(along, along));
+    const double p = perp2 > 0.0 ? sqrt(perp2) : 0.0;
+    const double a = AGB_CELL_RADIUS;
+    if (p <= 0.0) return 1.0;
+    if (p >= 2.0 * a) return 0.0;
+    const double x = __ddiv_rn(p, 2.0 * a);
+    const double s = sqrt(__dsub_rn(1.0, __dmul_rn(x, x)));
+    return __dmul_rn(2.0 / AGB_PI, __dsub_rn(acos(x), __dmul_rn(x, s)));
+}
+
+// feed_kernel (emission.cu:81-115).
+__global__ void __launch_bounds__(256) feed_kernel(DevState* S, Ctx c, TickParams p) {
+    const SoA v = S->cur;
+    const int32_t n = S->count;
+    const GridDev I = c.g[AGB_FIELD_IRRADIANCE];
+    const HashDev h = c.h;
+    const float two_a = (float)AGB_CELL_DIAMETER;
+    const float a_f = (float)AGB_CELL_RADIUS;
+    AGB_FOR_CELLS(i, n) {
+        const uint32_t f = v.flags[i];
+        if (!(f & AGB_FLAG_OCCUPIED) || !(f & AGB_FLAG_ALIVE)) continue;
+        const double px = v.x[i], py = v.y[i], pz = v.z[i];
+        float directional = fs(grid_sample(I, I.value, d2f(px), d2f(py), d2f(pz)), c.ambient_irr);
+        if (directional < 0.0f) directional = 0.0f;
+        if (c.occlusion_exact) {
+            const long long X = to_fix64(px, h.fix_k), Y = to_fix64(py, h.fix_k), Z = to_fix64(pz, h.fix_k);
+            int32_t gx, gy, gz;
+            hash_coords(h, px, py, pz, gx, gy, gz);
+            float open = 1.0f;
+            int32_t refined = 0;
+            walk_neighbours(h, gx, gy, gz, [&](int32_t k) {
+                const longlong2 r1 = __ldg(&h.snapA[k]);
+                const longlong2 r2 = __ldg(&h.snapB[k]);
+                const int32_t j = (int32_t)(unsigned int)(r2.y & 0xFFFFFFFFll);
+                if (j == i) return;
+                const uint32_t fj = v.flags[j];      // current flags: thermal may have starved j
+                if (!(fj & AGB_FLAG_OCCUPIED) || !(fj & AGB_FLAG_ALIVE)) return;
+                const long long Dx = X - r1.x, Dy = Y - r1.y, Dz = Z - r2.x;
+                const float dx = fix_diff_f(Dx, h.fix_inv_f), dy = fix_diff_f(Dy, h.fix_inv_f), dz = fix_diff_f(Dz, h.fix_inv_f);
+                const float along = dx * c.lx + dy * c.ly + dz * c.lz;
+                const float r2s = dx * dx + dy * dy + dz * dz;
+                // Fast decisions away from the thresholds; FP64 near them.
+                if (along < -1e-6f * two_a) return;
+                const float qx = dx - along * c.lx, qy = dy - along * c.ly, qz = dz - along * c.lz;
+                const float perp = sqrtf(qx * qx + qy * qy + qz * qz);
+                if (along > 1e-6f * two_a && perp >= two_a * (1.0f + 1e-6f)) return;
+                if (along > 1e-6f * two_a && perp > 1e-2f * two_a && perp < two_a * (1.0f - 1e-6f)) {
+                    const float x = perp / (2.0f * a_f);
+                    const float frac = 0.63661977f * (acosf(x) - x * sqrtf(1.0f - x * x));
+                    open *= (1.0f - frac);
+                    (void)r2s;
+                    return;
+                }
+                ++refined;
+                const double fr = shadow_fraction64(fix_diff_d(Dx, h.fix_inv), fix_diff_d(Dy, h.fix_inv), fix_diff_d(Dz, h.fix_inv), c);
+                open *= (float)(1.0 - fr);
+            });
+            if (refined) atomicAdd(&S->n_shadow_refine, refined);
+            directional *= open;
+        }
+        v.irradiance[i] = directional;
+        const float gained = (directional * (float)AGB_CELL_CROSS_SECTION +
+                              c.ambient_irr * (float)AGB_CELL_SURFACE_AREA) * p.dtf;
+        double e = v.energy[i] + f2d(gained);
+        if (dkey(e) > dkey(AGB_CELL_ENERGY_MAX)) e = AGB_CELL_ENERGY_MAX;
+        v.energy[i] = e;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Motion (src/sim/integrator.cu:20-150; src/sim/integrator.cuh:29-254)
+// ---------------------------------------------------------------------------
+
+// g(x) = 2x - 3 + 4e^-x - e^-2x (ou_position_shape, integrator.cuh:80-91) in
+// FP32 without cancellation: Taylor series (terms to x^12) below 0.5, and
+// 2(x + expm1(-x)) - expm1(-x)^2 above.
+__device__ __forceinline__ float ou_shape_f(float x) {
+    if (x < 0.5f) {
+        float s = -4092.0f / 479001600.0f;
+        s = 2044.0f / 39916800.0f + x * s;
+        s = -1020.0f / 3628800.0f + x * s;
+        s = 508.0f / 362880.0f + x * s;
+        s = -252.0f / 40320.0f + x * s;
+        s = 124.0f / 5040.0f + x * s;
+        s = -1.0f / 12.0f + x * s;
+        s = 7.0f / 30.0f + x * s;
+        s = -0.5f + x * s;
+        s = 2.0f / 3.0f + x * s;
+        return x * x * x * s;
+    }
+    const float em = expm1f(-x);
+    return 2.0f * (x + em) - em * em;
+}
+
+// One axis of the joint OU propagator (ou_advance_axis, integrator.cuh:128-154):
+// returns the position increment; updates the velocity.
+__device__ __forceinline__ float ou_axis(float& vel, float force, float gamma, float dtf, float ome,
+                                         float inv_beta, bool noise, float s_rr, float a, float b,
+                                         float s_vv, float z1, float z2) {
+    const float v_term = force / gamma;
+    float dpos = v_term * dtf + (vel - v_term) * ome * inv_beta;
+    float nvel = vel + (v_term - vel) * ome;
+    if (noise && s_rr > 0.0f) {
+        dpos += s_rr * z1;
+        nvel += a * z1 + b * z2;
+    } else if (noise) {
+        nvel += s_vv * z2;
+    }
+    vel = nvel;
+    return dpos;
+}
+
+// apply_boundary_axis (integrator.cuh:233-254) on FP64 state with integer compares.
+__device__ __forceinline__ bool boundary_axis(double& pos, float& vel, const Ctx& c, int ax, int mode) {
+    const unsigned long long k = dkey(pos);
+    if (k >= c.lo_key[ax] && k <= c.hi_key[ax]) return true;
+    if (mode == AGB_WALL_PERIODIC) {
+        // Bounded: a non-finite position must not spin forever.
+        const double span = 2.0 * c.half[ax];
+        for (int k = 0; k < 64 && pos < -c.half[ax]; ++k) pos += span;
+        for (int k = 0; k < 64 && pos > c.half[ax]; ++k) pos -= span;
+        return true;
+    }
+    if (mode == AGB_WALL_ABSORBING) return false;
+    pos = (k < c.lo_key[ax]) ? c.lo[ax] : c.hi[ax];
+    vel = 0.0f;
+    return true;
+}
+
+__global__ void __launch_bounds__(256) motion_kernel(DevState* S, Ctx c, TickParams p, float* fx_out,
+                                                     float* fy_out, float* fz_out) {
+    const SoA v = S->cur;
+    const int32_t n = S->count;
+    const HashDev h = c.h;
+    const GridDev T = c.g[AGB_FIELD_TEMPERATURE], C2 = c.g[AGB_FIELD_CO2], N2 = c.g[AGB_FIELD_N2];
+    const float two_a = (float)AGB_CELL_DIAMETER;
+    const float thr = two_a * two_a;
+    const double two_a64 = AGB_CELL_DIAMETER;
+    AGB_FOR_CELLS(i, n) {
+        const uint32_t flags = v.flags[i];
+        if (!(flags & AGB_FLAG_OCCUPIED)) {
+            fx_out[i] = 0.0f; fy_out[i] = 0.0f; fz_out[i] = 0.0f;
+            continue;
+        }
+        double px = v.x[i], py = v.y[i], pz = v.z[i];
+        const float xf = d2f(px), yf = d2f(py), zf = d2f(pz);
+        // field_sample_kernel (integrator.cu:20-30)
+        float t_local;
+        if (T.enabled) { t_local = grid_sample(T, T.value, xf, yf, zf); v.t_local[i] = t_local; }
+        else t_local = v.t_local[i];
+        if (C2.enabled) v.co2_local[i] = grid_sample(C2, C2.value, xf, yf, zf);
+        if (N2.enabled) v.n2_local[i] = grid_sample(N2, N2.value, xf, yf, zf);
+
+        // forces_kernel (integrator.cu:40-76)
+        const float mass = d2f(v.biomass[i]) + d2f(v.energy[i]) * (float)(1.0 / (AGB_C_LIGHT * AGB_C_LIGHT));
+        const bool alive = (flags & AGB_FLAG_ALIVE) != 0u;
+        const float wgt = -(mass - (float)(AGB_WATER_DENSITY * AGB_CELL_VOLUME)) * (float)AGB_G_ACCEL;
+        float Fx = 0.0f, Fy = 0.0f, Fz = 0.0f;
+        if (c.gravity_axis == AGB_GRAVITY_Y) Fy += wgt; else Fz += wgt;
+        const float thrust = alive ? v.emit_power[i] * (float)(1.0 / AGB_C_LIGHT) : 0.0f;
+        if (thrust != 0.0f) {
+            Fx -= v.dir_x[i] * thrust;
+            Fy -= v.dir_y[i] * thrust;
+            Fz -= v.dir_z[i] * thrust;
+        }
+        if (c.contact_enabled) {
+            const long long X = to_fix64(px, h.fix_k), Y = to_fix64(py, h.fix_k), Z = to_fix64(pz, h.fix_k);
+            int32_t gx, gy, gz;
+            hash_coords(h, px, py, pz, gx, gy, gz);
+            int32_t refined = 0;
+            const float kc = p.k_contact;
+            const double kc64 = p.k_contact64;
+            walk_neighbours(h, gx, gy, gz, [&](int32_t k) {
+                const longlong2 r1 = __ldg(&h.snapA[k]);
+                const longlong2 r2 = __ldg(&h.snapB[k]);
+                const int32_t j = (int32_t)(unsigned int)(r2.y & 0xFFFFFFFFll);
+                if (j == i || !((unsigned long long)r2.y >> 32 & AGB_FLAG_OCCUPIED)) return;
+                const long long Dx = X - r1.x, Dy = Y - r1.y, Dz = Z - r2.x;
+                const float dx = fix_diff_f(Dx, h.fix_inv_f), dy = fix_diff_f(Dy, h.fix_inv_f), dz = fix_diff_f(Dz, h.fix_inv_f);
+                const float r2s = dx * dx + dy * dy + dz * dz;
+                if (r2s >= thr * (1.0f + 1e-5f)) return;                 // clear of contact
+                if (r2s <= thr * (1.0f - 1e-5f) && r2s > 1e-12f * thr) { // in contact (contact_force)
+                    const float r = sqrtf(r2s);
+                    const float s = kc * (two_a - r) / r;
+                    Fx += dx * s; Fy += dy * s; Fz += dz * s;
+                    return;
+                }
+                ++refined;                  // settle in FP64, contact_force (integrator.cuh:210-219)
+                const double ddx = fix_diff_d(Dx, h.fix_inv), ddy = fix_diff_d(Dy, h.fix_inv),
+                             ddz = fix_diff_d(Dz, h.fix_inv);
+                const double rr = __dadd_rn(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)), __dmul_rn(ddz, ddz));
+                if (rr >= two_a64 * two_a64 || rr <= 0.0) return;
+                const double r = sqrt(rr);
+                const double s = __ddiv_rn(__dmul_rn((double)kc64, __dsub_rn(two_a64, r)), r);
+                Fx += (float)__dmul_rn(ddx, s); Fy += (float)__dmul_rn(ddy, s); Fz += (float)__dmul_rn(ddz, s);
+            });
+            if (refined) atomicAdd(&S->n_contact_refine, refined);
+        }
+        if (i == c.trap_slot) {                                  // trap_force (integrator.cuh:195-197)
+            Fx += p.k_trap * (float)(c.trap_x - px);
+            Fy += p.k_trap * (float)(c.trap_y - py);
+        }
+        fx_out[i] = Fx; fy_out[i] = Fy; fz_out[i] = Fz;
+
+        // integrate_kernel (integrator.cu:79-150)
+        const bool awake = (flags & AGB_FLAG_AWAKE) != 0u;
+        const float t_drag = awake ? (float)AGB_CELL_TEMP_SETPOINT : t_local;
+        float gamma = (float)(6.0 * AGB_PI * AGB_CELL_RADIUS * AGB_VF_A) *
+                      expf((float)AGB_VF_B / (t_drag - (float)AGB_VF_C));
+        if (flags & AGB_FLAG_STUCK) gamma *= (float)AGB_WALL_STUCK_DRAG_MULT;
+        // ou_coefficients (integrator.cuh:103-121)
+        const float beta = gamma / mass;
+        const float x = beta * p.dtf;
+        const float ome = -expm1f(-x);
+        const float inv_beta = 1.0f / beta;
+        const float kTm = (float)AGB_K_BOLTZ * t_drag / mass;
+        const float var_vv = kTm * (-expm1f(-2.0f * x));
+        const float var_rr = kTm * inv_beta * inv_beta * ou_shape_f(x);
+        const float s_vv = sqrtf(var_vv > 0.0f ? var_vv : 0.0f);
+        const float s_rr = sqrtf(var_rr > 0.0f ? var_rr : 0.0f);
+        const float s_rv = kTm * inv_beta * ome * ome;
+        float a = 0.0f, b = 0.0f;
+        if (s_rr > 0.0f) {
+            a = s_rv / s_rr;
+            const float b2 = s_vv * s_vv - a * a;
+            b = sqrtf(b2 > 0.0f ? b2 : 0.0f);
+        }
+        Pcg rng{v.rng_state[i], cell_stream_inc(v.id[i])};
+        float z1, z2, z3, z4, z5, z6;
+        gaussian_pair_f(rng, z1, z2);
+        gaussian_pair_f(rng, z3, z4);
+        gaussian_pair_f(rng, z5, z6);
+        float ux = d2f(v.vx[i]), uy = d2f(v.vy[i]), uz = d2f(v.vz[i]);
+        const bool noise = c.thermal_noise != 0;
+        const float dpx = ou_axis(ux, Fx, gamma, p.dtf, ome, inv_beta, noise, s_rr, a, b, s_vv, z1, z2);
+        const float dpy = ou_axis(uy, Fy, gamma, p.dtf, ome, inv_beta, noise, s_rr, a, b, s_vv, z3, z4);
+        const float dpz = ou_axis(uz, Fz, gamma, p.dtf, ome, inv_beta, noise, s_rr, a, b, s_vv, z5, z6);
+        px += f2d(dpx);
+        py += f2d(dpy);
+        pz += f2d(dpz);
+        bool kept = boundary_axis(px, ux, c, 0, c.boundary_x);
+        kept = boundary_axis(py, uy, c, 1, c.boundary_y) && kept;
+        const unsigned long long zb = (unsigned long long)__double_as_longlong(pz);
+        boundary_axis(pz, uz, c, 2, AGB_WALL_REFLECTING);
+        const bool touched = (unsigned long long)__double_as_longlong(pz) != zb;
+        uint32_t nf = flags;
+        if (c.adhesion_enabled) {
+            if (touched && !(flags & AGB_FLAG_STUCK)) {
+                if (uniform53(rng) < c.stick_bits) nf |= AGB_FLAG_STUCK;
+            } else if (flags & AGB_FLAG_STUCK) {
+                const float away = (pz < 0.0) ? Fz : -Fz;
+                if (away > (float)AGB_WALL_RELEASE_FORCE) nf &= ~AGB_FLAG_STUCK;
+            }
+        }
+        v.rng_state[i] = rng.state;
+        if (!kept) {
+            nf &= ~AGB_FLAG_ALIVE;
+            v.death_cause[i] = AGB_DEATH_CULLED;
+            v.emit_power[i] = 0.0f;
+        }
+        v.flags[i] = nf;
+        v.x[i] = px; v.y[i] = py; v.z[i] = pz;
+        v.vx[i] = f2d(ux); v.vy[i] = f2d(uy); v.vz[i] = f2d(uz);
+        v.age_s[i] = v.age_s[i] + p.dtf;
+    }
+}
+
+}  // namespace
+
+void launch_thermal(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, cudaStream_t s) {
+    thermal_kernel<<<blocks, 256, 0, s>>>(S, c, p);
+}
+void launch_emission(DevState* S, const Ctx& c, const TickParams& p, int32_t* stamp_idx, bool stamp,
+                     int32_t blocks, cudaStream_t s) {
+    clear_stamps_kernel<<<blocks, 256, 0, s>>>(S, c, stamp_idx);
+    if (stamp) stamp_kernel<<<blocks, 256, 0, s>>>(S, c, stamp_idx);
+    const GridDev& I = c.g[AGB_FIELD_IRRADIANCE];
+    const int32_t len = c.light_axis == 0 ? I.nx : (c.light_axis == 1 ? I.ny : I.nz);
+    const int64_t lines = I.count / len;
+    if (c.light_axis == 0) {
+        const int64_t blocks = (lines * 32 + 255) / 256;
+        sweep_rows_kernel<<<(unsigned)(blocks < 65535 ? blocks : 65535), 256, 0, s>>>(c);
+    } else {
+        sweep_kernel<<<(unsigned)((lines + 127) / 128), 128, 0, s>>>(c);
+    }
+    feed_kernel<<<blocks, 256, 0, s>>>(S, c, p);
+}
+void launch_motion(DevState* S, const Ctx& c, const TickParams& p, float* fx, float* fy, float* fz,
+                   int32_t blocks, cudaStream_t s) {
+    motion_kernel<<<blocks, 256, 0, s>>>(S, c, p, fx, fy, fz);
+}
+
+}  // namespace agb

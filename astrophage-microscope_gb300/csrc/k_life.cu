@@ -1,0 +1,577 @@
+// k_life.cu -- lifecycle (src/sim/lifecycle.cu:26-294), compaction
+// (src/sim/cell_store.cu:368-456), telemetry (src/sim/stats.cu:27-153) and
+// the seeded spawn (src/sim/cell_store.cu:42-130).
+//
+// The reference copies the birth and death counts to the host every tick and
+// again inside compaction (lifecycle.cu:250-252, cell_store.cu:428) to decide
+// whether to scan, divide and compact. Here those decisions are read from
+// device memory by the kernels themselves, so the tick never waits on the host
+// and can be captured as a CUDA graph. Slot, id and daughter-stream assignment
+// come from the same exclusive prefix sums, so they are identical.
+#include <cuda_runtime.h>
+
+#include "cells.h"
+
+namespace agb {
+
+namespace {
+
+constexpr int ST = 256;           // scan threads per block
+constexpr int SITEMS = 4;
+constexpr int STILE = ST * SITEMS;
+
+// ---------------------------------------------------------------------------
+// CO2 uptake (demand_kernel / uptake_kernel, lifecycle.cu:41-86)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float uptake_rate_f(float c) {     // co2_uptake_rate, lifecycle.cuh:24-28
+    if (c <= 0.0f) return 0.0f;
+    return (float)AGB_LIFE_CO2_UPTAKE_MAX * c / (c + (float)AGB_LIFE_CO2_HALF_SATURATION);
+}
+
+__global__ void __launch_bounds__(256) demand_kernel(DevState* S, Ctx c, TickParams p,
+                                                     unsigned long long* demand, float inv_gv) {
+    const SoA v = S->cur;
+    const int32_t n = S->count;
+    const GridDev C2 = c.g[AGB_FIELD_CO2];
+    AGB_FOR_CELLS(i, n) {
+        const uint32_t f = v.flags[i];
+        if (!(f & AGB_FLAG_OCCUPIED) || !(f & AGB_FLAG_ALIVE)) continue;
+        const int64_t idx = grid_nearest(C2, d2f(v.x[i]), d2f(v.y[i]), d2f(v.z[i]));
+        const float want = uptake_rate_f(C2.value[idx]) * (float)p.dt_bio;
+        if (want <= 0.0f) continue;
+        deposit_fixed(&demand[idx], to_fixed_f(want * inv_gv, (float)C2.scale));
+    }
+}
+
+__global__ void __launch_bounds__(256) uptake_kernel(DevState* S, Ctx c, TickParams p,
+                                                     const unsigned long long* __restrict__ demand,
+                                                     float inv_gv) {
+    const SoA v = S->cur;
+    const int32_t n = S->count;
+    const GridDev C2 = c.g[AGB_FIELD_CO2];
+    AGB_FOR_CELLS(i, n) {
+        const uint32_t f = v.flags[i];
+        if (!(f & AGB_FLAG_OCCUPIED) || !(f & AGB_FLAG_ALIVE)) continue;
+        const int64_t idx = grid_nearest(C2, d2f(v.x[i]), d2f(v.y[i]), d2f(v.z[i]));
+        const float available = C2.value[idx];
+        const float want = uptake_rate_f(available) * (float)p.dt_bio;
+        if (want <= 0.0f) continue;
+        const float asked = (float)(long long)demand[idx] * C2.inv_scale_f;   // from_fixed
+        float taken = want;
+        if (asked > available && asked > 0.0f) taken = want * (available / asked);
+        if (taken <= 0.0f) continue;
+        v.co2_held[i] = v.co2_held[i] + f2d(taken);
+        deposit_fixed(&C2.deposit[idx], to_fixed_f(-taken * inv_gv, (float)C2.scale));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Death (death_kernel, lifecycle.cu:100-112) fused with mark (mark_kernel,
+// lifecycle.cu:119-135): both read one cell and write only that cell.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool ready_to_divide(const Ctx& c, const SoA& v, int32_t i) {
+    if (c.division_predicate == AGB_DIVIDE_ENERGY) return v.energy[i] >= c.division_energy;
+    return v.co2_held[i] >= c.co2_quota;                    // lifecycle.cuh:33-36
+}
+
+__global__ void __launch_bounds__(256) death_mark_kernel(DevState* S, Ctx c, int32_t* divflag) {
+    const SoA v = S->cur;
+    const int32_t n = S->count;
+    int32_t births = 0, deads = 0;
+    AGB_FOR_CELLS(i, n) {
+        uint32_t f = v.flags[i];
+        if ((f & AGB_FLAG_OCCUPIED) && (f & AGB_FLAG_ALIVE) && v.t_local[i] > c.lethal_f) {
+            f &= ~AGB_FLAG_ALIVE;
+            v.flags[i] = f;
+            v.death_cause[i] = AGB_DEATH_OVERHEATED;
+            v.emit_power[i] = 0.0f;
+            if (c.store_disposition != AGB_STORE_RETAIN) v.energy[i] = 0.0;   // corpse_energy
+        }
+        const bool occ = (f & AGB_FLAG_OCCUPIED) != 0u, alive = (f & AGB_FLAG_ALIVE) != 0u;
+        const bool div = occ && alive && ready_to_divide(c, v, i);
+        divflag[i] = div ? 1 : 0;
+        births += div;
+        deads += (occ && !alive);
+    }
+    // Counts are order-free integer sums: one atomic per warp.
+    for (int o = 16; o > 0; o >>= 1) {
+        births += __shfl_down_sync(0xFFFFFFFFu, births, o);
+        deads += __shfl_down_sync(0xFFFFFFFFu, deads, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (births) atomicAdd(&S->births, births);
+        if (deads) atomicAdd(&S->deads, deads);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Two-level exclusive scan of a 0/1 predicate (the reference's CUB
+// ExclusiveSum, lifecycle.cu:269-270 and cell_store.cu:422). `gate` selects
+// the device flag that says whether a scan is needed this tick.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool scan_gate(const DevState* S, int gate) {
+    return gate == 0 ? S->births > 0 : S->compact_now != 0;
+}
+
+__global__ void __launch_bounds__(ST) scan_tiles_kernel(DevState* S, const int32_t* __restrict__ flag,
+                                                       int32_t* tile_sums, int gate) {
+    if (!scan_gate(S, gate)) return;
+    const int32_t n = S->count;
+    const int64_t base = (int64_t)blockIdx.x * STILE;
+    int32_t s = 0;
+    for (int u = 0; u < SITEMS; ++u) {
+        const int64_t e = base + u * ST + threadIdx.x;
+        if (e < n) s += flag[e];
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xFFFFFFFFu, s, o);
+    __shared__ int32_t ws[ST / 32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int32_t t = 0;
+        for (int w = 0; w < ST / 32; ++w) t += ws[w];
+        tile_sums[blockIdx.x] = t;
+    }
+}
+
+__global__ void __launch_bounds__(1024) scan_top_kernel(DevState* S, int32_t* tile_sums, int32_t ntiles,
+                                                       int gate) {
+    if (!scan_gate(S, gate)) return;
+    __shared__ int32_t part[1024];
+    const int t = threadIdx.x;
+    const int per = (ntiles + 1023) / 1024;
+    const int b = t * per, e = b + per < ntiles ? b + per : ntiles;
+    int32_t s = 0;
+    for (int i = b; i < e; ++i) s += tile_sums[i];
+    part[t] = s;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        const int32_t x = t >= off ? part[t - off] : 0;
+        __syncthreads();
+        part[t] += x;
+        __syncthreads();
+    }
+    int32_t run = t > 0 ? part[t - 1] : 0;
+    for (int i = b; i < e; ++i) {
+        const int32_t x = tile_sums[i];
+        tile_sums[i] = run;
+        run += x;
+    }
+    if (t == 1023 && gate == 1) S->live = part[1023];
+}
+
+__global__ void __launch_bounds__(ST) scan_apply_kernel(DevState* S, const int32_t* __restrict__ flag,
+                                                       const int32_t* __restrict__ tile_sums, int32_t* prefix,
+                                                       int gate) {
+    if (!scan_gate(S, gate)) return;
+    const int32_t n = S->count;
+    __shared__ int32_t warp_tot[ST / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int32_t run = tile_sums[blockIdx.x];
+    const int64_t base = (int64_t)blockIdx.x * STILE;
+    for (int u = 0; u < SITEMS; ++u) {
+        const int64_t e = base + u * ST + threadIdx.x;
+        const int32_t x = e < n ? flag[e] : 0;
+        int32_t inc = x;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t y = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        if (lane == 31) warp_tot[w] = inc;
+        __syncthreads();
+        int32_t before = 0, round = 0;
+        for (int q = 0; q < ST / 32; ++q) {
+            if (q < w) before += warp_tot[q];
+            round += warp_tot[q];
+        }
+        if (e < n) prefix[e] = run + before + inc - x;
+        run += round;
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Division (divide_kernel, lifecycle.cu:140-204). Rare per cell, so the
+// placement arithmetic stays in FP64 exactly as the reference has it.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) divide_kernel(DevState* S, Ctx c, const int32_t* __restrict__ divflag,
+                                                     const int32_t* __restrict__ prefix) {
+    if (S->births <= 0) return;
+    const SoA v = S->cur;
+    const int32_t n = S->count;                 // base = old count
+    const uint64_t first_id = S->next_id;
+    const double a = AGB_CELL_RADIUS;
+    const double hx = 0.5 * c.chamber_w - a, hy = 0.5 * c.chamber_h - a, hz = 0.5 * c.chamber_d - a;
+    AGB_FOR_CELLS(i, n) {
+        if (!divflag[i]) continue;
+        const int32_t slot = n + prefix[i];
+        if (slot >= c.capacity) continue;       // store full: skip, do not wrap
+        const uint64_t did = first_id + (uint64_t)prefix[i];
+        const double half0 = __dmul_rn(0.5, __dsub_rn(v.energy[i], AGB_LIFE_DIVISION_ENERGY_COST));
+        const double half = half0 > 0.0 ? half0 : 0.0;
+        v.energy[i] = half;
+        v.energy[slot] = half;
+        v.co2_held[i] = 0.0;
+        v.co2_held[slot] = 0.0;
+        v.biomass[slot] = AGB_CELL_MASS_DRY;
+        const uint64_t hsh = splitmix64(splitmix64(did));      // division_axis, lifecycle.cuh:87-99
+        const double u = (double)(hsh >> 33) * (1.0 / 2147483648.0) - 1.0;
+        const double phi = (double)(hsh & 0xFFFFFFFFull) * (AGB_TWO_PI / 4294967296.0);
+        const double uu = __dmul_rn(u, u);
+        const double sr = sqrt(uu < 1.0 ? __dsub_rn(1.0, uu) : 0.0);
+        const double ax = __dmul_rn(sr, cos(phi)), ay = __dmul_rn(sr, sin(phi)), az = u;
+        // Rounded as written in lifecycle.cu:169-171 (no contraction).
+        double x = v.x[i], y = v.y[i], z = v.z[i];
+        const double ox = __dmul_rn(a, ax), oy = __dmul_rn(a, ay), oz = __dmul_rn(a, az);
+        double xs = __dadd_rn(x, ox), ys = __dadd_rn(y, oy), zs = __dadd_rn(z, oz);
+        x = __dsub_rn(x, ox); y = __dsub_rn(y, oy); z = __dsub_rn(z, oz);
+        xs = xs < -hx ? -hx : (xs > hx ? hx : xs);
+        ys = ys < -hy ? -hy : (ys > hy ? hy : ys);
+        zs = zs < -hz ? -hz : (zs > hz ? hz : zs);
+        x = x < -hx ? -hx : (x > hx ? hx : x);
+        y = y < -hy ? -hy : (y > hy ? hy : y);
+        z = z < -hz ? -hz : (z > hz ? hz : z);
+        v.x[slot] = xs; v.y[slot] = ys; v.z[slot] = zs;
+        v.x[i] = x; v.y[i] = y; v.z[i] = z;
+        v.vx[slot] = v.vx[i]; v.vy[slot] = v.vy[i]; v.vz[slot] = v.vz[i];
+        v.id[slot] = did;
+        v.flags[slot] = v.flags[i];
+        v.death_cause[slot] = AGB_DEATH_NONE;
+        v.temp_cell[slot] = v.temp_cell[i];
+        v.emit_power[slot] = 0.0f;
+        v.dir_x[slot] = v.dir_x[i]; v.dir_y[slot] = v.dir_y[i]; v.dir_z[slot] = v.dir_z[i];
+        v.age_s[slot] = 0.0f;
+        v.rng_state[slot] = pcg_split(v.rng_state[i], did);
+        v.taxis_memory[slot] = 0.0f;
+        v.run_timer[slot] = 0.0f;
+        v.t_local[slot] = v.t_local[i];
+        v.irradiance[slot] = 0.0f;
+        v.co2_local[slot] = v.co2_local[i];
+        v.n2_local[slot] = v.n2_local[i];
+    }
+}
+
+// The host bookkeeping of lifecycle_step (lifecycle.cu:250-293), on the device.
+__global__ void life_finalize_kernel(DevState* S, int32_t capacity, int32_t compaction_allowed) {
+    int32_t births = S->births;
+    const int32_t deads = S->deads;
+    const int32_t n = S->count;
+    const int32_t new_deaths = deads - S->dead_slots_prev;
+    if (new_deaths > 0) S->deaths_total += new_deaths;
+    if (births > 0) {
+        if (n + births > capacity) births = capacity - n;
+        if (births > 0) {
+            S->divisions_this_window += births;
+            S->next_id += (uint64_t)births;
+            S->count = n + births;
+        }
+    }
+    const int32_t compact = (compaction_allowed && deads > 0) ? 1 : 0;
+    S->compact_now = compact;
+    S->dead_slots_prev = compact ? 0 : deads;
+    S->births = 0;
+    S->deads = 0;
+}
+
+// ---------------------------------------------------------------------------
+// Compaction (cell_store.cu:368-456): keep = OCCUPIED && ALIVE, stable by
+// prefix, gathered out of place into the spare SoA in one fused pass over all
+// 25 arrays, then the SoA pointers swap on the device.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) keep_kernel(DevState* S, int32_t* keep) {
+    if (!S->compact_now) return;
+    const SoA v = S->cur;
+    const int32_t n = S->count;
+    AGB_FOR_CELLS(i, n) {
+        const uint32_t f = v.flags[i];
+        keep[i] = ((f & AGB_FLAG_OCCUPIED) && (f & AGB_FLAG_ALIVE)) ? 1 : 0;
+    }
+}
+
+__global__ void __launch_bounds__(256) scatter_src_kernel(DevState* S, const int32_t* __restrict__ keep,
+                                                         const int32_t* __restrict__ prefix, int32_t* src) {
+    if (!S->compact_now) return;
+    const int32_t n = S->count;
+    AGB_FOR_CELLS(i, n) {
+        if (keep[i]) src[prefix[i]] = i;
+    }
+}
+
+__global__ void __launch_bounds__(256) gather_kernel(DevState* S, const int32_t* __restrict__ src) {
+    if (!S->compact_now) return;
+    const int32_t live = S->live;
+    if (live >= S->count) return;
+    const SoA a = S->cur;
+    const SoA b = S->spare;
+    AGB_FOR_CELLS(k, live) {
+        const int32_t i = src[k];
+        b.id[k] = a.id[i]; b.flags[k] = a.flags[i]; b.death_cause[k] = a.death_cause[i];
+        b.x[k] = a.x[i]; b.y[k] = a.y[i]; b.z[k] = a.z[i];
+        b.vx[k] = a.vx[i]; b.vy[k] = a.vy[i]; b.vz[k] = a.vz[i];
+        b.energy[k] = a.energy[i]; b.temp_cell[k] = a.temp_cell[i]; b.emit_power[k] = a.emit_power[i];
+        b.dir_x[k] = a.dir_x[i]; b.dir_y[k] = a.dir_y[i]; b.dir_z[k] = a.dir_z[i];
+        b.biomass[k] = a.biomass[i]; b.co2_held[k] = a.co2_held[i]; b.age_s[k] = a.age_s[i];
+        b.rng_state[k] = a.rng_state[i]; b.taxis_memory[k] = a.taxis_memory[i];
+        b.run_timer[k] = a.run_timer[i]; b.t_local[k] = a.t_local[i]; b.irradiance[k] = a.irradiance[i];
+        b.co2_local[k] = a.co2_local[i]; b.n2_local[k] = a.n2_local[i];
+    }
+}
+
+__global__ void swap_kernel(DevState* S) {
+    if (!S->compact_now) return;
+    const int32_t live = S->live;
+    if (live < S->count) {
+        const SoA t = S->cur;
+        S->cur = S->spare;
+        S->spare = t;
+        S->count = live;
+    }
+    S->compact_now = 0;
+}
+
+__global__ void force_compact_kernel(DevState* S) { S->compact_now = 1; }
+
+// ---------------------------------------------------------------------------
+// Telemetry (stats_cells_kernel / stats_field_kernel, stats.cu:27-60):
+// warp-shuffle sums, one atomic per warp and accumulator. Integer sums, so the
+// result is independent of the reduction order, as in the reference.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long warp_sum(unsigned long long x) {
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xFFFFFFFFu, x, o);
+    return x;
+}
+__device__ __forceinline__ unsigned long long warp_max(unsigned long long x) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long y = __shfl_down_sync(0xFFFFFFFFu, x, o);
+        x = y > x ? y : x;
+    }
+    return x;
+}
+
+__global__ void __launch_bounds__(256) stats_cells_kernel(DevState* S, unsigned long long* acc) {
+    const SoA v = S->cur;
+    const int32_t n = S->count;
+    unsigned long long energy = 0, temp = 0, na = 0, nd = 0, nw = 0, ns = 0;
+    AGB_FOR_CELLS(i, n) {
+        const uint32_t f = v.flags[i];
+        if (!(f & AGB_FLAG_OCCUPIED)) continue;
+        const bool alive = (f & AGB_FLAG_ALIVE) != 0u, awake = (f & AGB_FLAG_AWAKE) != 0u;
+        na += alive; nd += !alive; nw += awake; ns += !awake;
+        energy += (unsigned long long)llround(v.energy[i] * AGB_DEPOSIT_SCALE_STATS);
+        if (alive) temp += (unsigned long long)llround((double)v.temp_cell[i] * AGB_DEPOSIT_SCALE_STATS);
+    }
+    energy = warp_sum(energy); temp = warp_sum(temp);
+    na = warp_sum(na); nd = warp_sum(nd); nw = warp_sum(nw); ns = warp_sum(ns);
+    if ((threadIdx.x & 31) == 0) {
+        if (energy) atomicAdd(&acc[0], energy);
+        if (temp) atomicAdd(&acc[1], temp);
+        if (na) atomicAdd(&acc[7], na);
+        if (nd) atomicAdd(&acc[8], nd);
+        if (nw) atomicAdd(&acc[9], nw);
+        if (ns) atomicAdd(&acc[10], ns);
+    }
+}
+
+__global__ void __launch_bounds__(256) stats_field_kernel(const float* __restrict__ val, int64_t count,
+                                                          double scale, unsigned long long* sum,
+                                                          unsigned long long* mx) {
+    unsigned long long s = 0, m = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned long long q = (unsigned long long)llround((double)val[i] * scale);
+        s += q;
+        if (mx && q > m) m = q;
+    }
+    s = warp_sum(s);
+    if ((threadIdx.x & 31) == 0 && s) atomicAdd(sum, s);
+    if (mx) {
+        m = warp_max(m);
+        if ((threadIdx.x & 31) == 0) atomicMax(mx, m);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Seeded spawn (spawn_kernel, cell_store.cu:42-130, plus the extension
+// placements of include/agb.h). FP64, run once per population.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double uniform_range(Pcg& r, double lo, double hi) {   // rng.cuh:86-88
+    return __dadd_rn(lo, __dmul_rn(__dsub_rn(hi, lo), uniform01d(r)));
+}
+__device__ __forceinline__ void gaussian_pair_d(Pcg& r, double& z0, double& z1) {
+    double u1 = uniform01d(r);
+    if (u1 < 1.0e-300) u1 = 1.0e-300;
+    const double u2 = uniform01d(r);
+    const double mag = sqrt(__dmul_rn(-2.0, log(u1)));
+    const double ang = __dmul_rn(6.283185307179586476925286766559, u2);
+    z0 = __dmul_rn(mag, cos(ang));
+    z1 = __dmul_rn(mag, sin(ang));
+}
+
+__global__ void __launch_bounds__(256) spawn_kernel(DevState* S, Ctx c, agb_spawn p) {
+    const SoA v = S->cur;
+    const int32_t base = S->count;
+    const uint64_t first_id = S->next_id;
+    const double cw = c.chamber_w, ch = c.chamber_h, cd = c.chamber_d, a = AGB_CELL_RADIUS;
+    AGB_FOR_CELLS(i, p.count) {
+        const int32_t slot = base + i;
+        const uint64_t id = first_id + (uint64_t)i;
+        Pcg r{cell_rng_init(c.seed, id), cell_stream_inc(id)};
+        double x = 0.0, y = 0.0, z = 0.0;
+        bool z_done = false;
+        switch (p.placement) {
+            case AGB_PLACE_GAUSSIAN: {
+                double gx, gy;
+                gaussian_pair_d(r, gx, gy);
+                x = __dadd_rn(p.place_x, __dmul_rn(p.place_radius, gx));
+                y = __dadd_rn(p.place_y, __dmul_rn(p.place_radius, gy));
+                break;
+            }
+            case AGB_PLACE_DISC: {
+                const double rad = __dmul_rn(p.place_radius, sqrt(uniform01d(r)));
+                const double ang = uniform_range(r, 0.0, AGB_TWO_PI);
+                x = __dadd_rn(p.place_x, __dmul_rn(rad, cos(ang)));
+                y = __dadd_rn(p.place_y, __dmul_rn(rad, sin(ang)));
+                break;
+            }
+            case AGB_PLACE_GRID: {
+                const int side = (int)ceil(sqrt((double)p.count));
+                const int gx = i % side, gy = i / side;
+                x = ((double)gx / side - 0.5) * cw * 0.98;
+                y = ((double)gy / side - 0.5) * ch * 0.98;
+                break;
+            }
+            case AGB_PLACE_SLAB_X:
+                x = uniform_range(r, p.place_x - p.place_radius, p.place_x + p.place_radius);
+                y = uniform_range(r, -0.5 * ch, 0.5 * ch);
+                break;
+            case AGB_PLACE_CLUSTERS: {
+                int32_t k = (int32_t)(uniform01d(r) * (double)p.clusters);
+                if (k >= p.clusters) k = p.clusters - 1;
+                const uint64_t cid = 0xC1A5C1A5ull + (uint64_t)k;
+                Pcg cr{cell_rng_init(c.seed ^ 0x5EEDC1A5ull, cid), cell_stream_inc(cid)};
+                const double h = 0.5 * p.cluster_extent;
+                const double cx = uniform_range(cr, -h, h);
+                const double cy = uniform_range(cr, -h, h);
+                const double cz = uniform_range(cr, -h, h);
+                double gx, gy, gz, gw;
+                gaussian_pair_d(r, gx, gy);
+                gaussian_pair_d(r, gz, gw);
+                x = __dadd_rn(cx, __dmul_rn(p.place_radius, gx));
+                y = __dadd_rn(cy, __dmul_rn(p.place_radius, gy));
+                z = __dadd_rn(cz, __dmul_rn(p.place_radius, gz));
+                const double zl = -0.5 * cd + a, zh = 0.5 * cd - a;
+                z = z < zl ? zl : (z > zh ? zh : z);
+                z_done = true;
+                break;
+            }
+            default:
+                x = uniform_range(r, -0.5 * cw, 0.5 * cw);
+                y = uniform_range(r, -0.5 * ch, 0.5 * ch);
+                break;
+        }
+        {
+            const double xl = -0.5 * cw + a, xh = 0.5 * cw - a, yl = -0.5 * ch + a, yh = 0.5 * ch - a;
+            x = x < xl ? xl : (x > xh ? xh : x);
+            y = y < yl ? yl : (y > yh ? yh : y);
+        }
+        if (!z_done) z = uniform_range(r, -0.5 * cd + a, 0.5 * cd - a);
+        double charge;
+        switch (p.charge_dist) {
+            case AGB_DIST_UNIFORM: charge = uniform_range(r, p.charge_a, p.charge_b); break;
+            case AGB_DIST_NORMAL: { double g0, g1; gaussian_pair_d(r, g0, g1); charge = __dadd_rn(p.charge_a, __dmul_rn(p.charge_b, g0)); break; }
+            case AGB_DIST_LOGNORMAL: { double g0, g1; gaussian_pair_d(r, g0, g1); charge = exp(__dadd_rn(log(p.charge_a), __dmul_rn(p.charge_b, g0))); break; }
+            default: charge = p.charge_a; break;
+        }
+        charge = charge < 0.0 ? 0.0 : (charge > 1.0 ? 1.0 : charge);
+        if (p.charge_max > 0.0 && charge > p.charge_max) charge = p.charge_max;
+        v.id[slot] = id;
+        v.flags[slot] = AGB_FLAG_OCCUPIED | AGB_FLAG_ALIVE | (p.awake ? AGB_FLAG_AWAKE : 0u);
+        v.death_cause[slot] = AGB_DEATH_NONE;
+        v.x[slot] = x; v.y[slot] = y; v.z[slot] = z;
+        v.vx[slot] = 0.0; v.vy[slot] = 0.0; v.vz[slot] = 0.0;
+        v.energy[slot] = __dmul_rn(charge, AGB_CELL_ENERGY_MAX);
+        v.temp_cell[slot] = (float)(p.awake ? AGB_CELL_TEMP_SETPOINT : AGB_AMBIENT_TEMP_DEFAULT);
+        v.emit_power[slot] = 0.0f;
+        double dx, dy, dz, dd;                                    // gaussian3
+        gaussian_pair_d(r, dx, dy);
+        gaussian_pair_d(r, dz, dd);
+        const double l = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+        double ux = 0.0, uy = 0.0, uz = 1.0;                      // normalize, vec.cuh:34-37
+        if (l > 0.0) { const double il = 1.0 / l; ux = __dmul_rn(dx, il); uy = __dmul_rn(dy, il); uz = __dmul_rn(dz, il); }
+        v.dir_x[slot] = (float)ux; v.dir_y[slot] = (float)uy; v.dir_z[slot] = (float)uz;
+        v.biomass[slot] = AGB_CELL_MASS_DRY;
+        v.co2_held[slot] = 0.0;
+        v.age_s[slot] = 0.0f;
+        v.rng_state[slot] = r.state;
+        v.taxis_memory[slot] = 0.0f;
+        v.run_timer[slot] = 0.0f;
+        v.t_local[slot] = v.temp_cell[slot];
+        v.irradiance[slot] = 0.0f;
+        v.co2_local[slot] = 0.0f;
+        v.n2_local[slot] = 0.0f;
+    }
+}
+
+__global__ void spawn_finalize_kernel(DevState* S, int32_t count) {
+    S->count += count;
+    S->next_id += (uint64_t)count;
+}
+
+void launch_scan(DevState* S, const LifeBuffers& b, int32_t capacity, int gate, cudaStream_t s) {
+    const int32_t ntiles = (capacity + STILE - 1) / STILE;
+    scan_tiles_kernel<<<ntiles, ST, 0, s>>>(S, b.flags, b.tile_sums, gate);
+    scan_top_kernel<<<1, 1024, 0, s>>>(S, b.tile_sums, ntiles, gate);
+    scan_apply_kernel<<<ntiles, ST, 0, s>>>(S, b.flags, b.tile_sums, b.prefix, gate);
+}
+
+void launch_compact_kernels(DevState* S, const LifeBuffers& b, int32_t capacity, int32_t blocks,
+                            cudaStream_t s) {
+    keep_kernel<<<blocks, 256, 0, s>>>(S, b.flags);
+    launch_scan(S, b, capacity, 1, s);
+    scatter_src_kernel<<<blocks, 256, 0, s>>>(S, b.flags, b.prefix, b.src);
+    gather_kernel<<<blocks, 256, 0, s>>>(S, b.src);
+    swap_kernel<<<1, 1, 0, s>>>(S);
+}
+
+}  // namespace
+
+void launch_lifecycle(DevState* S, const Ctx& c, const TickParams& p, const LifeBuffers& b,
+                      bool compaction_allowed, int32_t blocks, cudaStream_t s) {
+    const GridDev& C2 = c.g[AGB_FIELD_CO2];
+    if (C2.enabled) {
+        const float inv_gv = (float)(1.0 / (C2.dx * C2.dx * C2.dz_eff));
+        demand_kernel<<<blocks, 256, 0, s>>>(S, c, p, b.co2_demand, inv_gv);
+        uptake_kernel<<<blocks, 256, 0, s>>>(S, c, p, b.co2_demand, inv_gv);
+        launch_flush_by_cells(S, C2, b.co2_demand, blocks, s);      // lifecycle.cu:235
+    }
+    death_mark_kernel<<<blocks, 256, 0, s>>>(S, c, b.flags);
+    launch_scan(S, b, c.capacity, 0, s);
+    divide_kernel<<<blocks, 256, 0, s>>>(S, c, b.flags, b.prefix);
+    life_finalize_kernel<<<1, 1, 0, s>>>(S, c.capacity, compaction_allowed ? 1 : 0);
+    // Compaction cannot run on this tick unless the host-side period allows it.
+    if (compaction_allowed) launch_compact_kernels(S, b, c.capacity, blocks, s);
+}
+
+void launch_compact(DevState* S, const Ctx& c, const LifeBuffers& b, int32_t blocks, cudaStream_t s) {
+    force_compact_kernel<<<1, 1, 0, s>>>(S);
+    launch_compact_kernels(S, b, c.capacity, blocks, s);
+}
+
+void launch_stats(DevState* S, const Ctx& c, unsigned long long* acc, int32_t blocks, cudaStream_t s) {
+    cudaMemsetAsync(acc, 0, sizeof(unsigned long long) * 12, s);
+    stats_cells_kernel<<<blocks, 256, 0, s>>>(S, acc);
+    const GridDev& T = c.g[AGB_FIELD_TEMPERATURE];
+    const GridDev& C2 = c.g[AGB_FIELD_CO2];
+    const GridDev& N2 = c.g[AGB_FIELD_N2];
+    auto nb = [](int64_t n) { const int64_t b = (n + 255) / 256; return (unsigned)(b > 2048 ? 2048 : (b < 1 ? 1 : b)); };
+    if (T.enabled) stats_field_kernel<<<nb(T.count), 256, 0, s>>>(T.value, T.count, AGB_DEPOSIT_SCALE_STATS, &acc[2], &acc[5]);
+    if (C2.enabled) stats_field_kernel<<<nb(C2.count), 256, 0, s>>>(C2.value, C2.count, AGB_STATS_SCALE_FIELD, &acc[3], nullptr);
+    if (N2.enabled) stats_field_kernel<<<nb(N2.count), 256, 0, s>>>(N2.value, N2.count, AGB_STATS_SCALE_FIELD, &acc[4], nullptr);
+}
+
+void launch_spawn(DevState* S, const Ctx& c, const agb_spawn& p, int32_t blocks, cudaStream_t s) {
+    spawn_kernel<<<blocks, 256, 0, s>>>(S, c, p);
+    spawn_finalize_kernel<<<1, 1, 0, s>>>(S, p.count);
+}
+
+}  // namespace agb

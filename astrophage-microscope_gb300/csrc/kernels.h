@@ -1,0 +1,27 @@
+// kernels.h -- host-side launchers of the engine's kernels (one per stage
+// piece). Every launcher enqueues on the given stream and never synchronises.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "dev.cuh"
+
+namespace agb {
+
+struct WorldConst;   // defined in world.cuh
+
+// Fields (k_grid.cu)
+void launch_fill(float* v, int64_t n, float value, cudaStream_t s);
+// One explicit FTCS pass src -> dst (src/fields/diffuse.cu:19-44; 7-point when nz > 1).
+void launch_ftcs(const GridDev& g, const float* src, float* dst, float coeff, const int32_t* bc,
+                 const float* face, float robin, cudaStream_t s);
+// Fold deposits into the field for the voxels cells sit in (flush_kernel,
+// src/fields/diffuse.cu:51-60, restricted to voxels that can hold a deposit).
+void launch_flush_by_cells(DevState* S, GridDev g, unsigned long long* demand_to_clear,
+                           int32_t grid_blocks, cudaStream_t s);
+
+// Spatial hash (k_hash.cu)
+void hash_build(DevState* S, const HashDev& h, int32_t capacity, uint32_t* sort_keys_alt,
+                uint32_t* sort_vals_alt, uint32_t* hist, int32_t grid_blocks, cudaStream_t s);
+
+}  // namespace agb

@@ -1,0 +1,845 @@
+// world.cu -- the C ABI (include/agb.h): world lifetime, import/export in
+// contract layout, the tick sequence of world_step (src/sim/step.cu:109-184)
+// and its CUDA-graph replay.
+//
+// The tick never synchronises with the host: population counts, division and
+// compaction decisions live in device memory (DevState), so a tick -- or many
+// ticks -- can be captured once and replayed as a single graph launch.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "cells.h"
+
+using namespace agb;
+
+struct GraphEntry {
+    int32_t ticks;
+    uint32_t parity;        // which buffer holds each field at capture start
+    uint64_t tick_phase;    // tick % compaction_period at capture start
+    cudaGraphExec_t exec;
+    uint32_t parity_after;
+    int32_t kernels;        // kernel nodes per replay
+};
+
+struct agb_world {
+    agb_world_desc d{};
+    int dev = 0;
+    int sm_count = 0;
+    Ctx c{};
+    TickParams tp{};
+    DevState* S = nullptr;
+    void* blob[2] = {nullptr, nullptr};
+    size_t blob_bytes = 0;
+    float* gbuf[AGB_FIELD_COUNT][2] = {};
+    int gcur[AGB_FIELD_COUNT] = {};
+    unsigned long long* gdep[AGB_FIELD_COUNT] = {};
+    int32_t gbc[AGB_FIELD_COUNT][6] = {};
+    float gface[AGB_FIELD_COUNT][6] = {};
+    float grobin[AGB_FIELD_COUNT] = {};
+    uint32_t *kalt = nullptr, *valt = nullptr, *hist = nullptr;
+    LifeBuffers life{};
+    int32_t* stamp_idx = nullptr;
+    float *fx = nullptr, *fy = nullptr, *fz = nullptr;
+    unsigned long long* acc = nullptr;
+    int32_t blocks = 1;
+    uint64_t tick = 0;
+    double sim_time = 0.0;
+    double physics_rate = 1.0, biology_rate = 1.0;
+    int64_t deaths_reported = 0;
+    unsigned long long acc_host[12] = {};
+    std::vector<GraphEntry> graphs;
+    cudaStream_t own_stream = nullptr;   // capture stream when the caller passes the default stream
+    int32_t last_graph_kernels = 0;
+    std::string err;
+    std::vector<void*> allocs;
+};
+
+namespace {
+
+agb_status fail(agb_world* w, agb_status s, const std::string& what) {
+    if (w) w->err = what;
+    return s;
+}
+
+agb_status cuda_fail(agb_world* w, cudaError_t e, const char* what) {
+    return fail(w, AGB_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define AGB_CUDA(w, call)                                       \
+    do {                                                        \
+        const cudaError_t _e = (call);                          \
+        if (_e != cudaSuccess) return cuda_fail((w), _e, #call); \
+    } while (0)
+
+template <typename T>
+cudaError_t dalloc(agb_world* w, T** p, size_t bytes) {
+    void* q = nullptr;
+    const cudaError_t e = cudaMalloc(&q, bytes ? bytes : 1);
+    if (e == cudaSuccess) { w->allocs.push_back(q); *p = static_cast<T*>(q); }
+    return e;
+}
+
+unsigned long long dkey_host(double v) {
+    unsigned long long b;
+    std::memcpy(&b, &v, 8);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+size_t align256(size_t n) { return (n + 255) / 256 * 256; }
+
+// One blob per SoA, 256-byte aligned arrays in contract order
+// (src/sim/cell_store.cu:139-193).
+SoA carve(void* blob, int32_t cap) {
+    char* p = static_cast<char*>(blob);
+    auto take = [&](size_t elem) { char* q = p; p += align256(elem * (size_t)cap); return q; };
+    SoA v{};
+    v.id = (uint64_t*)take(8); v.flags = (uint32_t*)take(4); v.death_cause = (uint8_t*)take(1);
+    v.x = (double*)take(8); v.y = (double*)take(8); v.z = (double*)take(8);
+    v.vx = (double*)take(8); v.vy = (double*)take(8); v.vz = (double*)take(8);
+    v.energy = (double*)take(8); v.temp_cell = (float*)take(4); v.emit_power = (float*)take(4);
+    v.dir_x = (float*)take(4); v.dir_y = (float*)take(4); v.dir_z = (float*)take(4);
+    v.biomass = (double*)take(8); v.co2_held = (double*)take(8); v.age_s = (float*)take(4);
+    v.rng_state = (uint64_t*)take(8); v.taxis_memory = (float*)take(4); v.run_timer = (float*)take(4);
+    v.t_local = (float*)take(4); v.irradiance = (float*)take(4); v.co2_local = (float*)take(4);
+    v.n2_local = (float*)take(4);
+    return v;
+}
+size_t soa_bytes(int32_t cap) {
+    const size_t sizes[25] = {8, 4, 1, 8, 8, 8, 8, 8, 8, 8, 4, 4, 4, 4, 4, 8, 8, 4, 8, 4, 4, 4, 4, 4, 4};
+    size_t t = 0;
+    for (size_t s : sizes) t += align256(s * (size_t)cap);
+    return t;
+}
+void soa_arrays(const SoA& v, void* p[25]) {
+    void* q[25] = {v.id, v.flags, v.death_cause, v.x, v.y, v.z, v.vx, v.vy, v.vz, v.energy,
+                   v.temp_cell, v.emit_power, v.dir_x, v.dir_y, v.dir_z, v.biomass, v.co2_held,
+                   v.age_s, v.rng_state, v.taxis_memory, v.run_timer, v.t_local, v.irradiance,
+                   v.co2_local, v.n2_local};
+    std::memcpy(p, q, sizeof(q));
+}
+void host_arrays(const agb_cells* h, void* p[25]) {
+    void* q[25] = {h->id, h->flags, h->death_cause, h->x, h->y, h->z, h->vx, h->vy, h->vz,
+                   h->energy, h->temp_cell, h->emit_power, h->dir_x, h->dir_y, h->dir_z,
+                   h->biomass, h->co2_held, h->age_s, h->rng_state, h->taxis_memory,
+                   h->run_timer, h->t_local, h->irradiance, h->co2_local, h->n2_local};
+    std::memcpy(p, q, sizeof(q));
+}
+const size_t kElem[25] = {8, 4, 1, 8, 8, 8, 8, 8, 8, 8, 4, 4, 4, 4, 4, 8, 8, 4, 8, 4, 4, 4, 4, 4, 4};
+
+float float_at_or_above(double v) {
+    float f = (float)v;
+    if ((double)f < v) f = std::nextafter(f, INFINITY);
+    return f;
+}
+float float_at_or_below(double v) {
+    float f = (float)v;
+    if ((double)f > v) f = std::nextafter(f, -INFINITY);
+    return f;
+}
+
+// Stable substep count (src/fields/grid.cuh:51-53; 1/6 bound for 3-D).
+int32_t substeps_for(const GridDev& g, double D, double dt) {
+    const double lim = g.nz > 1 ? 6.0 : 4.0;
+    return (int32_t)(dt / (g.dx * g.dx / (lim * D))) + 1;
+}
+bool coeff_ok(const GridDev& g, float c) { return g.nz > 1 ? c <= (float)(1.0 / 6.0) : c <= 0.25f; }
+
+agb_status compute_tick_params(agb_world* w) {
+    TickParams& p = w->tp;
+    const Ctx& c = w->c;
+    p.dt = AGB_DT_PHYSICS * w->physics_rate;
+    p.dtf = (float)p.dt;
+    p.k_contact = (float)(AGB_CONTACT_STIFFNESS / w->physics_rate);
+    p.k_contact64 = AGB_CONTACT_STIFFNESS / w->physics_rate;
+    p.k_trap = (float)(w->d.trap_stiffness / w->physics_rate);
+    p.dt_bio = p.dt * w->biology_rate;
+    const GridDev& T = c.g[AGB_FIELD_TEMPERATURE];
+    if (T.enabled) {
+        const double D = w->d.grid[AGB_FIELD_TEMPERATURE].diffusivity;
+        p.t_substeps = substeps_for(T, D, p.dt);
+        p.t_dt_sub = p.dt / p.t_substeps;
+        p.t_coeff = (float)(D * p.t_dt_sub / (T.dx * T.dx));
+        if (!coeff_ok(T, p.t_coeff)) return fail(w, AGB_INVALID_ARGUMENT, "diffusion coefficient unstable");
+        // thermal_step (src/sim/thermal.cu:86-90): capacity of one voxel of water.
+        p.t_cap = AGB_WATER_DENSITY * AGB_WATER_SPECIFIC_HEAT * T.dx * T.dx * T.dz_eff;
+        const double relax = -std::expm1(-AGB_CONDUCTION_COEFF * p.t_dt_sub / p.t_cap);
+        p.t_relax = (float)relax;
+        p.t_cap_relax = (float)(p.t_cap * relax);
+    }
+    for (int f : {AGB_FIELD_CO2, AGB_FIELD_N2}) {
+        const GridDev& g = c.g[f];
+        int32_t steps = 0;
+        float coeff = 0.0f;
+        if (g.enabled) {
+            const double D = w->d.grid[f].diffusivity;
+            steps = substeps_for(g, D, p.dt);
+            coeff = (float)(D * (p.dt / steps) / (g.dx * g.dx));
+            if (!coeff_ok(g, coeff)) return fail(w, AGB_INVALID_ARGUMENT, "diffusion coefficient unstable");
+        }
+        if (f == AGB_FIELD_CO2) { p.c_substeps = steps; p.c_coeff = coeff; }
+        else { p.n_substeps = steps; p.n_coeff = coeff; }
+    }
+    return AGB_OK;
+}
+
+void compute_light(agb_world* w) {
+    Ctx& c = w->c;
+    const agb_light& L = w->d.light;
+    double dx = L.dir_x, dy = L.dir_y, dz = L.dir_z;
+    const double l = std::sqrt(dx * dx + dy * dy + dz * dz);          // normalize, vec.cuh:34-37
+    if (l > 0.0) { dx *= 1.0 / l; dy *= 1.0 / l; dz *= 1.0 / l; }
+    else { dx = 0.0; dy = 0.0; dz = 1.0; }
+    c.ldx = dx; c.ldy = dy; c.ldz = dz;
+    c.lx = (float)dx; c.ly = (float)dy; c.lz = (float)dz;
+    const double ax = std::fabs(dx), ay = std::fabs(dy), az = std::fabs(dz);
+    int axis = ax >= ay ? 0 : 1;                                      // emission.cu:161-163
+    if (az > ax && az > ay) axis = 2;
+    const double comp = axis == 0 ? dx : (axis == 1 ? dy : dz);
+    c.light_axis = axis;
+    c.light_sign = comp >= 0.0 ? 1 : -1;
+    c.source = L.enabled ? L.irradiance : 0.0f;
+    c.ambient_irr = L.ambient;
+    const GridDev& I = c.g[AGB_FIELD_IRRADIANCE];
+    c.face_area = axis == 2 ? I.dx * I.dx : I.dx * I.dz_eff;          // emission.cu:164
+}
+
+float* field_value(agb_world* w, int f) { return w->gbuf[f][w->gcur[f]]; }
+
+void refresh_grid_ptrs(agb_world* w) {
+    for (int f = 0; f < AGB_FIELD_COUNT; ++f) {
+        w->c.g[f].value = w->gbuf[f][w->gcur[f]];
+        w->c.g[f].scratch = w->gbuf[f][1 - w->gcur[f]];
+    }
+}
+
+void ftcs(agb_world* w, int f, float coeff, cudaStream_t s) {
+    refresh_grid_ptrs(w);
+    launch_ftcs(w->c.g[f], field_value(w, f), w->gbuf[f][1 - w->gcur[f]], coeff, w->gbc[f], w->gface[f],
+                w->grobin[f], s);
+    w->gcur[f] = 1 - w->gcur[f];
+    refresh_grid_ptrs(w);
+}
+
+// Stage bodies (src/sim/step.cu:109-184 and the functions it calls).
+void stage_hash(agb_world* w, cudaStream_t s) {
+    hash_build(w->S, w->c.h, w->c.capacity, w->kalt, w->valt, w->hist, w->blocks, s);
+}
+
+void stage_thermal(agb_world* w, cudaStream_t s) {   // thermal_step, src/sim/thermal.cu:75-103
+    if (!w->c.g[AGB_FIELD_TEMPERATURE].enabled) return;
+    for (int32_t k = 0; k < w->tp.t_substeps; ++k) {
+        refresh_grid_ptrs(w);
+        if (w->d.thermal_enabled) {
+            launch_thermal(w->S, w->c, w->tp, w->blocks, s);
+            launch_flush_by_cells(w->S, w->c.g[AGB_FIELD_TEMPERATURE], nullptr, w->blocks, s);
+        }
+        ftcs(w, AGB_FIELD_TEMPERATURE, w->tp.t_coeff, s);
+    }
+}
+
+void stage_emission(agb_world* w, cudaStream_t s) {  // emission_step, src/sim/emission.cu:119-177
+    if (!w->c.g[AGB_FIELD_IRRADIANCE].enabled) return;
+    if (w->c.source <= 0.0f && w->c.ambient_irr <= 0.0f) return;
+    refresh_grid_ptrs(w);
+    launch_emission(w->S, w->c, w->tp, w->stamp_idx, w->c.source > 0.0f, w->blocks, s);
+}
+
+void stage_motion(agb_world* w, cudaStream_t s) {    // motion_step, src/sim/integrator.cu:154-177
+    refresh_grid_ptrs(w);
+    launch_motion(w->S, w->c, w->tp, w->fx, w->fy, w->fz, w->blocks, s);
+}
+
+// src/sim/step.cu:168-171. The flushes there are no-ops here by construction:
+// the only CO2 depositor (uptake) flushes its own deposits, and nothing
+// deposits into N2 without predators.
+void stage_slow_fields(agb_world* w, cudaStream_t s) {
+    if (w->c.g[AGB_FIELD_CO2].enabled)
+        for (int32_t k = 0; k < w->tp.c_substeps; ++k) ftcs(w, AGB_FIELD_CO2, w->tp.c_coeff, s);
+    if (w->c.g[AGB_FIELD_N2].enabled)
+        for (int32_t k = 0; k < w->tp.n_substeps; ++k) ftcs(w, AGB_FIELD_N2, w->tp.n_coeff, s);
+}
+
+bool compaction_allowed(const agb_world* w) {
+    const int32_t P = w->d.compaction_period > 0 ? w->d.compaction_period : 1;
+    return w->d.compaction_enabled && ((w->tick + 1) % (uint64_t)P) == 0;
+}
+
+void stage_lifecycle(agb_world* w, cudaStream_t s) {  // lifecycle_step, src/sim/lifecycle.cu:208-294
+    refresh_grid_ptrs(w);
+    launch_lifecycle(w->S, w->c, w->tp, w->life, compaction_allowed(w), w->blocks, s);
+}
+
+void stage_clock(agb_world* w) {
+    ++w->tick;
+    w->sim_time += w->tp.dt;
+}
+
+void tick_once(agb_world* w, cudaStream_t s) {
+    stage_hash(w, s);
+    if (w->d.thermal_enabled) stage_thermal(w, s);
+    if (w->d.emission_enabled) stage_emission(w, s);
+    stage_motion(w, s);
+    stage_slow_fields(w, s);
+    stage_lifecycle(w, s);
+    stage_clock(w);
+}
+
+uint32_t parity_bits(const agb_world* w) {
+    uint32_t p = 0;
+    for (int f = 0; f < AGB_FIELD_COUNT; ++f) p |= (uint32_t)w->gcur[f] << f;
+    return p;
+}
+
+void invalidate_graphs(agb_world* w) {
+    for (auto& g : w->graphs) cudaGraphExecDestroy(g.exec);
+    w->graphs.clear();
+}
+
+agb_status read_state(agb_world* w, DevState& out, cudaStream_t s) {
+    AGB_CUDA(w, cudaMemcpyAsync(&out, w->S, sizeof(DevState), cudaMemcpyDeviceToHost, s));
+    AGB_CUDA(w, cudaStreamSynchronize(s));
+    return AGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void agb_world_desc_default(agb_world_desc* d) {
+    std::memset(d, 0, sizeof(*d));
+    d->abi_version = AGB_ABI_VERSION;
+    d->chamber_w = AGB_CHAMBER_W;
+    d->chamber_h = AGB_CHAMBER_H;
+    d->chamber_d = AGB_CHAMBER_D;
+    d->capacity = AGB_DEFAULT_CELLS;
+    d->seed = 20260802ull;
+    d->boundary_x = d->boundary_y = AGB_WALL_REFLECTING;
+    d->gravity_axis = AGB_GRAVITY_Y;
+    d->thermal_noise = d->contact_enabled = d->adhesion_enabled = d->thermal_enabled = 1;
+    d->emission_enabled = d->taxis_enabled = d->occlusion_exact = 1;
+    d->compaction_enabled = 0;
+    d->store_disposition = AGB_STORE_VOID;
+    d->ambient_temp = AGB_AMBIENT_TEMP_DEFAULT;
+    const struct { int n; double D, init, scale; int bc; } g[4] = {
+        {AGB_FIELD_N_TEMP, AGB_WATER_THERMAL_DIFFUSIVITY, AGB_AMBIENT_TEMP_DEFAULT, AGB_DEPOSIT_SCALE_TEMPERATURE, AGB_BC_ROBIN},
+        {AGB_FIELD_N_CO2, AGB_CO2_DIFFUSIVITY_WATER, 0.0, AGB_DEPOSIT_SCALE_CO2, AGB_BC_NEUMANN},
+        {AGB_FIELD_N_N2, AGB_N2_DIFFUSIVITY, 0.0, AGB_DEPOSIT_SCALE_N2, AGB_BC_NEUMANN},
+        {AGB_FIELD_N_IRRAD, AGB_IRRADIANCE_NOMINAL_DIFFUSIVITY, 0.0, AGB_DEPOSIT_SCALE_IRRADIANCE, AGB_BC_NEUMANN}};
+    for (int f = 0; f < 4; ++f) {
+        d->grid[f].nx = d->grid[f].ny = g[f].n;
+        d->grid[f].nz = 1;
+        for (int k = 0; k < 6; ++k) { d->grid[f].bc[k] = g[f].bc; d->grid[f].face_value[k] = g[f].init; }
+        d->grid[f].diffusivity = g[f].D;
+        d->grid[f].init = g[f].init;
+        d->grid[f].deposit_scale = g[f].scale;
+    }
+    d->hash_cell_size = AGB_HASH_CELL_FACTOR * AGB_CELL_DIAMETER;
+    d->light.dir_x = 1.0f;
+    d->physics_rate = 1.0;
+    d->biology_rate = 1.0;
+    d->co2_mass_per_division = AGB_CO2_MASS_PER_DIVISION;
+    d->division_predicate = AGB_DIVIDE_CO2_QUOTA;
+    d->compaction_period = 1;
+    d->trap_slot = -1;
+}
+
+const char* agb_status_str(agb_status s) {
+    static const char* names[] = {"Ok", "OutOfMemory", "CudaError", "InvalidArgument", "NotFound",
+                                  "ParseError", "ContractVersionMismatch", "CapacityExceeded",
+                                  "FileIoError", "Unsupported", "DeviceTimeout"};
+    return (s >= 0 && s <= 10) ? names[s] : "Unknown";
+}
+
+const char* agb_last_error(const agb_world* w) { return w ? w->err.c_str() : ""; }
+
+agb_status agb_device_info(int32_t* device, int32_t* sm_version, int32_t* sm_count) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return AGB_CUDA_ERROR;
+    cudaDeviceProp p;
+    if (cudaGetDeviceProperties(&p, dev) != cudaSuccess) return AGB_CUDA_ERROR;
+    if (device) *device = dev;
+    if (sm_version) *sm_version = p.major * 10 + p.minor;
+    if (sm_count) *sm_count = p.multiProcessorCount;
+    return AGB_OK;
+}
+
+void agb_world_destroy(agb_world* w) {
+    if (!w) return;
+    invalidate_graphs(w);
+    if (w->own_stream) cudaStreamDestroy(w->own_stream);
+    for (void* p : w->allocs) cudaFree(p);
+    delete w;
+}
+
+agb_status agb_world_create(const agb_world_desc* d, agb_world** out) {
+    if (!out) return AGB_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (!d || d->abi_version != AGB_ABI_VERSION) return AGB_CONTRACT_VERSION_MISMATCH;
+    if (d->capacity <= 0 || d->capacity > AGB_MAX_CELLS) return AGB_INVALID_ARGUMENT;
+    if (!(d->chamber_w > 0 && d->chamber_h > 0 && d->chamber_d > 0) || d->chamber_w > 0.4 ||
+        d->chamber_h > 0.4 || d->chamber_d > 0.4)
+        return AGB_INVALID_ARGUMENT;
+    if (d->taxis_enabled) return AGB_UNSUPPORTED;
+    agb_world* w = new (std::nothrow) agb_world();
+    if (!w) return AGB_OUT_OF_MEMORY;
+    w->d = *d;
+    w->physics_rate = d->physics_rate;
+    w->biology_rate = d->biology_rate;
+    if (cudaGetDevice(&w->dev) != cudaSuccess) { delete w; return AGB_CUDA_ERROR; }
+    cudaDeviceGetAttribute(&w->sm_count, cudaDevAttrMultiProcessorCount, w->dev);
+    const int32_t cap = d->capacity;
+    {
+        const int64_t b = (cap + 255) / 256;
+        const int64_t lim = (int64_t)(w->sm_count > 0 ? w->sm_count : 1) * 8;
+        w->blocks = (int32_t)(b < lim ? b : lim);
+    }
+    Ctx& c = w->c;
+    c.chamber_w = d->chamber_w; c.chamber_h = d->chamber_h; c.chamber_d = d->chamber_d;
+    c.capacity = cap;
+    c.seed = d->seed;
+    c.boundary_x = d->boundary_x; c.boundary_y = d->boundary_y; c.gravity_axis = d->gravity_axis;
+    c.thermal_noise = d->thermal_noise; c.contact_enabled = d->contact_enabled;
+    c.adhesion_enabled = d->adhesion_enabled; c.occlusion_exact = d->occlusion_exact;
+    c.store_disposition = d->store_disposition; c.division_predicate = d->division_predicate;
+    c.division_energy = d->division_energy;
+    c.co2_quota = d->co2_mass_per_division;
+    c.trap_slot = d->trap_slot; c.trap_x = d->trap_x; c.trap_y = d->trap_y;
+    const double halves[3] = {0.5 * d->chamber_w, 0.5 * d->chamber_h, 0.5 * d->chamber_d};
+    for (int a = 0; a < 3; ++a) {
+        c.half[a] = halves[a];
+        c.lo[a] = -halves[a] + AGB_CELL_RADIUS;
+        c.hi[a] = halves[a] - AGB_CELL_RADIUS;
+        c.lo_key[a] = dkey_host(c.lo[a]);
+        c.hi_key[a] = dkey_host(c.hi[a]);
+    }
+    c.stamp_alive = std::llround(AGB_CELL_CROSS_SECTION * AGB_DEPOSIT_SCALE_IRRADIANCE);
+    c.stamp_dead = std::llround(AGB_CELL_CROSS_SECTION * (1.0 - AGB_CELL_ALBEDO_DEAD) * AGB_DEPOSIT_SCALE_IRRADIANCE);
+    c.setpoint_up = float_at_or_above(AGB_CELL_TEMP_SETPOINT);
+    c.setpoint_hi = (float)AGB_CELL_TEMP_SETPOINT;
+    c.setpoint_lo = (float)(AGB_CELL_TEMP_SETPOINT - (double)c.setpoint_hi);
+    c.lethal_f = float_at_or_below(AGB_CELL_LETHAL_TEMP);
+    c.stick_bits = (uint64_t)std::ceil(AGB_WALL_STICKINESS * 9007199254740992.0);
+
+    // Fields (grid_create, src/fields/diffuse.cu:91-119).
+    for (int f = 0; f < AGB_FIELD_COUNT; ++f) {
+        const agb_grid_desc& gd = d->grid[f];
+        GridDev& g = c.g[f];
+        std::memset(&g, 0, sizeof(g));
+        if (gd.nx <= 0) continue;
+        if (gd.nx <= 1 || gd.ny <= 1 || gd.nz < 1) { agb_world_destroy(w); return AGB_INVALID_ARGUMENT; }
+        g.enabled = 1;
+        g.nx = gd.nx; g.ny = gd.ny; g.nz = gd.nz;
+        g.count = (int64_t)gd.nx * gd.ny * gd.nz;
+        g.dx = d->chamber_w / (double)gd.nx;
+        g.dz_eff = d->chamber_d / (double)gd.nz;
+        if (gd.nz > 1 && std::fabs(g.dz_eff / g.dx - 1.0) > 1e-9) { agb_world_destroy(w); return AGB_UNSUPPORTED; }
+        g.dxf = (float)g.dx;
+        g.dzf = gd.nz > 1 ? (float)g.dz_eff : 0.0f;
+        g.hx = 0.5f * gd.nx * g.dxf;
+        g.hy = 0.5f * gd.ny * g.dxf;
+        g.hz = 0.5f * gd.nz * g.dzf;
+        g.scale = gd.deposit_scale;
+        g.inv_scale_f = (float)(1.0 / gd.deposit_scale);
+        for (int k = 0; k < 6; ++k) { w->gbc[f][k] = gd.bc[k]; w->gface[f][k] = (float)gd.face_value[k]; }
+        w->grobin[f] = (float)(g.dx * AGB_AIR_CONVECTION_H / AGB_WATER_CONDUCTIVITY);
+        for (int b = 0; b < 2; ++b)
+            if (dalloc(w, &w->gbuf[f][b], sizeof(float) * g.count) != cudaSuccess) {
+                agb_world_destroy(w); return AGB_OUT_OF_MEMORY;
+            }
+        if (dalloc(w, &w->gdep[f], sizeof(unsigned long long) * g.count) != cudaSuccess ||
+            cudaMemset(w->gdep[f], 0, sizeof(unsigned long long) * g.count) != cudaSuccess) {
+            agb_world_destroy(w); return AGB_OUT_OF_MEMORY;
+        }
+        g.deposit = w->gdep[f];
+        launch_fill(w->gbuf[f][0], g.count, (float)gd.init, nullptr);
+        launch_fill(w->gbuf[f][1], g.count, (float)gd.init, nullptr);
+    }
+    refresh_grid_ptrs(w);
+    compute_light(w);
+
+    // Hash (hash_create, src/sim/hash.cu:46-80).
+    HashDev& h = c.h;
+    const double cell = d->hash_cell_size > 0.0 ? d->hash_cell_size : AGB_HASH_CELL_FACTOR * AGB_CELL_DIAMETER;
+    h.nx = std::max(1, (int32_t)std::ceil(d->chamber_w / cell));
+    h.ny = std::max(1, (int32_t)std::ceil(d->chamber_h / cell));
+    h.nz = std::max(1, (int32_t)std::ceil(d->chamber_d / cell));
+    if ((double)h.nx * h.ny * h.nz >= 2147483647.0) { agb_world_destroy(w); return AGB_INVALID_ARGUMENT; }
+    h.buckets = h.nx * h.ny * h.nz;
+    h.cellf = (float)cell;
+    h.inv = (float)(1.0 / cell);
+    h.ox = (float)(-0.5 * h.nx * cell);
+    h.oy = (float)(-0.5 * h.ny * cell);
+    h.oz = (float)(-0.5 * h.nz * cell);
+    // |FP32 bucket coordinate - FP64 one| <= ~3 * 2^-24 * n; twice that margin.
+    h.margin = (float)(4.0e-7 * std::max(h.nx, std::max(h.ny, h.nz)) + 1.0e-6);
+    // Fixed-point exponent: the largest K with |x| * 2^K < 2^62 over the chamber.
+    {
+        const double half = 0.5 * std::max(d->chamber_w, std::max(d->chamber_h, d->chamber_d));
+        h.fix_k = 62 - (int32_t)std::ceil(std::log2(half));
+        h.fix_inv = std::ldexp(1.0, -h.fix_k);
+        h.fix_inv_f = (float)h.fix_inv;
+    }
+    const size_t n = (size_t)cap;
+    const int32_t tiles = (cap + 255) / 256;             // radix tiles (k_hash.cu)
+    bool ok = dalloc(w, &h.keys, 4 * n) == cudaSuccess && dalloc(w, &h.vals, 4 * n) == cudaSuccess &&
+              dalloc(w, &h.keys_sorted, 4 * n) == cudaSuccess && dalloc(w, &h.vals_sorted, 4 * n) == cudaSuccess &&
+              dalloc(w, &w->kalt, 4 * n) == cudaSuccess && dalloc(w, &w->valt, 4 * n) == cudaSuccess &&
+              dalloc(w, &w->hist, 4 * 256 * ((size_t)tiles + 1)) == cudaSuccess &&
+              dalloc(w, &h.ranges, 8 * (size_t)h.buckets) == cudaSuccess &&
+              dalloc(w, &h.snapA, 16 * n) == cudaSuccess && dalloc(w, &h.snapB, 16 * n) == cudaSuccess;
+    h.keys_prev = nullptr;
+    // Cells: two SoA blobs (live + compaction target).
+    w->blob_bytes = soa_bytes(cap);
+    ok = ok && dalloc(w, &w->blob[0], w->blob_bytes) == cudaSuccess &&
+         dalloc(w, &w->blob[1], w->blob_bytes) == cudaSuccess;
+    const int32_t stiles = (cap + 1023) / 1024;
+    ok = ok && dalloc(w, &w->life.flags, 4 * n) == cudaSuccess && dalloc(w, &w->life.prefix, 4 * n) == cudaSuccess &&
+         dalloc(w, &w->life.tile_sums, 4 * (size_t)stiles) == cudaSuccess &&
+         dalloc(w, &w->life.src, 4 * n) == cudaSuccess &&
+         dalloc(w, &w->stamp_idx, 4 * n) == cudaSuccess && dalloc(w, &w->fx, 4 * n) == cudaSuccess &&
+         dalloc(w, &w->fy, 4 * n) == cudaSuccess && dalloc(w, &w->fz, 4 * n) == cudaSuccess &&
+         dalloc(w, &w->acc, 8 * 12) == cudaSuccess && dalloc(w, &w->S, sizeof(DevState)) == cudaSuccess;
+    const int64_t co2n = c.g[AGB_FIELD_CO2].enabled ? c.g[AGB_FIELD_CO2].count : 1;
+    ok = ok && dalloc(w, &w->life.co2_demand, 8 * (size_t)co2n) == cudaSuccess;
+    if (!ok) { agb_world_destroy(w); return AGB_OUT_OF_MEMORY; }
+    cudaMemset(h.ranges, 0, 8 * (size_t)h.buckets);
+    cudaMemset(h.keys_sorted, 0, 4 * n);
+    cudaMemset(w->blob[0], 0, w->blob_bytes);
+    cudaMemset(w->blob[1], 0, w->blob_bytes);
+    cudaMemset(w->life.co2_demand, 0, 8 * (size_t)co2n);
+    cudaMemset(w->stamp_idx, 0xFF, 4 * n);
+    DevState st{};
+    st.cur = carve(w->blob[0], cap);
+    st.spare = carve(w->blob[1], cap);
+    st.next_id = 1;                                       // src/sim/cell_store.cuh:42
+    if (cudaMemcpy(w->S, &st, sizeof(st), cudaMemcpyHostToDevice) != cudaSuccess) {
+        agb_world_destroy(w); return AGB_CUDA_ERROR;
+    }
+    const agb_status ps = compute_tick_params(w);
+    if (ps != AGB_OK) { agb_world_destroy(w); return ps; }
+    const cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) { agb_world_destroy(w); return AGB_CUDA_ERROR; }
+    *out = w;
+    return AGB_OK;
+}
+
+agb_status agb_world_spawn(agb_world* w, const agb_spawn* p, agb_stream s) {
+    if (!w || !p) return AGB_INVALID_ARGUMENT;
+    if (p->count <= 0) return AGB_OK;
+    if (p->placement == AGB_PLACE_CLUSTERS && p->clusters <= 0) return fail(w, AGB_INVALID_ARGUMENT, "clusters");
+    DevState st;
+    agb_status rc = read_state(w, st, s);
+    if (rc) return rc;
+    if (st.count + p->count > w->c.capacity) return fail(w, AGB_CAPACITY_EXCEEDED, "spawn exceeds capacity");
+    launch_spawn(w->S, w->c, *p, w->blocks, s);
+    AGB_CUDA(w, cudaGetLastError());
+    return AGB_OK;
+}
+
+agb_status agb_world_count(agb_world* w, int32_t* count, agb_stream s) {
+    DevState st;
+    const agb_status rc = read_state(w, st, s);
+    if (rc) return rc;
+    *count = st.count;
+    return AGB_OK;
+}
+
+agb_status agb_world_device_cells(agb_world* w, agb_cells* dev) {
+    DevState st;
+    const agb_status rc = read_state(w, st, nullptr);
+    if (rc) return rc;
+    const SoA& v = st.cur;
+    agb_cells c = {v.id, v.flags, v.death_cause, v.x, v.y, v.z, v.vx, v.vy, v.vz, v.energy,
+                   v.temp_cell, v.emit_power, v.dir_x, v.dir_y, v.dir_z, v.biomass, v.co2_held,
+                   v.age_s, v.rng_state, v.taxis_memory, v.run_timer, v.t_local, v.irradiance,
+                   v.co2_local, v.n2_local};
+    *dev = c;
+    return AGB_OK;
+}
+
+agb_status agb_world_import_cells(agb_world* w, const agb_cells* src, int32_t count, uint64_t next_id,
+                                  agb_stream s) {
+    if (!w || !src || count < 0) return AGB_INVALID_ARGUMENT;
+    if (count > w->c.capacity) return fail(w, AGB_CAPACITY_EXCEEDED, "import exceeds capacity");
+    DevState st;
+    agb_status rc = read_state(w, st, s);
+    if (rc) return rc;
+    void* dst[25];
+    void* hst[25];
+    soa_arrays(st.cur, dst);
+    host_arrays(src, hst);
+    for (int k = 0; k < 25; ++k)
+        if (hst[k] && count > 0)
+            AGB_CUDA(w, cudaMemcpyAsync(dst[k], hst[k], kElem[k] * (size_t)count, cudaMemcpyHostToDevice, s));
+    st.count = count;
+    st.next_id = next_id;
+    AGB_CUDA(w, cudaMemcpyAsync(&w->S->count, &st.count, sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    AGB_CUDA(w, cudaMemcpyAsync(&w->S->next_id, &st.next_id, sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+    AGB_CUDA(w, cudaStreamSynchronize(s));
+    return AGB_OK;
+}
+
+agb_status agb_world_export_cells(agb_world* w, agb_cells* dst, int32_t max_count, int32_t* count,
+                                  uint64_t* next_id, agb_stream s) {
+    if (!w || !dst) return AGB_INVALID_ARGUMENT;
+    DevState st;
+    agb_status rc = read_state(w, st, s);
+    if (rc) return rc;
+    const int32_t n = st.count < max_count ? st.count : max_count;
+    void* srcp[25];
+    void* hst[25];
+    soa_arrays(st.cur, srcp);
+    host_arrays(dst, hst);
+    for (int k = 0; k < 25; ++k)
+        if (hst[k] && n > 0)
+            AGB_CUDA(w, cudaMemcpyAsync(hst[k], srcp[k], kElem[k] * (size_t)n, cudaMemcpyDeviceToHost, s));
+    AGB_CUDA(w, cudaStreamSynchronize(s));
+    if (count) *count = st.count;
+    if (next_id) *next_id = st.next_id;
+    return AGB_OK;
+}
+
+agb_status agb_world_import_field(agb_world* w, int32_t f, const float* src, agb_stream s) {
+    if (!w || f < 0 || f >= AGB_FIELD_COUNT || !w->c.g[f].enabled || !src) return AGB_INVALID_ARGUMENT;
+    AGB_CUDA(w, cudaMemcpyAsync(field_value(w, f), src, sizeof(float) * w->c.g[f].count,
+                                cudaMemcpyHostToDevice, s));
+    AGB_CUDA(w, cudaStreamSynchronize(s));
+    return AGB_OK;
+}
+
+agb_status agb_world_export_field(agb_world* w, int32_t f, float* dst, agb_stream s) {
+    if (!w || f < 0 || f >= AGB_FIELD_COUNT || !w->c.g[f].enabled || !dst) return AGB_INVALID_ARGUMENT;
+    AGB_CUDA(w, cudaMemcpyAsync(dst, field_value(w, f), sizeof(float) * w->c.g[f].count,
+                                cudaMemcpyDeviceToHost, s));
+    AGB_CUDA(w, cudaStreamSynchronize(s));
+    return AGB_OK;
+}
+
+agb_status agb_world_export_deposit(agb_world* w, int32_t f, uint64_t* dst, agb_stream s) {
+    if (!w || f < 0 || f >= AGB_FIELD_COUNT || !w->c.g[f].enabled || !dst) return AGB_INVALID_ARGUMENT;
+    AGB_CUDA(w, cudaMemcpyAsync(dst, w->gdep[f], 8 * w->c.g[f].count, cudaMemcpyDeviceToHost, s));
+    AGB_CUDA(w, cudaStreamSynchronize(s));
+    return AGB_OK;
+}
+
+agb_status agb_world_step(agb_world* w, int32_t ticks, agb_stream s) {
+    if (!w || ticks < 0) return AGB_INVALID_ARGUMENT;
+    for (int32_t t = 0; t < ticks; ++t) tick_once(w, s);
+    AGB_CUDA(w, cudaGetLastError());
+    return AGB_OK;
+}
+
+agb_status agb_world_step_graph(agb_world* w, int32_t ticks, agb_stream s) {
+    if (!w || ticks <= 0) return AGB_INVALID_ARGUMENT;
+    const uint64_t P = w->d.compaction_period > 0 ? (uint64_t)w->d.compaction_period : 1;
+    const uint32_t par = parity_bits(w);
+    const uint64_t phase = w->tick % P;
+    if (s == nullptr && w->own_stream) s = w->own_stream;
+    for (const GraphEntry& g : w->graphs) {
+        if (g.ticks == ticks && g.parity == par && g.tick_phase == phase) {
+            AGB_CUDA(w, cudaGraphLaunch(g.exec, s));
+            w->last_graph_kernels = g.kernels;
+            for (int f = 0; f < AGB_FIELD_COUNT; ++f) w->gcur[f] = (g.parity_after >> f) & 1;
+            refresh_grid_ptrs(w);
+            w->tick += (uint64_t)ticks;
+            w->sim_time += w->tp.dt * ticks;
+            return AGB_OK;
+        }
+    }
+    if (s == nullptr) {
+        // Capture needs a stream other than the legacy default one; a blocking
+        // stream keeps the launch ordered with the caller's default-stream work.
+        if (!w->own_stream) AGB_CUDA(w, cudaStreamCreate(&w->own_stream));
+        s = w->own_stream;
+    }
+    cudaGraph_t graph;
+    AGB_CUDA(w, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    for (int32_t t = 0; t < ticks; ++t) tick_once(w, s);
+    const cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    if (ce != cudaSuccess) return cuda_fail(w, ce, "cudaStreamEndCapture");
+    GraphEntry e{ticks, par, phase, nullptr, parity_bits(w), 0};
+    {
+        size_t nn = 0;
+        cudaGraphGetNodes(graph, nullptr, &nn);
+        std::vector<cudaGraphNode_t> nodes(nn);
+        if (nn) cudaGraphGetNodes(graph, nodes.data(), &nn);
+        for (auto nd : nodes) {
+            cudaGraphNodeType t;
+            if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++e.kernels;
+        }
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&e.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) return cuda_fail(w, ie, "cudaGraphInstantiate");
+    w->graphs.push_back(e);
+    w->last_graph_kernels = e.kernels;
+    // Capture advanced the host-side tick state; the graph has not run yet.
+    AGB_CUDA(w, cudaGraphLaunch(e.exec, s));
+    return AGB_OK;
+}
+
+agb_status agb_world_graph_kernels(agb_world* w, int32_t* kernels) {
+    if (!w || !kernels) return AGB_INVALID_ARGUMENT;
+    *kernels = w->last_graph_kernels;
+    return AGB_OK;
+}
+
+agb_status agb_world_stage(agb_world* w, int32_t stage, agb_stream s) {
+    if (!w) return AGB_INVALID_ARGUMENT;
+    switch (stage) {
+        case AGB_STAGE_HASH: stage_hash(w, s); break;
+        case AGB_STAGE_THERMAL: stage_thermal(w, s); break;
+        case AGB_STAGE_EMISSION: stage_emission(w, s); break;
+        case AGB_STAGE_MOTION: stage_motion(w, s); break;
+        case AGB_STAGE_SLOW_FIELDS: stage_slow_fields(w, s); break;
+        case AGB_STAGE_LIFECYCLE: stage_lifecycle(w, s); break;
+        case AGB_STAGE_COMPACT: launch_compact(w->S, w->c, w->life, w->blocks, s); break;
+        case AGB_STAGE_CLOCK: stage_clock(w); break;
+        default: return AGB_INVALID_ARGUMENT;
+    }
+    AGB_CUDA(w, cudaGetLastError());
+    return AGB_OK;
+}
+
+agb_status agb_world_diffuse(agb_world* w, int32_t f, double dt, agb_stream s) {
+    if (!w || f < 0 || f >= AGB_FIELD_COUNT) return AGB_INVALID_ARGUMENT;
+    const GridDev& g = w->c.g[f];
+    if (!g.enabled) return AGB_OK;
+    const double D = w->d.grid[f].diffusivity;
+    const int32_t steps = substeps_for(g, D, dt);         // grid_diffuse, diffuse.cu:159-186
+    if (steps <= 0) return AGB_OK;
+    const float coeff = (float)(D * (dt / steps) / (g.dx * g.dx));
+    if (!coeff_ok(g, coeff)) return fail(w, AGB_INVALID_ARGUMENT, "diffusion coefficient unstable");
+    for (int32_t k = 0; k < steps; ++k) ftcs(w, f, coeff, s);
+    AGB_CUDA(w, cudaGetLastError());
+    return AGB_OK;
+}
+
+agb_status agb_world_stats(agb_world* w, agb_stats* out, agb_stream s) {
+    if (!w || !out) return AGB_INVALID_ARGUMENT;
+    refresh_grid_ptrs(w);
+    launch_stats(w->S, w->c, w->acc, w->blocks, s);
+    AGB_CUDA(w, cudaGetLastError());
+    AGB_CUDA(w, cudaMemcpyAsync(w->acc_host, w->acc, sizeof(w->acc_host), cudaMemcpyDeviceToHost, s));
+    DevState st;
+    agb_status rc = read_state(w, st, s);
+    if (rc) return rc;
+    const unsigned long long* a = w->acc_host;
+    auto fx = [](unsigned long long raw, double scale) { return (double)(long long)raw / scale; };
+    agb_stats r;
+    std::memset(&r, 0, sizeof(r));
+    r.tick = w->tick;                                     // world_stats, src/sim/stats.cu:102-153
+    r.sim_time_s = w->sim_time;
+    r.physics_rate = w->physics_rate;
+    r.biology_rate = w->biology_rate;
+    const unsigned n_alive = (unsigned)a[7], n_dead = (unsigned)a[8];
+    r.n_live = (int32_t)n_alive;
+    r.n_dead = (int32_t)n_dead;
+    r.n_awake = (int32_t)a[9];
+    r.n_dormant = (int32_t)a[10];
+    r.total_energy_j = fx(a[0], AGB_DEPOSIT_SCALE_STATS);
+    r.mean_charge = (n_alive + n_dead) > 0u ? r.total_energy_j / ((n_alive + n_dead) * AGB_CELL_ENERGY_MAX) : 0.0;
+    r.mean_temp_cell_k = n_alive > 0u ? fx(a[1], AGB_DEPOSIT_SCALE_STATS) / n_alive : 0.0;
+    const GridDev& T = w->c.g[AGB_FIELD_TEMPERATURE];
+    const double cells = T.enabled ? (double)T.count : 0.0;
+    r.mean_temp_medium_k = cells > 0.0 ? fx(a[2], AGB_DEPOSIT_SCALE_STATS) / cells : 0.0;
+    r.max_temp_medium_k = fx(a[5], AGB_DEPOSIT_SCALE_STATS);
+    const GridDev& C2 = w->c.g[AGB_FIELD_CO2];
+    const GridDev& N2 = w->c.g[AGB_FIELD_N2];
+    const double vc = C2.enabled ? C2.dx * C2.dx * C2.dz_eff : 0.0;
+    const double vn = N2.enabled ? N2.dx * N2.dx * N2.dz_eff : 0.0;
+    r.co2_total_kg = fx(a[3], AGB_STATS_SCALE_FIELD) * vc;
+    r.n2_total_kg = fx(a[4], AGB_STATS_SCALE_FIELD) * vn;
+    r.divisions_this_window = st.divisions_this_window;
+    r.deaths_this_window = (int32_t)(st.deaths_total - w->deaths_reported);
+    w->deaths_reported = st.deaths_total;
+    const int32_t zero = 0;
+    AGB_CUDA(w, cudaMemcpyAsync(&w->S->divisions_this_window, &zero, sizeof(zero), cudaMemcpyHostToDevice, s));
+    AGB_CUDA(w, cudaStreamSynchronize(s));
+    r.boil_events = r.max_temp_medium_k >= AGB_WATER_BOILING_POINT ? 1 : 0;
+    *out = r;
+    return AGB_OK;
+}
+
+agb_status agb_world_stats_accum(agb_world* w, uint64_t out[12]) {
+    if (!w || !out) return AGB_INVALID_ARGUMENT;
+    for (int k = 0; k < 12; ++k) out[k] = w->acc_host[k];
+    return AGB_OK;
+}
+
+agb_status agb_world_set_clock(agb_world* w, double p, double b) {   // world_set_clock, step.cu:206-215
+    if (!w) return AGB_INVALID_ARGUMENT;
+    w->physics_rate = p < AGB_CLOCK_PHYSICS_MIN ? AGB_CLOCK_PHYSICS_MIN : (p > AGB_CLOCK_PHYSICS_MAX ? AGB_CLOCK_PHYSICS_MAX : p);
+    w->biology_rate = b < AGB_CLOCK_BIOLOGY_MIN ? AGB_CLOCK_BIOLOGY_MIN : (b > AGB_CLOCK_BIOLOGY_MAX ? AGB_CLOCK_BIOLOGY_MAX : b);
+    invalidate_graphs(w);
+    return compute_tick_params(w);
+}
+
+agb_status agb_world_set_light(agb_world* w, const agb_light* light) {
+    if (!w || !light) return AGB_INVALID_ARGUMENT;
+    w->d.light = *light;
+    compute_light(w);
+    invalidate_graphs(w);
+    return AGB_OK;
+}
+
+agb_status agb_world_export_hash(agb_world* w, int32_t dims[4], uint32_t* keys_sorted, uint32_t* vals_sorted,
+                                 int32_t* bucket_start, int32_t* bucket_end, agb_stream s) {
+    if (!w || !dims) return AGB_INVALID_ARGUMENT;
+    const HashDev& h = w->c.h;
+    dims[0] = h.nx; dims[1] = h.ny; dims[2] = h.nz; dims[3] = h.buckets;
+    DevState st;
+    agb_status rc = read_state(w, st, s);
+    if (rc) return rc;
+    const int32_t n = st.hash_count;
+    if (keys_sorted && n > 0)
+        AGB_CUDA(w, cudaMemcpyAsync(keys_sorted, h.keys_sorted, 4 * (size_t)n, cudaMemcpyDeviceToHost, s));
+    if (vals_sorted && n > 0)
+        AGB_CUDA(w, cudaMemcpyAsync(vals_sorted, h.vals_sorted, 4 * (size_t)n, cudaMemcpyDeviceToHost, s));
+    if (bucket_start || bucket_end) {
+        std::vector<int2> r((size_t)h.buckets);
+        AGB_CUDA(w, cudaMemcpyAsync(r.data(), h.ranges, 8 * (size_t)h.buckets, cudaMemcpyDeviceToHost, s));
+        AGB_CUDA(w, cudaStreamSynchronize(s));
+        for (int32_t b = 0; b < h.buckets; ++b) {
+            if (bucket_start) bucket_start[b] = r[b].x;
+            if (bucket_end) bucket_end[b] = r[b].y;
+        }
+    }
+    AGB_CUDA(w, cudaStreamSynchronize(s));
+    return AGB_OK;
+}
+
+agb_status agb_world_export_forces(agb_world* w, float* fx, float* fy, float* fz, agb_stream s) {
+    if (!w) return AGB_INVALID_ARGUMENT;
+    DevState st;
+    agb_status rc = read_state(w, st, s);
+    if (rc) return rc;
+    const size_t b = 4 * (size_t)st.count;
+    if (b) {
+        if (fx) AGB_CUDA(w, cudaMemcpyAsync(fx, w->fx, b, cudaMemcpyDeviceToHost, s));
+        if (fy) AGB_CUDA(w, cudaMemcpyAsync(fy, w->fy, b, cudaMemcpyDeviceToHost, s));
+        if (fz) AGB_CUDA(w, cudaMemcpyAsync(fz, w->fz, b, cudaMemcpyDeviceToHost, s));
+    }
+    AGB_CUDA(w, cudaStreamSynchronize(s));
+    return AGB_OK;
+}
+
+agb_status agb_world_counters(agb_world* w, int64_t out[4], agb_stream s) {
+    if (!w || !out) return AGB_INVALID_ARGUMENT;
+    DevState st;
+    agb_status rc = read_state(w, st, s);
+    if (rc) return rc;
+    out[0] = st.divisions_this_window;
+    out[1] = st.deaths_total;
+    out[2] = st.dead_slots_prev;
+    out[3] = st.error;
+    return AGB_OK;
+}
+
+}  // extern "C"

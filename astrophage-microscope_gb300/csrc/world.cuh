@@ -1,0 +1,64 @@
+// world.cuh -- per-world constants (Ctx, passed by value to kernels) and the
+// host-side world object behind the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "dev.cuh"
+
+namespace agb {
+
+// Everything a kernel needs that does not change during a tick.
+struct Ctx {
+    GridDev g[AGB_FIELD_COUNT];
+    HashDev h;
+    double chamber_w, chamber_h, chamber_d;
+    int32_t capacity;
+    uint64_t seed;
+    int32_t boundary_x, boundary_y, gravity_axis;
+    int32_t thermal_noise, contact_enabled, adhesion_enabled, occlusion_exact;
+    int32_t store_disposition, division_predicate;
+    double division_energy, co2_quota;
+    int32_t trap_slot;
+    double trap_x, trap_y;
+    // Wall limits of apply_boundary_axis (src/sim/integrator.cuh:233-254) per axis.
+    double lo[3], hi[3], half[3];
+    unsigned long long lo_key[3], hi_key[3];
+    // Light (src/sim/emission.cu:140-165)
+    float lx, ly, lz;          // unit light direction as float
+    double ldx, ldy, ldz;      // ... and as double (reference normalize)
+    int32_t light_axis, light_sign;
+    float source, ambient_irr;
+    double face_area;
+    long long stamp_alive, stamp_dead;   // fixed-point occlusion stamps
+    // Exact float thresholds equivalent to the reference's FP64 compares.
+    float setpoint_up;          // smallest float >= CELL_TEMP_SETPOINT
+    float setpoint_hi, setpoint_lo;
+    float lethal_f;             // t_local > CELL_LETHAL_TEMP  <=>  t_local > lethal_f
+    uint64_t stick_bits;        // uniform53 < stick_bits  <=>  uniform01d < WALL_STICKINESS
+};
+
+// Per-tick scalars derived from the clock.
+struct TickParams {
+    double dt;                  // DT_PHYSICS * physics_rate
+    float dtf;
+    float k_contact;            // CONTACT_STIFFNESS / physics_rate
+    double k_contact64;
+    float k_trap;
+    double dt_bio;
+    // thermal
+    int32_t t_substeps;
+    double t_dt_sub;
+    float t_coeff;
+    float t_cap_relax;          // capacity * (1 - exp(-G dt_sub / C)) as float
+    float t_relax;              // (1 - exp(-G dt_sub / C)) as float
+    double t_cap;
+    // slow fields
+    int32_t c_substeps, n_substeps;
+    float c_coeff, n_coeff;
+};
+
+}  // namespace agb

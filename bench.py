@@ -1,0 +1,422 @@
+#!/usr/bin/env python3
+"""Throughput of the per-tick physics step on GB300 (cell-steps/s, voxel-steps/s).
+
+Default workload (the plain step at README scale): a 4 mm cubic chamber with
+25,000 cells uniform in a 550 um-wide slab, lognormal charge (median 3 %,
+sigma_ln 0.5, clipped at 0.2), 128^3 temperature and CO2 grids, light along +x,
+division at a stored-energy threshold with compaction every 10 ticks, dt = 1 ms.
+Inputs are synthetic and seeded (the engine's own PCG32 spawn).
+
+One bench step is one tick of the whole world, replayed as a CUDA graph. The
+L2 cache is flushed (a 256 MB write) between timed steps, outside the timed
+intervals, which are CUDA events on the stream the tick runs on.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the reference algorithm on the host cores instead: the
+C oracle (a restatement of the reference's kernel bodies, pinned to the
+reference's own outputs) over the same world with all host threads.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+import helpers as H  # noqa: E402  (engine bindings; the oracle only for the CPU legs)
+
+agb = H.agb
+METRIC = "cell-steps/s & voxel-steps/s, 1 GB300: plain vs batched+surrogate @<=0.01 K err"
+EMAX = agb.CELL_ENERGY_MAX
+
+
+# ---------------------------------------------------------------------------
+# Workloads
+# ---------------------------------------------------------------------------
+def _grid3(n, D, init, scale, bc, face=None):
+    return agb.grid(n, n, D, init, scale, bc, face_value=face)
+
+
+def workload(name, seed=1):
+    """(desc, spawn, description) for the plain-step configurations."""
+    if name == "slab25k":
+        d = agb.default_desc(capacity=50000, seed=seed, co2_init=1.0)
+        d.chamber_w = d.chamber_h = d.chamber_d = 4.0e-3
+        d.grid[agb.FIELD_T] = _grid3(128, agb.WATER_THERMAL_DIFFUSIVITY, agb.AMBIENT_TEMP_DEFAULT, 1e9, agb.BC_ROBIN)
+        d.grid[agb.FIELD_CO2] = _grid3(128, agb.CO2_DIFFUSIVITY_WATER, 1.0, 1e15, agb.BC_NEUMANN)
+        d.grid[agb.FIELD_N2] = agb.GridDesc()
+        d.grid[agb.FIELD_IRR] = _grid3(128, agb.IRRADIANCE_NOMINAL_DIFFUSIVITY, 0.0, 1e18, agb.BC_NEUMANN)
+        d.taxis_enabled = 0
+        d.light = agb.Light(1.0, 0.0, 0.0, 1.0e4, 0.0, 1)
+        d.division_predicate = agb.DIVIDE_ENERGY
+        d.division_energy = 0.16 * EMAX
+        d.compaction_enabled = 1
+        d.compaction_period = 10
+        d.biology_rate = 1.0e5
+        sp = agb.spawn(25000, placement=agb.PLACE_SLAB_X, place_radius=275e-6, charge_dist=agb.DIST_LOGNORMAL,
+                       charge_a=0.03, charge_b=0.5, charge_max=0.2, awake=True)
+        return d, sp, dict(cells=25000, grid=128, chamber_mm=4.0, light="+x", division="energy>=0.16*Emax",
+                           compaction_period=10, hash_cell_um=22.0)
+    if name == "cube2k":
+        d = agb.default_desc(capacity=4000, seed=seed, co2_init=1.0)
+        d.chamber_w = d.chamber_h = d.chamber_d = 400e-6
+        face = [373.15, 293.15, 293.15, 293.15, 293.15, 293.15]
+        bc = [agb.BC_DIRICHLET] + [agb.BC_NEUMANN] * 5
+        d.grid[agb.FIELD_T] = _grid3(64, agb.WATER_THERMAL_DIFFUSIVITY, agb.AMBIENT_TEMP_DEFAULT, 1e9, bc, face)
+        d.grid[agb.FIELD_CO2] = _grid3(64, agb.CO2_DIFFUSIVITY_WATER, 1.0, 1e15, agb.BC_NEUMANN)
+        d.grid[agb.FIELD_N2] = agb.GridDesc()
+        d.grid[agb.FIELD_IRR] = _grid3(64, agb.IRRADIANCE_NOMINAL_DIFFUSIVITY, 0.0, 1e18, agb.BC_NEUMANN)
+        d.taxis_enabled = 0
+        d.hash_cell_size = 10e-6
+        d.light = agb.Light(0.0, 0.0, 1.0, 1.0e4, 0.0, 1)
+        sp = agb.spawn(2000, charge_dist=agb.DIST_UNIFORM, charge_a=0.0, charge_b=0.2, awake=True)
+        return d, sp, dict(cells=2000, grid=64, chamber_mm=0.4, light="+z", hash_cell_um=10.0)
+    if name == "clusters1m":
+        d = agb.default_desc(capacity=2000000, seed=seed, co2_init=1.5)
+        d.chamber_w = d.chamber_h = d.chamber_d = 4.0e-3
+        d.grid[agb.FIELD_T] = _grid3(256, agb.WATER_THERMAL_DIFFUSIVITY, agb.AMBIENT_TEMP_DEFAULT, 1e9, agb.BC_ROBIN)
+        d.grid[agb.FIELD_CO2] = _grid3(256, agb.CO2_DIFFUSIVITY_WATER, 1.5, 1e15, agb.BC_NEUMANN)
+        d.grid[agb.FIELD_N2] = agb.GridDesc()
+        d.grid[agb.FIELD_IRR] = _grid3(256, agb.IRRADIANCE_NOMINAL_DIFFUSIVITY, 0.0, 1e18, agb.BC_NEUMANN)
+        d.taxis_enabled = 0
+        d.light = agb.Light(0.0, 0.0, 1.0, 1.0e4, 0.0, 1)
+        d.compaction_enabled = 1
+        d.biology_rate = 1.38e5
+        sp = agb.spawn(1000000, placement=agb.PLACE_CLUSTERS, place_radius=40e-6, clusters=64,
+                       cluster_extent=3e-3, charge_dist=agb.DIST_UNIFORM, charge_a=0.0, charge_b=0.2, awake=True)
+        return d, sp, dict(cells=1000000, grid=256, chamber_mm=4.0, light="+z", clusters=64, hash_cell_um=22.0)
+    raise SystemExit("unknown workload " + name)
+
+
+def voxel_steps_per_tick(desc):
+    """FTCS voxel-steps of one tick: substeps x voxels for T, CO2 and N2."""
+    total = 0
+    for f in (agb.FIELD_T, agb.FIELD_CO2, agb.FIELD_N2):
+        g = desc.grid[f]
+        if g.nx <= 0:
+            continue
+        dx = desc.chamber_w / g.nx
+        lim = 6.0 if g.nz > 1 else 4.0
+        steps = int(agb.DT_PHYSICS * desc.physics_rate / (dx * dx / (lim * g.diffusivity))) + 1
+        total += steps * g.nx * g.ny * g.nz
+    return total
+
+
+# ---------------------------------------------------------------------------
+# Instrumentation
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.out = tempfile.TemporaryFile(mode="w+")
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.out.seek(0)
+        rows = [r.split(",") for r in self.out.read().strip().splitlines() if r.strip()]
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[0]))
+                mx.append(float(r[1]))
+            except (ValueError, IndexError):
+                continue
+            for k, n in enumerate(names):
+                if len(r) > 4 + k and r[4 + k].strip().lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(key):
+    """DRAM bytes per launch from the committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.exists(p):
+        return None
+    with open(p) as fh:
+        for line in fh:
+            parts = line.split()
+            if len(parts) >= 2 and parts[0] == key:
+                return float(parts[1])
+    return None
+
+
+# ---------------------------------------------------------------------------
+# Distributed plumbing (one process per GPU; replicas of independent chambers)
+# ---------------------------------------------------------------------------
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        return rank, ws, local, dist
+    return rank, ws, local, None
+
+
+def allreduce_max(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allreduce_sum(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# Arms
+# ---------------------------------------------------------------------------
+def cpu_oracle_rate(desc, sp, seconds, threads, state=None):
+    """Cell-steps/s of the C oracle on this host's cores over a bounded sample."""
+    orc = H.OracleWorld(desc, threads=threads)
+    if state is None:
+        orc.spawn(sp)
+    else:
+        cells, nid, fields = state
+        orc.import_cells(cells, nid)
+        for f, arr in fields.items():
+            orc.import_field(f, arr)
+    orc.step(1)                               # warm-up tick
+    ticks, t0 = 0, time.perf_counter()
+    cell_ticks = 0
+    while True:
+        n = orc.count()
+        orc.step(1)
+        ticks += 1
+        cell_ticks += n
+        el = time.perf_counter() - t0
+        if el >= seconds or ticks >= 2000:
+            break
+    orc.close()
+    return cell_ticks / el, ticks, el
+
+
+def run_reference(args, wl):
+    rank, ws, _, dist = (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), 0, None)
+    if rank != 0:
+        return 0
+    desc, sp, info = wl
+    threads = os.cpu_count() or 1
+    orc = H.OracleWorld(desc, threads=threads)
+    orc.spawn(sp)
+    orc.step(args.warmup)
+    cell_ticks, t0 = 0, time.perf_counter()
+    for _ in range(args.steps):
+        cell_ticks += orc.count()
+        orc.step(1)
+    el = time.perf_counter() - t0
+    value = cell_ticks / el
+    vox = voxel_steps_per_tick(desc) * args.steps / el
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded PCG32 spawn)",
+            "config": dict({"workload": args.workload}, **info),
+            "voxel_steps_per_s": vox,
+            "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": threads, "kind": "port",
+                             "sample": "%d ticks of the full workload (C oracle of the reference algorithm, "
+                                       "OpenMP over cells and voxels)" % args.steps},
+            "e2e": {"value": value, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--workload", default="slab25k", choices=["slab25k", "cube2k", "clusters1m"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    if args.impl == "reference":
+        return run_reference(args, workload(args.workload, seed=1))
+
+    import torch
+    rank, ws, local, dist = dist_init()
+    torch.cuda.set_device(local)
+    desc, sp, info = workload(args.workload, seed=1 + rank)
+    lib = agb.load()
+    world = agb.World(desc, lib)
+    world.spawn(sp)
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    l2_flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    # Initial state for the CPU baseline (before any tick).
+    state0 = None
+    if rank == 0 and not args.no_cpu:
+        cells0, nid0 = world.export_cells()
+        state0 = (cells0, nid0, {f: world.export_field(f) for f in range(4) if desc.grid[f].nx > 0})
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            world.step(1, graph=True, stream=sh)
+        torch.cuda.synchronize()
+        n_start = world.count(stream=sh)
+        kernels_per_tick = world.graph_kernels()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        sampler = ClockSampler(local)
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+        sampler.start()
+        for k in range(args.steps):
+            l2_flush.zero_()                           # L2 flush, outside the timed interval
+            starts[k].record(stream)
+            world.step(1, graph=True, stream=sh)
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+        clocks = sampler.stop()
+        if dist is not None:
+            dist.barrier()
+        n_end = world.count(stream=sh)
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_s = allreduce_max(dist, sum(step_ms) / 1e3)
+    cells_mean = 0.5 * (n_start + n_end)
+    cell_steps = allreduce_sum(dist, cells_mean * args.steps)
+    vox_steps = allreduce_sum(dist, float(voxel_steps_per_tick(desc)) * args.steps)
+    value = cell_steps / total_s
+
+    # Dominant-kernel roofline: the 3-D FTCS pass on the temperature grid, timed
+    # with events around back-to-back launches on the same stream.
+    peak, peak_kind = measured_peaks()
+    gT = desc.grid[agb.FIELD_T]
+    vox_T = gT.nx * gT.ny * gT.nz
+    reps = 50
+    with torch.cuda.stream(stream):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        world.diffuse(agb.FIELD_T, agb.DT_PHYSICS, stream=sh)
+        torch.cuda.synchronize()
+        l2_flush.zero_()
+        e0.record(stream)
+        for _ in range(reps):
+            world.diffuse(agb.FIELD_T, agb.DT_PHYSICS, stream=sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ftcs_s = e0.elapsed_time(e1) / 1e3 / reps
+    algo_bytes = 8.0 * vox_T
+    achieved = algo_bytes / ftcs_s / 1e9
+    traffic = profile_traffic("ftcs3d_%d" % gT.nx)
+
+    # End to end through the C ABI with host buffers: pinned state in, one tick,
+    # state out, every step.
+    e2e = None
+    if rank == 0:
+        n = world.count()
+        pinned = agb.CellArrays(n)
+        for name, t in agb.CELL_FIELDS:
+            pinned.a[name] = torch.empty(max(n, 1), dtype=getattr(torch, np.dtype(t).name),
+                                         pin_memory=True).numpy()
+        cells, nid = world.export_cells()
+        for name, _t in agb.CELL_FIELDS:
+            pinned.a[name][:n] = cells[name]
+        bytes_state = sum(np.dtype(t).itemsize for _n, t in agb.CELL_FIELDS) * n
+        e2e_steps = max(10, args.steps // 3)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            world.import_cells(pinned, nid, stream=sh)
+            world.step(1, graph=True, stream=sh)
+            out, nid = world.export_cells(stream=sh, into=pinned)
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        e2e = {"value": n * e2e_steps / el, "unit": "cell-steps/s", "h2d_bytes_per_step": bytes_state,
+               "d2h_bytes_per_step": bytes_state,
+               "path": "agb_world_import_cells + agb_world_step_graph + agb_world_export_cells, pinned host SoA"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        rate, ticks, el = cpu_oracle_rate(desc, sp, args.cpu_seconds, threads, state0)
+        cpu = {"value": rate, "unit": "cell-steps/s", "cores": threads, "kind": "port",
+               "sample": "%d ticks (%.1f s) of the same workload from the same initial state, C oracle "
+                         "(FP64, OpenMP over cells and voxels)" % (ticks, el)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 compute, f64 state",
+            "data": "synthetic (seeded PCG32 spawn of the workload's distributions)",
+            "config": dict({"workload": args.workload, "step": "one tick of the whole chamber",
+                            "l2": "flushed between timed steps (256 MB write, untimed)",
+                            "parallelism": "replicas (independent chambers per GPU)" if ws > 1 else "single GPU"},
+                           **info),
+            "voxel_steps_per_s": vox_steps / total_s,
+            "cells_start_end": [n_start, n_end],
+            "roofline": {"bound": "hbm", "kernel": "ftcs3d (temperature, %d^3)" % gT.nx,
+                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_source": peak_kind, "algorithmic_bytes_per_launch": algo_bytes,
+                         "launch_us": ftcs_s * 1e6, "traffic": traffic},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": kernels_per_tick * args.steps,
+            "clocks": clocks,
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -907,8 +907,8 @@ static int apply_boundary_axis(double* p, double* v, double half, double radius,
     if (*p >= lo && *p <= hi) return 1;
     if (mode == AGB_WALL_PERIODIC) {
         const double span = 2.0 * half;
-        while (*p < -half) *p += span;
-        while (*p > half) *p -= span;
+        for (int k = 0; k < 64 && *p < -half; ++k) *p += span;   /* bounded for non-finite input */
+        for (int k = 0; k < 64 && *p > half; ++k) *p -= span;
         return 1;
     }
     if (mode == AGB_WALL_ABSORBING) return 0;

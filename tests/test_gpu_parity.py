@@ -1,0 +1,187 @@
+"""GPU engine (libagb.so, through the C ABI) against the oracle, which is
+itself pinned to the reference (test_oracle_golden.py). Every comparison
+starts both from the identical imported state."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import helpers as H
+import parity as P
+import scenarios as S
+
+agb = H.agb
+pytestmark = pytest.mark.gpu
+NAMES = sorted(S.scenarios().keys())
+
+
+def pair(desc):
+    return agb.World(desc), H.OracleWorld(desc)
+
+
+def seeded(sc):
+    orc = H.OracleWorld(sc["desc"])
+    S.setup(orc, sc)
+    gpu = agb.World(sc["desc"])
+    P.copy_state(orc, gpu)
+    return gpu, orc
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_hash_bit_exact(name):
+    gpu, orc = seeded(S.scenarios()[name])
+    gpu.stage(agb.STAGE_HASH)
+    orc.stage(agb.STAGE_HASH)
+    hg, ho = gpu.export_hash(), orc.export_hash()
+    for k, what in enumerate(["dims", "keys_sorted", "vals_sorted", "bucket_start", "bucket_end"]):
+        assert np.array_equal(hg[k], ho[k]), what
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_each_stage_from_identical_state(name):
+    """One stage at a time, each from the oracle's state after the previous one."""
+    sc = S.scenarios()[name]
+    gpu, orc = seeded(sc)
+    errs = []
+    for t in range(sc["ticks"]):
+        for stage, sname in S.STAGES:
+            before, _ = orc.export_cells()
+            P.copy_state(orc, gpu)
+            if stage in (agb.STAGE_EMISSION, agb.STAGE_MOTION):
+                # Both walk the hash built at the top of the tick; positions have
+                # not moved since, so a rebuild here must reproduce it exactly.
+                gpu.stage(agb.STAGE_HASH)
+                for k, (x, y) in enumerate(zip(gpu.export_hash()[1:], orc.export_hash()[1:])):
+                    assert np.array_equal(x, y), "%s: hash array %d" % (sname, k)
+            gpu.stage(stage)
+            orc.stage(stage)
+            where = "tick %d %s" % (t, sname)
+            a, _ = gpu.export_cells()
+            b, _ = orc.export_cells()
+            errs += P.compare_cells(a, b, before, where=where)
+            errs += P.compare_fields(gpu, orc, where=where)
+            if stage == agb.STAGE_MOTION:
+                errs += P.compare_forces(gpu.export_forces(), orc.export_forces(), where)
+    assert not errs, "\n".join(errs[:20])
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_full_ticks_track_oracle(name):
+    """Whole ticks without re-synchronisation: integer state must stay equal."""
+    sc = S.scenarios()[name]
+    gpu, orc = seeded(sc)
+    before, _ = orc.export_cells()
+    gpu.step(1)
+    orc.step(1)
+    a, _ = gpu.export_cells()
+    b, _ = orc.export_cells()
+    errs = P.compare_cells(a, b, before, where="tick 0")
+    errs += P.compare_fields(gpu, orc, where="tick 0")
+    assert not errs, "\n".join(errs[:20])
+    gpu.step(sc["ticks"])
+    orc.step(sc["ticks"])
+    a, _ = gpu.export_cells()
+    b, _ = orc.export_cells()
+    assert a.n == b.n
+    for k in P.INT_FIELDS:
+        assert np.array_equal(a[k], b[k]), k
+    sg, so = gpu.stats(), orc.stats()
+    assert sg.n_live == so.n_live and sg.n_dead == so.n_dead and sg.n_awake == so.n_awake
+    assert sg.divisions_this_window == so.divisions_this_window
+    assert sg.deaths_this_window == so.deaths_this_window
+    assert abs(sg.total_energy_j - so.total_energy_j) <= 1e-9 * abs(so.total_energy_j) + 1e-6
+
+
+@pytest.mark.parametrize("name", ["slab_uniform", "lifecycle_compaction", "collinear_shadow"])
+def test_against_reference_fixture(name):
+    """The engine's first tick against the reference's own output (tests/golden)."""
+    sc = S.scenarios()[name]
+    gold = np.load(os.path.join(H.GOLDEN, name + "_tick0.npz"))
+    gpu, orc = seeded(sc)
+    before, _ = orc.export_cells()
+    gpu.step(1)
+    a, _ = gpu.export_cells()
+    ref = agb.CellArrays.from_dict({k[5:]: gold[k] for k in gold.files if k.startswith("cell_")})
+    errs = P.compare_cells(a, ref, before, where="vs reference")
+    for f in range(4):
+        g, r = gpu.export_field(f), gold["field_%d" % f]
+        tol = 1e-6 * np.max(np.abs(r)) + 1e-30
+        if np.abs(g - r).max() > tol:
+            errs.append("field %d max diff %g" % (f, float(np.abs(g - r).max())))
+    assert not errs, "\n".join(errs[:20])
+
+
+def test_collinear_rear_cell_exactly_dark():
+    sc = S.scenarios()["collinear_shadow"]
+    gpu, _ = seeded(sc)
+    gpu.step(1)
+    a, _ = gpu.export_cells()
+    assert a["irradiance"][0] > 0.0 and a["energy"][0] > 0.0
+    assert a["irradiance"][1] == 0.0 and a["energy"][1] == 0.0
+
+
+@pytest.mark.parametrize("nz,bcs", [(1, (agb.BC_NEUMANN,) * 6),
+                                    (1, (agb.BC_DIRICHLET, agb.BC_ROBIN, agb.BC_NEUMANN, agb.BC_ROBIN, 1, 1)),
+                                    (48, (agb.BC_DIRICHLET, agb.BC_NEUMANN, agb.BC_ROBIN, agb.BC_NEUMANN,
+                                          agb.BC_DIRICHLET, agb.BC_ROBIN))])
+def test_diffusion_bit_exact(nz, bcs):
+    """FTCS (src/fields/diffuse.cu:19-44) bit for bit, 2-D and 3-D, every BC kind."""
+    d = S.slab_desc(n_t=48, light=None)
+    d.chamber_d = d.chamber_w if nz > 1 else d.chamber_d
+    d.grid[agb.FIELD_T] = agb.grid(48, nz, agb.WATER_THERMAL_DIFFUSIVITY, 300.0, 1e9, list(bcs),
+                                   face_value=[373.15, 290.0, 300.0, 310.0, 280.0, 320.0])
+    gpu, orc = pair(d)
+    rng = np.random.default_rng(7)
+    f0 = (300.0 + 50.0 * rng.random((nz, 48, 48))).astype(np.float32)
+    gpu.import_field(agb.FIELD_T, f0)
+    orc.import_field(agb.FIELD_T, f0)
+    for _ in range(5):
+        gpu.diffuse(agb.FIELD_T, 1e-3)
+        orc.diffuse(agb.FIELD_T, 1e-3)
+    assert np.array_equal(gpu.export_field(agb.FIELD_T), orc.export_field(agb.FIELD_T))
+
+
+def test_spawn_matches_oracle():
+    d = S.slab_desc(cap=5000)
+    gpu, orc = pair(d)
+    for sp in (agb.spawn(1000, charge_dist=agb.DIST_UNIFORM, charge_a=0.0, charge_b=0.2, awake=True),
+               agb.spawn(700, placement=agb.PLACE_GAUSSIAN, place_radius=3e-4, charge_dist=agb.DIST_NORMAL,
+                         charge_a=0.1, charge_b=0.05),
+               agb.spawn(500, placement=agb.PLACE_DISC, place_radius=1e-3, charge_dist=agb.DIST_LOGNORMAL,
+                         charge_a=0.03, charge_b=0.5, charge_max=0.2),
+               agb.spawn(800, placement=agb.PLACE_CLUSTERS, place_radius=4e-5, clusters=8,
+                         cluster_extent=3e-3)):
+        gpu.spawn(sp)
+        orc.spawn(sp)
+    a, na = gpu.export_cells()
+    b, nb = orc.export_cells()
+    assert na == nb and a.n == b.n
+    for k in P.INT_FIELDS:
+        assert np.array_equal(a[k], b[k]), k
+    for k in ("x", "y", "z", "energy", "dir_x", "dir_y", "dir_z"):
+        assert np.allclose(a[k], b[k], rtol=1e-12, atol=1e-18), k
+
+
+def test_stats_accumulators_exact():
+    """stats.cu fixed-point sums: identical state gives identical integers."""
+    sc = S.scenarios()["hot_field"]
+    gpu, orc = seeded(sc)
+    gpu.stats(); orc.stats()
+    assert np.array_equal(gpu.stats_accum()[:11], orc.stats_accum()[:11])
+
+
+def test_graph_replay_equals_eager():
+    sc = S.scenarios()["lifecycle_compaction"]
+    g1, _ = seeded(sc)
+    g2, _ = seeded(sc)
+    g1.step(6)
+    for _ in range(3):
+        g2.step(2, graph=True)
+    a, na = g1.export_cells()
+    b, nb = g2.export_cells()
+    assert na == nb and a.n == b.n
+    for k, _t in agb.CELL_FIELDS:
+        assert np.array_equal(a[k], b[k]), k
+    for f in range(4):
+        assert np.array_equal(g1.export_field(f), g2.export_field(f))
