@@ -237,7 +237,7 @@ def load(path=LIB_PATH):
         "agb_world_step": (I32, [P, I32, P]),
         "agb_world_step_graph": (I32, [P, I32, P]),
         "agb_world_stage": (I32, [P, I32, P]),
-        "agb_world_graph_kernels": (I32, [P, C.POINTER(I32)]),
+        "agb_world_graph_kernels": (I32, [P, C.POINTER(C.c_int64)]),
         "agb_world_diffuse": (I32, [P, I32, C.c_double, P]),
         "agb_world_stats": (I32, [P, C.POINTER(Stats), P]),
         "agb_world_stats_accum": (I32, [P, P]),
@@ -351,7 +351,7 @@ class World:
         self._check(self.lib.agb_world_stage(self.h, s, None), "stage %d" % s)
 
     def graph_kernels(self):
-        k = C.c_int32()
+        k = C.c_int64()
         self._check(self.lib.agb_world_graph_kernels(self.h, C.byref(k)), "graph_kernels")
         return k.value
 

@@ -79,11 +79,13 @@ struct HashDev {
     uint32_t* vals_sorted;
     uint32_t* keys_prev;     // sorted keys of the previous build (ranges to clear)
     int2* ranges;            // dense bucket table {start, end}
-    longlong2* snapA;        // sorted-order snapshot: {X, Y} as x * 2^fix_k fixed point
-    longlong2* snapB;        // {Z, flags << 32 | slot}
-    int32_t fix_k;           // fixed-point exponent K
+    float4* rec;             // sorted-order snapshot: offsets from the bucket corner + packed bucket coords
+    int32_t fix_k;           // fixed-point exponent K of the corner arithmetic
     float fix_inv_f;         // 2^-K
     double fix_inv;
+    long long org_fix[3];    // hash origin, x * 2^K
+    long long cell_fix;      // bucket edge, x * 2^K
+    float cell_f;            // cell_fix * 2^-K
     int32_t nx, ny, nz, buckets;
     float cellf, inv, ox, oy, oz;
     float margin;            // FP32 bucket-coordinate error bound

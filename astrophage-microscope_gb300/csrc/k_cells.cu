@@ -3,10 +3,11 @@
 // (src/sim/emission.cu:17-177) and motion: field sample + forces + exact OU
 // integration (src/sim/integrator.cu:20-177).
 //
-// Forces and integration share one kernel here. The reference splits them
-// (ADR-018) because contact must read every neighbour's pre-step position; the
-// neighbour walk reads the hash's sorted snapshot, taken before any position
-// changes, so the fused kernel reads exactly what the split kernels read.
+// Forces and integration are two kernels, as in the reference (ADR-018): the
+// neighbour walks run in hash-sorted order (warp lanes share bucket
+// neighbourhoods), integration in slot order (coalesced state access). The
+// walks read the hash's sorted snapshot of positions, so they never see a
+// position this tick has already moved.
 #include <cuda_runtime.h>
 
 #include "cells.h"
@@ -46,6 +47,23 @@ __device__ __forceinline__ void walk_neighbours(const HashDev& h, int32_t gx, in
 #pragma unroll 1
     for (int r = 0; r < 9; ++r)
         for (int32_t k = lo[r]; k < hi[r]; ++k) f(k);
+}
+
+__device__ __forceinline__ void unpack_bucket(float w, int32_t& gx, int32_t& gy, int32_t& gz) {
+    const uint32_t u = __float_as_uint(w);
+    gx = (int32_t)(u & 0x7FFu);
+    gy = (int32_t)((u >> 11) & 0x7FFu);
+    gz = (int32_t)(u >> 22);
+}
+
+// Separation self - other from two snapshot records (FP32, ~2e-7 relative).
+__device__ __forceinline__ void rec_delta(const HashDev& h, const float4& a, int32_t ax, int32_t ay, int32_t az,
+                                          const float4& b, float& dx, float& dy, float& dz) {
+    int32_t bx, by, bz;
+    unpack_bucket(b.w, bx, by, bz);
+    dx = (float)(ax - bx) * h.cell_f + (a.x - b.x);
+    dy = (float)(ay - by) * h.cell_f + (a.y - b.y);
+    dz = (float)(az - bz) * h.cell_f + (a.z - b.z);
 }
 
 // ---------------------------------------------------------------------------
@@ -124,13 +142,31 @@ __global__ void stamp_kernel(DevState* S, Ctx c, int32_t* stamp_idx) {
     }
 }
 
+// column_transmittance (emission.cuh:43-47) of every stamped voxel, computed
+// once per cell in full warps (FP64 divisions in divergent sweep code would
+// cost a whole warp's FP64 issue time per stamped voxel). Duplicate cells of a
+// voxel write the same value.
+__global__ void __launch_bounds__(256) occlusion_factor_kernel(DevState* S, Ctx c,
+                                                               const int32_t* __restrict__ stamp_idx,
+                                                               double* factor) {
+    const int32_t n = S->n_stamps;
+    const GridDev I = c.g[AGB_FIELD_IRRADIANCE];
+    AGB_FOR_CELLS(i, n) {
+        const int32_t idx = stamp_idx[i];
+        if (idx < 0) continue;
+        const double area = (double)(long long)I.deposit[idx] / I.scale;   // from_fixed
+        const double tr = 1.0 - area / c.face_area;
+        factor[idx] = tr > 0.0 ? tr : 0.0;
+    }
+}
+
 // sweep_kernel (emission.cu:37-53): one thread per line in sweep order. The
 // FP64 transmittance recurrence runs only at stamped voxels (an empty voxel's
 // factor is exactly 1), and the float output only changes there, so empty
 // voxels cost one load and one store.
 constexpr int SWEEP_PF = 8;
 
-__global__ void __launch_bounds__(128) sweep_kernel(Ctx c) {
+__global__ void __launch_bounds__(128) sweep_kernel(Ctx c, const double* __restrict__ factor) {
     const GridDev I = c.g[AGB_FIELD_IRRADIANCE];
     const int32_t nx = I.nx, ny = I.ny;
     const int64_t plane = (int64_t)nx * ny;
@@ -138,8 +174,6 @@ __global__ void __launch_bounds__(128) sweep_kernel(Ctx c) {
     const int32_t len = axis == 0 ? nx : (axis == 1 ? ny : I.nz);
     const int64_t stride = axis == 0 ? 1 : (axis == 1 ? nx : plane);
     const int64_t lines = I.count / len;
-    const double inv_scale_unused = 0.0;
-    (void)inv_scale_unused;
     for (int64_t line = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; line < lines;
          line += (int64_t)gridDim.x * blockDim.x) {
         int64_t base;
@@ -163,9 +197,7 @@ __global__ void __launch_bounds__(128) sweep_kernel(Ctx c) {
                 const int32_t step = c.light_sign > 0 ? s : (len - 1 - s);
                 I.value[base + stride * step] = cur;
                 if (raw[u] != 0ull) {
-                    const double area = (double)(long long)raw[u] / I.scale;   // from_fixed
-                    const double tr = 1.0 - area / c.face_area;                // column_transmittance
-                    t *= tr > 0.0 ? tr : 0.0;
+                    t *= __ldg(&factor[base + stride * step]);
                     cur = fa(d2f((double)c.source * t), c.ambient_irr);
                 }
             }
@@ -176,7 +208,7 @@ __global__ void __launch_bounds__(128) sweep_kernel(Ctx c) {
 // x-axis sweep: rows are contiguous in memory, so one warp takes a row, 32
 // consecutive voxels per step (coalesced). Stamped voxels are rare; the FP64
 // recurrence walks them in sweep order, broadcasting each factor.
-__global__ void __launch_bounds__(256) sweep_rows_kernel(Ctx c) {
+__global__ void __launch_bounds__(256) sweep_rows_kernel(Ctx c, const double* __restrict__ factor) {
     const GridDev I = c.g[AGB_FIELD_IRRADIANCE];
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -195,12 +227,7 @@ __global__ void __launch_bounds__(256) sweep_rows_kernel(Ctx c) {
             unsigned mask = __ballot_sync(0xFFFFFFFFu, raw != 0ull);
             float mine = cur;
             if (mask) {
-                double f = 1.0;
-                if (raw != 0ull) {
-                    const double area = (double)(long long)raw / I.scale;
-                    const double tr = 1.0 - area / c.face_area;
-                    f = tr > 0.0 ? tr : 0.0;
-                }
+                const double f = raw != 0ull ? __ldg(&factor[idx]) : 1.0;
                 while (mask) {
                     const int b = __ffs(mask) - 1;
                     mask &= mask - 1u;
@@ -232,37 +259,37 @@ __device__ double shadow_fraction64(double dx, double dy, double dz, const Ctx& 
     return __dmul_rn(2.0 / AGB_PI, __dsub_rn(acos(x), __dmul_rn(x, s)));
 }
 
-// feed_kernel (emission.cu:81-115).
+// feed_kernel (emission.cu:81-115), one thread per hash-sorted entry: warp
+// lanes then share bucket neighbourhoods (broadcast loads of the candidate
+// records) instead of each streaming its own list.
 __global__ void __launch_bounds__(256) feed_kernel(DevState* S, Ctx c, TickParams p) {
     const SoA v = S->cur;
-    const int32_t n = S->count;
+    const int32_t n = S->hash_count;
     const GridDev I = c.g[AGB_FIELD_IRRADIANCE];
     const HashDev h = c.h;
     const float two_a = (float)AGB_CELL_DIAMETER;
     const float a_f = (float)AGB_CELL_RADIUS;
-    AGB_FOR_CELLS(i, n) {
+    AGB_FOR_CELLS(ks, n) {
+        const int32_t i = (int32_t)h.vals_sorted[ks];
         const uint32_t f = v.flags[i];
         if (!(f & AGB_FLAG_OCCUPIED) || !(f & AGB_FLAG_ALIVE)) continue;
         const double px = v.x[i], py = v.y[i], pz = v.z[i];
         float directional = fs(grid_sample(I, I.value, d2f(px), d2f(py), d2f(pz)), c.ambient_irr);
         if (directional < 0.0f) directional = 0.0f;
         if (c.occlusion_exact) {
-            const long long X = to_fix64(px, h.fix_k), Y = to_fix64(py, h.fix_k), Z = to_fix64(pz, h.fix_k);
+            const float4 me = h.rec[ks];
             int32_t gx, gy, gz;
-            hash_coords(h, px, py, pz, gx, gy, gz);
+            unpack_bucket(me.w, gx, gy, gz);
             float open = 1.0f;
             int32_t refined = 0;
             walk_neighbours(h, gx, gy, gz, [&](int32_t k) {
-                const longlong2 r1 = __ldg(&h.snapA[k]);
-                const longlong2 r2 = __ldg(&h.snapB[k]);
-                const int32_t j = (int32_t)(unsigned int)(r2.y & 0xFFFFFFFFll);
-                if (j == i) return;
+                if (k == ks) return;
+                const int32_t j = (int32_t)__ldg(&h.vals_sorted[k]);
                 const uint32_t fj = v.flags[j];      // current flags: thermal may have starved j
-                if (!(fj & AGB_FLAG_OCCUPIED) || !(fj & AGB_FLAG_ALIVE)) return;
-                const long long Dx = X - r1.x, Dy = Y - r1.y, Dz = Z - r2.x;
-                const float dx = fix_diff_f(Dx, h.fix_inv_f), dy = fix_diff_f(Dy, h.fix_inv_f), dz = fix_diff_f(Dz, h.fix_inv_f);
+                if (!(fj & AGB_FLAG_ALIVE)) return;  // bucket members are all occupied
+                float dx, dy, dz;
+                rec_delta(h, me, gx, gy, gz, __ldg(&h.rec[k]), dx, dy, dz);
                 const float along = dx * c.lx + dy * c.ly + dz * c.lz;
-                const float r2s = dx * dx + dy * dy + dz * dz;
                 // Fast decisions away from the thresholds; FP64 near them.
                 if (along < -1e-6f * two_a) return;
                 const float qx = dx - along * c.lx, qy = dy - along * c.ly, qz = dz - along * c.lz;
@@ -272,11 +299,11 @@ __global__ void __launch_bounds__(256) feed_kernel(DevState* S, Ctx c, TickParam
                     const float x = perp / (2.0f * a_f);
                     const float frac = 0.63661977f * (acosf(x) - x * sqrtf(1.0f - x * x));
                     open *= (1.0f - frac);
-                    (void)r2s;
                     return;
                 }
-                ++refined;
-                const double fr = shadow_fraction64(fix_diff_d(Dx, h.fix_inv), fix_diff_d(Dy, h.fix_inv), fix_diff_d(Dz, h.fix_inv), c);
+                ++refined;   // both positions are this tick's (feeding moves nothing)
+                const double fr = shadow_fraction64(__dsub_rn(px, v.x[j]), __dsub_rn(py, v.y[j]),
+                                                    __dsub_rn(pz, v.z[j]), c);
                 open *= (float)(1.0 - fr);
             });
             if (refined) atomicAdd(&S->n_shadow_refine, refined);
@@ -351,31 +378,22 @@ __device__ __forceinline__ bool boundary_axis(double& pos, float& vel, const Ctx
     return true;
 }
 
-__global__ void __launch_bounds__(256) motion_kernel(DevState* S, Ctx c, TickParams p, float* fx_out,
+// forces_kernel (integrator.cu:40-76), one thread per hash-sorted entry.
+__global__ void __launch_bounds__(256) forces_kernel(DevState* S, Ctx c, TickParams p, float* fx_out,
                                                      float* fy_out, float* fz_out) {
     const SoA v = S->cur;
-    const int32_t n = S->count;
+    const int32_t n = S->hash_count;
     const HashDev h = c.h;
-    const GridDev T = c.g[AGB_FIELD_TEMPERATURE], C2 = c.g[AGB_FIELD_CO2], N2 = c.g[AGB_FIELD_N2];
     const float two_a = (float)AGB_CELL_DIAMETER;
     const float thr = two_a * two_a;
     const double two_a64 = AGB_CELL_DIAMETER;
-    AGB_FOR_CELLS(i, n) {
-        const uint32_t flags = v.flags[i];
-        if (!(flags & AGB_FLAG_OCCUPIED)) {
+    AGB_FOR_CELLS(ks, n) {
+        const int32_t i = (int32_t)h.vals_sorted[ks];
+        if (h.keys_sorted[ks] >= (uint32_t)h.buckets) {          // unoccupied slot (sentinel key)
             fx_out[i] = 0.0f; fy_out[i] = 0.0f; fz_out[i] = 0.0f;
             continue;
         }
-        double px = v.x[i], py = v.y[i], pz = v.z[i];
-        const float xf = d2f(px), yf = d2f(py), zf = d2f(pz);
-        // field_sample_kernel (integrator.cu:20-30)
-        float t_local;
-        if (T.enabled) { t_local = grid_sample(T, T.value, xf, yf, zf); v.t_local[i] = t_local; }
-        else t_local = v.t_local[i];
-        if (C2.enabled) v.co2_local[i] = grid_sample(C2, C2.value, xf, yf, zf);
-        if (N2.enabled) v.n2_local[i] = grid_sample(N2, N2.value, xf, yf, zf);
-
-        // forces_kernel (integrator.cu:40-76)
+        const uint32_t flags = v.flags[i];
         const float mass = d2f(v.biomass[i]) + d2f(v.energy[i]) * (float)(1.0 / (AGB_C_LIGHT * AGB_C_LIGHT));
         const bool alive = (flags & AGB_FLAG_ALIVE) != 0u;
         const float wgt = -(mass - (float)(AGB_WATER_DENSITY * AGB_CELL_VOLUME)) * (float)AGB_G_ACCEL;
@@ -388,19 +406,16 @@ __global__ void __launch_bounds__(256) motion_kernel(DevState* S, Ctx c, TickPar
             Fz -= v.dir_z[i] * thrust;
         }
         if (c.contact_enabled) {
-            const long long X = to_fix64(px, h.fix_k), Y = to_fix64(py, h.fix_k), Z = to_fix64(pz, h.fix_k);
+            const float4 me = h.rec[ks];
             int32_t gx, gy, gz;
-            hash_coords(h, px, py, pz, gx, gy, gz);
+            unpack_bucket(me.w, gx, gy, gz);
             int32_t refined = 0;
             const float kc = p.k_contact;
             const double kc64 = p.k_contact64;
             walk_neighbours(h, gx, gy, gz, [&](int32_t k) {
-                const longlong2 r1 = __ldg(&h.snapA[k]);
-                const longlong2 r2 = __ldg(&h.snapB[k]);
-                const int32_t j = (int32_t)(unsigned int)(r2.y & 0xFFFFFFFFll);
-                if (j == i || !((unsigned long long)r2.y >> 32 & AGB_FLAG_OCCUPIED)) return;
-                const long long Dx = X - r1.x, Dy = Y - r1.y, Dz = Z - r2.x;
-                const float dx = fix_diff_f(Dx, h.fix_inv_f), dy = fix_diff_f(Dy, h.fix_inv_f), dz = fix_diff_f(Dz, h.fix_inv_f);
+                if (k == ks) return;                                    // bucket members are occupied
+                float dx, dy, dz;
+                rec_delta(h, me, gx, gy, gz, __ldg(&h.rec[k]), dx, dy, dz);
                 const float r2s = dx * dx + dy * dy + dz * dz;
                 if (r2s >= thr * (1.0f + 1e-5f)) return;                 // clear of contact
                 if (r2s <= thr * (1.0f - 1e-5f) && r2s > 1e-12f * thr) { // in contact (contact_force)
@@ -409,23 +424,47 @@ __global__ void __launch_bounds__(256) motion_kernel(DevState* S, Ctx c, TickPar
                     Fx += dx * s; Fy += dy * s; Fz += dz * s;
                     return;
                 }
-                ++refined;                  // settle in FP64, contact_force (integrator.cuh:210-219)
-                const double ddx = fix_diff_d(Dx, h.fix_inv), ddy = fix_diff_d(Dy, h.fix_inv),
-                             ddz = fix_diff_d(Dz, h.fix_inv);
+                ++refined;   // settle in FP64 from the pre-step positions (integrator.cuh:210-219)
+                const int32_t j = (int32_t)__ldg(&h.vals_sorted[k]);
+                const double ddx = __dsub_rn(v.x[i], v.x[j]), ddy = __dsub_rn(v.y[i], v.y[j]),
+                             ddz = __dsub_rn(v.z[i], v.z[j]);
                 const double rr = __dadd_rn(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)), __dmul_rn(ddz, ddz));
                 if (rr >= two_a64 * two_a64 || rr <= 0.0) return;
                 const double r = sqrt(rr);
-                const double s = __ddiv_rn(__dmul_rn((double)kc64, __dsub_rn(two_a64, r)), r);
+                const double s = __ddiv_rn(__dmul_rn(kc64, __dsub_rn(two_a64, r)), r);
                 Fx += (float)__dmul_rn(ddx, s); Fy += (float)__dmul_rn(ddy, s); Fz += (float)__dmul_rn(ddz, s);
             });
             if (refined) atomicAdd(&S->n_contact_refine, refined);
         }
         if (i == c.trap_slot) {                                  // trap_force (integrator.cuh:195-197)
-            Fx += p.k_trap * (float)(c.trap_x - px);
-            Fy += p.k_trap * (float)(c.trap_y - py);
+            Fx += p.k_trap * (float)(c.trap_x - v.x[i]);
+            Fy += p.k_trap * (float)(c.trap_y - v.y[i]);
         }
         fx_out[i] = Fx; fy_out[i] = Fy; fz_out[i] = Fz;
+    }
+}
 
+// field_sample_kernel (integrator.cu:20-30) + integrate_kernel (integrator.cu:79-150),
+// slot order (coalesced state access).
+__global__ void __launch_bounds__(256) integrate_kernel(DevState* S, Ctx c, TickParams p,
+                                                        const float* __restrict__ fx_in,
+                                                        const float* __restrict__ fy_in,
+                                                        const float* __restrict__ fz_in) {
+    const SoA v = S->cur;
+    const int32_t n = S->count;
+    const GridDev T = c.g[AGB_FIELD_TEMPERATURE], C2 = c.g[AGB_FIELD_CO2], N2 = c.g[AGB_FIELD_N2];
+    AGB_FOR_CELLS(i, n) {
+        const uint32_t flags = v.flags[i];
+        if (!(flags & AGB_FLAG_OCCUPIED)) continue;
+        double px = v.x[i], py = v.y[i], pz = v.z[i];
+        const float xf = d2f(px), yf = d2f(py), zf = d2f(pz);
+        float t_local;
+        if (T.enabled) { t_local = grid_sample(T, T.value, xf, yf, zf); v.t_local[i] = t_local; }
+        else t_local = v.t_local[i];
+        if (C2.enabled) v.co2_local[i] = grid_sample(C2, C2.value, xf, yf, zf);
+        if (N2.enabled) v.n2_local[i] = grid_sample(N2, N2.value, xf, yf, zf);
+        const float Fx = fx_in[i], Fy = fy_in[i], Fz = fz_in[i];
+        const float mass = d2f(v.biomass[i]) + d2f(v.energy[i]) * (float)(1.0 / (AGB_C_LIGHT * AGB_C_LIGHT));
         // integrate_kernel (integrator.cu:79-150)
         const bool awake = (flags & AGB_FLAG_AWAKE) != 0u;
         const float t_drag = awake ? (float)AGB_CELL_TEMP_SETPOINT : t_local;
@@ -494,24 +533,28 @@ __global__ void __launch_bounds__(256) motion_kernel(DevState* S, Ctx c, TickPar
 void launch_thermal(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, cudaStream_t s) {
     thermal_kernel<<<blocks, 256, 0, s>>>(S, c, p);
 }
-void launch_emission(DevState* S, const Ctx& c, const TickParams& p, int32_t* stamp_idx, bool stamp,
-                     int32_t blocks, cudaStream_t s) {
+void launch_emission(DevState* S, const Ctx& c, const TickParams& p, int32_t* stamp_idx, double* factor,
+                     bool stamp, int32_t blocks, cudaStream_t s) {
     clear_stamps_kernel<<<blocks, 256, 0, s>>>(S, c, stamp_idx);
-    if (stamp) stamp_kernel<<<blocks, 256, 0, s>>>(S, c, stamp_idx);
+    if (stamp) {
+        stamp_kernel<<<blocks, 256, 0, s>>>(S, c, stamp_idx);
+        occlusion_factor_kernel<<<blocks, 256, 0, s>>>(S, c, stamp_idx, factor);
+    }
     const GridDev& I = c.g[AGB_FIELD_IRRADIANCE];
     const int32_t len = c.light_axis == 0 ? I.nx : (c.light_axis == 1 ? I.ny : I.nz);
     const int64_t lines = I.count / len;
     if (c.light_axis == 0) {
         const int64_t blocks = (lines * 32 + 255) / 256;
-        sweep_rows_kernel<<<(unsigned)(blocks < 65535 ? blocks : 65535), 256, 0, s>>>(c);
+        sweep_rows_kernel<<<(unsigned)(blocks < 65535 ? blocks : 65535), 256, 0, s>>>(c, factor);
     } else {
-        sweep_kernel<<<(unsigned)((lines + 127) / 128), 128, 0, s>>>(c);
+        sweep_kernel<<<(unsigned)((lines + 127) / 128), 128, 0, s>>>(c, factor);
     }
     feed_kernel<<<blocks, 256, 0, s>>>(S, c, p);
 }
 void launch_motion(DevState* S, const Ctx& c, const TickParams& p, float* fx, float* fy, float* fz,
                    int32_t blocks, cudaStream_t s) {
-    motion_kernel<<<blocks, 256, 0, s>>>(S, c, p, fx, fy, fz);
+    forces_kernel<<<blocks, 256, 0, s>>>(S, c, p, fx, fy, fz);
+    integrate_kernel<<<blocks, 256, 0, s>>>(S, c, p, fx, fy, fz);
 }
 
 }  // namespace agb

@@ -7,9 +7,11 @@
 //   * a stable LSD radix sort runs over only ceil(log2(buckets + 1)) bits;
 //   * the dense {start, end} table is cleared only at the buckets the previous
 //     build wrote (read from its sorted keys before they are overwritten);
-//   * the ranges pass also writes a sorted-order snapshot of positions (exact
-//     64-bit fixed point), flags and slot, so neighbour walks stream contiguous
-//     32-byte records instead of gathering three FP64 arrays through an index.
+//   * the ranges pass also writes a sorted-order 16-byte snapshot per cell --
+//     position as FP32 offsets from its bucket's corner plus the packed bucket
+//     coordinates -- so a neighbour separation is (bucket delta) * cell +
+//     (offset delta) in FP32, streamed from contiguous records instead of three
+//     FP64 arrays gathered through an index.
 // Sorted output is the same as the reference's: stable order by key with
 // ascending slots inside a bucket.
 #include <cuda_runtime.h>
@@ -142,9 +144,15 @@ __global__ void ranges_kernel(DevState* S, HashDev h) {
             if (k == 0 || h.keys_sorted[k - 1] != key) h.ranges[key].x = k;
             if (k == n - 1 || h.keys_sorted[k + 1] != key) h.ranges[key].y = k + 1;
         }
-        h.snapA[k] = make_longlong2(to_fix64(v.x[slot], h.fix_k), to_fix64(v.y[slot], h.fix_k));
-        h.snapB[k] = make_longlong2(to_fix64(v.z[slot], h.fix_k),
-                                    (long long)(((unsigned long long)v.flags[slot] << 32) | slot));
+        // Offsets from the bucket's corner, formed exactly in fixed point and
+        // rounded once to FP32, plus the bucket coordinates (x, y: 11 bits; z: 10).
+        int32_t gx, gy, gz;
+        const double px = v.x[slot], py = v.y[slot], pz = v.z[slot];
+        hash_coords(h, px, py, pz, gx, gy, gz);
+        const float ox = __ll2float_rn(to_fix64(px, h.fix_k) - (h.org_fix[0] + gx * h.cell_fix)) * h.fix_inv_f;
+        const float oy = __ll2float_rn(to_fix64(py, h.fix_k) - (h.org_fix[1] + gy * h.cell_fix)) * h.fix_inv_f;
+        const float oz = __ll2float_rn(to_fix64(pz, h.fix_k) - (h.org_fix[2] + gz * h.cell_fix)) * h.fix_inv_f;
+        h.rec[k] = make_float4(ox, oy, oz, __uint_as_float((uint32_t)gx | ((uint32_t)gy << 11) | ((uint32_t)gz << 22)));
     }
 }
 

@@ -2,6 +2,7 @@
 // piece). Every launcher enqueues on the given stream and never synchronises.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "dev.cuh"
@@ -13,8 +14,10 @@ struct WorldConst;   // defined in world.cuh
 // Fields (k_grid.cu)
 void launch_fill(float* v, int64_t n, float value, cudaStream_t s);
 // One explicit FTCS pass src -> dst (src/fields/diffuse.cu:19-44; 7-point when nz > 1).
+// 3-D grids with a tensor map use the TMA-staged kernel.
 void launch_ftcs(const GridDev& g, const float* src, float* dst, float coeff, const int32_t* bc,
-                 const float* face, float robin, cudaStream_t s);
+                 const float* face, float robin, const CUtensorMap* src_map, uint32_t* err, cudaStream_t s);
+bool make_plane_map(CUtensorMap* map, float* base, int32_t nx, int32_t ny, int32_t nz);
 // Fold deposits into the field for the voxels cells sit in (flush_kernel,
 // src/fields/diffuse.cu:51-60, restricted to voxels that can hold a deposit).
 void launch_flush_by_cells(DevState* S, GridDev g, unsigned long long* demand_to_clear,

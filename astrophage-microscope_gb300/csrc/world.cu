@@ -9,6 +9,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -37,6 +38,9 @@ struct agb_world {
     void* blob[2] = {nullptr, nullptr};
     size_t blob_bytes = 0;
     float* gbuf[AGB_FIELD_COUNT][2] = {};
+    CUtensorMap tmap[AGB_FIELD_COUNT][2];      // TMA maps of each field buffer (3-D grids)
+    bool tmap_ok[AGB_FIELD_COUNT] = {};
+    bool use_tma = true;
     int gcur[AGB_FIELD_COUNT] = {};
     unsigned long long* gdep[AGB_FIELD_COUNT] = {};
     int32_t gbc[AGB_FIELD_COUNT][6] = {};
@@ -45,6 +49,9 @@ struct agb_world {
     uint32_t *kalt = nullptr, *valt = nullptr, *hist = nullptr;
     LifeBuffers life{};
     int32_t* stamp_idx = nullptr;
+    double* occl_factor = nullptr;       // per irradiance voxel: transmittance of stamped voxels
+    cudaStream_t side[2] = {nullptr, nullptr};   // concurrent branches of a tick
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     float *fx = nullptr, *fy = nullptr, *fz = nullptr;
     unsigned long long* acc = nullptr;
     int32_t blocks = 1;
@@ -55,7 +62,7 @@ struct agb_world {
     unsigned long long acc_host[12] = {};
     std::vector<GraphEntry> graphs;
     cudaStream_t own_stream = nullptr;   // capture stream when the caller passes the default stream
-    int32_t last_graph_kernels = 0;
+    int64_t graph_kernels_total = 0;     // kernel nodes launched by graph replays so far
     std::string err;
     std::vector<void*> allocs;
 };
@@ -220,8 +227,9 @@ void refresh_grid_ptrs(agb_world* w) {
 
 void ftcs(agb_world* w, int f, float coeff, cudaStream_t s) {
     refresh_grid_ptrs(w);
+    const CUtensorMap* map = (w->use_tma && w->tmap_ok[f]) ? &w->tmap[f][w->gcur[f]] : nullptr;
     launch_ftcs(w->c.g[f], field_value(w, f), w->gbuf[f][1 - w->gcur[f]], coeff, w->gbc[f], w->gface[f],
-                w->grobin[f], s);
+                w->grobin[f], map, &w->S->error, s);
     w->gcur[f] = 1 - w->gcur[f];
     refresh_grid_ptrs(w);
 }
@@ -247,7 +255,7 @@ void stage_emission(agb_world* w, cudaStream_t s) {  // emission_step, src/sim/e
     if (!w->c.g[AGB_FIELD_IRRADIANCE].enabled) return;
     if (w->c.source <= 0.0f && w->c.ambient_irr <= 0.0f) return;
     refresh_grid_ptrs(w);
-    launch_emission(w->S, w->c, w->tp, w->stamp_idx, w->c.source > 0.0f, w->blocks, s);
+    launch_emission(w->S, w->c, w->tp, w->stamp_idx, w->occl_factor, w->c.source > 0.0f, w->blocks, s);
 }
 
 void stage_motion(agb_world* w, cudaStream_t s) {    // motion_step, src/sim/integrator.cu:154-177
@@ -280,12 +288,34 @@ void stage_clock(agb_world* w) {
     w->sim_time += w->tp.dt;
 }
 
+// One tick as a small DAG. The thermal substeps and the CO2/N2 diffusion do
+// not touch what the hash build reads (positions, OCCUPIED), so they run on
+// side streams -- parallel branches of the captured graph -- joined where the
+// reference's order needs their results: thermal before emission (feeding sees
+// the post-thermostat store), slow fields before lifecycle (uptake reads the
+// diffused CO2). Motion samples CO2 and N2 from the buffers as they were
+// before this tick's diffusion, exactly as in src/sim/step.cu:164-171, while
+// the diffusion writes the other ping-pong buffer.
 void tick_once(agb_world* w, cudaStream_t s) {
+    cudaStream_t s1 = w->side[0], s2 = w->side[1];
+    cudaEventRecord(w->ev[0], s);
+    cudaStreamWaitEvent(s1, w->ev[0], 0);
+    cudaStreamWaitEvent(s2, w->ev[0], 0);
+    if (w->d.thermal_enabled) stage_thermal(w, s1);
+    cudaEventRecord(w->ev[1], s1);
+    refresh_grid_ptrs(w);
+    const Ctx pre = w->c;                       // CO2/N2 as motion must see them
+    stage_slow_fields(w, s2);
+    cudaEventRecord(w->ev[2], s2);
     stage_hash(w, s);
-    if (w->d.thermal_enabled) stage_thermal(w, s);
+    cudaStreamWaitEvent(s, w->ev[1], 0);
     if (w->d.emission_enabled) stage_emission(w, s);
-    stage_motion(w, s);
-    stage_slow_fields(w, s);
+    {
+        Ctx c = w->c;
+        for (int f : {AGB_FIELD_CO2, AGB_FIELD_N2}) c.g[f] = pre.g[f];
+        launch_motion(w->S, c, w->tp, w->fx, w->fy, w->fz, w->blocks, s);
+    }
+    cudaStreamWaitEvent(s, w->ev[2], 0);
     stage_lifecycle(w, s);
     stage_clock(w);
 }
@@ -373,6 +403,8 @@ void agb_world_destroy(agb_world* w) {
     if (!w) return;
     invalidate_graphs(w);
     if (w->own_stream) cudaStreamDestroy(w->own_stream);
+    for (cudaStream_t& st : w->side) if (st) cudaStreamDestroy(st);
+    for (cudaEvent_t& e : w->ev) if (e) cudaEventDestroy(e);
     for (void* p : w->allocs) cudaFree(p);
     delete w;
 }
@@ -388,6 +420,8 @@ agb_status agb_world_create(const agb_world_desc* d, agb_world** out) {
     if (d->taxis_enabled) return AGB_UNSUPPORTED;
     agb_world* w = new (std::nothrow) agb_world();
     if (!w) return AGB_OUT_OF_MEMORY;
+    // AGB_PLAIN_STENCIL=1 selects the plain 3-D stencil (for A/B checks of the TMA one).
+    if (const char* e = std::getenv("AGB_PLAIN_STENCIL")) w->use_tma = (e[0] != '1');
     w->d = *d;
     w->physics_rate = d->physics_rate;
     w->biology_rate = d->biology_rate;
@@ -457,6 +491,8 @@ agb_status agb_world_create(const agb_world_desc* d, agb_world** out) {
             agb_world_destroy(w); return AGB_OUT_OF_MEMORY;
         }
         g.deposit = w->gdep[f];
+        w->tmap_ok[f] = make_plane_map(&w->tmap[f][0], w->gbuf[f][0], g.nx, g.ny, g.nz) &&
+                        make_plane_map(&w->tmap[f][1], w->gbuf[f][1], g.nx, g.ny, g.nz);
         launch_fill(w->gbuf[f][0], g.count, (float)gd.init, nullptr);
         launch_fill(w->gbuf[f][1], g.count, (float)gd.init, nullptr);
     }
@@ -484,7 +520,12 @@ agb_status agb_world_create(const agb_world_desc* d, agb_world** out) {
         h.fix_k = 62 - (int32_t)std::ceil(std::log2(half));
         h.fix_inv = std::ldexp(1.0, -h.fix_k);
         h.fix_inv_f = (float)h.fix_inv;
+        const float org[3] = {h.ox, h.oy, h.oz};
+        for (int a = 0; a < 3; ++a) h.org_fix[a] = std::llround(std::ldexp((double)org[a], h.fix_k));
+        h.cell_fix = std::llround(std::ldexp(cell, h.fix_k));
+        h.cell_f = (float)std::ldexp((double)h.cell_fix, -h.fix_k);
     }
+    if (h.nx > 2047 || h.ny > 2047 || h.nz > 1023) { agb_world_destroy(w); return AGB_UNSUPPORTED; }
     const size_t n = (size_t)cap;
     const int32_t tiles = (cap + 255) / 256;             // radix tiles (k_hash.cu)
     bool ok = dalloc(w, &h.keys, 4 * n) == cudaSuccess && dalloc(w, &h.vals, 4 * n) == cudaSuccess &&
@@ -492,7 +533,7 @@ agb_status agb_world_create(const agb_world_desc* d, agb_world** out) {
               dalloc(w, &w->kalt, 4 * n) == cudaSuccess && dalloc(w, &w->valt, 4 * n) == cudaSuccess &&
               dalloc(w, &w->hist, 4 * 256 * ((size_t)tiles + 1)) == cudaSuccess &&
               dalloc(w, &h.ranges, 8 * (size_t)h.buckets) == cudaSuccess &&
-              dalloc(w, &h.snapA, 16 * n) == cudaSuccess && dalloc(w, &h.snapB, 16 * n) == cudaSuccess;
+              dalloc(w, &h.rec, 16 * n) == cudaSuccess;
     h.keys_prev = nullptr;
     // Cells: two SoA blobs (live + compaction target).
     w->blob_bytes = soa_bytes(cap);
@@ -505,6 +546,10 @@ agb_status agb_world_create(const agb_world_desc* d, agb_world** out) {
          dalloc(w, &w->stamp_idx, 4 * n) == cudaSuccess && dalloc(w, &w->fx, 4 * n) == cudaSuccess &&
          dalloc(w, &w->fy, 4 * n) == cudaSuccess && dalloc(w, &w->fz, 4 * n) == cudaSuccess &&
          dalloc(w, &w->acc, 8 * 12) == cudaSuccess && dalloc(w, &w->S, sizeof(DevState)) == cudaSuccess;
+    const int64_t irrn = c.g[AGB_FIELD_IRRADIANCE].enabled ? c.g[AGB_FIELD_IRRADIANCE].count : 1;
+    ok = ok && dalloc(w, &w->occl_factor, 8 * (size_t)irrn) == cudaSuccess;
+    for (cudaStream_t& st : w->side) ok = ok && cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess;
+    for (cudaEvent_t& e : w->ev) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
     const int64_t co2n = c.g[AGB_FIELD_CO2].enabled ? c.g[AGB_FIELD_CO2].count : 1;
     ok = ok && dalloc(w, &w->life.co2_demand, 8 * (size_t)co2n) == cudaSuccess;
     if (!ok) { agb_world_destroy(w); return AGB_OUT_OF_MEMORY; }
@@ -644,7 +689,7 @@ agb_status agb_world_step_graph(agb_world* w, int32_t ticks, agb_stream s) {
     for (const GraphEntry& g : w->graphs) {
         if (g.ticks == ticks && g.parity == par && g.tick_phase == phase) {
             AGB_CUDA(w, cudaGraphLaunch(g.exec, s));
-            w->last_graph_kernels = g.kernels;
+            w->graph_kernels_total += g.kernels;
             for (int f = 0; f < AGB_FIELD_COUNT; ++f) w->gcur[f] = (g.parity_after >> f) & 1;
             refresh_grid_ptrs(w);
             w->tick += (uint64_t)ticks;
@@ -678,15 +723,15 @@ agb_status agb_world_step_graph(agb_world* w, int32_t ticks, agb_stream s) {
     cudaGraphDestroy(graph);
     if (ie != cudaSuccess) return cuda_fail(w, ie, "cudaGraphInstantiate");
     w->graphs.push_back(e);
-    w->last_graph_kernels = e.kernels;
+    w->graph_kernels_total += e.kernels;
     // Capture advanced the host-side tick state; the graph has not run yet.
     AGB_CUDA(w, cudaGraphLaunch(e.exec, s));
     return AGB_OK;
 }
 
-agb_status agb_world_graph_kernels(agb_world* w, int32_t* kernels) {
+agb_status agb_world_graph_kernels(agb_world* w, int64_t* kernels) {
     if (!w || !kernels) return AGB_INVALID_ARGUMENT;
-    *kernels = w->last_graph_kernels;
+    *kernels = w->graph_kernels_total;
     return AGB_OK;
 }
 

@@ -91,10 +91,24 @@ def workload(name, seed=1):
         d.light = agb.Light(0.0, 0.0, 1.0, 1.0e4, 0.0, 1)
         d.compaction_enabled = 1
         d.biology_rate = 1.38e5
+        d.hash_cell_size = 10e-6
+        # Dormant: awake cells packed ~60 to a 15.6 um voxel overdrive the lumped
+        # thermostat exchange past the lethal temperature within a few ticks.
         sp = agb.spawn(1000000, placement=agb.PLACE_CLUSTERS, place_radius=40e-6, clusters=64,
-                       cluster_extent=3e-3, charge_dist=agb.DIST_UNIFORM, charge_a=0.0, charge_b=0.2, awake=True)
-        return d, sp, dict(cells=1000000, grid=256, chamber_mm=4.0, light="+z", clusters=64, hash_cell_um=22.0)
+                       cluster_extent=3e-3, charge_dist=agb.DIST_UNIFORM, charge_a=0.0, charge_b=0.2, awake=False)
+        return d, sp, dict(cells=1000000, grid=256, chamber_mm=4.0, light="+z", clusters=64, hash_cell_um=10.0,
+                           awake=False)
     raise SystemExit("unknown workload " + name)
+
+
+def substeps(desc, f):
+    """FTCS passes per tick of field f (src/fields/grid.cuh:51-53; 1/6 bound in 3-D)."""
+    g = desc.grid[f]
+    if g.nx <= 0:
+        return 0
+    dx = desc.chamber_w / g.nx
+    lim = 6.0 if g.nz > 1 else 4.0
+    return int(agb.DT_PHYSICS * desc.physics_rate / (dx * dx / (lim * g.diffusivity))) + 1
 
 
 def voxel_steps_per_tick(desc):
@@ -102,12 +116,8 @@ def voxel_steps_per_tick(desc):
     total = 0
     for f in (agb.FIELD_T, agb.FIELD_CO2, agb.FIELD_N2):
         g = desc.grid[f]
-        if g.nx <= 0:
-            continue
-        dx = desc.chamber_w / g.nx
-        lim = 6.0 if g.nz > 1 else 4.0
-        steps = int(agb.DT_PHYSICS * desc.physics_rate / (dx * dx / (lim * g.diffusivity))) + 1
-        total += steps * g.nx * g.ny * g.nz
+        if g.nx > 0:
+            total += substeps(desc, f) * g.nx * g.ny * g.nz
     return total
 
 
@@ -311,7 +321,7 @@ def main():
             world.step(1, graph=True, stream=sh)
         torch.cuda.synchronize()
         n_start = world.count(stream=sh)
-        kernels_per_tick = world.graph_kernels()
+        kernels_before = world.graph_kernels()
         starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
         ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
         sampler = ClockSampler(local)
@@ -329,6 +339,7 @@ def main():
         if dist is not None:
             dist.barrier()
         n_end = world.count(stream=sh)
+        launches = world.graph_kernels() - kernels_before
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     total_s = allreduce_max(dist, sum(step_ms) / 1e3)
     cells_mean = 0.5 * (n_start + n_end)
@@ -352,7 +363,7 @@ def main():
             world.diffuse(agb.FIELD_T, agb.DT_PHYSICS, stream=sh)
         e1.record(stream)
         torch.cuda.synchronize()
-    ftcs_s = e0.elapsed_time(e1) / 1e3 / reps
+    ftcs_s = e0.elapsed_time(e1) / 1e3 / (reps * substeps(desc, agb.FIELD_T))   # per pass
     algo_bytes = 8.0 * vox_T
     achieved = algo_bytes / ftcs_s / 1e9
     traffic = profile_traffic("ftcs3d_%d" % gT.nx)
@@ -409,7 +420,7 @@ def main():
                          "launch_us": ftcs_s * 1e6, "traffic": traffic},
             "cpu_baseline": cpu,
             "e2e": e2e,
-            "gpu_launches": kernels_per_tick * args.steps,
+            "gpu_launches": launches,
             "clocks": clocks,
         }
         print(json.dumps(line))

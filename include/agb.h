@@ -237,9 +237,9 @@ agb_status agb_world_step(agb_world* w, int32_t ticks, agb_stream s);
 /* Capture `ticks` ticks once as a CUDA graph and replay it on later calls with
  * the same tick count: one launch per call. */
 agb_status agb_world_step_graph(agb_world* w, int32_t ticks, agb_stream s);
-/* Kernel launches one replay of the most recently captured graph performs
- * (the graph's kernel nodes), for launch accounting. */
-agb_status agb_world_graph_kernels(agb_world* w, int32_t* kernels);
+/* Kernel launches performed by graph replays since the world was created
+ * (the sum of each replayed graph's kernel nodes), for launch accounting. */
+agb_status agb_world_graph_kernels(agb_world* w, int64_t* kernels);
 /* One stage of the tick at the world's dt (AGB_STAGE_*). */
 agb_status agb_world_stage(agb_world* w, int32_t stage, agb_stream s);
 /* grid_diffuse on one field for dt (src/fields/diffuse.cu:159-186). */

@@ -142,6 +142,34 @@ def test_diffusion_bit_exact(nz, bcs):
     assert np.array_equal(gpu.export_field(agb.FIELD_T), orc.export_field(agb.FIELD_T))
 
 
+@pytest.mark.parametrize("nx,ny,nz", [(100, 36, 20), (256, 20, 9), (64, 64, 64)])
+def test_diffusion_3d_partial_tiles_bit_exact(nx, ny, nz):
+    """The TMA-staged 3-D stencil on grids that leave partial tiles in every axis."""
+    dx = 1.0e-5
+    d = S.slab_desc(light=None)
+    d.chamber_w, d.chamber_h, d.chamber_d = nx * dx, ny * dx, nz * dx
+    g = agb.GridDesc()
+    g.nx, g.ny, g.nz = nx, ny, nz
+    bcs = [agb.BC_DIRICHLET, agb.BC_ROBIN, agb.BC_NEUMANN, agb.BC_DIRICHLET, agb.BC_ROBIN, agb.BC_NEUMANN]
+    for k in range(6):
+        g.bc[k] = bcs[k]
+        g.face_value[k] = 280.0 + 10.0 * k
+    g.diffusivity, g.init, g.deposit_scale = agb.WATER_THERMAL_DIFFUSIVITY, 300.0, 1e9
+    d.grid[agb.FIELD_T] = g
+    for f in (agb.FIELD_CO2, agb.FIELD_N2, agb.FIELD_IRR):
+        d.grid[f] = agb.GridDesc()
+    gpu, orc = pair(d)
+    rng = np.random.default_rng(nx + ny + nz)
+    f0 = (290.0 + 80.0 * rng.random((nz, ny, nx))).astype(np.float32)
+    gpu.import_field(agb.FIELD_T, f0)
+    orc.import_field(agb.FIELD_T, f0)
+    for _ in range(3):
+        gpu.diffuse(agb.FIELD_T, 2e-4)
+        orc.diffuse(agb.FIELD_T, 2e-4)
+    assert np.array_equal(gpu.export_field(agb.FIELD_T), orc.export_field(agb.FIELD_T))
+    assert gpu.counters()[3] == 0, "device error word"
+
+
 def test_spawn_matches_oracle():
     d = S.slab_desc(cap=5000)
     gpu, orc = pair(d)
