@@ -203,6 +203,19 @@ class AgbError(RuntimeError):
     pass
 
 
+NOALLOC_MAX_VOXELS = 4194304
+
+
+def grid_diffuse_noalloc(value_ptr, nx, ny, nz, dx, diffusivity, dt, bc, face_value, stream=None, lib=None):
+    """agb_grid_diffuse_noalloc on a caller-owned device buffer (an int pointer).
+    Returns the status code; the library allocates nothing for it."""
+    lib = lib or load()
+    b = (C.c_int32 * 6)(*bc)
+    f = (C.c_double * 6)(*face_value)
+    return lib.agb_grid_diffuse_noalloc(C.c_void_p(int(value_ptr)), nx, ny, nz, dx, diffusivity, dt, b, f,
+                                         None if stream is None else C.c_void_p(int(stream)))
+
+
 def status_name(s):
     return STATUS_NAMES[s] if 0 <= s < len(STATUS_NAMES) else "Unknown(%d)" % s
 
@@ -246,6 +259,8 @@ def load(path=LIB_PATH):
         "agb_world_export_hash": (I32, [P, P, P, P, P, P, P]),
         "agb_world_export_forces": (I32, [P, P, P, P, P]),
         "agb_world_counters": (I32, [P, P, P]),
+        "agb_grid_diffuse_noalloc": (I32, [P, I32, I32, I32, C.c_double, C.c_double, C.c_double,
+                                           C.POINTER(I32), C.POINTER(C.c_double), P]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -264,7 +279,7 @@ def exported_symbols():
             "agb_world_diffuse",
             "agb_world_stats", "agb_world_stats_accum", "agb_world_set_clock",
             "agb_world_set_light", "agb_world_export_hash", "agb_world_export_forces",
-            "agb_world_counters"]
+            "agb_world_counters", "agb_grid_diffuse_noalloc"]
 
 
 def _st(stream):

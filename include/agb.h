@@ -245,6 +245,27 @@ agb_status agb_world_stage(agb_world* w, int32_t stage, agb_stream s);
 /* grid_diffuse on one field for dt (src/fields/diffuse.cu:159-186). */
 agb_status agb_world_diffuse(agb_world* w, int32_t field, double dt, agb_stream s);
 
+/* Diffusion of one field the caller owns in device memory, with no device
+ * allocation: grid_diffuse's substepping and arithmetic (bit for bit), with the
+ * second ping-pong buffer taken from a fixed scratch array inside the library
+ * (AGB_NOALLOC_MAX_VOXELS floats, 16 MiB, held on every GPU that loads the
+ * library until the process exits). This entry point has no counterpart in
+ * the reference. It exists for callers that may not allocate device memory:
+ * applications with a fixed device-memory budget reserved at start-up, plugins
+ * inside a host that owns the CUDA context's allocation policy, and real-time
+ * loops that cannot afford cudaMalloc's implicit synchronisation.
+ * `value` is nx*ny*nz floats, x fastest; dx is the isotropic spacing; bc and
+ * face_value follow agb_grid_desc; the result is left in `value`.
+ * Returns AGB_CAPACITY_EXCEEDED for grids larger than AGB_NOALLOC_MAX_VOXELS.
+ * The first call on a device resolves the scratch array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the scratch array: calls whose work overlaps on the GPU race.
+ * Its contents are left over from the previous call and need no clearing. */
+#define AGB_NOALLOC_MAX_VOXELS 4194304
+agb_status agb_grid_diffuse_noalloc(float* value, int32_t nx, int32_t ny, int32_t nz, double dx,
+                                    double diffusivity, double dt, const int32_t bc[6],
+                                    const double face_value[6], agb_stream s);
+
 /* world_stats (src/sim/stats.cu:102-153): fixed-point reduction + window counters. Syncs. */
 agb_status agb_world_stats(agb_world* w, agb_stats* out, agb_stream s);
 /* The raw fixed-point sums of the last agb_world_stats, StatsAccum order
