@@ -44,9 +44,18 @@ __device__ __forceinline__ void walk_neighbours(const HashDev& h, int32_t gx, in
         lo[r] = l;
         hi[r] = e;
     }
+    // Visit entries in order, the next record's load in flight while the
+    // current one is evaluated.
 #pragma unroll 1
-    for (int r = 0; r < 9; ++r)
-        for (int32_t k = lo[r]; k < hi[r]; ++k) f(k);
+    for (int r = 0; r < 9; ++r) {
+        if (lo[r] >= hi[r]) continue;
+        float4 nxt = __ldg(&h.rec[lo[r]]);
+        for (int32_t k = lo[r]; k < hi[r]; ++k) {
+            const float4 cur = nxt;
+            if (k + 1 < hi[r]) nxt = __ldg(&h.rec[k + 1]);
+            f(k, cur);
+        }
+    }
 }
 
 __device__ __forceinline__ void unpack_bucket(float w, int32_t& gx, int32_t& gy, int32_t& gz) {
@@ -164,7 +173,7 @@ __global__ void __launch_bounds__(256) occlusion_factor_kernel(DevState* S, Ctx 
 // FP64 transmittance recurrence runs only at stamped voxels (an empty voxel's
 // factor is exactly 1), and the float output only changes there, so empty
 // voxels cost one load and one store.
-constexpr int SWEEP_PF = 8;
+constexpr int SWEEP_PF = 16;
 
 __global__ void __launch_bounds__(128) sweep_kernel(Ctx c, const double* __restrict__ factor) {
     const GridDev I = c.g[AGB_FIELD_IRRADIANCE];
@@ -282,19 +291,19 @@ __global__ void __launch_bounds__(256) feed_kernel(DevState* S, Ctx c, TickParam
             unpack_bucket(me.w, gx, gy, gz);
             float open = 1.0f;
             int32_t refined = 0;
-            walk_neighbours(h, gx, gy, gz, [&](int32_t k) {
+            walk_neighbours(h, gx, gy, gz, [&](int32_t k, const float4& rk) {
                 if (k == ks) return;
-                const int32_t j = (int32_t)__ldg(&h.vals_sorted[k]);
-                const uint32_t fj = v.flags[j];      // current flags: thermal may have starved j
-                if (!(fj & AGB_FLAG_ALIVE)) return;  // bucket members are all occupied
                 float dx, dy, dz;
-                rec_delta(h, me, gx, gy, gz, __ldg(&h.rec[k]), dx, dy, dz);
+                rec_delta(h, me, gx, gy, gz, rk, dx, dy, dz);
                 const float along = dx * c.lx + dy * c.ly + dz * c.lz;
-                // Fast decisions away from the thresholds; FP64 near them.
+                // Geometry first (cheap, rejects most candidates); FP64 only near
+                // the thresholds; the neighbour's flags only for real shadowers.
                 if (along < -1e-6f * two_a) return;
                 const float qx = dx - along * c.lx, qy = dy - along * c.ly, qz = dz - along * c.lz;
                 const float perp = sqrtf(qx * qx + qy * qy + qz * qz);
                 if (along > 1e-6f * two_a && perp >= two_a * (1.0f + 1e-6f)) return;
+                const int32_t j = (int32_t)__ldg(&h.vals_sorted[k]);
+                if (!(v.flags[j] & AGB_FLAG_ALIVE)) return;   // current flags: thermal may have starved j
                 if (along > 1e-6f * two_a && perp > 1e-2f * two_a && perp < two_a * (1.0f - 1e-6f)) {
                     const float x = perp / (2.0f * a_f);
                     const float frac = 0.63661977f * (acosf(x) - x * sqrtf(1.0f - x * x));
@@ -384,6 +393,7 @@ __global__ void __launch_bounds__(256) forces_kernel(DevState* S, Ctx c, TickPar
     const SoA v = S->cur;
     const int32_t n = S->hash_count;
     const HashDev h = c.h;
+    const GridDev T = c.g[AGB_FIELD_TEMPERATURE], C2 = c.g[AGB_FIELD_CO2], N2 = c.g[AGB_FIELD_N2];
     const float two_a = (float)AGB_CELL_DIAMETER;
     const float thr = two_a * two_a;
     const double two_a64 = AGB_CELL_DIAMETER;
@@ -394,6 +404,14 @@ __global__ void __launch_bounds__(256) forces_kernel(DevState* S, Ctx c, TickPar
             continue;
         }
         const uint32_t flags = v.flags[i];
+        // field_sample_kernel (integrator.cu:20-30), done here because sorted
+        // order makes neighbouring threads sample neighbouring voxels.
+        {
+            const float xf = d2f(v.x[i]), yf = d2f(v.y[i]), zf = d2f(v.z[i]);
+            if (T.enabled) v.t_local[i] = grid_sample(T, T.value, xf, yf, zf);
+            if (C2.enabled) v.co2_local[i] = grid_sample(C2, C2.value, xf, yf, zf);
+            if (N2.enabled) v.n2_local[i] = grid_sample(N2, N2.value, xf, yf, zf);
+        }
         const float mass = d2f(v.biomass[i]) + d2f(v.energy[i]) * (float)(1.0 / (AGB_C_LIGHT * AGB_C_LIGHT));
         const bool alive = (flags & AGB_FLAG_ALIVE) != 0u;
         const float wgt = -(mass - (float)(AGB_WATER_DENSITY * AGB_CELL_VOLUME)) * (float)AGB_G_ACCEL;
@@ -412,10 +430,10 @@ __global__ void __launch_bounds__(256) forces_kernel(DevState* S, Ctx c, TickPar
             int32_t refined = 0;
             const float kc = p.k_contact;
             const double kc64 = p.k_contact64;
-            walk_neighbours(h, gx, gy, gz, [&](int32_t k) {
+            walk_neighbours(h, gx, gy, gz, [&](int32_t k, const float4& rk) {
                 if (k == ks) return;                                    // bucket members are occupied
                 float dx, dy, dz;
-                rec_delta(h, me, gx, gy, gz, __ldg(&h.rec[k]), dx, dy, dz);
+                rec_delta(h, me, gx, gy, gz, rk, dx, dy, dz);
                 const float r2s = dx * dx + dy * dy + dz * dz;
                 if (r2s >= thr * (1.0f + 1e-5f)) return;                 // clear of contact
                 if (r2s <= thr * (1.0f - 1e-5f) && r2s > 1e-12f * thr) { // in contact (contact_force)
@@ -444,25 +462,18 @@ __global__ void __launch_bounds__(256) forces_kernel(DevState* S, Ctx c, TickPar
     }
 }
 
-// field_sample_kernel (integrator.cu:20-30) + integrate_kernel (integrator.cu:79-150),
-// slot order (coalesced state access).
+// integrate_kernel (integrator.cu:79-150), slot order (coalesced state access).
 __global__ void __launch_bounds__(256) integrate_kernel(DevState* S, Ctx c, TickParams p,
                                                         const float* __restrict__ fx_in,
                                                         const float* __restrict__ fy_in,
                                                         const float* __restrict__ fz_in) {
     const SoA v = S->cur;
     const int32_t n = S->count;
-    const GridDev T = c.g[AGB_FIELD_TEMPERATURE], C2 = c.g[AGB_FIELD_CO2], N2 = c.g[AGB_FIELD_N2];
     AGB_FOR_CELLS(i, n) {
         const uint32_t flags = v.flags[i];
         if (!(flags & AGB_FLAG_OCCUPIED)) continue;
         double px = v.x[i], py = v.y[i], pz = v.z[i];
-        const float xf = d2f(px), yf = d2f(py), zf = d2f(pz);
-        float t_local;
-        if (T.enabled) { t_local = grid_sample(T, T.value, xf, yf, zf); v.t_local[i] = t_local; }
-        else t_local = v.t_local[i];
-        if (C2.enabled) v.co2_local[i] = grid_sample(C2, C2.value, xf, yf, zf);
-        if (N2.enabled) v.n2_local[i] = grid_sample(N2, N2.value, xf, yf, zf);
+        const float t_local = v.t_local[i];       // sampled by forces_kernel this tick
         const float Fx = fx_in[i], Fy = fy_in[i], Fz = fz_in[i];
         const float mass = d2f(v.biomass[i]) + d2f(v.energy[i]) * (float)(1.0 / (AGB_C_LIGHT * AGB_C_LIGHT));
         // integrate_kernel (integrator.cu:79-150)

@@ -101,7 +101,7 @@ constexpr int TX = 64, TY = 16, HX = 4;                 // HX: leading x halo (a
 constexpr int BXW = TX + 2 * HX, BYH = TY + 2;          // box 72 x 18
 constexpr int PLANE_BYTES = BXW * BYH * 4;              // 5184
 constexpr int PLANE_STRIDE = (PLANE_BYTES + 127) / 128 * 128;
-constexpr int TZC = 8, NBUF = 4;
+constexpr int NBUF = 4;
 constexpr uint32_t WAIT_LIMIT = 1u << 26;               // bounded mbarrier polls
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -140,12 +140,13 @@ __device__ __forceinline__ void tma_load_plane(float* dst, const CUtensorMap* ma
 
 __global__ void __launch_bounds__(256) ftcs3d_tma_kernel(const __grid_constant__ CUtensorMap src_map,
                                                          float* __restrict__ dst, int32_t nx, int32_t ny,
-                                                         int32_t nz, float coeff, Faces f, uint32_t* err) {
+                                                         int32_t nz, int32_t zc, float coeff, Faces f,
+                                                         uint32_t* err) {
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + NBUF * PLANE_STRIDE);
     const int tid = threadIdx.x;
-    const int32_t x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, k0 = blockIdx.z * TZC;
-    const int32_t k1 = k0 + TZC < nz ? k0 + TZC : nz;
+    const int32_t x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, k0 = blockIdx.z * zc;
+    const int32_t k1 = k0 + zc < nz ? k0 + zc : nz;
     const int nplanes = (k1 - k0) + 2;                  // z = k0-1 .. k1
     auto buf = [&](int q) { return reinterpret_cast<float*>(smem + (q % NBUF) * PLANE_STRIDE); };
     if (tid == 0) {
@@ -246,8 +247,16 @@ void launch_ftcs(const GridDev& g, const float* src, float* dst, float coeff, co
     for (int k = 0; k < 6; ++k) { f.bc[k] = bc[k]; f.val[k] = face[k]; }
     f.robin = robin;
     if (g.nz > 1 && src_map != nullptr) {
-        const dim3 grid((g.nx + TX - 1) / TX, (g.ny + TY - 1) / TY, (g.nz + TZC - 1) / TZC);
-        ftcs3d_tma_kernel<<<grid, 256, NBUF * PLANE_STRIDE + 64, s>>>(*src_map, dst, g.nx, g.ny, g.nz, coeff, f, err);
+        // z planes per CTA: as many as keep the grid at >= 4 CTAs per SM (fewer
+        // planes per CTA re-read more halo planes, which come from L2), 2..16.
+        static int sms = 0;
+        if (sms == 0) { int d = 0; cudaGetDevice(&d); cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d); }
+        const int64_t tiles = (int64_t)((g.nx + TX - 1) / TX) * ((g.ny + TY - 1) / TY);
+        int32_t zc = (int32_t)(g.nz * tiles / (4 * (int64_t)(sms > 0 ? sms : 148)));
+        zc = zc < 2 ? 2 : (zc > 16 ? 16 : zc);
+        const dim3 grid((g.nx + TX - 1) / TX, (g.ny + TY - 1) / TY, (g.nz + zc - 1) / zc);
+        ftcs3d_tma_kernel<<<grid, 256, NBUF * PLANE_STRIDE + 64, s>>>(*src_map, dst, g.nx, g.ny, g.nz, zc, coeff, f,
+                                                                      err);
         return;
     }
     if (g.nz == 1) {

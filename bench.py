@@ -284,6 +284,27 @@ def run_reference(args, wl):
     return 0
 
 
+def profile_stencil(n, passes=6):
+    """A world holding one n^3 temperature grid (no cells): `passes` FTCS passes."""
+    d = agb.default_desc(capacity=16, seed=1)
+    d.taxis_enabled = 0
+    d.chamber_w = d.chamber_h = d.chamber_d = 4.0e-3
+    d.grid[agb.FIELD_T] = _grid3(n, agb.WATER_THERMAL_DIFFUSIVITY, agb.AMBIENT_TEMP_DEFAULT, 1e9, agb.BC_ROBIN)
+    for f in (agb.FIELD_CO2, agb.FIELD_N2, agb.FIELD_IRR):
+        d.grid[f] = agb.GridDesc()
+    w = agb.World(d)
+    rng = np.random.default_rng(5)
+    w.import_field(agb.FIELD_T, (290.0 + 80.0 * rng.random((n, n, n))).astype(np.float32))
+    dx = d.chamber_w / n
+    dt_pass = 0.9 * dx * dx / (6.0 * agb.WATER_THERMAL_DIFFUSIVITY)   # one pass per call
+    for _ in range(passes):
+        w.diffuse(agb.FIELD_T, dt_pass)
+    w.export_field(agb.FIELD_T)
+    assert w.counters()[3] == 0
+    print("profile-stencil %d^3: %d passes ok" % (n, passes))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -293,8 +314,12 @@ def main():
     ap.add_argument("--workload", default="slab25k", choices=["slab25k", "cube2k", "clusters1m"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-stencil", type=int, default=0,
+                    help="only run a few FTCS passes on an N^3 temperature grid (small case for ncu)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.profile_stencil:
+        return profile_stencil(args.profile_stencil)
 
     if args.impl == "reference":
         return run_reference(args, workload(args.workload, seed=1))
