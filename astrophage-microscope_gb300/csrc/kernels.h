@@ -13,11 +13,17 @@ struct WorldConst;   // defined in world.cuh
 
 // Fields (k_grid.cu)
 void launch_fill(float* v, int64_t n, float value, cudaStream_t s);
+// Tiling of the TMA stencil for a grid: lanes along x (16 or 32), rows per
+// thread (1, 2, 4) and z planes per CTA. A tensor map's box is made for one
+// tiling and is used only with it.
+struct FtcsPlan { int32_t lx, rpt, zc; };
+FtcsPlan ftcs_plan(int32_t nx, int32_t ny, int32_t nz);
 // One explicit FTCS pass src -> dst (src/fields/diffuse.cu:19-44; 7-point when nz > 1).
-// 3-D grids with a tensor map use the TMA-staged kernel.
+// 3-D grids with a tensor map (and the tiling it was made for) use the TMA-staged kernel.
 void launch_ftcs(const GridDev& g, const float* src, float* dst, float coeff, const int32_t* bc,
-                 const float* face, float robin, const CUtensorMap* src_map, uint32_t* err, cudaStream_t s);
-bool make_plane_map(CUtensorMap* map, float* base, int32_t nx, int32_t ny, int32_t nz);
+                 const float* face, float robin, const CUtensorMap* src_map, const FtcsPlan* plan, uint32_t* err,
+                 cudaStream_t s);
+bool make_plane_map(CUtensorMap* map, float* base, int32_t nx, int32_t ny, int32_t nz, const FtcsPlan& plan);
 // Fold deposits into the field for the voxels cells sit in (flush_kernel,
 // src/fields/diffuse.cu:51-60, restricted to voxels that can hold a deposit).
 void launch_flush_by_cells(DevState* S, GridDev g, unsigned long long* demand_to_clear,

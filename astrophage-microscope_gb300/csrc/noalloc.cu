@@ -74,7 +74,7 @@ extern "C" agb_status agb_grid_diffuse_noalloc(float* value, int32_t nx, int32_t
     float* src = value;
     float* dst = scratch;
     for (int32_t k = 0; k < steps; ++k) {
-        agb::launch_ftcs(g, src, dst, coeff, bc, face, robin, nullptr, nullptr, s);
+        agb::launch_ftcs(g, src, dst, coeff, bc, face, robin, nullptr, nullptr, nullptr, s);
         float* t = src; src = dst; dst = t;
     }
     if (src != value &&

@@ -40,6 +40,7 @@ struct agb_world {
     float* gbuf[AGB_FIELD_COUNT][2] = {};
     CUtensorMap tmap[AGB_FIELD_COUNT][2];      // TMA maps of each field buffer (3-D grids)
     bool tmap_ok[AGB_FIELD_COUNT] = {};
+    FtcsPlan tplan[AGB_FIELD_COUNT] = {};      // the tiling each field's maps were made for
     bool use_tma = true;
     int gcur[AGB_FIELD_COUNT] = {};
     unsigned long long* gdep[AGB_FIELD_COUNT] = {};
@@ -229,7 +230,7 @@ void ftcs(agb_world* w, int f, float coeff, cudaStream_t s) {
     refresh_grid_ptrs(w);
     const CUtensorMap* map = (w->use_tma && w->tmap_ok[f]) ? &w->tmap[f][w->gcur[f]] : nullptr;
     launch_ftcs(w->c.g[f], field_value(w, f), w->gbuf[f][1 - w->gcur[f]], coeff, w->gbc[f], w->gface[f],
-                w->grobin[f], map, &w->S->error, s);
+                w->grobin[f], map, &w->tplan[f], &w->S->error, s);
     w->gcur[f] = 1 - w->gcur[f];
     refresh_grid_ptrs(w);
 }
@@ -491,8 +492,9 @@ agb_status agb_world_create(const agb_world_desc* d, agb_world** out) {
             agb_world_destroy(w); return AGB_OUT_OF_MEMORY;
         }
         g.deposit = w->gdep[f];
-        w->tmap_ok[f] = make_plane_map(&w->tmap[f][0], w->gbuf[f][0], g.nx, g.ny, g.nz) &&
-                        make_plane_map(&w->tmap[f][1], w->gbuf[f][1], g.nx, g.ny, g.nz);
+        if (g.nz > 1) w->tplan[f] = ftcs_plan(g.nx, g.ny, g.nz);
+        w->tmap_ok[f] = g.nz > 1 && make_plane_map(&w->tmap[f][0], w->gbuf[f][0], g.nx, g.ny, g.nz, w->tplan[f]) &&
+                        make_plane_map(&w->tmap[f][1], w->gbuf[f][1], g.nx, g.ny, g.nz, w->tplan[f]);
         launch_fill(w->gbuf[f][0], g.count, (float)gd.init, nullptr);
         launch_fill(w->gbuf[f][1], g.count, (float)gd.init, nullptr);
     }

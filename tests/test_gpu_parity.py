@@ -145,6 +145,20 @@ def test_diffusion_bit_exact(nz, bcs):
 @pytest.mark.parametrize("nx,ny,nz", [(100, 36, 20), (256, 20, 9), (64, 64, 64)])
 def test_diffusion_3d_partial_tiles_bit_exact(nx, ny, nz):
     """The TMA-staged 3-D stencil on grids that leave partial tiles in every axis."""
+    check_3d_diffusion(nx, ny, nz)
+
+
+@pytest.mark.parametrize("tile", ["32,1,3", "32,2,1", "32,4,5", "16,1,7", "16,2,2", "32,2,64"])
+@pytest.mark.parametrize("nx,ny,nz", [(136, 40, 11), (64, 64, 64)])
+def test_diffusion_every_tiling_bit_exact(tile, nx, ny, nz, monkeypatch):
+    """Every tiling of the TMA stencil (lanes along x, rows per thread, z planes
+    per CTA), forced through AGB_FTCS_TILE at world creation, gives the oracle's
+    field bit for bit, including z chunks of one plane and of the whole grid."""
+    monkeypatch.setenv("AGB_FTCS_TILE", tile)
+    check_3d_diffusion(nx, ny, nz)
+
+
+def check_3d_diffusion(nx, ny, nz):
     dx = 1.0e-5
     d = S.slab_desc(light=None)
     d.chamber_w, d.chamber_h, d.chamber_d = nx * dx, ny * dx, nz * dx
