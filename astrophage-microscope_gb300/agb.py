@@ -117,6 +117,23 @@ class Stats(C.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+class BatchOpts(C.Structure):
+    _fields_ = [("abi_version", C.c_uint32), ("lanes", C.c_int32), ("autotune", C.c_int32),
+                ("n_hash_candidates", C.c_int32), ("hash_candidates", C.c_double * 8),
+                ("probe_ticks", C.c_int32)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("hash_cell_size", C.c_double), ("size_class", C.c_int32), ("lane", C.c_int32),
+                ("ftcs_lx", C.c_int32 * 3), ("ftcs_rpt", C.c_int32 * 3), ("ftcs_zc", C.c_int32 * 3),
+                ("probe_tick_ms", C.c_float), ("probe_pass_us", C.c_float)]
+
+    def as_dict(self):
+        return {"hash_cell_size": self.hash_cell_size, "size_class": self.size_class, "lane": self.lane,
+                "ftcs": [[self.ftcs_lx[f], self.ftcs_rpt[f], self.ftcs_zc[f]] for f in range(3)],
+                "probe_tick_ms": self.probe_tick_ms, "probe_pass_us": self.probe_pass_us}
+
+
 def grid(n, nz, diffusivity, init, scale, bc, face_value=None):
     g = GridDesc()
     g.nx, g.ny, g.nz = n, n, nz
@@ -261,6 +278,16 @@ def load(path=LIB_PATH):
         "agb_world_counters": (I32, [P, P, P]),
         "agb_grid_diffuse_noalloc": (I32, [P, I32, I32, I32, C.c_double, C.c_double, C.c_double,
                                            C.POINTER(I32), C.POINTER(C.c_double), P]),
+        "agb_batch_opts_default": (None, [C.POINTER(BatchOpts)]),
+        "agb_batch_create": (I32, [P, P, I32, C.POINTER(BatchOpts), C.POINTER(P)]),
+        "agb_batch_destroy": (None, [P]),
+        "agb_batch_last_error": (C.c_char_p, [P]),
+        "agb_batch_size": (I32, [P, C.POINTER(I32)]),
+        "agb_batch_world": (I32, [P, I32, C.POINTER(P)]),
+        "agb_batch_tuning": (I32, [P, I32, C.POINTER(Tuning)]),
+        "agb_batch_step": (I32, [P, I32, P]),
+        "agb_batch_graph_kernels": (I32, [P, C.POINTER(C.c_int64)]),
+        "agb_batch_stats": (I32, [P, P]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -279,7 +306,10 @@ def exported_symbols():
             "agb_world_diffuse",
             "agb_world_stats", "agb_world_stats_accum", "agb_world_set_clock",
             "agb_world_set_light", "agb_world_export_hash", "agb_world_export_forces",
-            "agb_world_counters", "agb_grid_diffuse_noalloc"]
+            "agb_world_counters", "agb_grid_diffuse_noalloc",
+            "agb_batch_opts_default", "agb_batch_create", "agb_batch_destroy", "agb_batch_last_error",
+            "agb_batch_size", "agb_batch_world", "agb_batch_tuning", "agb_batch_step",
+            "agb_batch_graph_kernels", "agb_batch_stats"]
 
 
 def _st(stream):
@@ -410,3 +440,86 @@ class World:
         out = np.zeros(4, dtype=np.int64)
         self._check(self.lib.agb_world_counters(self.h, out.ctypes.data, None), "counters")
         return out
+
+
+class _ChamberView(World):
+    """A chamber of a Batch: the World interface over a handle the batch owns."""
+
+    def __init__(self, handle, desc, lib, owner):
+        self.lib, self.desc, self.h, self._owner = lib, desc, handle, owner
+
+    def close(self):
+        self.h = None
+
+
+def batch_opts(autotune=False, lanes=0, hash_candidates=(), probe_ticks=4, lib=None):
+    lib = lib or load()
+    o = BatchOpts()
+    lib.agb_batch_opts_default(C.byref(o))
+    o.autotune = 1 if autotune else 0
+    o.lanes = lanes
+    o.n_hash_candidates = len(hash_candidates)
+    for k, h in enumerate(hash_candidates[:8]):
+        o.hash_candidates[k] = h
+    o.probe_ticks = probe_ticks
+    return o
+
+
+class Batch:
+    """Independent chambers advanced together, one graph launch per step()."""
+
+    def __init__(self, descs, spawns, opts=None, lib=None):
+        self.lib = lib or load()
+        n = len(descs)
+        self.descs = (WorldDesc * n)(*descs)
+        self.spawns = (Spawn * n)(*spawns) if spawns is not None else None
+        o = opts if opts is not None else batch_opts(lib=self.lib)
+        h = C.c_void_p()
+        rc = self.lib.agb_batch_create(C.cast(self.descs, C.c_void_p),
+                                       C.cast(self.spawns, C.c_void_p) if self.spawns is not None else None,
+                                       n, C.byref(o), C.byref(h))
+        if rc != OK:
+            raise AgbError("agb_batch_create failed: %s" % status_name(rc))
+        self.h = h
+        self.n = n
+        self.chambers = []
+        for i in range(n):
+            wh = C.c_void_p()
+            self._check(self.lib.agb_batch_world(self.h, i, C.byref(wh)), "agb_batch_world")
+            self.chambers.append(_ChamberView(wh, self.descs[i], self.lib, self))
+
+    def _check(self, rc, what):
+        if rc != OK:
+            msg = self.lib.agb_batch_last_error(self.h) if getattr(self, "h", None) else b""
+            raise AgbError("%s failed: %s %s" % (what, status_name(rc), (msg or b"").decode()))
+
+    def close(self):
+        if getattr(self, "h", None):
+            for c in self.chambers:
+                c.h = None
+            self.lib.agb_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, ticks=1, stream=None):
+        self._check(self.lib.agb_batch_step(self.h, ticks, _st(stream)), "agb_batch_step")
+
+    def tuning(self, i):
+        t = Tuning()
+        self._check(self.lib.agb_batch_tuning(self.h, i, C.byref(t)), "agb_batch_tuning")
+        return t
+
+    def graph_kernels(self):
+        k = C.c_int64()
+        self._check(self.lib.agb_batch_graph_kernels(self.h, C.byref(k)), "agb_batch_graph_kernels")
+        return k.value
+
+    def stats(self):
+        out = (Stats * self.n)()
+        self._check(self.lib.agb_batch_stats(self.h, C.cast(out, C.c_void_p)), "agb_batch_stats")
+        return list(out)

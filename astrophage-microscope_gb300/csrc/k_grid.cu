@@ -343,15 +343,10 @@ int sm_count() {
 // On a GB300 this measured 24.7 us per pass on 256^3 (5.4 TB/s) and 8.2 us on
 // 128^3, within 5 % of the best tiling of each. AGB_FTCS_TILE="lx,rpt,zc"
 // overrides the choice (a tuning knob; results are the same for every tiling).
-FtcsPlan ftcs_plan(int32_t nx, int32_t ny, int32_t nz) {
-    const int64_t voxels = (int64_t)nx * ny * nz;
-    FtcsPlan p{nx >= 256 ? 32 : 16, voxels >= (8 << 20) ? 2 : 1, 0};
-    if (const char* e = std::getenv("AGB_FTCS_TILE")) {
-        int lx = 0, rpt = 0, zc = 0;
-        if (std::sscanf(e, "%d,%d,%d", &lx, &rpt, &zc) >= 2 && (lx == 16 || lx == 32) &&
-            (rpt == 1 || rpt == 2 || rpt == 4) && !(lx == 16 && rpt == 4)) {
-            p.lx = lx; p.rpt = rpt; p.zc = zc > 0 ? zc : 0;
-        }
+FtcsPlan ftcs_plan_with(int32_t nx, int32_t ny, int32_t nz, int32_t lx, int32_t rpt, int32_t zc_in) {
+    FtcsPlan p{lx, rpt, zc_in > 0 ? zc_in : 0};
+    if (!(lx == 16 || lx == 32) || !(rpt == 1 || rpt == 2 || rpt == 4) || (lx == 16 && rpt == 4)) {
+        p.lx = 16; p.rpt = 1;
     }
     if (p.zc == 0) {
         int per_sm = 1;
@@ -367,6 +362,19 @@ FtcsPlan ftcs_plan(int32_t nx, int32_t ny, int32_t nz) {
         p.zc = (int32_t)((nz + chunks - 1) / chunks);
     }
     return p;
+}
+
+FtcsPlan ftcs_plan(int32_t nx, int32_t ny, int32_t nz) {
+    const int64_t voxels = (int64_t)nx * ny * nz;
+    int32_t lx = nx >= 256 ? 32 : 16, rpt = voxels >= (8 << 20) ? 2 : 1, zc = 0;
+    if (const char* e = std::getenv("AGB_FTCS_TILE")) {
+        int a = 0, b = 0, c = 0;
+        if (std::sscanf(e, "%d,%d,%d", &a, &b, &c) >= 2 && (a == 16 || a == 32) && (b == 1 || b == 2 || b == 4) &&
+            !(a == 16 && b == 4)) {
+            lx = a; rpt = b; zc = c > 0 ? c : 0;
+        }
+    }
+    return ftcs_plan_with(nx, ny, nz, lx, rpt, zc);
 }
 
 void launch_ftcs(const GridDev& g, const float* src, float* dst, float coeff, const int32_t* bc,

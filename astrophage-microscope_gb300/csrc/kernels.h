@@ -18,6 +18,9 @@ void launch_fill(float* v, int64_t n, float value, cudaStream_t s);
 // tiling and is used only with it.
 struct FtcsPlan { int32_t lx, rpt, zc; };
 FtcsPlan ftcs_plan(int32_t nx, int32_t ny, int32_t nz);
+// A given tiling (lx 16/32, rpt 1/2/4; lx 16 with rpt 4 is not built) with the
+// z chunk chosen as ftcs_plan chooses it when zc <= 0.
+FtcsPlan ftcs_plan_with(int32_t nx, int32_t ny, int32_t nz, int32_t lx, int32_t rpt, int32_t zc);
 // One explicit FTCS pass src -> dst (src/fields/diffuse.cu:19-44; 7-point when nz > 1).
 // 3-D grids with a tensor map (and the tiling it was made for) use the TMA-staged kernel.
 void launch_ftcs(const GridDev& g, const float* src, float* dst, float coeff, const int32_t* bc,

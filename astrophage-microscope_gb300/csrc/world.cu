@@ -15,58 +15,9 @@
 #include <string>
 #include <vector>
 
-#include "cells.h"
+#include "world_impl.cuh"
 
 using namespace agb;
-
-struct GraphEntry {
-    int32_t ticks;
-    uint32_t parity;        // which buffer holds each field at capture start
-    uint64_t tick_phase;    // tick % compaction_period at capture start
-    cudaGraphExec_t exec;
-    uint32_t parity_after;
-    int32_t kernels;        // kernel nodes per replay
-};
-
-struct agb_world {
-    agb_world_desc d{};
-    int dev = 0;
-    int sm_count = 0;
-    Ctx c{};
-    TickParams tp{};
-    DevState* S = nullptr;
-    void* blob[2] = {nullptr, nullptr};
-    size_t blob_bytes = 0;
-    float* gbuf[AGB_FIELD_COUNT][2] = {};
-    CUtensorMap tmap[AGB_FIELD_COUNT][2];      // TMA maps of each field buffer (3-D grids)
-    bool tmap_ok[AGB_FIELD_COUNT] = {};
-    FtcsPlan tplan[AGB_FIELD_COUNT] = {};      // the tiling each field's maps were made for
-    bool use_tma = true;
-    int gcur[AGB_FIELD_COUNT] = {};
-    unsigned long long* gdep[AGB_FIELD_COUNT] = {};
-    int32_t gbc[AGB_FIELD_COUNT][6] = {};
-    float gface[AGB_FIELD_COUNT][6] = {};
-    float grobin[AGB_FIELD_COUNT] = {};
-    uint32_t *kalt = nullptr, *valt = nullptr, *hist = nullptr;
-    LifeBuffers life{};
-    int32_t* stamp_idx = nullptr;
-    double* occl_factor = nullptr;       // per irradiance voxel: transmittance of stamped voxels
-    cudaStream_t side[2] = {nullptr, nullptr};   // concurrent branches of a tick
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-    float *fx = nullptr, *fy = nullptr, *fz = nullptr;
-    unsigned long long* acc = nullptr;
-    int32_t blocks = 1;
-    uint64_t tick = 0;
-    double sim_time = 0.0;
-    double physics_rate = 1.0, biology_rate = 1.0;
-    int64_t deaths_reported = 0;
-    unsigned long long acc_host[12] = {};
-    std::vector<GraphEntry> graphs;
-    cudaStream_t own_stream = nullptr;   // capture stream when the caller passes the default stream
-    int64_t graph_kernels_total = 0;     // kernel nodes launched by graph replays so far
-    std::string err;
-    std::vector<void*> allocs;
-};
 
 namespace {
 
@@ -330,6 +281,7 @@ uint32_t parity_bits(const agb_world* w) {
 void invalidate_graphs(agb_world* w) {
     for (auto& g : w->graphs) cudaGraphExecDestroy(g.exec);
     w->graphs.clear();
+    ++w->version;
 }
 
 agb_status read_state(agb_world* w, DevState& out, cudaStream_t s) {
@@ -339,6 +291,71 @@ agb_status read_state(agb_world* w, DevState& out, cudaStream_t s) {
 }
 
 }  // namespace
+
+// Entry points for the batch (batch.cu); see world_impl.cuh.
+namespace agb {
+
+void world_tick(agb_world* w, cudaStream_t s) { tick_once(w, s); }
+uint32_t world_parity(const agb_world* w) { return parity_bits(w); }
+void world_set_parity(agb_world* w, uint32_t bits) {
+    for (int f = 0; f < AGB_FIELD_COUNT; ++f) w->gcur[f] = (bits >> f) & 1;
+    refresh_grid_ptrs(w);
+}
+uint64_t world_phase(const agb_world* w) {
+    const uint64_t P = w->d.compaction_period > 0 ? (uint64_t)w->d.compaction_period : 1;
+    return w->tick % P;
+}
+void world_advance_clock(agb_world* w, int32_t ticks) {
+    w->tick += (uint64_t)ticks;
+    w->sim_time += w->tp.dt * ticks;
+}
+
+bool world_set_tiling(agb_world* w, int f, const FtcsPlan& p) {
+    const GridDev& g = w->c.g[f];
+    if (!g.enabled || g.nz <= 1 || !w->tmap_ok[f]) return false;
+    CUtensorMap m[2];
+    if (!make_plane_map(&m[0], w->gbuf[f][0], g.nx, g.ny, g.nz, p) ||
+        !make_plane_map(&m[1], w->gbuf[f][1], g.nx, g.ny, g.nz, p))
+        return false;
+    w->tmap[f][0] = m[0];
+    w->tmap[f][1] = m[1];
+    w->tplan[f] = p;
+    invalidate_graphs(w);
+    return true;
+}
+
+float world_time_passes(agb_world* w, int f, int passes, cudaStream_t s) {
+    const GridDev& g = w->c.g[f];
+    if (!g.enabled || passes <= 0) return -1.0f;
+    const float coeff = (float)(1.0 / 8.0);
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return -1.0f;
+    for (int k = 0; k < 2 * passes; ++k) ftcs(w, f, coeff, s);      // even: buffers end where they began
+    if (cudaStreamEndCapture(s, &graph) != cudaSuccess) return -1.0f;
+    const bool ok = cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+    cudaGraphDestroy(graph);
+    if (!ok) return -1.0f;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = -1.0f;
+    for (int r = 0; r < 4; ++r) {
+        cudaEventRecord(e0, s);
+        cudaGraphLaunch(exec, s);
+        cudaEventRecord(e1, s);
+        if (cudaEventSynchronize(e1) != cudaSuccess) { best = -1.0f; break; }
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (r > 0 && (best < 0.0f || ms < best)) best = ms;       // first replay warms up
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaGraphExecDestroy(exec);
+    return best < 0.0f ? best : best / (2.0f * passes);
+}
+
+}  // namespace agb
 
 extern "C" {
 

@@ -1,0 +1,82 @@
+// world_impl.cuh -- the world object behind the C ABI, shared by world.cu
+// (one chamber) and batch.cu (many chambers in one graph).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "cells.h"
+
+using namespace agb;   // internal header: the engine's own types
+
+struct GraphEntry {
+    int32_t ticks;
+    uint32_t parity;        // which buffer holds each field at capture start
+    uint64_t tick_phase;    // tick % compaction_period at capture start
+    cudaGraphExec_t exec;
+    uint32_t parity_after;
+    int32_t kernels;        // kernel nodes per replay
+};
+
+struct agb_world {
+    agb_world_desc d{};
+    int dev = 0;
+    int sm_count = 0;
+    Ctx c{};
+    TickParams tp{};
+    DevState* S = nullptr;
+    void* blob[2] = {nullptr, nullptr};
+    size_t blob_bytes = 0;
+    float* gbuf[AGB_FIELD_COUNT][2] = {};
+    CUtensorMap tmap[AGB_FIELD_COUNT][2];      // TMA maps of each field buffer (3-D grids)
+    bool tmap_ok[AGB_FIELD_COUNT] = {};
+    FtcsPlan tplan[AGB_FIELD_COUNT] = {};      // the tiling each field's maps were made for
+    bool use_tma = true;
+    int gcur[AGB_FIELD_COUNT] = {};
+    unsigned long long* gdep[AGB_FIELD_COUNT] = {};
+    int32_t gbc[AGB_FIELD_COUNT][6] = {};
+    float gface[AGB_FIELD_COUNT][6] = {};
+    float grobin[AGB_FIELD_COUNT] = {};
+    uint32_t *kalt = nullptr, *valt = nullptr, *hist = nullptr;
+    LifeBuffers life{};
+    int32_t* stamp_idx = nullptr;
+    double* occl_factor = nullptr;       // per irradiance voxel: transmittance of stamped voxels
+    cudaStream_t side[2] = {nullptr, nullptr};   // concurrent branches of a tick
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    float *fx = nullptr, *fy = nullptr, *fz = nullptr;
+    unsigned long long* acc = nullptr;
+    int32_t blocks = 1;
+    uint64_t tick = 0;
+    double sim_time = 0.0;
+    double physics_rate = 1.0, biology_rate = 1.0;
+    int64_t deaths_reported = 0;
+    unsigned long long acc_host[12] = {};
+    std::vector<GraphEntry> graphs;
+    cudaStream_t own_stream = nullptr;   // capture stream when the caller passes the default stream
+    int64_t graph_kernels_total = 0;     // kernel nodes launched by graph replays so far
+    uint64_t version = 0;                // bumped whenever captured graphs go stale
+    std::string err;
+    std::vector<void*> allocs;
+};
+
+namespace agb {
+
+// One tick of one world enqueued on s (forks onto the world's side streams
+// and joins back); advances the host-side tick state as it goes.
+void world_tick(agb_world* w, cudaStream_t s);
+// Which ping-pong buffer holds each field (bit f = field f), and setting it.
+uint32_t world_parity(const agb_world* w);
+void world_set_parity(agb_world* w, uint32_t bits);
+// tick % compaction period: which compaction decision the next tick takes.
+uint64_t world_phase(const agb_world* w);
+void world_advance_clock(agb_world* w, int32_t ticks);
+// Switch field f's stencil tiling (rebuilds its tensor maps); false when the
+// field has no TMA path or the maps cannot be made.
+bool world_set_tiling(agb_world* w, int f, const FtcsPlan& p);
+// Milliseconds per FTCS pass of field f, from a captured graph of 2 * passes
+// passes (best of three timed replays). Changes the field's contents.
+float world_time_passes(agb_world* w, int f, int passes, cudaStream_t s);
+
+}  // namespace agb

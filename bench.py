@@ -101,6 +101,85 @@ def workload(name, seed=1):
     raise SystemExit("unknown workload " + name)
 
 
+def batch_workload(n=64, seed=1):
+    """The batched ensemble: n independent 4 mm chambers with seeds seed..seed+n-1,
+    cell counts log-uniform in [1e3, 2e5], temperature/CO2/irradiance grid edge
+    drawn from {64, 96, 128, 192}, charge uniform in [0, q] with q swept
+    linearly up to 0.20 over the chambers. Otherwise the slab25k recipe: light
+    +x at 1e4 W/m^2, division at 0.16 Emax, compaction every 10 ticks, awake
+    cells placed uniformly. Draws come from a numpy generator seeded with seed."""
+    rng = np.random.default_rng(seed)
+    counts = np.rint(np.exp(rng.uniform(np.log(1.0e3), np.log(2.0e5), n))).astype(int)
+    edges = rng.choice([64, 96, 128, 192], n)
+    descs, spawns = [], []
+    for i in range(n):
+        d = agb.default_desc(capacity=int(2 * counts[i]), seed=seed + i, co2_init=1.0)
+        d.chamber_w = d.chamber_h = d.chamber_d = 4.0e-3
+        e = int(edges[i])
+        d.grid[agb.FIELD_T] = _grid3(e, agb.WATER_THERMAL_DIFFUSIVITY, agb.AMBIENT_TEMP_DEFAULT, 1e9, agb.BC_ROBIN)
+        d.grid[agb.FIELD_CO2] = _grid3(e, agb.CO2_DIFFUSIVITY_WATER, 1.0, 1e15, agb.BC_NEUMANN)
+        d.grid[agb.FIELD_N2] = agb.GridDesc()
+        d.grid[agb.FIELD_IRR] = _grid3(e, agb.IRRADIANCE_NOMINAL_DIFFUSIVITY, 0.0, 1e18, agb.BC_NEUMANN)
+        d.taxis_enabled = 0
+        d.light = agb.Light(1.0, 0.0, 0.0, 1.0e4, 0.0, 1)
+        d.division_predicate = agb.DIVIDE_ENERGY
+        d.division_energy = 0.16 * EMAX
+        d.compaction_enabled = 1
+        d.compaction_period = 10
+        d.biology_rate = 1.0e5
+        q = 0.20 * (i + 1) / n
+        descs.append(d)
+        spawns.append(agb.spawn(int(counts[i]), charge_dist=agb.DIST_UNIFORM, charge_a=0.0, charge_b=q,
+                                awake=True))
+    info = dict(chambers=n, cells=int(counts.sum()), cells_min=int(counts.min()), cells_max=int(counts.max()),
+                grid_edges={str(k): int((edges == k).sum()) for k in (64, 96, 128, 192)}, chamber_mm=4.0)
+    return descs, spawns, info
+
+
+def run_batch(args, stream, l2_flush):
+    """Time the batched ensemble: one graph launch per step for all chambers."""
+    import torch
+    descs, spawns, info = batch_workload(args.batch_chambers, seed=1)
+    t0 = time.perf_counter()
+    b = agb.Batch(descs, spawns, agb.batch_opts(autotune=True, lanes=args.batch_lanes))
+    setup_s = time.perf_counter() - t0
+    sh = stream.cuda_stream
+    with torch.cuda.stream(stream):
+        for _ in range(max(args.warmup, 20)):           # two compaction periods: every graph captured
+            b.step(1, stream=sh)
+        torch.cuda.synchronize()
+        n0 = sum(c.count() for c in b.chambers)
+        k0 = b.graph_kernels()
+        ms = []
+        for _ in range(args.batch_steps):
+            l2_flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            b.step(1, stream=sh)
+            e1.record(stream)
+            ms.append((e0, e1))
+        torch.cuda.synchronize()
+        n1 = sum(c.count() for c in b.chambers)
+        launches = b.graph_kernels() - k0
+    total_s = sum(a.elapsed_time(z) for a, z in ms) / 1e3
+    vox = sum(voxel_steps_per_tick(d) for d in descs)
+    classes = {}
+    for i in range(b.n):
+        t = b.tuning(i).as_dict()
+        classes.setdefault(t["size_class"], {"hash_cell_um": round(t["hash_cell_size"] * 1e6, 2),
+                                             "ftcs_T": t["ftcs"][0], "chambers": 0})["chambers"] += 1
+    out = {"cell_steps_per_s": 0.5 * (n0 + n1) * args.batch_steps / total_s,
+           "voxel_steps_per_s": vox * args.batch_steps / total_s,
+           "ms_per_step": total_s * 1e3 / args.batch_steps, "steps": args.batch_steps,
+           "cells_start_end": [n0, n1], "gpu_launches": launches, "setup_s": setup_s,
+           "lanes": args.batch_lanes or min(args.batch_chambers, 16),
+           "config": dict(info, workload="batch%d" % args.batch_chambers,
+                          step="one tick of every chamber, one graph launch"),
+           "autotune": classes}
+    b.close()
+    return out
+
+
 def substeps(desc, f):
     """FTCS passes per tick of field f (src/fields/grid.cuh:51-53; 1/6 bound in 3-D)."""
     g = desc.grid[f]
@@ -314,6 +393,10 @@ def main():
     ap.add_argument("--workload", default="slab25k", choices=["slab25k", "cube2k", "clusters1m"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--batch-steps", type=int, default=30,
+                    help="timed steps of the batched ensemble reported beside the plain step (0: skip)")
+    ap.add_argument("--batch-chambers", type=int, default=64)
+    ap.add_argument("--batch-lanes", type=int, default=0)
     ap.add_argument("--profile-stencil", type=int, default=0,
                     help="only run a few FTCS passes on an N^3 temperature grid (small case for ncu)")
     args = ap.parse_args()
@@ -372,23 +455,32 @@ def main():
     vox_steps = allreduce_sum(dist, float(voxel_steps_per_tick(desc)) * args.steps)
     value = cell_steps / total_s
 
-    # Dominant-kernel roofline: the 3-D FTCS pass on the temperature grid, timed
-    # with events around back-to-back launches on the same stream.
+    # Dominant-kernel roofline: the 3-D FTCS pass on the temperature grid. The
+    # passes of `reps` diffusion calls are captured in one CUDA graph (so host
+    # launch cost is not counted) and each replay, after an L2 flush, is timed
+    # with events on the stream it runs on.
     peak, peak_kind = measured_peaks()
     gT = desc.grid[agb.FIELD_T]
     vox_T = gT.nx * gT.ny * gT.nz
-    reps = 50
+    reps, replays = 20, 5
+    ftcs_graph = torch.cuda.CUDAGraph()
     with torch.cuda.stream(stream):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         world.diffuse(agb.FIELD_T, agb.DT_PHYSICS, stream=sh)
         torch.cuda.synchronize()
-        l2_flush.zero_()
-        e0.record(stream)
+    with torch.cuda.graph(ftcs_graph, stream=stream):
         for _ in range(reps):
-            world.diffuse(agb.FIELD_T, agb.DT_PHYSICS, stream=sh)
-        e1.record(stream)
-        torch.cuda.synchronize()
-    ftcs_s = e0.elapsed_time(e1) / 1e3 / (reps * substeps(desc, agb.FIELD_T))   # per pass
+            world.diffuse(agb.FIELD_T, agb.DT_PHYSICS, stream=torch.cuda.current_stream().cuda_stream)
+    ftcs_ms = 0.0
+    with torch.cuda.stream(stream):
+        for _ in range(replays):
+            l2_flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ftcs_graph.replay()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ftcs_ms += e0.elapsed_time(e1)
+    ftcs_s = ftcs_ms / 1e3 / (replays * reps * substeps(desc, agb.FIELD_T))   # per pass
     algo_bytes = 8.0 * vox_T
     achieved = algo_bytes / ftcs_s / 1e9
     traffic = profile_traffic("ftcs3d_%d" % gT.nx)
@@ -419,6 +511,11 @@ def main():
                "d2h_bytes_per_step": bytes_state,
                "path": "agb_world_import_cells + agb_world_step_graph + agb_world_export_cells, pinned host SoA"}
 
+    batched = None
+    if rank == 0 and args.batch_steps > 0:
+        world.close()
+        batched = run_batch(args, stream, l2_flush)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -442,11 +539,15 @@ def main():
             "roofline": {"bound": "hbm", "kernel": "ftcs3d (temperature, %d^3)" % gT.nx,
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_source": peak_kind, "algorithmic_bytes_per_launch": algo_bytes,
-                         "launch_us": ftcs_s * 1e6, "traffic": traffic},
+                         "launch_us": ftcs_s * 1e6, "traffic": traffic,
+                         "timing": "mean pass of %d graph-captured back-to-back passes after an L2 flush; "
+                                   "field %.0f MB (%s L2)" % (reps * substeps(desc, agb.FIELD_T), 4.0 * vox_T / 1e6,
+                                                              "inside" if 8.0 * vox_T < 100e6 else "larger than")},
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": launches,
             "clocks": clocks,
+            "batched": batched,
         }
         print(json.dumps(line))
     if dist is not None:

@@ -199,6 +199,32 @@ enum {
     AGB_STAGE_CLOCK = 8        /* ++tick; sim_time += dt, src/sim/step.cu:182-183 */
 };
 
+/* Batched ensembles (no counterpart in the reference, which runs one World per
+ * process): N independent chambers of uneven cell counts and grid sizes, each
+ * a full world, advanced together by one CUDA graph launch per
+ * agb_batch_step call. */
+typedef struct agb_batch agb_batch;
+#define AGB_BATCH_MAX_CHAMBERS 4096
+
+typedef struct agb_batch_opts {
+    uint32_t abi_version;       /* AGB_ABI_VERSION */
+    int32_t lanes;              /* concurrent branches of the batch graph; 0 = min(n, 16) */
+    int32_t autotune;           /* 1: time candidate hash cells and stencil tilings per size class */
+    int32_t n_hash_candidates;  /* 0: 1.0, 1.5, 2.2 and 3.0 cell diameters */
+    double hash_candidates[8];  /* metres; candidates under one cell diameter are skipped */
+    int32_t probe_ticks;        /* timed probe ticks per candidate (0 = 4) */
+} agb_batch_opts;
+
+/* What a chamber was built with, and what the autotuner measured for it. */
+typedef struct agb_tuning {
+    double hash_cell_size;      /* metres */
+    int32_t size_class;         /* chambers sharing temperature grid edge and cell-count decade */
+    int32_t lane;               /* branch of the batch graph */
+    int32_t ftcs_lx[3], ftcs_rpt[3], ftcs_zc[3];   /* stencil tiling of T, CO2, N2 (0: no TMA path) */
+    float probe_tick_ms;        /* best probe tick of the class (0 when not tuned) */
+    float probe_pass_us;        /* best probe FTCS pass of the class's temperature grid */
+} agb_tuning;
+
 /* Reference defaults: 4 mm x 4 mm x 60 um slab, 512^2 temperature (Robin),
  * 256^2 CO2, 128^2 N2 and 512^2 irradiance grids (all nz = 1), canon hash. */
 void agb_world_desc_default(agb_world_desc* d);
@@ -288,6 +314,26 @@ agb_status agb_world_export_forces(agb_world* w, float* fx, float* fy, float* fz
 /* Device counters: {divisions_this_window, deaths_total, dead_slots_prev,
  * device error word}. Syncs. */
 agb_status agb_world_counters(agb_world* w, int64_t out[4], agb_stream s);
+
+/* Batches. agb_batch_create builds chamber i from descs[i], seeds it with
+ * spawns[i] (may be NULL: no cells) and, with opts->autotune, first picks each
+ * size class's hash cell size and stencil tilings by timing probe chambers.
+ * agb_batch_step advances every chamber by `ticks` ticks in one graph launch
+ * on s (NULL: the batch's own stream); each chamber's result equals a
+ * standalone world built with agb_batch_tuning's hash cell size. Chamber
+ * handles from agb_batch_world are owned by the batch and accept every
+ * agb_world_* call between steps. agb_batch_stats fills n agb_stats. */
+void agb_batch_opts_default(agb_batch_opts* o);
+agb_status agb_batch_create(const agb_world_desc* descs, const agb_spawn* spawns, int32_t n,
+                            const agb_batch_opts* opts, agb_batch** out);
+void agb_batch_destroy(agb_batch* b);
+const char* agb_batch_last_error(const agb_batch* b);
+agb_status agb_batch_size(agb_batch* b, int32_t* n);
+agb_status agb_batch_world(agb_batch* b, int32_t i, agb_world** w);
+agb_status agb_batch_tuning(agb_batch* b, int32_t i, agb_tuning* out);
+agb_status agb_batch_step(agb_batch* b, int32_t ticks, agb_stream s);
+agb_status agb_batch_graph_kernels(agb_batch* b, int64_t* kernels);
+agb_status agb_batch_stats(agb_batch* b, agb_stats* out);
 
 #ifdef __cplusplus
 }
