@@ -278,6 +278,10 @@ def load(path=LIB_PATH):
         "agb_world_counters": (I32, [P, P, P]),
         "agb_grid_diffuse_noalloc": (I32, [P, I32, I32, I32, C.c_double, C.c_double, C.c_double,
                                            C.POINTER(I32), C.POINTER(C.c_double), P]),
+        "agb_fnv1a64": (C.c_uint64, [P, C.c_uint64, C.c_uint64]),
+        "agb_world_state_hash": (I32, [P, C.POINTER(C.c_uint64), P]),
+        "agb_world_snapshot_save": (I32, [P, C.c_char_p, P, C.c_int64, C.POINTER(C.c_int64), P]),
+        "agb_world_snapshot_load": (I32, [C.POINTER(WorldDesc), P, C.c_int64, C.POINTER(P)]),
         "agb_batch_opts_default": (None, [C.POINTER(BatchOpts)]),
         "agb_batch_create": (I32, [P, P, I32, C.POINTER(BatchOpts), C.POINTER(P)]),
         "agb_batch_destroy": (None, [P]),
@@ -307,6 +311,7 @@ def exported_symbols():
             "agb_world_stats", "agb_world_stats_accum", "agb_world_set_clock",
             "agb_world_set_light", "agb_world_export_hash", "agb_world_export_forces",
             "agb_world_counters", "agb_grid_diffuse_noalloc",
+            "agb_fnv1a64", "agb_world_state_hash", "agb_world_snapshot_save", "agb_world_snapshot_load",
             "agb_batch_opts_default", "agb_batch_create", "agb_batch_destroy", "agb_batch_last_error",
             "agb_batch_size", "agb_batch_world", "agb_batch_tuning", "agb_batch_step",
             "agb_batch_graph_kernels", "agb_batch_stats"]
@@ -436,10 +441,59 @@ class World:
                                                      f[2].ctypes.data, None), "export_forces")
         return [a[:n] for a in f]
 
+    def state_hash(self, stream=None):
+        h = C.c_uint64()
+        self._check(self.lib.agb_world_state_hash(self.h, C.byref(h), _st(stream)), "state_hash")
+        return h.value
+
+    def snapshot(self, scenario_id=b"test", stream=None):
+        n = C.c_int64()
+        self._check(self.lib.agb_world_snapshot_save(self.h, scenario_id, None, 0, C.byref(n), _st(stream)),
+                    "snapshot size")
+        buf = np.zeros(n.value, np.uint8)
+        self._check(self.lib.agb_world_snapshot_save(self.h, scenario_id, buf.ctypes.data, n.value, C.byref(n),
+                                                     _st(stream)), "snapshot")
+        return buf.tobytes()
+
     def counters(self):
         out = np.zeros(4, dtype=np.int64)
         self._check(self.lib.agb_world_counters(self.h, out.ctypes.data, None), "counters")
         return out
+
+
+SNAPSHOT_MAGIC = 0x48505341
+FNV1A64_OFFSET = 1469598103934665603
+
+
+def fnv1a64(data, h=FNV1A64_OFFSET, lib=None):
+    """contracts/snapshot_v1.h fnv1a64 over a bytes-like object (engine implementation)."""
+    lib = lib or load()
+    buf = np.frombuffer(bytes(data), np.uint8)
+    return int(lib.agb_fnv1a64(buf.ctypes.data if buf.size else None, buf.size, h))
+
+
+def snapshot_load(base_desc, data, lib=None):
+    """agb_world_snapshot_load: a World restored from snapshot bytes."""
+    lib = lib or load()
+    buf = np.frombuffer(bytes(data), np.uint8)
+    h = C.c_void_p()
+    rc = lib.agb_world_snapshot_load(C.byref(base_desc), buf.ctypes.data, buf.size, C.byref(h))
+    if rc != OK:
+        raise AgbError("agb_world_snapshot_load failed: %s" % status_name(rc))
+    w = World.__new__(World)
+    w.lib, w.desc, w.h = lib, base_desc, h
+    return w
+
+
+def snapshot_status(base_desc, data, lib=None):
+    """Status code of agb_world_snapshot_load (the world, if any, is destroyed)."""
+    lib = lib or load()
+    buf = np.frombuffer(bytes(data), np.uint8)
+    h = C.c_void_p()
+    rc = lib.agb_world_snapshot_load(C.byref(base_desc), buf.ctypes.data, buf.size, C.byref(h))
+    if rc == OK:
+        lib.agb_world_destroy(h)
+    return rc
 
 
 class _ChamberView(World):

@@ -309,6 +309,11 @@ void world_advance_clock(agb_world* w, int32_t ticks) {
     w->tick += (uint64_t)ticks;
     w->sim_time += w->tp.dt * ticks;
 }
+void world_set_clock_state(agb_world* w, uint64_t tick, double sim_time) {
+    invalidate_graphs(w);
+    w->tick = tick;
+    w->sim_time = sim_time;
+}
 
 bool world_set_tiling(agb_world* w, int f, const FtcsPlan& p) {
     const GridDev& g = w->c.g[f];

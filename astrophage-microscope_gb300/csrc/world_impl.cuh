@@ -72,6 +72,8 @@ void world_set_parity(agb_world* w, uint32_t bits);
 // tick % compaction period: which compaction decision the next tick takes.
 uint64_t world_phase(const agb_world* w);
 void world_advance_clock(agb_world* w, int32_t ticks);
+// Set the tick counter and simulated time (snapshot restore); drops graphs.
+void world_set_clock_state(agb_world* w, uint64_t tick, double sim_time);
 // Switch field f's stencil tiling (rebuilds its tensor maps); false when the
 // field has no TMA path or the maps cannot be made.
 bool world_set_tiling(agb_world* w, int f, const FtcsPlan& p);

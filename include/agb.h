@@ -199,6 +199,38 @@ enum {
     AGB_STAGE_CLOCK = 8        /* ++tick; sim_time += dt, src/sim/step.cu:182-183 */
 };
 
+/* Snapshots (contracts/snapshot_v1.h:17-63): file = header, then the body the
+ * state hash covers: overrides, the 25 cell arrays (contract order, count
+ * elements each), predator arrays (none in this engine), T, CO2, N2 values.
+ * Little-endian; the layout below is the contract's, field for field. */
+#define AGB_SNAPSHOT_MAGIC 0x48505341u          /* 'ASPH' */
+#define AGB_SNAPSHOT_VERSION 1u
+#define AGB_FNV1A64_OFFSET 1469598103934665603ull
+
+typedef struct agb_snapshot_header {
+    uint32_t magic, version;
+    uint64_t seed, tick;
+    double sim_time_s;
+    int32_t cell_count, cell_capacity;
+    int32_t taumoeba_count, taumoeba_capacity;
+    int32_t n_temp, n_co2, n_n2;                /* grid nx (the reference's n of an n x n grid) */
+    int32_t _pad0;                              /* natural alignment of the double that follows */
+    double chamber_w, chamber_h, chamber_d;
+    double physics_rate, biology_rate;
+    uint64_t next_cell_id;
+    int32_t override_count;
+    uint8_t non_canon_run;
+    uint8_t _pad[3];
+    char scenario_id[64];
+    char build_describe[64];
+    uint64_t state_hash;                        /* FNV-1a 64 over the body */
+} agb_snapshot_header;
+
+typedef struct agb_param_override {
+    char key[48];
+    double value;
+} agb_param_override;
+
 /* Batched ensembles (no counterpart in the reference, which runs one World per
  * process): N independent chambers of uneven cell counts and grid sizes, each
  * a full world, advanced together by one CUDA graph launch per
@@ -314,6 +346,22 @@ agb_status agb_world_export_forces(agb_world* w, float* fx, float* fy, float* fz
 /* Device counters: {divisions_this_window, deaths_total, dead_slots_prev,
  * device error word}. Syncs. */
 agb_status agb_world_counters(agb_world* w, int64_t out[4], agb_stream s);
+
+/* fnv1a64 (contracts/snapshot_v1.h:57-61): h = (h ^ byte) * 1099511628211,
+ * starting from h (AGB_FNV1A64_OFFSET for a fresh hash). */
+uint64_t agb_fnv1a64(const void* data, uint64_t n, uint64_t h);
+/* snapshot_state_hash (src/sim/snapshot.cu:126-132): FNV-1a of the body. */
+agb_status agb_world_state_hash(agb_world* w, uint64_t* hash, agb_stream s);
+/* snapshot_to_bytes (src/sim/snapshot.cu:134-165). buf == NULL: only *size is
+ * set; a cap under *size returns AGB_CAPACITY_EXCEEDED and writes nothing. */
+agb_status agb_world_snapshot_save(agb_world* w, const char* scenario_id, void* buf, int64_t cap,
+                                   int64_t* size, agb_stream s);
+/* snapshot_from_bytes (src/sim/snapshot.cu:167-246): the motion configuration
+ * and grid layout come from *base (the snapshot does not carry them), the
+ * chamber, capacity, seed, clock rates and state from the snapshot. A corrupt
+ * body (hash mismatch), bad magic or a grid resolution that differs from the
+ * header fails as the reference does. */
+agb_status agb_world_snapshot_load(const agb_world_desc* base, const void* data, int64_t n, agb_world** out);
 
 /* Batches. agb_batch_create builds chamber i from descs[i], seeds it with
  * spawns[i] (may be NULL: no cells) and, with opts->autotune, first picks each

@@ -71,6 +71,7 @@
 #define AGB_FIELD_N_IRRAD 512
 #define AGB_MAX_CELLS 2000000
 #define AGB_DEFAULT_CELLS 25000
+#define AGB_DEFAULT_TAUMOEBA 256          /* predator store capacity of a world that sets none */
 #define AGB_N2_DIFFUSIVITY 2.0e-9            /* src/sim/step.cu:38 literal */
 
 /* Fixed-point scales (contracts/fields_v1.h:47-70; stats field scale src/sim/stats.cu:19). */

@@ -18,7 +18,8 @@ CXX="${CXX:-g++}"
 FLAGS="-std=c++20 -O2 -fPIC -ffp-contract=off -w -include $HERE/ref_emu/emu.h -I$HERE/ref_emu -I$REF/src -I$REF"
 SRCS="src/fields/diffuse.cu src/sim/cell_store.cu src/sim/hash.cu src/sim/integrator.cu
       src/sim/thermal.cu src/sim/emission.cu src/sim/taxis.cu src/sim/flash.cu
-      src/sim/predation.cu src/sim/lifecycle.cu src/sim/stats.cu src/sim/step.cu"
+      src/sim/predation.cu src/sim/lifecycle.cu src/sim/stats.cu src/sim/step.cu
+      src/sim/snapshot.cu"
 OBJS=""
 pids=""
 for s in $SRCS; do

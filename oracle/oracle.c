@@ -1331,3 +1331,71 @@ int orc_world_stats_accum(orc_world* w, uint64_t out[12]) {
     memcpy(out, w->accum, sizeof(w->accum));
     return 0;
 }
+
+/* ------------------------------------------------------------------------- */
+/* Snapshot (contracts/snapshot_v1.h:17-63; src/sim/snapshot.cu:100-165)      */
+/* ------------------------------------------------------------------------- */
+uint64_t orc_fnv1a64(const void* data, uint64_t n, uint64_t h) {
+    const unsigned char* p = (const unsigned char*)data;
+    for (uint64_t i = 0; i < n; ++i) { h ^= p[i]; h *= 1099511628211ull; }
+    return h;
+}
+
+/* snapshot_to_bytes: header + [overrides][25 cell arrays][no predators][T, CO2, N2].
+ * Returns the byte count; writes into out when cap suffices. */
+int64_t orc_world_snapshot(orc_world* w, const char* scenario_id, char* out, int64_t cap) {
+    const int stored[3] = {AGB_FIELD_TEMPERATURE, AGB_FIELD_CO2, AGB_FIELD_N2};
+    size_t sz[25]; void* p[25];
+    soa_sizes(sz); soa_ptrs(&w->c, p);
+    const int has_override = w->d.co2_mass_per_division != AGB_CO2_MASS_PER_DIVISION;
+    int64_t body = has_override ? (int64_t)sizeof(agb_param_override) : 0;
+    for (int k = 0; k < 25; ++k) body += (int64_t)sz[k] * w->count;
+    for (int k = 0; k < 3; ++k)
+        if (w->g[stored[k]].enabled) body += 4 * (int64_t)w->g[stored[k]].count;
+    const int64_t total = (int64_t)sizeof(agb_snapshot_header) + body;
+    if (!out || cap < total) return total;
+    char* q = out + sizeof(agb_snapshot_header);
+    if (has_override) {
+        agb_param_override ov;
+        memset(&ov, 0, sizeof(ov));
+        strncpy(ov.key, "CO2_MASS_PER_DIVISION", sizeof(ov.key) - 1);
+        ov.value = w->d.co2_mass_per_division;
+        memcpy(q, &ov, sizeof(ov));
+        q += sizeof(ov);
+    }
+    for (int k = 0; k < 25; ++k) {
+        const size_t b = sz[k] * (size_t)w->count;
+        if (b) memcpy(q, *(void**)p[k], b);
+        q += b;
+    }
+    for (int k = 0; k < 3; ++k) {
+        const grid* g = &w->g[stored[k]];
+        if (!g->enabled) continue;
+        memcpy(q, g->value, 4 * (size_t)g->count);
+        q += 4 * (size_t)g->count;
+    }
+    agb_snapshot_header h;
+    memset(&h, 0, sizeof(h));
+    h.magic = AGB_SNAPSHOT_MAGIC;
+    h.version = AGB_SNAPSHOT_VERSION;
+    h.seed = w->d.seed;
+    h.tick = w->tick;
+    h.sim_time_s = w->sim_time;
+    h.cell_count = w->count;
+    h.cell_capacity = w->capacity;
+    h.taumoeba_capacity = AGB_DEFAULT_TAUMOEBA;   /* the reference world's default store, empty */
+    h.n_temp = w->g[AGB_FIELD_TEMPERATURE].enabled ? w->g[AGB_FIELD_TEMPERATURE].nx : 0;
+    h.n_co2 = w->g[AGB_FIELD_CO2].enabled ? w->g[AGB_FIELD_CO2].nx : 0;
+    h.n_n2 = w->g[AGB_FIELD_N2].enabled ? w->g[AGB_FIELD_N2].nx : 0;
+    h.chamber_w = w->d.chamber_w; h.chamber_h = w->d.chamber_h; h.chamber_d = w->d.chamber_d;
+    h.physics_rate = w->physics_rate;
+    h.biology_rate = w->biology_rate;
+    h.next_cell_id = w->next_id;
+    h.override_count = has_override;
+    h.non_canon_run = (uint8_t)has_override;
+    if (scenario_id) strncpy(h.scenario_id, scenario_id, sizeof(h.scenario_id) - 1);
+    strncpy(h.build_describe, "dev", sizeof(h.build_describe) - 1);
+    h.state_hash = orc_fnv1a64(out + sizeof(h), (uint64_t)body, AGB_FNV1A64_OFFSET);
+    memcpy(out, &h, sizeof(h));
+    return total;
+}

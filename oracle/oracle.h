@@ -54,6 +54,10 @@ void orc_pcg32_seed_draws(uint64_t initstate, uint64_t initseq, int32_t n, uint3
 uint64_t orc_cell_rng_init(uint64_t seed, uint64_t id);
 uint64_t orc_pcg_split(uint64_t parent_state, uint64_t daughter_id);
 
+/* Snapshot bytes (header + body) and the FNV-1a hash of contracts/snapshot_v1.h. */
+uint64_t orc_fnv1a64(const void* data, uint64_t n, uint64_t h);
+int64_t orc_world_snapshot(orc_world* w, const char* scenario_id, char* out, int64_t cap);
+
 #ifdef __cplusplus
 }
 #endif

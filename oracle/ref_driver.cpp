@@ -12,7 +12,10 @@
 #include "contracts/cell_store_v1.h"
 #include "contracts/telemetry_v1.h"
 #include "fields/grid.cuh"
+#include "sim/snapshot.h"
 #include "sim/world.cuh"
+
+#include <vector>
 
 namespace emu {
 uint3 g_block_idx{0, 0, 0}, g_thread_idx{0, 0, 0};
@@ -266,6 +269,22 @@ void ref_stats_accum(void* h, uint64_t* out /* 12 */) {
 void ref_counters(void* h, int64_t* out) {
     World* w = static_cast<World*>(h);
     out[0] = w->divisions_this_window; out[1] = w->deaths_total; out[2] = w->dead_slots_prev;
+}
+
+// snapshot_to_bytes (src/sim/snapshot.cu:134-165): returns the byte count and
+// copies the snapshot into out when cap is large enough; -1 on failure.
+int64_t ref_snapshot(void* h, const char* scenario_id, char* out, int64_t cap) {
+    std::vector<char> bytes;
+    if (snapshot_to_bytes(*static_cast<World*>(h), scenario_id, bytes)) return -1;
+    if (out && cap >= (int64_t)bytes.size()) std::memcpy(out, bytes.data(), bytes.size());
+    return (int64_t)bytes.size();
+}
+
+// snapshot_state_hash (src/sim/snapshot.cu:126-132).
+uint64_t ref_state_hash(void* h) {
+    uint64_t x = 0;
+    if (snapshot_state_hash(*static_cast<World*>(h), x)) return 0;
+    return x;
 }
 
 }  // extern "C"

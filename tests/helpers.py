@@ -65,6 +65,8 @@ def oracle_lib():
             "orc_pcg32_seed_draws": (None, [U64, U64, I32, P]),
             "orc_cell_rng_init": (U64, [U64, U64]),
             "orc_pcg_split": (U64, [U64, U64]),
+            "orc_fnv1a64": (U64, [P, U64, U64]),
+            "orc_world_snapshot": (C.c_int64, [P, C.c_char_p, P, C.c_int64]),
         }
         for name, (res, args) in sigs.items():
             fn = getattr(lib, name)
@@ -180,6 +182,12 @@ class OracleWorld:
         self.lib.orc_world_counters(self.h, out.ctypes.data)
         return out
 
+    def snapshot(self, scenario_id=b"test"):
+        n = self.lib.orc_world_snapshot(self.h, scenario_id, None, 0)
+        buf = np.zeros(n, np.uint8)
+        self.lib.orc_world_snapshot(self.h, scenario_id, buf.ctypes.data, n)
+        return buf.tobytes()
+
 
 # ---------------------------------------------------------------------------
 # The reference itself on the CPU (only where oracle/_ref was built from the
@@ -230,6 +238,10 @@ class RefWorld:
         lib.ref_grid_diffuse.argtypes = [C.c_void_p, C.c_int, C.c_double]
         lib.ref_grid_substeps.argtypes = [C.c_void_p, C.c_int, C.c_double]
         lib.ref_cells_io.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p), C.c_int32, C.c_uint64]
+        lib.ref_snapshot.restype = C.c_int64
+        lib.ref_snapshot.argtypes = [C.c_void_p, C.c_char_p, C.c_void_p, C.c_int64]
+        lib.ref_state_hash.restype = C.c_uint64
+        lib.ref_state_hash.argtypes = [C.c_void_p]
         self.lib = lib
         self.desc = desc
         g = desc.grid
@@ -335,3 +347,12 @@ class RefWorld:
         out = np.zeros(3, np.int64)
         self.lib.ref_counters(self.h, out.ctypes.data_as(C.c_void_p))
         return out
+
+    def snapshot(self, scenario_id=b"test"):
+        n = self.lib.ref_snapshot(self.h, scenario_id, None, 0)
+        buf = np.zeros(n, np.uint8)
+        assert self.lib.ref_snapshot(self.h, scenario_id, buf.ctypes.data, n) == n
+        return buf.tobytes()
+
+    def state_hash(self):
+        return int(self.lib.ref_state_hash(self.h))

@@ -110,6 +110,14 @@ def cells_digest(w):
     return out
 
 
+def snapshot_record(data):
+    """Snapshot file (contracts/snapshot_v1.h): its state hash, size and a digest
+    of every byte, header included."""
+    state_hash = int(np.frombuffer(data[248:256], np.uint64)[0])
+    return {"state_hash": "%016x" % state_hash, "bytes": len(data),
+            "digest": hashlib.sha256(data).hexdigest()[:24]}
+
+
 def setup(world, sc):
     """Spawn, then the scenario's mutation and field overrides, identically on any backend."""
     world.spawn(sc["spawn"])
@@ -127,6 +135,7 @@ def trace(world, sc, full_after=None):
     rec = {"spawn": cells_digest(world), "steps": []}
     setup(world, sc)
     rec["initial"] = cells_digest(world)
+    rec["snapshot_initial"] = snapshot_record(world.snapshot(b"golden"))
     full = None
     for t in range(sc["ticks"]):
         for stage, name in STAGES:
@@ -144,6 +153,7 @@ def trace(world, sc, full_after=None):
             full = {"cell_" + k: v for k, v in cells.as_dict().items()}
             for f in range(4):
                 full["field_%d" % f] = world.export_field(f)
+    rec["snapshot_final"] = snapshot_record(world.snapshot(b"golden"))
     st = world.stats()
     rec["stats"] = st if isinstance(st, dict) else st.as_dict()
     rec["accum"] = [int(v) for v in world.stats_accum()]

@@ -37,6 +37,8 @@ def test_oracle_matches_reference_digests(name):
             assert got["hash"] == want["hash"], where + ": hash"
         if "forces" in want:
             assert got["forces"] == want["forces"], where + ": forces"
+    assert rec["snapshot_initial"] == gold["snapshot_initial"], "snapshot_to_bytes (src/sim/snapshot.cu:134-165)"
+    assert rec["snapshot_final"] == gold["snapshot_final"], "snapshot after the last tick"
     assert rec["accum"] == gold["accum"], "fixed-point StatsAccum"
     assert rec["counters"] == gold["counters"]
     for k, v in gold["stats"].items():
@@ -82,3 +84,18 @@ def test_oracle_matches_live_reference_longer_run():
         assert np.array_equal(cr[name], co[name]), name
     for f in range(4):
         assert np.array_equal(r.export_field(f), o.export_field(f))
+
+
+def test_fnv1a64_engine_matches_restatement():
+    """contracts/snapshot_v1.h fnv1a64: engine (host code, no GPU), oracle and a
+    plain Python loop agree; the empty input leaves the offset basis."""
+    lib = H.oracle_lib()
+    rng = np.random.default_rng(3)
+    for n in (0, 1, 7, 4096):
+        data = rng.integers(0, 256, n, dtype=np.uint8).tobytes()
+        h = 1469598103934665603
+        for b in data:
+            h = ((h ^ b) * 1099511628211) & 0xFFFFFFFFFFFFFFFF
+        buf = np.frombuffer(data, np.uint8)
+        assert agb.fnv1a64(data) == h
+        assert lib.orc_fnv1a64(buf.ctypes.data if n else None, n, 1469598103934665603) == h
