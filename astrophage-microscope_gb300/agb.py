@@ -282,6 +282,10 @@ def load(path=LIB_PATH):
         "agb_world_state_hash": (I32, [P, C.POINTER(C.c_uint64), P]),
         "agb_world_snapshot_save": (I32, [P, C.c_char_p, P, C.c_int64, C.POINTER(C.c_int64), P]),
         "agb_world_snapshot_load": (I32, [C.POINTER(WorldDesc), P, C.c_int64, C.POINTER(P)]),
+        "agb_nn_conv3": (I32, [P, P, P, I32, I32, I32, I32, I32, I32, P, P, I32, P, P]),
+        "agb_nn_wgrad_scratch_bytes": (C.c_int64, [I32, I32, I32, I32, I32]),
+        "agb_nn_wgrad": (I32, [P, P, I32, I32, I32, I32, I32, P, P, P, C.c_int64, P, P]),
+        "agb_nn_flip_weights": (I32, [P, P, I32, I32, P]),
         "agb_batch_opts_default": (None, [C.POINTER(BatchOpts)]),
         "agb_batch_create": (I32, [P, P, I32, C.POINTER(BatchOpts), C.POINTER(P)]),
         "agb_batch_destroy": (None, [P]),
@@ -312,6 +316,7 @@ def exported_symbols():
             "agb_world_set_light", "agb_world_export_hash", "agb_world_export_forces",
             "agb_world_counters", "agb_grid_diffuse_noalloc",
             "agb_fnv1a64", "agb_world_state_hash", "agb_world_snapshot_save", "agb_world_snapshot_load",
+            "agb_nn_conv3", "agb_nn_wgrad_scratch_bytes", "agb_nn_wgrad", "agb_nn_flip_weights",
             "agb_batch_opts_default", "agb_batch_create", "agb_batch_destroy", "agb_batch_last_error",
             "agb_batch_size", "agb_batch_world", "agb_batch_tuning", "agb_batch_step",
             "agb_batch_graph_kernels", "agb_batch_stats"]

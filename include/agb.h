@@ -363,6 +363,24 @@ agb_status agb_world_snapshot_save(agb_world* w, const char* scenario_id, void* 
  * header fails as the reference does. */
 agb_status agb_world_snapshot_load(const agb_world_desc* base, const void* data, int64_t n, agb_world** out);
 
+/* Learned-surrogate layer primitives on caller-owned device buffers (no
+ * counterpart in the reference). Activations are channels-last BF16
+ * [D][H][W][C], weights [27][cout][cin] BF16 with tap (dz+1)*9+(dy+1)*3+(dx+1).
+ * agb_nn_conv3: 3x3x3 "same" convolution on the tensor cores, out =
+ * act(conv(x, w) + bias), zeroed where mask <= 0 when mask is given; BF16 or
+ * FP32 output. agb_nn_wgrad: dw[27][cout][cin] (and db[cout] when given) of
+ * that convolution from its input x and output gradient dy, FP32, using
+ * agb_nn_wgrad_scratch_bytes of scratch. agb_nn_flip_weights: the weights of
+ * the input-gradient convolution, wf[26-t][ci][co] = w[t][co][ci]. err is a
+ * device word set nonzero when a bounded wait inside a kernel expired. */
+agb_status agb_nn_conv3(const void* x, const void* w, const float* bias, int32_t D, int32_t H, int32_t W,
+                        int32_t cin, int32_t cout, int32_t act, const void* mask, void* out, int32_t out_f32,
+                        uint32_t* err, agb_stream s);
+int64_t agb_nn_wgrad_scratch_bytes(int32_t D, int32_t H, int32_t W, int32_t cin, int32_t cout);
+agb_status agb_nn_wgrad(const void* x, const void* dy, int32_t D, int32_t H, int32_t W, int32_t cin, int32_t cout,
+                        float* dw, float* db, void* scratch, int64_t scratch_bytes, uint32_t* err, agb_stream s);
+agb_status agb_nn_flip_weights(const void* w, void* wf, int32_t cout, int32_t cin, agb_stream s);
+
 /* Batches. agb_batch_create builds chamber i from descs[i], seeds it with
  * spawns[i] (may be NULL: no cells) and, with opts->autotune, first picks each
  * size class's hash cell size and stencil tilings by timing probe chambers.
