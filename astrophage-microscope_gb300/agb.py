@@ -44,6 +44,8 @@ IRRADIANCE_NOMINAL_DIFFUSIVITY = 1.0e-9
 DEPOSIT_SCALE = (1.0e9, 1.0e15, 1.0e15, 1.0e18)
 CO2_MASS_PER_DIVISION = 2.0999999999999999e-14
 HASH_CELL_FACTOR = 2.2000000000000002
+AIR_CONVECTION_H = 10.0
+WATER_CONDUCTIVITY = 0.59799999999999998
 
 
 class GridDesc(C.Structure):
@@ -286,6 +288,19 @@ def load(path=LIB_PATH):
         "agb_nn_wgrad_scratch_bytes": (C.c_int64, [I32, I32, I32, I32, I32]),
         "agb_nn_wgrad": (I32, [P, P, I32, I32, I32, I32, I32, P, P, P, C.c_int64, P, P]),
         "agb_nn_flip_weights": (I32, [P, P, I32, I32, P]),
+        "agb_surrogate_desc_default": (None, [C.POINTER(SurrogateDesc)]),
+        "agb_surrogate_create": (I32, [C.POINTER(SurrogateDesc), C.POINTER(P)]),
+        "agb_surrogate_destroy": (None, [P]),
+        "agb_surrogate_train": (I32, [P, I32, P, P]),
+        "agb_surrogate_advance": (I32, [P, P, P, P, P, I32, C.POINTER(SurrogateReport), P]),
+        "agb_surrogate_reference": (I32, [P, P, P, P, P, P]),
+        "agb_surrogate_window": (I32, [P, C.c_uint64, P, P, P, P, P]),
+        "agb_surrogate_gradients": (I32, [P, P, P, P, P, P, P, P, C.c_int64, C.POINTER(C.c_float), P]),
+        "agb_surrogate_params": (I32, [P, P, C.c_int64, C.POINTER(C.c_int64)]),
+        "agb_surrogate_set_params": (I32, [P, P, C.c_int64]),
+        "agb_surrogate_get_report": (I32, [P, C.POINTER(SurrogateReport)]),
+        "agb_surrogate_error_word": (I32, [P, C.POINTER(C.c_uint32)]),
+        "agb_world_attach_surrogate": (I32, [P, P, P]),
         "agb_batch_opts_default": (None, [C.POINTER(BatchOpts)]),
         "agb_batch_create": (I32, [P, P, I32, C.POINTER(BatchOpts), C.POINTER(P)]),
         "agb_batch_destroy": (None, [P]),
@@ -317,6 +332,10 @@ def exported_symbols():
             "agb_world_counters", "agb_grid_diffuse_noalloc",
             "agb_fnv1a64", "agb_world_state_hash", "agb_world_snapshot_save", "agb_world_snapshot_load",
             "agb_nn_conv3", "agb_nn_wgrad_scratch_bytes", "agb_nn_wgrad", "agb_nn_flip_weights",
+            "agb_surrogate_desc_default", "agb_surrogate_create", "agb_surrogate_destroy", "agb_surrogate_train",
+            "agb_surrogate_advance", "agb_surrogate_reference", "agb_surrogate_window", "agb_surrogate_gradients",
+            "agb_surrogate_params", "agb_surrogate_set_params", "agb_surrogate_get_report",
+            "agb_surrogate_error_word", "agb_world_attach_surrogate",
             "agb_batch_opts_default", "agb_batch_create", "agb_batch_destroy", "agb_batch_last_error",
             "agb_batch_size", "agb_batch_world", "agb_batch_tuning", "agb_batch_step",
             "agb_batch_graph_kernels", "agb_batch_stats"]
@@ -446,6 +465,12 @@ class World:
                                                      f[2].ctypes.data, None), "export_forces")
         return [a[:n] for a in f]
 
+    def attach_surrogate(self, sg, stream=None):
+        """Drive the temperature and CO2 grids by a Surrogate (None detaches)."""
+        self._check(self.lib.agb_world_attach_surrogate(self.h, sg.h if sg is not None else None, _st(stream)),
+                    "attach_surrogate")
+        self._sg = sg
+
     def state_hash(self, stream=None):
         h = C.c_uint64()
         self._check(self.lib.agb_world_state_hash(self.h, C.byref(h), _st(stream)), "state_hash")
@@ -499,6 +524,123 @@ def snapshot_status(base_desc, data, lib=None):
     if rc == OK:
         lib.agb_world_destroy(h)
     return rc
+
+
+class SurrogateDesc(C.Structure):
+    _fields_ = [("abi_version", C.c_uint32), ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
+                ("extent", C.c_double), ("dt", C.c_double), ("steps", C.c_int32), ("judge_every", C.c_int32),
+                ("tol_temperature", C.c_double), ("tol_energy", C.c_double), ("diffusivity", C.c_double * 2),
+                ("init", C.c_double * 2), ("bc", (C.c_int32 * 6) * 2), ("face", (C.c_double * 6) * 2),
+                ("seed", C.c_uint64), ("learning_rate", C.c_float),
+                ("train_temperature_amplitude", C.c_double), ("train_source_density", C.c_double),
+                ("train_heat_per_step", C.c_double), ("train_uptake_per_step", C.c_double)]
+
+    def as_dict(self):
+        return {"init": [self.init[0], self.init[1]], "steps": self.steps, "nx": self.nx, "extent": self.extent,
+                "dt": self.dt, "diffusivity": [self.diffusivity[0], self.diffusivity[1]],
+                "bc": [list(self.bc[0]), list(self.bc[1])], "face": [list(self.face[0]), list(self.face[1])],
+                "train_temperature_amplitude": self.train_temperature_amplitude,
+                "train_heat_per_step": self.train_heat_per_step,
+                "train_uptake_per_step": self.train_uptake_per_step}
+
+
+class SurrogateReport(C.Structure):
+    _fields_ = [("calls", C.c_int64), ("judged", C.c_int64), ("fallbacks", C.c_int64),
+                ("last_err_temperature", C.c_double), ("last_err_co2", C.c_double),
+                ("last_energy_drift", C.c_double), ("last_used_surrogate", C.c_int32), ("last_loss", C.c_float)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def surrogate_desc(lib=None, **kw):
+    lib = lib or load()
+    d = SurrogateDesc()
+    lib.agb_surrogate_desc_default(C.byref(d))
+    for k, v in kw.items():
+        setattr(d, k, v)
+    return d
+
+
+class Surrogate:
+    """The learned field surrogate; field arguments are device pointers (ints)."""
+
+    def __init__(self, desc=None, lib=None):
+        self.lib = lib or load()
+        self.desc = desc if desc is not None else surrogate_desc(self.lib)
+        h = C.c_void_p()
+        rc = self.lib.agb_surrogate_create(C.byref(self.desc), C.byref(h))
+        if rc != OK:
+            raise AgbError("agb_surrogate_create failed: %s" % status_name(rc))
+        self.h = h
+
+    def _ck(self, rc, what):
+        if rc != OK:
+            raise AgbError("%s failed: %s" % (what, status_name(rc)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.agb_surrogate_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _p(x):
+        return None if x is None else C.c_void_p(int(x))
+
+    def train(self, windows, stream=None):
+        losses = np.zeros(max(windows, 1), np.float32)
+        self._ck(self.lib.agb_surrogate_train(self.h, windows, losses.ctypes.data, _st(stream)), "train")
+        return losses[:windows]
+
+    def advance(self, T, Cf, qT, qC, judge=0, stream=None):
+        rep = SurrogateReport()
+        self._ck(self.lib.agb_surrogate_advance(self.h, self._p(T), self._p(Cf), self._p(qT), self._p(qC), judge,
+                                                C.byref(rep), _st(stream)), "advance")
+        return rep
+
+    def reference(self, T, Cf, qT, qC, stream=None):
+        self._ck(self.lib.agb_surrogate_reference(self.h, self._p(T), self._p(Cf), self._p(qT), self._p(qC),
+                                                  _st(stream)), "reference")
+
+    def window(self, index, T, Cf, qT, qC, stream=None):
+        self._ck(self.lib.agb_surrogate_window(self.h, index, self._p(T), self._p(Cf), self._p(qT), self._p(qC),
+                                               _st(stream)), "window")
+
+    def params(self):
+        n = C.c_int64()
+        self._ck(self.lib.agb_surrogate_params(self.h, None, 0, C.byref(n)), "params")
+        out = np.zeros(n.value, np.float32)
+        self._ck(self.lib.agb_surrogate_params(self.h, out.ctypes.data, n.value, C.byref(n)), "params")
+        return out
+
+    def set_params(self, flat):
+        a = np.ascontiguousarray(flat, np.float32)
+        self._ck(self.lib.agb_surrogate_set_params(self.h, a.ctypes.data, a.size), "set_params")
+
+    def gradients(self, T0, C0, qT, qC, T1, C1, stream=None):
+        n = self.params().size
+        g = np.zeros(n, np.float32)
+        loss = C.c_float()
+        self._ck(self.lib.agb_surrogate_gradients(self.h, self._p(T0), self._p(C0), self._p(qT), self._p(qC),
+                                                  self._p(T1), self._p(C1), g.ctypes.data, n, C.byref(loss),
+                                                  _st(stream)), "gradients")
+        return float(loss.value), g
+
+    def report(self):
+        rep = SurrogateReport()
+        self._ck(self.lib.agb_surrogate_get_report(self.h, C.byref(rep)), "report")
+        return rep
+
+    def error_word(self):
+        w = C.c_uint32()
+        self._ck(self.lib.agb_surrogate_error_word(self.h, C.byref(w)), "error_word")
+        return w.value
 
 
 class _ChamberView(World):

@@ -9,7 +9,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libagb.so")
-SOURCES = ["k_grid.cu", "k_hash.cu", "k_cells.cu", "k_life.cu", "world.cu", "batch.cu", "snapshot.cu", "conv_tc.cu", "nn_ops.cu", "nn_abi.cu", "noalloc.cu"]
+SOURCES = ["k_grid.cu", "k_hash.cu", "k_cells.cu", "k_life.cu", "world.cu", "batch.cu", "snapshot.cu", "conv_tc.cu", "nn_ops.cu", "nn_abi.cu", "surrogate.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
          "--threads", "2"]

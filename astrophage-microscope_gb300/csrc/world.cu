@@ -248,7 +248,10 @@ void stage_clock(agb_world* w) {
 // diffused CO2). Motion samples CO2 and N2 from the buffers as they were
 // before this tick's diffusion, exactly as in src/sim/step.cu:164-171, while
 // the diffusion writes the other ping-pong buffer.
+void tick_surrogate(agb_world* w, cudaStream_t s);
+
 void tick_once(agb_world* w, cudaStream_t s) {
+    if (w->sg) { tick_surrogate(w, s); return; }
     cudaStream_t s1 = w->side[0], s2 = w->side[1];
     cudaEventRecord(w->ev[0], s);
     cudaStreamWaitEvent(s1, w->ev[0], 0);
@@ -270,6 +273,32 @@ void tick_once(agb_world* w, cudaStream_t s) {
     cudaStreamWaitEvent(s, w->ev[2], 0);
     stage_lifecycle(w, s);
     stage_clock(w);
+}
+
+// A tick while the learned surrogate drives the temperature and CO2 grids:
+// the stages run as in tick_once, except that the cells' heat exchange
+// accumulates in the temperature deposit grid instead of being flushed, and
+// neither grid is diffused. Every sg_steps ticks the accumulated heat becomes
+// a constant per-step source and the surrogate advances both grids by the
+// whole window (its judge runs the plain FTCS window every judge_every-th
+// call and takes over when the network is off by more than its tolerance).
+// CO2 uptake is still folded into the grid every tick, so the window has no
+// CO2 source. Cells see the grids as they stood at the start of the window.
+void tick_surrogate(agb_world* w, cudaStream_t s) {
+    refresh_grid_ptrs(w);
+    stage_hash(w, s);
+    if (w->d.thermal_enabled && w->c.g[AGB_FIELD_TEMPERATURE].enabled)
+        for (int32_t k = 0; k < w->tp.t_substeps; ++k) launch_thermal(w->S, w->c, w->tp, w->blocks, s);
+    if (w->d.emission_enabled) stage_emission(w, s);
+    launch_motion(w->S, w->c, w->tp, w->fx, w->fy, w->fz, w->blocks, s);
+    stage_lifecycle(w, s);
+    stage_clock(w);
+    if (w->tick % (uint64_t)w->sg_steps == 0) {
+        const GridDev& T = w->c.g[AGB_FIELD_TEMPERATURE];
+        surrogate_source_from_deposit(w->gdep[AGB_FIELD_TEMPERATURE], w->sg_q, T.count, 1.0 / T.scale, w->sg_steps, s);
+        agb_surrogate_advance(w->sg, field_value(w, AGB_FIELD_TEMPERATURE), field_value(w, AGB_FIELD_CO2), w->sg_q,
+                              nullptr, 0, nullptr, s);
+    }
 }
 
 uint32_t parity_bits(const agb_world* w) {
@@ -706,6 +735,7 @@ agb_status agb_world_step(agb_world* w, int32_t ticks, agb_stream s) {
 
 agb_status agb_world_step_graph(agb_world* w, int32_t ticks, agb_stream s) {
     if (!w || ticks <= 0) return AGB_INVALID_ARGUMENT;
+    if (w->sg) return agb_world_step(w, ticks, s);    // the judge reads results on the host: no capture
     const uint64_t P = w->d.compaction_period > 0 ? (uint64_t)w->d.compaction_period : 1;
     const uint32_t par = parity_bits(w);
     const uint64_t phase = w->tick % P;
@@ -750,6 +780,40 @@ agb_status agb_world_step_graph(agb_world* w, int32_t ticks, agb_stream s) {
     w->graph_kernels_total += e.kernels;
     // Capture advanced the host-side tick state; the graph has not run yet.
     AGB_CUDA(w, cudaGraphLaunch(e.exec, s));
+    return AGB_OK;
+}
+
+agb_status agb_world_attach_surrogate(agb_world* w, agb_surrogate* sg, agb_stream stream) {
+    if (!w) return AGB_INVALID_ARGUMENT;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const GridDev& T = w->c.g[AGB_FIELD_TEMPERATURE];
+    const GridDev& C = w->c.g[AGB_FIELD_CO2];
+    if (!sg) {
+        if (w->sg && w->sg_q) {
+            // Detaching mid-window: fold the heat accumulated so far into the grid.
+            surrogate_source_from_deposit(w->gdep[AGB_FIELD_TEMPERATURE], w->sg_q, T.count, 1.0 / T.scale, 1, s);
+            surrogate_add(field_value(w, AGB_FIELD_TEMPERATURE), w->sg_q, T.count, s);
+        }
+        w->sg = nullptr;
+        invalidate_graphs(w);
+        AGB_CUDA(w, cudaGetLastError());
+        return AGB_OK;
+    }
+    int32_t dims[3], steps = 0, bc[2][6];
+    float coeff[2];
+    surrogate_info(sg, dims, &steps, coeff, bc);
+    if (!T.enabled || !C.enabled || T.nx != dims[0] || T.ny != dims[1] || T.nz != dims[2] || C.nx != dims[0] ||
+        C.ny != dims[1] || C.nz != dims[2])
+        return fail(w, AGB_INVALID_ARGUMENT, "surrogate grid differs from the world's temperature/CO2 grids");
+    if (w->tp.t_substeps != 1 || w->tp.c_substeps != 1 || coeff[0] != w->tp.t_coeff || coeff[1] != w->tp.c_coeff)
+        return fail(w, AGB_INVALID_ARGUMENT, "surrogate FTCS step differs from the world's (one pass per tick)");
+    for (int k = 0; k < 6; ++k)
+        if (bc[0][k] != w->gbc[AGB_FIELD_TEMPERATURE][k] || bc[1][k] != w->gbc[AGB_FIELD_CO2][k])
+            return fail(w, AGB_INVALID_ARGUMENT, "surrogate boundary conditions differ from the world's");
+    if (!w->sg_q && dalloc(w, &w->sg_q, 4 * (size_t)T.count) != cudaSuccess) return AGB_OUT_OF_MEMORY;
+    w->sg = sg;
+    w->sg_steps = steps;
+    invalidate_graphs(w);
     return AGB_OK;
 }
 

@@ -57,6 +57,9 @@ struct agb_world {
     cudaStream_t own_stream = nullptr;   // capture stream when the caller passes the default stream
     int64_t graph_kernels_total = 0;     // kernel nodes launched by graph replays so far
     uint64_t version = 0;                // bumped whenever captured graphs go stale
+    agb_surrogate* sg = nullptr;         // learned field surrogate driving T and CO2, if attached
+    int32_t sg_steps = 0;
+    float* sg_q = nullptr;               // per-step heat source of the current window (K)
     std::string err;
     std::vector<void*> allocs;
 };
@@ -80,5 +83,13 @@ bool world_set_tiling(agb_world* w, int f, const FtcsPlan& p);
 // Milliseconds per FTCS pass of field f, from a captured graph of 2 * passes
 // passes (best of three timed replays). Changes the field's contents.
 float world_time_passes(agb_world* w, int f, int passes, cudaStream_t s);
+
+// The surrogate's grid, FTCS steps per call and per-step coefficients (T, CO2).
+bool surrogate_info(const agb_surrogate* sg, int32_t dims[3], int32_t* steps, float coeff[2], int32_t bc[2][6]);
+// q[i] = deposit[i] / scale / steps (FP32), deposit[i] = 0, for every voxel.
+void surrogate_source_from_deposit(unsigned long long* dep, float* q, int64_t n, double inv_scale, int32_t steps,
+                                   cudaStream_t s);
+// x[i] += q[i].
+void surrogate_add(float* x, const float* q, int64_t n, cudaStream_t s);
 
 }  // namespace agb

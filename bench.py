@@ -180,6 +180,101 @@ def run_batch(args, stream, l2_flush):
     return out
 
 
+def surrogate_for(desc, seed=1):
+    """A surrogate descriptor matching a world's 3-D temperature and CO2 grids
+    (one FTCS pass per tick), trained on windows with heat sources and
+    temperature excursions of the size the 25,000-cell run produces."""
+    gT, gC = desc.grid[agb.FIELD_T], desc.grid[agb.FIELD_CO2]
+    sd = agb.surrogate_desc(nx=gT.nx, ny=gT.ny, nz=gT.nz, extent=desc.chamber_w, dt=agb.DT_PHYSICS * desc.physics_rate,
+                            seed=seed)
+    sd.diffusivity[0], sd.diffusivity[1] = gT.diffusivity, gC.diffusivity
+    sd.init[0], sd.init[1] = gT.init, gC.init
+    for k in range(6):
+        sd.bc[0][k], sd.face[0][k] = gT.bc[k], gT.face_value[k]
+        sd.bc[1][k], sd.face[1][k] = gC.bc[k], gC.face_value[k]
+    sd.train_temperature_amplitude = 20.0
+    sd.train_heat_per_step = 2.0
+    sd.train_source_density = 0.01
+    sd.train_uptake_per_step = 1.0e-5
+    return sd
+
+
+def run_surrogate(args, stream):
+    """The learned field surrogate on the 25,000-cell setup: train it on the
+    GPU, time one network window against the FTCS window it replaces, then
+    drive the world's temperature and CO2 grids with it (FTCS judge every 8th
+    window, fallback past 0.01 K or 1e-6 energy drift)."""
+    import torch
+    desc, sp, _info = workload("slab25k", seed=1)
+    sd = surrogate_for(desc)
+    sg = agb.Surrogate(sd)
+    sh = stream.cuda_stream
+    t0 = time.perf_counter()
+    losses = sg.train(args.surrogate_windows, stream=sh)
+    train_s = time.perf_counter() - t0
+    shape = (sd.nz, sd.ny, sd.nx)
+    T, Cf, qT, qC = [torch.zeros(shape, dtype=torch.float32, device="cuda") for _ in range(4)]
+
+    def timed(fn, reps=10):
+        with torch.cuda.stream(stream):
+            for _ in range(2):
+                fn()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    sg.window(10 ** 7, T.data_ptr(), Cf.data_ptr(), qT.data_ptr(), qC.data_ptr(), stream=sh)
+    net_ms = timed(lambda: sg.advance(T.data_ptr(), Cf.data_ptr(), qT.data_ptr(), qC.data_ptr(), judge=-1, stream=sh))
+    ftcs_ms = timed(lambda: sg.reference(T.data_ptr(), Cf.data_ptr(), qT.data_ptr(), qC.data_ptr(), stream=sh))
+    # Held-out accuracy against the FTCS window, and the do-nothing baseline.
+    errs, pers = [], []
+    for idx in range(3):
+        sg.window(10 ** 8 + idx, T.data_ptr(), Cf.data_ptr(), qT.data_ptr(), qC.data_ptr(), stream=sh)
+        rT, rC = T.clone(), Cf.clone()
+        sg.reference(rT.data_ptr(), rC.data_ptr(), qT.data_ptr(), qC.data_ptr(), stream=sh)
+        pers.append(float((rT - T).abs().max()))
+        sg.advance(T.data_ptr(), Cf.data_ptr(), qT.data_ptr(), qC.data_ptr(), judge=-1, stream=sh)
+        errs.append(float((T - rT).abs().max()))
+    # The world, driven by the surrogate.
+    w = agb.World(desc)
+    w.spawn(sp)
+    steps = sd.steps
+    w.attach_surrogate(sg, stream=sh)
+    with torch.cuda.stream(stream):
+        w.step(steps, stream=sh)                          # one warm-up window
+        torch.cuda.synchronize()
+        r0 = sg.report()
+        n0 = w.count(stream=sh)
+        ticks = steps * args.surrogate_windows_run
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        w.step(ticks, stream=sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        n1 = w.count(stream=sh)
+    el = e0.elapsed_time(e1) / 1e3
+    r1 = sg.report()
+    vox = 2 * sd.nx * sd.ny * sd.nz
+    out = {"train_windows": args.surrogate_windows, "train_s": train_s,
+           "loss_first_last": [float(losses[:20].mean()), float(losses[-20:].mean())] if len(losses) >= 20 else None,
+           "network_ms_per_window": net_ms, "ftcs_ms_per_window": ftcs_ms,
+           "held_out_max_err_K": max(errs), "persistence_max_err_K": max(pers),
+           "world": {"workload": "slab25k", "ticks": ticks, "ms_per_step": el * 1e3 / ticks,
+                     "cell_steps_per_s": 0.5 * (n0 + n1) * ticks / el, "voxel_steps_per_s": vox * ticks / el,
+                     "windows": int(r1.calls - r0.calls), "judged": int(r1.judged - r0.judged),
+                     "fallbacks": int(r1.fallbacks - r0.fallbacks),
+                     "last_judged_err_K": r1.last_err_temperature, "last_energy_drift": r1.last_energy_drift},
+           "note": "voxel-steps counted as the T and CO2 FTCS passes the windows stand for"}
+    w.attach_surrogate(None, stream=sh)
+    w.close()
+    sg.close()
+    return out
+
+
 def substeps(desc, f):
     """FTCS passes per tick of field f (src/fields/grid.cuh:51-53; 1/6 bound in 3-D)."""
     g = desc.grid[f]
@@ -397,6 +492,9 @@ def main():
                     help="timed steps of the batched ensemble reported beside the plain step (0: skip)")
     ap.add_argument("--batch-chambers", type=int, default=64)
     ap.add_argument("--batch-lanes", type=int, default=0)
+    ap.add_argument("--surrogate-windows", type=int, default=1500,
+                    help="training windows of the learned field surrogate (0: skip the surrogate leg)")
+    ap.add_argument("--surrogate-windows-run", type=int, default=16)
     ap.add_argument("--profile-stencil", type=int, default=0,
                     help="only run a few FTCS passes on an N^3 temperature grid (small case for ncu)")
     args = ap.parse_args()
@@ -516,6 +614,11 @@ def main():
         world.close()
         batched = run_batch(args, stream, l2_flush)
 
+    surrogate = None
+    if rank == 0 and args.surrogate_windows > 0:
+        surrogate = run_surrogate(args, stream)
+        surrogate["vs_plain_voxel_steps"] = surrogate["world"]["voxel_steps_per_s"] / (vox_steps / total_s)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -548,6 +651,7 @@ def main():
             "gpu_launches": launches,
             "clocks": clocks,
             "batched": batched,
+            "surrogate": surrogate,
         }
         print(json.dumps(line))
     if dist is not None:

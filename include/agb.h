@@ -231,6 +231,47 @@ typedef struct agb_param_override {
     double value;
 } agb_param_override;
 
+/* The learned field surrogate (no counterpart in the reference): advances the
+ * temperature and CO2 grids `steps` FTCS steps per call with a 3-level 3-D
+ * convolutional encoder-decoder (32/64/128 channels, 3x3x3 kernels, BF16
+ * weights and activations, FP32 accumulation, tensor cores), trained on the
+ * GPU on seeded FTCS windows. Every judge_every-th call also runs the plain
+ * FTCS window and falls back to its result when the largest temperature
+ * error exceeds tol_temperature or the relative drift of the summed
+ * temperature exceeds tol_energy. The window operator on both fields is
+ * `steps` times X <- FTCS(X + q) with constant per-step sources q. */
+typedef struct agb_surrogate agb_surrogate;
+
+typedef struct agb_surrogate_desc {
+    uint32_t abi_version;
+    int32_t nx, ny, nz;               /* nx 128 or 256; ny a multiple of 16; nz a multiple of 4 */
+    double extent;                    /* chamber width (m): dx = extent / nx, cubic voxels */
+    double dt;                        /* seconds per FTCS step */
+    int32_t steps;                    /* FTCS steps per call (16) */
+    int32_t judge_every;              /* judge every k-th call (8) */
+    double tol_temperature;           /* K (0.01) */
+    double tol_energy;                /* relative (1e-6) */
+    double diffusivity[2];            /* temperature, CO2 (m^2/s) */
+    double init[2];                   /* reference values the inputs are normalised about */
+    int32_t bc[2][6];                 /* boundary conditions per field and face */
+    double face[2][6];
+    uint64_t seed;
+    float learning_rate;
+    double train_temperature_amplitude;   /* K: blob amplitude of the training windows */
+    double train_source_density;          /* fraction of voxels holding a source */
+    double train_heat_per_step;           /* K per step: largest heating source */
+    double train_uptake_per_step;         /* kg/m^3 per step: largest CO2 uptake */
+} agb_surrogate_desc;
+
+typedef struct agb_surrogate_report {
+    int64_t calls, judged, fallbacks;
+    double last_err_temperature;      /* K, last judged call */
+    double last_err_co2;
+    double last_energy_drift;
+    int32_t last_used_surrogate;      /* 0: the last call's output is the judge's FTCS result */
+    float last_loss;                  /* last training loss (mean squared normalised error) */
+} agb_surrogate_report;
+
 /* Batched ensembles (no counterpart in the reference, which runs one World per
  * process): N independent chambers of uneven cell counts and grid sizes, each
  * a full world, advanced together by one CUDA graph launch per
@@ -380,6 +421,42 @@ int64_t agb_nn_wgrad_scratch_bytes(int32_t D, int32_t H, int32_t W, int32_t cin,
 agb_status agb_nn_wgrad(const void* x, const void* dy, int32_t D, int32_t H, int32_t W, int32_t cin, int32_t cout,
                         float* dw, float* db, void* scratch, int64_t scratch_bytes, uint32_t* err, agb_stream s);
 agb_status agb_nn_flip_weights(const void* w, void* wf, int32_t cout, int32_t cin, agb_stream s);
+
+/* Surrogate lifetime, training and use. Field pointers are device buffers of
+ * nx*ny*nz floats. agb_surrogate_train trains on `windows` seeded windows
+ * (losses[k] per window when given). agb_surrogate_advance updates T and C in
+ * place by one window; judge: 1 forces the judge, -1 skips it, 0 follows
+ * judge_every. agb_surrogate_reference is the plain FTCS window (the method
+ * without the network); agb_surrogate_window writes training window `index`.
+ * agb_surrogate_gradients runs one forward and backward pass against given
+ * targets without updating (for gradient checks); parameters and gradients
+ * are flat FP32 in layer order, each layer's [27][cout][cin] weights then its
+ * cout biases. */
+void agb_surrogate_desc_default(agb_surrogate_desc* d);
+agb_status agb_surrogate_create(const agb_surrogate_desc* d, agb_surrogate** out);
+void agb_surrogate_destroy(agb_surrogate* s);
+agb_status agb_surrogate_train(agb_surrogate* s, int32_t windows, float* losses, agb_stream st);
+agb_status agb_surrogate_advance(agb_surrogate* s, float* T, float* C, const float* qT, const float* qC,
+                                 int32_t judge, agb_surrogate_report* rep, agb_stream st);
+agb_status agb_surrogate_reference(agb_surrogate* s, float* T, float* C, const float* qT, const float* qC,
+                                   agb_stream st);
+agb_status agb_surrogate_window(agb_surrogate* s, uint64_t index, float* T, float* C, float* qT, float* qC,
+                                agb_stream st);
+agb_status agb_surrogate_gradients(agb_surrogate* s, const float* T0, const float* C0, const float* qT,
+                                   const float* qC, const float* T1, const float* C1, float* grads, int64_t cap,
+                                   float* loss, agb_stream st);
+agb_status agb_surrogate_params(agb_surrogate* s, float* out, int64_t cap, int64_t* count);
+agb_status agb_surrogate_set_params(agb_surrogate* s, const float* in, int64_t count);
+agb_status agb_surrogate_get_report(agb_surrogate* s, agb_surrogate_report* rep);
+agb_status agb_surrogate_error_word(agb_surrogate* s, uint32_t* word);
+/* Let the surrogate drive a world's temperature and CO2 grids (NULL detaches).
+ * The grids, the one-pass-per-tick FTCS coefficients and the boundary
+ * conditions must be the surrogate's. While attached, the cells' heat
+ * exchange accumulates over each window of `steps` ticks and becomes the
+ * window's per-step source; neither grid is diffused tick by tick; at the end
+ * of each window the surrogate (and, every judge_every-th window, its FTCS
+ * judge) advances both grids. Steps run eagerly (no graph capture). */
+agb_status agb_world_attach_surrogate(agb_world* w, agb_surrogate* sg, agb_stream s);
 
 /* Batches. agb_batch_create builds chamber i from descs[i], seeds it with
  * spawns[i] (may be NULL: no cells) and, with opts->autotune, first picks each
