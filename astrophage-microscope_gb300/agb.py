@@ -27,7 +27,7 @@ GRAVITY_Y, GRAVITY_Z = 0, 1
 DIVIDE_CO2_QUOTA, DIVIDE_ENERGY = 0, 1
 PLACE_UNIFORM, PLACE_GAUSSIAN, PLACE_GRID, PLACE_DISC, PLACE_SLAB_X, PLACE_CLUSTERS = range(6)
 DIST_CONSTANT, DIST_UNIFORM, DIST_NORMAL, DIST_LOGNORMAL = range(4)
-STAGE_HASH, STAGE_THERMAL, STAGE_EMISSION, STAGE_MOTION = 0, 1, 2, 4
+STAGE_HASH, STAGE_THERMAL, STAGE_EMISSION, STAGE_TAXIS, STAGE_MOTION = 0, 1, 2, 3, 4
 STAGE_SLOW_FIELDS, STAGE_LIFECYCLE, STAGE_COMPACT, STAGE_CLOCK = 5, 6, 7, 8
 FLAG_OCCUPIED, FLAG_ALIVE, FLAG_AWAKE, FLAG_STUCK = 1, 2, 4, 8
 
@@ -44,6 +44,7 @@ IRRADIANCE_NOMINAL_DIFFUSIVITY = 1.0e-9
 DEPOSIT_SCALE = (1.0e9, 1.0e15, 1.0e15, 1.0e18)
 CO2_MASS_PER_DIVISION = 2.0999999999999999e-14
 HASH_CELL_FACTOR = 2.2000000000000002
+PETROVA_MAX_POWER = 0.050000000000000003
 AIR_CONVECTION_H = 10.0
 WATER_CONDUCTIVITY = 0.59799999999999998
 
@@ -71,7 +72,7 @@ class WorldDesc(C.Structure):
                 ("store_disposition", C.c_int32), ("ambient_temp", C.c_double),
                 ("grid", GridDesc * 4), ("hash_cell_size", C.c_double), ("light", Light),
                 ("physics_rate", C.c_double), ("biology_rate", C.c_double),
-                ("co2_mass_per_division", C.c_double),
+                ("co2_mass_per_division", C.c_double), ("max_emit_power", C.c_double),
                 ("division_predicate", C.c_int32), ("division_energy", C.c_double),
                 ("compaction_period", C.c_int32), ("trap_slot", C.c_int32),
                 ("trap_x", C.c_double), ("trap_y", C.c_double), ("trap_stiffness", C.c_double)]
@@ -171,6 +172,7 @@ def default_desc(capacity=25000, seed=20260802, co2_init=0.0):
     d.light = Light(1.0, 0.0, 0.0, 0.0, 0.0, 0)
     d.physics_rate, d.biology_rate = 1.0, 1.0
     d.co2_mass_per_division = CO2_MASS_PER_DIVISION
+    d.max_emit_power = PETROVA_MAX_POWER
     d.division_predicate, d.division_energy = DIVIDE_CO2_QUOTA, 0.0
     d.compaction_period = 1
     d.trap_slot, d.trap_x, d.trap_y, d.trap_stiffness = -1, 0.0, 0.0, 0.0

@@ -539,6 +539,104 @@ __global__ void __launch_bounds__(256) integrate_kernel(DevState* S, Ctx c, Tick
     }
 }
 
+// ---------------------------------------------------------------------------
+// Taxis (src/sim/taxis.cu:13-77 with src/sim/taxis.cuh:31-143). Per cell, in
+// slot order. FP64 as the reference, every product and sum explicitly rounded
+// (no contraction), so integer outcomes (state, tumble, RNG draws) and the
+// stored floats follow the reference; log/sin/cos are CUDA's (within an ulp
+// or two of the host's).
+// ---------------------------------------------------------------------------
+struct V3 { double x, y, z; };
+__device__ __forceinline__ double dot3(V3 a, V3 b) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y)), __dmul_rn(a.z, b.z));
+}
+__device__ __forceinline__ V3 scale3(V3 a, double s) { return V3{__dmul_rn(a.x, s), __dmul_rn(a.y, s), __dmul_rn(a.z, s)}; }
+__device__ __forceinline__ V3 add3(V3 a, V3 b) { return V3{__dadd_rn(a.x, b.x), __dadd_rn(a.y, b.y), __dadd_rn(a.z, b.z)}; }
+__device__ __forceinline__ V3 cross3(V3 a, V3 b) {
+    return V3{__dsub_rn(__dmul_rn(a.y, b.z), __dmul_rn(a.z, b.y)), __dsub_rn(__dmul_rn(a.z, b.x), __dmul_rn(a.x, b.z)),
+              __dsub_rn(__dmul_rn(a.x, b.y), __dmul_rn(a.y, b.x))};
+}
+__device__ __forceinline__ V3 normalize3(V3 a) {                 // vec.cuh:34-37
+    const double l = __dsqrt_rn(dot3(a, a));
+    return l > 0.0 ? scale3(a, __drcp_rn(l)) : V3{0.0, 0.0, 1.0};
+}
+__device__ V3 taxis_tumble(V3 heading, Pcg& rng) {               // taxis.cuh:104-118
+    double theta = __dmul_rn(-AGB_TAXIS_TUMBLE_ANGLE_MEAN, log(__dsub_rn(1.0, uniform01d(rng))));
+    if (theta > AGB_PI) theta = AGB_PI;
+    const double azimuth = __dmul_rn(AGB_TWO_PI, uniform01d(rng));
+    const V3 h = normalize3(heading);
+    const double ax = fabs(h.x), ay = fabs(h.y), az = fabs(h.z);  // any_perpendicular, taxis.cuh:86-92
+    const V3 axis = (ax <= ay && ax <= az) ? V3{1.0, 0.0, 0.0} : (ay <= az) ? V3{0.0, 1.0, 0.0} : V3{0.0, 0.0, 1.0};
+    const V3 u = normalize3(cross3(h, axis));
+    const V3 w = cross3(h, u);
+    double sa, ca, st, ct;
+    sincos(azimuth, &sa, &ca);
+    sincos(theta, &st, &ct);
+    const V3 perp = add3(scale3(u, ca), scale3(w, sa));           // rotate_by, taxis.cuh:95-100
+    return normalize3(add3(scale3(h, ct), scale3(perp, st)));
+}
+
+__global__ void __launch_bounds__(256) taxis_kernel(DevState* S, Ctx c, TickParams p) {
+    const SoA v = S->cur;
+    const int32_t n = S->count;
+    AGB_FOR_CELLS(i, n) {
+        const uint32_t f = v.flags[i];
+        if (!(f & AGB_FLAG_OCCUPIED) || !(f & AGB_FLAG_ALIVE)) continue;
+        if (!(f & AGB_FLAG_AWAKE)) {                               // dormant: inert, no emission
+            v.emit_power[i] = 0.0f;
+            continue;
+        }
+        const double irr = (double)v.irradiance[i];
+        const double co2 = (double)v.co2_local[i];
+        const double energy = v.energy[i];
+        const double charge = __ddiv_rn(energy, AGB_CELL_ENERGY_MAX);
+        const bool dark = irr < AGB_TAXIS_DARK_THRESHOLD, co2_here = co2 > 0.0;   // taxis.cuh:56-62
+        int state = 0;                                             // 0 idle, 1 feed, 2 breed
+        if (!(dark && !co2_here)) {
+            if (!dark && charge < AGB_TAXIS_SEEK_FEED_BELOW) state = 1;
+            else if (charge > AGB_TAXIS_SEEK_BREED_ABOVE && co2_here) state = 2;
+        }
+        if (state == 0) {                                          // no draws on the idle path
+            v.emit_power[i] = 0.0f;
+            v.run_timer[i] = 0.0f;
+            v.taxis_memory[i] = 0.0f;
+            continue;
+        }
+        const double signal = state == 1 ? irr : co2;
+        const double mem = (double)v.taxis_memory[i];
+        const double delta = __dsub_rn(signal, mem);
+        v.taxis_memory[i] = (float)__dadd_rn(mem, __dmul_rn(p.taxis_alpha, __dsub_rn(signal, mem)));
+        V3 heading{-(double)v.dir_x[i], -(double)v.dir_y[i], -(double)v.dir_z[i]};
+        double run = __dadd_rn((double)v.run_timer[i], p.dt);
+        if (delta <= 0.0 || run >= AGB_TAXIS_RUN_MAX) {            // taxis_should_tumble
+            Pcg rng{v.rng_state[i], cell_stream_inc(v.id[i])};
+            heading = taxis_tumble(heading, rng);
+            v.rng_state[i] = rng.state;
+            run = 0.0;
+        }
+        v.run_timer[i] = (float)run;
+        const V3 nh = normalize3(heading);                         // taxis_emit_dir = -normalize(heading)
+        v.dir_x[i] = (float)(-nh.x);
+        v.dir_y[i] = (float)(-nh.y);
+        v.dir_z[i] = (float)(-nh.z);
+        double pw = 0.0;                                           // taxis_emit_power, taxis.cuh:136-141
+        if (energy > 0.0) {
+            const double avail = p.dt > 0.0 ? __ddiv_rn(energy, p.dt) : 0.0;
+            pw = p.max_emit_power < avail ? p.max_emit_power : avail;
+        }
+        v.emit_power[i] = (float)pw;
+        v.energy[i] = __dsub_rn(energy, __dmul_rn(pw, p.dt));
+    }
+}
+
+}  // namespace
+
+void launch_taxis(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, cudaStream_t s) {
+    taxis_kernel<<<blocks, 256, 0, s>>>(S, c, p);
+}
+
+namespace {
+
 }  // namespace
 
 void launch_thermal(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, cudaStream_t s) {

@@ -28,17 +28,21 @@ static_assert(sizeof(agb_param_override) == 56, "override record is 56 bytes");
 
 constexpr size_t kElem[25] = {8, 4, 1, 8, 8, 8, 8, 8, 8, 8, 4, 4, 4, 4, 4, 8, 8, 4, 8, 4, 4, 4, 4, 4, 4};
 
-// The overrides this engine carries (src/sim/snapshot.cu:75-80): only the
-// division quota exists here; the predator-flash keys are read and ignored.
+// The overrides this engine carries, in the reference's order
+// (src/sim/snapshot.cu:75-80): the emission cap and the division quota; the
+// flash power has no counterpart here (no flash stage) and is read and ignored.
 std::vector<agb_param_override> overrides(const agb_world* w) {
     std::vector<agb_param_override> out;
-    if (w->d.co2_mass_per_division != AGB_CO2_MASS_PER_DIVISION) {
+    auto add = [&](const char* key, double value) {
         agb_param_override ov;
         std::memset(&ov, 0, sizeof(ov));           // the key's padding is hashed
-        std::strncpy(ov.key, "CO2_MASS_PER_DIVISION", sizeof(ov.key) - 1);
-        ov.value = w->d.co2_mass_per_division;
+        std::strncpy(ov.key, key, sizeof(ov.key) - 1);
+        ov.value = value;
         out.push_back(ov);
-    }
+    };
+    const double pmax = w->d.max_emit_power > 0.0 ? w->d.max_emit_power : AGB_PETROVA_MAX_POWER;
+    if (pmax != AGB_PETROVA_MAX_POWER) add("PETROVA_MAX_POWER", pmax);
+    if (w->d.co2_mass_per_division != AGB_CO2_MASS_PER_DIVISION) add("CO2_MASS_PER_DIVISION", w->d.co2_mass_per_division);
     return out;
 }
 
@@ -198,6 +202,7 @@ agb_status agb_world_snapshot_load(const agb_world_desc* base, const void* data,
         std::memcpy(&ov, cur, sizeof(ov));
         cur += sizeof(ov);
         if (std::strncmp(ov.key, "CO2_MASS_PER_DIVISION", sizeof(ov.key)) == 0) d.co2_mass_per_division = ov.value;
+        if (std::strncmp(ov.key, "PETROVA_MAX_POWER", sizeof(ov.key)) == 0) d.max_emit_power = ov.value;
     }
     agb_world* w = nullptr;
     agb_status rc = agb_world_create(&d, &w);

@@ -118,6 +118,8 @@ agb_status compute_tick_params(agb_world* w) {
     p.k_contact64 = AGB_CONTACT_STIFFNESS / w->physics_rate;
     p.k_trap = (float)(w->d.trap_stiffness / w->physics_rate);
     p.dt_bio = p.dt * w->biology_rate;
+    p.taxis_alpha = 1.0 - std::exp(-p.dt / AGB_TAXIS_MEMORY_TIME);     // taxis.cuh:38-41
+    p.max_emit_power = w->d.max_emit_power > 0.0 ? w->d.max_emit_power : AGB_PETROVA_MAX_POWER;
     const GridDev& T = c.g[AGB_FIELD_TEMPERATURE];
     if (T.enabled) {
         const double D = w->d.grid[AGB_FIELD_TEMPERATURE].diffusivity;
@@ -265,6 +267,7 @@ void tick_once(agb_world* w, cudaStream_t s) {
     stage_hash(w, s);
     cudaStreamWaitEvent(s, w->ev[1], 0);
     if (w->d.emission_enabled) stage_emission(w, s);
+    if (w->d.taxis_enabled) launch_taxis(w->S, w->c, w->tp, w->blocks, s);   // step.cu:161-162
     {
         Ctx c = w->c;
         for (int f : {AGB_FIELD_CO2, AGB_FIELD_N2}) c.g[f] = pre.g[f];
@@ -290,6 +293,7 @@ void tick_surrogate(agb_world* w, cudaStream_t s) {
     if (w->d.thermal_enabled && w->c.g[AGB_FIELD_TEMPERATURE].enabled)
         for (int32_t k = 0; k < w->tp.t_substeps; ++k) launch_thermal(w->S, w->c, w->tp, w->blocks, s);
     if (w->d.emission_enabled) stage_emission(w, s);
+    if (w->d.taxis_enabled) launch_taxis(w->S, w->c, w->tp, w->blocks, s);
     launch_motion(w->S, w->c, w->tp, w->fx, w->fy, w->fz, w->blocks, s);
     stage_lifecycle(w, s);
     stage_clock(w);
@@ -426,6 +430,7 @@ void agb_world_desc_default(agb_world_desc* d) {
     d->physics_rate = 1.0;
     d->biology_rate = 1.0;
     d->co2_mass_per_division = AGB_CO2_MASS_PER_DIVISION;
+    d->max_emit_power = AGB_PETROVA_MAX_POWER;
     d->division_predicate = AGB_DIVIDE_CO2_QUOTA;
     d->compaction_period = 1;
     d->trap_slot = -1;
@@ -469,7 +474,6 @@ agb_status agb_world_create(const agb_world_desc* d, agb_world** out) {
     if (!(d->chamber_w > 0 && d->chamber_h > 0 && d->chamber_d > 0) || d->chamber_w > 0.4 ||
         d->chamber_h > 0.4 || d->chamber_d > 0.4)
         return AGB_INVALID_ARGUMENT;
-    if (d->taxis_enabled) return AGB_UNSUPPORTED;
     agb_world* w = new (std::nothrow) agb_world();
     if (!w) return AGB_OUT_OF_MEMORY;
     // AGB_PLAIN_STENCIL=1 selects the plain 3-D stencil (for A/B checks of the TMA one).
@@ -829,6 +833,7 @@ agb_status agb_world_stage(agb_world* w, int32_t stage, agb_stream s) {
         case AGB_STAGE_HASH: stage_hash(w, s); break;
         case AGB_STAGE_THERMAL: stage_thermal(w, s); break;
         case AGB_STAGE_EMISSION: stage_emission(w, s); break;
+        case AGB_STAGE_TAXIS: launch_taxis(w->S, w->c, w->tp, w->blocks, s); break;
         case AGB_STAGE_MOTION: stage_motion(w, s); break;
         case AGB_STAGE_SLOW_FIELDS: stage_slow_fields(w, s); break;
         case AGB_STAGE_LIFECYCLE: stage_lifecycle(w, s); break;

@@ -56,6 +56,9 @@ struct TickParams {
     float t_cap_relax;          // capacity * (1 - exp(-G dt_sub / C)) as float
     float t_relax;              // (1 - exp(-G dt_sub / C)) as float
     double t_cap;
+    // taxis
+    double taxis_alpha;         // 1 - exp(-dt / TAXIS_MEMORY_TIME) (taxis.cuh:38-41)
+    double max_emit_power;      // [W]
     // slow fields
     int32_t c_substeps, n_substeps;
     float c_coeff, n_coeff;

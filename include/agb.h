@@ -113,6 +113,7 @@ typedef struct agb_world_desc {
     agb_light light;
     double physics_rate, biology_rate;
     double co2_mass_per_division;             /* [kg] World override, canon by default */
+    double max_emit_power;                    /* [W] World::petrova_max_power, canon by default */
     /* Extensions; the defaults reproduce the reference. */
     int32_t division_predicate;               /* AGB_DIVIDE_* */
     double division_energy;                   /* [J] threshold for AGB_DIVIDE_ENERGY */
@@ -192,6 +193,7 @@ enum {
     AGB_STAGE_HASH = 0,        /* hash_build, src/sim/hash.cu:106-133 */
     AGB_STAGE_THERMAL = 1,     /* thermal_step, src/sim/thermal.cu:75-103 */
     AGB_STAGE_EMISSION = 2,    /* emission_step, src/sim/emission.cu:119-177 */
+    AGB_STAGE_TAXIS = 3,       /* taxis_step, src/sim/taxis.cu:80-85 */
     AGB_STAGE_MOTION = 4,      /* motion_step, src/sim/integrator.cu:154-177 */
     AGB_STAGE_SLOW_FIELDS = 5, /* CO2/N2 flush + diffuse, src/sim/step.cu:168-171 */
     AGB_STAGE_LIFECYCLE = 6,   /* lifecycle_step, src/sim/lifecycle.cu:208-294 */

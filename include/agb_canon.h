@@ -71,7 +71,15 @@
 #define AGB_FIELD_N_IRRAD 512
 #define AGB_MAX_CELLS 2000000
 #define AGB_DEFAULT_CELLS 25000
-#define AGB_DEFAULT_TAUMOEBA 256          /* predator store capacity of a world that sets none */
+#define AGB_DEFAULT_TAUMOEBA 256
+/* Run-and-tumble taxis (src/core/canon_generated.h:31,82-86,120). */
+#define AGB_PETROVA_MAX_POWER 0.050000000000000003
+#define AGB_TAXIS_MEMORY_TIME 0.10000000000000001
+#define AGB_TAXIS_DARK_THRESHOLD 0.001
+#define AGB_TAXIS_SEEK_FEED_BELOW 0.94999999999999996
+#define AGB_TAXIS_SEEK_BREED_ABOVE 0.97999999999999998
+#define AGB_TAXIS_TUMBLE_ANGLE_MEAN 1.1868238913561442
+#define AGB_TAXIS_RUN_MAX 0.40000000000000002          /* predator store capacity of a world that sets none */
 #define AGB_N2_DIFFUSIVITY 2.0e-9            /* src/sim/step.cu:38 literal */
 
 /* Fixed-point scales (contracts/fields_v1.h:47-70; stats field scale src/sim/stats.cu:19). */

@@ -1208,6 +1208,80 @@ static void lifecycle_step(orc_world* w, double dt) {    /* lifecycle_step, life
 }
 
 /* ------------------------------------------------------------------------- */
+/* Taxis: src/sim/taxis.cu:13-85, src/sim/taxis.cuh:31-143                   */
+/* ------------------------------------------------------------------------- */
+static vec3 vadd(vec3 a, vec3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+static vec3 vcross(vec3 a, vec3 b) {                      /* vec.cuh:39-41 */
+    return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+static vec3 any_perpendicular(vec3 v) {                   /* taxis.cuh:86-92 */
+    const double ax = fabs(v.x), ay = fabs(v.y), az = fabs(v.z);
+    const vec3 axis = (ax <= ay && ax <= az) ? v3(1.0, 0.0, 0.0) : (ay <= az) ? v3(0.0, 1.0, 0.0) : v3(0.0, 0.0, 1.0);
+    return vnormalize(vcross(v, axis));
+}
+static vec3 rotate_by(vec3 h, double theta, double azimuth) {   /* taxis.cuh:95-100 */
+    const vec3 u = any_perpendicular(h);
+    const vec3 w = vcross(h, u);
+    const vec3 perp = vadd(vscale(u, cos(azimuth)), vscale(w, sin(azimuth)));
+    return vnormalize(vadd(vscale(h, cos(theta)), vscale(perp, sin(theta))));
+}
+static vec3 taxis_tumble(vec3 heading, pcg32* rng) {      /* taxis.cuh:109-118 */
+    double theta = -AGB_TAXIS_TUMBLE_ANGLE_MEAN * log(1.0 - uniform01d(rng));
+    if (theta > AGB_PI) theta = AGB_PI;
+    const double azimuth = AGB_TWO_PI * uniform01d(rng);
+    return rotate_by(vnormalize(heading), theta, azimuth);
+}
+
+static void taxis_step(orc_world* w, double dt) {
+    const double max_power = w->d.max_emit_power > 0.0 ? w->d.max_emit_power : AGB_PETROVA_MAX_POWER;
+    soa* v = &w->c;
+#pragma omp parallel for schedule(static)
+    for (int32_t i = 0; i < w->count; ++i) {
+        const uint32_t f = v->flags[i];
+        if (!(f & AGB_FLAG_OCCUPIED) || !(f & AGB_FLAG_ALIVE)) continue;
+        if (!(f & AGB_FLAG_AWAKE)) { v->emit_power[i] = 0.0f; continue; }
+        const double irr = (double)v->irradiance[i];
+        const double co2 = (double)v->co2_local[i];
+        const double charge = v->energy[i] / AGB_CELL_ENERGY_MAX;
+        const int dark = irr < AGB_TAXIS_DARK_THRESHOLD, co2_here = co2 > 0.0;   /* taxis.cuh:56-62 */
+        int state = 0;
+        if (dark && !co2_here) state = 0;
+        else if (!dark && charge < AGB_TAXIS_SEEK_FEED_BELOW) state = 1;
+        else if (charge > AGB_TAXIS_SEEK_BREED_ABOVE && co2_here) state = 2;
+        if (state == 0) {
+            v->emit_power[i] = 0.0f;
+            v->run_timer[i] = 0.0f;
+            v->taxis_memory[i] = 0.0f;
+            continue;
+        }
+        const double signal = state == 1 ? irr : co2;
+        const double delta = signal - (double)v->taxis_memory[i];
+        const double alpha = 1.0 - exp(-dt / AGB_TAXIS_MEMORY_TIME);       /* taxis.cuh:38-41 */
+        v->taxis_memory[i] = (float)((double)v->taxis_memory[i] + alpha * (signal - (double)v->taxis_memory[i]));
+        vec3 heading = v3(-(double)v->dir_x[i], -(double)v->dir_y[i], -(double)v->dir_z[i]);
+        double run = (double)v->run_timer[i] + dt;
+        if (delta <= 0.0 || run >= AGB_TAXIS_RUN_MAX) {
+            pcg32 rng = cell_rng(v->rng_state[i], v->id[i]);
+            heading = taxis_tumble(heading, &rng);
+            v->rng_state[i] = rng.state;
+            run = 0.0;
+        }
+        v->run_timer[i] = (float)run;
+        const vec3 axis = vscale(vnormalize(heading), -1.0);           /* taxis_emit_dir */
+        v->dir_x[i] = (float)axis.x;
+        v->dir_y[i] = (float)axis.y;
+        v->dir_z[i] = (float)axis.z;
+        double p = 0.0;                                                 /* taxis.cuh:136-141 */
+        if (v->energy[i] > 0.0) {
+            const double avail = dt > 0.0 ? v->energy[i] / dt : 0.0;
+            p = max_power < avail ? max_power : avail;
+        }
+        v->emit_power[i] = (float)p;
+        v->energy[i] -= p * dt;
+    }
+}
+
+/* ------------------------------------------------------------------------- */
 /* Tick: world_step, src/sim/step.cu:109-184                                  */
 /* ------------------------------------------------------------------------- */
 static int slow_fields(orc_world* w, double dt) {         /* step.cu:168-171 */
@@ -1224,6 +1298,7 @@ int orc_world_stage(orc_world* w, int32_t stage) {
         case AGB_STAGE_HASH: return hash_build(w);
         case AGB_STAGE_THERMAL: return thermal_step(w, dt);
         case AGB_STAGE_EMISSION: emission_step(w, dt); return 0;
+        case AGB_STAGE_TAXIS: taxis_step(w, dt); return 0;
         case AGB_STAGE_MOTION: motion_step(w, dt); return 0;
         case AGB_STAGE_SLOW_FIELDS: return slow_fields(w, dt);
         case AGB_STAGE_LIFECYCLE: lifecycle_step(w, dt); return 0;
@@ -1234,13 +1309,13 @@ int orc_world_stage(orc_world* w, int32_t stage) {
 }
 
 int orc_world_step(orc_world* w, int32_t ticks) {
-    if (w->d.taxis_enabled) return AGB_UNSUPPORTED;
     for (int32_t t = 0; t < ticks; ++t) {
         const double dt = AGB_DT_PHYSICS * w->physics_rate;
         int rc = hash_build(w);
         if (!rc && w->d.thermal_enabled) rc = thermal_step(w, dt);
         if (rc) return rc;
         if (w->d.emission_enabled) emission_step(w, dt);
+        if (w->d.taxis_enabled) taxis_step(w, dt);                       /* step.cu:161-162 */
         motion_step(w, dt);
         rc = slow_fields(w, dt);
         if (rc) return rc;
@@ -1347,19 +1422,23 @@ int64_t orc_world_snapshot(orc_world* w, const char* scenario_id, char* out, int
     const int stored[3] = {AGB_FIELD_TEMPERATURE, AGB_FIELD_CO2, AGB_FIELD_N2};
     size_t sz[25]; void* p[25];
     soa_sizes(sz); soa_ptrs(&w->c, p);
-    const int has_override = w->d.co2_mass_per_division != AGB_CO2_MASS_PER_DIVISION;
-    int64_t body = has_override ? (int64_t)sizeof(agb_param_override) : 0;
+    const double pmax = w->d.max_emit_power > 0.0 ? w->d.max_emit_power : AGB_PETROVA_MAX_POWER;
+    const int ov_power = pmax != AGB_PETROVA_MAX_POWER;                    /* snapshot.cu:75-80 order */
+    const int ov_quota = w->d.co2_mass_per_division != AGB_CO2_MASS_PER_DIVISION;
+    const int has_override = ov_power + ov_quota;
+    int64_t body = (int64_t)has_override * (int64_t)sizeof(agb_param_override);
     for (int k = 0; k < 25; ++k) body += (int64_t)sz[k] * w->count;
     for (int k = 0; k < 3; ++k)
         if (w->g[stored[k]].enabled) body += 4 * (int64_t)w->g[stored[k]].count;
     const int64_t total = (int64_t)sizeof(agb_snapshot_header) + body;
     if (!out || cap < total) return total;
     char* q = out + sizeof(agb_snapshot_header);
-    if (has_override) {
+    for (int o = 0; o < 2; ++o) {
+        if (!(o == 0 ? ov_power : ov_quota)) continue;
         agb_param_override ov;
         memset(&ov, 0, sizeof(ov));
-        strncpy(ov.key, "CO2_MASS_PER_DIVISION", sizeof(ov.key) - 1);
-        ov.value = w->d.co2_mass_per_division;
+        strncpy(ov.key, o == 0 ? "PETROVA_MAX_POWER" : "CO2_MASS_PER_DIVISION", sizeof(ov.key) - 1);
+        ov.value = o == 0 ? pmax : w->d.co2_mass_per_division;
         memcpy(q, &ov, sizeof(ov));
         q += sizeof(ov);
     }
@@ -1392,7 +1471,7 @@ int64_t orc_world_snapshot(orc_world* w, const char* scenario_id, char* out, int
     h.biology_rate = w->biology_rate;
     h.next_cell_id = w->next_id;
     h.override_count = has_override;
-    h.non_canon_run = (uint8_t)has_override;
+    h.non_canon_run = (uint8_t)(has_override > 0);
     if (scenario_id) strncpy(h.scenario_id, scenario_id, sizeof(h.scenario_id) - 1);
     strncpy(h.build_describe, "dev", sizeof(h.build_describe) - 1);
     h.state_hash = orc_fnv1a64(out + sizeof(h), (uint64_t)body, AGB_FNV1A64_OFFSET);

@@ -17,6 +17,15 @@ STAGES = [(agb.STAGE_HASH, "hash"), (agb.STAGE_THERMAL, "thermal"), (agb.STAGE_E
           (agb.STAGE_LIFECYCLE, "lifecycle"), (agb.STAGE_CLOCK, "clock")]
 
 
+def stages_for(desc):
+    """world_step's stage order for this world: taxis (stage 3) runs between
+    emission and motion only when the world enables it (src/sim/step.cu:161-162)."""
+    out = list(STAGES)
+    if desc.taxis_enabled:
+        out.insert(3, (agb.STAGE_TAXIS, "taxis"))
+    return out
+
+
 def slab_desc(n_t=64, n_c=64, n_n=32, n_i=64, cap=3000, co2=1.0, bio=1e5, bc_t=agb.BC_ROBIN,
               light=(1.0, 0.0, 1e4, 0.0), compaction=0, seed=20260802):
     """The reference's default world (4 mm x 4 mm x 60 um slab) with smaller grids."""
@@ -62,6 +71,16 @@ def _collinear(cells, desc):
     cells.a["energy"][:2] = 0.0
 
 
+def _mut_taxis(cells, desc):
+    # Force both tumble triggers (run timer past TAXIS_RUN_MAX; a remembered
+    # signal above the current one) and mix in dormant and dark cells.
+    n = cells.n
+    cells.a["run_timer"][0:n:3] = 0.45
+    cells.a["taxis_memory"][1:n:3] = 1.0e9
+    cells.a["flags"][2:n:7] &= np.uint32(0xFFFFFFFF ^ agb.FLAG_AWAKE)
+    cells.a["energy"][5:n:11] = 0.0
+
+
 def scenarios():
     """name -> dict(desc, spawn, mutate, fields, ticks)."""
     s = {}
@@ -95,6 +114,11 @@ def scenarios():
         desc=d, ticks=2,
         spawn=agb.spawn(4000, placement=agb.PLACE_GAUSSIAN, place_radius=6e-5, charge_dist=agb.DIST_UNIFORM,
                         charge_a=0.0, charge_b=0.2, awake=True))
+    d = slab_desc(light=(1.0, 0.0, 1e4, 0.0))
+    d.taxis_enabled = 1
+    s["taxis_seek"] = dict(
+        desc=d, ticks=4, mutate=_mut_taxis,
+        spawn=agb.spawn(1500, charge_dist=agb.DIST_UNIFORM, charge_a=0.9, charge_b=1.0, awake=True))
     return s
 
 
@@ -138,7 +162,7 @@ def trace(world, sc, full_after=None):
     rec["snapshot_initial"] = snapshot_record(world.snapshot(b"golden"))
     full = None
     for t in range(sc["ticks"]):
-        for stage, name in STAGES:
+        for stage, name in stages_for(sc["desc"]):
             world.stage(stage)
             e = {"tick": t, "stage": name, "cells": cells_digest(world),
                  "fields": [digest(world.export_field(f)) for f in range(4)]}

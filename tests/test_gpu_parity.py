@@ -45,7 +45,7 @@ def test_each_stage_from_identical_state(name):
     gpu, orc = seeded(sc)
     errs = []
     for t in range(sc["ticks"]):
-        for stage, sname in S.STAGES:
+        for stage, sname in S.stages_for(sc["desc"]):
             before, _ = orc.export_cells()
             P.copy_state(orc, gpu)
             if stage in (agb.STAGE_EMISSION, agb.STAGE_MOTION):
