@@ -479,6 +479,24 @@ def profile_stencil(n, passes=6):
     return 0
 
 
+def profile_surrogate(calls):
+    """The surrogate on a 128^3 window: `calls` network windows and one training
+    step (small case for ncu: the convolution and weight-gradient kernels)."""
+    import torch
+    sd = agb.surrogate_desc(seed=1)
+    sg = agb.Surrogate(sd)
+    shape = (sd.nz, sd.ny, sd.nx)
+    T, Cf, qT, qC = [torch.zeros(shape, dtype=torch.float32, device="cuda") for _ in range(4)]
+    sg.window(1, T.data_ptr(), Cf.data_ptr(), qT.data_ptr(), qC.data_ptr())
+    for _ in range(calls):
+        sg.advance(T.data_ptr(), Cf.data_ptr(), qT.data_ptr(), qC.data_ptr(), judge=-1)
+    sg.train(1)
+    torch.cuda.synchronize()
+    assert sg.error_word() == 0
+    print("profile-surrogate: %d windows + 1 training step ok" % calls)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -497,10 +515,14 @@ def main():
     ap.add_argument("--surrogate-windows-run", type=int, default=16)
     ap.add_argument("--profile-stencil", type=int, default=0,
                     help="only run a few FTCS passes on an N^3 temperature grid (small case for ncu)")
+    ap.add_argument("--profile-surrogate", type=int, default=0,
+                    help="only run N surrogate windows and one training step (small case for ncu)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.profile_stencil:
         return profile_stencil(args.profile_stencil)
+    if args.profile_surrogate:
+        return profile_surrogate(args.profile_surrogate)
 
     if args.impl == "reference":
         return run_reference(args, workload(args.workload, seed=1))
