@@ -18,6 +18,39 @@
 
 namespace agb {
 
+// Programmatic dependent launch: the tick's kernels are launched with the
+// programmatic-serialization attribute, so a kernel's CTAs may be scheduled
+// while its predecessor on the stream drains. Every such kernel calls
+// pdl_wait() before its first memory access; it returns once the predecessor
+// grid has completed and its writes are visible (a no-op without the
+// attribute). AGB_NO_PDL=1 launches normally.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+inline bool pdl_enabled() {
+    static int on = -1;
+    if (on < 0) {
+        const char* e = std::getenv("AGB_NO_PDL");
+        on = (e && e[0] == '1') ? 0 : 1;
+    }
+    return on == 1;
+}
+
+template <typename... KArgs, typename... Args>
+inline void launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args&&... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl_enabled() ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
+
 // ---------------------------------------------------------------------------
 // Contract SoA (contracts/cell_store_v1.h:42-75), device pointers.
 // ---------------------------------------------------------------------------

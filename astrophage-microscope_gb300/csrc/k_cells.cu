@@ -79,6 +79,7 @@ __device__ __forceinline__ void rec_delta(const HashDev& h, const float4& a, int
 // Thermal substep (thermal_kernel, src/sim/thermal.cu:19-71)
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) thermal_kernel(DevState* S, Ctx c, TickParams p) {
+    pdl_wait();
     const SoA v = S->cur;
     const int32_t n = S->count;
     const GridDev T = c.g[AGB_FIELD_TEMPERATURE];
@@ -124,6 +125,7 @@ __global__ void __launch_bounds__(256) thermal_kernel(DevState* S, Ctx c, TickPa
 // Emission (src/sim/emission.cu:17-177)
 // ---------------------------------------------------------------------------
 __global__ void clear_stamps_kernel(DevState* S, Ctx c, const int32_t* __restrict__ stamp_idx) {
+    pdl_wait();
     const int32_t n = S->n_stamps;
     unsigned long long* dep = c.g[AGB_FIELD_IRRADIANCE].deposit;
     AGB_FOR_CELLS(i, n) {
@@ -135,6 +137,7 @@ __global__ void clear_stamps_kernel(DevState* S, Ctx c, const int32_t* __restric
 // occlusion_stamp_kernel (emission.cu:17-27). Also records each cell's voxel so
 // the next emission stage can clear exactly these voxels.
 __global__ void stamp_kernel(DevState* S, Ctx c, int32_t* stamp_idx) {
+    pdl_wait();
     const SoA v = S->cur;
     const int32_t n = S->count;
     if (blockIdx.x == 0 && threadIdx.x == 0) S->n_stamps = n;
@@ -158,6 +161,7 @@ __global__ void stamp_kernel(DevState* S, Ctx c, int32_t* stamp_idx) {
 __global__ void __launch_bounds__(256) occlusion_factor_kernel(DevState* S, Ctx c,
                                                                const int32_t* __restrict__ stamp_idx,
                                                                double* factor) {
+    pdl_wait();
     const int32_t n = S->n_stamps;
     const GridDev I = c.g[AGB_FIELD_IRRADIANCE];
     AGB_FOR_CELLS(i, n) {
@@ -176,6 +180,7 @@ __global__ void __launch_bounds__(256) occlusion_factor_kernel(DevState* S, Ctx 
 constexpr int SWEEP_PF = 16;
 
 __global__ void __launch_bounds__(128) sweep_kernel(Ctx c, const double* __restrict__ factor) {
+    pdl_wait();
     const GridDev I = c.g[AGB_FIELD_IRRADIANCE];
     const int32_t nx = I.nx, ny = I.ny;
     const int64_t plane = (int64_t)nx * ny;
@@ -218,6 +223,7 @@ __global__ void __launch_bounds__(128) sweep_kernel(Ctx c, const double* __restr
 // consecutive voxels per step (coalesced). Stamped voxels are rare; the FP64
 // recurrence walks them in sweep order, broadcasting each factor.
 __global__ void __launch_bounds__(256) sweep_rows_kernel(Ctx c, const double* __restrict__ factor) {
+    pdl_wait();
     const GridDev I = c.g[AGB_FIELD_IRRADIANCE];
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -272,6 +278,7 @@ __device__ double shadow_fraction64(double dx, double dy, double dz, const Ctx& 
 // lanes then share bucket neighbourhoods (broadcast loads of the candidate
 // records) instead of each streaming its own list.
 __global__ void __launch_bounds__(256) feed_kernel(DevState* S, Ctx c, TickParams p) {
+    pdl_wait();
     const SoA v = S->cur;
     const int32_t n = S->hash_count;
     const GridDev I = c.g[AGB_FIELD_IRRADIANCE];
@@ -390,6 +397,7 @@ __device__ __forceinline__ bool boundary_axis(double& pos, float& vel, const Ctx
 // forces_kernel (integrator.cu:40-76), one thread per hash-sorted entry.
 __global__ void __launch_bounds__(256) forces_kernel(DevState* S, Ctx c, TickParams p, float* fx_out,
                                                      float* fy_out, float* fz_out) {
+    pdl_wait();
     const SoA v = S->cur;
     const int32_t n = S->hash_count;
     const HashDev h = c.h;
@@ -467,6 +475,7 @@ __global__ void __launch_bounds__(256) integrate_kernel(DevState* S, Ctx c, Tick
                                                         const float* __restrict__ fx_in,
                                                         const float* __restrict__ fy_in,
                                                         const float* __restrict__ fz_in) {
+    pdl_wait();
     const SoA v = S->cur;
     const int32_t n = S->count;
     AGB_FOR_CELLS(i, n) {
@@ -577,6 +586,7 @@ __device__ V3 taxis_tumble(V3 heading, Pcg& rng) {               // taxis.cuh:10
 }
 
 __global__ void __launch_bounds__(256) taxis_kernel(DevState* S, Ctx c, TickParams p) {
+    pdl_wait();
     const SoA v = S->cur;
     const int32_t n = S->count;
     AGB_FOR_CELLS(i, n) {
@@ -632,7 +642,7 @@ __global__ void __launch_bounds__(256) taxis_kernel(DevState* S, Ctx c, TickPara
 }  // namespace
 
 void launch_taxis(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, cudaStream_t s) {
-    taxis_kernel<<<blocks, 256, 0, s>>>(S, c, p);
+    launch_k(taxis_kernel, blocks, 256, 0, s, S, c, p);
 }
 
 namespace {
@@ -640,30 +650,30 @@ namespace {
 }  // namespace
 
 void launch_thermal(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, cudaStream_t s) {
-    thermal_kernel<<<blocks, 256, 0, s>>>(S, c, p);
+    launch_k(thermal_kernel, blocks, 256, 0, s, S, c, p);
 }
 void launch_emission(DevState* S, const Ctx& c, const TickParams& p, int32_t* stamp_idx, double* factor,
                      bool stamp, int32_t blocks, cudaStream_t s) {
-    clear_stamps_kernel<<<blocks, 256, 0, s>>>(S, c, stamp_idx);
+    launch_k(clear_stamps_kernel, blocks, 256, 0, s, S, c, stamp_idx);
     if (stamp) {
-        stamp_kernel<<<blocks, 256, 0, s>>>(S, c, stamp_idx);
-        occlusion_factor_kernel<<<blocks, 256, 0, s>>>(S, c, stamp_idx, factor);
+        launch_k(stamp_kernel, blocks, 256, 0, s, S, c, stamp_idx);
+        launch_k(occlusion_factor_kernel, blocks, 256, 0, s, S, c, stamp_idx, factor);
     }
     const GridDev& I = c.g[AGB_FIELD_IRRADIANCE];
     const int32_t len = c.light_axis == 0 ? I.nx : (c.light_axis == 1 ? I.ny : I.nz);
     const int64_t lines = I.count / len;
     if (c.light_axis == 0) {
         const int64_t blocks = (lines * 32 + 255) / 256;
-        sweep_rows_kernel<<<(unsigned)(blocks < 65535 ? blocks : 65535), 256, 0, s>>>(c, factor);
+        launch_k(sweep_rows_kernel, (unsigned)(blocks < 65535 ? blocks : 65535), 256, 0, s, c, factor);
     } else {
-        sweep_kernel<<<(unsigned)((lines + 127) / 128), 128, 0, s>>>(c, factor);
+        launch_k(sweep_kernel, (unsigned)((lines + 127) / 128), 128, 0, s, c, factor);
     }
-    feed_kernel<<<blocks, 256, 0, s>>>(S, c, p);
+    launch_k(feed_kernel, blocks, 256, 0, s, S, c, p);
 }
 void launch_motion(DevState* S, const Ctx& c, const TickParams& p, float* fx, float* fy, float* fz,
                    int32_t blocks, cudaStream_t s) {
-    forces_kernel<<<blocks, 256, 0, s>>>(S, c, p, fx, fy, fz);
-    integrate_kernel<<<blocks, 256, 0, s>>>(S, c, p, fx, fy, fz);
+    launch_k(forces_kernel, blocks, 256, 0, s, S, c, p, fx, fy, fz);
+    launch_k(integrate_kernel, blocks, 256, 0, s, S, c, p, fx, fy, fz);
 }
 
 }  // namespace agb

@@ -19,6 +19,7 @@ namespace agb {
 namespace {
 
 __global__ void fill_kernel(float* v, int64_t n, float value) {
+    pdl_wait();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
         v[i] = value;
@@ -40,6 +41,7 @@ __device__ __forceinline__ float ghost(const Faces& f, int face, float c) {
 // 2-D (nz == 1): the reference's 5-point formula.
 __global__ void __launch_bounds__(256) ftcs2d_kernel(const float* __restrict__ src, float* __restrict__ dst,
                                                      int32_t nx, int32_t ny, float coeff, Faces f) {
+    pdl_wait();
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const int32_t j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= nx || j >= ny) return;
@@ -61,6 +63,7 @@ constexpr int ZCHUNK = 8;
 __global__ void __launch_bounds__(256) ftcs3d_kernel(const float* __restrict__ src, float* __restrict__ dst,
                                                      int32_t nx, int32_t ny, int32_t nz, float coeff,
                                                      Faces f) {
+    pdl_wait();
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const int32_t j = blockIdx.y * blockDim.y + threadIdx.y;
     const int32_t k0 = blockIdx.z * ZCHUNK;
@@ -166,6 +169,7 @@ __global__ void __launch_bounds__(256) ftcs3d_tma_kernel(const __grid_constant__
                                                          float* __restrict__ dst, int32_t nx, int32_t ny,
                                                          int32_t nz, int32_t zc, float coeff, Faces f,
                                                          uint32_t* err) {
+    pdl_wait();
     using T = TmaTile<LX, RPT>;
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + NBUF * T::PLANE_STRIDE);
@@ -271,6 +275,7 @@ __global__ void __launch_bounds__(256) ftcs3d_tma_kernel(const __grid_constant__
 // depositing cell holds zero). Optionally also zeroes a per-voxel demand
 // accumulator of the same grid (the CO2 rationing buffer).
 __global__ void flush_by_cells_kernel(DevState* S, GridDev g, unsigned long long* demand) {
+    pdl_wait();
     const SoA v = S->cur;
     const int32_t n = S->count;
     AGB_FOR_CELLS(i, n) {
@@ -290,7 +295,7 @@ __global__ void flush_by_cells_kernel(DevState* S, GridDev g, unsigned long long
 
 void launch_fill(float* v, int64_t n, float value, cudaStream_t s) {
     const int64_t blocks = (n + 255) / 256;
-    fill_kernel<<<(unsigned)(blocks > 4096 ? 4096 : blocks), 256, 0, s>>>(v, n, value);
+    launch_k(fill_kernel, (unsigned)(blocks > 4096 ? 4096 : blocks), 256, 0, s, v, n, value);
 }
 
 namespace {
@@ -318,7 +323,7 @@ struct TmaInstance {
         using T = TmaTile<LX, RPT>;
         (void)slots_per_sm();                           // sets the shared-memory attribute once
         const dim3 grid((g.nx + T::TXW - 1) / T::TXW, (g.ny + T::TYH - 1) / T::TYH, (g.nz + zc - 1) / zc);
-        ftcs3d_tma_kernel<LX, RPT><<<grid, 256, T::SMEM, s>>>(*map, dst, g.nx, g.ny, g.nz, zc, coeff, f, err);
+        launch_k(ftcs3d_tma_kernel<LX, RPT>, grid, 256, T::SMEM, s, *map, dst, g.nx, g.ny, g.nz, zc, coeff, f, err);
     }
 };
 
@@ -398,17 +403,17 @@ void launch_ftcs(const GridDev& g, const float* src, float* dst, float coeff, co
     if (g.nz == 1) {
         const dim3 block(32, 8);
         const dim3 grid((g.nx + 31) / 32, (g.ny + 7) / 8);
-        ftcs2d_kernel<<<grid, block, 0, s>>>(src, dst, g.nx, g.ny, coeff, f);
+        launch_k(ftcs2d_kernel, grid, block, 0, s, src, dst, g.nx, g.ny, coeff, f);
     } else {
         const dim3 block(32, 8);
         const dim3 grid((g.nx + 31) / 32, (g.ny + 7) / 8, (g.nz + ZCHUNK - 1) / ZCHUNK);
-        ftcs3d_kernel<<<grid, block, 0, s>>>(src, dst, g.nx, g.ny, g.nz, coeff, f);
+        launch_k(ftcs3d_kernel, grid, block, 0, s, src, dst, g.nx, g.ny, g.nz, coeff, f);
     }
 }
 
 void launch_flush_by_cells(DevState* S, GridDev g, unsigned long long* demand, int32_t grid_blocks,
                            cudaStream_t s) {
-    flush_by_cells_kernel<<<grid_blocks, 256, 0, s>>>(S, g, demand);
+    launch_k(flush_by_cells_kernel, grid_blocks, 256, 0, s, S, g, demand);
 }
 
 }  // namespace agb

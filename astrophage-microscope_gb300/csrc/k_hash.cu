@@ -22,9 +22,8 @@ namespace agb {
 
 namespace {
 
-constexpr int RT = 256;           // radix threads per tile = keys per tile
-
 __global__ void clear_prev_ranges_kernel(DevState* S, HashDev h) {
+    pdl_wait();
     const int32_t n = S->hash_count;
     AGB_FOR_CELLS(k, n) {
         const uint32_t key = h.keys_sorted[k];
@@ -34,6 +33,7 @@ __global__ void clear_prev_ranges_kernel(DevState* S, HashDev h) {
 
 // key_kernel, src/sim/hash.cu:15-25
 __global__ void key_kernel(DevState* S, HashDev h) {
+    pdl_wait();
     const SoA v = S->cur;
     const int32_t n = S->count;
     AGB_FOR_CELLS(i, n) {
@@ -48,92 +48,156 @@ __global__ void key_kernel(DevState* S, HashDev h) {
     }
 }
 
-// Per-tile digit histogram, digit-major: hist[d * tiles + t].
-__global__ void __launch_bounds__(RT) radix_upsweep(DevState* S, const uint32_t* __restrict__ kin,
-                                                   uint32_t* hist, int shift, int num_tiles) {
-    __shared__ uint32_t cnt[256];
-    const int tile = blockIdx.x;
-    cnt[threadIdx.x] = 0;
-    __syncthreads();
-    const int64_t e = (int64_t)tile * RT + threadIdx.x;
-    if (e < S->count) atomicAdd(&cnt[(kin[e] >> shift) & 255u], 1u);
-    __syncthreads();
-    hist[threadIdx.x * num_tiles + tile] = cnt[threadIdx.x];
-}
+// ---------------------------------------------------------------------------
+// Stable LSD radix sort, one kernel per 8-bit pass (a single-sweep scheme):
+//   * radix_hist_kernel reads every key once and counts the digits of all
+//     passes (global histograms, then their exclusive scans in each pass);
+//   * radix_pass_kernel: a CTA takes the next 2048-key tile (tile order = the
+//     order CTAs start, so every tile it waits on is already running), ranks
+//     its keys stably (warp match_any per 32-key group, then a per-digit scan
+//     over the tile's 64 groups), publishes its per-digit count, looks back
+//     over earlier tiles' published counts/prefixes (decoupled look-back) and
+//     scatters. Look-back waits are bounded; a timeout sets the error word and
+//     the CTA writes nothing.
+// ---------------------------------------------------------------------------
+constexpr int SORT_THREADS = 256;
+constexpr uint32_t FLAG_AGG = 1u << 30, FLAG_PRE = 2u << 30, VALUE_MASK = (1u << 30) - 1u;
+constexpr int LOOKBACK_BATCH = 8;                                // predecessor words read per round trip
+constexpr uint32_t LOOKBACK_LIMIT = 1u << 24;
 
-// Exclusive scan of each digit's row across tiles (one block per digit);
-// totals[d] = the digit's count over all tiles.
-__global__ void __launch_bounds__(1024) radix_scan_digits(uint32_t* hist, uint32_t* totals, int num_tiles) {
-    __shared__ uint32_t part[1024];
-    uint32_t* row = hist + (int64_t)blockIdx.x * num_tiles;
-    const int t = threadIdx.x;
-    const int per = (num_tiles + 1023) / 1024;
-    const int b = t * per, e = b + per < num_tiles ? b + per : num_tiles;
-    uint32_t s = 0;
-    for (int i = b; i < e; ++i) s += row[i];
-    part[t] = s;
+__global__ void __launch_bounds__(256) radix_hist_kernel(DevState* S, const uint32_t* __restrict__ kin,
+                                                         uint32_t* __restrict__ ghist, int passes) {
+    pdl_wait();
+    __shared__ uint32_t h[4][256];
+    for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) (&h[0][0])[i] = 0u;
     __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {
-        const uint32_t v = t >= off ? part[t - off] : 0u;
-        __syncthreads();
-        part[t] += v;
-        __syncthreads();
-    }
-    uint32_t run = t > 0 ? part[t - 1] : 0u;
-    for (int i = b; i < e; ++i) {
-        const uint32_t x = row[i];
-        row[i] = run;
-        run += x;
-    }
-    if (t == 1023) totals[blockIdx.x] = part[1023];
-}
-
-// Stable scatter of one 256-key tile: rank = earlier same-digit keys in the
-// warp (match_any) + same-digit keys in earlier warps of the tile; the global
-// offset = (keys of smaller digits) + (same digit in earlier tiles).
-__global__ void __launch_bounds__(RT) radix_downsweep(DevState* S, const uint32_t* __restrict__ kin,
-                                                     const uint32_t* __restrict__ vin, uint32_t* kout,
-                                                     uint32_t* vout, const uint32_t* __restrict__ offs,
-                                                     const uint32_t* __restrict__ totals, int shift,
-                                                     int num_tiles) {
-    __shared__ uint32_t dbase[256];
-    __shared__ uint32_t wcnt[RT / 32][256];
-    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-    const int tile = blockIdx.x;
     const int32_t n = S->count;
-    const int64_t e = (int64_t)tile * RT + t;
-    if ((int64_t)tile * RT >= n) return;                 // whole block beyond the live count
-    // Exclusive scan of the 256 digit totals (every block recomputes it).
-    dbase[t] = totals[t];
-    for (int q = 0; q < RT / 32; ++q) wcnt[q][t] = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t k = kin[i];
+        for (int p = 0; p < passes; ++p) atomicAdd(&h[p][(k >> (8 * p)) & 255u], 1u);
+    }
     __syncthreads();
+    for (int i = threadIdx.x; i < passes * 256; i += blockDim.x) {
+        const uint32_t c = (&h[0][0])[i];
+        if (c) atomicAdd(&ghist[i], c);
+    }
+}
+
+// PER keys per thread: a tile is 256 * PER keys in 8 * PER warp-groups.
+template <int PER>
+__global__ void __launch_bounds__(SORT_THREADS) radix_pass_kernel(DevState* S, const uint32_t* __restrict__ kin,
+                                                                  const uint32_t* __restrict__ vin,
+                                                                  uint32_t* __restrict__ kout,
+                                                                  uint32_t* __restrict__ vout,
+                                                                  const uint32_t* __restrict__ ghist,
+                                                                  uint32_t* status, uint32_t* tile_counter,
+                                                                  int shift) {
+    pdl_wait();
+    constexpr int SORT_TILE = SORT_THREADS * PER;
+    constexpr int SORT_GROUPS = SORT_TILE / 32;
+    __shared__ uint16_t cnt[SORT_GROUPS][256];     // per group and digit: count, then exclusive prefix
+    __shared__ uint32_t dbase[256];                // global base of each digit for this tile
+    __shared__ uint32_t tile_id;
+    __shared__ int ok_all;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const int32_t n = S->count;
+    const int ntiles = (n + SORT_TILE - 1) / SORT_TILE;
+    if (t == 0) tile_id = atomicAdd(tile_counter, 1u);
+    for (int g = 0; g < SORT_GROUPS; ++g) cnt[g][t] = 0;
+    __syncthreads();
+    const int tile = (int)tile_id;
+    if (tile >= ntiles) return;                      // block-uniform
+    const int64_t base = (int64_t)tile * SORT_TILE;
+    // Element order inside the tile: e = k * 256 + t (k = 0..7); group = k * 8 + w.
+    uint32_t key[PER], dig[PER], rank[PER];
+    unsigned peers_lt[PER];
+    const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int64_t e = base + k * SORT_THREADS + t;
+        const bool valid = e < n;
+        key[k] = valid ? kin[e] : 0xFFFFFFFFu;
+        dig[k] = valid ? (key[k] >> shift) & 255u : 256u + (unsigned)lane;   // invalid: unique, never counted
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, dig[k]);
+        peers_lt[k] = __popc(peers & lt);
+        if (valid && (peers & lt) == 0u) cnt[k * 8 + w][dig[k]] = (uint16_t)__popc(peers);
+    }
+    __syncthreads();
+    // Exclusive scan of each digit's column over the 64 groups (thread = digit).
+    uint32_t run = 0;
+    for (int g = 0; g < SORT_GROUPS; ++g) {
+        const uint32_t c = cnt[g][t];
+        cnt[g][t] = (uint16_t)run;
+        run += c;
+    }
+    const uint32_t my_count = run;                   // keys of digit t in this tile
+    // Publish the aggregate (tile 0 publishes its inclusive prefix directly),
+    // then look back for the exclusive prefix over earlier tiles.
+    uint32_t* st = status + (int64_t)tile * 256;
+    if (tile == 0) {
+        atomicExch(&st[t], FLAG_PRE | my_count);
+    } else {
+        atomicExch(&st[t], FLAG_AGG | my_count);
+    }
+    // Look back in batches: the words of up to LOOKBACK_BATCH predecessors are
+    // loaded together (one round trip), nearest first; summing stops at the
+    // nearest inclusive prefix. A word not yet published is polled again.
+    uint32_t excl = 0;
+    bool ok = true;
+    for (int j0 = tile - 1; j0 >= 0 && ok;) {
+        const int nb = j0 + 1 < LOOKBACK_BATCH ? j0 + 1 : LOOKBACK_BATCH;
+        uint32_t v[LOOKBACK_BATCH];
+#pragma unroll
+        for (int q = 0; q < LOOKBACK_BATCH; ++q)
+            v[q] = q < nb ? *(volatile const uint32_t*)(status + (int64_t)(j0 - q) * 256 + t) : FLAG_PRE;
+        bool done = false;
+        for (int q = 0; q < nb && ok && !done; ++q) {
+            uint32_t it = 0;
+            while (!(v[q] & (FLAG_AGG | FLAG_PRE)) && it < LOOKBACK_LIMIT) {
+                v[q] = *(volatile const uint32_t*)(status + (int64_t)(j0 - q) * 256 + t);
+                ++it;
+            }
+            if (!(v[q] & (FLAG_AGG | FLAG_PRE))) { ok = false; set_error(S, 5u); break; }
+            excl += v[q] & VALUE_MASK;
+            if (v[q] & FLAG_PRE) done = true;
+        }
+        if (done) break;
+        j0 -= nb;
+    }
+    if (tile > 0 && ok) {
+        __threadfence();
+        atomicExch(&st[t], FLAG_PRE | (excl + my_count));
+    }
+    // Digit base = (keys of smaller digits over all tiles) + (this digit in earlier tiles).
+    dbase[t] = ghist[t];
+    if (t == 0) ok_all = 1;
+    __syncthreads();
+    if (!ok) ok_all = 0;
     for (int off = 1; off < 256; off <<= 1) {
         const uint32_t v = t >= off ? dbase[t - off] : 0u;
         __syncthreads();
         dbase[t] += v;
         __syncthreads();
     }
-    const uint32_t mybase = (t > 0 ? dbase[t - 1] : 0u);
+    const uint32_t smaller = t > 0 ? dbase[t - 1] : 0u;
     __syncthreads();
-    dbase[t] = mybase + offs[t * num_tiles + tile];
-    const bool valid = e < n;
-    const uint32_t key = valid ? kin[e] : 0u;
-    const uint32_t d = (key >> shift) & 255u;
-    const unsigned lt = (1u << lane) - 1u;
-    const unsigned peers = __match_any_sync(0xFFFFFFFFu, valid ? d : (0x100u | (unsigned)lane));
-    if (valid && (peers & lt) == 0u) wcnt[w][d] = __popc(peers);
+    dbase[t] = smaller + excl;
     __syncthreads();
-    if (valid) {
-        uint32_t pos = __popc(peers & lt);
-        for (int q = 0; q < w; ++q) pos += wcnt[q][d];
-        const uint32_t o = dbase[d] + pos;
-        kout[o] = key;
-        vout[o] = vin[e];
+    if (!ok_all) return;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int64_t e = base + k * SORT_THREADS + t;
+        if (e >= n) continue;
+        const uint32_t d = dig[k];
+        rank[k] = dbase[d] + cnt[k * 8 + w][d] + peers_lt[k];
+        kout[rank[k]] = key[k];
+        vout[rank[k]] = vin[e];
     }
 }
 
 // range_kernel (src/sim/hash.cu:29-38) + the sorted snapshot.
 __global__ void ranges_kernel(DevState* S, HashDev h) {
+    pdl_wait();
     const SoA v = S->cur;
     const int32_t n = S->count;
     if (blockIdx.x == 0 && threadIdx.x == 0) S->hash_count = n;
@@ -160,25 +224,45 @@ __global__ void ranges_kernel(DevState* S, HashDev h) {
 
 void hash_build(DevState* S, const HashDev& h, int32_t capacity, uint32_t* kalt, uint32_t* valt,
                 uint32_t* hist, int32_t grid_blocks, cudaStream_t s) {
-    clear_prev_ranges_kernel<<<grid_blocks, 256, 0, s>>>(S, h);
-    key_kernel<<<grid_blocks, 256, 0, s>>>(S, h);
+    launch_k(clear_prev_ranges_kernel, grid_blocks, 256, 0, s, S, h);
+    launch_k(key_kernel, grid_blocks, 256, 0, s, S, h);
     int bits = 0;
     while (bits < 32 && ((uint64_t)(uint32_t)h.buckets >> bits) != 0) ++bits;
     const int passes = (bits + 7) / 8;
-    const int num_tiles = (capacity + RT - 1) / RT;
-    uint32_t* totals = hist + (size_t)256 * num_tiles;
+    // Populations up to 256k cells sort in 1024-key tiles (more CTAs), larger
+    // ones in 2048-key tiles.
+    const int per = capacity <= (256 << 10) ? 4 : 8;
+    const int tile_keys = SORT_THREADS * per;
+    const int max_tiles = (capacity + tile_keys - 1) / tile_keys;
+    // hist layout: [4][256] digit histograms | [4] tile counters | [4][max_tiles][256] status words.
+    uint32_t* ghist = hist;
+    uint32_t* counters = hist + 4 * 256;
+    uint32_t* status = counters + 4;
+    cudaMemsetAsync(hist, 0, sizeof(uint32_t) * (4 * 256 + 4 + (size_t)passes * max_tiles * 256), s);
+    launch_k(radix_hist_kernel, grid_blocks, 256, 0, s, S, h.keys, ghist, passes);
     uint32_t* kin = h.keys;
     uint32_t* vin = h.vals;
     for (int p = 0; p < passes; ++p) {
         uint32_t* kout = (p == passes - 1) ? h.keys_sorted : ((p & 1) ? h.keys : kalt);
         uint32_t* vout = (p == passes - 1) ? h.vals_sorted : ((p & 1) ? h.vals : valt);
-        radix_upsweep<<<num_tiles, RT, 0, s>>>(S, kin, hist, p * 8, num_tiles);
-        radix_scan_digits<<<256, 1024, 0, s>>>(hist, totals, num_tiles);
-        radix_downsweep<<<num_tiles, RT, 0, s>>>(S, kin, vin, kout, vout, hist, totals, p * 8, num_tiles);
+        uint32_t* st = status + (size_t)p * max_tiles * 256;
+        if (per == 4)
+            launch_k(radix_pass_kernel<4>, max_tiles, SORT_THREADS, 0, s, S, kin, vin, kout, vout, ghist + p * 256, st,
+                                                                    counters + p, p * 8);
+        else
+            launch_k(radix_pass_kernel<8>, max_tiles, SORT_THREADS, 0, s, S, kin, vin, kout, vout, ghist + p * 256, st,
+                                                                    counters + p, p * 8);
         kin = kout;
         vin = vout;
     }
-    ranges_kernel<<<grid_blocks, 256, 0, s>>>(S, h);
+    launch_k(ranges_kernel, grid_blocks, 256, 0, s, S, h);
+}
+
+size_t hash_sort_scratch_words(int32_t capacity) {
+    const int per = capacity <= (256 << 10) ? 4 : 8;
+    const size_t tile_keys = (size_t)SORT_THREADS * per;
+    const size_t max_tiles = ((size_t)capacity + tile_keys - 1) / tile_keys;
+    return 4 * 256 + 4 + 4 * max_tiles * 256;
 }
 
 }  // namespace agb

@@ -30,6 +30,7 @@ __device__ __forceinline__ float uptake_rate_f(float c) {     // co2_uptake_rate
 
 __global__ void __launch_bounds__(256) demand_kernel(DevState* S, Ctx c, TickParams p,
                                                      unsigned long long* demand, float inv_gv) {
+    pdl_wait();
     const SoA v = S->cur;
     const int32_t n = S->count;
     const GridDev C2 = c.g[AGB_FIELD_CO2];
@@ -46,6 +47,7 @@ __global__ void __launch_bounds__(256) demand_kernel(DevState* S, Ctx c, TickPar
 __global__ void __launch_bounds__(256) uptake_kernel(DevState* S, Ctx c, TickParams p,
                                                      const unsigned long long* __restrict__ demand,
                                                      float inv_gv) {
+    pdl_wait();
     const SoA v = S->cur;
     const int32_t n = S->count;
     const GridDev C2 = c.g[AGB_FIELD_CO2];
@@ -75,6 +77,7 @@ __device__ __forceinline__ bool ready_to_divide(const Ctx& c, const SoA& v, int3
 }
 
 __global__ void __launch_bounds__(256) death_mark_kernel(DevState* S, Ctx c, int32_t* divflag) {
+    pdl_wait();
     const SoA v = S->cur;
     const int32_t n = S->count;
     int32_t births = 0, deads = 0;
@@ -115,6 +118,7 @@ __device__ __forceinline__ bool scan_gate(const DevState* S, int gate) {
 
 __global__ void __launch_bounds__(ST) scan_tiles_kernel(DevState* S, const int32_t* __restrict__ flag,
                                                        int32_t* tile_sums, int gate) {
+    pdl_wait();
     if (!scan_gate(S, gate)) return;
     const int32_t n = S->count;
     const int64_t base = (int64_t)blockIdx.x * STILE;
@@ -136,6 +140,7 @@ __global__ void __launch_bounds__(ST) scan_tiles_kernel(DevState* S, const int32
 
 __global__ void __launch_bounds__(1024) scan_top_kernel(DevState* S, int32_t* tile_sums, int32_t ntiles,
                                                        int gate) {
+    pdl_wait();
     if (!scan_gate(S, gate)) return;
     __shared__ int32_t part[1024];
     const int t = threadIdx.x;
@@ -163,6 +168,7 @@ __global__ void __launch_bounds__(1024) scan_top_kernel(DevState* S, int32_t* ti
 __global__ void __launch_bounds__(ST) scan_apply_kernel(DevState* S, const int32_t* __restrict__ flag,
                                                        const int32_t* __restrict__ tile_sums, int32_t* prefix,
                                                        int gate) {
+    pdl_wait();
     if (!scan_gate(S, gate)) return;
     const int32_t n = S->count;
     __shared__ int32_t warp_tot[ST / 32];
@@ -196,6 +202,7 @@ __global__ void __launch_bounds__(ST) scan_apply_kernel(DevState* S, const int32
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) divide_kernel(DevState* S, Ctx c, const int32_t* __restrict__ divflag,
                                                      const int32_t* __restrict__ prefix) {
+    pdl_wait();
     if (S->births <= 0) return;
     const SoA v = S->cur;
     const int32_t n = S->count;                 // base = old count
@@ -253,6 +260,7 @@ __global__ void __launch_bounds__(256) divide_kernel(DevState* S, Ctx c, const i
 
 // The host bookkeeping of lifecycle_step (lifecycle.cu:250-293), on the device.
 __global__ void life_finalize_kernel(DevState* S, int32_t capacity, int32_t compaction_allowed) {
+    pdl_wait();
     int32_t births = S->births;
     const int32_t deads = S->deads;
     const int32_t n = S->count;
@@ -279,6 +287,7 @@ __global__ void life_finalize_kernel(DevState* S, int32_t capacity, int32_t comp
 // 25 arrays, then the SoA pointers swap on the device.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) keep_kernel(DevState* S, int32_t* keep) {
+    pdl_wait();
     if (!S->compact_now) return;
     const SoA v = S->cur;
     const int32_t n = S->count;
@@ -290,6 +299,7 @@ __global__ void __launch_bounds__(256) keep_kernel(DevState* S, int32_t* keep) {
 
 __global__ void __launch_bounds__(256) scatter_src_kernel(DevState* S, const int32_t* __restrict__ keep,
                                                          const int32_t* __restrict__ prefix, int32_t* src) {
+    pdl_wait();
     if (!S->compact_now) return;
     const int32_t n = S->count;
     AGB_FOR_CELLS(i, n) {
@@ -298,6 +308,7 @@ __global__ void __launch_bounds__(256) scatter_src_kernel(DevState* S, const int
 }
 
 __global__ void __launch_bounds__(256) gather_kernel(DevState* S, const int32_t* __restrict__ src) {
+    pdl_wait();
     if (!S->compact_now) return;
     const int32_t live = S->live;
     if (live >= S->count) return;
@@ -318,6 +329,7 @@ __global__ void __launch_bounds__(256) gather_kernel(DevState* S, const int32_t*
 }
 
 __global__ void swap_kernel(DevState* S) {
+    pdl_wait();
     if (!S->compact_now) return;
     const int32_t live = S->live;
     if (live < S->count) {
@@ -329,7 +341,8 @@ __global__ void swap_kernel(DevState* S) {
     S->compact_now = 0;
 }
 
-__global__ void force_compact_kernel(DevState* S) { S->compact_now = 1; }
+__global__ void force_compact_kernel(DevState* S) {
+    pdl_wait(); S->compact_now = 1; }
 
 // ---------------------------------------------------------------------------
 // Telemetry (stats_cells_kernel / stats_field_kernel, stats.cu:27-60):
@@ -349,6 +362,7 @@ __device__ __forceinline__ unsigned long long warp_max(unsigned long long x) {
 }
 
 __global__ void __launch_bounds__(256) stats_cells_kernel(DevState* S, unsigned long long* acc) {
+    pdl_wait();
     const SoA v = S->cur;
     const int32_t n = S->count;
     unsigned long long energy = 0, temp = 0, na = 0, nd = 0, nw = 0, ns = 0;
@@ -375,6 +389,7 @@ __global__ void __launch_bounds__(256) stats_cells_kernel(DevState* S, unsigned 
 __global__ void __launch_bounds__(256) stats_field_kernel(const float* __restrict__ val, int64_t count,
                                                           double scale, unsigned long long* sum,
                                                           unsigned long long* mx) {
+    pdl_wait();
     unsigned long long s = 0, m = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count;
          i += (int64_t)gridDim.x * blockDim.x) {
@@ -408,6 +423,7 @@ __device__ __forceinline__ void gaussian_pair_d(Pcg& r, double& z0, double& z1) 
 }
 
 __global__ void __launch_bounds__(256) spawn_kernel(DevState* S, Ctx c, agb_spawn p) {
+    pdl_wait();
     const SoA v = S->cur;
     const int32_t base = S->count;
     const uint64_t first_id = S->next_id;
@@ -513,24 +529,25 @@ __global__ void __launch_bounds__(256) spawn_kernel(DevState* S, Ctx c, agb_spaw
 }
 
 __global__ void spawn_finalize_kernel(DevState* S, int32_t count) {
+    pdl_wait();
     S->count += count;
     S->next_id += (uint64_t)count;
 }
 
 void launch_scan(DevState* S, const LifeBuffers& b, int32_t capacity, int gate, cudaStream_t s) {
     const int32_t ntiles = (capacity + STILE - 1) / STILE;
-    scan_tiles_kernel<<<ntiles, ST, 0, s>>>(S, b.flags, b.tile_sums, gate);
-    scan_top_kernel<<<1, 1024, 0, s>>>(S, b.tile_sums, ntiles, gate);
-    scan_apply_kernel<<<ntiles, ST, 0, s>>>(S, b.flags, b.tile_sums, b.prefix, gate);
+    launch_k(scan_tiles_kernel, ntiles, ST, 0, s, S, b.flags, b.tile_sums, gate);
+    launch_k(scan_top_kernel, 1, 1024, 0, s, S, b.tile_sums, ntiles, gate);
+    launch_k(scan_apply_kernel, ntiles, ST, 0, s, S, b.flags, b.tile_sums, b.prefix, gate);
 }
 
 void launch_compact_kernels(DevState* S, const LifeBuffers& b, int32_t capacity, int32_t blocks,
                             cudaStream_t s) {
-    keep_kernel<<<blocks, 256, 0, s>>>(S, b.flags);
+    launch_k(keep_kernel, blocks, 256, 0, s, S, b.flags);
     launch_scan(S, b, capacity, 1, s);
-    scatter_src_kernel<<<blocks, 256, 0, s>>>(S, b.flags, b.prefix, b.src);
-    gather_kernel<<<blocks, 256, 0, s>>>(S, b.src);
-    swap_kernel<<<1, 1, 0, s>>>(S);
+    launch_k(scatter_src_kernel, blocks, 256, 0, s, S, b.flags, b.prefix, b.src);
+    launch_k(gather_kernel, blocks, 256, 0, s, S, b.src);
+    launch_k(swap_kernel, 1, 1, 0, s, S);
 }
 
 }  // namespace
@@ -540,38 +557,38 @@ void launch_lifecycle(DevState* S, const Ctx& c, const TickParams& p, const Life
     const GridDev& C2 = c.g[AGB_FIELD_CO2];
     if (C2.enabled) {
         const float inv_gv = (float)(1.0 / (C2.dx * C2.dx * C2.dz_eff));
-        demand_kernel<<<blocks, 256, 0, s>>>(S, c, p, b.co2_demand, inv_gv);
-        uptake_kernel<<<blocks, 256, 0, s>>>(S, c, p, b.co2_demand, inv_gv);
+        launch_k(demand_kernel, blocks, 256, 0, s, S, c, p, b.co2_demand, inv_gv);
+        launch_k(uptake_kernel, blocks, 256, 0, s, S, c, p, b.co2_demand, inv_gv);
         launch_flush_by_cells(S, C2, b.co2_demand, blocks, s);      // lifecycle.cu:235
     }
-    death_mark_kernel<<<blocks, 256, 0, s>>>(S, c, b.flags);
+    launch_k(death_mark_kernel, blocks, 256, 0, s, S, c, b.flags);
     launch_scan(S, b, c.capacity, 0, s);
-    divide_kernel<<<blocks, 256, 0, s>>>(S, c, b.flags, b.prefix);
-    life_finalize_kernel<<<1, 1, 0, s>>>(S, c.capacity, compaction_allowed ? 1 : 0);
+    launch_k(divide_kernel, blocks, 256, 0, s, S, c, b.flags, b.prefix);
+    launch_k(life_finalize_kernel, 1, 1, 0, s, S, c.capacity, compaction_allowed ? 1 : 0);
     // Compaction cannot run on this tick unless the host-side period allows it.
     if (compaction_allowed) launch_compact_kernels(S, b, c.capacity, blocks, s);
 }
 
 void launch_compact(DevState* S, const Ctx& c, const LifeBuffers& b, int32_t blocks, cudaStream_t s) {
-    force_compact_kernel<<<1, 1, 0, s>>>(S);
+    launch_k(force_compact_kernel, 1, 1, 0, s, S);
     launch_compact_kernels(S, b, c.capacity, blocks, s);
 }
 
 void launch_stats(DevState* S, const Ctx& c, unsigned long long* acc, int32_t blocks, cudaStream_t s) {
     cudaMemsetAsync(acc, 0, sizeof(unsigned long long) * 12, s);
-    stats_cells_kernel<<<blocks, 256, 0, s>>>(S, acc);
+    launch_k(stats_cells_kernel, blocks, 256, 0, s, S, acc);
     const GridDev& T = c.g[AGB_FIELD_TEMPERATURE];
     const GridDev& C2 = c.g[AGB_FIELD_CO2];
     const GridDev& N2 = c.g[AGB_FIELD_N2];
     auto nb = [](int64_t n) { const int64_t b = (n + 255) / 256; return (unsigned)(b > 2048 ? 2048 : (b < 1 ? 1 : b)); };
-    if (T.enabled) stats_field_kernel<<<nb(T.count), 256, 0, s>>>(T.value, T.count, AGB_DEPOSIT_SCALE_STATS, &acc[2], &acc[5]);
-    if (C2.enabled) stats_field_kernel<<<nb(C2.count), 256, 0, s>>>(C2.value, C2.count, AGB_STATS_SCALE_FIELD, &acc[3], nullptr);
-    if (N2.enabled) stats_field_kernel<<<nb(N2.count), 256, 0, s>>>(N2.value, N2.count, AGB_STATS_SCALE_FIELD, &acc[4], nullptr);
+    if (T.enabled) launch_k(stats_field_kernel, nb(T.count), 256, 0, s, T.value, T.count, AGB_DEPOSIT_SCALE_STATS, &acc[2], &acc[5]);
+    if (C2.enabled) launch_k(stats_field_kernel, nb(C2.count), 256, 0, s, C2.value, C2.count, AGB_STATS_SCALE_FIELD, &acc[3], nullptr);
+    if (N2.enabled) launch_k(stats_field_kernel, nb(N2.count), 256, 0, s, N2.value, N2.count, AGB_STATS_SCALE_FIELD, &acc[4], nullptr);
 }
 
 void launch_spawn(DevState* S, const Ctx& c, const agb_spawn& p, int32_t blocks, cudaStream_t s) {
-    spawn_kernel<<<blocks, 256, 0, s>>>(S, c, p);
-    spawn_finalize_kernel<<<1, 1, 0, s>>>(S, p.count);
+    launch_k(spawn_kernel, blocks, 256, 0, s, S, c, p);
+    launch_k(spawn_finalize_kernel, 1, 1, 0, s, S, p.count);
 }
 
 }  // namespace agb

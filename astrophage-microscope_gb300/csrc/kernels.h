@@ -35,5 +35,7 @@ void launch_flush_by_cells(DevState* S, GridDev g, unsigned long long* demand_to
 // Spatial hash (k_hash.cu)
 void hash_build(DevState* S, const HashDev& h, int32_t capacity, uint32_t* sort_keys_alt,
                 uint32_t* sort_vals_alt, uint32_t* hist, int32_t grid_blocks, cudaStream_t s);
+// 32-bit words of sort scratch (`hist`) hash_build needs at this capacity.
+size_t hash_sort_scratch_words(int32_t capacity);
 
 }  // namespace agb

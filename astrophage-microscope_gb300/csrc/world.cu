@@ -584,11 +584,10 @@ agb_status agb_world_create(const agb_world_desc* d, agb_world** out) {
     }
     if (h.nx > 2047 || h.ny > 2047 || h.nz > 1023) { agb_world_destroy(w); return AGB_UNSUPPORTED; }
     const size_t n = (size_t)cap;
-    const int32_t tiles = (cap + 255) / 256;             // radix tiles (k_hash.cu)
     bool ok = dalloc(w, &h.keys, 4 * n) == cudaSuccess && dalloc(w, &h.vals, 4 * n) == cudaSuccess &&
               dalloc(w, &h.keys_sorted, 4 * n) == cudaSuccess && dalloc(w, &h.vals_sorted, 4 * n) == cudaSuccess &&
               dalloc(w, &w->kalt, 4 * n) == cudaSuccess && dalloc(w, &w->valt, 4 * n) == cudaSuccess &&
-              dalloc(w, &w->hist, 4 * 256 * ((size_t)tiles + 1)) == cudaSuccess &&
+              dalloc(w, &w->hist, 4 * hash_sort_scratch_words(cap)) == cudaSuccess &&
               dalloc(w, &h.ranges, 8 * (size_t)h.buckets) == cudaSuccess &&
               dalloc(w, &h.rec, 16 * n) == cudaSuccess;
     h.keys_prev = nullptr;
