@@ -18,6 +18,12 @@ struct LifeBuffers {
 void launch_thermal(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, cudaStream_t s);
 void launch_emission(DevState* S, const Ctx& c, const TickParams& p, int32_t* stamp_idx, double* factor,
                      bool stamp, int32_t blocks, cudaStream_t s);
+// The two halves of launch_emission: the irradiance field (stamps, occlusion
+// factors, sweep; needs the post-thermal cells, not the hash) and feeding
+// (walks the hash).
+void launch_emission_prep(DevState* S, const Ctx& c, const TickParams& p, int32_t* stamp_idx, double* factor,
+                          bool stamp, int32_t blocks, cudaStream_t s);
+void launch_feed(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, cudaStream_t s);
 // taxis_step (src/sim/taxis.cu:13-85): run-and-tumble state machine, emission.
 void launch_taxis(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, cudaStream_t s);
 void launch_motion(DevState* S, const Ctx& c, const TickParams& p, float* fx, float* fy, float* fz,

@@ -645,15 +645,12 @@ void launch_taxis(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks
     launch_k(taxis_kernel, blocks, 256, 0, s, S, c, p);
 }
 
-namespace {
-
-}  // namespace
-
 void launch_thermal(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, cudaStream_t s) {
     launch_k(thermal_kernel, blocks, 256, 0, s, S, c, p);
 }
-void launch_emission(DevState* S, const Ctx& c, const TickParams& p, int32_t* stamp_idx, double* factor,
-                     bool stamp, int32_t blocks, cudaStream_t s) {
+void launch_emission_prep(DevState* S, const Ctx& c, const TickParams& p, int32_t* stamp_idx, double* factor,
+                          bool stamp, int32_t blocks, cudaStream_t s) {
+    (void)p;
     launch_k(clear_stamps_kernel, blocks, 256, 0, s, S, c, stamp_idx);
     if (stamp) {
         launch_k(stamp_kernel, blocks, 256, 0, s, S, c, stamp_idx);
@@ -668,7 +665,14 @@ void launch_emission(DevState* S, const Ctx& c, const TickParams& p, int32_t* st
     } else {
         launch_k(sweep_kernel, (unsigned)((lines + 127) / 128), 128, 0, s, c, factor);
     }
+}
+void launch_feed(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, cudaStream_t s) {
     launch_k(feed_kernel, blocks, 256, 0, s, S, c, p);
+}
+void launch_emission(DevState* S, const Ctx& c, const TickParams& p, int32_t* stamp_idx, double* factor,
+                     bool stamp, int32_t blocks, cudaStream_t s) {
+    launch_emission_prep(S, c, p, stamp_idx, factor, stamp, blocks, s);
+    launch_feed(S, c, p, blocks, s);
 }
 void launch_motion(DevState* S, const Ctx& c, const TickParams& p, float* fx, float* fy, float* fz,
                    int32_t blocks, cudaStream_t s) {

@@ -22,37 +22,11 @@ namespace agb {
 
 namespace {
 
-__global__ void clear_prev_ranges_kernel(DevState* S, HashDev h) {
-    pdl_wait();
-    const int32_t n = S->hash_count;
-    AGB_FOR_CELLS(k, n) {
-        const uint32_t key = h.keys_sorted[k];
-        if (key < (uint32_t)h.buckets) h.ranges[key] = make_int2(0, 0);
-    }
-}
-
-// key_kernel, src/sim/hash.cu:15-25
-__global__ void key_kernel(DevState* S, HashDev h) {
-    pdl_wait();
-    const SoA v = S->cur;
-    const int32_t n = S->count;
-    AGB_FOR_CELLS(i, n) {
-        h.vals[i] = (uint32_t)i;
-        uint32_t key = (uint32_t)h.buckets;
-        if (v.flags[i] & AGB_FLAG_OCCUPIED) {
-            int32_t gx, gy, gz;
-            hash_coords(h, v.x[i], v.y[i], v.z[i], gx, gy, gz);
-            key = (uint32_t)((gz * h.ny + gy) * h.nx + gx);
-        }
-        h.keys[i] = key;
-    }
-}
-
 // ---------------------------------------------------------------------------
 // Stable LSD radix sort, one kernel per 8-bit pass (a single-sweep scheme):
-//   * radix_hist_kernel reads every key once and counts the digits of all
-//     passes (global histograms, then their exclusive scans in each pass);
-//   * radix_pass_kernel: a CTA takes the next 2048-key tile (tile order = the
+//   * key_hist_kernel (below) writes every key once and counts the digits of
+//     all passes (global histograms, then their exclusive scans in each pass);
+//   * radix_pass_kernel: a CTA takes the next 1024- or 2048-key tile (tile order = the
 //     order CTAs start, so every tile it waits on is already running), ranks
 //     its keys stably (warp match_any per 32-key group, then a per-digit scan
 //     over the tile's 64 groups), publishes its per-digit count, looks back
@@ -64,24 +38,6 @@ constexpr int SORT_THREADS = 256;
 constexpr uint32_t FLAG_AGG = 1u << 30, FLAG_PRE = 2u << 30, VALUE_MASK = (1u << 30) - 1u;
 constexpr int LOOKBACK_BATCH = 8;                                // predecessor words read per round trip
 constexpr uint32_t LOOKBACK_LIMIT = 1u << 24;
-
-__global__ void __launch_bounds__(256) radix_hist_kernel(DevState* S, const uint32_t* __restrict__ kin,
-                                                         uint32_t* __restrict__ ghist, int passes) {
-    pdl_wait();
-    __shared__ uint32_t h[4][256];
-    for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) (&h[0][0])[i] = 0u;
-    __syncthreads();
-    const int32_t n = S->count;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t k = kin[i];
-        for (int p = 0; p < passes; ++p) atomicAdd(&h[p][(k >> (8 * p)) & 255u], 1u);
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < passes * 256; i += blockDim.x) {
-        const uint32_t c = (&h[0][0])[i];
-        if (c) atomicAdd(&ghist[i], c);
-    }
-}
 
 // PER keys per thread: a tile is 256 * PER keys in 8 * PER warp-groups.
 template <int PER>
@@ -195,6 +151,42 @@ __global__ void __launch_bounds__(SORT_THREADS) radix_pass_kernel(DevState* S, c
     }
 }
 
+// The hash build's first pass, fused: clear the bucket ranges the previous
+// build wrote, compute every slot's key (key_kernel, src/sim/hash.cu:15-25)
+// and count the digits of all radix passes.
+__global__ void __launch_bounds__(256) key_hist_kernel(DevState* S, HashDev h, uint32_t* __restrict__ ghist,
+                                                       int passes) {
+    pdl_wait();
+    __shared__ uint32_t hs[4][256];
+    for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) (&hs[0][0])[i] = 0u;
+    __syncthreads();
+    const SoA v = S->cur;
+    const int32_t n = S->count, nprev = S->hash_count;
+    const int32_t m = n > nprev ? n : nprev;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        if (i < nprev) {
+            const uint32_t old = h.keys_sorted[i];
+            if (old < (uint32_t)h.buckets) h.ranges[old] = make_int2(0, 0);
+        }
+        if (i < n) {
+            h.vals[i] = (uint32_t)i;
+            uint32_t key = (uint32_t)h.buckets;
+            if (v.flags[i] & AGB_FLAG_OCCUPIED) {
+                int32_t gx, gy, gz;
+                hash_coords(h, v.x[i], v.y[i], v.z[i], gx, gy, gz);
+                key = (uint32_t)((gz * h.ny + gy) * h.nx + gx);
+            }
+            h.keys[i] = key;
+            for (int p = 0; p < passes; ++p) atomicAdd(&hs[p][(key >> (8 * p)) & 255u], 1u);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < passes * 256; i += blockDim.x) {
+        const uint32_t c = (&hs[0][0])[i];
+        if (c) atomicAdd(&ghist[i], c);
+    }
+}
+
 // range_kernel (src/sim/hash.cu:29-38) + the sorted snapshot.
 __global__ void ranges_kernel(DevState* S, HashDev h) {
     pdl_wait();
@@ -224,8 +216,6 @@ __global__ void ranges_kernel(DevState* S, HashDev h) {
 
 void hash_build(DevState* S, const HashDev& h, int32_t capacity, uint32_t* kalt, uint32_t* valt,
                 uint32_t* hist, int32_t grid_blocks, cudaStream_t s) {
-    launch_k(clear_prev_ranges_kernel, grid_blocks, 256, 0, s, S, h);
-    launch_k(key_kernel, grid_blocks, 256, 0, s, S, h);
     int bits = 0;
     while (bits < 32 && ((uint64_t)(uint32_t)h.buckets >> bits) != 0) ++bits;
     const int passes = (bits + 7) / 8;
@@ -239,7 +229,7 @@ void hash_build(DevState* S, const HashDev& h, int32_t capacity, uint32_t* kalt,
     uint32_t* counters = hist + 4 * 256;
     uint32_t* status = counters + 4;
     cudaMemsetAsync(hist, 0, sizeof(uint32_t) * (4 * 256 + 4 + (size_t)passes * max_tiles * 256), s);
-    launch_k(radix_hist_kernel, grid_blocks, 256, 0, s, S, h.keys, ghist, passes);
+    launch_k(key_hist_kernel, grid_blocks, 256, 0, s, S, h, ghist, passes);
     uint32_t* kin = h.keys;
     uint32_t* vin = h.vals;
     for (int p = 0; p < passes; ++p) {

@@ -205,6 +205,11 @@ void stage_thermal(agb_world* w, cudaStream_t s) {   // thermal_step, src/sim/th
     }
 }
 
+bool emission_active(const agb_world* w) {
+    return w->d.emission_enabled && w->c.g[AGB_FIELD_IRRADIANCE].enabled &&
+           (w->c.source > 0.0f || w->c.ambient_irr > 0.0f);
+}
+
 void stage_emission(agb_world* w, cudaStream_t s) {  // emission_step, src/sim/emission.cu:119-177
     if (!w->c.g[AGB_FIELD_IRRADIANCE].enabled) return;
     if (w->c.source <= 0.0f && w->c.ambient_irr <= 0.0f) return;
@@ -242,14 +247,16 @@ void stage_clock(agb_world* w) {
     w->sim_time += w->tp.dt;
 }
 
-// One tick as a small DAG. The thermal substeps and the CO2/N2 diffusion do
-// not touch what the hash build reads (positions, OCCUPIED), so they run on
-// side streams -- parallel branches of the captured graph -- joined where the
-// reference's order needs their results: thermal before emission (feeding sees
-// the post-thermostat store), slow fields before lifecycle (uptake reads the
-// diffused CO2). Motion samples CO2 and N2 from the buffers as they were
-// before this tick's diffusion, exactly as in src/sim/step.cu:164-171, while
-// the diffusion writes the other ping-pong buffer.
+// One tick as a small DAG. The thermal substeps, the irradiance field they
+// precede (stamps, occlusion factors, sweep: they read the post-thermal cells
+// but not the hash) and the CO2/N2 diffusion do not touch what the hash build
+// reads (positions, OCCUPIED), so they run on side streams -- parallel
+// branches of the captured graph -- joined where the reference's order needs
+// their results: the irradiance field before feeding (which walks the hash),
+// slow fields before lifecycle (uptake reads the diffused CO2). Motion samples
+// CO2 and N2 from the buffers as they were before this tick's diffusion,
+// exactly as in src/sim/step.cu:164-171, while the diffusion writes the other
+// ping-pong buffer.
 void tick_surrogate(agb_world* w, cudaStream_t s);
 
 void tick_once(agb_world* w, cudaStream_t s) {
@@ -259,6 +266,11 @@ void tick_once(agb_world* w, cudaStream_t s) {
     cudaStreamWaitEvent(s1, w->ev[0], 0);
     cudaStreamWaitEvent(s2, w->ev[0], 0);
     if (w->d.thermal_enabled) stage_thermal(w, s1);
+    const bool emit = emission_active(w);
+    if (emit) {
+        refresh_grid_ptrs(w);
+        launch_emission_prep(w->S, w->c, w->tp, w->stamp_idx, w->occl_factor, w->c.source > 0.0f, w->blocks, s1);
+    }
     cudaEventRecord(w->ev[1], s1);
     refresh_grid_ptrs(w);
     const Ctx pre = w->c;                       // CO2/N2 as motion must see them
@@ -266,7 +278,7 @@ void tick_once(agb_world* w, cudaStream_t s) {
     cudaEventRecord(w->ev[2], s2);
     stage_hash(w, s);
     cudaStreamWaitEvent(s, w->ev[1], 0);
-    if (w->d.emission_enabled) stage_emission(w, s);
+    if (emit) launch_feed(w->S, w->c, w->tp, w->blocks, s);
     if (w->d.taxis_enabled) launch_taxis(w->S, w->c, w->tp, w->blocks, s);   // step.cu:161-162
     {
         Ctx c = w->c;
