@@ -88,7 +88,9 @@ struct DevState {
     int32_t n_boundary_refine;  // counters of FP64 decision refinements (diagnostics)
     int32_t n_contact_refine;
     int32_t n_shadow_refine;
-    int32_t pad;
+    uint32_t fin_count;      // CTAs of the division pass that have finished (the last one finalises)
+    uint32_t scan_tile;      // next tile of the single-pass scan
+    uint32_t scan_done;      // CTAs of the single-pass scan that have finished (the last one resets)
 };
 
 // Immutable per-world constants, passed by value.

@@ -76,13 +76,26 @@ __device__ __forceinline__ bool ready_to_divide(const Ctx& c, const SoA& v, int3
     return v.co2_held[i] >= c.co2_quota;                    // lifecycle.cuh:33-36
 }
 
-__global__ void __launch_bounds__(256) death_mark_kernel(DevState* S, Ctx c, int32_t* divflag) {
+// Per cell, after uptake: the CO2 flush (flush_kernel restricted to the
+// voxels cells sit in, lifecycle.cu:235; it also clears the rationing
+// demand there) and death_kernel + mark_kernel (lifecycle.cu:90-134). The
+// flush reads only OCCUPIED, which death never changes, so the two share one
+// pass over the cells.
+__global__ void __launch_bounds__(256) death_mark_kernel(DevState* S, Ctx c, int32_t* divflag,
+                                                         unsigned long long* demand) {
     pdl_wait();
     const SoA v = S->cur;
     const int32_t n = S->count;
+    const GridDev C2 = c.g[AGB_FIELD_CO2];
     int32_t births = 0, deads = 0;
     AGB_FOR_CELLS(i, n) {
         uint32_t f = v.flags[i];
+        if (demand && (f & AGB_FLAG_OCCUPIED)) {
+            const int64_t idx = grid_nearest(C2, (float)v.x[i], (float)v.y[i], (float)v.z[i]);
+            const unsigned long long raw = atomicExch(&C2.deposit[idx], 0ull);
+            if (raw != 0ull) C2.value[idx] = fa(C2.value[idx], (float)(long long)raw * C2.inv_scale_f);
+            demand[idx] = 0ull;
+        }
         if ((f & AGB_FLAG_OCCUPIED) && (f & AGB_FLAG_ALIVE) && v.t_local[i] > c.lethal_f) {
             f &= ~AGB_FLAG_ALIVE;
             v.flags[i] = f;
@@ -116,83 +129,98 @@ __device__ __forceinline__ bool scan_gate(const DevState* S, int gate) {
     return gate == 0 ? S->births > 0 : S->compact_now != 0;
 }
 
-__global__ void __launch_bounds__(ST) scan_tiles_kernel(DevState* S, const int32_t* __restrict__ flag,
-                                                       int32_t* tile_sums, int gate) {
+constexpr uint32_t SCAN_AGG = 1u << 30, SCAN_PRE = 2u << 30, SCAN_VALUE = (1u << 30) - 1u;
+constexpr uint32_t SCAN_LOOKBACK_LIMIT = 1u << 24;
+
+// Single pass (decoupled look-back): a CTA takes the next 1024-element tile
+// (tiles are numbered in the order CTAs start, so every tile it waits on is
+// already running), scans it, publishes its total, takes the exclusive prefix
+// of the tiles before it from their published totals/prefixes and writes the
+// prefix. The last CTA to finish clears the status words and counters for
+// the next scan. gate 1 (compaction) also stores the grand total in S->live.
+// Waits are bounded; a timeout sets the error word.
+__global__ void __launch_bounds__(ST) scan_kernel(DevState* S, const int32_t* __restrict__ flag, int32_t* prefix,
+                                                 uint32_t* status, int gate) {
     pdl_wait();
-    if (!scan_gate(S, gate)) return;
+    if (!scan_gate(S, gate)) return;                     // uniform over the grid
+    __shared__ int32_t warp_tot[SITEMS][ST / 32];
+    __shared__ uint32_t tile_sh;
+    __shared__ int32_t excl_sh;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int32_t n = S->count;
-    const int64_t base = (int64_t)blockIdx.x * STILE;
-    int32_t s = 0;
-    for (int u = 0; u < SITEMS; ++u) {
-        const int64_t e = base + u * ST + threadIdx.x;
-        if (e < n) s += flag[e];
+    const int32_t ntiles = (n + STILE - 1) / STILE;
+    if (threadIdx.x == 0) tile_sh = atomicAdd(&S->scan_tile, 1u);
+    __syncthreads();
+    const int32_t tile = (int32_t)tile_sh;
+    if (tile < ntiles) {
+        const int64_t base = (int64_t)tile * STILE;
+        int32_t x[SITEMS], inc[SITEMS];
+        for (int u = 0; u < SITEMS; ++u) {
+            const int64_t e = base + u * ST + threadIdx.x;
+            x[u] = e < n ? flag[e] : 0;
+            int32_t v = x[u];
+            for (int o = 1; o < 32; o <<= 1) {
+                const int32_t y = __shfl_up_sync(0xFFFFFFFFu, v, o);
+                if (lane >= o) v += y;
+            }
+            inc[u] = v;
+            if (lane == 31) warp_tot[u][w] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int32_t agg = 0;
+            for (int u = 0; u < SITEMS; ++u)
+                for (int q = 0; q < ST / 32; ++q) agg += warp_tot[u][q];
+            int32_t excl = 0;
+            if (tile == 0) {
+                atomicExch(&status[0], SCAN_PRE | (uint32_t)agg);
+            } else {
+                atomicExch(&status[tile], SCAN_AGG | (uint32_t)agg);
+                bool ok = true;
+                for (int j = tile - 1; j >= 0;) {
+                    uint32_t vj = 0, it = 0;
+                    for (; it < SCAN_LOOKBACK_LIMIT; ++it) {
+                        vj = *(volatile const uint32_t*)&status[j];
+                        if (vj & (SCAN_AGG | SCAN_PRE)) break;
+                    }
+                    if (it == SCAN_LOOKBACK_LIMIT) { ok = false; set_error(S, 6u); break; }
+                    excl += (int32_t)(vj & SCAN_VALUE);
+                    if (vj & SCAN_PRE) break;
+                    --j;
+                }
+                if (ok) atomicExch(&status[tile], SCAN_PRE | (uint32_t)(excl + agg));
+            }
+            excl_sh = excl;
+            if (gate == 1 && tile == ntiles - 1) S->live = excl + agg;
+        }
+        __syncthreads();
+        int32_t run = excl_sh;
+        for (int u = 0; u < SITEMS; ++u) {
+            int32_t before = 0, round = 0;
+            for (int q = 0; q < ST / 32; ++q) {
+                if (q < w) before += warp_tot[u][q];
+                round += warp_tot[u][q];
+            }
+            const int64_t e = base + u * ST + threadIdx.x;
+            if (e < n) prefix[e] = run + before + inc[u] - x[u];
+            run += round;
+        }
     }
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xFFFFFFFFu, s, o);
-    __shared__ int32_t ws[ST / 32];
-    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    // The last CTA out resets the tile counter and the status words it used.
+    __shared__ int last;
     __syncthreads();
     if (threadIdx.x == 0) {
-        int32_t t = 0;
-        for (int w = 0; w < ST / 32; ++w) t += ws[w];
-        tile_sums[blockIdx.x] = t;
+        __threadfence();
+        last = atomicAdd(&S->scan_done, 1u) == gridDim.x - 1;
     }
-}
-
-__global__ void __launch_bounds__(1024) scan_top_kernel(DevState* S, int32_t* tile_sums, int32_t ntiles,
-                                                       int gate) {
-    pdl_wait();
-    if (!scan_gate(S, gate)) return;
-    __shared__ int32_t part[1024];
-    const int t = threadIdx.x;
-    const int per = (ntiles + 1023) / 1024;
-    const int b = t * per, e = b + per < ntiles ? b + per : ntiles;
-    int32_t s = 0;
-    for (int i = b; i < e; ++i) s += tile_sums[i];
-    part[t] = s;
     __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {
-        const int32_t x = t >= off ? part[t - off] : 0;
-        __syncthreads();
-        part[t] += x;
-        __syncthreads();
-    }
-    int32_t run = t > 0 ? part[t - 1] : 0;
-    for (int i = b; i < e; ++i) {
-        const int32_t x = tile_sums[i];
-        tile_sums[i] = run;
-        run += x;
-    }
-    if (t == 1023 && gate == 1) S->live = part[1023];
-}
-
-__global__ void __launch_bounds__(ST) scan_apply_kernel(DevState* S, const int32_t* __restrict__ flag,
-                                                       const int32_t* __restrict__ tile_sums, int32_t* prefix,
-                                                       int gate) {
-    pdl_wait();
-    if (!scan_gate(S, gate)) return;
-    const int32_t n = S->count;
-    __shared__ int32_t warp_tot[ST / 32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int32_t run = tile_sums[blockIdx.x];
-    const int64_t base = (int64_t)blockIdx.x * STILE;
-    for (int u = 0; u < SITEMS; ++u) {
-        const int64_t e = base + u * ST + threadIdx.x;
-        const int32_t x = e < n ? flag[e] : 0;
-        int32_t inc = x;
-        for (int o = 1; o < 32; o <<= 1) {
-            const int32_t y = __shfl_up_sync(0xFFFFFFFFu, inc, o);
-            if (lane >= o) inc += y;
+    if (last) {
+        for (int32_t j = threadIdx.x; j < ntiles; j += ST) status[j] = 0u;
+        if (threadIdx.x == 0) {
+            S->scan_tile = 0u;
+            S->scan_done = 0u;
         }
-        if (lane == 31) warp_tot[w] = inc;
-        __syncthreads();
-        int32_t before = 0, round = 0;
-        for (int q = 0; q < ST / 32; ++q) {
-            if (q < w) before += warp_tot[q];
-            round += warp_tot[q];
-        }
-        if (e < n) prefix[e] = run + before + inc - x;
-        run += round;
-        __syncthreads();
+        __threadfence();
     }
 }
 
@@ -200,16 +228,19 @@ __global__ void __launch_bounds__(ST) scan_apply_kernel(DevState* S, const int32
 // Division (divide_kernel, lifecycle.cu:140-204). Rare per cell, so the
 // placement arithmetic stays in FP64 exactly as the reference has it.
 // ---------------------------------------------------------------------------
+__device__ void life_finalize(DevState* S, int32_t capacity, int32_t compaction_allowed);
+
 __global__ void __launch_bounds__(256) divide_kernel(DevState* S, Ctx c, const int32_t* __restrict__ divflag,
-                                                     const int32_t* __restrict__ prefix) {
+                                                     const int32_t* __restrict__ prefix,
+                                                     int32_t compaction_allowed) {
     pdl_wait();
-    if (S->births <= 0) return;
+    const int32_t births_now = S->births;
     const SoA v = S->cur;
     const int32_t n = S->count;                 // base = old count
     const uint64_t first_id = S->next_id;
     const double a = AGB_CELL_RADIUS;
     const double hx = 0.5 * c.chamber_w - a, hy = 0.5 * c.chamber_h - a, hz = 0.5 * c.chamber_d - a;
-    AGB_FOR_CELLS(i, n) {
+    AGB_FOR_CELLS(i, births_now > 0 ? n : 0) {
         if (!divflag[i]) continue;
         const int32_t slot = n + prefix[i];
         if (slot >= c.capacity) continue;       // store full: skip, do not wrap
@@ -256,11 +287,21 @@ __global__ void __launch_bounds__(256) divide_kernel(DevState* S, Ctx c, const i
         v.co2_local[slot] = v.co2_local[i];
         v.n2_local[slot] = v.n2_local[i];
     }
+    // The last CTA to finish runs the tick's bookkeeping (every division of
+    // this pass has been written by then).
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&S->fin_count, 1u) == gridDim.x - 1) {
+            __threadfence();
+            life_finalize(S, c.capacity, compaction_allowed);
+            S->fin_count = 0u;
+        }
+    }
 }
 
 // The host bookkeeping of lifecycle_step (lifecycle.cu:250-293), on the device.
-__global__ void life_finalize_kernel(DevState* S, int32_t capacity, int32_t compaction_allowed) {
-    pdl_wait();
+__device__ void life_finalize(DevState* S, int32_t capacity, int32_t compaction_allowed) {
     int32_t births = S->births;
     const int32_t deads = S->deads;
     const int32_t n = S->count;
@@ -536,9 +577,7 @@ __global__ void spawn_finalize_kernel(DevState* S, int32_t count) {
 
 void launch_scan(DevState* S, const LifeBuffers& b, int32_t capacity, int gate, cudaStream_t s) {
     const int32_t ntiles = (capacity + STILE - 1) / STILE;
-    launch_k(scan_tiles_kernel, ntiles, ST, 0, s, S, b.flags, b.tile_sums, gate);
-    launch_k(scan_top_kernel, 1, 1024, 0, s, S, b.tile_sums, ntiles, gate);
-    launch_k(scan_apply_kernel, ntiles, ST, 0, s, S, b.flags, b.tile_sums, b.prefix, gate);
+    launch_k(scan_kernel, ntiles, ST, 0, s, S, b.flags, b.prefix, reinterpret_cast<uint32_t*>(b.tile_sums), gate);
 }
 
 void launch_compact_kernels(DevState* S, const LifeBuffers& b, int32_t capacity, int32_t blocks,
@@ -559,12 +598,11 @@ void launch_lifecycle(DevState* S, const Ctx& c, const TickParams& p, const Life
         const float inv_gv = (float)(1.0 / (C2.dx * C2.dx * C2.dz_eff));
         launch_k(demand_kernel, blocks, 256, 0, s, S, c, p, b.co2_demand, inv_gv);
         launch_k(uptake_kernel, blocks, 256, 0, s, S, c, p, b.co2_demand, inv_gv);
-        launch_flush_by_cells(S, C2, b.co2_demand, blocks, s);      // lifecycle.cu:235
     }
-    launch_k(death_mark_kernel, blocks, 256, 0, s, S, c, b.flags);
+    // CO2 flush (lifecycle.cu:235) fused with death and division marks.
+    launch_k(death_mark_kernel, blocks, 256, 0, s, S, c, b.flags, C2.enabled ? b.co2_demand : nullptr);
     launch_scan(S, b, c.capacity, 0, s);
-    launch_k(divide_kernel, blocks, 256, 0, s, S, c, b.flags, b.prefix);
-    launch_k(life_finalize_kernel, 1, 1, 0, s, S, c.capacity, compaction_allowed ? 1 : 0);
+    launch_k(divide_kernel, blocks, 256, 0, s, S, c, b.flags, b.prefix, compaction_allowed ? 1 : 0);
     // Compaction cannot run on this tick unless the host-side period allows it.
     if (compaction_allowed) launch_compact_kernels(S, b, c.capacity, blocks, s);
 }

@@ -626,6 +626,7 @@ agb_status agb_world_create(const agb_world_desc* d, agb_world** out) {
     cudaMemset(w->blob[0], 0, w->blob_bytes);
     cudaMemset(w->blob[1], 0, w->blob_bytes);
     cudaMemset(w->life.co2_demand, 0, 8 * (size_t)co2n);
+    cudaMemset(w->life.tile_sums, 0, 4 * (size_t)stiles);       // single-pass scan status words
     cudaMemset(w->stamp_idx, 0xFF, 4 * n);
     DevState st{};
     st.cur = carve(w->blob[0], cap);
