@@ -19,19 +19,32 @@ namespace {
 // ASTRO_FOR_EACH_NEIGHBOUR (src/sim/hash.cuh:88-111): buckets in z, y, x
 // order, entries in sorted order. The three x-adjacent buckets of a row are
 // consecutive keys, hence one contiguous run of the sorted arrays.
+//
+// skip_axis / skip_side (optional) drop the neighbour buckets one step along
+// that axis on that side: the feeding walk uses it for the downstream layer
+// under axis-aligned light, whose cells can only lie in the cell's shadow-free
+// half-space (see feed_kernel).
 template <class F>
-__device__ __forceinline__ void walk_neighbours(const HashDev& h, int32_t gx, int32_t gy, int32_t gz, F&& f) {
-    const int32_t xlo = gx > 0 ? gx - 1 : 0;
-    const int32_t nxr = (gx < h.nx - 1 ? gx + 1 : h.nx - 1) - xlo;
+__device__ __forceinline__ void walk_neighbours(const HashDev& h, int32_t gx, int32_t gy, int32_t gz, F&& f,
+                                                int skip_axis = -1, int skip_side = 0) {
+    int32_t xlo = gx > 0 ? gx - 1 : 0;
+    int32_t xhi = gx < h.nx - 1 ? gx + 1 : h.nx - 1;
+    if (skip_axis == 0) {
+        if (skip_side > 0) xhi = gx;
+        else xlo = gx;
+    }
+    const int32_t nxr = xhi - xlo;
     // All nine rows' bucket ranges are loaded before any entry is visited, so
     // the 27 table reads overlap instead of serialising row by row.
     int32_t lo[9], hi[9];
 #pragma unroll
     for (int r = 0; r < 9; ++r) {
-        const int32_t cz = gz + r / 3 - 1, cy = gy + r % 3 - 1;
+        const int32_t oz = r / 3 - 1, oy = r % 3 - 1;
+        const int32_t cz = gz + oz, cy = gy + oy;
         lo[r] = 0;
         hi[r] = 0;
         if (cz < 0 || cz >= h.nz || cy < 0 || cy >= h.ny) continue;
+        if ((skip_axis == 2 && oz == skip_side) || (skip_axis == 1 && oy == skip_side)) continue;
         const int32_t b0 = (cz * h.ny + cy) * h.nx + xlo;
         const int2 r0 = __ldg(&h.ranges[b0]);
         const int2 r1 = nxr >= 1 ? __ldg(&h.ranges[b0 + 1]) : make_int2(0, 0);
@@ -298,6 +311,17 @@ __global__ void __launch_bounds__(256) feed_kernel(DevState* S, Ctx c, TickParam
             unpack_bucket(me.w, gx, gy, gz);
             float open = 1.0f;
             int32_t refined = 0;
+            // Under axis-aligned light every cell of the next bucket layer
+            // downstream has `along` < 0 (it sits in this cell's shadow-free
+            // half-space) and leaves `open` unchanged; that layer is skipped
+            // when this cell is clear of its downstream bucket face by more
+            // than the FP32 offsets' error, so the product is unchanged.
+            int skip_axis = -1, skip_side = 0;
+            if (c.light_axis_exact >= 0) {
+                const float off = c.light_axis_exact == 0 ? me.x : (c.light_axis_exact == 1 ? me.y : me.z);
+                const float face = c.light_sign > 0 ? h.cellf - off : off;
+                if (face > 4.0e-6f * h.cellf) { skip_axis = c.light_axis_exact; skip_side = c.light_sign; }
+            }
             walk_neighbours(h, gx, gy, gz, [&](int32_t k, const float4& rk) {
                 if (k == ks) return;
                 float dx, dy, dz;
@@ -321,7 +345,7 @@ __global__ void __launch_bounds__(256) feed_kernel(DevState* S, Ctx c, TickParam
                 const double fr = shadow_fraction64(__dsub_rn(px, v.x[j]), __dsub_rn(py, v.y[j]),
                                                     __dsub_rn(pz, v.z[j]), c);
                 open *= (float)(1.0 - fr);
-            });
+            }, skip_axis, skip_side);
             if (refined) atomicAdd(&S->n_shadow_refine, refined);
             directional *= open;
         }

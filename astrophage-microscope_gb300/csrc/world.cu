@@ -164,6 +164,8 @@ void compute_light(agb_world* w) {
     const double comp = axis == 0 ? dx : (axis == 1 ? dy : dz);
     c.light_axis = axis;
     c.light_sign = comp >= 0.0 ? 1 : -1;
+    const int zeros = (c.lx == 0.0f) + (c.ly == 0.0f) + (c.lz == 0.0f);
+    c.light_axis_exact = zeros == 2 ? axis : -1;
     c.source = L.enabled ? L.irradiance : 0.0f;
     c.ambient_irr = L.ambient;
     const GridDev& I = c.g[AGB_FIELD_IRRADIANCE];

@@ -31,6 +31,7 @@ struct Ctx {
     float lx, ly, lz;          // unit light direction as float
     double ldx, ldy, ldz;      // ... and as double (reference normalize)
     int32_t light_axis, light_sign;
+    int32_t light_axis_exact;  // light exactly along light_axis (other components 0), else -1
     float source, ambient_irr;
     double face_area;
     long long stamp_alive, stamp_dead;   // fixed-point occlusion stamps
