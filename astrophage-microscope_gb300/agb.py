@@ -391,11 +391,21 @@ class World:
                     "import_cells")
 
     def export_cells(self, stream=None, into=None):
-        """Copy the population out; `into` reuses caller-owned (e.g. pinned) buffers."""
-        n = self.count(stream)
-        cells = into if (into is not None and into.n >= n) else CellArrays(n)
-        s = cells.struct()
+        """Copy the population out; `into` reuses caller-owned (e.g. pinned)
+        buffers in one call (their length bounds the copy; larger populations
+        get fresh arrays)."""
         cnt, nid = C.c_int32(), C.c_uint64()
+        if into is not None:
+            cap = len(into.a["id"])
+            s = into.struct()
+            self._check(self.lib.agb_world_export_cells(self.h, C.byref(s), cap, C.byref(cnt), C.byref(nid),
+                                                        _st(stream)), "export_cells")
+            if cnt.value <= cap:
+                into.n = cnt.value
+                return into, nid.value
+        n = self.count(stream)
+        cells = CellArrays(n)
+        s = cells.struct()
         self._check(self.lib.agb_world_export_cells(self.h, C.byref(s), n, C.byref(cnt), C.byref(nid),
                                                     _st(stream)), "export_cells")
         return cells, nid.value

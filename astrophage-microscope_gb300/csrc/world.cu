@@ -331,6 +331,80 @@ void invalidate_graphs(agb_world* w) {
     ++w->version;
 }
 
+// Host <-> device cell transfer through device-accessible host memory
+// (pinned, or any memory on a system where the GPU reads host page tables,
+// e.g. Grace over NVLink-C2C): one kernel gathers or scatters all 25 arrays
+// in contract layout, instead of 25 copies and a state round trip.
+struct HostCells { void* p[25]; };
+__constant__ uint8_t kElemDev[25] = {8, 4, 1, 8, 8, 8, 8, 8, 8, 8, 4, 4, 4, 4, 4, 8, 8, 4, 8, 4, 4, 4, 4, 4, 4};
+
+__device__ __forceinline__ void soa_ptrs_dev(const SoA& v, void* p[25]) {
+    p[0] = v.id; p[1] = v.flags; p[2] = v.death_cause; p[3] = v.x; p[4] = v.y; p[5] = v.z; p[6] = v.vx;
+    p[7] = v.vy; p[8] = v.vz; p[9] = v.energy; p[10] = v.temp_cell; p[11] = v.emit_power; p[12] = v.dir_x;
+    p[13] = v.dir_y; p[14] = v.dir_z; p[15] = v.biomass; p[16] = v.co2_held; p[17] = v.age_s;
+    p[18] = v.rng_state; p[19] = v.taxis_memory; p[20] = v.run_timer; p[21] = v.t_local;
+    p[22] = v.irradiance; p[23] = v.co2_local; p[24] = v.n2_local;
+}
+
+__device__ __forceinline__ void copy_elems(void* dst, const void* src, int e, int64_t n) {
+    const int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, st = (int64_t)gridDim.x * blockDim.x;
+    if (e == 8) for (int64_t i = t0; i < n; i += st) static_cast<uint64_t*>(dst)[i] = static_cast<const uint64_t*>(src)[i];
+    else if (e == 4) for (int64_t i = t0; i < n; i += st) static_cast<uint32_t*>(dst)[i] = static_cast<const uint32_t*>(src)[i];
+    else for (int64_t i = t0; i < n; i += st) static_cast<uint8_t*>(dst)[i] = static_cast<const uint8_t*>(src)[i];
+}
+
+__global__ void __launch_bounds__(256) cells_import_kernel(DevState* S, HostCells h, int32_t count,
+                                                           uint64_t next_id) {
+    void* d[25];
+    soa_ptrs_dev(S->cur, d);
+#pragma unroll 1
+    for (int k = 0; k < 25; ++k)
+        if (h.p[k]) copy_elems(d[k], h.p[k], kElemDev[k], count);
+    if (blockIdx.x == 0 && threadIdx.x == 0) { S->count = count; S->next_id = next_id; }
+}
+
+__global__ void __launch_bounds__(256) cells_export_kernel(DevState* S, HostCells h, int32_t max_count,
+                                                           int64_t* out) {
+    void* d[25];
+    soa_ptrs_dev(S->cur, d);
+    const int32_t n = S->count < max_count ? S->count : max_count;
+#pragma unroll 1
+    for (int k = 0; k < 25; ++k)
+        if (h.p[k]) copy_elems(h.p[k], d[k], kElemDev[k], n);
+    if (blockIdx.x == 0 && threadIdx.x == 0) { out[0] = S->count; out[1] = (int64_t)S->next_id; }
+}
+
+// True when the GPU can address every non-null host array directly and each
+// is aligned to its element size (the kernels move whole elements; arrays
+// packed end to end, as in a snapshot body, can start mid-element and take
+// the copy path). The answer for the last pointer set is cached (a loop
+// passes the same buffers).
+bool host_cells_direct(agb_world* w, void* const hst[25]) {
+    for (int k = 0; k < 25; ++k)
+        if (hst[k] && (reinterpret_cast<uintptr_t>(hst[k]) % kElem[k]) != 0) return false;
+    bool same = true;
+    for (int k = 0; k < 25; ++k) same = same && w->direct_ptrs[k] == hst[k];
+    if (same) return w->direct_ok;
+    static int pageable = -1;
+    if (pageable < 0) {
+        int a = 0, b = 0;
+        cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, w->dev);
+        cudaDeviceGetAttribute(&b, cudaDevAttrPageableMemoryAccessUsesHostPageTables, w->dev);
+        pageable = (a && b) ? 1 : 0;
+    }
+    bool ok = true;
+    for (int k = 0; k < 25 && ok; ++k) {
+        if (!hst[k]) continue;
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, hst[k]) != cudaSuccess) { cudaGetLastError(); ok = false; break; }
+        ok = at.type == cudaMemoryTypeHost || at.type == cudaMemoryTypeManaged ||
+             (at.type == cudaMemoryTypeUnregistered && pageable == 1);
+    }
+    for (int k = 0; k < 25; ++k) w->direct_ptrs[k] = hst[k];
+    w->direct_ok = ok;
+    return ok;
+}
+
 agb_status read_state(agb_world* w, DevState& out, cudaStream_t s) {
     AGB_CUDA(w, cudaMemcpyAsync(&out, w->S, sizeof(DevState), cudaMemcpyDeviceToHost, s));
     AGB_CUDA(w, cudaStreamSynchronize(s));
@@ -477,6 +551,7 @@ void agb_world_destroy(agb_world* w) {
     for (cudaStream_t& st : w->side) if (st) cudaStreamDestroy(st);
     for (cudaEvent_t& e : w->ev) if (e) cudaEventDestroy(e);
     for (void* p : w->allocs) cudaFree(p);
+    if (w->xfer_host) cudaFreeHost(w->xfer_host);
     delete w;
 }
 
@@ -630,6 +705,9 @@ agb_status agb_world_create(const agb_world_desc* d, agb_world** out) {
     cudaMemset(w->life.co2_demand, 0, 8 * (size_t)co2n);
     cudaMemset(w->life.tile_sums, 0, 4 * (size_t)stiles);       // single-pass scan status words
     cudaMemset(w->stamp_idx, 0xFF, 4 * n);
+    if (cudaHostAlloc(reinterpret_cast<void**>(&w->xfer_host), 2 * sizeof(int64_t), cudaHostAllocMapped) !=
+        cudaSuccess)
+        w->xfer_host = nullptr;                           // export then takes the copy path
     DevState st{};
     st.cur = carve(w->blob[0], cap);
     st.spare = carve(w->blob[1], cap);
@@ -683,13 +761,25 @@ agb_status agb_world_import_cells(agb_world* w, const agb_cells* src, int32_t co
                                   agb_stream s) {
     if (!w || !src || count < 0) return AGB_INVALID_ARGUMENT;
     if (count > w->c.capacity) return fail(w, AGB_CAPACITY_EXCEEDED, "import exceeds capacity");
+    void* hst[25];
+    host_arrays(src, hst);
+    if (host_cells_direct(w, hst)) {
+        // One gather kernel; the stream's later work sees the cells. The host
+        // arrays must stay valid until the stream reaches it (NULL stream: on return).
+        HostCells h;
+        for (int k = 0; k < 25; ++k) h.p[k] = hst[k];
+        const int64_t blocks = ((int64_t)count + 255) / 256;
+        cells_import_kernel<<<(unsigned)(blocks < 1 ? 1 : (blocks > 4096 ? 4096 : blocks)), 256, 0, s>>>(
+            w->S, h, count, next_id);
+        AGB_CUDA(w, cudaGetLastError());
+        if (s == nullptr) AGB_CUDA(w, cudaStreamSynchronize(s));
+        return AGB_OK;
+    }
     DevState st;
     agb_status rc = read_state(w, st, s);
     if (rc) return rc;
     void* dst[25];
-    void* hst[25];
     soa_arrays(st.cur, dst);
-    host_arrays(src, hst);
     for (int k = 0; k < 25; ++k)
         if (hst[k] && count > 0)
             AGB_CUDA(w, cudaMemcpyAsync(dst[k], hst[k], kElem[k] * (size_t)count, cudaMemcpyHostToDevice, s));
@@ -704,14 +794,28 @@ agb_status agb_world_import_cells(agb_world* w, const agb_cells* src, int32_t co
 agb_status agb_world_export_cells(agb_world* w, agb_cells* dst, int32_t max_count, int32_t* count,
                                   uint64_t* next_id, agb_stream s) {
     if (!w || !dst) return AGB_INVALID_ARGUMENT;
+    void* hst[25];
+    host_arrays(dst, hst);
+    if (max_count < 0) max_count = 0;
+    if (w->xfer_host && host_cells_direct(w, hst)) {
+        // One scatter kernel writes the arrays and the count; one synchronisation.
+        HostCells h;
+        for (int k = 0; k < 25; ++k) h.p[k] = hst[k];
+        const int64_t blocks = ((int64_t)w->c.capacity + 255) / 256;
+        cells_export_kernel<<<(unsigned)(blocks < 1 ? 1 : (blocks > 4096 ? 4096 : blocks)), 256, 0, s>>>(
+            w->S, h, max_count, w->xfer_host);
+        AGB_CUDA(w, cudaGetLastError());
+        AGB_CUDA(w, cudaStreamSynchronize(s));
+        if (count) *count = (int32_t)w->xfer_host[0];
+        if (next_id) *next_id = (uint64_t)w->xfer_host[1];
+        return AGB_OK;
+    }
     DevState st;
     agb_status rc = read_state(w, st, s);
     if (rc) return rc;
     const int32_t n = st.count < max_count ? st.count : max_count;
     void* srcp[25];
-    void* hst[25];
     soa_arrays(st.cur, srcp);
-    host_arrays(dst, hst);
     for (int k = 0; k < 25; ++k)
         if (hst[k] && n > 0)
             AGB_CUDA(w, cudaMemcpyAsync(hst[k], srcp[k], kElem[k] * (size_t)n, cudaMemcpyDeviceToHost, s));

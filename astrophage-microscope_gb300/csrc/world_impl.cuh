@@ -57,6 +57,9 @@ struct agb_world {
     cudaStream_t own_stream = nullptr;   // capture stream when the caller passes the default stream
     int64_t graph_kernels_total = 0;     // kernel nodes launched by graph replays so far
     uint64_t version = 0;                // bumped whenever captured graphs go stale
+    int64_t* xfer_host = nullptr;        // pinned {count, next_id} written by the export kernel
+    const void* direct_ptrs[25] = {};    // host arrays last checked as device-accessible
+    bool direct_ok = false;
     agb_surrogate* sg = nullptr;         // learned field surrogate driving T and CO2, if attached
     int32_t sg_steps = 0;
     float* sg_q = nullptr;               // per-step heat source of the current window (K)
