@@ -114,6 +114,7 @@ struct HashDev {
     uint32_t* vals_sorted;
     uint32_t* keys_prev;     // sorted keys of the previous build (ranges to clear)
     int2* ranges;            // dense bucket table {start, end}
+    uint32_t* occ;           // one bit per bucket: occupied in the current build
     float4* rec;             // sorted-order snapshot: offsets from the bucket corner + packed bucket coords
     int32_t fix_k;           // fixed-point exponent K of the corner arithmetic
     float fix_inv_f;         // 2^-K

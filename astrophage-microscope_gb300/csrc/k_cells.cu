@@ -46,9 +46,15 @@ __device__ __forceinline__ void walk_neighbours(const HashDev& h, int32_t gx, in
         if (cz < 0 || cz >= h.nz || cy < 0 || cy >= h.ny) continue;
         if ((skip_axis == 2 && oz == skip_side) || (skip_axis == 1 && oy == skip_side)) continue;
         const int32_t b0 = (cz * h.ny + cy) * h.nx + xlo;
-        const int2 r0 = __ldg(&h.ranges[b0]);
-        const int2 r1 = nxr >= 1 ? __ldg(&h.ranges[b0 + 1]) : make_int2(0, 0);
-        const int2 r2 = nxr >= 2 ? __ldg(&h.ranges[b0 + 2]) : make_int2(0, 0);
+        // The occupancy bits of the row's 1-3 buckets (one 64-bit window over
+        // the bitmap, which stays cache-resident) decide which ranges to load.
+        const uint32_t wi = (uint32_t)b0 >> 5, sh = (uint32_t)b0 & 31u;
+        const uint64_t win = ((uint64_t)__ldg(&h.occ[wi + 1]) << 32) | __ldg(&h.occ[wi]);
+        const uint32_t bits = (uint32_t)(win >> sh) & ((2u << nxr) - 1u);
+        if (bits == 0u) continue;
+        const int2 r0 = (bits & 1u) ? __ldg(&h.ranges[b0]) : make_int2(0, 0);
+        const int2 r1 = (bits & 2u) ? __ldg(&h.ranges[b0 + 1]) : make_int2(0, 0);
+        const int2 r2 = (bits & 4u) ? __ldg(&h.ranges[b0 + 2]) : make_int2(0, 0);
         int32_t l = 0, e = 0;
         bool found = false;
         if (r0.y > r0.x) { l = r0.x; e = r0.y; found = true; }

@@ -166,7 +166,10 @@ __global__ void __launch_bounds__(256) key_hist_kernel(DevState* S, HashDev h, u
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
         if (i < nprev) {
             const uint32_t old = h.keys_sorted[i];
-            if (old < (uint32_t)h.buckets) h.ranges[old] = make_int2(0, 0);
+            if (old < (uint32_t)h.buckets) {
+                h.ranges[old] = make_int2(0, 0);
+                if (i == 0 || h.keys_sorted[i - 1] != old) atomicAnd(&h.occ[old >> 5], ~(1u << (old & 31u)));
+            }
         }
         if (i < n) {
             h.vals[i] = (uint32_t)i;
@@ -197,7 +200,10 @@ __global__ void ranges_kernel(DevState* S, HashDev h) {
         const uint32_t key = h.keys_sorted[k];
         const uint32_t slot = h.vals_sorted[k];
         if (key < (uint32_t)h.buckets) {
-            if (k == 0 || h.keys_sorted[k - 1] != key) h.ranges[key].x = k;
+            if (k == 0 || h.keys_sorted[k - 1] != key) {
+                h.ranges[key].x = k;
+                atomicOr(&h.occ[key >> 5], 1u << (key & 31u));
+            }
             if (k == n - 1 || h.keys_sorted[k + 1] != key) h.ranges[key].y = k + 1;
         }
         // Offsets from the bucket's corner, formed exactly in fixed point and

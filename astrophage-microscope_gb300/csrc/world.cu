@@ -678,6 +678,7 @@ agb_status agb_world_create(const agb_world_desc* d, agb_world** out) {
               dalloc(w, &w->kalt, 4 * n) == cudaSuccess && dalloc(w, &w->valt, 4 * n) == cudaSuccess &&
               dalloc(w, &w->hist, 4 * hash_sort_scratch_words(cap)) == cudaSuccess &&
               dalloc(w, &h.ranges, 8 * (size_t)h.buckets) == cudaSuccess &&
+              dalloc(w, &h.occ, 4 * (((size_t)h.buckets + 31) / 32 + 1)) == cudaSuccess &&
               dalloc(w, &h.rec, 16 * n) == cudaSuccess;
     h.keys_prev = nullptr;
     // Cells: two SoA blobs (live + compaction target).
@@ -699,6 +700,7 @@ agb_status agb_world_create(const agb_world_desc* d, agb_world** out) {
     ok = ok && dalloc(w, &w->life.co2_demand, 8 * (size_t)co2n) == cudaSuccess;
     if (!ok) { agb_world_destroy(w); return AGB_OUT_OF_MEMORY; }
     cudaMemset(h.ranges, 0, 8 * (size_t)h.buckets);
+    cudaMemset(h.occ, 0, 4 * (((size_t)h.buckets + 31) / 32 + 1));
     cudaMemset(h.keys_sorted, 0, 4 * n);
     cudaMemset(w->blob[0], 0, w->blob_bytes);
     cudaMemset(w->blob[1], 0, w->blob_bytes);
