@@ -510,6 +510,8 @@ def main():
                     help="timed steps of the batched ensemble reported beside the plain step (0: skip)")
     ap.add_argument("--batch-chambers", type=int, default=64)
     ap.add_argument("--batch-lanes", type=int, default=0)
+    ap.add_argument("--batch-only", action="store_true",
+                    help="run only the batched ensemble and print its result (profiling)")
     ap.add_argument("--surrogate-windows", type=int, default=1500,
                     help="training windows of the learned field surrogate (0: skip the surrogate leg)")
     ap.add_argument("--surrogate-windows-run", type=int, default=16)
@@ -526,6 +528,12 @@ def main():
 
     if args.impl == "reference":
         return run_reference(args, workload(args.workload, seed=1))
+    if args.batch_only:
+        import torch
+        stream = torch.cuda.Stream()
+        l2_flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+        print(json.dumps(run_batch(args, stream, l2_flush)))
+        return 0
 
     import torch
     rank, ws, local, dist = dist_init()
