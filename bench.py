@@ -168,7 +168,10 @@ def run_batch(args, stream, l2_flush):
         t = b.tuning(i).as_dict()
         classes.setdefault(t["size_class"], {"hash_cell_um": round(t["hash_cell_size"] * 1e6, 2),
                                              "ftcs_T": t["ftcs"][0], "chambers": 0})["chambers"] += 1
-    out = {"cell_steps_per_s": 0.5 * (n0 + n1) * args.batch_steps / total_s,
+    peak, _kind = measured_peaks()
+    out = {"roofline_step": step_roofline(0.5 * (n0 + n1) * args.batch_steps / total_s,
+                                          vox * args.batch_steps / total_s, peak),
+           "cell_steps_per_s": 0.5 * (n0 + n1) * args.batch_steps / total_s,
            "voxel_steps_per_s": vox * args.batch_steps / total_s,
            "ms_per_step": total_s * 1e3 / args.batch_steps, "steps": args.batch_steps,
            "cells_start_end": [n0, n1], "gpu_launches": launches, "setup_s": setup_s,
@@ -273,6 +276,19 @@ def run_surrogate(args, stream):
     w.close()
     sg.close()
     return out
+
+
+CELL_STEP_BYTES = 200.0       # algorithmic bytes of one cell-step (state read + written, key, sort, ranges)
+VOXEL_STEP_BYTES = 8.0        # one FTCS pass over one FP32 voxel (read + write)
+
+
+def step_roofline(cell_steps_per_s, voxel_steps_per_s, peak):
+    """Whole-step HBM roofline: (cell-steps x 200 B + voxel-steps x 8 B) per
+    second against the measured copy bandwidth (moved cells of divisions and
+    compactions are not counted)."""
+    gbs = (cell_steps_per_s * CELL_STEP_BYTES + voxel_steps_per_s * VOXEL_STEP_BYTES) / 1e9
+    return {"achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+            "formula": "(cell_steps/s * 200 B + voxel_steps/s * 8 B) / peak"}
 
 
 def substeps(desc, f):
@@ -669,6 +685,7 @@ def main():
                            **info),
             "voxel_steps_per_s": vox_steps / total_s,
             "cells_start_end": [n_start, n_end],
+            "roofline_step": step_roofline(value, vox_steps / total_s, peak),
             "roofline": {"bound": "hbm", "kernel": "ftcs3d (temperature, %d^3)" % gT.nx,
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_source": peak_kind, "algorithmic_bytes_per_launch": algo_bytes,
