@@ -136,10 +136,17 @@ def batch_workload(n=64, seed=1):
     return descs, spawns, info
 
 
-def run_batch(args, stream, l2_flush):
-    """Time the batched ensemble: one graph launch per step for all chambers."""
+def run_batch(args, stream, l2_flush, dist=None, rank=0, ws=1):
+    """Time the batched ensemble: one graph launch per step for all chambers.
+    With several ranks the chambers are sharded (heaviest first onto the
+    least-loaded rank); the rate is the sum over ranks over the slowest rank."""
     import torch
     descs, spawns, info = batch_workload(args.batch_chambers, seed=1)
+    if ws > 1:
+        costs = [sp.count * 200.0 + 8.0 * voxel_steps_per_tick(d) for d, sp in zip(descs, spawns)]
+        mine = MR.lpt_shards(costs, ws)[rank]
+        descs = [descs[i] for i in mine]
+        spawns = [spawns[i] for i in mine]
     t0 = time.perf_counter()
     b = agb.Batch(descs, spawns, agb.batch_opts(autotune=True, lanes=args.batch_lanes))
     setup_s = time.perf_counter() - t0
@@ -161,8 +168,10 @@ def run_batch(args, stream, l2_flush):
         torch.cuda.synchronize()
         n1 = sum(c.count() for c in b.chambers)
         launches = b.graph_kernels() - k0
-    total_s = sum(a.elapsed_time(z) for a, z in ms) / 1e3
-    vox = sum(voxel_steps_per_tick(d) for d in descs)
+    total_s = MR.reduce_max(dist, sum(a.elapsed_time(z) for a, z in ms) / 1e3)
+    vox = MR.reduce_sum(dist, sum(voxel_steps_per_tick(d) for d in descs))
+    n0 = MR.reduce_sum(dist, n0)
+    n1 = MR.reduce_sum(dist, n1)
     classes = {}
     for i in range(b.n):
         t = b.tuning(i).as_dict()
@@ -398,22 +407,24 @@ def dist_init():
     return rank, ws, local, None
 
 
+def _load_multirank():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "multirank", os.path.join(ROOT, "astrophage-microscope_gb300", "multirank.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+MR = _load_multirank()
+
+
 def allreduce_max(dist, v):
-    if dist is None:
-        return v
-    import torch
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    return MR.reduce_max(dist, v)
 
 
 def allreduce_sum(dist, v):
-    if dist is None:
-        return v
-    import torch
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    return MR.reduce_sum(dist, v)
 
 
 # ---------------------------------------------------------------------------
@@ -656,9 +667,9 @@ def main():
                "path": "agb_world_import_cells + agb_world_step_graph + agb_world_export_cells, pinned host SoA"}
 
     batched = None
-    if rank == 0 and args.batch_steps > 0:
+    if args.batch_steps > 0:
         world.close()
-        batched = run_batch(args, stream, l2_flush)
+        batched = run_batch(args, stream, l2_flush, dist, rank, ws)
 
     surrogate = None
     if rank == 0 and args.surrogate_windows > 0:
