@@ -264,6 +264,8 @@ def load(path=LIB_PATH):
         "agb_world_import_cells": (I32, [P, C.POINTER(Cells), I32, U64, P]),
         "agb_world_export_cells": (I32, [P, C.POINTER(Cells), I32, C.POINTER(I32), C.POINTER(U64), P]),
         "agb_world_device_cells": (I32, [P, C.POINTER(Cells)]),
+        "agb_world_step_host": (I32, [P, C.POINTER(Cells), I32, U64, I32, C.POINTER(Cells), I32, C.POINTER(I32),
+                                      C.POINTER(U64), P]),
         "agb_world_count": (I32, [P, C.POINTER(I32), P]),
         "agb_world_import_field": (I32, [P, I32, P, P]),
         "agb_world_export_field": (I32, [P, I32, P, P]),
@@ -325,7 +327,7 @@ def exported_symbols():
     """Names declared in include/agb.h, for the symbol-export test."""
     return ["agb_world_desc_default", "agb_status_str", "agb_last_error", "agb_device_info",
             "agb_world_create", "agb_world_destroy", "agb_world_spawn", "agb_world_import_cells",
-            "agb_world_export_cells", "agb_world_device_cells", "agb_world_count",
+            "agb_world_export_cells", "agb_world_device_cells", "agb_world_step_host", "agb_world_count",
             "agb_world_import_field", "agb_world_export_field", "agb_world_export_deposit",
             "agb_world_step", "agb_world_step_graph", "agb_world_graph_kernels", "agb_world_stage",
             "agb_world_diffuse",
@@ -409,6 +411,20 @@ class World:
         self._check(self.lib.agb_world_export_cells(self.h, C.byref(s), n, C.byref(cnt), C.byref(nid),
                                                     _st(stream)), "export_cells")
         return cells, nid.value
+
+    def step_host(self, cells_in, next_id, ticks=1, into=None, stream=None):
+        """Import host cells, run `ticks` ticks, export into `into` (default:
+        the input buffers): one engine call and one synchronisation."""
+        out = into if into is not None else cells_in
+        si, so = cells_in.struct(), out.struct()
+        cnt, nid = C.c_int32(), C.c_uint64()
+        self._check(self.lib.agb_world_step_host(self.h, C.byref(si), cells_in.n, next_id, ticks, C.byref(so),
+                                                 len(out.a["id"]), C.byref(cnt), C.byref(nid), _st(stream)),
+                    "step_host")
+        if cnt.value > len(out.a["id"]):
+            raise AgbError("step_host: population %d exceeds the output buffers" % cnt.value)
+        out.n = cnt.value
+        return out, nid.value
 
     def count(self, stream=None):
         c = C.c_int32()

@@ -353,6 +353,8 @@ __device__ __forceinline__ void copy_elems(void* dst, const void* src, int e, in
     else for (int64_t i = t0; i < n; i += st) static_cast<uint8_t*>(dst)[i] = static_cast<const uint8_t*>(src)[i];
 }
 
+// All threads walk the 25 arrays in the same order, so the host link sees one
+// array's pages at a time.
 __global__ void __launch_bounds__(256) cells_import_kernel(DevState* S, HostCells h, int32_t count,
                                                            uint64_t next_id) {
     void* d[25];
@@ -803,7 +805,8 @@ agb_status agb_world_export_cells(agb_world* w, agb_cells* dst, int32_t max_coun
         // One scatter kernel writes the arrays and the count; one synchronisation.
         HostCells h;
         for (int k = 0; k < 25; ++k) h.p[k] = hst[k];
-        const int64_t blocks = ((int64_t)w->c.capacity + 255) / 256;
+        const int64_t cap = max_count < w->c.capacity ? max_count : w->c.capacity;
+        const int64_t blocks = (cap + 255) / 256;
         cells_export_kernel<<<(unsigned)(blocks < 1 ? 1 : (blocks > 4096 ? 4096 : blocks)), 256, 0, s>>>(
             w->S, h, max_count, w->xfer_host);
         AGB_CUDA(w, cudaGetLastError());
@@ -825,6 +828,24 @@ agb_status agb_world_export_cells(agb_world* w, agb_cells* dst, int32_t max_coun
     if (count) *count = st.count;
     if (next_id) *next_id = st.next_id;
     return AGB_OK;
+}
+
+agb_status agb_world_step_host(agb_world* w, const agb_cells* in, int32_t count, uint64_t next_id,
+                               int32_t ticks, agb_cells* out, int32_t max_out, int32_t* out_count,
+                               uint64_t* out_next_id, agb_stream s) {
+    if (!w || !in || !out || ticks < 0) return AGB_INVALID_ARGUMENT;
+    if (s == nullptr && ticks > 0 && !w->sg) {
+        // The tick graph needs a capture-capable stream; run all three on it.
+        if (!w->own_stream) AGB_CUDA(w, cudaStreamCreate(&w->own_stream));
+        s = w->own_stream;
+    }
+    agb_status rc = agb_world_import_cells(w, in, count, next_id, s);
+    if (rc != AGB_OK) return rc;
+    if (ticks > 0) {
+        rc = agb_world_step_graph(w, ticks, s);
+        if (rc != AGB_OK) return rc;
+    }
+    return agb_world_export_cells(w, out, max_out, out_count, out_next_id, s);
 }
 
 agb_status agb_world_import_field(agb_world* w, int32_t f, const float* src, agb_stream s) {

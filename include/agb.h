@@ -325,6 +325,14 @@ agb_status agb_world_export_cells(agb_world* w, agb_cells* dst, int32_t max_coun
                                   int32_t* count, uint64_t* next_id, agb_stream s);
 /* Device pointers of the SoA (the reference's CellStore::view); count via agb_world_count. */
 agb_status agb_world_device_cells(agb_world* w, agb_cells* dev);
+/* One call per host-driven step: import `count` cells from host arrays, run
+ * `ticks` ticks (one graph launch), export into host arrays (at most max_out
+ * per array) and synchronise once. With device-accessible host arrays
+ * (pinned, or host page tables) both transfers are single kernels over the
+ * host link. */
+agb_status agb_world_step_host(agb_world* w, const agb_cells* in, int32_t count, uint64_t next_id,
+                               int32_t ticks, agb_cells* out, int32_t max_out, int32_t* out_count,
+                               uint64_t* out_next_id, agb_stream s);
 agb_status agb_world_count(agb_world* w, int32_t* count, agb_stream s);
 
 /* Field values, nx*ny*nz floats, x fastest (reference: [x + n*y]). */

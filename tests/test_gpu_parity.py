@@ -252,3 +252,19 @@ def test_cell_transfer_paths_agree():
     assert nid3 == nid and back.n == n
     for name, _t in agb.CELL_FIELDS:
         assert np.array_equal(back[name], plain[name]), name
+
+
+def test_step_host_equals_separate_calls():
+    """agb_world_step_host (import, graph ticks, export, one sync) gives the
+    same cells as import_cells + step + export_cells."""
+    sc = S.scenarios()["slab_uniform"]
+    a, _ = seeded(sc)
+    b, _ = seeded(sc)
+    cells, nid = a.export_cells()
+    a.import_cells(cells, nid)
+    a.step(2, graph=True)
+    want, nid_a = a.export_cells()
+    out, nid_b = b.step_host(cells.copy(), nid, 2, into=agb.CellArrays(cells.n + 64))
+    assert nid_b == nid_a and out.n == want.n
+    for name, _t in agb.CELL_FIELDS:
+        assert np.array_equal(out[name], want[name]), name
