@@ -194,9 +194,18 @@ class CellArrays:
         self.a = {name: np.zeros(max(n, 1), dtype=t) for name, t in CELL_FIELDS}
 
     def struct(self):
+        """The agb_cells view of the arrays. Building it costs tens of
+        microseconds (25 ctypes pointer casts), so it is kept while the same
+        array objects stay in `a`; the kept references also stop a replaced
+        array's id from being reused by a new one."""
+        arrs = [self.a[name] for name, _t in CELL_FIELDS]
+        held = getattr(self, "_struct_arrays", None)
+        if held is not None and all(x is y for x, y in zip(held, arrs)):
+            return self._struct
         c = Cells()
-        for name, t in CELL_FIELDS:
-            setattr(c, name, self.a[name].ctypes.data_as(C.POINTER(_CT[t])))
+        for (name, t), arr in zip(CELL_FIELDS, arrs):
+            setattr(c, name, arr.ctypes.data_as(C.POINTER(_CT[t])))
+        self._struct, self._struct_arrays = c, arrs
         return c
 
     def __getitem__(self, k):

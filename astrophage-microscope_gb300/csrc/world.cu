@@ -336,7 +336,6 @@ void invalidate_graphs(agb_world* w) {
 // e.g. Grace over NVLink-C2C): one kernel gathers or scatters all 25 arrays
 // in contract layout, instead of 25 copies and a state round trip.
 struct HostCells { void* p[25]; };
-__constant__ uint8_t kElemDev[25] = {8, 4, 1, 8, 8, 8, 8, 8, 8, 8, 4, 4, 4, 4, 4, 8, 8, 4, 8, 4, 4, 4, 4, 4, 4};
 
 __device__ __forceinline__ void soa_ptrs_dev(const SoA& v, void* p[25]) {
     p[0] = v.id; p[1] = v.flags; p[2] = v.death_cause; p[3] = v.x; p[4] = v.y; p[5] = v.z; p[6] = v.vx;
@@ -346,34 +345,59 @@ __device__ __forceinline__ void soa_ptrs_dev(const SoA& v, void* p[25]) {
     p[22] = v.irradiance; p[23] = v.co2_local; p[24] = v.n2_local;
 }
 
-__device__ __forceinline__ void copy_elems(void* dst, const void* src, int e, int64_t n) {
-    const int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, st = (int64_t)gridDim.x * blockDim.x;
-    if (e == 8) for (int64_t i = t0; i < n; i += st) static_cast<uint64_t*>(dst)[i] = static_cast<const uint64_t*>(src)[i];
-    else if (e == 4) for (int64_t i = t0; i < n; i += st) static_cast<uint32_t*>(dst)[i] = static_cast<const uint32_t*>(src)[i];
-    else for (int64_t i = t0; i < n; i += st) static_cast<uint8_t*>(dst)[i] = static_cast<const uint8_t*>(src)[i];
+// One thread per cell: every load of the cell's 25 elements is issued before
+// the first store, so each thread keeps up to 25 requests in flight over the
+// host link instead of one round trip per array. Null `pres` entries (arrays
+// the caller left out) are skipped.
+__device__ __forceinline__ void move_cell(void* const* dst, const void* const* src, const void* const* pres,
+                                          int64_t i) {
+    constexpr uint8_t E[25] = {8, 4, 1, 8, 8, 8, 8, 8, 8, 8, 4, 4, 4, 4, 4, 8, 8, 4, 8, 4, 4, 4, 4, 4, 4};
+    uint64_t v[25];
+#pragma unroll
+    for (int k = 0; k < 25; ++k) {
+        v[k] = 0;
+        if (pres[k]) {
+            if (E[k] == 8) v[k] = static_cast<const uint64_t*>(src[k])[i];
+            else if (E[k] == 4) v[k] = static_cast<const uint32_t*>(src[k])[i];
+            else v[k] = static_cast<const uint8_t*>(src[k])[i];
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 25; ++k) {
+        if (pres[k]) {
+            if (E[k] == 8) static_cast<uint64_t*>(dst[k])[i] = v[k];
+            else if (E[k] == 4) static_cast<uint32_t*>(dst[k])[i] = (uint32_t)v[k];
+            else static_cast<uint8_t*>(dst[k])[i] = (uint8_t)v[k];
+        }
+    }
 }
 
-// All threads walk the 25 arrays in the same order, so the host link sees one
-// array's pages at a time.
-__global__ void __launch_bounds__(256) cells_import_kernel(DevState* S, HostCells h, int32_t count,
-                                                           uint64_t next_id) {
+constexpr int kXferThreads = 128;
+
+__global__ void __launch_bounds__(kXferThreads) cells_import_kernel(DevState* S, HostCells h, int32_t count,
+                                                                    uint64_t next_id) {
     void* d[25];
     soa_ptrs_dev(S->cur, d);
-#pragma unroll 1
-    for (int k = 0; k < 25; ++k)
-        if (h.p[k]) copy_elems(d[k], h.p[k], kElemDev[k], count);
+    const int64_t st = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += st)
+        move_cell(d, h.p, h.p, i);
     if (blockIdx.x == 0 && threadIdx.x == 0) { S->count = count; S->next_id = next_id; }
 }
 
-__global__ void __launch_bounds__(256) cells_export_kernel(DevState* S, HostCells h, int32_t max_count,
-                                                           int64_t* out) {
+__global__ void __launch_bounds__(kXferThreads) cells_export_kernel(DevState* S, HostCells h, int32_t max_count,
+                                                                    int64_t* out) {
     void* d[25];
     soa_ptrs_dev(S->cur, d);
     const int32_t n = S->count < max_count ? S->count : max_count;
-#pragma unroll 1
-    for (int k = 0; k < 25; ++k)
-        if (h.p[k]) copy_elems(h.p[k], d[k], kElemDev[k], n);
+    const int64_t st = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += st)
+        move_cell(h.p, d, h.p, i);
     if (blockIdx.x == 0 && threadIdx.x == 0) { out[0] = S->count; out[1] = (int64_t)S->next_id; }
+}
+
+static unsigned xfer_blocks(int64_t n) {
+    const int64_t b = (n + kXferThreads - 1) / kXferThreads;
+    return (unsigned)(b < 1 ? 1 : (b > 65535 ? 65535 : b));
 }
 
 // True when the GPU can address every non-null host array directly and each
@@ -772,9 +796,7 @@ agb_status agb_world_import_cells(agb_world* w, const agb_cells* src, int32_t co
         // arrays must stay valid until the stream reaches it (NULL stream: on return).
         HostCells h;
         for (int k = 0; k < 25; ++k) h.p[k] = hst[k];
-        const int64_t blocks = ((int64_t)count + 255) / 256;
-        cells_import_kernel<<<(unsigned)(blocks < 1 ? 1 : (blocks > 4096 ? 4096 : blocks)), 256, 0, s>>>(
-            w->S, h, count, next_id);
+        cells_import_kernel<<<xfer_blocks(count), kXferThreads, 0, s>>>(w->S, h, count, next_id);
         AGB_CUDA(w, cudaGetLastError());
         if (s == nullptr) AGB_CUDA(w, cudaStreamSynchronize(s));
         return AGB_OK;
@@ -806,9 +828,7 @@ agb_status agb_world_export_cells(agb_world* w, agb_cells* dst, int32_t max_coun
         HostCells h;
         for (int k = 0; k < 25; ++k) h.p[k] = hst[k];
         const int64_t cap = max_count < w->c.capacity ? max_count : w->c.capacity;
-        const int64_t blocks = (cap + 255) / 256;
-        cells_export_kernel<<<(unsigned)(blocks < 1 ? 1 : (blocks > 4096 ? 4096 : blocks)), 256, 0, s>>>(
-            w->S, h, max_count, w->xfer_host);
+        cells_export_kernel<<<xfer_blocks(cap), kXferThreads, 0, s>>>(w->S, h, max_count, w->xfer_host);
         AGB_CUDA(w, cudaGetLastError());
         AGB_CUDA(w, cudaStreamSynchronize(s));
         if (count) *count = (int32_t)w->xfer_host[0];

@@ -653,18 +653,33 @@ def main():
         for name, _t in agb.CELL_FIELDS:
             pinned.a[name][:n] = cells[name]
         bytes_state = sum(np.dtype(t).itemsize for _n, t in agb.CELL_FIELDS) * n
-        e2e_steps = max(10, args.steps // 3)
+        e2e_steps = max(30, args.steps)
+        # Untimed warm-up of each loop over a whole compaction period, so that
+        # every tick phase has its graph captured before timing starts.
+        e2e_warm = max(args.warmup, desc.compaction_period if desc.compaction_period > 0 else 1)
+
+        def fused(k, pinned, nid):
+            for _ in range(k):
+                pinned, nid = world.step_host(pinned, nid, 1, stream=sh)
+            return pinned, nid
+
+        def separate(k, pinned, nid):
+            for _ in range(k):
+                world.import_cells(pinned, nid, stream=sh)
+                world.step(1, graph=True, stream=sh)
+                pinned, nid = world.export_cells(stream=sh, into=pinned)
+            return pinned, nid
+
+        pinned, nid = fused(e2e_warm, pinned, nid)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for _ in range(e2e_steps):
-            pinned, nid = world.step_host(pinned, nid, 1, stream=sh)
+        pinned, nid = fused(e2e_steps, pinned, nid)
         torch.cuda.synchronize()
         el_fused = time.perf_counter() - t0
+        pinned, nid = separate(e2e_warm, pinned, nid)
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for _ in range(e2e_steps):
-            world.import_cells(pinned, nid, stream=sh)
-            world.step(1, graph=True, stream=sh)
-            pinned, nid = world.export_cells(stream=sh, into=pinned)
+        pinned, nid = separate(e2e_steps, pinned, nid)
         torch.cuda.synchronize()
         el_sep = time.perf_counter() - t0
         e2e = {"value": n * e2e_steps / min(el_fused, el_sep), "unit": "cell-steps/s",
