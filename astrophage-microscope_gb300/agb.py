@@ -283,6 +283,8 @@ def load(path=LIB_PATH):
         "agb_world_step_graph": (I32, [P, I32, P]),
         "agb_world_stage": (I32, [P, I32, P]),
         "agb_world_graph_kernels": (I32, [P, C.POINTER(C.c_int64)]),
+        "agb_world_set_walk": (I32, [P, I32, I32]),
+        "agb_world_walk": (I32, [P, C.POINTER(I32), C.POINTER(I32)]),
         "agb_world_diffuse": (I32, [P, I32, C.c_double, P]),
         "agb_world_stats": (I32, [P, C.POINTER(Stats), P]),
         "agb_world_stats_accum": (I32, [P, P]),
@@ -338,7 +340,8 @@ def exported_symbols():
             "agb_world_create", "agb_world_destroy", "agb_world_spawn", "agb_world_import_cells",
             "agb_world_export_cells", "agb_world_device_cells", "agb_world_step_host", "agb_world_count",
             "agb_world_import_field", "agb_world_export_field", "agb_world_export_deposit",
-            "agb_world_step", "agb_world_step_graph", "agb_world_graph_kernels", "agb_world_stage",
+            "agb_world_step", "agb_world_step_graph", "agb_world_graph_kernels", "agb_world_set_walk",
+            "agb_world_walk", "agb_world_stage",
             "agb_world_diffuse",
             "agb_world_stats", "agb_world_stats_accum", "agb_world_set_clock",
             "agb_world_set_light", "agb_world_export_hash", "agb_world_export_forces",
@@ -465,6 +468,18 @@ class World:
         k = C.c_int64()
         self._check(self.lib.agb_world_graph_kernels(self.h, C.byref(k)), "graph_kernels")
         return k.value
+
+    def walk(self, lanes=None, fused=None):
+        """(lanes per cell, fused) of the feeding/contact walks; sets whichever
+        is given, keeping the other."""
+        k, f = C.c_int32(), C.c_int32()
+        self._check(self.lib.agb_world_walk(self.h, C.byref(k), C.byref(f)), "walk")
+        if lanes is not None or fused is not None:
+            lanes = k.value if lanes is None else int(lanes)
+            fused = f.value if fused is None else int(bool(fused))
+            self._check(self.lib.agb_world_set_walk(self.h, lanes, fused), "set_walk")
+            self._check(self.lib.agb_world_walk(self.h, C.byref(k), C.byref(f)), "walk")
+        return k.value, bool(f.value)
 
     def diffuse(self, f, dt, stream=None):
         self._check(self.lib.agb_world_diffuse(self.h, f, dt, _st(stream)), "diffuse")

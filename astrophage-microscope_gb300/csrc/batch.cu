@@ -127,6 +127,13 @@ struct ClassChoice {
     float tick_ms = 0.0f, pass_us = 0.0f;
 };
 
+// Chambers run concurrently, so each keeps one thread per cell in its
+// neighbour walks (the other chambers fill the GPU); small ones still fuse
+// feeding, taxis and forces into one pass. Measured on GB300 with 64 chambers
+// of 2.6M cells: 3.85 ms/step at 1 lane fused, 4.33 at 2 lanes fused, 3.97
+// at 1 lane as separate kernels.
+static void batch_walk(agb_world* w) { w->walk_lanes = 1; }
+
 // Time every candidate on probes built from one representative chamber.
 agb_status tune_class(agb_batch* b, const agb_world_desc& rep, const agb_spawn& sp, const agb_batch_opts& o,
                       cudaStream_t s, ClassChoice* out) {
@@ -145,6 +152,7 @@ agb_status tune_class(agb_batch* b, const agb_world_desc& rep, const agb_spawn& 
         agb_status rc = agb_world_create(&d, &w);
         if (rc == AGB_UNSUPPORTED || rc == AGB_INVALID_ARGUMENT) continue;   // e.g. too many buckets
         if (rc != AGB_OK) return bfail(b, rc, "autotune: probe chamber");
+        batch_walk(w);
         rc = agb_world_spawn(w, &sp, s);
         if (rc != AGB_OK) { agb_world_destroy(w); return bfail(b, rc, "autotune: probe spawn"); }
         const float t = time_ticks(w, ticks, s);
@@ -263,6 +271,7 @@ agb_status agb_batch_create(const agb_world_desc* descs, const agb_spawn* spawns
         agb_status rc = agb_world_create(&di, &b->worlds[(size_t)i]);
         if (rc != AGB_OK) { agb_batch_destroy(b); return rc; }
         agb_world* w = b->worlds[(size_t)i];
+        batch_walk(w);
         agb_tuning& t = b->tuning[(size_t)i];
         t.hash_cell_size = di.hash_cell_size > 0.0 ? di.hash_cell_size : AGB_HASH_CELL_FACTOR * AGB_CELL_DIAMETER;
         t.probe_tick_ms = choice[(size_t)i].tick_ms;

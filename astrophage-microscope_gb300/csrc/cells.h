@@ -16,18 +16,27 @@ struct LifeBuffers {
 };
 
 void launch_thermal(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, cudaStream_t s);
+// `lanes` (1, 2, 4 or 8) threads share each cell's neighbour walk in the
+// feeding and contact-force kernels; `blocks` sizes one thread per cell.
 void launch_emission(DevState* S, const Ctx& c, const TickParams& p, int32_t* stamp_idx, double* factor,
-                     bool stamp, int32_t blocks, cudaStream_t s);
+                     bool stamp, int32_t blocks, int lanes, cudaStream_t s);
 // The two halves of launch_emission: the irradiance field (stamps, occlusion
 // factors, sweep; needs the post-thermal cells, not the hash) and feeding
 // (walks the hash).
 void launch_emission_prep(DevState* S, const Ctx& c, const TickParams& p, int32_t* stamp_idx, double* factor,
                           bool stamp, int32_t blocks, cudaStream_t s);
-void launch_feed(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, cudaStream_t s);
+void launch_feed(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, int lanes, cudaStream_t s);
 // taxis_step (src/sim/taxis.cu:13-85): run-and-tumble state machine, emission.
 void launch_taxis(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, cudaStream_t s);
 void launch_motion(DevState* S, const Ctx& c, const TickParams& p, float* fx, float* fy, float* fz,
-                   int32_t blocks, cudaStream_t s);
+                   int32_t blocks, int lanes, cudaStream_t s);
+// Feeding (when `feed`), taxis (when `taxis`) and motion in one per-cell pass
+// plus integration: the same cell values as launch_feed, launch_taxis and
+// launch_motion in turn, with two kernels fewer on the tick's critical path.
+// `c` is the motion context (CO2/N2 as they stood before this tick's slow
+// fields; feeding reads only the irradiance grid).
+void launch_cell_step(DevState* S, const Ctx& c, const TickParams& p, float* fx, float* fy, float* fz,
+                      int32_t blocks, int lanes, bool feed, bool taxis, cudaStream_t s);
 // lifecycle_step (src/sim/lifecycle.cu:208-294), compaction included.
 void launch_lifecycle(DevState* S, const Ctx& c, const TickParams& p, const LifeBuffers& b,
                       bool compaction_allowed, int32_t blocks, cudaStream_t s);

@@ -24,9 +24,12 @@ namespace {
 // that axis on that side: the feeding walk uses it for the downstream layer
 // under axis-aligned light, whose cells can only lie in the cell's shadow-free
 // half-space (see feed_kernel).
-template <class F>
+//
+// lane / L split one walk over L threads: lane j visits entries j, j+L, ...
+// of every row (L = 1: the whole walk in one thread).
+template <int L = 1, class F>
 __device__ __forceinline__ void walk_neighbours(const HashDev& h, int32_t gx, int32_t gy, int32_t gz, F&& f,
-                                                int skip_axis = -1, int skip_side = 0) {
+                                                int skip_axis = -1, int skip_side = 0, int lane = 0) {
     int32_t xlo = gx > 0 ? gx - 1 : 0;
     int32_t xhi = gx < h.nx - 1 ? gx + 1 : h.nx - 1;
     if (skip_axis == 0) {
@@ -67,14 +70,42 @@ __device__ __forceinline__ void walk_neighbours(const HashDev& h, int32_t gx, in
     // current one is evaluated.
 #pragma unroll 1
     for (int r = 0; r < 9; ++r) {
-        if (lo[r] >= hi[r]) continue;
-        float4 nxt = __ldg(&h.rec[lo[r]]);
-        for (int32_t k = lo[r]; k < hi[r]; ++k) {
+        const int32_t k0 = lo[r] + lane;
+        if (k0 >= hi[r]) continue;
+        float4 nxt = __ldg(&h.rec[k0]);
+        for (int32_t k = k0; k < hi[r]; k += L) {
             const float4 cur = nxt;
-            if (k + 1 < hi[r]) nxt = __ldg(&h.rec[k + 1]);
+            if (k + L < hi[r]) nxt = __ldg(&h.rec[k + L]);
             f(k, cur);
         }
     }
+}
+
+// Lanes of one walk group (L consecutive lanes of a warp, L a power of two
+// up to 8) and reductions over them. Butterfly order is symmetric, so every
+// lane of the group ends with the same bits.
+template <int L>
+__device__ __forceinline__ unsigned group_mask() {
+    if (L == 1) return 1u << (threadIdx.x & 31u);
+    return ((1u << L) - 1u) << ((threadIdx.x & 31u) & ~(unsigned)(L - 1));
+}
+template <int L>
+__device__ __forceinline__ float group_sum(float v, unsigned m) {
+#pragma unroll
+    for (int o = L / 2; o > 0; o >>= 1) v += __shfl_xor_sync(m, v, o, L);
+    return v;
+}
+template <int L>
+__device__ __forceinline__ float group_prod(float v, unsigned m) {
+#pragma unroll
+    for (int o = L / 2; o > 0; o >>= 1) v *= __shfl_xor_sync(m, v, o, L);
+    return v;
+}
+template <int L>
+__device__ __forceinline__ int32_t group_isum(int32_t v, unsigned m) {
+#pragma unroll
+    for (int o = L / 2; o > 0; o >>= 1) v += __shfl_xor_sync(m, v, o, L);
+    return v;
 }
 
 __device__ __forceinline__ void unpack_bucket(float w, int32_t& gx, int32_t& gy, int32_t& gz) {
@@ -296,71 +327,114 @@ __device__ double shadow_fraction64(double dx, double dy, double dz, const Ctx& 
 // feed_kernel (emission.cu:81-115), one thread per hash-sorted entry: warp
 // lanes then share bucket neighbourhoods (broadcast loads of the candidate
 // records) instead of each streaming its own list.
+//
+// With L > 1, L lanes share one cell's walk (small populations: more threads
+// in flight per cell); the shading product is combined across them and lane 0
+// writes the cell.
+// One candidate k, at offset (dx, dy, dz) from the feeding cell (FP64
+// position px, py, pz), against that cell's open fraction.
+__device__ __forceinline__ void shade_candidate(const SoA& v, const Ctx& c, const HashDev& h, int32_t k, float dx,
+                                                float dy, float dz, double px, double py, double pz, float& open,
+                                                int32_t& refined) {
+    const float two_a = (float)AGB_CELL_DIAMETER;
+    const float a_f = (float)AGB_CELL_RADIUS;
+    const float along = dx * c.lx + dy * c.ly + dz * c.lz;
+    // Geometry first (cheap, rejects most candidates); FP64 only near the
+    // thresholds; the neighbour's flags only for real shadowers.
+    if (along < -1e-6f * two_a) return;
+    const float qx = dx - along * c.lx, qy = dy - along * c.ly, qz = dz - along * c.lz;
+    const float perp = sqrtf(qx * qx + qy * qy + qz * qz);
+    if (along > 1e-6f * two_a && perp >= two_a * (1.0f + 1e-6f)) return;
+    const int32_t j = (int32_t)__ldg(&h.vals_sorted[k]);
+    if (!(v.flags[j] & AGB_FLAG_ALIVE)) return;   // current flags: thermal may have starved j
+    if (along > 1e-6f * two_a && perp > 1e-2f * two_a && perp < two_a * (1.0f - 1e-6f)) {
+        const float x = perp / (2.0f * a_f);
+        const float frac = 0.63661977f * (acosf(x) - x * sqrtf(1.0f - x * x));
+        open *= (1.0f - frac);
+        return;
+    }
+    ++refined;   // both positions are this tick's (feeding moves nothing)
+    const double fr = shadow_fraction64(__dsub_rn(px, v.x[j]), __dsub_rn(py, v.y[j]), __dsub_rn(pz, v.z[j]), c);
+    open *= (float)(1.0 - fr);
+}
+
+// Under axis-aligned light every cell of the next bucket layer downstream has
+// `along` < 0 (it sits in this cell's shadow-free half-space) and leaves
+// `open` unchanged; a shading-only walk skips that layer when this cell is
+// clear of its downstream bucket face by more than the FP32 offsets' error,
+// so the product is unchanged.
+__device__ __forceinline__ void shade_skip(const Ctx& c, const HashDev& h, const float4& me, int& skip_axis,
+                                           int& skip_side) {
+    skip_axis = -1;
+    skip_side = 0;
+    if (c.light_axis_exact >= 0) {
+        const float off = c.light_axis_exact == 0 ? me.x : (c.light_axis_exact == 1 ? me.y : me.z);
+        const float face = c.light_sign > 0 ? h.cellf - off : off;
+        if (face > 4.0e-6f * h.cellf) { skip_axis = c.light_axis_exact; skip_side = c.light_sign; }
+    }
+}
+
+// Directional irradiance at cell i before occlusion.
+__device__ __forceinline__ float feed_directional(const Ctx& c, double px, double py, double pz) {
+    const GridDev& I = c.g[AGB_FIELD_IRRADIANCE];
+    const float d = fs(grid_sample(I, I.value, d2f(px), d2f(py), d2f(pz)), c.ambient_irr);
+    return d < 0.0f ? 0.0f : d;
+}
+
+// Feeding's writes for cell i: irradiance and the energy gained.
+__device__ __forceinline__ void feed_finish(const SoA& v, const Ctx& c, const TickParams& p, int32_t i,
+                                            float directional) {
+    v.irradiance[i] = directional;
+    const float gained = (directional * (float)AGB_CELL_CROSS_SECTION +
+                          c.ambient_irr * (float)AGB_CELL_SURFACE_AREA) * p.dtf;
+    double e = v.energy[i] + f2d(gained);
+    if (dkey(e) > dkey(AGB_CELL_ENERGY_MAX)) e = AGB_CELL_ENERGY_MAX;
+    v.energy[i] = e;
+}
+
+template <int L>
+__device__ __forceinline__ void feed_cell(DevState* S, const SoA& v, const Ctx& c, const TickParams& p,
+                                          int32_t ks, int32_t i, int lane, unsigned gm) {
+    const HashDev h = c.h;
+    const double px = v.x[i], py = v.y[i], pz = v.z[i];
+    float directional = feed_directional(c, px, py, pz);
+    if (c.occlusion_exact) {
+        const float4 me = h.rec[ks];
+        int32_t gx, gy, gz;
+        unpack_bucket(me.w, gx, gy, gz);
+        float open = 1.0f;
+        int32_t refined = 0;
+        int skip_axis, skip_side;
+        shade_skip(c, h, me, skip_axis, skip_side);
+        walk_neighbours<L>(h, gx, gy, gz, [&](int32_t k, const float4& rk) {
+            if (k == ks) return;
+            float dx, dy, dz;
+            rec_delta(h, me, gx, gy, gz, rk, dx, dy, dz);
+            shade_candidate(v, c, h, k, dx, dy, dz, px, py, pz, open, refined);
+        }, skip_axis, skip_side, lane);
+        if (L > 1) {
+            open = group_prod<L>(open, gm);
+            refined = group_isum<L>(refined, gm);
+        }
+        if (refined && lane == 0) atomicAdd(&S->n_shadow_refine, refined);
+        directional *= open;
+    }
+    if (lane == 0) feed_finish(v, c, p, i, directional);
+}
+
+template <int L>
 __global__ void __launch_bounds__(256) feed_kernel(DevState* S, Ctx c, TickParams p) {
     pdl_wait();
     const SoA v = S->cur;
     const int32_t n = S->hash_count;
-    const GridDev I = c.g[AGB_FIELD_IRRADIANCE];
-    const HashDev h = c.h;
-    const float two_a = (float)AGB_CELL_DIAMETER;
-    const float a_f = (float)AGB_CELL_RADIUS;
-    AGB_FOR_CELLS(ks, n) {
-        const int32_t i = (int32_t)h.vals_sorted[ks];
+    const int32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = t & (L - 1);
+    const unsigned gm = group_mask<L>();
+    for (int32_t ks = t / L; ks < n; ks += (int32_t)(gridDim.x * blockDim.x) / L) {
+        const int32_t i = (int32_t)c.h.vals_sorted[ks];
         const uint32_t f = v.flags[i];
         if (!(f & AGB_FLAG_OCCUPIED) || !(f & AGB_FLAG_ALIVE)) continue;
-        const double px = v.x[i], py = v.y[i], pz = v.z[i];
-        float directional = fs(grid_sample(I, I.value, d2f(px), d2f(py), d2f(pz)), c.ambient_irr);
-        if (directional < 0.0f) directional = 0.0f;
-        if (c.occlusion_exact) {
-            const float4 me = h.rec[ks];
-            int32_t gx, gy, gz;
-            unpack_bucket(me.w, gx, gy, gz);
-            float open = 1.0f;
-            int32_t refined = 0;
-            // Under axis-aligned light every cell of the next bucket layer
-            // downstream has `along` < 0 (it sits in this cell's shadow-free
-            // half-space) and leaves `open` unchanged; that layer is skipped
-            // when this cell is clear of its downstream bucket face by more
-            // than the FP32 offsets' error, so the product is unchanged.
-            int skip_axis = -1, skip_side = 0;
-            if (c.light_axis_exact >= 0) {
-                const float off = c.light_axis_exact == 0 ? me.x : (c.light_axis_exact == 1 ? me.y : me.z);
-                const float face = c.light_sign > 0 ? h.cellf - off : off;
-                if (face > 4.0e-6f * h.cellf) { skip_axis = c.light_axis_exact; skip_side = c.light_sign; }
-            }
-            walk_neighbours(h, gx, gy, gz, [&](int32_t k, const float4& rk) {
-                if (k == ks) return;
-                float dx, dy, dz;
-                rec_delta(h, me, gx, gy, gz, rk, dx, dy, dz);
-                const float along = dx * c.lx + dy * c.ly + dz * c.lz;
-                // Geometry first (cheap, rejects most candidates); FP64 only near
-                // the thresholds; the neighbour's flags only for real shadowers.
-                if (along < -1e-6f * two_a) return;
-                const float qx = dx - along * c.lx, qy = dy - along * c.ly, qz = dz - along * c.lz;
-                const float perp = sqrtf(qx * qx + qy * qy + qz * qz);
-                if (along > 1e-6f * two_a && perp >= two_a * (1.0f + 1e-6f)) return;
-                const int32_t j = (int32_t)__ldg(&h.vals_sorted[k]);
-                if (!(v.flags[j] & AGB_FLAG_ALIVE)) return;   // current flags: thermal may have starved j
-                if (along > 1e-6f * two_a && perp > 1e-2f * two_a && perp < two_a * (1.0f - 1e-6f)) {
-                    const float x = perp / (2.0f * a_f);
-                    const float frac = 0.63661977f * (acosf(x) - x * sqrtf(1.0f - x * x));
-                    open *= (1.0f - frac);
-                    return;
-                }
-                ++refined;   // both positions are this tick's (feeding moves nothing)
-                const double fr = shadow_fraction64(__dsub_rn(px, v.x[j]), __dsub_rn(py, v.y[j]),
-                                                    __dsub_rn(pz, v.z[j]), c);
-                open *= (float)(1.0 - fr);
-            }, skip_axis, skip_side);
-            if (refined) atomicAdd(&S->n_shadow_refine, refined);
-            directional *= open;
-        }
-        v.irradiance[i] = directional;
-        const float gained = (directional * (float)AGB_CELL_CROSS_SECTION +
-                              c.ambient_irr * (float)AGB_CELL_SURFACE_AREA) * p.dtf;
-        double e = v.energy[i] + f2d(gained);
-        if (dkey(e) > dkey(AGB_CELL_ENERGY_MAX)) e = AGB_CELL_ENERGY_MAX;
-        v.energy[i] = e;
+        feed_cell<L>(S, v, c, p, ks, i, lane, gm);
     }
 }
 
@@ -425,78 +499,116 @@ __device__ __forceinline__ bool boundary_axis(double& pos, float& vel, const Ctx
 }
 
 // forces_kernel (integrator.cu:40-76), one thread per hash-sorted entry.
+// With L > 1, L lanes share one cell's contact walk; their partial sums are
+// combined and lane 0 writes the cell.
+// One candidate k, at offset (dx, dy, dz) from cell i, against i's contact
+// force (contact_force, integrator.cuh:200-219).
+__device__ __forceinline__ void contact_candidate(const SoA& v, const HashDev& h, const TickParams& p, int32_t k,
+                                                  int32_t i, float dx, float dy, float dz, float& Cx, float& Cy,
+                                                  float& Cz, int32_t& refined) {
+    const float two_a = (float)AGB_CELL_DIAMETER;
+    const float thr = two_a * two_a;
+    const double two_a64 = AGB_CELL_DIAMETER;
+    const float r2s = dx * dx + dy * dy + dz * dz;
+    if (r2s >= thr * (1.0f + 1e-5f)) return;                     // clear of contact
+    if (r2s <= thr * (1.0f - 1e-5f) && r2s > 1e-12f * thr) {     // in contact
+        const float r = sqrtf(r2s);
+        const float s = p.k_contact * (two_a - r) / r;
+        Cx += dx * s; Cy += dy * s; Cz += dz * s;
+        return;
+    }
+    ++refined;   // settle in FP64 from the pre-step positions (integrator.cuh:210-219)
+    const int32_t j = (int32_t)__ldg(&h.vals_sorted[k]);
+    const double ddx = __dsub_rn(v.x[i], v.x[j]), ddy = __dsub_rn(v.y[i], v.y[j]), ddz = __dsub_rn(v.z[i], v.z[j]);
+    const double rr = __dadd_rn(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)), __dmul_rn(ddz, ddz));
+    if (rr >= two_a64 * two_a64 || rr <= 0.0) return;
+    const double r = sqrt(rr);
+    const double s = __ddiv_rn(__dmul_rn(p.k_contact64, __dsub_rn(two_a64, r)), r);
+    Cx += (float)__dmul_rn(ddx, s); Cy += (float)__dmul_rn(ddy, s); Cz += (float)__dmul_rn(ddz, s);
+}
+
+// field_sample_kernel (integrator.cu:20-30) for cell i: sorted order makes
+// neighbouring threads sample neighbouring voxels.
+__device__ __forceinline__ void sample_fields(const SoA& v, const Ctx& c, int32_t i) {
+    const GridDev& T = c.g[AGB_FIELD_TEMPERATURE];
+    const GridDev& C2 = c.g[AGB_FIELD_CO2];
+    const GridDev& N2 = c.g[AGB_FIELD_N2];
+    const float xf = d2f(v.x[i]), yf = d2f(v.y[i]), zf = d2f(v.z[i]);
+    if (T.enabled) v.t_local[i] = grid_sample(T, T.value, xf, yf, zf);
+    if (C2.enabled) v.co2_local[i] = grid_sample(C2, C2.value, xf, yf, zf);
+    if (N2.enabled) v.n2_local[i] = grid_sample(N2, N2.value, xf, yf, zf);
+}
+
+// Net force on cell i (integrator.cu:40-76): buoyancy, photon thrust, the
+// summed contacts (Cx, Cy, Cz; added only when contacts are on) and the trap.
+__device__ __forceinline__ void forces_finish(const SoA& v, const Ctx& c, const TickParams& p, int32_t i, float Cx,
+                                              float Cy, float Cz, float* fx_out, float* fy_out, float* fz_out) {
+    const uint32_t flags = v.flags[i];
+    const float mass = d2f(v.biomass[i]) + d2f(v.energy[i]) * (float)(1.0 / (AGB_C_LIGHT * AGB_C_LIGHT));
+    const bool alive = (flags & AGB_FLAG_ALIVE) != 0u;
+    const float wgt = -(mass - (float)(AGB_WATER_DENSITY * AGB_CELL_VOLUME)) * (float)AGB_G_ACCEL;
+    float Fx = 0.0f, Fy = 0.0f, Fz = 0.0f;
+    if (c.gravity_axis == AGB_GRAVITY_Y) Fy += wgt; else Fz += wgt;
+    const float thrust = alive ? v.emit_power[i] * (float)(1.0 / AGB_C_LIGHT) : 0.0f;
+    if (thrust != 0.0f) {
+        Fx -= v.dir_x[i] * thrust;
+        Fy -= v.dir_y[i] * thrust;
+        Fz -= v.dir_z[i] * thrust;
+    }
+    if (c.contact_enabled) { Fx += Cx; Fy += Cy; Fz += Cz; }
+    if (i == c.trap_slot) {                                      // trap_force (integrator.cuh:195-197)
+        Fx += p.k_trap * (float)(c.trap_x - v.x[i]);
+        Fy += p.k_trap * (float)(c.trap_y - v.y[i]);
+    }
+    fx_out[i] = Fx; fy_out[i] = Fy; fz_out[i] = Fz;
+}
+
+template <int L>
+__device__ __forceinline__ void forces_cell(DevState* S, const SoA& v, const Ctx& c, const TickParams& p,
+                                            int32_t ks, int32_t i, int lane, unsigned gm, float* fx_out,
+                                            float* fy_out, float* fz_out) {
+    const HashDev h = c.h;
+    float Cx = 0.0f, Cy = 0.0f, Cz = 0.0f;
+    if (c.contact_enabled) {
+        const float4 me = h.rec[ks];
+        int32_t gx, gy, gz;
+        unpack_bucket(me.w, gx, gy, gz);
+        int32_t refined = 0;
+        walk_neighbours<L>(h, gx, gy, gz, [&](int32_t k, const float4& rk) {
+            if (k == ks) return;                                    // bucket members are occupied
+            float dx, dy, dz;
+            rec_delta(h, me, gx, gy, gz, rk, dx, dy, dz);
+            contact_candidate(v, h, p, k, i, dx, dy, dz, Cx, Cy, Cz, refined);
+        }, -1, 0, lane);
+        if (L > 1) {
+            Cx = group_sum<L>(Cx, gm);
+            Cy = group_sum<L>(Cy, gm);
+            Cz = group_sum<L>(Cz, gm);
+            refined = group_isum<L>(refined, gm);
+        }
+        if (refined && lane == 0) atomicAdd(&S->n_contact_refine, refined);
+    }
+    if (lane != 0) return;
+    sample_fields(v, c, i);
+    forces_finish(v, c, p, i, Cx, Cy, Cz, fx_out, fy_out, fz_out);
+}
+
+template <int L>
 __global__ void __launch_bounds__(256) forces_kernel(DevState* S, Ctx c, TickParams p, float* fx_out,
                                                      float* fy_out, float* fz_out) {
     pdl_wait();
     const SoA v = S->cur;
     const int32_t n = S->hash_count;
-    const HashDev h = c.h;
-    const GridDev T = c.g[AGB_FIELD_TEMPERATURE], C2 = c.g[AGB_FIELD_CO2], N2 = c.g[AGB_FIELD_N2];
-    const float two_a = (float)AGB_CELL_DIAMETER;
-    const float thr = two_a * two_a;
-    const double two_a64 = AGB_CELL_DIAMETER;
-    AGB_FOR_CELLS(ks, n) {
-        const int32_t i = (int32_t)h.vals_sorted[ks];
-        if (h.keys_sorted[ks] >= (uint32_t)h.buckets) {          // unoccupied slot (sentinel key)
-            fx_out[i] = 0.0f; fy_out[i] = 0.0f; fz_out[i] = 0.0f;
+    const int32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = t & (L - 1);
+    const unsigned gm = group_mask<L>();
+    for (int32_t ks = t / L; ks < n; ks += (int32_t)(gridDim.x * blockDim.x) / L) {
+        const int32_t i = (int32_t)c.h.vals_sorted[ks];
+        if (c.h.keys_sorted[ks] >= (uint32_t)c.h.buckets) {      // unoccupied slot (sentinel key)
+            if (lane == 0) { fx_out[i] = 0.0f; fy_out[i] = 0.0f; fz_out[i] = 0.0f; }
             continue;
         }
-        const uint32_t flags = v.flags[i];
-        // field_sample_kernel (integrator.cu:20-30), done here because sorted
-        // order makes neighbouring threads sample neighbouring voxels.
-        {
-            const float xf = d2f(v.x[i]), yf = d2f(v.y[i]), zf = d2f(v.z[i]);
-            if (T.enabled) v.t_local[i] = grid_sample(T, T.value, xf, yf, zf);
-            if (C2.enabled) v.co2_local[i] = grid_sample(C2, C2.value, xf, yf, zf);
-            if (N2.enabled) v.n2_local[i] = grid_sample(N2, N2.value, xf, yf, zf);
-        }
-        const float mass = d2f(v.biomass[i]) + d2f(v.energy[i]) * (float)(1.0 / (AGB_C_LIGHT * AGB_C_LIGHT));
-        const bool alive = (flags & AGB_FLAG_ALIVE) != 0u;
-        const float wgt = -(mass - (float)(AGB_WATER_DENSITY * AGB_CELL_VOLUME)) * (float)AGB_G_ACCEL;
-        float Fx = 0.0f, Fy = 0.0f, Fz = 0.0f;
-        if (c.gravity_axis == AGB_GRAVITY_Y) Fy += wgt; else Fz += wgt;
-        const float thrust = alive ? v.emit_power[i] * (float)(1.0 / AGB_C_LIGHT) : 0.0f;
-        if (thrust != 0.0f) {
-            Fx -= v.dir_x[i] * thrust;
-            Fy -= v.dir_y[i] * thrust;
-            Fz -= v.dir_z[i] * thrust;
-        }
-        if (c.contact_enabled) {
-            const float4 me = h.rec[ks];
-            int32_t gx, gy, gz;
-            unpack_bucket(me.w, gx, gy, gz);
-            int32_t refined = 0;
-            const float kc = p.k_contact;
-            const double kc64 = p.k_contact64;
-            walk_neighbours(h, gx, gy, gz, [&](int32_t k, const float4& rk) {
-                if (k == ks) return;                                    // bucket members are occupied
-                float dx, dy, dz;
-                rec_delta(h, me, gx, gy, gz, rk, dx, dy, dz);
-                const float r2s = dx * dx + dy * dy + dz * dz;
-                if (r2s >= thr * (1.0f + 1e-5f)) return;                 // clear of contact
-                if (r2s <= thr * (1.0f - 1e-5f) && r2s > 1e-12f * thr) { // in contact (contact_force)
-                    const float r = sqrtf(r2s);
-                    const float s = kc * (two_a - r) / r;
-                    Fx += dx * s; Fy += dy * s; Fz += dz * s;
-                    return;
-                }
-                ++refined;   // settle in FP64 from the pre-step positions (integrator.cuh:210-219)
-                const int32_t j = (int32_t)__ldg(&h.vals_sorted[k]);
-                const double ddx = __dsub_rn(v.x[i], v.x[j]), ddy = __dsub_rn(v.y[i], v.y[j]),
-                             ddz = __dsub_rn(v.z[i], v.z[j]);
-                const double rr = __dadd_rn(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)), __dmul_rn(ddz, ddz));
-                if (rr >= two_a64 * two_a64 || rr <= 0.0) return;
-                const double r = sqrt(rr);
-                const double s = __ddiv_rn(__dmul_rn(kc64, __dsub_rn(two_a64, r)), r);
-                Fx += (float)__dmul_rn(ddx, s); Fy += (float)__dmul_rn(ddy, s); Fz += (float)__dmul_rn(ddz, s);
-            });
-            if (refined) atomicAdd(&S->n_contact_refine, refined);
-        }
-        if (i == c.trap_slot) {                                  // trap_force (integrator.cuh:195-197)
-            Fx += p.k_trap * (float)(c.trap_x - v.x[i]);
-            Fy += p.k_trap * (float)(c.trap_y - v.y[i]);
-        }
-        fx_out[i] = Fx; fy_out[i] = Fy; fz_out[i] = Fz;
+        forces_cell<L>(S, v, c, p, ks, i, lane, gm, fx_out, fy_out, fz_out);
     }
 }
 
@@ -615,57 +727,134 @@ __device__ V3 taxis_tumble(V3 heading, Pcg& rng) {               // taxis.cuh:10
     return normalize3(add3(scale3(h, ct), scale3(perp, st)));
 }
 
+__device__ __forceinline__ void taxis_cell(const SoA& v, const TickParams& p, int32_t i) {
+    const uint32_t f = v.flags[i];
+    if (!(f & AGB_FLAG_OCCUPIED) || !(f & AGB_FLAG_ALIVE)) return;
+    if (!(f & AGB_FLAG_AWAKE)) {                               // dormant: inert, no emission
+        v.emit_power[i] = 0.0f;
+        return;
+    }
+    const double irr = (double)v.irradiance[i];
+    const double co2 = (double)v.co2_local[i];
+    const double energy = v.energy[i];
+    const double charge = __ddiv_rn(energy, AGB_CELL_ENERGY_MAX);
+    const bool dark = irr < AGB_TAXIS_DARK_THRESHOLD, co2_here = co2 > 0.0;   // taxis.cuh:56-62
+    int state = 0;                                             // 0 idle, 1 feed, 2 breed
+    if (!(dark && !co2_here)) {
+        if (!dark && charge < AGB_TAXIS_SEEK_FEED_BELOW) state = 1;
+        else if (charge > AGB_TAXIS_SEEK_BREED_ABOVE && co2_here) state = 2;
+    }
+    if (state == 0) {                                          // no draws on the idle path
+        v.emit_power[i] = 0.0f;
+        v.run_timer[i] = 0.0f;
+        v.taxis_memory[i] = 0.0f;
+        return;
+    }
+    const double signal = state == 1 ? irr : co2;
+    const double mem = (double)v.taxis_memory[i];
+    const double delta = __dsub_rn(signal, mem);
+    v.taxis_memory[i] = (float)__dadd_rn(mem, __dmul_rn(p.taxis_alpha, __dsub_rn(signal, mem)));
+    V3 heading{-(double)v.dir_x[i], -(double)v.dir_y[i], -(double)v.dir_z[i]};
+    double run = __dadd_rn((double)v.run_timer[i], p.dt);
+    if (delta <= 0.0 || run >= AGB_TAXIS_RUN_MAX) {            // taxis_should_tumble
+        Pcg rng{v.rng_state[i], cell_stream_inc(v.id[i])};
+        heading = taxis_tumble(heading, rng);
+        v.rng_state[i] = rng.state;
+        run = 0.0;
+    }
+    v.run_timer[i] = (float)run;
+    const V3 nh = normalize3(heading);                         // taxis_emit_dir = -normalize(heading)
+    v.dir_x[i] = (float)(-nh.x);
+    v.dir_y[i] = (float)(-nh.y);
+    v.dir_z[i] = (float)(-nh.z);
+    double pw = 0.0;                                           // taxis_emit_power, taxis.cuh:136-141
+    if (energy > 0.0) {
+        const double avail = p.dt > 0.0 ? __ddiv_rn(energy, p.dt) : 0.0;
+        pw = p.max_emit_power < avail ? p.max_emit_power : avail;
+    }
+    v.emit_power[i] = (float)pw;
+    v.energy[i] = __dsub_rn(energy, __dmul_rn(pw, p.dt));
+}
+
 __global__ void __launch_bounds__(256) taxis_kernel(DevState* S, Ctx c, TickParams p) {
     pdl_wait();
     const SoA v = S->cur;
     const int32_t n = S->count;
-    AGB_FOR_CELLS(i, n) {
+    AGB_FOR_CELLS(i, n) taxis_cell(v, p, i);
+}
+
+// The per-cell middle of the tick in one pass over the hash-sorted entries:
+// feeding (emission.cu:81-115), taxis (taxis.cu:13-85) and field sample +
+// forces (integrator.cu:20-76) for each cell in turn, with ONE neighbour walk
+// that applies both the shading and the contact test to every candidate.
+// Each stage reads and writes only its own cell's state, apart from
+// neighbours' positions and flags, which none of them changes, and each lane
+// visits candidates in the order of the separate walks, so every cell gets
+// the values the three separate passes give it. (A shading-only walk may skip
+// the downstream layer under axis-aligned light; the shared walk visits it,
+// and its candidates leave `open` unchanged.) `feed` / `taxis` select the
+// stages this tick runs; with L > 1 the group shares the walk and lane 0
+// finishes the cell.
+template <int L>
+__global__ void __launch_bounds__(256) cell_step_kernel(DevState* S, Ctx c, TickParams p, int feed, int taxis,
+                                                        float* fx_out, float* fy_out, float* fz_out) {
+    pdl_wait();
+    const SoA v = S->cur;
+    const HashDev h = c.h;
+    const int32_t n = S->hash_count;
+    const int32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = t & (L - 1);
+    const unsigned gm = group_mask<L>();
+    const bool contact = c.contact_enabled != 0;
+    for (int32_t ks = t / L; ks < n; ks += (int32_t)(gridDim.x * blockDim.x) / L) {
+        const int32_t i = (int32_t)h.vals_sorted[ks];
+        if (h.keys_sorted[ks] >= (uint32_t)h.buckets) {          // unoccupied slot (sentinel key)
+            if (lane == 0) { fx_out[i] = 0.0f; fy_out[i] = 0.0f; fz_out[i] = 0.0f; }
+            continue;
+        }
         const uint32_t f = v.flags[i];
-        if (!(f & AGB_FLAG_OCCUPIED) || !(f & AGB_FLAG_ALIVE)) continue;
-        if (!(f & AGB_FLAG_AWAKE)) {                               // dormant: inert, no emission
-            v.emit_power[i] = 0.0f;
-            continue;
+        const bool fd = feed && (f & AGB_FLAG_OCCUPIED) && (f & AGB_FLAG_ALIVE);
+        const bool shade = fd && c.occlusion_exact;
+        const double px = v.x[i], py = v.y[i], pz = v.z[i];
+        float open = 1.0f, Cx = 0.0f, Cy = 0.0f, Cz = 0.0f;
+        int32_t rs = 0, rc = 0;
+        if (shade || contact) {
+            const float4 me = h.rec[ks];
+            int32_t gx, gy, gz;
+            unpack_bucket(me.w, gx, gy, gz);
+            int skip_axis = -1, skip_side = 0;
+            if (!contact) shade_skip(c, h, me, skip_axis, skip_side);
+            walk_neighbours<L>(h, gx, gy, gz, [&](int32_t k, const float4& rk) {
+                if (k == ks) return;
+                float dx, dy, dz;
+                rec_delta(h, me, gx, gy, gz, rk, dx, dy, dz);
+                if (shade) shade_candidate(v, c, h, k, dx, dy, dz, px, py, pz, open, rs);
+                if (contact) contact_candidate(v, h, p, k, i, dx, dy, dz, Cx, Cy, Cz, rc);
+            }, skip_axis, skip_side, lane);
+            if (L > 1) {
+                if (shade) {
+                    open = group_prod<L>(open, gm);
+                    rs = group_isum<L>(rs, gm);
+                }
+                if (contact) {
+                    Cx = group_sum<L>(Cx, gm);
+                    Cy = group_sum<L>(Cy, gm);
+                    Cz = group_sum<L>(Cz, gm);
+                    rc = group_isum<L>(rc, gm);
+                }
+            }
         }
-        const double irr = (double)v.irradiance[i];
-        const double co2 = (double)v.co2_local[i];
-        const double energy = v.energy[i];
-        const double charge = __ddiv_rn(energy, AGB_CELL_ENERGY_MAX);
-        const bool dark = irr < AGB_TAXIS_DARK_THRESHOLD, co2_here = co2 > 0.0;   // taxis.cuh:56-62
-        int state = 0;                                             // 0 idle, 1 feed, 2 breed
-        if (!(dark && !co2_here)) {
-            if (!dark && charge < AGB_TAXIS_SEEK_FEED_BELOW) state = 1;
-            else if (charge > AGB_TAXIS_SEEK_BREED_ABOVE && co2_here) state = 2;
+        if (lane != 0) continue;
+        if (rs) atomicAdd(&S->n_shadow_refine, rs);
+        if (rc) atomicAdd(&S->n_contact_refine, rc);
+        if (fd) {
+            float directional = feed_directional(c, px, py, pz);
+            if (shade) directional *= open;
+            feed_finish(v, c, p, i, directional);
         }
-        if (state == 0) {                                          // no draws on the idle path
-            v.emit_power[i] = 0.0f;
-            v.run_timer[i] = 0.0f;
-            v.taxis_memory[i] = 0.0f;
-            continue;
-        }
-        const double signal = state == 1 ? irr : co2;
-        const double mem = (double)v.taxis_memory[i];
-        const double delta = __dsub_rn(signal, mem);
-        v.taxis_memory[i] = (float)__dadd_rn(mem, __dmul_rn(p.taxis_alpha, __dsub_rn(signal, mem)));
-        V3 heading{-(double)v.dir_x[i], -(double)v.dir_y[i], -(double)v.dir_z[i]};
-        double run = __dadd_rn((double)v.run_timer[i], p.dt);
-        if (delta <= 0.0 || run >= AGB_TAXIS_RUN_MAX) {            // taxis_should_tumble
-            Pcg rng{v.rng_state[i], cell_stream_inc(v.id[i])};
-            heading = taxis_tumble(heading, rng);
-            v.rng_state[i] = rng.state;
-            run = 0.0;
-        }
-        v.run_timer[i] = (float)run;
-        const V3 nh = normalize3(heading);                         // taxis_emit_dir = -normalize(heading)
-        v.dir_x[i] = (float)(-nh.x);
-        v.dir_y[i] = (float)(-nh.y);
-        v.dir_z[i] = (float)(-nh.z);
-        double pw = 0.0;                                           // taxis_emit_power, taxis.cuh:136-141
-        if (energy > 0.0) {
-            const double avail = p.dt > 0.0 ? __ddiv_rn(energy, p.dt) : 0.0;
-            pw = p.max_emit_power < avail ? p.max_emit_power : avail;
-        }
-        v.emit_power[i] = (float)pw;
-        v.energy[i] = __dsub_rn(energy, __dmul_rn(pw, p.dt));
+        if (taxis) taxis_cell(v, p, i);
+        sample_fields(v, c, i);
+        forces_finish(v, c, p, i, Cx, Cy, Cz, fx_out, fy_out, fz_out);
     }
 }
 
@@ -696,17 +885,47 @@ void launch_emission_prep(DevState* S, const Ctx& c, const TickParams& p, int32_
         launch_k(sweep_kernel, (unsigned)((lines + 127) / 128), 128, 0, s, c, factor);
     }
 }
-void launch_feed(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, cudaStream_t s) {
-    launch_k(feed_kernel, blocks, 256, 0, s, S, c, p);
+// Grid for a walk kernel with `lanes` threads per cell: `blocks` covers the
+// population one thread per cell, so it grows by `lanes` (bounded).
+static unsigned walk_blocks(int32_t blocks, int lanes) {
+    const int64_t b = (int64_t)blocks * lanes;
+    return (unsigned)(b < 65535 ? b : 65535);
+}
+void launch_feed(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, int lanes, cudaStream_t s) {
+    const unsigned g = walk_blocks(blocks, lanes);
+    switch (lanes) {
+        case 8: launch_k(feed_kernel<8>, g, 256, 0, s, S, c, p); break;
+        case 4: launch_k(feed_kernel<4>, g, 256, 0, s, S, c, p); break;
+        case 2: launch_k(feed_kernel<2>, g, 256, 0, s, S, c, p); break;
+        default: launch_k(feed_kernel<1>, blocks, 256, 0, s, S, c, p); break;
+    }
 }
 void launch_emission(DevState* S, const Ctx& c, const TickParams& p, int32_t* stamp_idx, double* factor,
-                     bool stamp, int32_t blocks, cudaStream_t s) {
+                     bool stamp, int32_t blocks, int lanes, cudaStream_t s) {
     launch_emission_prep(S, c, p, stamp_idx, factor, stamp, blocks, s);
-    launch_feed(S, c, p, blocks, s);
+    launch_feed(S, c, p, blocks, lanes, s);
+}
+void launch_cell_step(DevState* S, const Ctx& c, const TickParams& p, float* fx, float* fy, float* fz,
+                      int32_t blocks, int lanes, bool feed, bool taxis, cudaStream_t s) {
+    const unsigned g = walk_blocks(blocks, lanes);
+    const int fe = feed ? 1 : 0, tx = taxis ? 1 : 0;
+    switch (lanes) {
+        case 8: launch_k(cell_step_kernel<8>, g, 256, 0, s, S, c, p, fe, tx, fx, fy, fz); break;
+        case 4: launch_k(cell_step_kernel<4>, g, 256, 0, s, S, c, p, fe, tx, fx, fy, fz); break;
+        case 2: launch_k(cell_step_kernel<2>, g, 256, 0, s, S, c, p, fe, tx, fx, fy, fz); break;
+        default: launch_k(cell_step_kernel<1>, blocks, 256, 0, s, S, c, p, fe, tx, fx, fy, fz); break;
+    }
+    launch_k(integrate_kernel, blocks, 256, 0, s, S, c, p, fx, fy, fz);
 }
 void launch_motion(DevState* S, const Ctx& c, const TickParams& p, float* fx, float* fy, float* fz,
-                   int32_t blocks, cudaStream_t s) {
-    launch_k(forces_kernel, blocks, 256, 0, s, S, c, p, fx, fy, fz);
+                   int32_t blocks, int lanes, cudaStream_t s) {
+    const unsigned g = walk_blocks(blocks, lanes);
+    switch (lanes) {
+        case 8: launch_k(forces_kernel<8>, g, 256, 0, s, S, c, p, fx, fy, fz); break;
+        case 4: launch_k(forces_kernel<4>, g, 256, 0, s, S, c, p, fx, fy, fz); break;
+        case 2: launch_k(forces_kernel<2>, g, 256, 0, s, S, c, p, fx, fy, fz); break;
+        default: launch_k(forces_kernel<1>, blocks, 256, 0, s, S, c, p, fx, fy, fz); break;
+    }
     launch_k(integrate_kernel, blocks, 256, 0, s, S, c, p, fx, fy, fz);
 }
 

@@ -48,6 +48,8 @@ struct agb_world {
     float *fx = nullptr, *fy = nullptr, *fz = nullptr;
     unsigned long long* acc = nullptr;
     int32_t blocks = 1;
+    int walk_lanes = 1;                  // threads sharing one cell's neighbour walk (1, 2, 4, 8)
+    bool fuse_cells = false;             // feeding, taxis and forces in one kernel with one walk
     uint64_t tick = 0;
     double sim_time = 0.0;
     double physics_rate = 1.0, biology_rate = 1.0;

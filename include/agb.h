@@ -349,6 +349,16 @@ agb_status agb_world_step_graph(agb_world* w, int32_t ticks, agb_stream s);
 /* Kernel launches performed by graph replays since the world was created
  * (the sum of each replayed graph's kernel nodes), for launch accounting. */
 agb_status agb_world_graph_kernels(agb_world* w, int64_t* kernels);
+/* How a tick runs the neighbour walks of feeding (src/sim/emission.cu:81-115)
+ * and contact forces (src/sim/integrator.cu:40-76): `lanes` threads share each
+ * cell's walk (1, 2, 4 or 8), and `fused` = 1 runs feeding, taxis and forces
+ * as one kernel with one walk per cell, 0 as separate kernels. Default: 2
+ * lanes fused for capacities up to 512 cells per SM, else 1 lane separate;
+ * chambers of a batch use 1 lane. Results agree to FP32
+ * summation order; integer state is unchanged. Captured graphs are rebuilt.
+ * No reference counterpart (a launch-shape knob of this engine). */
+agb_status agb_world_set_walk(agb_world* w, int32_t lanes, int32_t fused);
+agb_status agb_world_walk(agb_world* w, int32_t* lanes, int32_t* fused);
 /* One stage of the tick at the world's dt (AGB_STAGE_*). */
 agb_status agb_world_stage(agb_world* w, int32_t stage, agb_stream s);
 /* grid_diffuse on one field for dt (src/fields/diffuse.cu:159-186). */

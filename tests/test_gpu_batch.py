@@ -43,10 +43,14 @@ def chambers():
     return descs, spawns
 
 
-def standalone(desc, sp, ticks, hash_cell=None):
+def standalone(desc, sp, ticks, hash_cell=None, walk=None):
+    """A world on its own, with the chamber's hash cell and walk shape (lanes
+    per cell, fused): the same launch shape gives the same bits."""
     if hash_cell is not None:
         desc.hash_cell_size = hash_cell
     w = agb.World(desc)
+    if walk is not None:
+        w.walk(*walk)
     w.spawn(sp)
     w.step(ticks)
     return w
@@ -75,7 +79,7 @@ def test_batch_equals_standalone_worlds():
         t = b.tuning(i)
         assert 0 <= t.lane < 3
         d, s = chambers()
-        w = standalone(d[i], s[i], total)
+        w = standalone(d[i], s[i], total, walk=b.chambers[i].walk())
         assert_same(b.chambers[i], w, "chamber %d" % i)
     assert b.graph_kernels() > 0
 
@@ -89,7 +93,7 @@ def test_batch_graph_replay_repeats():
     k1 = b.graph_kernels()
     d, s = chambers()
     for i in range(b.n):
-        w = standalone(d[i], s[i], 8)
+        w = standalone(d[i], s[i], 8, walk=b.chambers[i].walk())
         assert_same(b.chambers[i], w, "chamber %d" % i)
     b.step(1)
     assert b.graph_kernels() > k1
@@ -107,7 +111,7 @@ def test_autotuned_batch_matches_tuned_standalone():
         assert t.probe_tick_ms > 0.0
         assert t.ftcs_lx[0] in (16, 32) and t.ftcs_rpt[0] in (1, 2, 4) and t.ftcs_zc[0] >= 1
         d, s = chambers()
-        w = standalone(d[i], s[i], 4, hash_cell=t.hash_cell_size)
+        w = standalone(d[i], s[i], 4, hash_cell=t.hash_cell_size, walk=b.chambers[i].walk())
         assert_same(b.chambers[i], w, "tuned chamber %d" % i)
 
 

@@ -41,8 +41,42 @@ def test_hash_bit_exact(name):
 @pytest.mark.parametrize("name", NAMES)
 def test_each_stage_from_identical_state(name):
     """One stage at a time, each from the oracle's state after the previous one."""
+    stage_by_stage(S.scenarios()[name])
+
+
+@pytest.mark.parametrize("fused", [False, True])
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8])
+@pytest.mark.parametrize("name", ["dense_cluster", "diagonal_light_dormant", "collinear_shadow", "slab_uniform",
+                                  "taxis_seek"])
+def test_walk_shapes_track_oracle(name, lanes, fused):
+    """Every split of the feeding and contact walks over 1-8 lanes per cell,
+    as separate kernels (the per-stage path too) or as the fused per-cell pass
+    of whole ticks: parity stage by stage, equal integer state over whole
+    ticks, and cell values within the parity bounds after the first tick."""
     sc = S.scenarios()[name]
+    stage_by_stage(sc, lanes)
     gpu, orc = seeded(sc)
+    assert gpu.walk(lanes, fused) == (lanes, fused)
+    before, _ = orc.export_cells()
+    gpu.step(1, graph=True)
+    orc.step(1)
+    a, _ = gpu.export_cells()
+    b, _ = orc.export_cells()
+    errs = P.compare_cells(a, b, before, where="tick 0")
+    assert not errs, "\n".join(errs[:20])
+    gpu.step(sc["ticks"], graph=True)
+    orc.step(sc["ticks"])
+    a, _ = gpu.export_cells()
+    b, _ = orc.export_cells()
+    assert a.n == b.n
+    for k in P.INT_FIELDS:
+        assert np.array_equal(a[k], b[k]), k
+
+
+def stage_by_stage(sc, lanes=None):
+    gpu, orc = seeded(sc)
+    if lanes is not None:
+        gpu.walk(lanes=lanes)
     errs = []
     for t in range(sc["ticks"]):
         for stage, sname in S.stages_for(sc["desc"]):
