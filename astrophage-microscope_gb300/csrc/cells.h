@@ -15,6 +15,21 @@ struct LifeBuffers {
     unsigned long long* co2_demand;   // per CO2 voxel, fixed point (src/sim/world.cuh:108)
 };
 
+// co2_uptake_rate (src/sim/lifecycle.cuh:24-28) in FP32.
+__device__ __forceinline__ float co2_uptake_rate_f(float c) {
+    if (c <= 0.0f) return 0.0f;
+    return (float)AGB_LIFE_CO2_UPTAKE_MAX * c / (c + (float)AGB_LIFE_CO2_HALF_SATURATION);
+}
+
+// One live cell's CO2 demand at (x, y, z) into the voxel's rationing word
+// (demand_kernel body, src/sim/lifecycle.cu:41-57).
+__device__ __forceinline__ void co2_demand_cell(const GridDev& C2, const TickParams& p, float x, float y, float z,
+                                                unsigned long long* demand, float inv_gv) {
+    const int64_t idx = grid_nearest(C2, x, y, z);
+    const float want = co2_uptake_rate_f(C2.value[idx]) * (float)p.dt_bio;
+    if (want > 0.0f) deposit_fixed(&demand[idx], to_fixed_f(want * inv_gv, (float)C2.scale));
+}
+
 void launch_thermal(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, cudaStream_t s);
 // `lanes` (1, 2, 4 or 8) threads share each cell's neighbour walk in the
 // feeding and contact-force kernels; `blocks` sizes one thread per cell.
@@ -30,16 +45,27 @@ void launch_feed(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks,
 void launch_taxis(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, cudaStream_t s);
 void launch_motion(DevState* S, const Ctx& c, const TickParams& p, float* fx, float* fy, float* fz,
                    int32_t blocks, int lanes, cudaStream_t s);
-// Feeding (when `feed`), taxis (when `taxis`) and motion in one per-cell pass
-// plus integration: the same cell values as launch_feed, launch_taxis and
-// launch_motion in turn, with two kernels fewer on the tick's critical path.
+// The two halves of launch_motion: forces (field sample + contact walk) and
+// integration. With `demand` set, integration also enters each live cell's
+// CO2 demand at its new position into `demand` from the grid `co2` (the
+// lifecycle's first pass, which needs the CO2 as diffused this tick).
+void launch_forces(DevState* S, const Ctx& c, const TickParams& p, float* fx, float* fy, float* fz,
+                   int32_t blocks, int lanes, cudaStream_t s);
+void launch_integrate(DevState* S, const Ctx& c, const TickParams& p, const float* fx, const float* fy,
+                      const float* fz, int32_t blocks, const GridDev& co2, unsigned long long* demand,
+                      float inv_gv, cudaStream_t s);
+// Feeding (when `feed`), taxis (when `taxis`) and forces in one per-cell pass
+// with one neighbour walk: the same cell values as launch_feed, launch_taxis
+// and launch_forces in turn, with two kernels fewer on the tick's critical
+// path (integration follows separately).
 // `c` is the motion context (CO2/N2 as they stood before this tick's slow
 // fields; feeding reads only the irradiance grid).
 void launch_cell_step(DevState* S, const Ctx& c, const TickParams& p, float* fx, float* fy, float* fz,
                       int32_t blocks, int lanes, bool feed, bool taxis, cudaStream_t s);
 // lifecycle_step (src/sim/lifecycle.cu:208-294), compaction included.
+// `demand_done`: integration already entered this tick's CO2 demand.
 void launch_lifecycle(DevState* S, const Ctx& c, const TickParams& p, const LifeBuffers& b,
-                      bool compaction_allowed, int32_t blocks, cudaStream_t s);
+                      bool compaction_allowed, int32_t blocks, cudaStream_t s, bool demand_done = false);
 // cell_store_compact (src/sim/cell_store.cu:414-456) on its own.
 void launch_compact(DevState* S, const Ctx& c, const LifeBuffers& b, int32_t blocks, cudaStream_t s);
 // stats_step (src/sim/stats.cu:79-100): fixed-point sums into acc[12].

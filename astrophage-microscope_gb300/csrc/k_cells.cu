@@ -613,10 +613,13 @@ __global__ void __launch_bounds__(256) forces_kernel(DevState* S, Ctx c, TickPar
 }
 
 // integrate_kernel (integrator.cu:79-150), slot order (coalesced state access).
+// With `demand` set, the lifecycle's demand pass (demand_kernel,
+// lifecycle.cu:41-57) runs here on each live cell at its new position.
 __global__ void __launch_bounds__(256) integrate_kernel(DevState* S, Ctx c, TickParams p,
                                                         const float* __restrict__ fx_in,
                                                         const float* __restrict__ fy_in,
-                                                        const float* __restrict__ fz_in) {
+                                                        const float* __restrict__ fz_in, GridDev co2,
+                                                        unsigned long long* demand, float inv_gv) {
     pdl_wait();
     const SoA v = S->cur;
     const int32_t n = S->count;
@@ -687,6 +690,7 @@ __global__ void __launch_bounds__(256) integrate_kernel(DevState* S, Ctx c, Tick
         v.x[i] = px; v.y[i] = py; v.z[i] = pz;
         v.vx[i] = f2d(ux); v.vy[i] = f2d(uy); v.vz[i] = f2d(uz);
         v.age_s[i] = v.age_s[i] + p.dtf;
+        if (demand && (nf & AGB_FLAG_ALIVE)) co2_demand_cell(co2, p, d2f(px), d2f(py), d2f(pz), demand, inv_gv);
     }
 }
 
@@ -915,9 +919,8 @@ void launch_cell_step(DevState* S, const Ctx& c, const TickParams& p, float* fx,
         case 2: launch_k(cell_step_kernel<2>, g, 256, 0, s, S, c, p, fe, tx, fx, fy, fz); break;
         default: launch_k(cell_step_kernel<1>, blocks, 256, 0, s, S, c, p, fe, tx, fx, fy, fz); break;
     }
-    launch_k(integrate_kernel, blocks, 256, 0, s, S, c, p, fx, fy, fz);
 }
-void launch_motion(DevState* S, const Ctx& c, const TickParams& p, float* fx, float* fy, float* fz,
+void launch_forces(DevState* S, const Ctx& c, const TickParams& p, float* fx, float* fy, float* fz,
                    int32_t blocks, int lanes, cudaStream_t s) {
     const unsigned g = walk_blocks(blocks, lanes);
     switch (lanes) {
@@ -926,7 +929,16 @@ void launch_motion(DevState* S, const Ctx& c, const TickParams& p, float* fx, fl
         case 2: launch_k(forces_kernel<2>, g, 256, 0, s, S, c, p, fx, fy, fz); break;
         default: launch_k(forces_kernel<1>, blocks, 256, 0, s, S, c, p, fx, fy, fz); break;
     }
-    launch_k(integrate_kernel, blocks, 256, 0, s, S, c, p, fx, fy, fz);
+}
+void launch_integrate(DevState* S, const Ctx& c, const TickParams& p, const float* fx, const float* fy,
+                      const float* fz, int32_t blocks, const GridDev& co2, unsigned long long* demand,
+                      float inv_gv, cudaStream_t s) {
+    launch_k(integrate_kernel, blocks, 256, 0, s, S, c, p, fx, fy, fz, co2, demand, inv_gv);
+}
+void launch_motion(DevState* S, const Ctx& c, const TickParams& p, float* fx, float* fy, float* fz,
+                   int32_t blocks, int lanes, cudaStream_t s) {
+    launch_forces(S, c, p, fx, fy, fz, blocks, lanes, s);
+    launch_integrate(S, c, p, fx, fy, fz, blocks, c.g[AGB_FIELD_CO2], nullptr, 0.0f, s);
 }
 
 }  // namespace agb

@@ -23,11 +23,9 @@ constexpr int STILE = ST * SITEMS;
 // ---------------------------------------------------------------------------
 // CO2 uptake (demand_kernel / uptake_kernel, lifecycle.cu:41-86)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float uptake_rate_f(float c) {     // co2_uptake_rate, lifecycle.cuh:24-28
-    if (c <= 0.0f) return 0.0f;
-    return (float)AGB_LIFE_CO2_UPTAKE_MAX * c / (c + (float)AGB_LIFE_CO2_HALF_SATURATION);
-}
-
+// demand_kernel (lifecycle.cu:41-57). The tick itself folds this pass into
+// integration (integrate_kernel), which has the moved cell at hand; the
+// per-stage lifecycle runs it here.
 __global__ void __launch_bounds__(256) demand_kernel(DevState* S, Ctx c, TickParams p,
                                                      unsigned long long* demand, float inv_gv) {
     pdl_wait();
@@ -37,52 +35,24 @@ __global__ void __launch_bounds__(256) demand_kernel(DevState* S, Ctx c, TickPar
     AGB_FOR_CELLS(i, n) {
         const uint32_t f = v.flags[i];
         if (!(f & AGB_FLAG_OCCUPIED) || !(f & AGB_FLAG_ALIVE)) continue;
-        const int64_t idx = grid_nearest(C2, d2f(v.x[i]), d2f(v.y[i]), d2f(v.z[i]));
-        const float want = uptake_rate_f(C2.value[idx]) * (float)p.dt_bio;
-        if (want <= 0.0f) continue;
-        deposit_fixed(&demand[idx], to_fixed_f(want * inv_gv, (float)C2.scale));
+        co2_demand_cell(C2, p, d2f(v.x[i]), d2f(v.y[i]), d2f(v.z[i]), demand, inv_gv);
     }
 }
 
-__global__ void __launch_bounds__(256) uptake_kernel(DevState* S, Ctx c, TickParams p,
-                                                     const unsigned long long* __restrict__ demand,
-                                                     float inv_gv) {
-    pdl_wait();
-    const SoA v = S->cur;
-    const int32_t n = S->count;
-    const GridDev C2 = c.g[AGB_FIELD_CO2];
-    AGB_FOR_CELLS(i, n) {
-        const uint32_t f = v.flags[i];
-        if (!(f & AGB_FLAG_OCCUPIED) || !(f & AGB_FLAG_ALIVE)) continue;
-        const int64_t idx = grid_nearest(C2, d2f(v.x[i]), d2f(v.y[i]), d2f(v.z[i]));
-        const float available = C2.value[idx];
-        const float want = uptake_rate_f(available) * (float)p.dt_bio;
-        if (want <= 0.0f) continue;
-        const float asked = (float)(long long)demand[idx] * C2.inv_scale_f;   // from_fixed
-        float taken = want;
-        if (asked > available && asked > 0.0f) taken = want * (available / asked);
-        if (taken <= 0.0f) continue;
-        v.co2_held[i] = v.co2_held[i] + f2d(taken);
-        deposit_fixed(&C2.deposit[idx], to_fixed_f(-taken * inv_gv, (float)C2.scale));
-    }
-}
-
-// ---------------------------------------------------------------------------
-// Death (death_kernel, lifecycle.cu:100-112) fused with mark (mark_kernel,
-// lifecycle.cu:119-135): both read one cell and write only that cell.
-// ---------------------------------------------------------------------------
 __device__ __forceinline__ bool ready_to_divide(const Ctx& c, const SoA& v, int32_t i) {
     if (c.division_predicate == AGB_DIVIDE_ENERGY) return v.energy[i] >= c.division_energy;
     return v.co2_held[i] >= c.co2_quota;                    // lifecycle.cuh:33-36
 }
 
-// Per cell, after uptake: the CO2 flush (flush_kernel restricted to the
-// voxels cells sit in, lifecycle.cu:235; it also clears the rationing
-// demand there) and death_kernel + mark_kernel (lifecycle.cu:90-134). The
-// flush reads only OCCUPIED, which death never changes, so the two share one
-// pass over the cells.
-__global__ void __launch_bounds__(256) death_mark_kernel(DevState* S, Ctx c, int32_t* divflag,
-                                                         unsigned long long* demand) {
+// Per cell, after every demand is in: CO2 uptake (uptake_kernel,
+// lifecycle.cu:59-86; `demand` null when there is no CO2 grid), then
+// death_kernel + mark_kernel (lifecycle.cu:90-134). Each reads one cell and
+// writes only that cell, besides uptake's deposit into its voxel's deposit
+// word, which nothing here reads; the CO2 flush that must follow every
+// deposit (lifecycle.cu:235) runs in the divide pass.
+__global__ void __launch_bounds__(256) uptake_mark_kernel(DevState* S, Ctx c, TickParams p,
+                                                          const unsigned long long* __restrict__ demand,
+                                                          float inv_gv, int32_t* divflag) {
     pdl_wait();
     const SoA v = S->cur;
     const int32_t n = S->count;
@@ -90,11 +60,19 @@ __global__ void __launch_bounds__(256) death_mark_kernel(DevState* S, Ctx c, int
     int32_t births = 0, deads = 0;
     AGB_FOR_CELLS(i, n) {
         uint32_t f = v.flags[i];
-        if (demand && (f & AGB_FLAG_OCCUPIED)) {
-            const int64_t idx = grid_nearest(C2, (float)v.x[i], (float)v.y[i], (float)v.z[i]);
-            const unsigned long long raw = atomicExch(&C2.deposit[idx], 0ull);
-            if (raw != 0ull) C2.value[idx] = fa(C2.value[idx], (float)(long long)raw * C2.inv_scale_f);
-            demand[idx] = 0ull;
+        if (demand && (f & AGB_FLAG_OCCUPIED) && (f & AGB_FLAG_ALIVE)) {
+            const int64_t idx = grid_nearest(C2, d2f(v.x[i]), d2f(v.y[i]), d2f(v.z[i]));
+            const float available = C2.value[idx];
+            const float want = co2_uptake_rate_f(available) * (float)p.dt_bio;
+            if (want > 0.0f) {
+                const float asked = (float)(long long)demand[idx] * C2.inv_scale_f;   // from_fixed
+                float taken = want;
+                if (asked > available && asked > 0.0f) taken = want * (available / asked);
+                if (taken > 0.0f) {
+                    v.co2_held[i] = v.co2_held[i] + f2d(taken);
+                    deposit_fixed(&C2.deposit[idx], to_fixed_f(-taken * inv_gv, (float)C2.scale));
+                }
+            }
         }
         if ((f & AGB_FLAG_OCCUPIED) && (f & AGB_FLAG_ALIVE) && v.t_local[i] > c.lethal_f) {
             f &= ~AGB_FLAG_ALIVE;
@@ -230,9 +208,14 @@ __global__ void __launch_bounds__(ST) scan_kernel(DevState* S, const int32_t* __
 // ---------------------------------------------------------------------------
 __device__ void life_finalize(DevState* S, int32_t capacity, int32_t compaction_allowed);
 
+//
+// With `demand` set (a CO2 grid), the same pass first runs the CO2 flush
+// (flush_kernel, lifecycle.cu:235, restricted to the voxels cells sit in: only
+// uptake deposited this tick, into exactly those) from each parent's position
+// before division moves it, and clears the rationing demand there.
 __global__ void __launch_bounds__(256) divide_kernel(DevState* S, Ctx c, const int32_t* __restrict__ divflag,
                                                      const int32_t* __restrict__ prefix,
-                                                     int32_t compaction_allowed) {
+                                                     int32_t compaction_allowed, unsigned long long* demand) {
     pdl_wait();
     const int32_t births_now = S->births;
     const SoA v = S->cur;
@@ -240,8 +223,15 @@ __global__ void __launch_bounds__(256) divide_kernel(DevState* S, Ctx c, const i
     const uint64_t first_id = S->next_id;
     const double a = AGB_CELL_RADIUS;
     const double hx = 0.5 * c.chamber_w - a, hy = 0.5 * c.chamber_h - a, hz = 0.5 * c.chamber_d - a;
-    AGB_FOR_CELLS(i, births_now > 0 ? n : 0) {
-        if (!divflag[i]) continue;
+    const GridDev C2 = c.g[AGB_FIELD_CO2];
+    AGB_FOR_CELLS(i, (births_now > 0 || demand) ? n : 0) {
+        if (demand && (v.flags[i] & AGB_FLAG_OCCUPIED)) {
+            const int64_t idx = grid_nearest(C2, (float)v.x[i], (float)v.y[i], (float)v.z[i]);
+            const unsigned long long raw = atomicExch(&C2.deposit[idx], 0ull);
+            if (raw != 0ull) C2.value[idx] = fa(C2.value[idx], (float)(long long)raw * C2.inv_scale_f);
+            demand[idx] = 0ull;
+        }
+        if (births_now <= 0 || !divflag[i]) continue;
         const int32_t slot = n + prefix[i];
         if (slot >= c.capacity) continue;       // store full: skip, do not wrap
         const uint64_t did = first_id + (uint64_t)prefix[i];
@@ -592,17 +582,14 @@ void launch_compact_kernels(DevState* S, const LifeBuffers& b, int32_t capacity,
 }  // namespace
 
 void launch_lifecycle(DevState* S, const Ctx& c, const TickParams& p, const LifeBuffers& b,
-                      bool compaction_allowed, int32_t blocks, cudaStream_t s) {
+                      bool compaction_allowed, int32_t blocks, cudaStream_t s, bool demand_done) {
     const GridDev& C2 = c.g[AGB_FIELD_CO2];
-    if (C2.enabled) {
-        const float inv_gv = (float)(1.0 / (C2.dx * C2.dx * C2.dz_eff));
-        launch_k(demand_kernel, blocks, 256, 0, s, S, c, p, b.co2_demand, inv_gv);
-        launch_k(uptake_kernel, blocks, 256, 0, s, S, c, p, b.co2_demand, inv_gv);
-    }
-    // CO2 flush (lifecycle.cu:235) fused with death and division marks.
-    launch_k(death_mark_kernel, blocks, 256, 0, s, S, c, b.flags, C2.enabled ? b.co2_demand : nullptr);
+    unsigned long long* dem = C2.enabled ? b.co2_demand : nullptr;
+    const float inv_gv = C2.enabled ? (float)(1.0 / (C2.dx * C2.dx * C2.dz_eff)) : 0.0f;
+    if (C2.enabled && !demand_done) launch_k(demand_kernel, blocks, 256, 0, s, S, c, p, dem, inv_gv);
+    launch_k(uptake_mark_kernel, blocks, 256, 0, s, S, c, p, dem, inv_gv, b.flags);
     launch_scan(S, b, c.capacity, 0, s);
-    launch_k(divide_kernel, blocks, 256, 0, s, S, c, b.flags, b.prefix, compaction_allowed ? 1 : 0);
+    launch_k(divide_kernel, blocks, 256, 0, s, S, c, b.flags, b.prefix, compaction_allowed ? 1 : 0, dem);
     // Compaction cannot run on this tick unless the host-side period allows it.
     if (compaction_allowed) launch_compact_kernels(S, b, c.capacity, blocks, s);
 }

@@ -240,9 +240,9 @@ bool compaction_allowed(const agb_world* w) {
     return w->d.compaction_enabled && ((w->tick + 1) % (uint64_t)P) == 0;
 }
 
-void stage_lifecycle(agb_world* w, cudaStream_t s) {  // lifecycle_step, src/sim/lifecycle.cu:208-294
+void stage_lifecycle(agb_world* w, cudaStream_t s, bool demand_done = false) {  // src/sim/lifecycle.cu:208-294
     refresh_grid_ptrs(w);
-    launch_lifecycle(w->S, w->c, w->tp, w->life, compaction_allowed(w), w->blocks, s);
+    launch_lifecycle(w->S, w->c, w->tp, w->life, compaction_allowed(w), w->blocks, s, demand_done);
 }
 
 void stage_clock(agb_world* w) {
@@ -250,25 +250,45 @@ void stage_clock(agb_world* w) {
     w->sim_time += w->tp.dt;
 }
 
-// One tick as a small DAG. The thermal substeps, the irradiance field they
-// precede (stamps, occlusion factors, sweep: they read the post-thermal cells
-// but not the hash) and the CO2/N2 diffusion do not touch what the hash build
-// reads (positions, OCCUPIED), so they run on side streams -- parallel
-// branches of the captured graph -- joined where the reference's order needs
-// their results: the irradiance field before feeding (which walks the hash),
-// slow fields before lifecycle (uptake reads the diffused CO2). Motion samples
-// CO2 and N2 from the buffers as they were before this tick's diffusion,
-// exactly as in src/sim/step.cu:164-171, while the diffusion writes the other
-// ping-pong buffer.
+// One tick as a small DAG. The irradiance field (stamps, occlusion factors,
+// sweep) reads the cells as thermal leaves them but not the hash; the last
+// thermal substep's flush and FTCS pass touch only the temperature grid; the
+// CO2/N2 diffusion touches only those grids. So three side streams -- branches
+// of the captured graph -- run them beside the hash build, joined where the
+// reference's order needs their results: the irradiance field and the
+// diffused temperature before the per-cell pass (feeding walks the hash,
+// forces sample T), the slow fields before integration, which also enters
+// the lifecycle's CO2 demand from the diffused CO2 (uptake reads it too).
+// Motion samples CO2 and N2 from the buffers as they were before this tick's
+// diffusion, exactly as in src/sim/step.cu:164-171, while the diffusion
+// writes the other ping-pong buffer.
 void tick_surrogate(agb_world* w, cudaStream_t s);
 
 void tick_once(agb_world* w, cudaStream_t s) {
     if (w->sg) { tick_surrogate(w, s); return; }
-    cudaStream_t s1 = w->side[0], s2 = w->side[1];
+    cudaStream_t s1 = w->side[0], s2 = w->side[1], s3 = w->side[2];
     cudaEventRecord(w->ev[0], s);
     cudaStreamWaitEvent(s1, w->ev[0], 0);
     cudaStreamWaitEvent(s2, w->ev[0], 0);
-    if (w->d.thermal_enabled) stage_thermal(w, s1);
+    // thermal_step (thermal.cu:75-103): all substeps on s1 except the last
+    // one's flush and FTCS pass, which fork onto s3 once its thermal kernel
+    // has run.
+    const bool thermal = w->d.thermal_enabled && w->c.g[AGB_FIELD_TEMPERATURE].enabled;
+    const int32_t nsub = thermal ? w->tp.t_substeps : 0;
+    for (int32_t k = 0; k < nsub; ++k) {
+        refresh_grid_ptrs(w);
+        launch_thermal(w->S, w->c, w->tp, w->blocks, s1);
+        if (k + 1 == nsub) break;
+        launch_flush_by_cells(w->S, w->c.g[AGB_FIELD_TEMPERATURE], nullptr, w->blocks, s1);
+        ftcs(w, AGB_FIELD_TEMPERATURE, w->tp.t_coeff, s1);
+    }
+    cudaEventRecord(w->ev[3], s1);
+    cudaStreamWaitEvent(s3, w->ev[3], 0);
+    if (nsub > 0) {
+        launch_flush_by_cells(w->S, w->c.g[AGB_FIELD_TEMPERATURE], nullptr, w->blocks, s3);
+        ftcs(w, AGB_FIELD_TEMPERATURE, w->tp.t_coeff, s3);
+    }
+    cudaEventRecord(w->ev[4], s3);
     const bool emit = emission_active(w);
     if (emit) {
         refresh_grid_ptrs(w);
@@ -281,23 +301,25 @@ void tick_once(agb_world* w, cudaStream_t s) {
     cudaEventRecord(w->ev[2], s2);
     stage_hash(w, s);
     cudaStreamWaitEvent(s, w->ev[1], 0);
-    {
-        // Feeding, taxis (step.cu:161-162) and motion: one kernel per cell
-        // pass, or the three passes in turn. Motion sees CO2/N2 as they stood
-        // before this tick's diffusion; feeding reads only the irradiance grid.
-        Ctx c = w->c;
-        for (int f : {AGB_FIELD_CO2, AGB_FIELD_N2}) c.g[f] = pre.g[f];
-        if (w->fuse_cells) {
-            launch_cell_step(w->S, c, w->tp, w->fx, w->fy, w->fz, w->blocks, w->walk_lanes, emit,
-                             w->d.taxis_enabled != 0, s);
-        } else {
-            if (emit) launch_feed(w->S, w->c, w->tp, w->blocks, w->walk_lanes, s);
-            if (w->d.taxis_enabled) launch_taxis(w->S, w->c, w->tp, w->blocks, s);
-            launch_motion(w->S, c, w->tp, w->fx, w->fy, w->fz, w->blocks, w->walk_lanes, s);
-        }
+    cudaStreamWaitEvent(s, w->ev[4], 0);
+    // Feeding, taxis (step.cu:161-162) and forces: one kernel per cell pass,
+    // or the three passes in turn. Feeding reads only the irradiance grid.
+    Ctx c = w->c;
+    for (int f : {AGB_FIELD_CO2, AGB_FIELD_N2}) c.g[f] = pre.g[f];
+    if (w->fuse_cells) {
+        launch_cell_step(w->S, c, w->tp, w->fx, w->fy, w->fz, w->blocks, w->walk_lanes, emit,
+                         w->d.taxis_enabled != 0, s);
+    } else {
+        if (emit) launch_feed(w->S, w->c, w->tp, w->blocks, w->walk_lanes, s);
+        if (w->d.taxis_enabled) launch_taxis(w->S, w->c, w->tp, w->blocks, s);
+        launch_forces(w->S, c, w->tp, w->fx, w->fy, w->fz, w->blocks, w->walk_lanes, s);
     }
     cudaStreamWaitEvent(s, w->ev[2], 0);
-    stage_lifecycle(w, s);
+    const GridDev& co2 = w->c.g[AGB_FIELD_CO2];
+    const float inv_gv = co2.enabled ? (float)(1.0 / (co2.dx * co2.dx * co2.dz_eff)) : 0.0f;
+    launch_integrate(w->S, c, w->tp, w->fx, w->fy, w->fz, w->blocks, co2,
+                     co2.enabled ? w->life.co2_demand : nullptr, inv_gv, s);
+    stage_lifecycle(w, s, co2.enabled);
     stage_clock(w);
 }
 

@@ -43,8 +43,8 @@ struct agb_world {
     LifeBuffers life{};
     int32_t* stamp_idx = nullptr;
     double* occl_factor = nullptr;       // per irradiance voxel: transmittance of stamped voxels
-    cudaStream_t side[2] = {nullptr, nullptr};   // concurrent branches of a tick
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaStream_t side[3] = {nullptr, nullptr, nullptr};   // concurrent branches of a tick
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     float *fx = nullptr, *fy = nullptr, *fz = nullptr;
     unsigned long long* acc = nullptr;
     int32_t blocks = 1;
