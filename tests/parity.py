@@ -88,11 +88,11 @@ def compare_cells(got, want, before=None, rtol=RTOL, where=""):
     return errs
 
 
-def compare_forces(fg, fo, where=""):
+def compare_forces(fg, fo, where="", rtol=RTOL):
     errs = []
     for ax in range(3):
         b = np.asarray(fo[ax], np.float64)
-        nb, mx = _close(fg[ax], b, RTOL, 1e-4 * _rms(b) + 1e-30)
+        nb, mx = _close(fg[ax], b, rtol, 1e-4 * _rms(b) + 1e-30)
         if nb:
             errs.append("%s: force axis %d out of tolerance in %d cells (max %.3g)" % (where, ax, nb, mx))
     return errs

@@ -73,7 +73,7 @@ def test_walk_shapes_track_oracle(name, lanes, fused):
         assert np.array_equal(a[k], b[k]), k
 
 
-def stage_by_stage(sc, lanes=None):
+def stage_by_stage(sc, lanes=None, force_rtol=P.RTOL):
     gpu, orc = seeded(sc)
     if lanes is not None:
         gpu.walk(lanes=lanes)
@@ -96,7 +96,80 @@ def stage_by_stage(sc, lanes=None):
             errs += P.compare_cells(a, b, before, where=where)
             errs += P.compare_fields(gpu, orc, where=where)
             if stage == agb.STAGE_MOTION:
-                errs += P.compare_forces(gpu.export_forces(), orc.export_forces(), where)
+                errs += P.compare_forces(gpu.export_forces(), orc.export_forces(), where, force_rtol)
+    assert not errs, "\n".join(errs[:20])
+
+
+def _bucket_face_pairs(cells, desc):
+    """Isolated pairs of cells straddling hash-bucket faces, edges and corners
+    (canon 22 um buckets) at separations within 1e-4 of contact, with the
+    nearer cell 0.5, 1 - 1e-3 or 1 - 1e-6 of the separation from the crossed
+    faces; and pairs along the +x beam with a perpendicular offset across a
+    y face within 1e-4 of one diameter: contacts and shadows that the
+    neighbour walks find only across bucket boundaries, at the thresholds of
+    the FP32 tests and the FP64 settle bands."""
+    cell = agb.HASH_CELL_FACTOR * agb.CELL_DIAMETER
+    two_a = agb.CELL_DIAMETER
+    nb = int(np.ceil(desc.chamber_w / cell))
+    org = -0.5 * nb * cell
+    zf = -0.5 * int(np.ceil(desc.chamber_d / cell)) * cell + cell        # the lower inner z face
+    pts = []
+
+    def home(k):
+        return np.array([org + (12 + 7 * (k % 22)) * cell, org + (12 + 7 * (k // 22)) * cell, zf])
+
+    k = 0
+    for axes in ([0], [1], [2], [0, 1], [0, 2], [1, 2], [0, 1, 2]):
+        u = np.zeros(3)
+        u[axes] = 1.0
+        u /= np.linalg.norm(u)
+        for e in (-1e-4, -1e-6, 0.0, 1e-6, 4.9e-5, 5.1e-5, 1e-4):
+            for t in (0.5, 1 - 1e-3, 1 - 1e-6):
+                f = home(k)
+                mid = f + 0.5 * cell
+                base = np.where(u > 0, f, mid)                           # the crossed faces' corner
+                s = two_a * (1.0 + e)
+                pts += [base - u * s * t, base + u * s * (1.0 - t)]
+                k += 1
+    for e in (-1e-4, -1e-6, 1e-6, 5.1e-5):
+        for dxb in (3e-6, 12e-6, 25e-6):
+            f = home(k)
+            p = two_a * (1.0 + e)
+            a = np.array([f[0] + 0.5 * cell, f[1] - 0.999 * p, f[2] + 0.5 * cell])
+            pts += [a, a + np.array([-dxb, p, 0.0])]
+            k += 1
+    pts = np.array(pts)
+    n = len(pts)
+    cells.a["x"][:n], cells.a["y"][:n], cells.a["z"][:n] = pts[:, 0], pts[:, 1], pts[:, 2]
+
+
+# Contact forces here come from overlaps down to 1e-4 of a diameter: the
+# FP32 contact path forms (2a - r) with r good to about 1.5 ulp (1.4e-12 m),
+# so at a 1e-9 m overlap their relative error reaches ~1.4e-3 (measured:
+# 1.37e-3; the FP64 settle band starts at overlaps of 1e-5). A contact the
+# walk missed would be off by 100% of that force.
+FACE_FORCE_RTOL = 1e-2
+
+
+@pytest.mark.parametrize("lanes,fused", [(1, False), (2, False), (1, True), (2, True)])
+def test_contacts_across_bucket_faces(lanes, fused):
+    """Contacts and shadows across bucket faces, edges and corners at the
+    contact and shading thresholds, stage by stage and over a fused or
+    separate tick, against the oracle."""
+    d = S.slab_desc(cap=400, light=(1.0, 0.0, 1e4, 0.0))
+    d.contact_enabled = 1
+    sc = dict(desc=d, ticks=1, mutate=_bucket_face_pairs,              # 318 cells, all placed
+              spawn=agb.spawn(318, charge_dist=agb.DIST_UNIFORM, charge_a=0.0, charge_b=0.2, awake=True))
+    stage_by_stage(sc, lanes, FACE_FORCE_RTOL)
+    gpu, orc = seeded(sc)
+    gpu.walk(lanes, fused)
+    before, _ = orc.export_cells()
+    gpu.step(1, graph=True)
+    orc.step(1)
+    a, _ = gpu.export_cells()
+    b, _ = orc.export_cells()
+    errs = P.compare_cells(a, b, before, where="tick")
+    errs += P.compare_forces(gpu.export_forces(), orc.export_forces(), "tick", FACE_FORCE_RTOL)
     assert not errs, "\n".join(errs[:20])
 
 
