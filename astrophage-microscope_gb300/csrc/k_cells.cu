@@ -67,16 +67,19 @@ __device__ __forceinline__ void walk_neighbours(const HashDev& h, int32_t gx, in
         hi[r] = e;
     }
     // Visit entries in order, the next record's load in flight while the
-    // current one is evaluated.
+    // current one is evaluated. A row's y and z bucket offsets are fixed, so
+    // their part of the separation, (g - b) * cell with g - b in {-1, 0, 1},
+    // is passed along as an exact constant (cy, cz).
 #pragma unroll 1
     for (int r = 0; r < 9; ++r) {
         const int32_t k0 = lo[r] + lane;
         if (k0 >= hi[r]) continue;
+        const float cy = (float)(1 - r % 3) * h.cell_f, cz = (float)(1 - r / 3) * h.cell_f;
         float4 nxt = __ldg(&h.rec[k0]);
         for (int32_t k = k0; k < hi[r]; k += L) {
             const float4 cur = nxt;
             if (k + L < hi[r]) nxt = __ldg(&h.rec[k + L]);
-            f(k, cur);
+            f(k, cur, cy, cz);
         }
     }
 }
@@ -115,14 +118,17 @@ __device__ __forceinline__ void unpack_bucket(float w, int32_t& gx, int32_t& gy,
     gz = (int32_t)(u >> 22);
 }
 
-// Separation self - other from two snapshot records (FP32, ~2e-7 relative).
-__device__ __forceinline__ void rec_delta(const HashDev& h, const float4& a, int32_t ax, int32_t ay, int32_t az,
-                                          const float4& b, float& dx, float& dy, float& dz) {
-    int32_t bx, by, bz;
-    unpack_bucket(b.w, bx, by, bz);
+// Separation self - other from two snapshot records (FP32, ~2e-7 relative):
+// (bucket delta) * cell + (offset delta), one rounding per axis. The walk
+// supplies the y and z bucket terms of the row (cy, cz; exact, as the delta
+// is -1, 0 or 1), so only the x bucket is unpacked here; the result is the
+// same single rounding of the same exact sum.
+__device__ __forceinline__ void rec_delta(const HashDev& h, const float4& a, int32_t ax, const float4& b,
+                                          float cy, float cz, float& dx, float& dy, float& dz) {
+    const int32_t bx = (int32_t)(__float_as_uint(b.w) & 0x7FFu);
     dx = (float)(ax - bx) * h.cell_f + (a.x - b.x);
-    dy = (float)(ay - by) * h.cell_f + (a.y - b.y);
-    dz = (float)(az - bz) * h.cell_f + (a.z - b.z);
+    dy = cy + (a.y - b.y);
+    dz = cz + (a.z - b.z);
 }
 
 // ---------------------------------------------------------------------------
@@ -406,10 +412,10 @@ __device__ __forceinline__ void feed_cell(DevState* S, const SoA& v, const Ctx& 
         int32_t refined = 0;
         int skip_axis, skip_side;
         shade_skip(c, h, me, skip_axis, skip_side);
-        walk_neighbours<L>(h, gx, gy, gz, [&](int32_t k, const float4& rk) {
+        walk_neighbours<L>(h, gx, gy, gz, [&](int32_t k, const float4& rk, float cy, float cz) {
             if (k == ks) return;
             float dx, dy, dz;
-            rec_delta(h, me, gx, gy, gz, rk, dx, dy, dz);
+            rec_delta(h, me, gx, rk, cy, cz, dx, dy, dz);
             shade_candidate(v, c, h, k, dx, dy, dz, px, py, pz, open, refined);
         }, skip_axis, skip_side, lane);
         if (L > 1) {
@@ -574,10 +580,10 @@ __device__ __forceinline__ void forces_cell(DevState* S, const SoA& v, const Ctx
         int32_t gx, gy, gz;
         unpack_bucket(me.w, gx, gy, gz);
         int32_t refined = 0;
-        walk_neighbours<L>(h, gx, gy, gz, [&](int32_t k, const float4& rk) {
+        walk_neighbours<L>(h, gx, gy, gz, [&](int32_t k, const float4& rk, float cy, float cz) {
             if (k == ks) return;                                    // bucket members are occupied
             float dx, dy, dz;
-            rec_delta(h, me, gx, gy, gz, rk, dx, dy, dz);
+            rec_delta(h, me, gx, rk, cy, cz, dx, dy, dz);
             contact_candidate(v, h, p, k, i, dx, dy, dz, Cx, Cy, Cz, refined);
         }, -1, 0, lane);
         if (L > 1) {
@@ -828,10 +834,10 @@ __global__ void __launch_bounds__(256) cell_step_kernel(DevState* S, Ctx c, Tick
             unpack_bucket(me.w, gx, gy, gz);
             int skip_axis = -1, skip_side = 0;
             if (!contact) shade_skip(c, h, me, skip_axis, skip_side);
-            walk_neighbours<L>(h, gx, gy, gz, [&](int32_t k, const float4& rk) {
+            walk_neighbours<L>(h, gx, gy, gz, [&](int32_t k, const float4& rk, float cy, float cz) {
                 if (k == ks) return;
                 float dx, dy, dz;
-                rec_delta(h, me, gx, gy, gz, rk, dx, dy, dz);
+                rec_delta(h, me, gx, rk, cy, cz, dx, dy, dz);
                 if (shade) shade_candidate(v, c, h, k, dx, dy, dz, px, py, pz, open, rs);
                 if (contact) contact_candidate(v, h, p, k, i, dx, dy, dz, Cx, Cy, Cz, rc);
             }, skip_axis, skip_side, lane);
