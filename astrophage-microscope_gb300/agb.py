@@ -123,7 +123,7 @@ class Stats(C.Structure):
 class BatchOpts(C.Structure):
     _fields_ = [("abi_version", C.c_uint32), ("lanes", C.c_int32), ("autotune", C.c_int32),
                 ("n_hash_candidates", C.c_int32), ("hash_candidates", C.c_double * 8),
-                ("probe_ticks", C.c_int32)]
+                ("probe_ticks", C.c_int32), ("staged", C.c_int32)]
 
 
 class Tuning(C.Structure):
@@ -325,6 +325,7 @@ def load(path=LIB_PATH):
         "agb_batch_tuning": (I32, [P, I32, C.POINTER(Tuning)]),
         "agb_batch_step": (I32, [P, I32, P]),
         "agb_batch_graph_kernels": (I32, [P, C.POINTER(C.c_int64)]),
+        "agb_batch_staged": (I32, [P, C.POINTER(I32)]),
         "agb_batch_stats": (I32, [P, P]),
     }
     for name, (res, args) in sigs.items():
@@ -354,7 +355,7 @@ def exported_symbols():
             "agb_surrogate_error_word", "agb_world_attach_surrogate",
             "agb_batch_opts_default", "agb_batch_create", "agb_batch_destroy", "agb_batch_last_error",
             "agb_batch_size", "agb_batch_world", "agb_batch_tuning", "agb_batch_step",
-            "agb_batch_graph_kernels", "agb_batch_stats"]
+            "agb_batch_graph_kernels", "agb_batch_staged", "agb_batch_stats"]
 
 
 def _st(stream):
@@ -705,12 +706,13 @@ class _ChamberView(World):
         self.h = None
 
 
-def batch_opts(autotune=False, lanes=0, hash_candidates=(), probe_ticks=4, lib=None):
+def batch_opts(autotune=False, lanes=0, hash_candidates=(), probe_ticks=4, staged=True, lib=None):
     lib = lib or load()
     o = BatchOpts()
     lib.agb_batch_opts_default(C.byref(o))
     o.autotune = 1 if autotune else 0
     o.lanes = lanes
+    o.staged = 1 if staged else 0
     o.n_hash_candidates = len(hash_candidates)
     for k, h in enumerate(hash_candidates[:8]):
         o.hash_candidates[k] = h
@@ -771,6 +773,12 @@ class Batch:
         k = C.c_int64()
         self._check(self.lib.agb_batch_graph_kernels(self.h, C.byref(k)), "agb_batch_graph_kernels")
         return k.value
+
+    def staged(self):
+        """True when steps run one launch per stage over every chamber."""
+        k = C.c_int32()
+        self._check(self.lib.agb_batch_staged(self.h, C.byref(k)), "agb_batch_staged")
+        return bool(k.value)
 
     def stats(self):
         out = (Stats * self.n)()

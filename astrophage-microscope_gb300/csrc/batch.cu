@@ -17,10 +17,21 @@
 // with the same operations); the hash cell size changes the order in which
 // contacts are summed, so a tuned chamber equals, bit for bit, a standalone
 // world built with the hash cell size the tuner picked (agb_batch_tuning).
+//
+// Staged ticks (the default when every chamber allows them): instead of each
+// chamber launching its own ~20 kernels per tick, each stage of the tick is
+// one launch over every chamber. The per-world kernel bodies run unchanged;
+// a block finds its chamber and its block within that chamber in a block map
+// and the chamber's arguments in a table, both in device memory owned by the
+// captured graph. FTCS passes are one launch per group of chambers with equal
+// grids and tiling, each with its own tensor map. The stages keep the tick's
+// order and branches (thermal + irradiance | slow fields | hash), so every
+// chamber computes what its own tick would with the same walk shape.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <map>
 #include <new>
 #include <string>
@@ -36,6 +47,7 @@ struct BatchGraph {
     cudaGraphExec_t exec;
     std::vector<uint32_t> parity_after;
     int32_t kernels;
+    char* arena;                            // staged graphs: their argument tables and block maps
 };
 
 }  // namespace
@@ -49,6 +61,9 @@ struct agb_batch {
     std::vector<cudaEvent_t> lane_join;
     cudaEvent_t fork = nullptr;
     cudaStream_t own_stream = nullptr;
+    bool staged = false;                    // one launch per stage over every chamber
+    cudaStream_t side[2] = {nullptr, nullptr};
+    cudaEvent_t sev[3] = {nullptr, nullptr, nullptr};
     std::vector<BatchGraph> graphs;
     int64_t graph_kernels_total = 0;
     std::string err;
@@ -88,8 +103,309 @@ std::vector<uint64_t> batch_key(const agb_batch* b, int32_t ticks) {
 }
 
 void drop_graphs(agb_batch* b) {
-    for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);
+    for (auto& g : b->graphs) {
+        cudaGraphExecDestroy(g.exec);
+        if (g.arena) cudaFree(g.arena);
+    }
     b->graphs.clear();
+}
+
+// ---------------------------------------------------------------------------
+// Staged ticks. plan_tick walks every chamber through one tick in tick_once's
+// order, advancing each chamber's host-side state (buffer parities, clock) as
+// tick_once does, and records the launches with their tables; run_plan
+// replays the recording on the streams (under capture).
+// ---------------------------------------------------------------------------
+enum class OpKind { Launch, Ftcs, Record, Wait };
+
+struct StagedOp {
+    OpKind kind;
+    int32_t stream;                         // 0: the step's stream; 1, 2: the batch's side streams
+    BStage st;
+    size_t tab, map;                        // offsets into the arena
+    int32_t blocks, arg;
+    int32_t nch, nx, ny, nz;
+    FtcsPlan plan;
+    int32_t event;
+};
+
+struct StagedPlan {
+    std::vector<char> bytes;
+    std::vector<StagedOp> ops;
+    std::map<std::vector<uint32_t>, size_t> maps;   // each distinct block map is stored once
+
+    size_t put(const void* p, size_t n) {
+        const size_t off = (bytes.size() + 127) & ~(size_t)127;
+        bytes.resize(off + n);
+        std::memcpy(bytes.data() + off, p, n);
+        return off;
+    }
+    void record(int32_t stream, int32_t ev) {
+        StagedOp o{};
+        o.kind = OpKind::Record; o.stream = stream; o.event = ev;
+        ops.push_back(o);
+    }
+    void wait(int32_t stream, int32_t ev) {
+        StagedOp o{};
+        o.kind = OpKind::Wait; o.stream = stream; o.event = ev;
+        ops.push_back(o);
+    }
+    // One batched stage over the chambers of `args` (each with its nblk).
+    void stage(int32_t stream, BStage st, const std::vector<ChamberArgs>& args, int32_t arg = 0) {
+        std::vector<uint32_t> map;
+        for (size_t k = 0; k < args.size(); ++k)
+            for (int32_t x = 0; x < args[k].nblk; ++x) map.push_back(((uint32_t)k << 16) | (uint32_t)x);
+        if (map.empty()) return;
+        StagedOp o{};
+        o.kind = OpKind::Launch; o.stream = stream; o.st = st; o.arg = arg;
+        o.blocks = (int32_t)map.size();
+        o.tab = put(args.data(), args.size() * sizeof(ChamberArgs));
+        auto it = maps.find(map);
+        if (it == maps.end()) it = maps.emplace(map, put(map.data(), map.size() * sizeof(uint32_t))).first;
+        o.map = it->second;
+        ops.push_back(o);
+    }
+};
+
+ChamberArgs chamber_args(agb_world* w) {
+    world_refresh(w);
+    ChamberArgs a{};
+    a.S = w->S;
+    a.c = w->c;
+    a.p = w->tp;
+    a.stamp_idx = w->stamp_idx;
+    a.factor = w->occl_factor;
+    a.fx = w->fx; a.fy = w->fy; a.fz = w->fz;
+    a.life = w->life;
+    a.kalt = w->kalt; a.valt = w->valt; a.hist = w->hist;
+    a.nblk = w->blocks;
+    const GridDev& co2 = w->c.g[AGB_FIELD_CO2];
+    a.demand = co2.enabled ? w->life.co2_demand : nullptr;
+    a.inv_gv = co2.enabled ? (float)(1.0 / (co2.dx * co2.dx * co2.dz_eff)) : 0.0f;
+    bool per4 = true;
+    hash_sort_shape(w->c.h, w->c.capacity, a.passes, a.max_tiles, per4);
+    return a;
+}
+
+// One FTCS pass of field f for each chamber of `ws`, grouped by grid and
+// tiling; flips each chamber's buffer parity as ftcs() does.
+void plan_ftcs(StagedPlan& P, int32_t stream, const std::vector<agb_world*>& ws, int f) {
+    std::map<std::vector<int32_t>, std::vector<FtcsChamber>> groups;
+    for (agb_world* w : ws) {
+        world_refresh(w);
+        const GridDev& g = w->c.g[f];
+        const FtcsPlan& pl = w->tplan[f];
+        FtcsChamber e{};
+        e.map = w->tmap[f][w->gcur[f]];
+        e.dst = w->gbuf[f][1 - w->gcur[f]];
+        e.err = &w->S->error;
+        e.coeff = f == AGB_FIELD_TEMPERATURE ? w->tp.t_coeff : (f == AGB_FIELD_CO2 ? w->tp.c_coeff : w->tp.n_coeff);
+        e.robin = w->grobin[f];
+        for (int k = 0; k < 6; ++k) { e.bc[k] = w->gbc[f][k]; e.face[k] = w->gface[f][k]; }
+        groups[{g.nx, g.ny, g.nz, pl.lx, pl.rpt}].push_back(e);
+        w->gcur[f] = 1 - w->gcur[f];
+        world_refresh(w);
+    }
+    for (const auto& kv : groups) {
+        StagedOp o{};
+        o.kind = OpKind::Ftcs; o.stream = stream;
+        o.nx = kv.first[0]; o.ny = kv.first[1]; o.nz = kv.first[2];
+        o.nch = (int32_t)kv.second.size();
+        // Tilings give the same bits; the z chunk is re-chosen for the group.
+        o.plan = ftcs_plan_copies(o.nx, o.ny, o.nz, kv.first[3], kv.first[4], 0, o.nch);
+        o.tab = P.put(kv.second.data(), kv.second.size() * sizeof(FtcsChamber));
+        P.ops.push_back(o);
+    }
+}
+
+// Whether every chamber can run staged ticks: every diffused grid 3-D with a
+// TMA stencil, no surrogate, one lane per cell in fused walks.
+bool staged_ok(const agb_batch* b) {
+    for (const agb_world* w : b->worlds) {
+        if (w->sg || w->walk_lanes != 1 || !w->fuse_cells) return false;
+        for (int f = 0; f < 3; ++f) {
+            const GridDev& g = w->c.g[f];
+            if (g.enabled && (g.nz <= 1 || !w->use_tma || !w->tmap_ok[f])) return false;
+        }
+    }
+    return true;
+}
+
+// tick_once (world.cu) for every chamber at once.
+void plan_tick(agb_batch* b, StagedPlan& P) {
+    const std::vector<agb_world*>& W = b->worlds;
+    const size_t n = W.size();
+    P.record(0, 0);
+    P.wait(1, 0);
+    P.wait(2, 0);
+    // Branch 1: thermal substeps (thermal, flush, FTCS), then the irradiance field.
+    std::vector<int32_t> nsub(n, 0);
+    int32_t maxsub = 0;
+    for (size_t i = 0; i < n; ++i) {
+        const agb_world* w = W[i];
+        nsub[i] = (w->d.thermal_enabled && w->c.g[AGB_FIELD_TEMPERATURE].enabled) ? w->tp.t_substeps : 0;
+        maxsub = std::max(maxsub, nsub[i]);
+    }
+    for (int32_t k = 0; k < maxsub; ++k) {
+        std::vector<agb_world*> act;
+        std::vector<ChamberArgs> th, fl;
+        for (size_t i = 0; i < n; ++i) {
+            if (k >= nsub[i]) continue;
+            ChamberArgs a = chamber_args(W[i]);
+            th.push_back(a);
+            a.g = W[i]->c.g[AGB_FIELD_TEMPERATURE];
+            fl.push_back(a);
+            act.push_back(W[i]);
+        }
+        P.stage(1, BStage::Thermal, th);
+        P.stage(1, BStage::Flush, fl);
+        plan_ftcs(P, 1, act, AGB_FIELD_TEMPERATURE);
+    }
+    std::vector<uint8_t> emit(n, 0);
+    {
+        std::vector<ChamberArgs> clr, stp, swr, swl;
+        for (size_t i = 0; i < n; ++i) {
+            agb_world* w = W[i];
+            if (!world_emission_active(w)) continue;
+            emit[i] = 1;
+            ChamberArgs a = chamber_args(w);
+            clr.push_back(a);
+            if (w->c.source > 0.0f) stp.push_back(a);
+            const GridDev& I = w->c.g[AGB_FIELD_IRRADIANCE];
+            const int axis = w->c.light_axis;
+            const int64_t len = axis == 0 ? I.nx : (axis == 1 ? I.ny : I.nz);
+            const int64_t lines = I.count / len;
+            if (axis == 0) {
+                const int64_t bl = (lines * 32 + 255) / 256;
+                a.nblk = (int32_t)(bl < 65535 ? bl : 65535);
+                swr.push_back(a);
+            } else {
+                a.nblk = (int32_t)((lines + 127) / 128);
+                swl.push_back(a);
+            }
+        }
+        P.stage(1, BStage::ClearStamps, clr);
+        P.stage(1, BStage::Stamp, stp);
+        P.stage(1, BStage::Occlusion, stp);
+        P.stage(1, BStage::SweepRows, swr);
+        P.stage(1, BStage::SweepLines, swl);
+    }
+    P.record(1, 1);
+    // Motion samples CO2 and N2 as they stand before this tick's slow fields.
+    std::vector<Ctx> pre(n);
+    for (size_t i = 0; i < n; ++i) {
+        world_refresh(W[i]);
+        pre[i] = W[i]->c;
+    }
+    // Branch 2: slow fields.
+    for (int f : {AGB_FIELD_CO2, AGB_FIELD_N2}) {
+        int32_t maxs = 0;
+        for (const agb_world* w : W)
+            if (w->c.g[f].enabled) maxs = std::max(maxs, f == AGB_FIELD_CO2 ? w->tp.c_substeps : w->tp.n_substeps);
+        for (int32_t k = 0; k < maxs; ++k) {
+            std::vector<agb_world*> act;
+            for (agb_world* w : W)
+                if (w->c.g[f].enabled && k < (f == AGB_FIELD_CO2 ? w->tp.c_substeps : w->tp.n_substeps))
+                    act.push_back(w);
+            plan_ftcs(P, 2, act, f);
+        }
+    }
+    P.record(2, 2);
+    // Main branch: the hash.
+    {
+        std::vector<ChamberArgs> hc, kh;
+        int32_t maxp = 0;
+        for (agb_world* w : W) {
+            ChamberArgs a = chamber_args(w);
+            kh.push_back(a);
+            a.nblk = hash_clear_blocks(a.passes, a.max_tiles);
+            hc.push_back(a);
+            maxp = std::max(maxp, a.passes);
+        }
+        P.stage(0, BStage::HashClear, hc);
+        P.stage(0, BStage::KeyHist, kh);
+        for (int32_t p = 0; p < maxp; ++p) {
+            std::vector<ChamberArgs> r4, r8;
+            for (size_t i = 0; i < n; ++i) {
+                if (p >= kh[i].passes) continue;
+                ChamberArgs a = kh[i];
+                int32_t passes = 0, tiles = 0;
+                bool per4 = true;
+                hash_sort_shape(W[i]->c.h, W[i]->c.capacity, passes, tiles, per4);
+                a.nblk = tiles;
+                (per4 ? r4 : r8).push_back(a);
+            }
+            P.stage(0, BStage::Radix4, r4, p);
+            P.stage(0, BStage::Radix8, r8, p);
+        }
+        P.stage(0, BStage::Ranges, kh);
+    }
+    P.wait(0, 1);
+    // Feeding, taxis and forces in one pass; then integration with the CO2 demand.
+    {
+        std::vector<ChamberArgs> cs, ig;
+        for (size_t i = 0; i < n; ++i) {
+            agb_world* w = W[i];
+            ChamberArgs a = chamber_args(w);
+            for (int f : {AGB_FIELD_CO2, AGB_FIELD_N2}) a.c.g[f] = pre[i].g[f];
+            a.arg = (emit[i] ? 1 : 0) | (w->d.taxis_enabled ? 2 : 0);
+            cs.push_back(a);
+            a.g = w->c.g[AGB_FIELD_CO2];
+            ig.push_back(a);
+        }
+        P.stage(0, BStage::CellStep, cs);
+        P.wait(0, 2);
+        P.stage(0, BStage::Integrate, ig);
+    }
+    // Lifecycle and, on compaction ticks, compaction.
+    {
+        std::vector<ChamberArgs> um, sc, dv, kp, sc1, ga, sw;
+        for (agb_world* w : W) {
+            ChamberArgs a = chamber_args(w);
+            const bool compact = world_compaction_allowed(w);
+            um.push_back(a);
+            ChamberArgs d = a;
+            d.arg = compact ? 1 : 0;
+            dv.push_back(d);
+            ChamberArgs q = a;
+            q.nblk = scan_blocks(w->c.capacity);
+            sc.push_back(q);
+            if (compact) {
+                kp.push_back(a);
+                sc1.push_back(q);
+                ChamberArgs one = a;
+                one.nblk = 1;
+                sw.push_back(one);
+            }
+        }
+        P.stage(0, BStage::UptakeMark, um);
+        P.stage(0, BStage::Scan, sc, 0);
+        P.stage(0, BStage::Divide, dv);
+        P.stage(0, BStage::Keep, kp);
+        P.stage(0, BStage::Scan, sc1, 1);
+        P.stage(0, BStage::ScatterSrc, kp);
+        P.stage(0, BStage::Gather, kp);
+        P.stage(0, BStage::Swap, sw);
+    }
+    for (agb_world* w : W) world_advance_clock(w, 1);
+}
+
+void run_plan(agb_batch* b, const StagedPlan& P, char* arena, cudaStream_t s) {
+    cudaStream_t st[3] = {s, b->side[0], b->side[1]};
+    for (const StagedOp& o : P.ops) {
+        switch (o.kind) {
+            case OpKind::Launch:
+                launch_batched(o.st, reinterpret_cast<const ChamberArgs*>(arena + o.tab),
+                               reinterpret_cast<const uint32_t*>(arena + o.map), o.blocks, o.arg, st[o.stream]);
+                break;
+            case OpKind::Ftcs:
+                launch_ftcs_batch(reinterpret_cast<const FtcsChamber*>(arena + o.tab), o.nch, o.nx, o.ny, o.nz,
+                                  o.plan, st[o.stream]);
+                break;
+            case OpKind::Record: cudaEventRecord(b->sev[o.event], st[o.stream]); break;
+            case OpKind::Wait: cudaStreamWaitEvent(st[o.stream], b->sev[o.event], 0); break;
+        }
+    }
 }
 
 // Median ms per tick of `ticks` graph-replayed ticks. The warm-up runs two
@@ -199,6 +515,7 @@ void agb_batch_opts_default(agb_batch_opts* o) {
     o->autotune = 0;
     o->n_hash_candidates = 0;
     o->probe_ticks = 4;
+    o->staged = 1;
 }
 
 void agb_batch_destroy(agb_batch* b) {
@@ -208,6 +525,8 @@ void agb_batch_destroy(agb_batch* b) {
     for (cudaStream_t st : b->lane_streams) if (st) cudaStreamDestroy(st);
     for (cudaEvent_t e : b->lane_join) if (e) cudaEventDestroy(e);
     if (b->fork) cudaEventDestroy(b->fork);
+    for (cudaStream_t st : b->side) if (st) cudaStreamDestroy(st);
+    for (cudaEvent_t e : b->sev) if (e) cudaEventDestroy(e);
     if (b->own_stream) cudaStreamDestroy(b->own_stream);
     delete b;
 }
@@ -311,8 +630,18 @@ agb_status agb_batch_create(const agb_world_desc* descs, const agb_spawn* spawns
     for (int32_t l = 0; l < b->lanes && ok; ++l)
         ok = cudaStreamCreateWithFlags(&b->lane_streams[(size_t)l], cudaStreamNonBlocking) == cudaSuccess &&
              cudaEventCreateWithFlags(&b->lane_join[(size_t)l], cudaEventDisableTiming) == cudaSuccess;
+    for (cudaStream_t& st : b->side)
+        ok = ok && cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess;
+    for (cudaEvent_t& e : b->sev) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
     ok = ok && cudaStreamSynchronize(s) == cudaSuccess;
     if (!ok) { agb_batch_destroy(b); return AGB_CUDA_ERROR; }
+    // Staged ticks run every chamber's walks fused, one lane per cell.
+    if (o.staged) {
+        for (agb_world* w : b->worlds) w->fuse_cells = true;
+        b->staged = staged_ok(b);
+        if (!b->staged)
+            for (agb_world* w : b->worlds) w->fuse_cells = (int64_t)w->c.capacity <= (int64_t)w->sm_count * 512;
+    }
     *out = b;
     return AGB_OK;
 }
@@ -352,25 +681,50 @@ agb_status agb_batch_step(agb_batch* b, int32_t ticks, agb_stream stream) {
         }
         return AGB_OK;
     }
-    // Capture: fork every lane off s, run each lane's chambers one after the
-    // other (each tick forks onto the chamber's own side streams), join.
-    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) return bfail(b, AGB_CUDA_ERROR, std::string("cudaStreamBeginCapture: ") + cudaGetErrorString(e));
-    cudaEventRecord(b->fork, s);
-    for (cudaStream_t ls : b->lane_streams) cudaStreamWaitEvent(ls, b->fork, 0);
-    for (int32_t i : b->order) {
-        agb_world* w = b->worlds[(size_t)i];
-        cudaStream_t ls = b->lane_streams[(size_t)b->tuning[(size_t)i].lane];
-        for (int32_t t = 0; t < ticks; ++t) world_tick(w, ls);
+    const bool staged = b->staged && staged_ok(b);
+    StagedPlan plan;
+    char* arena = nullptr;
+    if (staged) {
+        // Plan every tick (advancing the chambers' host state), then put the
+        // tables in device memory before capturing the launches that read them.
+        for (int32_t t = 0; t < ticks; ++t) plan_tick(b, plan);
+        cudaError_t e = cudaMalloc(&arena, plan.bytes.size() > 0 ? plan.bytes.size() : 128);
+        if (e == cudaSuccess && !plan.bytes.empty())
+            e = cudaMemcpy(arena, plan.bytes.data(), plan.bytes.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            if (arena) cudaFree(arena);
+            return bfail(b, AGB_CUDA_ERROR, std::string("staged tables: ") + cudaGetErrorString(e));
+        }
     }
-    for (int32_t l = 0; l < b->lanes; ++l) {
-        cudaEventRecord(b->lane_join[(size_t)l], b->lane_streams[(size_t)l]);
-        cudaStreamWaitEvent(s, b->lane_join[(size_t)l], 0);
+    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        if (arena) cudaFree(arena);
+        return bfail(b, AGB_CUDA_ERROR, std::string("cudaStreamBeginCapture: ") + cudaGetErrorString(e));
+    }
+    if (staged) {
+        run_plan(b, plan, arena, s);
+    } else {
+        // Fork every lane off s, run each lane's chambers one after the other
+        // (each tick forks onto the chamber's own side streams), join.
+        cudaEventRecord(b->fork, s);
+        for (cudaStream_t ls : b->lane_streams) cudaStreamWaitEvent(ls, b->fork, 0);
+        for (int32_t i : b->order) {
+            agb_world* w = b->worlds[(size_t)i];
+            cudaStream_t ls = b->lane_streams[(size_t)b->tuning[(size_t)i].lane];
+            for (int32_t t = 0; t < ticks; ++t) world_tick(w, ls);
+        }
+        for (int32_t l = 0; l < b->lanes; ++l) {
+            cudaEventRecord(b->lane_join[(size_t)l], b->lane_streams[(size_t)l]);
+            cudaStreamWaitEvent(s, b->lane_join[(size_t)l], 0);
+        }
     }
     cudaGraph_t graph = nullptr;
     e = cudaStreamEndCapture(s, &graph);
-    if (e != cudaSuccess) return bfail(b, AGB_CUDA_ERROR, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
-    BatchGraph bg{key, nullptr, {}, 0};
+    if (e != cudaSuccess) {
+        if (arena) cudaFree(arena);
+        return bfail(b, AGB_CUDA_ERROR, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
+    }
+    BatchGraph bg{key, nullptr, {}, 0, arena};
     {
         size_t nn = 0;
         cudaGraphGetNodes(graph, nullptr, &nn);
@@ -383,13 +737,22 @@ agb_status agb_batch_step(agb_batch* b, int32_t ticks, agb_stream stream) {
     }
     e = cudaGraphInstantiate(&bg.exec, graph, 0);
     cudaGraphDestroy(graph);
-    if (e != cudaSuccess) return bfail(b, AGB_CUDA_ERROR, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    if (e != cudaSuccess) {
+        if (arena) cudaFree(arena);
+        return bfail(b, AGB_CUDA_ERROR, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    }
     // Capture advanced each chamber's host-side state; the graph has not run yet.
     for (agb_world* w : b->worlds) bg.parity_after.push_back(world_parity(w));
     e = cudaGraphLaunch(bg.exec, s);
     b->graphs.push_back(std::move(bg));
     if (e != cudaSuccess) return bfail(b, AGB_CUDA_ERROR, std::string("cudaGraphLaunch: ") + cudaGetErrorString(e));
     b->graph_kernels_total += b->graphs.back().kernels;
+    return AGB_OK;
+}
+
+agb_status agb_batch_staged(agb_batch* b, int32_t* staged) {
+    if (!b || !staged) return AGB_INVALID_ARGUMENT;
+    *staged = (b->staged && staged_ok(b)) ? 1 : 0;
     return AGB_OK;
 }
 

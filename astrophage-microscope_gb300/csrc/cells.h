@@ -15,6 +15,69 @@ struct LifeBuffers {
     unsigned long long* co2_demand;   // per CO2 voxel, fixed point (src/sim/world.cuh:108)
 };
 
+// ---------------------------------------------------------------------------
+// Batched stages (agb_batch): one launch runs a stage for many chambers. The
+// grid's blocks are shared out over the chambers: block k works for chamber
+// map[k] >> 16 as its block map[k] & 0xFFFF of that chamber's nblk, with the
+// chamber's entry of a device table of ChamberArgs, through the same kernel
+// bodies as the per-world launches.
+// ---------------------------------------------------------------------------
+struct ChamberArgs {
+    DevState* S;
+    Ctx c;                        // the chamber's context as this stage sees it
+    TickParams p;
+    GridDev g;                    // flush: the grid flushed; integrate: the diffused CO2 grid
+    int32_t* stamp_idx;
+    double* factor;
+    float *fx, *fy, *fz;
+    unsigned long long* demand;   // CO2 rationing words (null: no CO2 grid)
+    LifeBuffers life;
+    uint32_t *kalt, *valt, *hist; // hash sort scratch
+    float inv_gv;
+    int32_t nblk;                 // the chamber's blocks in this launch
+    int32_t arg;                  // stage switch (cell step: feed | taxis << 1; divide: compaction allowed)
+    int32_t passes, max_tiles;    // hash sort: digit passes, tiles per pass
+};
+
+// A batched kernel NAME(tab, map): finds its chamber and block, then CALL
+// (which sees the chamber's arguments as `a` and its block as `blk`).
+#define AGB_BATCHED(NAME, THREADS, CALL)                                                             \
+    __global__ void __launch_bounds__(THREADS) NAME(const ChamberArgs* __restrict__ tab,              \
+                                                    const uint32_t* __restrict__ map) {              \
+        pdl_wait();                                                                                  \
+        int32_t ch_, x_;                                                                             \
+        batch_block(map, ch_, x_);                                                                   \
+        const ChamberArgs& a = tab[ch_];                                                             \
+        const Blk blk{x_, a.nblk};                                                                   \
+        CALL;                                                                                        \
+    }
+
+enum class BStage : int32_t {
+    Thermal, ClearStamps, Stamp, Occlusion, SweepRows, SweepLines, CellStep, Integrate,   // k_cells.cu
+    Flush,                                                                                // k_grid.cu
+    HashClear, KeyHist, Radix4, Radix8, Ranges,                                           // k_hash.cu
+    UptakeMark, Scan, Divide, Keep, ScatterSrc, Gather, Swap                              // k_life.cu
+};
+// Threads per block of a batched stage.
+int32_t bstage_threads(BStage st);
+// Enqueue one batched stage over `blocks` blocks. `arg`: the radix pass index
+// (Radix4/8) or the scan gate (Scan: 0 division, 1 compaction).
+void launch_batched(BStage st, const ChamberArgs* tab, const uint32_t* map, int32_t blocks, int32_t arg,
+                    cudaStream_t s);
+// The per-file halves of launch_batched; each returns false for a stage it does not own.
+bool launch_batched_cells(BStage st, const ChamberArgs* tab, const uint32_t* map, int32_t blocks, cudaStream_t s);
+bool launch_batched_grid(BStage st, const ChamberArgs* tab, const uint32_t* map, int32_t blocks, cudaStream_t s);
+bool launch_batched_hash(BStage st, const ChamberArgs* tab, const uint32_t* map, int32_t blocks, int32_t arg,
+                         cudaStream_t s);
+bool launch_batched_life(BStage st, const ChamberArgs* tab, const uint32_t* map, int32_t blocks, int32_t arg,
+                         cudaStream_t s);
+// Blocks of a chamber in a batched stage, as the per-world launches size them.
+int32_t hash_clear_blocks(int32_t passes, int32_t max_tiles);
+int32_t scan_blocks(int32_t capacity);
+// Digit passes and tiles per pass of the hash sort for a world, and whether its
+// tiles are 1024 keys (Radix4) or 2048 (Radix8).
+void hash_sort_shape(const HashDev& h, int32_t capacity, int32_t& passes, int32_t& max_tiles, bool& per4);
+
 // co2_uptake_rate (src/sim/lifecycle.cuh:24-28) in FP32.
 __device__ __forceinline__ float co2_uptake_rate_f(float c) {
     if (c <= 0.0f) return 0.0f;

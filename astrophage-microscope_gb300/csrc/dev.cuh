@@ -378,4 +378,23 @@ __device__ __forceinline__ unsigned long long dkey(double v) {
 #define AGB_FOR_CELLS(i, n) \
     for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += gridDim.x * blockDim.x)
 
+// The block a kernel body works as: a plain launch over one world uses its
+// own grid; a batched launch over many chambers gives each chamber a run of
+// the grid's blocks, and a body sees only its chamber's block index and count.
+struct Blk {
+    int32_t x, n;
+};
+__device__ __forceinline__ Blk grid_blk() { return Blk{(int32_t)blockIdx.x, (int32_t)gridDim.x}; }
+#define AGB_FOR_CELLS_B(i_, blk_, count_)                                                      \
+    for (int32_t i_ = (blk_).x * (int32_t)blockDim.x + (int32_t)threadIdx.x; i_ < (count_); \
+         i_ += (blk_).n * (int32_t)blockDim.x)
+
+// Block map of a batched launch: entry k = (chamber << 16) | (block within the
+// chamber) for block k of the grid.
+__device__ __forceinline__ void batch_block(const uint32_t* __restrict__ map, int32_t& ch, int32_t& x) {
+    const uint32_t m = __ldg(&map[blockIdx.x]);
+    ch = (int32_t)(m >> 16);
+    x = (int32_t)(m & 0xFFFFu);
+}
+
 }  // namespace agb

@@ -134,12 +134,11 @@ __device__ __forceinline__ void rec_delta(const HashDev& h, const float4& a, int
 // ---------------------------------------------------------------------------
 // Thermal substep (thermal_kernel, src/sim/thermal.cu:19-71)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) thermal_kernel(DevState* S, Ctx c, TickParams p) {
-    pdl_wait();
+__device__ __forceinline__ void thermal_kernel_body(DevState* S, const Ctx& c, const TickParams& p, Blk blk) {
     const SoA v = S->cur;
     const int32_t n = S->count;
     const GridDev T = c.g[AGB_FIELD_TEMPERATURE];
-    AGB_FOR_CELLS(i, n) {
+    AGB_FOR_CELLS_B(i, blk, n) {
         const uint32_t flags = v.flags[i];
         if (!(flags & AGB_FLAG_OCCUPIED)) continue;
         const int64_t idx = grid_nearest(T, d2f(v.x[i]), d2f(v.y[i]), d2f(v.z[i]));
@@ -177,50 +176,73 @@ __global__ void __launch_bounds__(256) thermal_kernel(DevState* S, Ctx c, TickPa
     }
 }
 
+__global__ void __launch_bounds__(256) thermal_kernel(DevState* S, Ctx c, TickParams p) {
+    pdl_wait();
+    thermal_kernel_body(S, c, p, grid_blk());
+}
+
 // ---------------------------------------------------------------------------
 // Emission (src/sim/emission.cu:17-177)
 // ---------------------------------------------------------------------------
-__global__ void clear_stamps_kernel(DevState* S, Ctx c, const int32_t* __restrict__ stamp_idx) {
-    pdl_wait();
+__device__ __forceinline__ void clear_stamps_kernel_body(DevState* S, const Ctx& c,
+                                                         const int32_t* __restrict__ stamp_idx, Blk blk) {
     const int32_t n = S->n_stamps;
     unsigned long long* dep = c.g[AGB_FIELD_IRRADIANCE].deposit;
-    AGB_FOR_CELLS(i, n) {
+    AGB_FOR_CELLS_B(i, blk, n) {
         const int32_t idx = stamp_idx[i];
         if (idx >= 0) dep[idx] = 0ull;
     }
 }
 
+__global__ void clear_stamps_kernel(DevState* S, Ctx c, const int32_t* __restrict__ stamp_idx) {
+    pdl_wait();
+    clear_stamps_kernel_body(S, c, stamp_idx, grid_blk());
+}
+
+// The sweep line through voxel idx for light along `axis` (the numbering the
+// sweeps use: x rows by y + ny z, y columns by x + nx z, z columns by x + nx y).
+__device__ __forceinline__ int64_t irr_line(const GridDev& I, int axis, int64_t idx) {
+    const int64_t plane = (int64_t)I.nx * I.ny;
+    if (axis == 0) return idx / I.nx;
+    if (axis == 1) return idx % I.nx + (int64_t)I.nx * (idx / plane);
+    return idx % plane;
+}
+
 // occlusion_stamp_kernel (emission.cu:17-27). Also records each cell's voxel so
 // the next emission stage can clear exactly these voxels.
-__global__ void stamp_kernel(DevState* S, Ctx c, int32_t* stamp_idx) {
-    pdl_wait();
+__device__ __forceinline__ void stamp_kernel_body(DevState* S, const Ctx& c, int32_t* stamp_idx, Blk blk) {
     const SoA v = S->cur;
     const int32_t n = S->count;
-    if (blockIdx.x == 0 && threadIdx.x == 0) S->n_stamps = n;
+    if (blk.x == 0 && threadIdx.x == 0) S->n_stamps = n;
     const GridDev I = c.g[AGB_FIELD_IRRADIANCE];
-    AGB_FOR_CELLS(i, n) {
+    AGB_FOR_CELLS_B(i, blk, n) {
         const uint32_t f = v.flags[i];
         int32_t rec = -1;
         if (f & AGB_FLAG_OCCUPIED) {
             const int64_t idx = grid_nearest(I, d2f(v.x[i]), d2f(v.y[i]), d2f(v.z[i]));
             deposit_fixed(&I.deposit[idx], (f & AGB_FLAG_ALIVE) ? c.stamp_alive : c.stamp_dead);
             rec = (int32_t)idx;
+            if (c.irr_marks) c.irr_marks[irr_line(I, c.light_axis, idx)] = 1;
         }
         stamp_idx[i] = rec;
     }
+}
+
+__global__ void stamp_kernel(DevState* S, Ctx c, int32_t* stamp_idx) {
+    pdl_wait();
+    stamp_kernel_body(S, c, stamp_idx, grid_blk());
 }
 
 // column_transmittance (emission.cuh:43-47) of every stamped voxel, computed
 // once per cell in full warps (FP64 divisions in divergent sweep code would
 // cost a whole warp's FP64 issue time per stamped voxel). Duplicate cells of a
 // voxel write the same value.
-__global__ void __launch_bounds__(256) occlusion_factor_kernel(DevState* S, Ctx c,
-                                                               const int32_t* __restrict__ stamp_idx,
-                                                               double* factor) {
-    pdl_wait();
+__device__ __forceinline__ void occlusion_factor_kernel_body(DevState* S, const Ctx& c,
+                                                             const int32_t* __restrict__ stamp_idx, double* factor,
+                                                             Blk blk) {
     const int32_t n = S->n_stamps;
     const GridDev I = c.g[AGB_FIELD_IRRADIANCE];
-    AGB_FOR_CELLS(i, n) {
+    AGB_FOR_CELLS_B(i, blk, n) {
         const int32_t idx = stamp_idx[i];
         if (idx < 0) continue;
         const double area = (double)(long long)I.deposit[idx] / I.scale;   // from_fixed
@@ -229,14 +251,20 @@ __global__ void __launch_bounds__(256) occlusion_factor_kernel(DevState* S, Ctx 
     }
 }
 
+__global__ void __launch_bounds__(256) occlusion_factor_kernel(DevState* S, Ctx c,
+                                                               const int32_t* __restrict__ stamp_idx,
+                                                               double* factor) {
+    pdl_wait();
+    occlusion_factor_kernel_body(S, c, stamp_idx, factor, grid_blk());
+}
+
 // sweep_kernel (emission.cu:37-53): one thread per line in sweep order. The
 // FP64 transmittance recurrence runs only at stamped voxels (an empty voxel's
 // factor is exactly 1), and the float output only changes there, so empty
 // voxels cost one load and one store.
 constexpr int SWEEP_PF = 16;
 
-__global__ void __launch_bounds__(128) sweep_kernel(Ctx c, const double* __restrict__ factor) {
-    pdl_wait();
+__device__ __forceinline__ void sweep_kernel_body(const Ctx& c, const double* __restrict__ factor, Blk blk) {
     const GridDev I = c.g[AGB_FIELD_IRRADIANCE];
     const int32_t nx = I.nx, ny = I.ny;
     const int64_t plane = (int64_t)nx * ny;
@@ -244,8 +272,11 @@ __global__ void __launch_bounds__(128) sweep_kernel(Ctx c, const double* __restr
     const int32_t len = axis == 0 ? nx : (axis == 1 ? ny : I.nz);
     const int64_t stride = axis == 0 ? 1 : (axis == 1 ? nx : plane);
     const int64_t lines = I.count / len;
-    for (int64_t line = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; line < lines;
-         line += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t line = blk.x * (int64_t)blockDim.x + threadIdx.x; line < lines;
+         line += (int64_t)blk.n * blockDim.x) {
+        const uint8_t mark = c.irr_marks ? c.irr_marks[line] : 1;
+        if (mark == 0) continue;                           // values already unshadowed
+        if (c.irr_marks) c.irr_marks[line] = mark == 1 ? 2 : 0;
         int64_t base;
         if (axis == 0) base = line * nx;
         else if (axis == 1) base = (line % nx) + (line / nx) * plane;
@@ -275,18 +306,26 @@ __global__ void __launch_bounds__(128) sweep_kernel(Ctx c, const double* __restr
     }
 }
 
+__global__ void __launch_bounds__(128) sweep_kernel(Ctx c, const double* __restrict__ factor) {
+    pdl_wait();
+    sweep_kernel_body(c, factor, grid_blk());
+}
+
 // x-axis sweep: rows are contiguous in memory, so one warp takes a row, 32
 // consecutive voxels per step (coalesced). Stamped voxels are rare; the FP64
 // recurrence walks them in sweep order, broadcasting each factor.
-__global__ void __launch_bounds__(256) sweep_rows_kernel(Ctx c, const double* __restrict__ factor) {
-    pdl_wait();
+__device__ __forceinline__ void sweep_rows_kernel_body(const Ctx& c, const double* __restrict__ factor, Blk blk) {
     const GridDev I = c.g[AGB_FIELD_IRRADIANCE];
     const int lane = threadIdx.x & 31;
-    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t warp = ((int64_t)blk.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)blk.n * blockDim.x) >> 5;
     const int32_t len = I.nx;
     const int64_t lines = I.count / len;
     for (int64_t line = warp; line < lines; line += nwarps) {
+        const uint8_t mark = c.irr_marks ? c.irr_marks[line] : 1;    // one byte, broadcast to the warp
+        if (mark == 0) continue;                                    // values already unshadowed
+        __syncwarp();
+        if (c.irr_marks && lane == 0) c.irr_marks[line] = mark == 1 ? 2 : 0;
         const int64_t base = line * len;
         double t = 1.0;
         float cur = fa(d2f((double)c.source * t), c.ambient_irr);
@@ -310,6 +349,11 @@ __global__ void __launch_bounds__(256) sweep_rows_kernel(Ctx c, const double* __
             if (in) I.value[idx] = mine;
         }
     }
+}
+
+__global__ void __launch_bounds__(256) sweep_rows_kernel(Ctx c, const double* __restrict__ factor) {
+    pdl_wait();
+    sweep_rows_kernel_body(c, factor, grid_blk());
 }
 
 // disc_overlap_fraction / shadow_fraction in FP64 (emission.cuh:19-37): the
@@ -344,18 +388,20 @@ __device__ __forceinline__ void shade_candidate(const SoA& v, const Ctx& c, cons
                                                 int32_t& refined) {
     const float two_a = (float)AGB_CELL_DIAMETER;
     const float a_f = (float)AGB_CELL_RADIUS;
-    const float along = dx * c.lx + dy * c.ly + dz * c.lz;
+    // Products and sums rounded explicitly: every kernel that inlines this
+    // (per world or batched) forms the same bits.
+    const float along = __fmaf_rn(dz, c.lz, __fmaf_rn(dy, c.ly, __fmul_rn(dx, c.lx)));
     // Geometry first (cheap, rejects most candidates); FP64 only near the
     // thresholds; the neighbour's flags only for real shadowers.
     if (along < -1e-6f * two_a) return;
-    const float qx = dx - along * c.lx, qy = dy - along * c.ly, qz = dz - along * c.lz;
-    const float perp = sqrtf(qx * qx + qy * qy + qz * qz);
+    const float qx = __fmaf_rn(-along, c.lx, dx), qy = __fmaf_rn(-along, c.ly, dy), qz = __fmaf_rn(-along, c.lz, dz);
+    const float perp = sqrtf(__fmaf_rn(qz, qz, __fmaf_rn(qy, qy, __fmul_rn(qx, qx))));
     if (along > 1e-6f * two_a && perp >= two_a * (1.0f + 1e-6f)) return;
     const int32_t j = (int32_t)__ldg(&h.vals_sorted[k]);
     if (!(v.flags[j] & AGB_FLAG_ALIVE)) return;   // current flags: thermal may have starved j
     if (along > 1e-6f * two_a && perp > 1e-2f * two_a && perp < two_a * (1.0f - 1e-6f)) {
         const float x = perp / (2.0f * a_f);
-        const float frac = 0.63661977f * (acosf(x) - x * sqrtf(1.0f - x * x));
+        const float frac = __fmul_rn(0.63661977f, __fmaf_rn(-x, sqrtf(__fmaf_rn(-x, x, 1.0f)), acosf(x)));
         open *= (1.0f - frac);
         return;
     }
@@ -391,8 +437,9 @@ __device__ __forceinline__ float feed_directional(const Ctx& c, double px, doubl
 __device__ __forceinline__ void feed_finish(const SoA& v, const Ctx& c, const TickParams& p, int32_t i,
                                             float directional) {
     v.irradiance[i] = directional;
-    const float gained = (directional * (float)AGB_CELL_CROSS_SECTION +
-                          c.ambient_irr * (float)AGB_CELL_SURFACE_AREA) * p.dtf;
+    const float gained = __fmul_rn(__fmaf_rn(directional, (float)AGB_CELL_CROSS_SECTION,
+                                             __fmul_rn(c.ambient_irr, (float)AGB_CELL_SURFACE_AREA)),
+                                   p.dtf);
     double e = v.energy[i] + f2d(gained);
     if (dkey(e) > dkey(AGB_CELL_ENERGY_MAX)) e = AGB_CELL_ENERGY_MAX;
     v.energy[i] = e;
@@ -466,7 +513,7 @@ __device__ __forceinline__ float ou_shape_f(float x) {
         return x * x * x * s;
     }
     const float em = expm1f(-x);
-    return 2.0f * (x + em) - em * em;
+    return __fmaf_rn(-em, em, __fmul_rn(2.0f, x + em));
 }
 
 // One axis of the joint OU propagator (ou_advance_axis, integrator.cuh:128-154):
@@ -475,13 +522,13 @@ __device__ __forceinline__ float ou_axis(float& vel, float force, float gamma, f
                                          float inv_beta, bool noise, float s_rr, float a, float b,
                                          float s_vv, float z1, float z2) {
     const float v_term = force / gamma;
-    float dpos = v_term * dtf + (vel - v_term) * ome * inv_beta;
-    float nvel = vel + (v_term - vel) * ome;
+    float dpos = __fmaf_rn(v_term, dtf, __fmul_rn(__fmul_rn(vel - v_term, ome), inv_beta));
+    float nvel = __fmaf_rn(v_term - vel, ome, vel);
     if (noise && s_rr > 0.0f) {
-        dpos += s_rr * z1;
-        nvel += a * z1 + b * z2;
+        dpos = __fmaf_rn(s_rr, z1, dpos);
+        nvel = __fadd_rn(nvel, __fmaf_rn(a, z1, __fmul_rn(b, z2)));
     } else if (noise) {
-        nvel += s_vv * z2;
+        nvel = __fmaf_rn(s_vv, z2, nvel);
     }
     vel = nvel;
     return dpos;
@@ -515,12 +562,12 @@ __device__ __forceinline__ void contact_candidate(const SoA& v, const HashDev& h
     const float two_a = (float)AGB_CELL_DIAMETER;
     const float thr = two_a * two_a;
     const double two_a64 = AGB_CELL_DIAMETER;
-    const float r2s = dx * dx + dy * dy + dz * dz;
+    const float r2s = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
     if (r2s >= thr * (1.0f + 1e-5f)) return;                     // clear of contact
     if (r2s <= thr * (1.0f - 1e-5f) && r2s > 1e-12f * thr) {     // in contact
         const float r = sqrtf(r2s);
         const float s = p.k_contact * (two_a - r) / r;
-        Cx += dx * s; Cy += dy * s; Cz += dz * s;
+        Cx = __fmaf_rn(dx, s, Cx); Cy = __fmaf_rn(dy, s, Cy); Cz = __fmaf_rn(dz, s, Cz);
         return;
     }
     ++refined;   // settle in FP64 from the pre-step positions (integrator.cuh:210-219)
@@ -550,21 +597,21 @@ __device__ __forceinline__ void sample_fields(const SoA& v, const Ctx& c, int32_
 __device__ __forceinline__ void forces_finish(const SoA& v, const Ctx& c, const TickParams& p, int32_t i, float Cx,
                                               float Cy, float Cz, float* fx_out, float* fy_out, float* fz_out) {
     const uint32_t flags = v.flags[i];
-    const float mass = d2f(v.biomass[i]) + d2f(v.energy[i]) * (float)(1.0 / (AGB_C_LIGHT * AGB_C_LIGHT));
+    const float mass = __fmaf_rn(d2f(v.energy[i]), (float)(1.0 / (AGB_C_LIGHT * AGB_C_LIGHT)), d2f(v.biomass[i]));
     const bool alive = (flags & AGB_FLAG_ALIVE) != 0u;
     const float wgt = -(mass - (float)(AGB_WATER_DENSITY * AGB_CELL_VOLUME)) * (float)AGB_G_ACCEL;
     float Fx = 0.0f, Fy = 0.0f, Fz = 0.0f;
     if (c.gravity_axis == AGB_GRAVITY_Y) Fy += wgt; else Fz += wgt;
     const float thrust = alive ? v.emit_power[i] * (float)(1.0 / AGB_C_LIGHT) : 0.0f;
     if (thrust != 0.0f) {
-        Fx -= v.dir_x[i] * thrust;
-        Fy -= v.dir_y[i] * thrust;
-        Fz -= v.dir_z[i] * thrust;
+        Fx = __fmaf_rn(-v.dir_x[i], thrust, Fx);
+        Fy = __fmaf_rn(-v.dir_y[i], thrust, Fy);
+        Fz = __fmaf_rn(-v.dir_z[i], thrust, Fz);
     }
     if (c.contact_enabled) { Fx += Cx; Fy += Cy; Fz += Cz; }
     if (i == c.trap_slot) {                                      // trap_force (integrator.cuh:195-197)
-        Fx += p.k_trap * (float)(c.trap_x - v.x[i]);
-        Fy += p.k_trap * (float)(c.trap_y - v.y[i]);
+        Fx = __fmaf_rn(p.k_trap, (float)(c.trap_x - v.x[i]), Fx);
+        Fy = __fmaf_rn(p.k_trap, (float)(c.trap_y - v.y[i]), Fy);
     }
     fx_out[i] = Fx; fy_out[i] = Fy; fz_out[i] = Fz;
 }
@@ -621,21 +668,20 @@ __global__ void __launch_bounds__(256) forces_kernel(DevState* S, Ctx c, TickPar
 // integrate_kernel (integrator.cu:79-150), slot order (coalesced state access).
 // With `demand` set, the lifecycle's demand pass (demand_kernel,
 // lifecycle.cu:41-57) runs here on each live cell at its new position.
-__global__ void __launch_bounds__(256) integrate_kernel(DevState* S, Ctx c, TickParams p,
-                                                        const float* __restrict__ fx_in,
-                                                        const float* __restrict__ fy_in,
-                                                        const float* __restrict__ fz_in, GridDev co2,
-                                                        unsigned long long* demand, float inv_gv) {
-    pdl_wait();
+__device__ __forceinline__ void integrate_kernel_body(DevState* S, const Ctx& c, const TickParams& p,
+                                                      const float* __restrict__ fx_in,
+                                                      const float* __restrict__ fy_in,
+                                                      const float* __restrict__ fz_in, const GridDev& co2,
+                                                      unsigned long long* demand, float inv_gv, Blk blk) {
     const SoA v = S->cur;
     const int32_t n = S->count;
-    AGB_FOR_CELLS(i, n) {
+    AGB_FOR_CELLS_B(i, blk, n) {
         const uint32_t flags = v.flags[i];
         if (!(flags & AGB_FLAG_OCCUPIED)) continue;
         double px = v.x[i], py = v.y[i], pz = v.z[i];
         const float t_local = v.t_local[i];       // sampled by forces_kernel this tick
         const float Fx = fx_in[i], Fy = fy_in[i], Fz = fz_in[i];
-        const float mass = d2f(v.biomass[i]) + d2f(v.energy[i]) * (float)(1.0 / (AGB_C_LIGHT * AGB_C_LIGHT));
+        const float mass = __fmaf_rn(d2f(v.energy[i]), (float)(1.0 / (AGB_C_LIGHT * AGB_C_LIGHT)), d2f(v.biomass[i]));
         // integrate_kernel (integrator.cu:79-150)
         const bool awake = (flags & AGB_FLAG_AWAKE) != 0u;
         const float t_drag = awake ? (float)AGB_CELL_TEMP_SETPOINT : t_local;
@@ -656,7 +702,7 @@ __global__ void __launch_bounds__(256) integrate_kernel(DevState* S, Ctx c, Tick
         float a = 0.0f, b = 0.0f;
         if (s_rr > 0.0f) {
             a = s_rv / s_rr;
-            const float b2 = s_vv * s_vv - a * a;
+            const float b2 = __fmaf_rn(s_vv, s_vv, -__fmul_rn(a, a));
             b = sqrtf(b2 > 0.0f ? b2 : 0.0f);
         }
         Pcg rng{v.rng_state[i], cell_stream_inc(v.id[i])};
@@ -698,6 +744,15 @@ __global__ void __launch_bounds__(256) integrate_kernel(DevState* S, Ctx c, Tick
         v.age_s[i] = v.age_s[i] + p.dtf;
         if (demand && (nf & AGB_FLAG_ALIVE)) co2_demand_cell(co2, p, d2f(px), d2f(py), d2f(pz), demand, inv_gv);
     }
+}
+
+__global__ void __launch_bounds__(256) integrate_kernel(DevState* S, Ctx c, TickParams p,
+                                                        const float* __restrict__ fx_in,
+                                                        const float* __restrict__ fy_in,
+                                                        const float* __restrict__ fz_in, GridDev co2,
+                                                        unsigned long long* demand, float inv_gv) {
+    pdl_wait();
+    integrate_kernel_body(S, c, p, fx_in, fy_in, fz_in, co2, demand, inv_gv, grid_blk());
 }
 
 // ---------------------------------------------------------------------------
@@ -806,17 +861,17 @@ __global__ void __launch_bounds__(256) taxis_kernel(DevState* S, Ctx c, TickPara
 // stages this tick runs; with L > 1 the group shares the walk and lane 0
 // finishes the cell.
 template <int L>
-__global__ void __launch_bounds__(256) cell_step_kernel(DevState* S, Ctx c, TickParams p, int feed, int taxis,
-                                                        float* fx_out, float* fy_out, float* fz_out) {
-    pdl_wait();
+__device__ __forceinline__ void cell_step_kernel_body(DevState* S, const Ctx& c, const TickParams& p, int feed,
+                                                      int taxis, float* fx_out, float* fy_out, float* fz_out,
+                                                      Blk blk) {
     const SoA v = S->cur;
     const HashDev h = c.h;
     const int32_t n = S->hash_count;
-    const int32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int32_t t = blk.x * blockDim.x + threadIdx.x;
     const int lane = t & (L - 1);
     const unsigned gm = group_mask<L>();
     const bool contact = c.contact_enabled != 0;
-    for (int32_t ks = t / L; ks < n; ks += (int32_t)(gridDim.x * blockDim.x) / L) {
+    for (int32_t ks = t / L; ks < n; ks += (int32_t)(blk.n * blockDim.x) / L) {
         const int32_t i = (int32_t)h.vals_sorted[ks];
         if (h.keys_sorted[ks] >= (uint32_t)h.buckets) {          // unoccupied slot (sentinel key)
             if (lane == 0) { fx_out[i] = 0.0f; fy_out[i] = 0.0f; fz_out[i] = 0.0f; }
@@ -868,7 +923,61 @@ __global__ void __launch_bounds__(256) cell_step_kernel(DevState* S, Ctx c, Tick
     }
 }
 
+template <int L>
+__global__ void __launch_bounds__(256) cell_step_kernel(DevState* S, Ctx c, TickParams p, int feed, int taxis,
+                                                        float* fx_out, float* fy_out, float* fz_out) {
+    pdl_wait();
+    cell_step_kernel_body<L>(S, c, p, feed, taxis, fx_out, fy_out, fz_out, grid_blk());
+}
+
+// ---------------------------------------------------------------------------
+// Batched launches of the per-cell stages (agb_batch): one grid over many
+// chambers, each block running the per-world body for its chamber.
+// ---------------------------------------------------------------------------
+AGB_BATCHED(thermal_batch, 256, thermal_kernel_body(a.S, a.c, a.p, blk))
+AGB_BATCHED(clear_stamps_batch, 256, clear_stamps_kernel_body(a.S, a.c, a.stamp_idx, blk))
+AGB_BATCHED(stamp_batch, 256, stamp_kernel_body(a.S, a.c, a.stamp_idx, blk))
+AGB_BATCHED(occlusion_factor_batch, 256, occlusion_factor_kernel_body(a.S, a.c, a.stamp_idx, a.factor, blk))
+AGB_BATCHED(sweep_rows_batch, 256, sweep_rows_kernel_body(a.c, a.factor, blk))
+AGB_BATCHED(sweep_lines_batch, 128, sweep_kernel_body(a.c, a.factor, blk))
+AGB_BATCHED(cell_step_batch, 256,
+            cell_step_kernel_body<1>(a.S, a.c, a.p, a.arg & 1, (a.arg >> 1) & 1, a.fx, a.fy, a.fz, blk))
+AGB_BATCHED(integrate_batch, 256,
+            integrate_kernel_body(a.S, a.c, a.p, a.fx, a.fy, a.fz, a.g, a.demand, a.inv_gv, blk))
+
 }  // namespace
+
+int32_t bstage_threads(BStage st) {
+    switch (st) {
+        case BStage::SweepLines: return 128;
+        case BStage::Swap: return 32;
+        default: return 256;
+    }
+}
+
+void launch_batched(BStage st, const ChamberArgs* tab, const uint32_t* map, int32_t blocks, int32_t arg,
+                    cudaStream_t s) {
+    if (blocks <= 0) return;
+    if (launch_batched_cells(st, tab, map, blocks, s)) return;
+    if (launch_batched_grid(st, tab, map, blocks, s)) return;
+    if (launch_batched_hash(st, tab, map, blocks, arg, s)) return;
+    launch_batched_life(st, tab, map, blocks, arg, s);
+}
+
+bool launch_batched_cells(BStage st, const ChamberArgs* tab, const uint32_t* map, int32_t blocks, cudaStream_t s) {
+    const unsigned g = (unsigned)blocks;
+    switch (st) {
+        case BStage::Thermal: launch_k(thermal_batch, g, 256, 0, s, tab, map); return true;
+        case BStage::ClearStamps: launch_k(clear_stamps_batch, g, 256, 0, s, tab, map); return true;
+        case BStage::Stamp: launch_k(stamp_batch, g, 256, 0, s, tab, map); return true;
+        case BStage::Occlusion: launch_k(occlusion_factor_batch, g, 256, 0, s, tab, map); return true;
+        case BStage::SweepRows: launch_k(sweep_rows_batch, g, 256, 0, s, tab, map); return true;
+        case BStage::SweepLines: launch_k(sweep_lines_batch, g, 128, 0, s, tab, map); return true;
+        case BStage::CellStep: launch_k(cell_step_batch, g, 256, 0, s, tab, map); return true;
+        case BStage::Integrate: launch_k(integrate_batch, g, 256, 0, s, tab, map); return true;
+        default: return false;
+    }
+}
 
 void launch_taxis(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, cudaStream_t s) {
     launch_k(taxis_kernel, blocks, 256, 0, s, S, c, p);

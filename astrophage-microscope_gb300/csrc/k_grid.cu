@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstdlib>
 
+#include "cells.h"
 #include "kernels.h"
 
 namespace agb {
@@ -164,23 +165,23 @@ __device__ __forceinline__ float ftcs7(float c, float l, float r, float d, float
     return fa(c, fm(coeff, sum));
 }
 
+// One CTA's tile (bx, by) and z chunk bz of a pass, reading the source through
+// the tensor map at `src_map` (a kernel parameter or a table entry).
 template <int LX, int RPT>
-__global__ void __launch_bounds__(256) ftcs3d_tma_kernel(const __grid_constant__ CUtensorMap src_map,
-                                                         float* __restrict__ dst, int32_t nx, int32_t ny,
-                                                         int32_t nz, int32_t zc, float coeff, Faces f,
-                                                         uint32_t* err) {
-    pdl_wait();
+__device__ __forceinline__ void ftcs3d_tma_body(const CUtensorMap* src_map, float* __restrict__ dst, int32_t nx,
+                                                int32_t ny, int32_t nz, int32_t zc, float coeff, const Faces& f,
+                                                uint32_t* err, int32_t bx, int32_t by, int32_t bz) {
     using T = TmaTile<LX, RPT>;
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + NBUF * T::PLANE_STRIDE);
     const int tid = threadIdx.x;
-    const int32_t x0 = blockIdx.x * T::TXW, y0 = blockIdx.y * T::TYH, k0 = blockIdx.z * zc;
+    const int32_t x0 = bx * T::TXW, y0 = by * T::TYH, k0 = bz * zc;
     const int32_t k1 = k0 + zc < nz ? k0 + zc : nz;
     const int nplanes = (k1 - k0) + 2;                  // plane q holds z = k0 - 1 + q
     auto buf = [&](int q) { return reinterpret_cast<const float*>(smem + (q % NBUF) * T::PLANE_STRIDE); };
     auto issue = [&](int q) {
         mbar_expect_tx(&bar[q % NBUF], T::PLANE_BYTES);
-        tma_load_plane(reinterpret_cast<float*>(smem + (q % NBUF) * T::PLANE_STRIDE), &src_map, &bar[q % NBUF],
+        tma_load_plane(reinterpret_cast<float*>(smem + (q % NBUF) * T::PLANE_STRIDE), src_map, &bar[q % NBUF],
                        x0 - HX, y0 - 1, k0 - 1 + q);
     };
     auto wait = [&](int q) { return mbar_wait(&bar[q % NBUF], (uint32_t)((q / NBUF) & 1), err); };
@@ -269,16 +270,44 @@ __global__ void __launch_bounds__(256) ftcs3d_tma_kernel(const __grid_constant__
         for (int q = waited; q < issued; ++q) (void)wait(q);
 }
 
+template <int LX, int RPT>
+__global__ void __launch_bounds__(256) ftcs3d_tma_kernel(const __grid_constant__ CUtensorMap src_map,
+                                                         float* __restrict__ dst, int32_t nx, int32_t ny,
+                                                         int32_t nz, int32_t zc, float coeff, Faces f,
+                                                         uint32_t* err) {
+    pdl_wait();
+    ftcs3d_tma_body<LX, RPT>(&src_map, dst, nx, ny, nz, zc, coeff, f, err, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// Batched passes (agb_batch): chambers of equal grids and tiling, chamber
+// blockIdx.z / zchunks. Each tensor map sits in a device table written before
+// the launch; the issuing thread acquires it for the tensor-map proxy first.
+template <int LX, int RPT>
+__global__ void __launch_bounds__(256) ftcs3d_tma_batch(const FtcsChamber* __restrict__ tab, int32_t nx,
+                                                        int32_t ny, int32_t nz, int32_t zc, int32_t zchunks) {
+    pdl_wait();
+    const int32_t ch = blockIdx.z / zchunks;
+    const FtcsChamber& a = tab[ch];
+    Faces f;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) { f.bc[k] = a.bc[k]; f.val[k] = a.face[k]; }
+    f.robin = a.robin;
+    if (threadIdx.x == 0)
+        asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(&a.map) : "memory");
+    ftcs3d_tma_body<LX, RPT>(&a.map, a.dst, nx, ny, nz, zc, a.coeff, f, a.err, blockIdx.x, blockIdx.y,
+                             blockIdx.z - ch * zchunks);
+}
+
 // Sparse flush: every occupied cell exchanges its voxel's accumulator for zero;
 // exactly one thread per voxel sees the nonzero sum and folds it in, so the
 // result equals the reference's dense flush over all voxels (a voxel without a
 // depositing cell holds zero). Optionally also zeroes a per-voxel demand
 // accumulator of the same grid (the CO2 rationing buffer).
-__global__ void flush_by_cells_kernel(DevState* S, GridDev g, unsigned long long* demand) {
-    pdl_wait();
+__device__ __forceinline__ void flush_by_cells_kernel_body(DevState* S, const GridDev& g, unsigned long long* demand,
+                                                           Blk blk) {
     const SoA v = S->cur;
     const int32_t n = S->count;
-    AGB_FOR_CELLS(i, n) {
+    AGB_FOR_CELLS_B(i, blk, n) {
         if (!(v.flags[i] & AGB_FLAG_OCCUPIED)) continue;
         const int64_t idx = grid_nearest(g, (float)v.x[i], (float)v.y[i], (float)v.z[i]);
         const unsigned long long raw = atomicExch(&g.deposit[idx], 0ull);
@@ -291,7 +320,20 @@ __global__ void flush_by_cells_kernel(DevState* S, GridDev g, unsigned long long
     }
 }
 
+__global__ void flush_by_cells_kernel(DevState* S, GridDev g, unsigned long long* demand) {
+    pdl_wait();
+    flush_by_cells_kernel_body(S, g, demand, grid_blk());
+}
+
+AGB_BATCHED(flush_batch, 256, flush_by_cells_kernel_body(a.S, a.g, nullptr, blk))
+
 }  // namespace
+
+bool launch_batched_grid(BStage st, const ChamberArgs* tab, const uint32_t* map, int32_t blocks, cudaStream_t s) {
+    if (st != BStage::Flush) return false;
+    launch_k(flush_batch, (unsigned)blocks, 256, 0, s, tab, map);
+    return true;
+}
 
 void launch_fill(float* v, int64_t n, float value, cudaStream_t s) {
     const int64_t blocks = (n + 255) / 256;
@@ -317,6 +359,18 @@ struct TmaInstance {
             n = b;
         }
         return n;
+    }
+    static void launch_batch(const FtcsChamber* tab, int32_t nch, int32_t nx, int32_t ny, int32_t nz, int32_t zc,
+                             cudaStream_t s) {
+        using T = TmaTile<LX, RPT>;
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(ftcs3d_tma_batch<LX, RPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, T::SMEM);
+            attr = true;
+        }
+        const int32_t zchunks = (nz + zc - 1) / zc;
+        const dim3 grid((nx + T::TXW - 1) / T::TXW, (ny + T::TYH - 1) / T::TYH, zchunks * nch);
+        launch_k(ftcs3d_tma_batch<LX, RPT>, grid, 256, T::SMEM, s, tab, nx, ny, nz, zc, zchunks);
     }
     static void launch(const GridDev& g, int zc, const CUtensorMap* map, float* dst, float coeff, const Faces& f,
                        uint32_t* err, cudaStream_t s) {
@@ -349,10 +403,16 @@ int sm_count() {
 // 128^3, within 5 % of the best tiling of each. AGB_FTCS_TILE="lx,rpt,zc"
 // overrides the choice (a tuning knob; results are the same for every tiling).
 FtcsPlan ftcs_plan_with(int32_t nx, int32_t ny, int32_t nz, int32_t lx, int32_t rpt, int32_t zc_in) {
+    return ftcs_plan_copies(nx, ny, nz, lx, rpt, zc_in, 1);
+}
+
+FtcsPlan ftcs_plan_copies(int32_t nx, int32_t ny, int32_t nz, int32_t lx, int32_t rpt, int32_t zc_in,
+                          int32_t copies) {
     FtcsPlan p{lx, rpt, zc_in > 0 ? zc_in : 0};
     if (!(lx == 16 || lx == 32) || !(rpt == 1 || rpt == 2 || rpt == 4) || (lx == 16 && rpt == 4)) {
         p.lx = 16; p.rpt = 1;
     }
+    if (copies < 1) copies = 1;
     if (p.zc == 0) {
         int per_sm = 1;
         if (p.lx == 32) per_sm = p.rpt == 1 ? TmaInstance<32, 1>::slots_per_sm()
@@ -361,7 +421,7 @@ FtcsPlan ftcs_plan_with(int32_t nx, int32_t ny, int32_t nz, int32_t lx, int32_t 
         const int64_t tx = 4 * p.lx, ty = (256 / p.lx) * p.rpt;
         const int64_t tiles = ((nx + tx - 1) / tx) * ((ny + ty - 1) / ty);
         const int64_t slots = (int64_t)sm_count() * per_sm;
-        int64_t zc = (tiles * nz + slots - 1) / slots;
+        int64_t zc = (tiles * nz * copies + slots - 1) / slots;
         zc = zc < 2 ? 2 : (zc > 32 ? 32 : zc);
         const int64_t chunks = (nz + zc - 1) / zc;
         p.zc = (int32_t)((nz + chunks - 1) / chunks);
@@ -408,6 +468,19 @@ void launch_ftcs(const GridDev& g, const float* src, float* dst, float coeff, co
         const dim3 block(32, 8);
         const dim3 grid((g.nx + 31) / 32, (g.ny + 7) / 8, (g.nz + ZCHUNK - 1) / ZCHUNK);
         launch_k(ftcs3d_kernel, grid, block, 0, s, src, dst, g.nx, g.ny, g.nz, coeff, f);
+    }
+}
+
+void launch_ftcs_batch(const FtcsChamber* tab, int32_t nch, int32_t nx, int32_t ny, int32_t nz,
+                       const FtcsPlan& p, cudaStream_t s) {
+    if (nch <= 0) return;
+    if (p.lx == 32) {
+        if (p.rpt == 1) TmaInstance<32, 1>::launch_batch(tab, nch, nx, ny, nz, p.zc, s);
+        else if (p.rpt == 2) TmaInstance<32, 2>::launch_batch(tab, nch, nx, ny, nz, p.zc, s);
+        else TmaInstance<32, 4>::launch_batch(tab, nch, nx, ny, nz, p.zc, s);
+    } else {
+        if (p.rpt == 1) TmaInstance<16, 1>::launch_batch(tab, nch, nx, ny, nz, p.zc, s);
+        else TmaInstance<16, 2>::launch_batch(tab, nch, nx, ny, nz, p.zc, s);
     }
 }
 

@@ -16,6 +16,7 @@
 // ascending slots inside a bucket.
 #include <cuda_runtime.h>
 
+#include "cells.h"
 #include "kernels.h"
 
 namespace agb {
@@ -41,14 +42,11 @@ constexpr uint32_t LOOKBACK_LIMIT = 1u << 24;
 
 // PER keys per thread: a tile is 256 * PER keys in 8 * PER warp-groups.
 template <int PER>
-__global__ void __launch_bounds__(SORT_THREADS) radix_pass_kernel(DevState* S, const uint32_t* __restrict__ kin,
-                                                                  const uint32_t* __restrict__ vin,
-                                                                  uint32_t* __restrict__ kout,
-                                                                  uint32_t* __restrict__ vout,
-                                                                  const uint32_t* __restrict__ ghist,
-                                                                  uint32_t* status, uint32_t* tile_counter,
-                                                                  int shift) {
-    pdl_wait();
+__device__ __forceinline__ void radix_pass_kernel_body(DevState* S, const uint32_t* __restrict__ kin,
+                                                       const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
+                                                       uint32_t* __restrict__ vout,
+                                                       const uint32_t* __restrict__ ghist, uint32_t* status,
+                                                       uint32_t* tile_counter, int shift, Blk blk) {
     constexpr int SORT_TILE = SORT_THREADS * PER;
     constexpr int SORT_GROUPS = SORT_TILE / 32;
     __shared__ uint16_t cnt[SORT_GROUPS][256];     // per group and digit: count, then exclusive prefix
@@ -151,19 +149,30 @@ __global__ void __launch_bounds__(SORT_THREADS) radix_pass_kernel(DevState* S, c
     }
 }
 
+template <int PER>
+__global__ void __launch_bounds__(SORT_THREADS) radix_pass_kernel(DevState* S, const uint32_t* __restrict__ kin,
+                                                                  const uint32_t* __restrict__ vin,
+                                                                  uint32_t* __restrict__ kout,
+                                                                  uint32_t* __restrict__ vout,
+                                                                  const uint32_t* __restrict__ ghist,
+                                                                  uint32_t* status, uint32_t* tile_counter,
+                                                                  int shift) {
+    pdl_wait();
+    radix_pass_kernel_body<PER>(S, kin, vin, kout, vout, ghist, status, tile_counter, shift, grid_blk());
+}
+
 // The hash build's first pass, fused: clear the bucket ranges the previous
 // build wrote, compute every slot's key (key_kernel, src/sim/hash.cu:15-25)
 // and count the digits of all radix passes.
-__global__ void __launch_bounds__(256) key_hist_kernel(DevState* S, HashDev h, uint32_t* __restrict__ ghist,
-                                                       int passes) {
-    pdl_wait();
+__device__ __forceinline__ void key_hist_kernel_body(DevState* S, const HashDev& h, uint32_t* __restrict__ ghist,
+                                                     int passes, Blk blk) {
     __shared__ uint32_t hs[4][256];
     for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) (&hs[0][0])[i] = 0u;
     __syncthreads();
     const SoA v = S->cur;
     const int32_t n = S->count, nprev = S->hash_count;
     const int32_t m = n > nprev ? n : nprev;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t i = blk.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)blk.n * blockDim.x) {
         if (i < nprev) {
             const uint32_t old = h.keys_sorted[i];
             if (old < (uint32_t)h.buckets) {
@@ -190,13 +199,18 @@ __global__ void __launch_bounds__(256) key_hist_kernel(DevState* S, HashDev h, u
     }
 }
 
-// range_kernel (src/sim/hash.cu:29-38) + the sorted snapshot.
-__global__ void ranges_kernel(DevState* S, HashDev h) {
+__global__ void __launch_bounds__(256) key_hist_kernel(DevState* S, HashDev h, uint32_t* __restrict__ ghist,
+                                                       int passes) {
     pdl_wait();
+    key_hist_kernel_body(S, h, ghist, passes, grid_blk());
+}
+
+// range_kernel (src/sim/hash.cu:29-38) + the sorted snapshot.
+__device__ __forceinline__ void ranges_kernel_body(DevState* S, const HashDev& h, Blk blk) {
     const SoA v = S->cur;
     const int32_t n = S->count;
-    if (blockIdx.x == 0 && threadIdx.x == 0) S->hash_count = n;
-    AGB_FOR_CELLS(k, n) {
+    if (blk.x == 0 && threadIdx.x == 0) S->hash_count = n;
+    AGB_FOR_CELLS_B(k, blk, n) {
         const uint32_t key = h.keys_sorted[k];
         const uint32_t slot = h.vals_sorted[k];
         if (key < (uint32_t)h.buckets) {
@@ -218,7 +232,73 @@ __global__ void ranges_kernel(DevState* S, HashDev h) {
     }
 }
 
+__global__ void ranges_kernel(DevState* S, HashDev h) {
+    pdl_wait();
+    ranges_kernel_body(S, h, grid_blk());
+}
+
+// Batched hash builds (agb_batch). A chamber's sort scratch is laid out as in
+// hash_build: [4][256] digit histograms | [4] tile counters | per pass
+// [max_tiles][256] look-back words; pass p reads the keys pass p - 1 wrote.
+__device__ __forceinline__ uint32_t hash_scratch_words(const ChamberArgs& a) {
+    return 4u * 256u + 4u + (uint32_t)a.passes * (uint32_t)a.max_tiles * 256u;
+}
+AGB_BATCHED(hash_clear_batch, 256, {
+    const uint32_t words = hash_scratch_words(a);
+    for (uint32_t i = (uint32_t)blk.x * blockDim.x + threadIdx.x; i < words; i += (uint32_t)blk.n * blockDim.x)
+        a.hist[i] = 0u;
+})
+AGB_BATCHED(key_hist_batch, 256, key_hist_kernel_body(a.S, a.c.h, a.hist, a.passes, blk))
+AGB_BATCHED(ranges_batch, 256, ranges_kernel_body(a.S, a.c.h, blk))
+
+template <int PER>
+__global__ void __launch_bounds__(SORT_THREADS) radix_batch(const ChamberArgs* __restrict__ tab,
+                                                            const uint32_t* __restrict__ map, int32_t pass) {
+    pdl_wait();
+    int32_t ch, x;
+    batch_block(map, ch, x);
+    const ChamberArgs& a = tab[ch];
+    const HashDev& h = a.c.h;
+    const bool odd_in = ((pass - 1) & 1) != 0;
+    const uint32_t* kin = pass == 0 ? h.keys : (odd_in ? h.keys : a.kalt);
+    const uint32_t* vin = pass == 0 ? h.vals : (odd_in ? h.vals : a.valt);
+    uint32_t* kout = pass == a.passes - 1 ? h.keys_sorted : ((pass & 1) ? h.keys : a.kalt);
+    uint32_t* vout = pass == a.passes - 1 ? h.vals_sorted : ((pass & 1) ? h.vals : a.valt);
+    uint32_t* counters = a.hist + 4 * 256;
+    uint32_t* status = counters + 4 + (size_t)pass * a.max_tiles * 256;
+    radix_pass_kernel_body<PER>(a.S, kin, vin, kout, vout, a.hist + pass * 256, status, counters + pass, pass * 8,
+                                Blk{x, a.nblk});
+}
+
 }  // namespace
+
+void hash_sort_shape(const HashDev& h, int32_t capacity, int32_t& passes, int32_t& max_tiles, bool& per4) {
+    int bits = 0;
+    while (bits < 32 && ((uint64_t)(uint32_t)h.buckets >> bits) != 0) ++bits;
+    passes = (bits + 7) / 8;
+    per4 = capacity <= (256 << 10);
+    const int tile_keys = SORT_THREADS * (per4 ? 4 : 8);
+    max_tiles = (capacity + tile_keys - 1) / tile_keys;
+}
+
+int32_t hash_clear_blocks(int32_t passes, int32_t max_tiles) {
+    const int64_t words = 4 * 256 + 4 + (int64_t)passes * max_tiles * 256;
+    const int64_t b = (words + 4 * 256 - 1) / (4 * 256);
+    return (int32_t)(b < 1 ? 1 : (b > 1024 ? 1024 : b));
+}
+
+bool launch_batched_hash(BStage st, const ChamberArgs* tab, const uint32_t* map, int32_t blocks, int32_t arg,
+                         cudaStream_t s) {
+    const unsigned g = (unsigned)blocks;
+    switch (st) {
+        case BStage::HashClear: launch_k(hash_clear_batch, g, 256, 0, s, tab, map); return true;
+        case BStage::KeyHist: launch_k(key_hist_batch, g, 256, 0, s, tab, map); return true;
+        case BStage::Radix4: launch_k(radix_batch<4>, g, SORT_THREADS, 0, s, tab, map, arg); return true;
+        case BStage::Radix8: launch_k(radix_batch<8>, g, SORT_THREADS, 0, s, tab, map, arg); return true;
+        case BStage::Ranges: launch_k(ranges_batch, g, 256, 0, s, tab, map); return true;
+        default: return false;
+    }
+}
 
 void hash_build(DevState* S, const HashDev& h, int32_t capacity, uint32_t* kalt, uint32_t* valt,
                 uint32_t* hist, int32_t grid_blocks, cudaStream_t s) {

@@ -50,15 +50,14 @@ __device__ __forceinline__ bool ready_to_divide(const Ctx& c, const SoA& v, int3
 // writes only that cell, besides uptake's deposit into its voxel's deposit
 // word, which nothing here reads; the CO2 flush that must follow every
 // deposit (lifecycle.cu:235) runs in the divide pass.
-__global__ void __launch_bounds__(256) uptake_mark_kernel(DevState* S, Ctx c, TickParams p,
-                                                          const unsigned long long* __restrict__ demand,
-                                                          float inv_gv, int32_t* divflag) {
-    pdl_wait();
+__device__ __forceinline__ void uptake_mark_kernel_body(DevState* S, const Ctx& c, const TickParams& p,
+                                                        const unsigned long long* __restrict__ demand, float inv_gv,
+                                                        int32_t* divflag, Blk blk) {
     const SoA v = S->cur;
     const int32_t n = S->count;
     const GridDev C2 = c.g[AGB_FIELD_CO2];
     int32_t births = 0, deads = 0;
-    AGB_FOR_CELLS(i, n) {
+    AGB_FOR_CELLS_B(i, blk, n) {
         uint32_t f = v.flags[i];
         if (demand && (f & AGB_FLAG_OCCUPIED) && (f & AGB_FLAG_ALIVE)) {
             const int64_t idx = grid_nearest(C2, d2f(v.x[i]), d2f(v.y[i]), d2f(v.z[i]));
@@ -98,6 +97,13 @@ __global__ void __launch_bounds__(256) uptake_mark_kernel(DevState* S, Ctx c, Ti
     }
 }
 
+__global__ void __launch_bounds__(256) uptake_mark_kernel(DevState* S, Ctx c, TickParams p,
+                                                          const unsigned long long* __restrict__ demand,
+                                                          float inv_gv, int32_t* divflag) {
+    pdl_wait();
+    uptake_mark_kernel_body(S, c, p, demand, inv_gv, divflag, grid_blk());
+}
+
 // ---------------------------------------------------------------------------
 // Two-level exclusive scan of a 0/1 predicate (the reference's CUB
 // ExclusiveSum, lifecycle.cu:269-270 and cell_store.cu:422). `gate` selects
@@ -117,9 +123,8 @@ constexpr uint32_t SCAN_LOOKBACK_LIMIT = 1u << 24;
 // prefix. The last CTA to finish clears the status words and counters for
 // the next scan. gate 1 (compaction) also stores the grand total in S->live.
 // Waits are bounded; a timeout sets the error word.
-__global__ void __launch_bounds__(ST) scan_kernel(DevState* S, const int32_t* __restrict__ flag, int32_t* prefix,
-                                                 uint32_t* status, int gate) {
-    pdl_wait();
+__device__ __forceinline__ void scan_kernel_body(DevState* S, const int32_t* __restrict__ flag, int32_t* prefix,
+                                                 uint32_t* status, int gate, Blk blk) {
     if (!scan_gate(S, gate)) return;                     // uniform over the grid
     __shared__ int32_t warp_tot[SITEMS][ST / 32];
     __shared__ uint32_t tile_sh;
@@ -189,7 +194,7 @@ __global__ void __launch_bounds__(ST) scan_kernel(DevState* S, const int32_t* __
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
-        last = atomicAdd(&S->scan_done, 1u) == gridDim.x - 1;
+        last = atomicAdd(&S->scan_done, 1u) == blk.n - 1;
     }
     __syncthreads();
     if (last) {
@@ -200,6 +205,12 @@ __global__ void __launch_bounds__(ST) scan_kernel(DevState* S, const int32_t* __
         }
         __threadfence();
     }
+}
+
+__global__ void __launch_bounds__(ST) scan_kernel(DevState* S, const int32_t* __restrict__ flag, int32_t* prefix,
+                                                 uint32_t* status, int gate) {
+    pdl_wait();
+    scan_kernel_body(S, flag, prefix, status, gate, grid_blk());
 }
 
 // ---------------------------------------------------------------------------
@@ -213,10 +224,9 @@ __device__ void life_finalize(DevState* S, int32_t capacity, int32_t compaction_
 // (flush_kernel, lifecycle.cu:235, restricted to the voxels cells sit in: only
 // uptake deposited this tick, into exactly those) from each parent's position
 // before division moves it, and clears the rationing demand there.
-__global__ void __launch_bounds__(256) divide_kernel(DevState* S, Ctx c, const int32_t* __restrict__ divflag,
-                                                     const int32_t* __restrict__ prefix,
-                                                     int32_t compaction_allowed, unsigned long long* demand) {
-    pdl_wait();
+__device__ __forceinline__ void divide_kernel_body(DevState* S, const Ctx& c, const int32_t* __restrict__ divflag,
+                                                   const int32_t* __restrict__ prefix, int32_t compaction_allowed,
+                                                   unsigned long long* demand, Blk blk) {
     const int32_t births_now = S->births;
     const SoA v = S->cur;
     const int32_t n = S->count;                 // base = old count
@@ -224,7 +234,7 @@ __global__ void __launch_bounds__(256) divide_kernel(DevState* S, Ctx c, const i
     const double a = AGB_CELL_RADIUS;
     const double hx = 0.5 * c.chamber_w - a, hy = 0.5 * c.chamber_h - a, hz = 0.5 * c.chamber_d - a;
     const GridDev C2 = c.g[AGB_FIELD_CO2];
-    AGB_FOR_CELLS(i, (births_now > 0 || demand) ? n : 0) {
+    AGB_FOR_CELLS_B(i, blk, (births_now > 0 || demand) ? n : 0) {
         if (demand && (v.flags[i] & AGB_FLAG_OCCUPIED)) {
             const int64_t idx = grid_nearest(C2, (float)v.x[i], (float)v.y[i], (float)v.z[i]);
             const unsigned long long raw = atomicExch(&C2.deposit[idx], 0ull);
@@ -282,12 +292,19 @@ __global__ void __launch_bounds__(256) divide_kernel(DevState* S, Ctx c, const i
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
-        if (atomicAdd(&S->fin_count, 1u) == gridDim.x - 1) {
+        if (atomicAdd(&S->fin_count, 1u) == blk.n - 1) {
             __threadfence();
             life_finalize(S, c.capacity, compaction_allowed);
             S->fin_count = 0u;
         }
     }
+}
+
+__global__ void __launch_bounds__(256) divide_kernel(DevState* S, Ctx c, const int32_t* __restrict__ divflag,
+                                                     const int32_t* __restrict__ prefix,
+                                                     int32_t compaction_allowed, unsigned long long* demand) {
+    pdl_wait();
+    divide_kernel_body(S, c, divflag, prefix, compaction_allowed, demand, grid_blk());
 }
 
 // The host bookkeeping of lifecycle_step (lifecycle.cu:250-293), on the device.
@@ -317,35 +334,43 @@ __device__ void life_finalize(DevState* S, int32_t capacity, int32_t compaction_
 // prefix, gathered out of place into the spare SoA in one fused pass over all
 // 25 arrays, then the SoA pointers swap on the device.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) keep_kernel(DevState* S, int32_t* keep) {
-    pdl_wait();
+__device__ __forceinline__ void keep_kernel_body(DevState* S, int32_t* keep, Blk blk) {
     if (!S->compact_now) return;
     const SoA v = S->cur;
     const int32_t n = S->count;
-    AGB_FOR_CELLS(i, n) {
+    AGB_FOR_CELLS_B(i, blk, n) {
         const uint32_t f = v.flags[i];
         keep[i] = ((f & AGB_FLAG_OCCUPIED) && (f & AGB_FLAG_ALIVE)) ? 1 : 0;
+    }
+}
+
+__global__ void __launch_bounds__(256) keep_kernel(DevState* S, int32_t* keep) {
+    pdl_wait();
+    keep_kernel_body(S, keep, grid_blk());
+}
+
+__device__ __forceinline__ void scatter_src_kernel_body(DevState* S, const int32_t* __restrict__ keep,
+                                                        const int32_t* __restrict__ prefix, int32_t* src, Blk blk) {
+    if (!S->compact_now) return;
+    const int32_t n = S->count;
+    AGB_FOR_CELLS_B(i, blk, n) {
+        if (keep[i]) src[prefix[i]] = i;
     }
 }
 
 __global__ void __launch_bounds__(256) scatter_src_kernel(DevState* S, const int32_t* __restrict__ keep,
                                                          const int32_t* __restrict__ prefix, int32_t* src) {
     pdl_wait();
-    if (!S->compact_now) return;
-    const int32_t n = S->count;
-    AGB_FOR_CELLS(i, n) {
-        if (keep[i]) src[prefix[i]] = i;
-    }
+    scatter_src_kernel_body(S, keep, prefix, src, grid_blk());
 }
 
-__global__ void __launch_bounds__(256) gather_kernel(DevState* S, const int32_t* __restrict__ src) {
-    pdl_wait();
+__device__ __forceinline__ void gather_kernel_body(DevState* S, const int32_t* __restrict__ src, Blk blk) {
     if (!S->compact_now) return;
     const int32_t live = S->live;
     if (live >= S->count) return;
     const SoA a = S->cur;
     const SoA b = S->spare;
-    AGB_FOR_CELLS(k, live) {
+    AGB_FOR_CELLS_B(k, blk, live) {
         const int32_t i = src[k];
         b.id[k] = a.id[i]; b.flags[k] = a.flags[i]; b.death_cause[k] = a.death_cause[i];
         b.x[k] = a.x[i]; b.y[k] = a.y[i]; b.z[k] = a.z[i];
@@ -359,8 +384,12 @@ __global__ void __launch_bounds__(256) gather_kernel(DevState* S, const int32_t*
     }
 }
 
-__global__ void swap_kernel(DevState* S) {
+__global__ void __launch_bounds__(256) gather_kernel(DevState* S, const int32_t* __restrict__ src) {
     pdl_wait();
+    gather_kernel_body(S, src, grid_blk());
+}
+
+__device__ __forceinline__ void swap_kernel_body(DevState* S, Blk blk) {
     if (!S->compact_now) return;
     const int32_t live = S->live;
     if (live < S->count) {
@@ -370,6 +399,11 @@ __global__ void swap_kernel(DevState* S) {
         S->count = live;
     }
     S->compact_now = 0;
+}
+
+__global__ void swap_kernel(DevState* S) {
+    pdl_wait();
+    swap_kernel_body(S, grid_blk());
 }
 
 __global__ void force_compact_kernel(DevState* S) {
@@ -579,7 +613,43 @@ void launch_compact_kernels(DevState* S, const LifeBuffers& b, int32_t capacity,
     launch_k(swap_kernel, 1, 1, 0, s, S);
 }
 
+AGB_BATCHED(uptake_mark_batch, 256,
+            uptake_mark_kernel_body(a.S, a.c, a.p, a.demand, a.inv_gv, a.life.flags, blk))
+AGB_BATCHED(divide_batch, 256,
+            divide_kernel_body(a.S, a.c, a.life.flags, a.life.prefix, a.arg, a.demand, blk))
+AGB_BATCHED(keep_batch, 256, keep_kernel_body(a.S, a.life.flags, blk))
+AGB_BATCHED(scatter_src_batch, 256, scatter_src_kernel_body(a.S, a.life.flags, a.life.prefix, a.life.src, blk))
+AGB_BATCHED(gather_batch, 256, gather_kernel_body(a.S, a.life.src, blk))
+AGB_BATCHED(swap_batch, 32, if (threadIdx.x == 0) swap_kernel_body(a.S, blk))
+
+__global__ void __launch_bounds__(ST) scan_batch(const ChamberArgs* __restrict__ tab,
+                                                 const uint32_t* __restrict__ map, int32_t gate) {
+    pdl_wait();
+    int32_t ch, x;
+    batch_block(map, ch, x);
+    const ChamberArgs& a = tab[ch];
+    scan_kernel_body(a.S, a.life.flags, a.life.prefix, reinterpret_cast<uint32_t*>(a.life.tile_sums), gate,
+                     Blk{x, a.nblk});
+}
+
 }  // namespace
+
+int32_t scan_blocks(int32_t capacity) { return (capacity + STILE - 1) / STILE; }
+
+bool launch_batched_life(BStage st, const ChamberArgs* tab, const uint32_t* map, int32_t blocks, int32_t arg,
+                         cudaStream_t s) {
+    const unsigned g = (unsigned)blocks;
+    switch (st) {
+        case BStage::UptakeMark: launch_k(uptake_mark_batch, g, 256, 0, s, tab, map); return true;
+        case BStage::Scan: launch_k(scan_batch, g, ST, 0, s, tab, map, arg); return true;
+        case BStage::Divide: launch_k(divide_batch, g, 256, 0, s, tab, map); return true;
+        case BStage::Keep: launch_k(keep_batch, g, 256, 0, s, tab, map); return true;
+        case BStage::ScatterSrc: launch_k(scatter_src_batch, g, 256, 0, s, tab, map); return true;
+        case BStage::Gather: launch_k(gather_batch, g, 256, 0, s, tab, map); return true;
+        case BStage::Swap: launch_k(swap_batch, g, 32, 0, s, tab, map); return true;
+        default: return false;
+    }
+}
 
 void launch_lifecycle(DevState* S, const Ctx& c, const TickParams& p, const LifeBuffers& b,
                       bool compaction_allowed, int32_t blocks, cudaStream_t s, bool demand_done) {

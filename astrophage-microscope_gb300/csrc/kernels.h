@@ -21,12 +21,29 @@ FtcsPlan ftcs_plan(int32_t nx, int32_t ny, int32_t nz);
 // A given tiling (lx 16/32, rpt 1/2/4; lx 16 with rpt 4 is not built) with the
 // z chunk chosen as ftcs_plan chooses it when zc <= 0.
 FtcsPlan ftcs_plan_with(int32_t nx, int32_t ny, int32_t nz, int32_t lx, int32_t rpt, int32_t zc);
+// The same for `copies` grids in one launch (batched passes): the z chunk fills
+// one wave with all of them.
+FtcsPlan ftcs_plan_copies(int32_t nx, int32_t ny, int32_t nz, int32_t lx, int32_t rpt, int32_t zc,
+                          int32_t copies);
 // One explicit FTCS pass src -> dst (src/fields/diffuse.cu:19-44; 7-point when nz > 1).
 // 3-D grids with a tensor map (and the tiling it was made for) use the TMA-staged kernel.
 void launch_ftcs(const GridDev& g, const float* src, float* dst, float coeff, const int32_t* bc,
                  const float* face, float robin, const CUtensorMap* src_map, const FtcsPlan* plan, uint32_t* err,
                  cudaStream_t s);
 bool make_plane_map(CUtensorMap* map, float* base, int32_t nx, int32_t ny, int32_t nz, const FtcsPlan& plan);
+// One chamber's FTCS pass in a batched launch (agb_batch). The chambers of a
+// launch share grid dimensions and tiling; each has its own tensor map (over
+// the pass's source buffer, made for that tiling), destination and faces.
+struct FtcsChamber {
+    CUtensorMap map;
+    float* dst;
+    uint32_t* err;
+    float coeff, robin;
+    int32_t bc[6];
+    float face[6];
+};
+void launch_ftcs_batch(const FtcsChamber* tab, int32_t nch, int32_t nx, int32_t ny, int32_t nz,
+                       const FtcsPlan& plan, cudaStream_t s);
 // Fold deposits into the field for the voxels cells sit in (flush_kernel,
 // src/fields/diffuse.cu:51-60, restricted to voxels that can hold a deposit).
 void launch_flush_by_cells(DevState* S, GridDev g, unsigned long long* demand_to_clear,

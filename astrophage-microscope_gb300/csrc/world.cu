@@ -174,6 +174,12 @@ void compute_light(agb_world* w) {
 
 float* field_value(agb_world* w, int f) { return w->gbuf[f][w->gcur[f]]; }
 
+// The irradiance field changed outside the sweep: the next sweep rewrites
+// every line (enqueued on s).
+void irr_all_lines(agb_world* w, cudaStream_t s) {
+    if (w->c.irr_marks) cudaMemsetAsync(w->c.irr_marks, 2, (size_t)w->irr_mark_bytes, s);
+}
+
 void refresh_grid_ptrs(agb_world* w) {
     for (int f = 0; f < AGB_FIELD_COUNT; ++f) {
         w->c.g[f].value = w->gbuf[f][w->gcur[f]];
@@ -474,6 +480,9 @@ agb_status read_state(agb_world* w, DevState& out, cudaStream_t s) {
 namespace agb {
 
 void world_tick(agb_world* w, cudaStream_t s) { tick_once(w, s); }
+void world_refresh(agb_world* w) { refresh_grid_ptrs(w); }
+bool world_emission_active(const agb_world* w) { return emission_active(w); }
+bool world_compaction_allowed(const agb_world* w) { return compaction_allowed(w); }
 uint32_t world_parity(const agb_world* w) { return parity_bits(w); }
 void world_set_parity(agb_world* w, uint32_t bits) {
     for (int f = 0; f < AGB_FIELD_COUNT; ++f) w->gcur[f] = (bits >> f) & 1;
@@ -762,11 +771,18 @@ agb_status agb_world_create(const agb_world_desc* d, agb_world** out) {
          dalloc(w, &w->acc, 8 * 12) == cudaSuccess && dalloc(w, &w->S, sizeof(DevState)) == cudaSuccess;
     const int64_t irrn = c.g[AGB_FIELD_IRRADIANCE].enabled ? c.g[AGB_FIELD_IRRADIANCE].count : 1;
     ok = ok && dalloc(w, &w->occl_factor, 8 * (size_t)irrn) == cudaSuccess;
+    if (c.g[AGB_FIELD_IRRADIANCE].enabled) {
+        const GridDev& I = c.g[AGB_FIELD_IRRADIANCE];
+        const int64_t yz = (int64_t)I.ny * I.nz, xz = (int64_t)I.nx * I.nz, xy = (int64_t)I.nx * I.ny;
+        w->irr_mark_bytes = std::max(yz, std::max(xz, xy));
+        ok = ok && dalloc(w, &c.irr_marks, (size_t)w->irr_mark_bytes) == cudaSuccess;
+    }
     for (cudaStream_t& st : w->side) ok = ok && cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess;
     for (cudaEvent_t& e : w->ev) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
     const int64_t co2n = c.g[AGB_FIELD_CO2].enabled ? c.g[AGB_FIELD_CO2].count : 1;
     ok = ok && dalloc(w, &w->life.co2_demand, 8 * (size_t)co2n) == cudaSuccess;
     if (!ok) { agb_world_destroy(w); return AGB_OUT_OF_MEMORY; }
+    if (c.irr_marks) cudaMemset(c.irr_marks, 2, (size_t)w->irr_mark_bytes);   // first sweep: every line
     cudaMemset(h.ranges, 0, 8 * (size_t)h.buckets);
     cudaMemset(h.occ, 0, 4 * (((size_t)h.buckets + 31) / 32 + 1));
     cudaMemset(h.keys_sorted, 0, 4 * n);
@@ -914,6 +930,7 @@ agb_status agb_world_import_field(agb_world* w, int32_t f, const float* src, agb
     if (!w || f < 0 || f >= AGB_FIELD_COUNT || !w->c.g[f].enabled || !src) return AGB_INVALID_ARGUMENT;
     AGB_CUDA(w, cudaMemcpyAsync(field_value(w, f), src, sizeof(float) * w->c.g[f].count,
                                 cudaMemcpyHostToDevice, s));
+    if (f == AGB_FIELD_IRRADIANCE) irr_all_lines(w, s);
     AGB_CUDA(w, cudaStreamSynchronize(s));
     return AGB_OK;
 }
@@ -1070,6 +1087,7 @@ agb_status agb_world_diffuse(agb_world* w, int32_t f, double dt, agb_stream s) {
     if (!w || f < 0 || f >= AGB_FIELD_COUNT) return AGB_INVALID_ARGUMENT;
     const GridDev& g = w->c.g[f];
     if (!g.enabled) return AGB_OK;
+    if (f == AGB_FIELD_IRRADIANCE) irr_all_lines(w, s);
     const double D = w->d.grid[f].diffusivity;
     const int32_t steps = substeps_for(g, D, dt);         // grid_diffuse, diffuse.cu:159-186
     if (steps <= 0) return AGB_OK;
@@ -1145,6 +1163,11 @@ agb_status agb_world_set_light(agb_world* w, const agb_light* light) {
     w->d.light = *light;
     compute_light(w);
     invalidate_graphs(w);
+    // Every line's unshadowed value (and the line numbering) may change: the
+    // next sweep rewrites them all.
+    AGB_CUDA(w, cudaDeviceSynchronize());
+    irr_all_lines(w, nullptr);
+    AGB_CUDA(w, cudaDeviceSynchronize());
     return AGB_OK;
 }
 

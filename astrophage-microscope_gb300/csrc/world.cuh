@@ -33,6 +33,11 @@ struct Ctx {
     int32_t light_axis, light_sign;
     int32_t light_axis_exact;  // light exactly along light_axis (other components 0), else -1
     float source, ambient_irr;
+    // One byte per irradiance line of the sweep: 1 = a cell stamped a voxel of
+    // it this tick, 2 = stamped last tick only (recompute once to clear the old
+    // shadow), 0 = no stamp in either, so its values are already the
+    // unshadowed ones and the sweep leaves it alone. Null: sweep every line.
+    uint8_t* irr_marks;
     double face_area;
     long long stamp_alive, stamp_dead;   // fixed-point occlusion stamps
     // Exact float thresholds equivalent to the reference's FP64 compares.

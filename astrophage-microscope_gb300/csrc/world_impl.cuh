@@ -50,6 +50,7 @@ struct agb_world {
     int32_t blocks = 1;
     int walk_lanes = 1;                  // threads sharing one cell's neighbour walk (1, 2, 4, 8)
     bool fuse_cells = false;             // feeding, taxis and forces in one kernel with one walk
+    int64_t irr_mark_bytes = 0;          // size of c.irr_marks (irradiance lines over any light axis)
     uint64_t tick = 0;
     double sim_time = 0.0;
     double physics_rate = 1.0, biology_rate = 1.0;
@@ -79,6 +80,12 @@ uint32_t world_parity(const agb_world* w);
 void world_set_parity(agb_world* w, uint32_t bits);
 // tick % compaction period: which compaction decision the next tick takes.
 uint64_t world_phase(const agb_world* w);
+// Point the context's field views at the current ping-pong buffers.
+void world_refresh(agb_world* w);
+// Whether this tick runs the irradiance field and feeding; whether the next
+// lifecycle stage may compact.
+bool world_emission_active(const agb_world* w);
+bool world_compaction_allowed(const agb_world* w);
 void world_advance_clock(agb_world* w, int32_t ticks);
 // Set the tick counter and simulated time (snapshot restore); drops graphs.
 void world_set_clock_state(agb_world* w, uint64_t tick, double sim_time);

@@ -148,7 +148,8 @@ def run_batch(args, stream, l2_flush, dist=None, rank=0, ws=1):
         descs = [descs[i] for i in mine]
         spawns = [spawns[i] for i in mine]
     t0 = time.perf_counter()
-    b = agb.Batch(descs, spawns, agb.batch_opts(autotune=True, lanes=args.batch_lanes))
+    b = agb.Batch(descs, spawns, agb.batch_opts(autotune=True, lanes=args.batch_lanes,
+                                                 staged=bool(args.batch_staged)))
     setup_s = time.perf_counter() - t0
     sh = stream.cuda_stream
     with torch.cuda.stream(stream):
@@ -184,7 +185,7 @@ def run_batch(args, stream, l2_flush, dist=None, rank=0, ws=1):
            "voxel_steps_per_s": vox * args.batch_steps / total_s,
            "ms_per_step": total_s * 1e3 / args.batch_steps, "steps": args.batch_steps,
            "cells_start_end": [n0, n1], "gpu_launches": launches, "setup_s": setup_s,
-           "lanes": args.batch_lanes or min(args.batch_chambers, 16),
+           "lanes": args.batch_lanes or min(args.batch_chambers, 16), "staged": b.staged(),
            "config": dict(info, workload="batch%d" % args.batch_chambers,
                           step="one tick of every chamber, one graph launch"),
            "autotune": classes}
@@ -537,6 +538,8 @@ def main():
                     help="timed steps of the batched ensemble reported beside the plain step (0: skip)")
     ap.add_argument("--batch-chambers", type=int, default=64)
     ap.add_argument("--batch-lanes", type=int, default=0)
+    ap.add_argument("--batch-staged", type=int, default=1,
+                    help="1: one launch per stage over every chamber; 0: each chamber's tick on the lanes")
     ap.add_argument("--batch-only", action="store_true",
                     help="run only the batched ensemble and print its result (profiling)")
     ap.add_argument("--surrogate-windows", type=int, default=1500,

@@ -288,6 +288,9 @@ typedef struct agb_batch_opts {
     int32_t n_hash_candidates;  /* 0: 1.0, 1.5, 2.2 and 3.0 cell diameters */
     double hash_candidates[8];  /* metres; candidates under one cell diameter are skipped */
     int32_t probe_ticks;        /* timed probe ticks per candidate (0 = 4) */
+    int32_t staged;             /* 1 (default): each stage of the tick is one launch over every chamber,
+                                   when every enabled grid is 3-D with a TMA stencil and no chamber has a
+                                   surrogate attached; 0: each chamber's tick is launched on the lanes */
 } agb_batch_opts;
 
 /* What a chamber was built with, and what the autotuner measured for it. */
@@ -496,6 +499,8 @@ agb_status agb_batch_world(agb_batch* b, int32_t i, agb_world** w);
 agb_status agb_batch_tuning(agb_batch* b, int32_t i, agb_tuning* out);
 agb_status agb_batch_step(agb_batch* b, int32_t ticks, agb_stream s);
 agb_status agb_batch_graph_kernels(agb_batch* b, int64_t* kernels);
+/* 1 when steps run staged (one launch per stage over every chamber), 0 on lanes. */
+agb_status agb_batch_staged(agb_batch* b, int32_t* staged);
 agb_status agb_batch_stats(agb_batch* b, agb_stats* out);
 
 #ifdef __cplusplus

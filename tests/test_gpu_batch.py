@@ -68,9 +68,11 @@ def assert_same(chamber, world, where):
     assert chamber.counters()[3] == 0 and world.counters()[3] == 0
 
 
-def test_batch_equals_standalone_worlds():
+@pytest.mark.parametrize("staged", [True, False])
+def test_batch_equals_standalone_worlds(staged):
     descs, spawns = chambers()
-    b = agb.Batch(descs, spawns, agb.batch_opts(lanes=3))
+    b = agb.Batch(descs, spawns, agb.batch_opts(lanes=3, staged=staged))
+    assert b.staged() == staged
     ticks = [1, 2, 1, 3, 1]                # mixed step sizes cross the compaction period
     for t in ticks:
         b.step(t)
@@ -84,10 +86,12 @@ def test_batch_equals_standalone_worlds():
     assert b.graph_kernels() > 0
 
 
-def test_batch_graph_replay_repeats():
+@pytest.mark.parametrize("staged", [True, False])
+def test_batch_graph_replay_repeats(staged):
     """Stepping one tick at a time replays cached graphs; results still match."""
     descs, spawns = chambers()
-    b = agb.Batch(descs, spawns, agb.batch_opts(lanes=2))
+    b = agb.Batch(descs, spawns, agb.batch_opts(lanes=2, staged=staged))
+    assert b.staged() == staged
     for _ in range(8):
         b.step(1)
     k1 = b.graph_kernels()
