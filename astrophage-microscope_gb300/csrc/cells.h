@@ -41,9 +41,11 @@ struct ChamberArgs {
 
 // A batched kernel NAME(tab, map): finds its chamber and block, then CALL
 // (which sees the chamber's arguments as `a` and its block as `blk`).
-#define AGB_BATCHED(NAME, THREADS, CALL)                                                             \
-    __global__ void __launch_bounds__(THREADS) NAME(const ChamberArgs* __restrict__ tab,              \
-                                                    const uint32_t* __restrict__ map) {              \
+#define AGB_BATCHED(NAME, THREADS, CALL) AGB_BATCHED_MB(NAME, THREADS, 1, CALL)
+// ... with at least MINB resident blocks per SM (a register budget).
+#define AGB_BATCHED_MB(NAME, THREADS, MINB, CALL)                                                    \
+    __global__ void __launch_bounds__(THREADS, MINB) NAME(const ChamberArgs* __restrict__ tab,        \
+                                                          const uint32_t* __restrict__ map) {        \
         pdl_wait();                                                                                  \
         int32_t ch_, x_;                                                                             \
         batch_block(map, ch_, x_);                                                                   \

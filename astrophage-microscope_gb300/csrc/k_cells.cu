@@ -188,9 +188,13 @@ __device__ __forceinline__ void clear_stamps_kernel_body(DevState* S, const Ctx&
                                                          const int32_t* __restrict__ stamp_idx, Blk blk) {
     const int32_t n = S->n_stamps;
     unsigned long long* dep = c.g[AGB_FIELD_IRRADIANCE].deposit;
+    uint32_t* bits = c.irr_stamp_bits;
     AGB_FOR_CELLS_B(i, blk, n) {
         const int32_t idx = stamp_idx[i];
-        if (idx >= 0) dep[idx] = 0ull;
+        if (idx >= 0) {
+            dep[idx] = 0ull;
+            if (bits) atomicAnd(&bits[idx >> 5], ~(1u << (idx & 31)));
+        }
     }
 }
 
@@ -223,6 +227,7 @@ __device__ __forceinline__ void stamp_kernel_body(DevState* S, const Ctx& c, int
             deposit_fixed(&I.deposit[idx], (f & AGB_FLAG_ALIVE) ? c.stamp_alive : c.stamp_dead);
             rec = (int32_t)idx;
             if (c.irr_marks) c.irr_marks[irr_line(I, c.light_axis, idx)] = 1;
+            if (c.irr_stamp_bits) atomicOr(&c.irr_stamp_bits[idx >> 5], 1u << (idx & 31));
         }
         stamp_idx[i] = rec;
     }
@@ -258,6 +263,13 @@ __global__ void __launch_bounds__(256) occlusion_factor_kernel(DevState* S, Ctx 
     occlusion_factor_kernel_body(S, c, stamp_idx, factor, grid_blk());
 }
 
+// Whether irradiance voxel idx was stamped this tick: its bit when the world
+// keeps the bitmap, else its deposit word.
+__device__ __forceinline__ bool stamped(const Ctx& c, const GridDev& I, int64_t idx) {
+    if (c.irr_stamp_bits) return (__ldg(&c.irr_stamp_bits[idx >> 5]) >> (idx & 31)) & 1u;
+    return __ldg(&I.deposit[idx]) != 0ull;
+}
+
 // sweep_kernel (emission.cu:37-53): one thread per line in sweep order. The
 // FP64 transmittance recurrence runs only at stamped voxels (an empty voxel's
 // factor is exactly 1), and the float output only changes there, so empty
@@ -284,12 +296,12 @@ __device__ __forceinline__ void sweep_kernel_body(const Ctx& c, const double* __
         double t = 1.0;
         float cur = fa(d2f((double)c.source * t), c.ambient_irr);
         for (int32_t s0 = 0; s0 < len; s0 += SWEEP_PF) {
-            unsigned long long raw[SWEEP_PF];
+            bool raw[SWEEP_PF];
 #pragma unroll
             for (int u = 0; u < SWEEP_PF; ++u) {
                 const int32_t s = s0 + u;
                 const int32_t step = c.light_sign > 0 ? s : (len - 1 - s);
-                raw[u] = s < len ? __ldg(&I.deposit[base + stride * step]) : 0ull;
+                raw[u] = s < len && stamped(c, I, base + stride * step);
             }
 #pragma unroll
             for (int u = 0; u < SWEEP_PF; ++u) {
@@ -297,7 +309,7 @@ __device__ __forceinline__ void sweep_kernel_body(const Ctx& c, const double* __
                 if (s >= len) break;
                 const int32_t step = c.light_sign > 0 ? s : (len - 1 - s);
                 I.value[base + stride * step] = cur;
-                if (raw[u] != 0ull) {
+                if (raw[u]) {
                     t *= __ldg(&factor[base + stride * step]);
                     cur = fa(d2f((double)c.source * t), c.ambient_irr);
                 }
@@ -333,11 +345,11 @@ __device__ __forceinline__ void sweep_rows_kernel_body(const Ctx& c, const doubl
             const int32_t s = s0 + lane;
             const bool in = s < len;
             const int64_t idx = base + (c.light_sign > 0 ? s : (len - 1 - s));
-            const unsigned long long raw = in ? __ldg(&I.deposit[idx]) : 0ull;
-            unsigned mask = __ballot_sync(0xFFFFFFFFu, raw != 0ull);
+            const bool raw = in && stamped(c, I, idx);
+            unsigned mask = __ballot_sync(0xFFFFFFFFu, raw);
             float mine = cur;
             if (mask) {
-                const double f = raw != 0ull ? __ldg(&factor[idx]) : 1.0;
+                const double f = raw ? __ldg(&factor[idx]) : 1.0;
                 while (mask) {
                     const int b = __ffs(mask) - 1;
                     mask &= mask - 1u;
@@ -940,9 +952,9 @@ AGB_BATCHED(stamp_batch, 256, stamp_kernel_body(a.S, a.c, a.stamp_idx, blk))
 AGB_BATCHED(occlusion_factor_batch, 256, occlusion_factor_kernel_body(a.S, a.c, a.stamp_idx, a.factor, blk))
 AGB_BATCHED(sweep_rows_batch, 256, sweep_rows_kernel_body(a.c, a.factor, blk))
 AGB_BATCHED(sweep_lines_batch, 128, sweep_kernel_body(a.c, a.factor, blk))
-AGB_BATCHED(cell_step_batch, 256,
+AGB_BATCHED_MB(cell_step_batch, 256, 3,
             cell_step_kernel_body<1>(a.S, a.c, a.p, a.arg & 1, (a.arg >> 1) & 1, a.fx, a.fy, a.fz, blk))
-AGB_BATCHED(integrate_batch, 256,
+AGB_BATCHED_MB(integrate_batch, 256, 3,
             integrate_kernel_body(a.S, a.c, a.p, a.fx, a.fy, a.fz, a.g, a.demand, a.inv_gv, blk))
 
 }  // namespace

@@ -213,6 +213,58 @@ __global__ void __launch_bounds__(ST) scan_kernel(DevState* S, const int32_t* __
     scan_kernel_body(S, flag, prefix, status, gate, grid_blk());
 }
 
+// Division of parent i into `slot` with id `did` (divide_kernel body,
+// lifecycle.cu:140-204). Out of line: it is rare, and inlined its FP64
+// placement would set the register budget of the whole pass, which mostly
+// runs the per-cell CO2 flush.
+// (hx, hy, hz: the chamber's half extents less one cell radius.)
+__device__ __noinline__ void divide_one(DevState* S, int32_t i, int32_t slot, uint64_t did, double hx, double hy,
+                                        double hz) {
+    const SoA v = S->cur;
+    const double a = AGB_CELL_RADIUS;
+    const double half0 = __dmul_rn(0.5, __dsub_rn(v.energy[i], AGB_LIFE_DIVISION_ENERGY_COST));
+    const double half = half0 > 0.0 ? half0 : 0.0;
+    v.energy[i] = half;
+    v.energy[slot] = half;
+    v.co2_held[i] = 0.0;
+    v.co2_held[slot] = 0.0;
+    v.biomass[slot] = AGB_CELL_MASS_DRY;
+    const uint64_t hsh = splitmix64(splitmix64(did));      // division_axis, lifecycle.cuh:87-99
+    const double u = (double)(hsh >> 33) * (1.0 / 2147483648.0) - 1.0;
+    const double phi = (double)(hsh & 0xFFFFFFFFull) * (AGB_TWO_PI / 4294967296.0);
+    const double uu = __dmul_rn(u, u);
+    const double sr = sqrt(uu < 1.0 ? __dsub_rn(1.0, uu) : 0.0);
+    const double ax = __dmul_rn(sr, cos(phi)), ay = __dmul_rn(sr, sin(phi)), az = u;
+    // Rounded as written in lifecycle.cu:169-171 (no contraction).
+    double x = v.x[i], y = v.y[i], z = v.z[i];
+    const double ox = __dmul_rn(a, ax), oy = __dmul_rn(a, ay), oz = __dmul_rn(a, az);
+    double xs = __dadd_rn(x, ox), ys = __dadd_rn(y, oy), zs = __dadd_rn(z, oz);
+    x = __dsub_rn(x, ox); y = __dsub_rn(y, oy); z = __dsub_rn(z, oz);
+    xs = xs < -hx ? -hx : (xs > hx ? hx : xs);
+    ys = ys < -hy ? -hy : (ys > hy ? hy : ys);
+    zs = zs < -hz ? -hz : (zs > hz ? hz : zs);
+    x = x < -hx ? -hx : (x > hx ? hx : x);
+    y = y < -hy ? -hy : (y > hy ? hy : y);
+    z = z < -hz ? -hz : (z > hz ? hz : z);
+    v.x[slot] = xs; v.y[slot] = ys; v.z[slot] = zs;
+    v.x[i] = x; v.y[i] = y; v.z[i] = z;
+    v.vx[slot] = v.vx[i]; v.vy[slot] = v.vy[i]; v.vz[slot] = v.vz[i];
+    v.id[slot] = did;
+    v.flags[slot] = v.flags[i];
+    v.death_cause[slot] = AGB_DEATH_NONE;
+    v.temp_cell[slot] = v.temp_cell[i];
+    v.emit_power[slot] = 0.0f;
+    v.dir_x[slot] = v.dir_x[i]; v.dir_y[slot] = v.dir_y[i]; v.dir_z[slot] = v.dir_z[i];
+    v.age_s[slot] = 0.0f;
+    v.rng_state[slot] = pcg_split(v.rng_state[i], did);
+    v.taxis_memory[slot] = 0.0f;
+    v.run_timer[slot] = 0.0f;
+    v.t_local[slot] = v.t_local[i];
+    v.irradiance[slot] = 0.0f;
+    v.co2_local[slot] = v.co2_local[i];
+    v.n2_local[slot] = v.n2_local[i];
+}
+
 // ---------------------------------------------------------------------------
 // Division (divide_kernel, lifecycle.cu:140-204). Rare per cell, so the
 // placement arithmetic stays in FP64 exactly as the reference has it.
@@ -231,8 +283,6 @@ __device__ __forceinline__ void divide_kernel_body(DevState* S, const Ctx& c, co
     const SoA v = S->cur;
     const int32_t n = S->count;                 // base = old count
     const uint64_t first_id = S->next_id;
-    const double a = AGB_CELL_RADIUS;
-    const double hx = 0.5 * c.chamber_w - a, hy = 0.5 * c.chamber_h - a, hz = 0.5 * c.chamber_d - a;
     const GridDev C2 = c.g[AGB_FIELD_CO2];
     AGB_FOR_CELLS_B(i, blk, (births_now > 0 || demand) ? n : 0) {
         if (demand && (v.flags[i] & AGB_FLAG_OCCUPIED)) {
@@ -244,48 +294,8 @@ __device__ __forceinline__ void divide_kernel_body(DevState* S, const Ctx& c, co
         if (births_now <= 0 || !divflag[i]) continue;
         const int32_t slot = n + prefix[i];
         if (slot >= c.capacity) continue;       // store full: skip, do not wrap
-        const uint64_t did = first_id + (uint64_t)prefix[i];
-        const double half0 = __dmul_rn(0.5, __dsub_rn(v.energy[i], AGB_LIFE_DIVISION_ENERGY_COST));
-        const double half = half0 > 0.0 ? half0 : 0.0;
-        v.energy[i] = half;
-        v.energy[slot] = half;
-        v.co2_held[i] = 0.0;
-        v.co2_held[slot] = 0.0;
-        v.biomass[slot] = AGB_CELL_MASS_DRY;
-        const uint64_t hsh = splitmix64(splitmix64(did));      // division_axis, lifecycle.cuh:87-99
-        const double u = (double)(hsh >> 33) * (1.0 / 2147483648.0) - 1.0;
-        const double phi = (double)(hsh & 0xFFFFFFFFull) * (AGB_TWO_PI / 4294967296.0);
-        const double uu = __dmul_rn(u, u);
-        const double sr = sqrt(uu < 1.0 ? __dsub_rn(1.0, uu) : 0.0);
-        const double ax = __dmul_rn(sr, cos(phi)), ay = __dmul_rn(sr, sin(phi)), az = u;
-        // Rounded as written in lifecycle.cu:169-171 (no contraction).
-        double x = v.x[i], y = v.y[i], z = v.z[i];
-        const double ox = __dmul_rn(a, ax), oy = __dmul_rn(a, ay), oz = __dmul_rn(a, az);
-        double xs = __dadd_rn(x, ox), ys = __dadd_rn(y, oy), zs = __dadd_rn(z, oz);
-        x = __dsub_rn(x, ox); y = __dsub_rn(y, oy); z = __dsub_rn(z, oz);
-        xs = xs < -hx ? -hx : (xs > hx ? hx : xs);
-        ys = ys < -hy ? -hy : (ys > hy ? hy : ys);
-        zs = zs < -hz ? -hz : (zs > hz ? hz : zs);
-        x = x < -hx ? -hx : (x > hx ? hx : x);
-        y = y < -hy ? -hy : (y > hy ? hy : y);
-        z = z < -hz ? -hz : (z > hz ? hz : z);
-        v.x[slot] = xs; v.y[slot] = ys; v.z[slot] = zs;
-        v.x[i] = x; v.y[i] = y; v.z[i] = z;
-        v.vx[slot] = v.vx[i]; v.vy[slot] = v.vy[i]; v.vz[slot] = v.vz[i];
-        v.id[slot] = did;
-        v.flags[slot] = v.flags[i];
-        v.death_cause[slot] = AGB_DEATH_NONE;
-        v.temp_cell[slot] = v.temp_cell[i];
-        v.emit_power[slot] = 0.0f;
-        v.dir_x[slot] = v.dir_x[i]; v.dir_y[slot] = v.dir_y[i]; v.dir_z[slot] = v.dir_z[i];
-        v.age_s[slot] = 0.0f;
-        v.rng_state[slot] = pcg_split(v.rng_state[i], did);
-        v.taxis_memory[slot] = 0.0f;
-        v.run_timer[slot] = 0.0f;
-        v.t_local[slot] = v.t_local[i];
-        v.irradiance[slot] = 0.0f;
-        v.co2_local[slot] = v.co2_local[i];
-        v.n2_local[slot] = v.n2_local[i];
+        divide_one(S, i, slot, first_id + (uint64_t)prefix[i], 0.5 * c.chamber_w - AGB_CELL_RADIUS,
+                   0.5 * c.chamber_h - AGB_CELL_RADIUS, 0.5 * c.chamber_d - AGB_CELL_RADIUS);
     }
     // The last CTA to finish runs the tick's bookkeeping (every division of
     // this pass has been written by then).
@@ -615,7 +625,7 @@ void launch_compact_kernels(DevState* S, const LifeBuffers& b, int32_t capacity,
 
 AGB_BATCHED(uptake_mark_batch, 256,
             uptake_mark_kernel_body(a.S, a.c, a.p, a.demand, a.inv_gv, a.life.flags, blk))
-AGB_BATCHED(divide_batch, 256,
+AGB_BATCHED_MB(divide_batch, 256, 3,
             divide_kernel_body(a.S, a.c, a.life.flags, a.life.prefix, a.arg, a.demand, blk))
 AGB_BATCHED(keep_batch, 256, keep_kernel_body(a.S, a.life.flags, blk))
 AGB_BATCHED(scatter_src_batch, 256, scatter_src_kernel_body(a.S, a.life.flags, a.life.prefix, a.life.src, blk))

@@ -776,6 +776,8 @@ agb_status agb_world_create(const agb_world_desc* d, agb_world** out) {
         const int64_t yz = (int64_t)I.ny * I.nz, xz = (int64_t)I.nx * I.nz, xy = (int64_t)I.nx * I.ny;
         w->irr_mark_bytes = std::max(yz, std::max(xz, xy));
         ok = ok && dalloc(w, &c.irr_marks, (size_t)w->irr_mark_bytes) == cudaSuccess;
+        w->irr_bit_words = (I.count + 31) / 32;
+        ok = ok && dalloc(w, &c.irr_stamp_bits, 4 * (size_t)w->irr_bit_words) == cudaSuccess;
     }
     for (cudaStream_t& st : w->side) ok = ok && cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess;
     for (cudaEvent_t& e : w->ev) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
@@ -783,6 +785,7 @@ agb_status agb_world_create(const agb_world_desc* d, agb_world** out) {
     ok = ok && dalloc(w, &w->life.co2_demand, 8 * (size_t)co2n) == cudaSuccess;
     if (!ok) { agb_world_destroy(w); return AGB_OUT_OF_MEMORY; }
     if (c.irr_marks) cudaMemset(c.irr_marks, 2, (size_t)w->irr_mark_bytes);   // first sweep: every line
+    if (c.irr_stamp_bits) cudaMemset(c.irr_stamp_bits, 0, 4 * (size_t)w->irr_bit_words);
     cudaMemset(h.ranges, 0, 8 * (size_t)h.buckets);
     cudaMemset(h.occ, 0, 4 * (((size_t)h.buckets + 31) / 32 + 1));
     cudaMemset(h.keys_sorted, 0, 4 * n);

@@ -38,6 +38,10 @@ struct Ctx {
     // shadow), 0 = no stamp in either, so its values are already the
     // unshadowed ones and the sweep leaves it alone. Null: sweep every line.
     uint8_t* irr_marks;
+    // One bit per irradiance voxel: set where this tick's stamps deposited
+    // (mirrors deposit != 0), so the sweep tests bits instead of reading the
+    // 8-byte deposit of every voxel.
+    uint32_t* irr_stamp_bits;
     double face_area;
     long long stamp_alive, stamp_dead;   // fixed-point occlusion stamps
     // Exact float thresholds equivalent to the reference's FP64 compares.

@@ -51,6 +51,7 @@ struct agb_world {
     int walk_lanes = 1;                  // threads sharing one cell's neighbour walk (1, 2, 4, 8)
     bool fuse_cells = false;             // feeding, taxis and forces in one kernel with one walk
     int64_t irr_mark_bytes = 0;          // size of c.irr_marks (irradiance lines over any light axis)
+    int64_t irr_bit_words = 0;           // size of c.irr_stamp_bits in 32-bit words
     uint64_t tick = 0;
     double sim_time = 0.0;
     double physics_rate = 1.0, biology_rate = 1.0;
