@@ -486,6 +486,29 @@ def run_reference(args, wl):
     return 0
 
 
+def profile_batch(steps, staged=True):
+    """The 64-chamber batch after 20 warm-up steps, then `steps` steps inside an
+    NVTX range named "timed" (ncu --nvtx --nvtx-include "timed/" selects them)."""
+    import torch
+    descs, spawns, _info = batch_workload(64, seed=1)
+    b = agb.Batch(descs, spawns, agb.batch_opts(autotune=True, staged=staged))
+    st = torch.cuda.Stream()
+    sh = st.cuda_stream
+    with torch.cuda.stream(st):
+        for _ in range(20):
+            b.step(1, stream=sh)
+        torch.cuda.synchronize()
+        k0 = b.graph_kernels()
+        torch.cuda.nvtx.range_push("timed")
+        for _ in range(steps):
+            b.step(1, stream=sh)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+    print("profile-batch: %d steps, %d kernels, staged %s" % (steps, b.graph_kernels() - k0, b.staged()))
+    b.close()
+    return 0
+
+
 def profile_stencil(n, passes=6):
     """A world holding one n^3 temperature grid (no cells): `passes` FTCS passes."""
     d = agb.default_desc(capacity=16, seed=1)
@@ -545,12 +568,16 @@ def main():
     ap.add_argument("--surrogate-windows", type=int, default=1500,
                     help="training windows of the learned field surrogate (0: skip the surrogate leg)")
     ap.add_argument("--surrogate-windows-run", type=int, default=16)
+    ap.add_argument("--profile-batch", type=int, default=0,
+                    help="only run N steps of the batched ensemble inside an NVTX range (small case for ncu)")
     ap.add_argument("--profile-stencil", type=int, default=0,
                     help="only run a few FTCS passes on an N^3 temperature grid (small case for ncu)")
     ap.add_argument("--profile-surrogate", type=int, default=0,
                     help="only run N surrogate windows and one training step (small case for ncu)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.profile_batch:
+        return profile_batch(args.profile_batch, staged=bool(args.batch_staged))
     if args.profile_stencil:
         return profile_stencil(args.profile_stencil)
     if args.profile_surrogate:
