@@ -183,7 +183,7 @@ ChamberArgs chamber_args(agb_world* w) {
     a.demand = co2.enabled ? w->life.co2_demand : nullptr;
     a.inv_gv = co2.enabled ? (float)(1.0 / (co2.dx * co2.dx * co2.dz_eff)) : 0.0f;
     bool per4 = true;
-    hash_sort_shape(w->c.h, w->c.capacity, a.passes, a.max_tiles, per4);
+    hash_sort_shape(w->c.h, w->c.capacity, a.passes, a.max_tiles, per4, a.radix_bits);
     return a;
 }
 
@@ -318,24 +318,25 @@ void plan_tick(agb_batch* b, StagedPlan& P) {
         for (agb_world* w : W) {
             ChamberArgs a = chamber_args(w);
             kh.push_back(a);
-            a.nblk = hash_clear_blocks(a.passes, a.max_tiles);
+            a.nblk = hash_clear_blocks(a.passes, a.max_tiles, a.radix_bits);
             hc.push_back(a);
             maxp = std::max(maxp, a.passes);
         }
         P.stage(0, BStage::HashClear, hc);
         P.stage(0, BStage::KeyHist, kh);
         for (int32_t p = 0; p < maxp; ++p) {
-            std::vector<ChamberArgs> r4, r8;
+            std::vector<ChamberArgs> r4, r49, r8;
             for (size_t i = 0; i < n; ++i) {
                 if (p >= kh[i].passes) continue;
                 ChamberArgs a = kh[i];
-                int32_t passes = 0, tiles = 0;
+                int32_t passes = 0, tiles = 0, rb = 8;
                 bool per4 = true;
-                hash_sort_shape(W[i]->c.h, W[i]->c.capacity, passes, tiles, per4);
+                hash_sort_shape(W[i]->c.h, W[i]->c.capacity, passes, tiles, per4, rb);
                 a.nblk = tiles;
-                (per4 ? r4 : r8).push_back(a);
+                (!per4 ? r8 : (rb == 9 ? r49 : r4)).push_back(a);
             }
             P.stage(0, BStage::Radix4, r4, p);
+            P.stage(0, BStage::Radix4x9, r49, p);
             P.stage(0, BStage::Radix8, r8, p);
         }
         P.stage(0, BStage::Ranges, kh);

@@ -37,6 +37,7 @@ struct ChamberArgs {
     int32_t nblk;                 // the chamber's blocks in this launch
     int32_t arg;                  // stage switch (cell step: feed | taxis << 1; divide: compaction allowed)
     int32_t passes, max_tiles;    // hash sort: digit passes, tiles per pass
+    int32_t radix_bits;           // hash sort: bits per digit (8 or 9)
 };
 
 // A batched kernel NAME(tab, map): finds its chamber and block, then CALL
@@ -57,7 +58,7 @@ struct ChamberArgs {
 enum class BStage : int32_t {
     Thermal, ClearStamps, Stamp, Occlusion, SweepRows, SweepLines, CellStep, Integrate,   // k_cells.cu
     Flush,                                                                                // k_grid.cu
-    HashClear, KeyHist, Radix4, Radix8, Ranges,                                           // k_hash.cu
+    HashClear, KeyHist, Radix4, Radix4x9, Radix8, Ranges,                                 // k_hash.cu
     UptakeMark, Scan, Divide, Keep, ScatterSrc, Gather, Swap                              // k_life.cu
 };
 // Threads per block of a batched stage.
@@ -74,11 +75,13 @@ bool launch_batched_hash(BStage st, const ChamberArgs* tab, const uint32_t* map,
 bool launch_batched_life(BStage st, const ChamberArgs* tab, const uint32_t* map, int32_t blocks, int32_t arg,
                          cudaStream_t s);
 // Blocks of a chamber in a batched stage, as the per-world launches size them.
-int32_t hash_clear_blocks(int32_t passes, int32_t max_tiles);
+int32_t hash_clear_blocks(int32_t passes, int32_t max_tiles, int32_t radix_bits);
 int32_t scan_blocks(int32_t capacity);
-// Digit passes and tiles per pass of the hash sort for a world, and whether its
-// tiles are 1024 keys (Radix4) or 2048 (Radix8).
-void hash_sort_shape(const HashDev& h, int32_t capacity, int32_t& passes, int32_t& max_tiles, bool& per4);
+// Digit passes, tiles per pass and digit width of the hash sort for a world,
+// and whether its tiles are 1024 keys (Radix4, Radix4x9 for 9-bit digits) or
+// 2048 (Radix8).
+void hash_sort_shape(const HashDev& h, int32_t capacity, int32_t& passes, int32_t& max_tiles, bool& per4,
+                     int32_t& radix_bits);
 
 // co2_uptake_rate (src/sim/lifecycle.cuh:24-28) in FP32.
 __device__ __forceinline__ float co2_uptake_rate_f(float c) {

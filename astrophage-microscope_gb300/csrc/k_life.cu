@@ -214,9 +214,8 @@ __global__ void __launch_bounds__(ST) scan_kernel(DevState* S, const int32_t* __
 }
 
 // Division of parent i into `slot` with id `did` (divide_kernel body,
-// lifecycle.cu:140-204). Out of line: it is rare, and inlined its FP64
-// placement would set the register budget of the whole pass, which mostly
-// runs the per-cell CO2 flush.
+// lifecycle.cu:140-204); called only for the cells that divide, from the pass
+// that otherwise runs the per-cell CO2 flush.
 // (hx, hy, hz: the chamber's half extents less one cell radius.)
 __device__ __noinline__ void divide_one(DevState* S, int32_t i, int32_t slot, uint64_t did, double hx, double hy,
                                         double hz) {
