@@ -62,8 +62,8 @@ struct agb_batch {
     cudaEvent_t fork = nullptr;
     cudaStream_t own_stream = nullptr;
     bool staged = false;                    // one launch per stage over every chamber
-    cudaStream_t side[2] = {nullptr, nullptr};
-    cudaEvent_t sev[3] = {nullptr, nullptr, nullptr};
+    cudaStream_t side[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t sev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     std::vector<BatchGraph> graphs;
     int64_t graph_kernels_total = 0;
     std::string err;
@@ -120,7 +120,7 @@ enum class OpKind { Launch, Ftcs, Record, Wait };
 
 struct StagedOp {
     OpKind kind;
-    int32_t stream;                         // 0: the step's stream; 1, 2: the batch's side streams
+    int32_t stream;                         // 0: the step's stream; 1-3: the batch's side streams
     BStage st;
     size_t tab, map;                        // offsets into the arena
     int32_t blocks, arg;
@@ -238,7 +238,11 @@ void plan_tick(agb_batch* b, StagedPlan& P) {
     P.record(0, 0);
     P.wait(1, 0);
     P.wait(2, 0);
-    // Branch 1: thermal substeps (thermal, flush, FTCS), then the irradiance field.
+    P.wait(3, 0);
+    // Branch 1: thermal substeps, then the irradiance field. A chamber's last
+    // substep's flush and FTCS pass fork onto branch 3 once its thermal
+    // kernel has run (as in tick_once), beside the irradiance field; earlier
+    // substeps' stay on branch 1, ahead of the next thermal kernel.
     std::vector<int32_t> nsub(n, 0);
     int32_t maxsub = 0;
     for (size_t i = 0; i < n; ++i) {
@@ -247,20 +251,28 @@ void plan_tick(agb_batch* b, StagedPlan& P) {
         maxsub = std::max(maxsub, nsub[i]);
     }
     for (int32_t k = 0; k < maxsub; ++k) {
-        std::vector<agb_world*> act;
-        std::vector<ChamberArgs> th, fl;
+        std::vector<agb_world*> mid, fin;
+        std::vector<ChamberArgs> th, flm, flf;
         for (size_t i = 0; i < n; ++i) {
             if (k >= nsub[i]) continue;
             ChamberArgs a = chamber_args(W[i]);
             th.push_back(a);
             a.g = W[i]->c.g[AGB_FIELD_TEMPERATURE];
-            fl.push_back(a);
-            act.push_back(W[i]);
+            const bool last = k + 1 == nsub[i];
+            (last ? flf : flm).push_back(a);
+            (last ? fin : mid).push_back(W[i]);
         }
         P.stage(1, BStage::Thermal, th);
-        P.stage(1, BStage::Flush, fl);
-        plan_ftcs(P, 1, act, AGB_FIELD_TEMPERATURE);
+        if (!fin.empty()) {
+            P.record(1, 3);
+            P.wait(3, 3);
+            P.stage(3, BStage::Flush, flf);
+            plan_ftcs(P, 3, fin, AGB_FIELD_TEMPERATURE);
+        }
+        P.stage(1, BStage::Flush, flm);
+        plan_ftcs(P, 1, mid, AGB_FIELD_TEMPERATURE);
     }
+    P.record(3, 4);
     std::vector<uint8_t> emit(n, 0);
     {
         std::vector<ChamberArgs> clr, stp, swr, swl;
@@ -342,6 +354,7 @@ void plan_tick(agb_batch* b, StagedPlan& P) {
         P.stage(0, BStage::Ranges, kh);
     }
     P.wait(0, 1);
+    P.wait(0, 4);
     // Feeding, taxis and forces in one pass; then integration with the CO2 demand.
     {
         std::vector<ChamberArgs> cs, ig;
@@ -392,7 +405,7 @@ void plan_tick(agb_batch* b, StagedPlan& P) {
 }
 
 void run_plan(agb_batch* b, const StagedPlan& P, char* arena, cudaStream_t s) {
-    cudaStream_t st[3] = {s, b->side[0], b->side[1]};
+    cudaStream_t st[4] = {s, b->side[0], b->side[1], b->side[2]};
     for (const StagedOp& o : P.ops) {
         switch (o.kind) {
             case OpKind::Launch:
