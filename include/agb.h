@@ -289,8 +289,9 @@ typedef struct agb_batch_opts {
     double hash_candidates[8];  /* metres; candidates under one cell diameter are skipped */
     int32_t probe_ticks;        /* timed probe ticks per candidate (0 = 4) */
     int32_t staged;             /* 1 (default): each stage of the tick is one launch over every chamber,
-                                   when every enabled grid is 3-D with a TMA stencil and no chamber has a
-                                   surrogate attached; 0: each chamber's tick is launched on the lanes */
+                                   when every enabled grid is 3-D with a TMA stencil, no chamber has a
+                                   surrogate attached and none exceeds ~67M cells of capacity; 0: each
+                                   chamber's tick is launched on the lanes */
 } agb_batch_opts;
 
 /* What a chamber was built with, and what the autotuner measured for it. */
