@@ -22,6 +22,7 @@ STATUS_NAMES = ["Ok", "OutOfMemory", "CudaError", "InvalidArgument", "NotFound",
                 "DeviceTimeout"]
 BC_DIRICHLET, BC_NEUMANN, BC_ROBIN = 0, 1, 2
 FIELD_T, FIELD_CO2, FIELD_N2, FIELD_IRR = 0, 1, 2, 3
+BRUSH_HEAT, BRUSH_CHILL, BRUSH_INJECT_CO2, BRUSH_INJECT_N2 = 0, 1, 2, 3       # src/sim/world.cuh:33
 WALL_REFLECTING, WALL_PERIODIC, WALL_ABSORBING = 0, 1, 2
 GRAVITY_Y, GRAVITY_Z = 0, 1
 DIVIDE_CO2_QUOTA, DIVIDE_ENERGY = 0, 1
@@ -279,6 +280,7 @@ def load(path=LIB_PATH):
         "agb_world_import_field": (I32, [P, I32, P, P]),
         "agb_world_export_field": (I32, [P, I32, P, P]),
         "agb_world_export_deposit": (I32, [P, I32, P, P]),
+        "agb_world_apply_brush": (I32, [P, I32, C.c_double, C.c_double, C.c_double, C.c_double, P]),
         "agb_world_step": (I32, [P, I32, P]),
         "agb_world_step_graph": (I32, [P, I32, P]),
         "agb_world_stage": (I32, [P, I32, P]),
@@ -341,6 +343,7 @@ def exported_symbols():
             "agb_world_create", "agb_world_destroy", "agb_world_spawn", "agb_world_import_cells",
             "agb_world_export_cells", "agb_world_device_cells", "agb_world_step_host", "agb_world_count",
             "agb_world_import_field", "agb_world_export_field", "agb_world_export_deposit",
+            "agb_world_apply_brush",
             "agb_world_step", "agb_world_step_graph", "agb_world_graph_kernels", "agb_world_set_walk",
             "agb_world_walk", "agb_world_stage",
             "agb_world_diffuse",
@@ -457,6 +460,12 @@ class World:
         out = np.zeros(field_shape(self.desc, f), dtype=np.uint64)
         self._check(self.lib.agb_world_export_deposit(self.h, f, out.ctypes.data, None), "export_deposit")
         return out
+
+    def apply_brush(self, kind, x, y, radius, strength, stream=None):
+        """world_apply_brush (src/sim/step.cu:80-89): a smooth disc of `strength`
+        added to (chill: taken from) the brush kind's field between ticks."""
+        self._check(self.lib.agb_world_apply_brush(self.h, kind, x, y, radius, strength, _st(stream)),
+                    "apply_brush")
 
     def step(self, ticks=1, graph=False, stream=None):
         fn = self.lib.agb_world_step_graph if graph else self.lib.agb_world_step

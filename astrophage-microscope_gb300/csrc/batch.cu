@@ -291,8 +291,7 @@ void plan_tick(agb_batch* b, StagedPlan& P) {
             const int64_t len = axis == 0 ? I.nx : (axis == 1 ? I.ny : I.nz);
             const int64_t lines = I.count / len;
             if (axis == 0) {
-                const int64_t bl = (lines * 32 + 255) / 256;
-                a.nblk = (int32_t)(bl < 65535 ? bl : 65535);
+                a.nblk = sweep_rows_blocks(lines);
                 swr.push_back(a);
             } else {
                 a.nblk = (int32_t)((lines + 127) / 128);

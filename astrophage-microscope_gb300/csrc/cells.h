@@ -77,6 +77,11 @@ bool launch_batched_life(BStage st, const ChamberArgs* tab, const uint32_t* map,
 // Blocks of a chamber in a batched stage, as the per-world launches size them.
 int32_t hash_clear_blocks(int32_t passes, int32_t max_tiles, int32_t radix_bits);
 int32_t scan_blocks(int32_t capacity);
+// Blocks of the x-axis sweep over `lines` rows: a warp per 32 rows, 8 warps a block.
+inline int32_t sweep_rows_blocks(int64_t lines) {
+    const int64_t b = ((lines + 31) / 32 + 7) / 8;
+    return (int32_t)(b < 65535 ? b : 65535);
+}
 // Digit passes, tiles per pass and digit width of the hash sort for a world,
 // and whether its tiles are 1024 keys (Radix4, Radix4x9 for 9-bit digits) or
 // 2048 (Radix8).

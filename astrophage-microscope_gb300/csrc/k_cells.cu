@@ -323,42 +323,81 @@ __global__ void __launch_bounds__(128) sweep_kernel(Ctx c, const double* __restr
     sweep_kernel_body(c, factor, grid_blk());
 }
 
-// x-axis sweep: rows are contiguous in memory, so one warp takes a row, 32
-// consecutive voxels per step (coalesced). Stamped voxels are rare; the FP64
-// recurrence walks them in sweep order, broadcasting each factor.
+// 32 stamp bits of the row starting at voxel `rowbase`: bit m is voxel xa + m;
+// voxels outside [0, len) read 0.
+__device__ __forceinline__ uint32_t row_stamp_bits(const uint32_t* __restrict__ bits, int64_t nwords,
+                                                   int64_t rowbase, int32_t xa, int32_t len) {
+    const int32_t lo = xa < 0 ? 0 : xa;
+    const int32_t hi = xa + 32 < len ? xa + 32 : len;
+    if (hi <= lo) return 0u;
+    const int64_t q = rowbase + lo;
+    const int64_t wi = q >> 5;
+    const int sh = (int)(q & 31);
+    uint32_t v = __ldg(&bits[wi]) >> sh;
+    if (sh && wi + 1 < nwords) v |= __ldg(&bits[wi + 1]) << (32 - sh);
+    const int32_t n = hi - lo;
+    if (n < 32) v &= (1u << n) - 1u;
+    return v << (lo - xa);
+}
+
+// x-axis sweep (light along x): rows are contiguous in memory. A warp takes
+// 32 rows and moves along them 32 voxels at a time. Each lane runs its own
+// row's FP64 transmittance recurrence over the chunk's stamped voxels only,
+// so the warp issues FP64 work as often as its busiest row has stamps in the
+// chunk, not once per stamp of every row (FP64 issues at a small fraction of
+// the FP32 rate). The value following each stamp goes to shared memory; the
+// warp then writes the chunk row by row, 32 consecutive voxels per store: a
+// voxel takes the value after its row's last stamp before it in sweep order,
+// else the value the row entered the chunk with.
+constexpr int SWEEP_ROW_WARPS = 8;       // sweep_rows_blocks and the batched launch assume 256 threads
+
 __device__ __forceinline__ void sweep_rows_kernel_body(const Ctx& c, const double* __restrict__ factor, Blk blk) {
+    __shared__ float after[SWEEP_ROW_WARPS][32][33];
     const GridDev I = c.g[AGB_FIELD_IRRADIANCE];
-    const int lane = threadIdx.x & 31;
-    const int64_t warp = ((int64_t)blk.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)blk.n * blockDim.x) >> 5;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    float (*buf)[33] = after[wib];
     const int32_t len = I.nx;
     const int64_t lines = I.count / len;
-    for (int64_t line = warp; line < lines; line += nwarps) {
-        const uint8_t mark = c.irr_marks ? c.irr_marks[line] : 1;    // one byte, broadcast to the warp
-        if (mark == 0) continue;                                    // values already unshadowed
-        __syncwarp();
-        if (c.irr_marks && lane == 0) c.irr_marks[line] = mark == 1 ? 2 : 0;
-        const int64_t base = line * len;
+    const int64_t groups = (lines + 31) / 32;
+    const int64_t nwords = (I.count + 31) / 32;
+    const float entry = fa(d2f((double)c.source * 1.0), c.ambient_irr);
+    for (int64_t g = (int64_t)blk.x * SWEEP_ROW_WARPS + wib; g < groups; g += (int64_t)blk.n * SWEEP_ROW_WARPS) {
+        const int64_t row = g * 32 + lane;
+        uint8_t mark = 0;
+        if (row < lines) {
+            mark = c.irr_marks ? c.irr_marks[row] : 1;
+            if (c.irr_marks && mark) c.irr_marks[row] = mark == 1 ? 2 : 0;
+        }
+        const unsigned active = __ballot_sync(0xFFFFFFFFu, mark != 0);
+        if (!active) continue;                              // every row already unshadowed
+        const int64_t rowbase = row * len;
         double t = 1.0;
-        float cur = fa(d2f((double)c.source * t), c.ambient_irr);
+        float cur = entry;
         for (int32_t s0 = 0; s0 < len; s0 += 32) {
-            const int32_t s = s0 + lane;
-            const bool in = s < len;
-            const int64_t idx = base + (c.light_sign > 0 ? s : (len - 1 - s));
-            const bool raw = in && stamped(c, I, idx);
-            unsigned mask = __ballot_sync(0xFFFFFFFFu, raw);
-            float mine = cur;
-            if (mask) {
-                const double f = raw ? __ldg(&factor[idx]) : 1.0;
-                while (mask) {
-                    const int b = __ffs(mask) - 1;
-                    mask &= mask - 1u;
-                    t *= __shfl_sync(0xFFFFFFFFu, f, b);
-                    cur = fa(d2f((double)c.source * t), c.ambient_irr);
-                    if (lane > b) mine = cur;
-                }
+            uint32_t sb = 0u;
+            if (mark) {
+                sb = c.light_sign > 0 ? row_stamp_bits(c.irr_stamp_bits, nwords, rowbase, s0, len)
+                                      : __brev(row_stamp_bits(c.irr_stamp_bits, nwords, rowbase, len - s0 - 32, len));
             }
-            if (in) I.value[idx] = mine;
+            for (uint32_t m = sb; m; m &= m - 1u) {
+                const int j = __ffs(m) - 1;
+                const int32_t x = c.light_sign > 0 ? s0 + j : len - 1 - (s0 + j);
+                t *= __ldg(&factor[rowbase + x]);
+                buf[lane][j] = fa(d2f((double)c.source * t), c.ambient_irr);
+            }
+            __syncwarp();
+            const int32_t s = s0 + lane;
+            const int32_t x = c.light_sign > 0 ? s : len - 1 - s;
+            const uint32_t before = (1u << lane) - 1u;
+            for (unsigned a = active; a; a &= a - 1u) {
+                const int r = __ffs(a) - 1;
+                const uint32_t rb = __shfl_sync(0xFFFFFFFFu, sb, r) & before;
+                const float rc = __shfl_sync(0xFFFFFFFFu, cur, r);
+                const float v = rb ? buf[r][31 - __clz(rb)] : rc;
+                if (s < len) I.value[(g * 32 + r) * len + x] = v;
+            }
+            if (sb) cur = buf[lane][31 - __clz(sb)];
+            __syncwarp();
         }
     }
 }
@@ -1010,8 +1049,7 @@ void launch_emission_prep(DevState* S, const Ctx& c, const TickParams& p, int32_
     const int32_t len = c.light_axis == 0 ? I.nx : (c.light_axis == 1 ? I.ny : I.nz);
     const int64_t lines = I.count / len;
     if (c.light_axis == 0) {
-        const int64_t blocks = (lines * 32 + 255) / 256;
-        launch_k(sweep_rows_kernel, (unsigned)(blocks < 65535 ? blocks : 65535), 256, 0, s, c, factor);
+        launch_k(sweep_rows_kernel, (unsigned)sweep_rows_blocks(lines), 32 * SWEEP_ROW_WARPS, 0, s, c, factor);
     } else {
         launch_k(sweep_kernel, (unsigned)((lines + 127) / 128), 128, 0, s, c, factor);
     }

@@ -26,6 +26,34 @@ __global__ void fill_kernel(float* v, int64_t n, float value) {
         v[i] = value;
 }
 
+// brush_kernel (src/fields/diffuse.cu:62-77): value += amount * (1 - t^2)^2 with
+// t = r / radius, r the in-plane distance of the voxel centre from (cx, cy),
+// for r <= radius. The launch covers the disc's bounding box of columns
+// [x0, x0 + bw) x [y0, y0 + bh) on every z plane (nz == 1 is the reference's
+// grid; a 3-D grid takes the same disc on each plane). Explicitly rounded, in
+// the reference's order of operations.
+__global__ void brush_kernel(float* v, GridDev g, float cx, float cy, float radius, float amount,
+                             int32_t x0, int32_t y0, int32_t bw, int32_t bh) {
+    pdl_wait();
+    const int64_t n = (int64_t)bw * bh * g.nz;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t i = x0 + (int32_t)(k % bw);
+        const int64_t r2 = k / bw;
+        const int32_t j = y0 + (int32_t)(r2 % bh);
+        const int32_t z = (int32_t)(r2 / bh);
+        const float x = fs(fm(fa((float)i, 0.5f), g.dxf), g.hx);
+        const float y = fs(fm(fa((float)j, 0.5f), g.dxf), g.hy);
+        const float ex = fs(x, cx), ey = fs(y, cy);
+        const float r = sqrtf(fa(fm(ex, ex), fm(ey, ey)));
+        if (r > radius) continue;
+        const float t = __fdiv_rn(r, radius);
+        const float q = fs(1.0f, fm(t, t));
+        const int64_t idx = i + (int64_t)g.nx * (j + (int64_t)g.ny * z);
+        v[idx] = fa(v[idx], fm(amount, fm(q, q)));
+    }
+}
+
 struct Faces {
     int32_t bc[6];
     float val[6];
@@ -338,6 +366,15 @@ bool launch_batched_grid(BStage st, const ChamberArgs* tab, const uint32_t* map,
 void launch_fill(float* v, int64_t n, float value, cudaStream_t s) {
     const int64_t blocks = (n + 255) / 256;
     launch_k(fill_kernel, (unsigned)(blocks > 4096 ? 4096 : blocks), 256, 0, s, v, n, value);
+}
+
+void launch_brush(float* v, const GridDev& g, float cx, float cy, float radius, float amount,
+                  int32_t x0, int32_t y0, int32_t bw, int32_t bh, cudaStream_t s) {
+    const int64_t n = (int64_t)bw * bh * g.nz;
+    if (n <= 0) return;
+    const int64_t blocks = (n + 255) / 256;
+    launch_k(brush_kernel, (unsigned)(blocks > 4096 ? 4096 : blocks), 256, 0, s, v, g, cx, cy, radius, amount,
+             x0, y0, bw, bh);
 }
 
 namespace {

@@ -13,6 +13,9 @@ struct WorldConst;   // defined in world.cuh
 
 // Fields (k_grid.cu)
 void launch_fill(float* v, int64_t n, float value, cudaStream_t s);
+// The brush disc over columns [x0, x0 + bw) x [y0, y0 + bh) of every plane.
+void launch_brush(float* v, const GridDev& g, float cx, float cy, float radius, float amount,
+                  int32_t x0, int32_t y0, int32_t bw, int32_t bh, cudaStream_t s);
 // Tiling of the TMA stencil for a grid: lanes along x (16 or 32), rows per
 // thread (1, 2, 4) and z planes per CTA. A tensor map's box is made for one
 // tiling and is used only with it.

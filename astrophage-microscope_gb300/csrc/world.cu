@@ -953,6 +953,42 @@ agb_status agb_world_export_deposit(agb_world* w, int32_t f, uint64_t* dst, agb_
     return AGB_OK;
 }
 
+agb_status agb_world_apply_brush(agb_world* w, int32_t kind, double x, double y, double radius,
+                                 double strength, agb_stream s) {
+    if (!w) return AGB_INVALID_ARGUMENT;
+    int32_t f;
+    double amount = strength;
+    switch (kind) {
+        case AGB_BRUSH_HEAT: f = AGB_FIELD_TEMPERATURE; break;
+        case AGB_BRUSH_CHILL: f = AGB_FIELD_TEMPERATURE; amount = -strength; break;
+        case AGB_BRUSH_INJECT_CO2: f = AGB_FIELD_CO2; break;
+        case AGB_BRUSH_INJECT_N2: f = AGB_FIELD_N2; break;
+        default: return fail(w, AGB_INVALID_ARGUMENT, "unknown brush");
+    }
+    if (!std::isfinite(x) || !std::isfinite(y) || !std::isfinite(radius) || !std::isfinite(strength))
+        return fail(w, AGB_INVALID_ARGUMENT, "brush arguments must be finite");
+    const GridDev& g = w->c.g[f];
+    if (!g.enabled) return fail(w, AGB_INVALID_ARGUMENT, "brush on a field the world does not have");
+    if (radius <= 0.0) return AGB_OK;                  // grid_brush: an empty brush is a no-op
+    const float cx = (float)x, cy = (float)y, rad = (float)radius;
+    // Columns whose centres can lie within the disc, with two voxels of margin
+    // for float rounding; the kernel applies the exact test to each.
+    auto span = [&](float c, float half, int32_t n, int32_t& lo, int32_t& cnt) {
+        const double a = std::floor(((double)c - rad + half) / g.dxf - 0.5) - 2.0;
+        const double b = std::ceil(((double)c + rad + half) / g.dxf - 0.5) + 2.0;
+        const double l = a < 0.0 ? 0.0 : a, h = b > n - 1.0 ? n - 1.0 : b;
+        lo = (int32_t)l;
+        cnt = h >= l ? (int32_t)(h - l) + 1 : 0;
+    };
+    int32_t x0, bw, y0, bh;
+    span(cx, g.hx, g.nx, x0, bw);
+    span(cy, g.hy, g.ny, y0, bh);
+    if (s == nullptr && w->own_stream) s = w->own_stream;
+    launch_brush(field_value(w, f), g, cx, cy, rad, (float)amount, x0, y0, bw, bh, s);
+    AGB_CUDA(w, cudaGetLastError());
+    return AGB_OK;
+}
+
 agb_status agb_world_step(agb_world* w, int32_t ticks, agb_stream s) {
     if (!w || ticks < 0) return AGB_INVALID_ARGUMENT;
     for (int32_t t = 0; t < ticks; ++t) tick_once(w, s);

@@ -64,6 +64,8 @@ enum { AGB_STORE_VOID = 0, AGB_STORE_FLASH = 1, AGB_STORE_RETAIN = 2 };
 /* Division predicate. CO2 quota is the reference (src/sim/lifecycle.cuh:33-36);
  * the stored-energy threshold is an opt-in extension, not reference behaviour. */
 enum { AGB_DIVIDE_CO2_QUOTA = 0, AGB_DIVIDE_ENERGY = 1 };
+/* src/sim/world.cuh:33 BrushKind */
+enum { AGB_BRUSH_HEAT = 0, AGB_BRUSH_CHILL = 1, AGB_BRUSH_INJECT_CO2 = 2, AGB_BRUSH_INJECT_N2 = 3 };
 /* Face order of agb_grid_desc.bc / face_value. */
 enum { AGB_FACE_XMIN = 0, AGB_FACE_XMAX = 1, AGB_FACE_YMIN = 2, AGB_FACE_YMAX = 3,
        AGB_FACE_ZMIN = 4, AGB_FACE_ZMAX = 5 };
@@ -344,6 +346,14 @@ agb_status agb_world_import_field(agb_world* w, int32_t field, const float* src,
 agb_status agb_world_export_field(agb_world* w, int32_t field, float* dst, agb_stream s);
 /* Raw fixed-point accumulator (irradiance: the occlusion stamp of the last emission stage). */
 agb_status agb_world_export_deposit(agb_world* w, int32_t field, uint64_t* dst, agb_stream s);
+
+/* world_apply_brush (src/sim/step.cu:80-89, grid_brush src/fields/diffuse.cu:81-89): add
+ * strength * (1 - (r/radius)^2)^2 to the kind's field (chill: subtract) at voxels whose
+ * centre lies within `radius` [m] of (x, y) in the chamber frame; a 3-D grid takes the disc on
+ * every z plane. radius <= 0 is a no-op. Call between ticks; no host synchronisation.
+ * Errors: unknown kind, non-finite arguments, or a field the world does not have. */
+agb_status agb_world_apply_brush(agb_world* w, int32_t kind, double x, double y, double radius,
+                                 double strength, agb_stream s);
 
 /* world_step x ticks (src/sim/step.cu:109-184). No host synchronisation. */
 agb_status agb_world_step(agb_world* w, int32_t ticks, agb_stream s);

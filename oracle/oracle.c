@@ -467,6 +467,40 @@ int orc_world_export_field(orc_world* w, int32_t f, float* dst) {
     memcpy(dst, w->g[f].value, sizeof(float) * (size_t)w->g[f].count);
     return 0;
 }
+/* world_apply_brush (src/sim/step.cu:80-89) over grid_brush and brush_kernel
+ * (src/fields/diffuse.cu:62-89): value += amount * (1 - t^2)^2, t = r / radius, for
+ * voxel centres within radius of (x, y). EXTENSION: a 3-D grid takes the disc on
+ * every z plane; non-finite arguments and absent fields are rejected. */
+int orc_world_apply_brush(orc_world* w, int32_t kind, double x, double y, double radius, double strength) {
+    int32_t f;
+    double amount = strength;
+    switch (kind) {
+        case AGB_BRUSH_HEAT: f = AGB_FIELD_TEMPERATURE; break;
+        case AGB_BRUSH_CHILL: f = AGB_FIELD_TEMPERATURE; amount = -strength; break;
+        case AGB_BRUSH_INJECT_CO2: f = AGB_FIELD_CO2; break;
+        case AGB_BRUSH_INJECT_N2: f = AGB_FIELD_N2; break;
+        default: return AGB_INVALID_ARGUMENT;
+    }
+    if (!isfinite(x) || !isfinite(y) || !isfinite(radius) || !isfinite(strength)) return AGB_INVALID_ARGUMENT;
+    grid* g = &w->g[f];
+    if (!g->enabled) return AGB_INVALID_ARGUMENT;
+    if (radius <= 0.0) return 0;
+    const float dx = g->dxf, cx = (float)x, cy = (float)y, rad = (float)radius, amt = (float)amount;
+    const float hx = 0.5f * g->nx * dx, hy = 0.5f * g->ny * dx;
+    for (int32_t z = 0; z < g->nz; ++z)
+        for (int32_t j = 0; j < g->ny; ++j)
+            for (int32_t i = 0; i < g->nx; ++i) {
+                const float px = (i + 0.5f) * dx - hx;
+                const float py = (j + 0.5f) * dx - hy;
+                const float r = sqrtf((px - cx) * (px - cx) + (py - cy) * (py - cy));
+                if (r > rad) continue;
+                const float t = r / rad;
+                const float q = (1.0f - t * t) * (1.0f - t * t);
+                g->value[i + (int64_t)g->nx * (j + (int64_t)g->ny * z)] += amt * q;
+            }
+    return 0;
+}
+
 int orc_world_export_deposit(orc_world* w, int32_t f, uint64_t* dst) {
     if (f < 0 || f >= AGB_FIELD_COUNT || !w->g[f].enabled) return AGB_INVALID_ARGUMENT;
     memcpy(dst, w->g[f].deposit, sizeof(uint64_t) * (size_t)w->g[f].count);

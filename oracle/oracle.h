@@ -37,6 +37,7 @@ int orc_world_export_cells(orc_world* w, agb_cells* dst, int32_t max_count, int3
 int orc_world_import_field(orc_world* w, int32_t field, const float* src);
 int orc_world_export_field(orc_world* w, int32_t field, float* dst);
 int orc_world_export_deposit(orc_world* w, int32_t field, uint64_t* dst);
+int orc_world_apply_brush(orc_world* w, int32_t kind, double x, double y, double radius, double strength);
 
 int orc_world_step(orc_world* w, int32_t ticks);
 int orc_world_stage(orc_world* w, int32_t stage);

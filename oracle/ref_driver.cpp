@@ -185,6 +185,12 @@ int ref_field_deposit(void* h, int fid, uint64_t* host) {
     return 0;
 }
 
+// world_apply_brush (src/sim/step.cu:80-89).
+int ref_apply_brush(void* h, int kind, double x, double y, double radius, double strength) {
+    return static_cast<int>(world_apply_brush(*static_cast<World*>(h), static_cast<BrushKind>(kind), x, y,
+                                              radius, strength).status);
+}
+
 void ref_step(void* h, int32_t ticks) {
     World* w = static_cast<World*>(h);
     for (int32_t t = 0; t < ticks; ++t) world_step(*w);

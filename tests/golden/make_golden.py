@@ -4,7 +4,8 @@ Builds the reference's own src/sim + src/fields sources for the host
 (oracle/build_ref.sh, serial CUDA emulation; sources read in place) and runs
 every scenario in tests/scenarios.py through its World API, recording a
 digest of every array after every stage of every tick, the final Stats, and
-for two scenarios the full state after the first tick. Run from the repo
+for three scenarios the full state after the first tick; and the fields after
+each of a list of brush strokes. Run from the repo
 root: python tests/golden/make_golden.py [reference_root]
 """
 import json
@@ -34,6 +35,11 @@ def main():
         if full is not None:
             np.savez_compressed(os.path.join(HERE, name + "_tick0.npz"), **full)
         print("golden", name, "count", rec["initial"]["count"], "->", rec["steps"][-1]["cells"]["count"])
+    w = H.RefWorld(S.brush_desc())
+    with open(os.path.join(HERE, "brushes.json"), "w") as fh:
+        json.dump({"brushes": S.brush_trace(w)}, fh, indent=0)
+    w.close()
+    print("golden brushes")
 
 
 if __name__ == "__main__":

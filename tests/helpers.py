@@ -53,6 +53,7 @@ def oracle_lib():
             "orc_world_import_field": (I32, [P, I32, P]),
             "orc_world_export_field": (I32, [P, I32, P]),
             "orc_world_export_deposit": (I32, [P, I32, P]),
+            "orc_world_apply_brush": (I32, [P, I32, C.c_double, C.c_double, C.c_double, C.c_double]),
             "orc_world_step": (I32, [P, I32]),
             "orc_world_stage": (I32, [P, I32]),
             "orc_world_diffuse": (I32, [P, I32, C.c_double]),
@@ -138,6 +139,9 @@ class OracleWorld:
         out = np.zeros(agb.field_shape(self.desc, f), dtype=np.uint64)
         self._ck(self.lib.orc_world_export_deposit(self.h, f, out.ctypes.data), "export_deposit")
         return out
+
+    def apply_brush(self, kind, x, y, radius, strength):
+        self._ck(self.lib.orc_world_apply_brush(self.h, kind, x, y, radius, strength), "apply_brush")
 
     def step(self, ticks=1, graph=False):
         self._ck(self.lib.orc_world_step(self.h, ticks), "step")
@@ -236,6 +240,7 @@ class RefWorld:
             getattr(lib, name).argtypes = None
         lib.ref_next_id.restype = C.c_uint64
         lib.ref_grid_diffuse.argtypes = [C.c_void_p, C.c_int, C.c_double]
+        lib.ref_apply_brush.argtypes = [C.c_void_p, C.c_int] + [C.c_double] * 4
         lib.ref_grid_substeps.argtypes = [C.c_void_p, C.c_int, C.c_double]
         lib.ref_cells_io.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p), C.c_int32, C.c_uint64]
         lib.ref_snapshot.restype = C.c_int64
@@ -295,6 +300,9 @@ class RefWorld:
     def import_field(self, f, arr):
         a = np.ascontiguousarray(arr, dtype=np.float32)
         self.lib.ref_field_io(self.h, f, 1, a.ctypes.data_as(C.c_void_p))
+
+    def apply_brush(self, kind, x, y, radius, strength):
+        assert self.lib.ref_apply_brush(self.h, kind, x, y, radius, strength) == 0
 
     def export_deposit(self, f):
         n = self.lib.ref_field_n(self.h, f)

@@ -183,3 +183,30 @@ def trace(world, sc, full_after=None):
     rec["accum"] = [int(v) for v in world.stats_accum()]
     rec["counters"] = [int(v) for v in world.counters()[:3]]
     return rec, full
+
+
+# Brush strokes (world_apply_brush, src/sim/step.cu:80-89) on a slab world:
+# (kind, x, y, radius, strength). A disc inside the chamber, one crossing the
+# chamber's corner, one centred outside it, a chamber-global stroke (radius ten
+# times the chamber, as the reference's scenario driver uses), a stroke smaller
+# than a voxel, and an empty one (radius 0).
+BRUSHES = [(agb.BRUSH_HEAT, 0.0, 0.0, 5.0e-4, 2.5),
+           (agb.BRUSH_CHILL, 3.0e-4, -7.0e-4, 2.0e-4, 1.25),
+           (agb.BRUSH_INJECT_CO2, 1.9e-3, 1.9e-3, 6.0e-4, 0.75),
+           (agb.BRUSH_INJECT_CO2, -2.3e-3, 1.0e-3, 5.0e-4, 0.5),
+           (agb.BRUSH_INJECT_N2, 0.0, 0.0, 8.0e-2, 0.3),
+           (agb.BRUSH_HEAT, 1.0e-4, 1.0e-4, 1.0e-5, 7.0),
+           (agb.BRUSH_CHILL, 0.0, 0.0, 0.0, 9.0)]
+
+
+def brush_desc():
+    return slab_desc(n_t=96, n_c=64, n_n=32, n_i=32, cap=16)
+
+
+def brush_trace(world):
+    """Digest of the temperature, CO2 and N2 fields after each stroke."""
+    out = []
+    for kind, x, y, r, s in BRUSHES:
+        world.apply_brush(kind, x, y, r, s)
+        out.append([digest(world.export_field(f)) for f in (agb.FIELD_T, agb.FIELD_CO2, agb.FIELD_N2)])
+    return out

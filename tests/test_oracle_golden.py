@@ -45,6 +45,23 @@ def test_oracle_matches_reference_digests(name):
         assert float(rec["stats"][k]) == v, "Stats." + k
 
 
+def test_oracle_brushes_match_reference():
+    """world_apply_brush (src/sim/step.cu:80-89): the fields after each stroke
+    carry the digests the reference's own brush kernel produced."""
+    gold = load("brushes")["brushes"]
+    w = H.OracleWorld(S.brush_desc())
+    assert S.brush_trace(w) == gold
+
+
+def test_oracle_brush_rejects_bad_strokes():
+    """Unknown kinds and non-finite strokes return InvalidArgument (status 3)."""
+    w = H.OracleWorld(S.brush_desc())
+    lib = H.oracle_lib()
+    assert lib.orc_world_apply_brush(w.h, 9, 0.0, 0.0, 1e-4, 1.0) == 3
+    assert lib.orc_world_apply_brush(w.h, agb.BRUSH_HEAT, float("nan"), 0.0, 1e-4, 1.0) == 3
+    assert lib.orc_world_apply_brush(w.h, agb.BRUSH_HEAT, 0.0, 0.0, float("inf"), 1.0) == 3
+
+
 def test_pcg32_reference_vectors():
     # pcg32_srandom_r(42, 54) then six draws: the PCG reference demo's published
     # output, which tests/physics/test_rng.cpp:16-22 also pins.
