@@ -99,8 +99,8 @@ __device__ __forceinline__ float co2_uptake_rate_f(float c) {
 __device__ __forceinline__ void co2_demand_cell(const GridDev& C2, const TickParams& p, float x, float y, float z,
                                                 unsigned long long* demand, float inv_gv) {
     const int64_t idx = grid_nearest(C2, x, y, z);
-    const float want = co2_uptake_rate_f(C2.value[idx]) * (float)p.dt_bio;
-    if (want > 0.0f) deposit_fixed(&demand[idx], to_fixed_f(want * inv_gv, (float)C2.scale));
+    const float want = co2_uptake_rate_f(C2.value[idx]) * p.dt_bio_f;
+    if (want > 0.0f) deposit_fixed(&demand[idx], to_fixed_f(want * inv_gv, C2.scale_f));
 }
 
 void launch_thermal(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, cudaStream_t s);

@@ -105,6 +105,7 @@ struct GridDev {
     double dx, dz_eff;
     double scale;
     float inv_scale_f;
+    float scale_f;       // (float)scale
 };
 
 struct HashDev {
@@ -179,6 +180,43 @@ __device__ __forceinline__ double uniform01d(Pcg& r) {
     return (double)uniform53(r) * (1.0 / 9007199254740992.0);
 }
 
+// Round-to-nearest-even conversions between 64-bit integers and float with
+// integer instructions. The hardware's 64-bit integer <-> float conversions
+// issue on the FP64 pipe, a small fraction of the FP32 rate on this part;
+// these give the same results (round to nearest, ties to even).
+__device__ __forceinline__ float u64_to_f(unsigned long long v) {
+    if (v < (1ull << 24)) return __uint2float_rn((unsigned int)v);      // exact
+    const int lz = __clzll((long long)v);
+    const unsigned long long nrm = v << lz;                              // leading one at bit 63
+    unsigned int m = (unsigned int)(nrm >> 40);                          // 24 significant bits
+    const unsigned long long rest = nrm << 24;                           // the 40 dropped bits
+    if (rest > 0x8000000000000000ull || (rest == 0x8000000000000000ull && (m & 1u))) ++m;
+    // value m * 2^(e - 23), e = 63 - lz; a carry out of m moves into the exponent
+    return __uint_as_float(((unsigned int)(63 - lz + 127) << 23) + m - 0x800000u);
+}
+__device__ __forceinline__ float ll_to_f(long long v) {
+    const float f = u64_to_f(v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v);
+    return v < 0 ? -f : f;
+}
+// float -> int64, round to nearest even (__float2ll_rn) for |v| < 2^63.
+__device__ __forceinline__ long long f_to_ll(float v) {
+    const unsigned int u = __float_as_uint(v);
+    const int ex = (int)((u >> 23) & 0xFFu);
+    if (ex >= 127 + 63) return __float2ll_rn(v);                         // out of range, inf, NaN
+    if (ex < 126) return 0;                                              // |v| < 0.5
+    const unsigned long long m = (u & 0x7FFFFFu) | 0x800000u;            // v = m * 2^(ex - 150)
+    const int sh = ex - 150;
+    unsigned long long r;
+    if (sh >= 0) {
+        r = m << sh;
+    } else {
+        const int rs = -sh;                                              // 1..24
+        const unsigned long long q = m >> rs, rem = m & ((1ull << rs) - 1ull), half = 1ull << (rs - 1);
+        r = q + ((rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull);
+    }
+    return (u >> 31) ? -(long long)r : (long long)r;
+}
+
 // Box-Muller in FP32 from the reference's 53-bit uniforms (rng.cuh:92-101).
 // ln(u1) is taken as log1p(-(1-u1)) for u1 > 1/2, with 1-u1 exact in integers,
 // so the magnitude keeps ~1e-7 relative accuracy near u1 = 1. The reference
@@ -190,14 +228,14 @@ __device__ __forceinline__ void gaussian_pair_f(Pcg& r, float& z0, float& z1) {
     float lg;
     if (b1 == 0ull) b1 = 1ull;
     if (b1 > (1ull << 52)) {
-        const float w = (float)((1ull << 53) - b1) * 1.1102230246251565e-16f;  // 1 - u1, exact bits
+        const float w = u64_to_f((1ull << 53) - b1) * 1.1102230246251565e-16f;  // 1 - u1, exact bits
         lg = log1pf(-w);
     } else {
-        lg = logf((float)b1 * 1.1102230246251565e-16f);
+        lg = logf(u64_to_f(b1) * 1.1102230246251565e-16f);
     }
     const float mag = sqrtf(-2.0f * lg);
     float s, c;
-    sincospif((float)b2 * 2.220446049250313e-16f, &s, &c);   // angle = 2*pi*u2
+    sincospif(u64_to_f(b2) * 2.220446049250313e-16f, &s, &c);   // angle = 2*pi*u2
     z0 = mag * c;
     z1 = mag * s;
 }
@@ -210,7 +248,7 @@ __device__ __forceinline__ void deposit_fixed(unsigned long long* acc, long long
 }
 // FP32 value -> fixed point (llround semantics except exact .5 ties).
 __device__ __forceinline__ long long to_fixed_f(float v, float scale) {
-    return __float2ll_rn(v * scale);
+    return f_to_ll(v * scale);
 }
 
 // ---------------------------------------------------------------------------
@@ -323,6 +361,13 @@ __device__ __forceinline__ double f2d(float v) {
 // FP64, clamped. The FP32 estimate decides unless it lies within `margin` of
 // an integer boundary, where the FP64 expression settles it.
 // ---------------------------------------------------------------------------
+// The FP64 expression, out of line so that it runs only in warps where a lane
+// needs it (inline, the compiler may evaluate it for every lane, and FP64
+// issues at a small fraction of the FP32 rate).
+static __device__ __noinline__ int32_t hash_axis_fp64(double x, float o, float inv) {
+    return (int32_t)((x - (double)o) * (double)inv);
+}
+
 __device__ __forceinline__ int32_t hash_axis(double x, float o, float inv, int32_t n, float margin) {
     float hi, lo;
     split_double(x, hi, lo);
@@ -333,7 +378,7 @@ __device__ __forceinline__ int32_t hash_axis(double x, float o, float inv, int32
         c = (int32_t)fl;                     // v > 0 here or clamps to 0 below
         if (v < 0.0f) c = -1;
     } else {
-        c = (int32_t)((x - (double)o) * (double)inv);
+        c = hash_axis_fp64(x, o, inv);
     }
     return c < 0 ? 0 : (c > n - 1 ? n - 1 : c);
 }
@@ -364,8 +409,17 @@ __device__ __forceinline__ long long to_fix64(double x, int K) {
     else X = 0;
     return (b >> 63) ? -X : X;
 }
-__device__ __forceinline__ float fix_diff_f(long long d, float inv) { return __ll2float_rn(d) * inv; }
+__device__ __forceinline__ float fix_diff_f(long long d, float inv) { return ll_to_f(d) * inv; }
 __device__ __forceinline__ double fix_diff_d(long long d, double inv) { return __dmul_rn((double)d, inv); }
+
+// column_transmittance of a stamped voxel (src/sim/emission.cuh:43-47) from
+// its fixed-point stamp: 1 - area / face, floored at 0. The same FP64
+// operations on the host and the device.
+__host__ __device__ inline double occlusion_of(long long dep, double scale, double face) {
+    const double area = (double)dep / scale;
+    const double tr = 1.0 - area / face;
+    return tr > 0.0 ? tr : 0.0;
+}
 
 // Order-preserving map of a double onto uint64: compares of finite doubles
 // become integer compares (no FP64 pipe).

@@ -167,7 +167,7 @@ __device__ __forceinline__ void thermal_kernel_body(DevState* S, const Ctx& c, c
             En = AGB_CELL_ENERGY_MAX;
         }
         v.energy[i] = En;
-        deposit_fixed(&T.deposit[idx], to_fixed_f(amount, (float)T.scale));
+        deposit_fixed(&T.deposit[idx], to_fixed_f(amount, T.scale_f));
         if (dkey(En) <= dkey(0.0)) {                     // starved
             v.flags[i] = nf & ~AGB_FLAG_ALIVE;
             v.death_cause[i] = AGB_DEATH_STARVED;
@@ -238,10 +238,18 @@ __global__ void stamp_kernel(DevState* S, Ctx c, int32_t* stamp_idx) {
     stamp_kernel_body(S, c, stamp_idx, grid_blk());
 }
 
+// The FP64 divisions, out of line: only warps with a voxel outside the
+// lookup table issue them.
+__device__ __noinline__ double occlusion_fp64(unsigned long long dep, double scale, double face) {
+    return occlusion_of((long long)dep, scale, face);
+}
+
 // column_transmittance (emission.cuh:43-47) of every stamped voxel, computed
-// once per cell in full warps (FP64 divisions in divergent sweep code would
-// cost a whole warp's FP64 issue time per stamped voxel). Duplicate cells of a
-// voxel write the same value.
+// once per cell, before the sweep (FP64 divisions in divergent sweep code
+// would cost a whole warp's FP64 issue time per stamped voxel). Voxels holding
+// one, two or three live cells or one dead cell take the factor from the
+// world's table (the same bits); others divide. Duplicate cells of a voxel
+// write the same value.
 __device__ __forceinline__ void occlusion_factor_kernel_body(DevState* S, const Ctx& c,
                                                              const int32_t* __restrict__ stamp_idx, double* factor,
                                                              Blk blk) {
@@ -250,9 +258,14 @@ __device__ __forceinline__ void occlusion_factor_kernel_body(DevState* S, const 
     AGB_FOR_CELLS_B(i, blk, n) {
         const int32_t idx = stamp_idx[i];
         if (idx < 0) continue;
-        const double area = (double)(long long)I.deposit[idx] / I.scale;   // from_fixed
-        const double tr = 1.0 - area / c.face_area;
-        factor[idx] = tr > 0.0 ? tr : 0.0;
+        const unsigned long long dep = I.deposit[idx];
+        double f;
+        if (dep == c.occl_dep[0]) f = c.occl_fac[0];
+        else if (dep == c.occl_dep[1]) f = c.occl_fac[1];
+        else if (dep == c.occl_dep[2]) f = c.occl_fac[2];
+        else if (dep == c.occl_dep[3]) f = c.occl_fac[3];
+        else f = occlusion_fp64(dep, I.scale, c.face_area);
+        factor[idx] = f;
     }
 }
 
@@ -294,7 +307,7 @@ __device__ __forceinline__ void sweep_kernel_body(const Ctx& c, const double* __
         else if (axis == 1) base = (line % nx) + (line / nx) * plane;
         else base = line;
         double t = 1.0;
-        float cur = fa(d2f((double)c.source * t), c.ambient_irr);
+        float cur = fa(d2f(c.source_d * t), c.ambient_irr);
         for (int32_t s0 = 0; s0 < len; s0 += SWEEP_PF) {
             bool raw[SWEEP_PF];
 #pragma unroll
@@ -311,7 +324,7 @@ __device__ __forceinline__ void sweep_kernel_body(const Ctx& c, const double* __
                 I.value[base + stride * step] = cur;
                 if (raw[u]) {
                     t *= __ldg(&factor[base + stride * step]);
-                    cur = fa(d2f((double)c.source * t), c.ambient_irr);
+                    cur = fa(d2f(c.source_d * t), c.ambient_irr);
                 }
             }
         }
@@ -360,7 +373,7 @@ __device__ __forceinline__ void sweep_rows_kernel_body(const Ctx& c, const doubl
     const int64_t lines = I.count / len;
     const int64_t groups = (lines + 31) / 32;
     const int64_t nwords = (I.count + 31) / 32;
-    const float entry = fa(d2f((double)c.source * 1.0), c.ambient_irr);
+    const float entry = fa(d2f(c.source_d * 1.0), c.ambient_irr);
     for (int64_t g = (int64_t)blk.x * SWEEP_ROW_WARPS + wib; g < groups; g += (int64_t)blk.n * SWEEP_ROW_WARPS) {
         const int64_t row = g * 32 + lane;
         uint8_t mark = 0;
@@ -383,7 +396,7 @@ __device__ __forceinline__ void sweep_rows_kernel_body(const Ctx& c, const doubl
                 const int j = __ffs(m) - 1;
                 const int32_t x = c.light_sign > 0 ? s0 + j : len - 1 - (s0 + j);
                 t *= __ldg(&factor[rowbase + x]);
-                buf[lane][j] = fa(d2f((double)c.source * t), c.ambient_irr);
+                buf[lane][j] = fa(d2f(c.source_d * t), c.ambient_irr);
             }
             __syncwarp();
             const int32_t s = s0 + lane;

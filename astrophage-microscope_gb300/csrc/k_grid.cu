@@ -342,7 +342,7 @@ __device__ __forceinline__ void flush_by_cells_kernel_body(DevState* S, const Gr
         if (raw != 0ull) {
             // (float)(raw / scale): FP32 scaling; identical to the reference's
             // double division except in the last bit of a ~1e-2 increment.
-            g.value[idx] = fa(g.value[idx], (float)(long long)raw * g.inv_scale_f);
+            g.value[idx] = fa(g.value[idx], ll_to_f((long long)raw) * g.inv_scale_f);
         }
         if (demand) demand[idx] = 0ull;
     }

@@ -258,9 +258,9 @@ __device__ __forceinline__ void ranges_kernel_body(DevState* S, const HashDev& h
         int32_t gx, gy, gz;
         const double px = v.x[slot], py = v.y[slot], pz = v.z[slot];
         hash_coords(h, px, py, pz, gx, gy, gz);
-        const float ox = __ll2float_rn(to_fix64(px, h.fix_k) - (h.org_fix[0] + gx * h.cell_fix)) * h.fix_inv_f;
-        const float oy = __ll2float_rn(to_fix64(py, h.fix_k) - (h.org_fix[1] + gy * h.cell_fix)) * h.fix_inv_f;
-        const float oz = __ll2float_rn(to_fix64(pz, h.fix_k) - (h.org_fix[2] + gz * h.cell_fix)) * h.fix_inv_f;
+        const float ox = ll_to_f(to_fix64(px, h.fix_k) - (h.org_fix[0] + gx * h.cell_fix)) * h.fix_inv_f;
+        const float oy = ll_to_f(to_fix64(py, h.fix_k) - (h.org_fix[1] + gy * h.cell_fix)) * h.fix_inv_f;
+        const float oz = ll_to_f(to_fix64(pz, h.fix_k) - (h.org_fix[2] + gz * h.cell_fix)) * h.fix_inv_f;
         h.rec[k] = make_float4(ox, oy, oz, __uint_as_float((uint32_t)gx | ((uint32_t)gy << 11) | ((uint32_t)gz << 22)));
     }
 }

@@ -62,14 +62,14 @@ __device__ __forceinline__ void uptake_mark_kernel_body(DevState* S, const Ctx& 
         if (demand && (f & AGB_FLAG_OCCUPIED) && (f & AGB_FLAG_ALIVE)) {
             const int64_t idx = grid_nearest(C2, d2f(v.x[i]), d2f(v.y[i]), d2f(v.z[i]));
             const float available = C2.value[idx];
-            const float want = co2_uptake_rate_f(available) * (float)p.dt_bio;
+            const float want = co2_uptake_rate_f(available) * p.dt_bio_f;
             if (want > 0.0f) {
-                const float asked = (float)(long long)demand[idx] * C2.inv_scale_f;   // from_fixed
+                const float asked = ll_to_f((long long)demand[idx]) * C2.inv_scale_f;   // from_fixed
                 float taken = want;
                 if (asked > available && asked > 0.0f) taken = want * (available / asked);
                 if (taken > 0.0f) {
                     v.co2_held[i] = v.co2_held[i] + f2d(taken);
-                    deposit_fixed(&C2.deposit[idx], to_fixed_f(-taken * inv_gv, (float)C2.scale));
+                    deposit_fixed(&C2.deposit[idx], to_fixed_f(-taken * inv_gv, C2.scale_f));
                 }
             }
         }
@@ -287,7 +287,7 @@ __device__ __forceinline__ void divide_kernel_body(DevState* S, const Ctx& c, co
         if (demand && (v.flags[i] & AGB_FLAG_OCCUPIED)) {
             const int64_t idx = grid_nearest(C2, (float)v.x[i], (float)v.y[i], (float)v.z[i]);
             const unsigned long long raw = atomicExch(&C2.deposit[idx], 0ull);
-            if (raw != 0ull) C2.value[idx] = fa(C2.value[idx], (float)(long long)raw * C2.inv_scale_f);
+            if (raw != 0ull) C2.value[idx] = fa(C2.value[idx], ll_to_f((long long)raw) * C2.inv_scale_f);
             demand[idx] = 0ull;
         }
         if (births_now <= 0 || !divflag[i]) continue;

@@ -118,6 +118,7 @@ agb_status compute_tick_params(agb_world* w) {
     p.k_contact64 = AGB_CONTACT_STIFFNESS / w->physics_rate;
     p.k_trap = (float)(w->d.trap_stiffness / w->physics_rate);
     p.dt_bio = p.dt * w->biology_rate;
+    p.dt_bio_f = (float)p.dt_bio;
     p.taxis_alpha = 1.0 - std::exp(-p.dt / AGB_TAXIS_MEMORY_TIME);     // taxis.cuh:38-41
     p.max_emit_power = w->d.max_emit_power > 0.0 ? w->d.max_emit_power : AGB_PETROVA_MAX_POWER;
     const GridDev& T = c.g[AGB_FIELD_TEMPERATURE];
@@ -167,9 +168,15 @@ void compute_light(agb_world* w) {
     const int zeros = (c.lx == 0.0f) + (c.ly == 0.0f) + (c.lz == 0.0f);
     c.light_axis_exact = zeros == 2 ? axis : -1;
     c.source = L.enabled ? L.irradiance : 0.0f;
+    c.source_d = (double)c.source;
     c.ambient_irr = L.ambient;
     const GridDev& I = c.g[AGB_FIELD_IRRADIANCE];
     c.face_area = axis == 2 ? I.dx * I.dx : I.dx * I.dz_eff;          // emission.cu:164
+    const long long deps[4] = {c.stamp_alive, 2 * c.stamp_alive, 3 * c.stamp_alive, c.stamp_dead};
+    for (int k = 0; k < 4; ++k) {
+        c.occl_dep[k] = (unsigned long long)deps[k];
+        c.occl_fac[k] = occlusion_of(deps[k], I.scale, c.face_area);
+    }
 }
 
 float* field_value(agb_world* w, int f) { return w->gbuf[f][w->gcur[f]]; }
@@ -702,6 +709,7 @@ agb_status agb_world_create(const agb_world_desc* d, agb_world** out) {
         g.hz = 0.5f * gd.nz * g.dzf;
         g.scale = gd.deposit_scale;
         g.inv_scale_f = (float)(1.0 / gd.deposit_scale);
+        g.scale_f = (float)g.scale;
         for (int k = 0; k < 6; ++k) { w->gbc[f][k] = gd.bc[k]; w->gface[f][k] = (float)gd.face_value[k]; }
         w->grobin[f] = (float)(g.dx * AGB_AIR_CONVECTION_H / AGB_WATER_CONDUCTIVITY);
         for (int b = 0; b < 2; ++b)

@@ -33,6 +33,7 @@ struct Ctx {
     int32_t light_axis, light_sign;
     int32_t light_axis_exact;  // light exactly along light_axis (other components 0), else -1
     float source, ambient_irr;
+    double source_d;           // (double)source
     // One byte per irradiance line of the sweep: 1 = a cell stamped a voxel of
     // it this tick, 2 = stamped last tick only (recompute once to clear the old
     // shadow), 0 = no stamp in either, so its values are already the
@@ -44,6 +45,12 @@ struct Ctx {
     uint32_t* irr_stamp_bits;
     double face_area;
     long long stamp_alive, stamp_dead;   // fixed-point occlusion stamps
+    // Occlusion factors of the commonest stamped voxels (one, two or three
+    // live cells, or one dead cell), computed on the host with the same FP64
+    // operations as the device, which looks these deposits up instead of
+    // dividing.
+    unsigned long long occl_dep[4];
+    double occl_fac[4];
     // Exact float thresholds equivalent to the reference's FP64 compares.
     float setpoint_up;          // smallest float >= CELL_TEMP_SETPOINT
     float setpoint_hi, setpoint_lo;
@@ -59,6 +66,7 @@ struct TickParams {
     double k_contact64;
     float k_trap;
     double dt_bio;
+    float dt_bio_f;             // (float)dt_bio
     // thermal
     int32_t t_substeps;
     double t_dt_sub;

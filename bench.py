@@ -486,11 +486,12 @@ def run_reference(args, wl):
     return 0
 
 
-def profile_batch(steps, staged=True):
-    """The 64-chamber batch after 20 warm-up steps, then `steps` steps inside an
-    NVTX range named "timed" (ncu --nvtx --nvtx-include "timed/" selects them)."""
+def profile_batch(steps, staged=True, chambers=64):
+    """The batch (64 chambers unless asked otherwise) after 20 warm-up steps,
+    then `steps` steps inside an NVTX range named "timed" (ncu --nvtx
+    --nvtx-include "timed/" selects them)."""
     import torch
-    descs, spawns, _info = batch_workload(64, seed=1)
+    descs, spawns, _info = batch_workload(chambers, seed=1)
     b = agb.Batch(descs, spawns, agb.batch_opts(autotune=True, staged=staged))
     st = torch.cuda.Stream()
     sh = st.cuda_stream
@@ -577,7 +578,7 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.profile_batch:
-        return profile_batch(args.profile_batch, staged=bool(args.batch_staged))
+        return profile_batch(args.profile_batch, staged=bool(args.batch_staged), chambers=args.batch_chambers)
     if args.profile_stencil:
         return profile_stencil(args.profile_stencil)
     if args.profile_surrogate:
