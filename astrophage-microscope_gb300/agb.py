@@ -25,6 +25,7 @@ FIELD_T, FIELD_CO2, FIELD_N2, FIELD_IRR = 0, 1, 2, 3
 BRUSH_HEAT, BRUSH_CHILL, BRUSH_INJECT_CO2, BRUSH_INJECT_N2 = 0, 1, 2, 3       # src/sim/world.cuh:33
 WALL_REFLECTING, WALL_PERIODIC, WALL_ABSORBING = 0, 1, 2
 GRAVITY_Y, GRAVITY_Z = 0, 1
+STORE_VOID, STORE_FLASH, STORE_RETAIN = 0, 1, 2
 DIVIDE_CO2_QUOTA, DIVIDE_ENERGY = 0, 1
 PLACE_UNIFORM, PLACE_GAUSSIAN, PLACE_GRID, PLACE_DISC, PLACE_SLAB_X, PLACE_CLUSTERS = range(6)
 DIST_CONSTANT, DIST_UNIFORM, DIST_NORMAL, DIST_LOGNORMAL = range(4)
@@ -48,6 +49,15 @@ HASH_CELL_FACTOR = 2.2000000000000002
 PETROVA_MAX_POWER = 0.050000000000000003
 AIR_CONVECTION_H = 10.0
 WATER_CONDUCTIVITY = 0.59799999999999998
+CHAMBER_W, CHAMBER_H, CHAMBER_D = 0.0040000000000000001, 0.0040000000000000001, 6.0000000000000002e-05
+DEFAULT_CELLS, MAX_CELLS = 25000, 2000000
+DEFAULT_TAUMOEBA, MAX_TAUMOEBA = 256, 65536
+CLOCK_PHYSICS_MIN, CLOCK_PHYSICS_MAX = 0.10000000000000001, 100.0
+CLOCK_BIOLOGY_MIN, CLOCK_BIOLOGY_MAX = 1.0, 1000000.0
+CLOCK_REALTIME_PHYSICS, CLOCK_REALTIME_BIOLOGY = 1.0, 1.0
+CLOCK_MOTION_PHYSICS, CLOCK_MOTION_BIOLOGY = 10.0, 1.0
+CLOCK_METABOLIC_PHYSICS, CLOCK_METABOLIC_BIOLOGY = 1.0, 10000.0
+CLOCK_GENERATIONAL_PHYSICS, CLOCK_GENERATIONAL_BIOLOGY = 0.5, 1000000.0
 
 
 class GridDesc(C.Structure):
@@ -271,6 +281,7 @@ def load(path=LIB_PATH):
         "agb_world_create": (I32, [C.POINTER(WorldDesc), C.POINTER(P)]),
         "agb_world_destroy": (None, [P]),
         "agb_world_spawn": (I32, [P, C.POINTER(Spawn), P]),
+        "agb_world_spawn_seeded": (I32, [P, C.POINTER(Spawn), U64, P]),
         "agb_world_import_cells": (I32, [P, C.POINTER(Cells), I32, U64, P]),
         "agb_world_export_cells": (I32, [P, C.POINTER(Cells), I32, C.POINTER(I32), C.POINTER(U64), P]),
         "agb_world_device_cells": (I32, [P, C.POINTER(Cells)]),
@@ -340,7 +351,7 @@ def load(path=LIB_PATH):
 def exported_symbols():
     """Names declared in include/agb.h, for the symbol-export test."""
     return ["agb_world_desc_default", "agb_status_str", "agb_last_error", "agb_device_info",
-            "agb_world_create", "agb_world_destroy", "agb_world_spawn", "agb_world_import_cells",
+            "agb_world_create", "agb_world_destroy", "agb_world_spawn", "agb_world_spawn_seeded", "agb_world_import_cells",
             "agb_world_export_cells", "agb_world_device_cells", "agb_world_step_host", "agb_world_count",
             "agb_world_import_field", "agb_world_export_field", "agb_world_export_deposit",
             "agb_world_apply_brush",
@@ -400,8 +411,16 @@ class World:
         except Exception:
             pass
 
-    def spawn(self, p, stream=None):
-        self._check(self.lib.agb_world_spawn(self.h, C.byref(p), _st(stream)), "spawn")
+    def spawn(self, p, stream=None, seed=None):
+        """cell_store_spawn: `seed` defaults to the world's seed."""
+        if seed is None:
+            self._check(self.lib.agb_world_spawn(self.h, C.byref(p), _st(stream)), "spawn")
+        else:
+            self._check(self.lib.agb_world_spawn_seeded(self.h, C.byref(p), seed, _st(stream)), "spawn")
+
+    def set_light(self, light):
+        """Replace the primary light source (dir, irradiance, ambient, enabled)."""
+        self._check(self.lib.agb_world_set_light(self.h, C.byref(light)), "set_light")
 
     def import_cells(self, cells, next_id, stream=None):
         s = cells.struct()

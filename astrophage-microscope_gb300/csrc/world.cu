@@ -820,7 +820,7 @@ agb_status agb_world_create(const agb_world_desc* d, agb_world** out) {
     return AGB_OK;
 }
 
-agb_status agb_world_spawn(agb_world* w, const agb_spawn* p, agb_stream s) {
+agb_status agb_world_spawn_seeded(agb_world* w, const agb_spawn* p, uint64_t seed, agb_stream s) {
     if (!w || !p) return AGB_INVALID_ARGUMENT;
     if (p->count <= 0) return AGB_OK;
     if (p->placement == AGB_PLACE_CLUSTERS && p->clusters <= 0) return fail(w, AGB_INVALID_ARGUMENT, "clusters");
@@ -828,9 +828,16 @@ agb_status agb_world_spawn(agb_world* w, const agb_spawn* p, agb_stream s) {
     agb_status rc = read_state(w, st, s);
     if (rc) return rc;
     if (st.count + p->count > w->c.capacity) return fail(w, AGB_CAPACITY_EXCEEDED, "spawn exceeds capacity");
-    launch_spawn(w->S, w->c, *p, w->blocks, s);
+    Ctx c = w->c;
+    c.seed = seed;
+    launch_spawn(w->S, c, *p, w->blocks, s);
     AGB_CUDA(w, cudaGetLastError());
     return AGB_OK;
+}
+
+agb_status agb_world_spawn(agb_world* w, const agb_spawn* p, agb_stream s) {
+    if (!w) return AGB_INVALID_ARGUMENT;
+    return agb_world_spawn_seeded(w, p, w->c.seed, s);
 }
 
 agb_status agb_world_count(agb_world* w, int32_t* count, agb_stream s) {

@@ -321,6 +321,10 @@ void agb_world_destroy(agb_world* w);
 
 /* cell_store_spawn (src/sim/cell_store.cuh:73): appends p->count seeded cells. */
 agb_status agb_world_spawn(agb_world* w, const agb_spawn* p, agb_stream s);
+/* The same with the spawn seed given (cell_store_spawn's `seed` argument; the call
+ * above passes the world's seed): the scenario loader seeds population i with
+ * seed + i and a top-up with seed + tick (src/sim/scenario.cpp:368-385, 436-452). */
+agb_status agb_world_spawn_seeded(agb_world* w, const agb_spawn* p, uint64_t seed, agb_stream s);
 
 /* Replace the whole population with `count` cells in contract layout; next_id
  * is the id the next daughter gets (CellStore::next_id). */

@@ -532,7 +532,8 @@ static vec3 cluster_centre(uint64_t seed, int32_t k, double extent) {
     return v3(x, y, z);
 }
 
-int orc_world_spawn(orc_world* w, const agb_spawn* p) {
+/* cell_store_spawn (src/sim/cell_store.cu:42-130, 250-280) with its seed argument. */
+int orc_world_spawn_seeded(orc_world* w, const agb_spawn* p, uint64_t seed) {
     if (p->count <= 0) return 0;
     if (w->count + p->count > w->capacity) return AGB_CAPACITY_EXCEEDED;   /* cell_store.cu:264-265 */
     if (p->placement == AGB_PLACE_CLUSTERS && p->clusters <= 0) return AGB_INVALID_ARGUMENT;
@@ -542,7 +543,7 @@ int orc_world_spawn(orc_world* w, const agb_spawn* p) {
     for (int32_t i = 0; i < p->count; ++i) {
         const int32_t slot = w->count + i;
         const uint64_t id = w->next_id + (uint64_t)i;
-        const uint64_t state = cell_rng_init(w->d.seed, id);
+        const uint64_t state = cell_rng_init(seed, id);
         pcg32 r = cell_rng(state, id);
         double x = 0.0, y = 0.0, z = 0.0;
         int z_done = 0;
@@ -575,7 +576,7 @@ int orc_world_spawn(orc_world* w, const agb_spawn* p) {
             case AGB_PLACE_CLUSTERS: {
                 int32_t k = (int32_t)(uniform01d(&r) * (double)p->clusters);
                 if (k >= p->clusters) k = p->clusters - 1;
-                const vec3 c0 = cluster_centre(w->d.seed, k, p->cluster_extent);
+                const vec3 c0 = cluster_centre(seed, k, p->cluster_extent);
                 double gx, gy, gz, gw;
                 gaussian_pair(&r, &gx, &gy);
                 gaussian_pair(&r, &gz, &gw);
@@ -621,6 +622,14 @@ int orc_world_spawn(orc_world* w, const agb_spawn* p) {
     }
     w->count += p->count;
     w->next_id += (uint64_t)p->count;
+    return 0;
+}
+
+int orc_world_spawn(orc_world* w, const agb_spawn* p) { return orc_world_spawn_seeded(w, p, w->d.seed); }
+
+/* The primary light source, replaced between ticks (the emission stage reads it). */
+int orc_world_set_light(orc_world* w, const agb_light* light) {
+    w->d.light = *light;
     return 0;
 }
 

@@ -12,6 +12,8 @@
 #include "contracts/cell_store_v1.h"
 #include "contracts/telemetry_v1.h"
 #include "fields/grid.cuh"
+#include "sim/accept.h"
+#include "sim/scenario.h"
 #include "sim/snapshot.h"
 #include "sim/world.cuh"
 
@@ -291,6 +293,38 @@ uint64_t ref_state_hash(void* h) {
     uint64_t x = 0;
     if (snapshot_state_hash(*static_cast<World*>(h), x)) return 0;
     return x;
+}
+
+// A scenario (the text of a scenarios/*.json file) through the reference's own
+// loader and driver (src/sim/scenario.cpp) and accept evaluation
+// (src/sim/accept.cpp): instantiate, then `ticks` ticks as the headless
+// runner's --assert loop takes them (tools/headless.cpp:197-233: drive, step,
+// Stats and aggregates every `stride` ticks, final Stats), then one measured
+// value per accept check. Returns the World (for the other ref_* readers; free
+// it with ref_world_destroy) or null when the scenario does not parse or build.
+void* ref_scenario_run(const char* text, int64_t ticks, double* measured, int32_t* n_checks) {
+    static contract::Scenario sc;
+    if (scenario_parse(std::string(text), sc)) return nullptr;
+    World* w = new (std::nothrow) World{};
+    if (!w) return nullptr;
+    if (scenario_instantiate(sc, *w)) { delete w; return nullptr; }
+    const int64_t stride = ticks > 2000 ? ticks / 2000 : 1;
+    const MetricNeeds needs = metric_needs(sc);
+    RunAggregates agg;
+    contract::Stats st{};
+    for (int64_t t = 0; t < ticks; ++t) {
+        scenario_apply_drive(*w, sc);
+        world_step(*w);
+        if (t % stride == 0) {
+            st = world_stats(*w);
+            aggregates_sample(agg, st, *w, needs, 2.0, 4.0);
+        }
+    }
+    st = world_stats(*w);
+    aggregates_sample(agg, st, *w, needs, 2.0, 4.0);
+    for (int i = 0; i < sc.accept_count; ++i) measured[i] = metric_measure(sc.accept[i].metric, st, agg, *w, sc);
+    *n_checks = sc.accept_count;
+    return w;
 }
 
 }  // extern "C"

@@ -7,6 +7,7 @@ import ctypes as C
 import importlib.util
 import os
 import subprocess
+import sys
 
 import numpy as np
 
@@ -17,14 +18,27 @@ REF_SO = os.path.join(ROOT, "oracle", "_ref", "libastro_ref.so")
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 
 
-def load_agb():
-    spec = importlib.util.spec_from_file_location("agb", os.path.join(PKG, "agb.py"))
+def _load(name):
+    """A module of the package, registered so that its own imports (scenario.py
+    imports agb) resolve to the same module objects."""
+    if name in sys.modules:
+        return sys.modules[name]
+    spec = importlib.util.spec_from_file_location(name, os.path.join(PKG, name + ".py"))
     mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
     spec.loader.exec_module(mod)
     return mod
 
 
+def load_agb():
+    return _load("agb")
+
+
 agb = load_agb()
+
+
+def load_scenario():
+    return _load("scenario")
 
 
 def build_oracle():
@@ -48,6 +62,8 @@ def oracle_lib():
             "orc_world_destroy": (None, [P]),
             "orc_set_threads": (None, [C.c_int]),
             "orc_world_spawn": (I32, [P, C.POINTER(agb.Spawn)]),
+            "orc_world_spawn_seeded": (I32, [P, C.POINTER(agb.Spawn), U64]),
+            "orc_world_set_light": (I32, [P, C.POINTER(agb.Light)]),
             "orc_world_import_cells": (I32, [P, C.POINTER(agb.Cells), I32, U64]),
             "orc_world_export_cells": (I32, [P, C.POINTER(agb.Cells), I32, C.POINTER(I32), C.POINTER(U64)]),
             "orc_world_import_field": (I32, [P, I32, P]),
@@ -105,8 +121,14 @@ class OracleWorld:
         except Exception:
             pass
 
-    def spawn(self, p):
-        self._ck(self.lib.orc_world_spawn(self.h, C.byref(p)), "spawn")
+    def spawn(self, p, seed=None):
+        if seed is None:
+            self._ck(self.lib.orc_world_spawn(self.h, C.byref(p)), "spawn")
+        else:
+            self._ck(self.lib.orc_world_spawn_seeded(self.h, C.byref(p), seed), "spawn")
+
+    def set_light(self, light):
+        self._ck(self.lib.orc_world_set_light(self.h, C.byref(light)), "set_light")
 
     def import_cells(self, cells, next_id):
         s = cells.struct()
@@ -224,12 +246,13 @@ def ref_available():
     return os.path.exists(REF_SO)
 
 
-class RefWorld:
-    """The reference's own World (src/sim/world.cuh) run on the CPU, driven from
-    an agb.WorldDesc restricted to what the reference can express (nz = 1, one
-    BC per field, in-plane light)."""
+_ref = None
 
-    def __init__(self, desc):
+
+def ref_lib():
+    """The reference built for the CPU (oracle/_ref/libastro_ref.so), loaded once."""
+    global _ref
+    if _ref is None:
         lib = C.CDLL(REF_SO)
         lib.ref_world_create.restype = C.c_void_p
         lib.ref_world_create.argtypes = [C.POINTER(RefParams)]
@@ -247,6 +270,19 @@ class RefWorld:
         lib.ref_snapshot.argtypes = [C.c_void_p, C.c_char_p, C.c_void_p, C.c_int64]
         lib.ref_state_hash.restype = C.c_uint64
         lib.ref_state_hash.argtypes = [C.c_void_p]
+        lib.ref_scenario_run.restype = C.c_void_p
+        lib.ref_scenario_run.argtypes = [C.c_char_p, C.c_int64, C.c_void_p, C.POINTER(C.c_int32)]
+        _ref = lib
+    return _ref
+
+
+class RefWorld:
+    """The reference's own World (src/sim/world.cuh) run on the CPU, driven from
+    an agb.WorldDesc restricted to what the reference can express (nz = 1, one
+    BC per field, in-plane light)."""
+
+    def __init__(self, desc):
+        lib = ref_lib()
         self.lib = lib
         self.desc = desc
         g = desc.grid
@@ -265,6 +301,22 @@ class RefWorld:
         self.h = C.c_void_p(lib.ref_world_create(C.byref(p)))
         if not self.h:
             raise RuntimeError("ref_world_create failed")
+
+    @classmethod
+    def from_scenario(cls, text, ticks, desc):
+        """ref_scenario_run: the reference's scenario loader, driver and accept
+        evaluation over `ticks` ticks. Returns (world, measured values); `desc` is
+        the agb.WorldDesc the scenario builds (for field shapes)."""
+        lib = ref_lib()
+        out = np.zeros(16, np.float64)
+        n = C.c_int32(0)
+        h = lib.ref_scenario_run(text.encode() if isinstance(text, str) else text, ticks,
+                                 out.ctypes.data, C.byref(n))
+        if not h:
+            raise RuntimeError("ref_scenario_run failed")
+        w = cls.__new__(cls)
+        w.lib, w.desc, w.h = lib, desc, C.c_void_p(h)
+        return w, list(out[:n.value])
 
     def close(self):
         if self.h:

@@ -1,0 +1,116 @@
+"""The scenario spine on the GPU: each of the reference's scenarios the engine
+supports, and this suite's driven scenario, run through the spine on the
+engine and on the oracle from the same scenario text. Integer cell state and
+counts must stay equal tick for tick; fields, Stats and the measured accept
+values within the floating-point tolerance."""
+import glob
+import json
+import os
+
+import numpy as np
+import pytest
+
+import helpers as H
+import parity as P
+import test_scenario as TS
+
+agb = H.agb
+S = H.load_scenario()
+pytestmark = pytest.mark.gpu
+
+SUPPORTED = ["first-light", "three-percent-line", "bloom", "komorov", "shadow-garden", "demo-herd", "sandbox"]
+HAVE = {os.path.basename(p)[:-5] for p in glob.glob(os.path.join(TS.SCEN_DIR, "*.json"))}
+MEASURE_RTOL = 1e-4        # correlations and fits over FP32-computed positions
+
+
+def run_both(text, ticks):
+    s = S.parse(text)
+    gpu = S.instantiate(s)
+    orc = S.instantiate(s, make_world=H.OracleWorld)
+    for dw in (gpu, orc):
+        for _ in range(ticks):
+            S.apply_drive(dw)
+            dw.step()
+    return s, gpu, orc
+
+
+def assert_tracks(s, gpu, orc, where):
+    a, na = gpu.world.export_cells()
+    b, nb = orc.world.export_cells()
+    assert a.n == b.n and na == nb, where
+    for k in P.INT_FIELDS:
+        assert np.array_equal(a[k], b[k]), "%s: %s" % (where, k)
+    errs = P.compare_fields(gpu.world, orc.world, where=where)
+    assert not errs, "\n".join(errs[:10])
+    sg, so = gpu.world.stats(), orc.world.stats()
+    for k in ("tick", "n_live", "n_dead", "n_awake", "n_dormant", "divisions_this_window", "deaths_this_window",
+              "boil_events", "ignitions_this_window"):
+        assert getattr(sg, k) == getattr(so, k), "%s: Stats.%s" % (where, k)
+    for k in ("sim_time_s", "mean_charge", "total_energy_j", "mean_temp_medium_k", "max_temp_medium_k"):
+        x, y = getattr(sg, k), getattr(so, k)
+        assert abs(x - y) <= 1e-6 * abs(y) + 1e-9, "%s: Stats.%s %r vs %r" % (where, k, x, y)
+
+
+@pytest.mark.parametrize("sid", SUPPORTED)
+def test_reference_scenario_tracks_oracle(sid):
+    if sid not in HAVE:
+        pytest.skip("reference scenario files not present")
+    s, gpu, orc = run_both(TS.text_of(sid), 30)
+    assert_tracks(s, gpu, orc, sid)
+
+
+def test_driven_scenario_tracks_oracle():
+    s, gpu, orc = run_both(json.dumps(TS.DRIVEN), 45)
+    assert gpu.world.count() == 1000
+    assert_tracks(s, gpu, orc, "driven")
+
+
+def test_measured_accept_values_agree():
+    text = json.dumps(TS.DRIVEN)
+    s = S.parse(text)
+    res = []
+    for make in (None, H.OracleWorld):
+        dw = S.instantiate(s, make_world=make)
+        ok, r = S.run_assert(s, dw, ticks=45, graph=make is None)
+        res.append((ok, r))
+    (ok_g, rg), (ok_o, ro) = res
+    assert ok_g == ok_o
+    for (m, vg, pg), (_m, vo, po) in zip(rg, ro):
+        assert pg == po, m
+        assert abs(vg - vo) <= MEASURE_RTOL * abs(vo) + 1e-6, (m, vg, vo)
+
+
+def test_unsupported_scenarios_refuse():
+    for sid in ("taumoeba", "spin-drive-face"):
+        if sid not in HAVE:
+            continue
+        with pytest.raises(S.ScenarioUnsupported):
+            S.instantiate(S.parse(TS.text_of(sid)))
+
+
+@pytest.mark.parametrize("sid", ["shadow-garden", "komorov", "bloom", "three-percent-line", "first-light"])
+def test_reference_scenario_accepts(sid):
+    """`--scenario ID --assert` at the scenario's own horizon (300 to 60,000
+    ticks): the reference's acceptance gate, run on the engine, accepts."""
+    if sid not in HAVE:
+        pytest.skip("reference scenario files not present")
+    s = S.parse(TS.text_of(sid))
+    ok, res = S.run_assert(s, S.instantiate(s))
+    assert ok, res
+    assert len(res) == len(s.accept)
+
+
+def test_headless_entry_point():
+    """scenario.py's command line: ACCEPT exits 0, an unsupported scenario 3."""
+    import subprocess
+    import sys
+    if "komorov" not in HAVE or "taumoeba" not in HAVE:
+        pytest.skip("reference scenario files not present")
+    script = os.path.join(H.PKG, "scenario.py")
+    r = subprocess.run([sys.executable, script, "--scenario", "komorov", "--scenarios-dir", TS.SCEN_DIR, "--assert"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "scenario komorov: ACCEPT" in r.stdout
+    r = subprocess.run([sys.executable, script, "--scenario", os.path.join(TS.SCEN_DIR, "taumoeba.json"), "--assert"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 3 and "unsupported" in r.stdout
