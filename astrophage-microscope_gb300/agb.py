@@ -30,7 +30,7 @@ DIVIDE_CO2_QUOTA, DIVIDE_ENERGY = 0, 1
 PLACE_UNIFORM, PLACE_GAUSSIAN, PLACE_GRID, PLACE_DISC, PLACE_SLAB_X, PLACE_CLUSTERS = range(6)
 DIST_CONSTANT, DIST_UNIFORM, DIST_NORMAL, DIST_LOGNORMAL = range(4)
 STAGE_HASH, STAGE_THERMAL, STAGE_EMISSION, STAGE_TAXIS, STAGE_MOTION = 0, 1, 2, 3, 4
-STAGE_SLOW_FIELDS, STAGE_LIFECYCLE, STAGE_COMPACT, STAGE_CLOCK = 5, 6, 7, 8
+STAGE_SLOW_FIELDS, STAGE_LIFECYCLE, STAGE_COMPACT, STAGE_CLOCK, STAGE_FLASH = 5, 6, 7, 8, 9
 FLAG_OCCUPIED, FLAG_ALIVE, FLAG_AWAKE, FLAG_STUCK = 1, 2, 4, 8
 
 # Canon values the Python side needs (include/agb_canon.h).
@@ -49,6 +49,8 @@ HASH_CELL_FACTOR = 2.2000000000000002
 PETROVA_MAX_POWER = 0.050000000000000003
 AIR_CONVECTION_H = 10.0
 WATER_CONDUCTIVITY = 0.59799999999999998
+C_LIGHT = 299792458.0
+PETROVA_FLASH_POWER = 3000000.0
 CHAMBER_W, CHAMBER_H, CHAMBER_D = 0.0040000000000000001, 0.0040000000000000001, 6.0000000000000002e-05
 DEFAULT_CELLS, MAX_CELLS = 25000, 2000000
 DEFAULT_TAUMOEBA, MAX_TAUMOEBA = 256, 65536
@@ -292,6 +294,8 @@ def load(path=LIB_PATH):
         "agb_world_export_field": (I32, [P, I32, P, P]),
         "agb_world_export_deposit": (I32, [P, I32, P, P]),
         "agb_world_apply_brush": (I32, [P, I32, C.c_double, C.c_double, C.c_double, C.c_double, P]),
+        "agb_world_set_flash": (I32, [P, I32, C.c_double]),
+        "agb_world_flash_audit": (I32, [P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
         "agb_world_step": (I32, [P, I32, P]),
         "agb_world_step_graph": (I32, [P, I32, P]),
         "agb_world_stage": (I32, [P, I32, P]),
@@ -354,7 +358,7 @@ def exported_symbols():
             "agb_world_create", "agb_world_destroy", "agb_world_spawn", "agb_world_spawn_seeded", "agb_world_import_cells",
             "agb_world_export_cells", "agb_world_device_cells", "agb_world_step_host", "agb_world_count",
             "agb_world_import_field", "agb_world_export_field", "agb_world_export_deposit",
-            "agb_world_apply_brush",
+            "agb_world_apply_brush", "agb_world_set_flash", "agb_world_flash_audit",
             "agb_world_step", "agb_world_step_graph", "agb_world_graph_kernels", "agb_world_set_walk",
             "agb_world_walk", "agb_world_stage",
             "agb_world_diffuse",
@@ -417,6 +421,16 @@ class World:
             self._check(self.lib.agb_world_spawn(self.h, C.byref(p), _st(stream)), "spawn")
         else:
             self._check(self.lib.agb_world_spawn_seeded(self.h, C.byref(p), seed, _st(stream)), "spawn")
+
+    def set_flash(self, active, power=0.0):
+        """Arm (or disarm) the spin-drive flash; power <= 0 is the canon rate."""
+        self._check(self.lib.agb_world_set_flash(self.h, int(bool(active)), power), "set_flash")
+
+    def flash_audit(self):
+        """(delivered impulse [N s], discharged store [J]) since creation."""
+        i, e = C.c_double(), C.c_double()
+        self._check(self.lib.agb_world_flash_audit(self.h, C.byref(i), C.byref(e)), "flash_audit")
+        return i.value, e.value
 
     def set_light(self, light):
         """Replace the primary light source (dir, irradiance, ambient, enabled)."""

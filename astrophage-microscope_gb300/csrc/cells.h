@@ -104,6 +104,8 @@ __device__ __forceinline__ void co2_demand_cell(const GridDev& C2, const TickPar
 }
 
 void launch_thermal(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, cudaStream_t s);
+// flash_step (src/sim/flash.cu:59-67) while the spin-drive flash is armed.
+void launch_flash(DevState* S, double dt, double power, unsigned long long* accum, int32_t blocks, cudaStream_t s);
 // `lanes` (1, 2, 4 or 8) threads share each cell's neighbour walk in the
 // feeding and contact-force kernels; `blocks` sizes one thread per cell.
 void launch_emission(DevState* S, const Ctx& c, const TickParams& p, int32_t* stamp_idx, double* factor,

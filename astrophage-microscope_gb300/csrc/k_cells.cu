@@ -905,6 +905,45 @@ __device__ __forceinline__ void taxis_cell(const SoA& v, const TickParams& p, in
     v.energy[i] = __dsub_rn(energy, __dmul_rn(pw, p.dt));
 }
 
+// flash_kernel (src/sim/flash.cu:31-56): every awake live cell discharges
+// power * dt of its store (no more than it holds), with no free-cell thrust;
+// the photon impulse (along -z) and the discharged energy go to the audit in
+// fixed point, summed per warp first (integer sums: any order gives the same
+// words).
+__global__ void __launch_bounds__(256) flash_kernel(DevState* S, double dt, double power,
+                                                    unsigned long long* accum) {
+    pdl_wait();
+    const SoA v = S->cur;
+    const int32_t n = S->count;
+    const double de0 = __dmul_rn(power, dt);
+    for (int32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const int32_t i = base + threadIdx.x;
+        long long imp_q = 0, e_q = 0;
+        if (i < n) {
+            const uint32_t f = v.flags[i];
+            if ((f & AGB_FLAG_OCCUPIED) && (f & AGB_FLAG_ALIVE) && (f & AGB_FLAG_AWAKE)) {
+                const double e = v.energy[i];
+                v.emit_power[i] = 0.0f;
+                if (!(e <= 0.0)) {
+                    const double de = de0 > e ? e : de0;
+                    v.energy[i] = __dsub_rn(e, de);
+                    const double imp = __ddiv_rn(de, AGB_C_LIGHT);
+                    imp_q = llround(__dmul_rn(-imp, AGB_FLASH_IMPULSE_SCALE));
+                    e_q = llround(__dmul_rn(de, AGB_FLASH_ENERGY_SCALE));
+                }
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            imp_q += __shfl_down_sync(0xFFFFFFFFu, imp_q, o);
+            e_q += __shfl_down_sync(0xFFFFFFFFu, e_q, o);
+        }
+        if ((threadIdx.x & 31) == 0 && (imp_q | e_q)) {
+            atomicAdd(&accum[2], (unsigned long long)imp_q);
+            atomicAdd(&accum[3], (unsigned long long)e_q);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(256) taxis_kernel(DevState* S, Ctx c, TickParams p) {
     pdl_wait();
     const SoA v = S->cur;
@@ -1041,6 +1080,10 @@ bool launch_batched_cells(BStage st, const ChamberArgs* tab, const uint32_t* map
         case BStage::Integrate: launch_k(integrate_batch, g, 256, 0, s, tab, map); return true;
         default: return false;
     }
+}
+
+void launch_flash(DevState* S, double dt, double power, unsigned long long* accum, int32_t blocks, cudaStream_t s) {
+    launch_k(flash_kernel, blocks, 256, 0, s, S, dt, power, accum);
 }
 
 void launch_taxis(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, cudaStream_t s) {

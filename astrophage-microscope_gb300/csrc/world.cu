@@ -248,6 +248,12 @@ void stage_slow_fields(agb_world* w, cudaStream_t s) {
         for (int32_t k = 0; k < w->tp.n_substeps; ++k) ftcs(w, AGB_FIELD_N2, w->tp.n_coeff, s);
 }
 
+// Stage 9b or 3: the flash when armed, else taxis when enabled (step.cu:158-162).
+void stage_flash_or_taxis(agb_world* w, cudaStream_t s) {
+    if (w->flash_active) launch_flash(w->S, w->tp.dt, w->flash_power, w->flash_accum, w->blocks, s);
+    else if (w->d.taxis_enabled) launch_taxis(w->S, w->c, w->tp, w->blocks, s);
+}
+
 bool compaction_allowed(const agb_world* w) {
     const int32_t P = w->d.compaction_period > 0 ? w->d.compaction_period : 1;
     return w->d.compaction_enabled && ((w->tick + 1) % (uint64_t)P) == 0;
@@ -319,12 +325,14 @@ void tick_once(agb_world* w, cudaStream_t s) {
     // or the three passes in turn. Feeding reads only the irradiance grid.
     Ctx c = w->c;
     for (int f : {AGB_FIELD_CO2, AGB_FIELD_N2}) c.g[f] = pre.g[f];
-    if (w->fuse_cells) {
+    // While the spin-drive flash is armed it replaces taxis (step.cu:158-162);
+    // those ticks take the three passes in turn.
+    if (w->fuse_cells && !w->flash_active) {
         launch_cell_step(w->S, c, w->tp, w->fx, w->fy, w->fz, w->blocks, w->walk_lanes, emit,
                          w->d.taxis_enabled != 0, s);
     } else {
         if (emit) launch_feed(w->S, w->c, w->tp, w->blocks, w->walk_lanes, s);
-        if (w->d.taxis_enabled) launch_taxis(w->S, w->c, w->tp, w->blocks, s);
+        stage_flash_or_taxis(w, s);
         launch_forces(w->S, c, w->tp, w->fx, w->fy, w->fz, w->blocks, w->walk_lanes, s);
     }
     cudaStreamWaitEvent(s, w->ev[2], 0);
@@ -351,7 +359,7 @@ void tick_surrogate(agb_world* w, cudaStream_t s) {
     if (w->d.thermal_enabled && w->c.g[AGB_FIELD_TEMPERATURE].enabled)
         for (int32_t k = 0; k < w->tp.t_substeps; ++k) launch_thermal(w->S, w->c, w->tp, w->blocks, s);
     if (w->d.emission_enabled) stage_emission(w, s);
-    if (w->d.taxis_enabled) launch_taxis(w->S, w->c, w->tp, w->blocks, s);
+    stage_flash_or_taxis(w, s);
     launch_motion(w->S, w->c, w->tp, w->fx, w->fy, w->fz, w->blocks, w->walk_lanes, s);
     stage_lifecycle(w, s);
     stage_clock(w);
@@ -791,7 +799,9 @@ agb_status agb_world_create(const agb_world_desc* d, agb_world** out) {
     for (cudaEvent_t& e : w->ev) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
     const int64_t co2n = c.g[AGB_FIELD_CO2].enabled ? c.g[AGB_FIELD_CO2].count : 1;
     ok = ok && dalloc(w, &w->life.co2_demand, 8 * (size_t)co2n) == cudaSuccess;
+    ok = ok && dalloc(w, &w->flash_accum, 8 * 4) == cudaSuccess;
     if (!ok) { agb_world_destroy(w); return AGB_OUT_OF_MEMORY; }
+    cudaMemset(w->flash_accum, 0, 8 * 4);                 // zeroed once (src/sim/step.cu:58-64)
     if (c.irr_marks) cudaMemset(c.irr_marks, 2, (size_t)w->irr_mark_bytes);   // first sweep: every line
     if (c.irr_stamp_bits) cudaMemset(c.irr_stamp_bits, 0, 4 * (size_t)w->irr_bit_words);
     cudaMemset(h.ranges, 0, 8 * (size_t)h.buckets);
@@ -968,6 +978,31 @@ agb_status agb_world_export_deposit(agb_world* w, int32_t f, uint64_t* dst, agb_
     return AGB_OK;
 }
 
+agb_status agb_world_set_flash(agb_world* w, int32_t active, double power) {
+    if (!w || !std::isfinite(power)) return AGB_INVALID_ARGUMENT;
+    const bool on = active != 0;
+    const double pw = power > 0.0 ? power : AGB_PETROVA_FLASH_POWER;
+    if (on != w->flash_active || pw != w->flash_power) {
+        w->flash_active = on;
+        w->flash_power = pw;
+        invalidate_graphs(w);                             // captured ticks baked the old stage
+    }
+    return AGB_OK;
+}
+
+agb_status agb_world_flash_audit(agb_world* w, double* impulse_ns, double* discharged_j) {
+    if (!w || !impulse_ns || !discharged_j) return AGB_INVALID_ARGUMENT;
+    unsigned long long raw[4];
+    AGB_CUDA(w, cudaDeviceSynchronize());
+    AGB_CUDA(w, cudaMemcpy(raw, w->flash_accum, sizeof(raw), cudaMemcpyDeviceToHost));
+    const double ix = (double)(long long)raw[0] / AGB_FLASH_IMPULSE_SCALE;
+    const double iy = (double)(long long)raw[1] / AGB_FLASH_IMPULSE_SCALE;
+    const double iz = (double)(long long)raw[2] / AGB_FLASH_IMPULSE_SCALE;
+    *impulse_ns = std::sqrt(ix * ix + iy * iy + iz * iz);
+    *discharged_j = (double)(long long)raw[3] / AGB_FLASH_ENERGY_SCALE;
+    return AGB_OK;
+}
+
 agb_status agb_world_apply_brush(agb_world* w, int32_t kind, double x, double y, double radius,
                                  double strength, agb_stream s) {
     if (!w) return AGB_INVALID_ARGUMENT;
@@ -1126,6 +1161,9 @@ agb_status agb_world_stage(agb_world* w, int32_t stage, agb_stream s) {
         case AGB_STAGE_THERMAL: stage_thermal(w, s); break;
         case AGB_STAGE_EMISSION: stage_emission(w, s); break;
         case AGB_STAGE_TAXIS: launch_taxis(w->S, w->c, w->tp, w->blocks, s); break;
+        case AGB_STAGE_FLASH:
+            if (w->flash_active) launch_flash(w->S, w->tp.dt, w->flash_power, w->flash_accum, w->blocks, s);
+            break;
         case AGB_STAGE_MOTION: stage_motion(w, s); break;
         case AGB_STAGE_SLOW_FIELDS: stage_slow_fields(w, s); break;
         case AGB_STAGE_LIFECYCLE: stage_lifecycle(w, s); break;

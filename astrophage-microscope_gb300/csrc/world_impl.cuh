@@ -50,6 +50,9 @@ struct agb_world {
     int32_t blocks = 1;
     int walk_lanes = 1;                  // threads sharing one cell's neighbour walk (1, 2, 4, 8)
     bool fuse_cells = false;             // feeding, taxis and forces in one kernel with one walk
+    bool flash_active = false;           // spin-drive flash armed: the flash stage replaces taxis
+    double flash_power = AGB_PETROVA_FLASH_POWER;
+    unsigned long long* flash_accum = nullptr;   // imp_x, imp_y, imp_z, energy (fixed point)
     int64_t irr_mark_bytes = 0;          // size of c.irr_marks (irradiance lines over any light axis)
     int64_t irr_bit_words = 0;           // size of c.irr_stamp_bits in 32-bit words
     uint64_t tick = 0;

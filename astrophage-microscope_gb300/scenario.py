@@ -12,15 +12,14 @@ documented defaults; scope, tools, param_overrides, density_model and
 thermal_bc are parsed and not applied, as there.
 
 The world is duck-typed: anything with the agb.World operations used below
-(spawn with a seed, import_field, set_light, set_clock, apply_brush, step,
-stats, count, export_cells) can be driven, so the same scenario runs on the
-engine and, in the tests, on the CPU oracle.
+(spawn with a seed, import_field, set_light, set_flash, flash_audit,
+apply_brush, step, stats, count, export_cells) can be driven, so the same
+scenario runs on the engine and, in the tests, on the CPU oracle.
 
-Not supported, because the engine does not build these stages: Taumoeba
-populations with their metrics (predation, src/sim/predation.cu) and the
-spin-drive flash (the `flash` stimulus and impulse_per_cycle,
-src/sim/flash.cu). A scenario that needs one raises ScenarioUnsupported from
-instantiate(); parse() accepts it.
+Not supported, because the engine does not build predation
+(src/sim/predation.cu): Taumoeba populations and their metrics. A scenario
+that needs them raises ScenarioUnsupported from instantiate(); parse()
+accepts it.
 """
 import json
 import math
@@ -41,7 +40,7 @@ class ScenarioError(Exception):
 
 
 class ScenarioUnsupported(Exception):
-    """The scenario needs a stage the engine does not build (predation, flash)."""
+    """The scenario needs a stage the engine does not build (predation)."""
 
 
 # contracts/scenario_v3.h enums (values as there).
@@ -61,7 +60,6 @@ METRICS = ["awake_fraction", "medium_temp_mean", "medium_temp_max", "boil_event_
            "charge_depth_correlation", "charge_height_correlation", "rise_velocity_empty",
            "fall_velocity_full", "doubling_time_s", "impulse_per_cycle"]
 TAU_METRICS = {"mean_tau_tolerance", "max_tau_tolerance"}
-FLASH_METRICS = {"impulse_per_cycle"}
 MAX_LIGHT_SOURCES, MAX_POPULATIONS, MAX_ACCEPT_CHECKS, MAX_STIMULI, MAX_OVERRIDES = 8, 8, 16, 16, 32
 
 TOOLS = {"heat": 1 << 0, "chill": 1 << 1, "illuminate": 1 << 2, "inject_co2": 1 << 3, "inject_n2": 1 << 4,
@@ -339,13 +337,8 @@ def unsupported(s):
     """Why the engine cannot run `s`, or None."""
     if any(p.kind == TAUMOEBA and p.count > 0 for p in s.populations):
         return "Taumoeba populations (predation) are not built"
-    if any(d.kind == FLASH for d in s.drive):
-        return "the spin-drive flash is not built"
-    for c in s.accept:
-        if c.metric in TAU_METRICS:
-            return "Taumoeba metrics (predation) are not built"
-        if c.metric in FLASH_METRICS:
-            return "the spin-drive flash audit is not built"
+    if any(c.metric in TAU_METRICS for c in s.accept):
+        return "Taumoeba metrics (predation) are not built"
     return None
 
 
@@ -393,6 +386,7 @@ class Driven:
         self.physics_rate, self.biology_rate = desc.physics_rate, desc.biology_rate
         self.light = agb.Light(desc.light.dir_x, desc.light.dir_y, desc.light.dir_z, desc.light.irradiance,
                                desc.light.ambient, desc.light.enabled)
+        self.flash = False                  # World::flash_active as last set
 
     @property
     def dt(self):
@@ -437,9 +431,11 @@ def _spawn_of(p, count):
 def apply_drive(dw):
     """scenario_apply_drive (src/sim/scenario.cpp:399-468) for the current tick:
     every stimulus whose window holds the world's time. Brush strengths are
-    rates times this tick's dt; set_light and set_n2 are absolute levels."""
+    rates times this tick's dt; set_light and set_n2 are absolute levels; the
+    flash is armed for exactly the ticks inside a flash window."""
     s, w = dw.s, dw.world
     t, dt = dw.sim_time_s, dw.dt
+    flash = False
     for st in s.drive:
         open_ended = st.t1_s <= st.t0_s
         if t < st.t0_s:
@@ -475,7 +471,10 @@ def apply_drive(dw):
                     w.spawn(_spawn_of(p, deficit), seed=(s.seed + dw.tick) & 0xFFFFFFFFFFFFFFFF)
                 break
         elif st.kind == FLASH:
-            raise ScenarioUnsupported("the spin-drive flash is not built")
+            flash = True
+    if flash != dw.flash:
+        w.set_flash(flash)
+        dw.flash = flash
 
 
 # ---------------------------------------------------------------------------
@@ -642,6 +641,9 @@ def metric_measure(metric, fin, agg, dw):
         return agg.fall_velocity_full
     if metric == "doubling_time_s":
         return _doubling_time(agg, dw.biology_rate)
+    if metric == "impulse_per_cycle":
+        imp, dis = dw.world.flash_audit()
+        return imp * agb.C_LIGHT / dis if dis > 0.0 else 0.0
     raise ScenarioUnsupported("metric %s needs a stage the engine does not build" % metric)
 
 
@@ -747,7 +749,7 @@ def run_assert(s, dw, ticks=None, csv_path=None, graph=True, out=None):
 def main(argv=None):
     """`scenario.py --scenario ID|PATH [--scenarios-dir DIR] [--assert] [--ticks N]
     [--csv PATH]`: headless's scenario mode. Exit status 0 on ACCEPT (or a run
-    without --assert), 1 on REJECT, 2 on a bad scenario, 3 when unsupported."""
+    without --assert), 1 on REJECT, 2 on a bad scenario, 3 when unsupported (predation)."""
     import argparse
     ap = argparse.ArgumentParser(description=main.__doc__)
     ap.add_argument("--scenario", required=True)

@@ -200,7 +200,8 @@ enum {
     AGB_STAGE_SLOW_FIELDS = 5, /* CO2/N2 flush + diffuse, src/sim/step.cu:168-171 */
     AGB_STAGE_LIFECYCLE = 6,   /* lifecycle_step, src/sim/lifecycle.cu:208-294 */
     AGB_STAGE_COMPACT = 7,     /* cell_store_compact, src/sim/cell_store.cu:414-456 */
-    AGB_STAGE_CLOCK = 8        /* ++tick; sim_time += dt, src/sim/step.cu:182-183 */
+    AGB_STAGE_CLOCK = 8,       /* ++tick; sim_time += dt, src/sim/step.cu:182-183 */
+    AGB_STAGE_FLASH = 9        /* flash_step, src/sim/flash.cu:59-67 (a no-op unless armed) */
 };
 
 /* Snapshots (contracts/snapshot_v1.h:17-63): file = header, then the body the
@@ -350,6 +351,15 @@ agb_status agb_world_import_field(agb_world* w, int32_t field, const float* src,
 agb_status agb_world_export_field(agb_world* w, int32_t field, float* dst, agb_stream s);
 /* Raw fixed-point accumulator (irradiance: the occlusion stamp of the last emission stage). */
 agb_status agb_world_export_deposit(agb_world* w, int32_t field, uint64_t* dst, agb_stream s);
+
+/* The spin-drive flash (World::flash_active / petrova_flash_power, src/sim/world.cuh:169-179):
+ * while armed, each tick's flash stage replaces taxis (src/sim/step.cu:158-162) and every
+ * awake charged cell discharges power * dt of its store (src/sim/flash.cu:31-56); power <= 0
+ * takes the canon AGB_PETROVA_FLASH_POWER. Call between ticks. */
+agb_status agb_world_set_flash(agb_world* w, int32_t active, double power);
+/* world_flash_audit (src/sim/flash.cu:69-78): delivered impulse [N s] and discharged store [J]
+ * since creation. Synchronises. */
+agb_status agb_world_flash_audit(agb_world* w, double* impulse_ns, double* discharged_j);
 
 /* world_apply_brush (src/sim/step.cu:80-89, grid_brush src/fields/diffuse.cu:81-89): add
  * strength * (1 - (r/radius)^2)^2 to the kind's field (chill: subtract) at voxels whose

@@ -12,6 +12,10 @@
 
 /* Universal constants (canon_generated.h:12-19). */
 #define AGB_C_LIGHT 299792458.0
+#define AGB_PETROVA_FLASH_POWER 3000000.0          /* canon_generated.h:33, spin-drive discharge [W] */
+/* Fixed-point scales of the flash audit (src/sim/flash.cu:24-27). */
+#define AGB_FLASH_IMPULSE_SCALE 1.0e15
+#define AGB_FLASH_ENERGY_SCALE 1.0e6
 #define AGB_K_BOLTZ 1.3806490000000001e-23
 #define AGB_G_ACCEL 9.8066499999999994
 

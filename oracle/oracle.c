@@ -320,6 +320,10 @@ struct orc_world {
     uint64_t tick;
     double sim_time, physics_rate, biology_rate;
     uint64_t accum[12];
+    /* the spin-drive flash (World::flash_active, petrova_flash_power, d_flash_accum) */
+    int flash_active;
+    double flash_power;
+    uint64_t flash_accum[4];
 };
 
 static void soa_sizes(size_t sz[25]) {
@@ -375,6 +379,7 @@ int orc_world_create(const agb_world_desc* d, orc_world** out) {
     w->d = *d;
     w->capacity = d->capacity;
     w->next_id = 1;                                      /* cell_store.cuh:42 */
+    w->flash_power = AGB_PETROVA_FLASH_POWER;            /* World::petrova_flash_power */
     size_t sz[25];
     soa_sizes(sz);
     void* p[25];
@@ -1335,6 +1340,43 @@ static int slow_fields(orc_world* w, double dt) {         /* step.cu:168-171 */
     return grid_diffuse(&w->g[AGB_FIELD_N2], dt);
 }
 
+/* flash_step / flash_kernel (src/sim/flash.cu:31-67): while armed, every awake
+ * live cell discharges power * dt of its store at full rate, emit_power 0, the
+ * photon impulse (-z) and the energy into the audit in fixed point. */
+static void flash_step(orc_world* w, double dt) {
+    if (!w->flash_active) return;
+    soa* v = &w->c;
+    for (int32_t i = 0; i < w->count; ++i) {
+        const uint32_t f = v->flags[i];
+        if (!(f & AGB_FLAG_OCCUPIED) || !(f & AGB_FLAG_ALIVE) || !(f & AGB_FLAG_AWAKE)) continue;
+        const double e = v->energy[i];
+        v->emit_power[i] = 0.0f;
+        if (e <= 0.0) continue;
+        double de = w->flash_power * dt;
+        if (de > e) de = e;
+        v->energy[i] = e - de;
+        const double imp = de / AGB_C_LIGHT;
+        w->flash_accum[2] += (uint64_t)llround(-imp * AGB_FLASH_IMPULSE_SCALE);
+        w->flash_accum[3] += (uint64_t)llround(de * AGB_FLASH_ENERGY_SCALE);
+    }
+}
+
+int orc_world_set_flash(orc_world* w, int32_t active, double power) {
+    w->flash_active = active != 0;
+    w->flash_power = power > 0.0 ? power : AGB_PETROVA_FLASH_POWER;
+    return 0;
+}
+
+/* world_flash_audit (src/sim/flash.cu:69-78). */
+int orc_world_flash_audit(orc_world* w, double* impulse_ns, double* discharged_j) {
+    const double ix = (double)(int64_t)w->flash_accum[0] / AGB_FLASH_IMPULSE_SCALE;
+    const double iy = (double)(int64_t)w->flash_accum[1] / AGB_FLASH_IMPULSE_SCALE;
+    const double iz = (double)(int64_t)w->flash_accum[2] / AGB_FLASH_IMPULSE_SCALE;
+    *impulse_ns = sqrt(ix * ix + iy * iy + iz * iz);
+    *discharged_j = (double)(int64_t)w->flash_accum[3] / AGB_FLASH_ENERGY_SCALE;
+    return 0;
+}
+
 int orc_world_stage(orc_world* w, int32_t stage) {
     const double dt = AGB_DT_PHYSICS * w->physics_rate;
     switch (stage) {
@@ -1347,6 +1389,7 @@ int orc_world_stage(orc_world* w, int32_t stage) {
         case AGB_STAGE_LIFECYCLE: lifecycle_step(w, dt); return 0;
         case AGB_STAGE_COMPACT: return compact(w);
         case AGB_STAGE_CLOCK: ++w->tick; w->sim_time += dt; return 0;
+        case AGB_STAGE_FLASH: flash_step(w, dt); return 0;
     }
     return AGB_INVALID_ARGUMENT;
 }
@@ -1358,7 +1401,8 @@ int orc_world_step(orc_world* w, int32_t ticks) {
         if (!rc && w->d.thermal_enabled) rc = thermal_step(w, dt);
         if (rc) return rc;
         if (w->d.emission_enabled) emission_step(w, dt);
-        if (w->d.taxis_enabled) taxis_step(w, dt);                       /* step.cu:161-162 */
+        if (w->flash_active) flash_step(w, dt);                          /* step.cu:158-162 */
+        else if (w->d.taxis_enabled) taxis_step(w, dt);
         motion_step(w, dt);
         rc = slow_fields(w, dt);
         if (rc) return rc;

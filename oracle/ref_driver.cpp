@@ -187,6 +187,16 @@ int ref_field_deposit(void* h, int fid, uint64_t* host) {
     return 0;
 }
 
+// World::flash_active / petrova_flash_power and world_flash_audit (src/sim/flash.cu:69-78).
+void ref_set_flash(void* h, int active, double power) {
+    World* w = static_cast<World*>(h);
+    w->flash_active = active != 0;
+    if (power > 0.0) w->petrova_flash_power = power;
+}
+void ref_flash_audit(void* h, double* impulse_ns, double* discharged_j) {
+    world_flash_audit(*static_cast<World*>(h), *impulse_ns, *discharged_j);
+}
+
 // world_apply_brush (src/sim/step.cu:80-89).
 int ref_apply_brush(void* h, int kind, double x, double y, double radius, double strength) {
     return static_cast<int>(world_apply_brush(*static_cast<World*>(h), static_cast<BrushKind>(kind), x, y,

@@ -64,6 +64,8 @@ def oracle_lib():
             "orc_world_spawn": (I32, [P, C.POINTER(agb.Spawn)]),
             "orc_world_spawn_seeded": (I32, [P, C.POINTER(agb.Spawn), U64]),
             "orc_world_set_light": (I32, [P, C.POINTER(agb.Light)]),
+            "orc_world_set_flash": (I32, [P, I32, C.c_double]),
+            "orc_world_flash_audit": (I32, [P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
             "orc_world_import_cells": (I32, [P, C.POINTER(agb.Cells), I32, U64]),
             "orc_world_export_cells": (I32, [P, C.POINTER(agb.Cells), I32, C.POINTER(I32), C.POINTER(U64)]),
             "orc_world_import_field": (I32, [P, I32, P]),
@@ -129,6 +131,14 @@ class OracleWorld:
 
     def set_light(self, light):
         self._ck(self.lib.orc_world_set_light(self.h, C.byref(light)), "set_light")
+
+    def set_flash(self, active, power=0.0):
+        self._ck(self.lib.orc_world_set_flash(self.h, int(bool(active)), power), "set_flash")
+
+    def flash_audit(self):
+        i, e = C.c_double(), C.c_double()
+        self._ck(self.lib.orc_world_flash_audit(self.h, C.byref(i), C.byref(e)), "flash_audit")
+        return i.value, e.value
 
     def import_cells(self, cells, next_id):
         s = cells.struct()
@@ -270,6 +280,8 @@ def ref_lib():
         lib.ref_snapshot.argtypes = [C.c_void_p, C.c_char_p, C.c_void_p, C.c_int64]
         lib.ref_state_hash.restype = C.c_uint64
         lib.ref_state_hash.argtypes = [C.c_void_p]
+        lib.ref_set_flash.argtypes = [C.c_void_p, C.c_int, C.c_double]
+        lib.ref_flash_audit.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         lib.ref_scenario_run.restype = C.c_void_p
         lib.ref_scenario_run.argtypes = [C.c_char_p, C.c_int64, C.c_void_p, C.POINTER(C.c_int32)]
         _ref = lib

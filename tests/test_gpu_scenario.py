@@ -18,7 +18,8 @@ agb = H.agb
 S = H.load_scenario()
 pytestmark = pytest.mark.gpu
 
-SUPPORTED = ["first-light", "three-percent-line", "bloom", "komorov", "shadow-garden", "demo-herd", "sandbox"]
+SUPPORTED = ["first-light", "three-percent-line", "bloom", "komorov", "shadow-garden", "spin-drive-face",
+             "demo-herd", "sandbox"]
 HAVE = {os.path.basename(p)[:-5] for p in glob.glob(os.path.join(TS.SCEN_DIR, "*.json"))}
 MEASURE_RTOL = 1e-4        # correlations and fits over FP32-computed positions
 
@@ -81,14 +82,15 @@ def test_measured_accept_values_agree():
 
 
 def test_unsupported_scenarios_refuse():
-    for sid in ("taumoeba", "spin-drive-face"):
+    for sid in ("taumoeba",):
         if sid not in HAVE:
             continue
         with pytest.raises(S.ScenarioUnsupported):
             S.instantiate(S.parse(TS.text_of(sid)))
 
 
-@pytest.mark.parametrize("sid", ["shadow-garden", "komorov", "bloom", "three-percent-line", "first-light"])
+@pytest.mark.parametrize("sid", ["shadow-garden", "komorov", "bloom", "three-percent-line", "first-light",
+                                 "spin-drive-face"])
 def test_reference_scenario_accepts(sid):
     """`--scenario ID --assert` at the scenario's own horizon (300 to 60,000
     ticks): the reference's acceptance gate, run on the engine, accepts."""
@@ -114,3 +116,53 @@ def test_headless_entry_point():
     r = subprocess.run([sys.executable, script, "--scenario", os.path.join(TS.SCEN_DIR, "taumoeba.json"), "--assert"],
                        capture_output=True, text=True, timeout=600)
     assert r.returncode == 3 and "unsupported" in r.stdout
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_flash_tracks_oracle(graph):
+    """The spin-drive flash armed for 12 ticks, then disarmed (taxis resumes):
+    integer state equal to the oracle's, the audit within the FP tolerance."""
+    import scenarios as TSD
+    d = TSD.slab_desc(cap=900, light=(1.0, 0.0, 1e4, 0.0))
+    d.taxis_enabled = 1
+    sc = dict(desc=d, ticks=0,
+              spawn=agb.spawn(800, charge_dist=agb.DIST_UNIFORM, charge_a=0.0, charge_b=0.004, awake=True))
+    orc = H.OracleWorld(d)
+    TSD.setup(orc, sc)
+    gpu = agb.World(d)
+    P.copy_state(orc, gpu)
+    for k in range(18):
+        on = k < 12
+        gpu.set_flash(on)
+        orc.set_flash(on)
+        gpu.step(1, graph=graph)
+        orc.step(1)
+    a, _ = gpu.export_cells()
+    b, _ = orc.export_cells()
+    for k in P.INT_FIELDS:
+        assert np.array_equal(a[k], b[k]), k
+    gi, gd = gpu.flash_audit()
+    oi, od = orc.flash_audit()
+    assert od > 0.0
+    assert abs(gd - od) <= 1e-9 * od and abs(gi - oi) <= 1e-9 * oi
+    assert abs(gi * agb.C_LIGHT / gd - 1.0) < 1e-6
+    assert gpu.counters()[3] == 0
+
+
+def test_flash_armed_batch_chamber_equals_standalone():
+    """A batch whose chamber has the flash armed leaves the staged path for the
+    lanes path and still equals that chamber run on its own."""
+    import test_gpu_batch as TB
+    descs, spawns = TB.chambers()
+    b = agb.Batch(descs, spawns, agb.batch_opts(lanes=2, staged=True))
+    b.chambers[1].set_flash(True)
+    for t in (2, 1):
+        b.step(t)
+    d, s = TB.chambers()
+    w = TB.standalone(d[1], s[1], 0, walk=b.chambers[1].walk())
+    w.set_flash(True)
+    w.step(3)
+    TB.assert_same(b.chambers[1], w, "flash chamber")
+    for i in (0, 2, 3):
+        d, s = TB.chambers()
+        TB.assert_same(b.chambers[i], TB.standalone(d[i], s[i], 3, walk=b.chambers[i].walk()), "chamber %d" % i)

@@ -4,6 +4,7 @@ acceptance fits, and -- where the reference is built here -- the whole spine
 (parse, instantiate, drive, sample, measure) over the oracle against the
 reference's own scenario code (src/sim/scenario.cpp, src/sim/accept.cpp) over
 the reference's World: the same cells, fields and measured values, bit for bit."""
+import ctypes as C
 import glob
 import json
 import math
@@ -13,6 +14,7 @@ import numpy as np
 import pytest
 
 import helpers as H
+import scenarios as TSD
 
 agb = H.agb
 S = H.load_scenario()
@@ -51,7 +53,8 @@ DRIVEN = {
         {"kind": "inject_n2", "t0_s": 0.02, "t1_s": 0.06, "x": 0.0, "y": 0.0, "radius": 1.0e-3, "v0": 1.0, "v1": 3.0},
         {"kind": "set_light", "t0_s": 0.02, "t1_s": 0.05, "v0": 8000.0, "v1": 0.0},
         {"kind": "set_n2", "t0_s": 0.06, "t1_s": 0.07, "value": 0.125},
-        {"kind": "seed_cells", "t0_s": 0.04, "t1_s": 0.0, "value": 1000.0}],
+        {"kind": "seed_cells", "t0_s": 0.04, "t1_s": 0.0, "value": 1000.0},
+        {"kind": "flash", "t0_s": 0.05, "t1_s": 0.07}],
     "objective": {"text": "exercise the driver", "accept": [
         {"metric": "awake_fraction", "op": ">=", "value": 0.0},
         {"metric": "medium_temp_mean", "op": "~=", "value": 295.0, "tol": 0.1},
@@ -63,7 +66,8 @@ DRIVEN = {
         {"metric": "total_energy_j", "op": ">", "value": 0.0},
         {"metric": "charge_depth_correlation", "op": "<=", "value": 1.0},
         {"metric": "charge_height_correlation", "op": ">=", "value": -1.0},
-        {"metric": "doubling_time_s", "op": ">=", "value": 0.0}]},
+        {"metric": "doubling_time_s", "op": ">=", "value": 0.0},
+        {"metric": "impulse_per_cycle", "op": "~=", "value": 1.0, "tol": 0.01}]},
 }
 
 
@@ -74,7 +78,7 @@ def test_driven_scenario_parses():
     assert [p.count for p in s.populations] == [600, 0, 300]
     assert s.populations[2].charge_a == 0.9 and s.populations[2].placement == agb.PLACE_DISC
     assert [d.kind for d in s.drive] == [S.HEAT, S.CHILL, S.INJECT_CO2, S.INJECT_N2, S.SET_LIGHT, S.SET_N2,
-                                         S.SEED_CELLS]
+                                         S.SEED_CELLS, S.FLASH]
     assert s.drive[1].v0 == s.drive[1].v1 == 80.0
     assert s.clock == S.CUSTOM and S.clock_rates(s.clock, s.physics_rate, s.biology_rate) == (2.0, 5.0e4)
     assert S.unsupported(s) is None
@@ -88,9 +92,9 @@ def test_reference_scenarios_parse():
         s = S.load(path)
         ids[s.id] = s
         assert s.populations, s.id
-    assert S.unsupported(ids["taumoeba"]) and S.unsupported(ids["spin-drive-face"])
+    assert S.unsupported(ids["taumoeba"])
     supported = [k for k, s in ids.items() if S.unsupported(s) is None]
-    assert len(supported) == len(ids) - 2
+    assert len(supported) == len(ids) - 1
 
 
 def test_parse_defaults_comments_and_errors():
@@ -140,7 +144,7 @@ def test_accept_eval_and_fits():
 
 @needs_ref
 @pytest.mark.parametrize("sid,ticks", [("first-light", 40), ("three-percent-line", 12), ("bloom", 40),
-                                       ("komorov", 40), ("shadow-garden", 25)])
+                                       ("komorov", 40), ("shadow-garden", 25), ("spin-drive-face", 60)])
 def test_spine_matches_reference_scenario_code(sid, ticks):
     text = text_of(sid)
     s = S.parse(text)
@@ -179,3 +183,33 @@ def test_driven_scenario_matches_reference():
             assert np.array_equal(dw.world.export_field(f).ravel(), rw.export_field(f).ravel()), f
     finally:
         rw.close()
+
+
+@needs_ref
+def test_flash_matches_reference():
+    """flash_step (src/sim/flash.cu): armed for 30 ticks then disarmed for 10,
+    the oracle's cells and audit equal the reference's, bit for bit."""
+    d = TSD.slab_desc(cap=900, light=(1.0, 0.0, 1e4, 0.0))
+    d.taxis_enabled = 1
+    sp = agb.spawn(800, charge_dist=agb.DIST_UNIFORM, charge_a=0.0, charge_b=0.004, awake=True)
+    r, o = H.RefWorld(d), H.OracleWorld(d)
+    try:
+        r.spawn(sp)
+        o.spawn(sp)
+        for k in range(40):
+            on = k < 30
+            r.lib.ref_set_flash(r.h, int(on), 0.0)
+            o.set_flash(on)
+            r.step(1)
+            o.step(1)
+        a, _ = o.export_cells()
+        b, _ = r.export_cells()
+        for name, _t in agb.CELL_FIELDS:
+            assert np.array_equal(a[name].view(np.uint8), b[name].view(np.uint8)), name
+        ri, rd = C.c_double(), C.c_double()
+        r.lib.ref_flash_audit(r.h, C.byref(ri), C.byref(rd))
+        oi, od = o.flash_audit()
+        assert (oi, od) == (ri.value, rd.value)
+        assert od > 0.0 and abs(oi * agb.C_LIGHT / od - 1.0) < 1e-6
+    finally:
+        r.close()
