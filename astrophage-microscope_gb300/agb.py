@@ -30,7 +30,7 @@ DIVIDE_CO2_QUOTA, DIVIDE_ENERGY = 0, 1
 PLACE_UNIFORM, PLACE_GAUSSIAN, PLACE_GRID, PLACE_DISC, PLACE_SLAB_X, PLACE_CLUSTERS = range(6)
 DIST_CONSTANT, DIST_UNIFORM, DIST_NORMAL, DIST_LOGNORMAL = range(4)
 STAGE_HASH, STAGE_THERMAL, STAGE_EMISSION, STAGE_TAXIS, STAGE_MOTION = 0, 1, 2, 3, 4
-STAGE_SLOW_FIELDS, STAGE_LIFECYCLE, STAGE_COMPACT, STAGE_CLOCK, STAGE_FLASH = 5, 6, 7, 8, 9
+STAGE_SLOW_FIELDS, STAGE_LIFECYCLE, STAGE_COMPACT, STAGE_CLOCK, STAGE_FLASH, STAGE_PREDATION = 5, 6, 7, 8, 9, 10
 FLAG_OCCUPIED, FLAG_ALIVE, FLAG_AWAKE, FLAG_STUCK = 1, 2, 4, 8
 
 # Canon values the Python side needs (include/agb_canon.h).
@@ -88,7 +88,8 @@ class WorldDesc(C.Structure):
                 ("co2_mass_per_division", C.c_double), ("max_emit_power", C.c_double),
                 ("division_predicate", C.c_int32), ("division_energy", C.c_double),
                 ("compaction_period", C.c_int32), ("trap_slot", C.c_int32),
-                ("trap_x", C.c_double), ("trap_y", C.c_double), ("trap_stiffness", C.c_double)]
+                ("trap_x", C.c_double), ("trap_y", C.c_double), ("trap_stiffness", C.c_double),
+                ("tau_capacity", C.c_int32), ("tau_compaction_enabled", C.c_int32)]
 
 
 # The 25 arrays of contracts/cell_store_v1.h:42-75, in declaration order.
@@ -101,12 +102,25 @@ CELL_FIELDS = [("id", np.uint64), ("flags", np.uint32), ("death_cause", np.uint8
                ("rng_state", np.uint64), ("taxis_memory", np.float32), ("run_timer", np.float32),
                ("t_local", np.float32), ("irradiance", np.float32), ("co2_local", np.float32),
                ("n2_local", np.float32)]
-_CT = {np.uint64: C.c_uint64, np.uint32: C.c_uint32, np.uint8: C.c_uint8,
+_CT = {np.uint64: C.c_uint64, np.uint32: C.c_uint32, np.uint8: C.c_uint8, np.int32: C.c_int32,
        np.float64: C.c_double, np.float32: C.c_float}
 
 
 class Cells(C.Structure):
     _fields_ = [(n, C.POINTER(_CT[t])) for n, t in CELL_FIELDS]
+
+
+class Taumoeba(C.Structure):
+    """agb_taumoeba: one pointer per predator-store array."""
+    _fields_ = [("id", C.POINTER(C.c_uint64)), ("flags", C.POINTER(C.c_uint32)),
+                ("x", C.POINTER(C.c_double)), ("y", C.POINTER(C.c_double)), ("z", C.POINTER(C.c_double)),
+                ("vx", C.POINTER(C.c_double)), ("vy", C.POINTER(C.c_double)), ("vz", C.POINTER(C.c_double)),
+                ("dir_x", C.POINTER(C.c_float)), ("dir_y", C.POINTER(C.c_float)), ("dir_z", C.POINTER(C.c_float)),
+                ("biomass", C.POINTER(C.c_double)), ("prey_biomass", C.POINTER(C.c_double)),
+                ("digest_timer", C.POINTER(C.c_float)), ("tolerance", C.POINTER(C.c_float)),
+                ("generation", C.POINTER(C.c_uint32)), ("rng_state", C.POINTER(C.c_uint64)),
+                ("density_ema", C.POINTER(C.c_float)), ("run_timer", C.POINTER(C.c_float)),
+                ("target", C.POINTER(C.c_int32))]
 
 
 class Spawn(C.Structure):
@@ -189,6 +203,7 @@ def default_desc(capacity=25000, seed=20260802, co2_init=0.0):
     d.division_predicate, d.division_energy = DIVIDE_CO2_QUOTA, 0.0
     d.compaction_period = 1
     d.trap_slot, d.trap_x, d.trap_y, d.trap_stiffness = -1, 0.0, 0.0, 0.0
+    d.tau_capacity, d.tau_compaction_enabled = 0, 0
     return d
 
 
@@ -197,6 +212,32 @@ def spawn(count, placement=PLACE_UNIFORM, charge_dist=DIST_CONSTANT, awake=False
           charge_max=0.0, clusters=0, cluster_extent=0.0):
     return Spawn(count, placement, charge_dist, int(bool(awake)), place_x, place_y, place_radius,
                  charge_a, charge_b, charge_max, clusters, cluster_extent)
+
+
+# TaumoebaStore (src/sim/predation.cuh:85-105), field for field.
+TAU_FIELDS = [("id", np.uint64), ("flags", np.uint32), ("x", np.float64), ("y", np.float64), ("z", np.float64),
+              ("vx", np.float64), ("vy", np.float64), ("vz", np.float64), ("dir_x", np.float32),
+              ("dir_y", np.float32), ("dir_z", np.float32), ("biomass", np.float64), ("prey_biomass", np.float64),
+              ("digest_timer", np.float32), ("tolerance", np.float32), ("generation", np.uint32),
+              ("rng_state", np.uint64), ("density_ema", np.float32), ("run_timer", np.float32),
+              ("target", np.int32)]
+
+
+class TaumoebaArrays:
+    """Host buffers of the predator store, one numpy array per field."""
+
+    def __init__(self, n):
+        self.n = n
+        self.a = {name: np.zeros(max(n, 1), dtype=t) for name, t in TAU_FIELDS}
+
+    def struct(self):
+        t = Taumoeba()
+        for name, ty in TAU_FIELDS:
+            setattr(t, name, self.a[name].ctypes.data_as(C.POINTER(_CT[ty])))
+        return t
+
+    def __getitem__(self, k):
+        return self.a[k][:self.n]
 
 
 class CellArrays:
@@ -295,6 +336,9 @@ def load(path=LIB_PATH):
         "agb_world_export_deposit": (I32, [P, I32, P, P]),
         "agb_world_apply_brush": (I32, [P, I32, C.c_double, C.c_double, C.c_double, C.c_double, P]),
         "agb_world_set_flash": (I32, [P, I32, C.c_double]),
+        "agb_world_spawn_taumoeba": (I32, [P, I32, U64, P]),
+        "agb_world_import_taumoeba": (I32, [P, C.POINTER(Taumoeba), I32, U64, P]),
+        "agb_world_export_taumoeba": (I32, [P, C.POINTER(Taumoeba), I32, C.POINTER(I32), C.POINTER(U64), P]),
         "agb_world_flash_audit": (I32, [P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
         "agb_world_step": (I32, [P, I32, P]),
         "agb_world_step_graph": (I32, [P, I32, P]),
@@ -359,6 +403,7 @@ def exported_symbols():
             "agb_world_export_cells", "agb_world_device_cells", "agb_world_step_host", "agb_world_count",
             "agb_world_import_field", "agb_world_export_field", "agb_world_export_deposit",
             "agb_world_apply_brush", "agb_world_set_flash", "agb_world_flash_audit",
+            "agb_world_spawn_taumoeba", "agb_world_import_taumoeba", "agb_world_export_taumoeba",
             "agb_world_step", "agb_world_step_graph", "agb_world_graph_kernels", "agb_world_set_walk",
             "agb_world_walk", "agb_world_stage",
             "agb_world_diffuse",
@@ -421,6 +466,27 @@ class World:
             self._check(self.lib.agb_world_spawn(self.h, C.byref(p), _st(stream)), "spawn")
         else:
             self._check(self.lib.agb_world_spawn_seeded(self.h, C.byref(p), seed, _st(stream)), "spawn")
+
+    def spawn_taumoeba(self, count, seed, stream=None):
+        """taumoeba_spawn: `count` predators, streams from (splitmix64(seed), id)."""
+        self._check(self.lib.agb_world_spawn_taumoeba(self.h, count, seed, _st(stream)), "spawn_taumoeba")
+
+    def import_taumoeba(self, tau, next_id, stream=None):
+        s = tau.struct()
+        self._check(self.lib.agb_world_import_taumoeba(self.h, C.byref(s), tau.n, next_id, _st(stream)),
+                    "import_taumoeba")
+
+    def export_taumoeba(self, stream=None):
+        """(TaumoebaArrays, next predator id)."""
+        cnt, nid = C.c_int32(), C.c_uint64()
+        empty = Taumoeba()
+        self._check(self.lib.agb_world_export_taumoeba(self.h, C.byref(empty), 0, C.byref(cnt), C.byref(nid),
+                                                       _st(stream)), "export_taumoeba")
+        out = TaumoebaArrays(cnt.value)
+        s = out.struct()
+        self._check(self.lib.agb_world_export_taumoeba(self.h, C.byref(s), cnt.value, C.byref(cnt), C.byref(nid),
+                                                       _st(stream)), "export_taumoeba")
+        return out, nid.value
 
     def set_flash(self, active, power=0.0):
         """Arm (or disarm) the spin-drive flash; power <= 0 is the canon rate."""

@@ -9,10 +9,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libagb.so")
-SOURCES = ["k_grid.cu", "k_hash.cu", "k_cells.cu", "k_life.cu", "world.cu", "batch.cu", "snapshot.cu", "conv_tc.cu", "nn_ops.cu", "nn_abi.cu", "surrogate.cu", "noalloc.cu"]
+SOURCES = ["k_grid.cu", "k_hash.cu", "k_cells.cu", "k_life.cu", "k_tau.cu", "world.cu", "batch.cu", "snapshot.cu", "conv_tc.cu", "nn_ops.cu", "nn_abi.cu", "surrogate.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Host code that restates the reference's FP64 expressions (per-world constants)
+# must not be contracted into FMAs by the host compiler (aarch64 gcc would).
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
-         "--threads", "2"]
+         "-Xcompiler", "-ffp-contract=off", "--threads", "2"]
 
 
 def nvcc():

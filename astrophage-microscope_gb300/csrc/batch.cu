@@ -219,12 +219,12 @@ void plan_ftcs(StagedPlan& P, int32_t stream, const std::vector<agb_world*>& ws,
 }
 
 // Whether every chamber can run staged ticks: every diffused grid 3-D with a
-// TMA stencil, no surrogate, no spin-drive flash armed, one lane per cell in
+// TMA stencil, no surrogate, no spin-drive flash armed, no predators, one lane per cell in
 // fused walks, and at most 65,535 blocks per stage (capacities up to about 67M
 // cells). Checked at each capture; the lanes path takes the rest.
 bool staged_ok(const agb_batch* b) {
     for (const agb_world* w : b->worlds) {
-        if (w->sg || w->walk_lanes != 1 || !w->fuse_cells || w->flash_active) return false;
+        if (w->sg || w->walk_lanes != 1 || !w->fuse_cells || w->flash_active || w->tau_active) return false;
         // A block map entry holds a chamber's block index in 16 bits.
         if (scan_blocks(w->c.capacity) > 0xFFFF || w->blocks > 0xFFFF) return false;
         for (int f = 0; f < 3; ++f) {

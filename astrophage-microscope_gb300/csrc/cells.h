@@ -148,4 +148,50 @@ void launch_stats(DevState* S, const Ctx& c, unsigned long long* acc, int32_t bl
 // spawn_kernel (src/sim/cell_store.cu:42-130) for `count` new cells.
 void launch_spawn(DevState* S, const Ctx& c, const agb_spawn& p, int32_t blocks, cudaStream_t s);
 
+// ---------------------------------------------------------------------------
+// Taumoeba, the predator (src/sim/predation.cuh:82-118, k_tau.cu)
+// ---------------------------------------------------------------------------
+struct TauSoA {
+    uint64_t* id;
+    uint32_t* flags;
+    double *x, *y, *z, *vx, *vy, *vz;
+    float *dir_x, *dir_y, *dir_z;
+    double *biomass, *prey_biomass;
+    float *digest_timer, *tolerance;
+    uint32_t* generation;
+    uint64_t* rng_state;
+    float *density_ema, *run_timer;
+    int32_t* target;
+};
+// Device-resident store state: the live and spare arrays (compaction writes
+// the spare and swaps), the count and the next predator id.
+struct TauState {
+    TauSoA cur, spare;
+    int32_t count, capacity;
+    uint64_t next_id;
+};
+// Per-world constants of a predator tick, computed on the host in FP64 with
+// the reference's expressions: the OU step of TAU_MASS under the Stokes drag
+// at the ambient temperature (ou_coefficients, integrator.cuh:103-121), the
+// run-and-tumble memory weight (predation.cuh:38), the walls.
+struct TauParams {
+    double dt, dt_bio, alpha;
+    float dt_f, dt_bio_f;
+    double gamma, ome, inv_beta, s_rr, s_vv, noise_a, noise_b;
+    double lo[3], hi[3], half[3], span[3];
+    int32_t boundary_x, boundary_y, noise, disposition, compaction;
+};
+// The 20 arrays carved from one blob of `capacity` predators (snapshot order).
+TauSoA tau_carve(void* blob, int32_t capacity);
+size_t tau_blob_bytes(int32_t capacity);
+// taumoeba_spawn (predation.cu:33-74, 420-432): `count` predators appended at
+// the device-side count.
+void launch_tau_spawn(TauState* T, int32_t count, uint64_t seed, const TauParams& p, cudaStream_t s);
+// predation_step (predation.cu:434-484): claim reset, hunt, resolve, nitrogen,
+// then division and (if enabled) compaction in one CTA.
+void launch_predation(TauState* T, DevState* S, const HashDev& h, const GridDev& n2, const TauParams& p,
+                      unsigned long long* claim, int32_t cell_capacity, int32_t tau_capacity, cudaStream_t s);
+// stats_taumoeba_kernel (stats.cu:65-73): alive count into acc[11], tolerance into acc[6].
+void launch_tau_stats(TauState* T, int32_t tau_capacity, unsigned long long* acc, cudaStream_t s);
+
 }  // namespace agb

@@ -217,6 +217,21 @@ __device__ __forceinline__ long long f_to_ll(float v) {
     return (u >> 31) ? -(long long)r : (long long)r;
 }
 
+// FP64 draws as the reference takes them (rng.cuh:86-101), for the seeded
+// spawns and the predators: explicitly rounded, CUDA's log/cos/sin.
+__device__ __forceinline__ double uniform_range(Pcg& r, double lo, double hi) {   // rng.cuh:86-88
+    return __dadd_rn(lo, __dmul_rn(__dsub_rn(hi, lo), uniform01d(r)));
+}
+__device__ __forceinline__ void gaussian_pair_d(Pcg& r, double& z0, double& z1) {
+    double u1 = uniform01d(r);
+    if (u1 < 1.0e-300) u1 = 1.0e-300;
+    const double u2 = uniform01d(r);
+    const double mag = sqrt(__dmul_rn(-2.0, log(u1)));
+    const double ang = __dmul_rn(6.283185307179586476925286766559, u2);
+    z0 = __dmul_rn(mag, cos(ang));
+    z1 = __dmul_rn(mag, sin(ang));
+}
+
 // Box-Muller in FP32 from the reference's 53-bit uniforms (rng.cuh:92-101).
 // ln(u1) is taken as log1p(-(1-u1)) for u1 > 1/2, with 1-u1 exact in integers,
 // so the magnitude keeps ~1e-7 relative accuracy near u1 = 1. The reference

@@ -483,18 +483,6 @@ __global__ void __launch_bounds__(256) stats_field_kernel(const float* __restric
 // Seeded spawn (spawn_kernel, cell_store.cu:42-130, plus the extension
 // placements of include/agb.h). FP64, run once per population.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double uniform_range(Pcg& r, double lo, double hi) {   // rng.cuh:86-88
-    return __dadd_rn(lo, __dmul_rn(__dsub_rn(hi, lo), uniform01d(r)));
-}
-__device__ __forceinline__ void gaussian_pair_d(Pcg& r, double& z0, double& z1) {
-    double u1 = uniform01d(r);
-    if (u1 < 1.0e-300) u1 = 1.0e-300;
-    const double u2 = uniform01d(r);
-    const double mag = sqrt(__dmul_rn(-2.0, log(u1)));
-    const double ang = __dmul_rn(6.283185307179586476925286766559, u2);
-    z0 = __dmul_rn(mag, cos(ang));
-    z1 = __dmul_rn(mag, sin(ang));
-}
 
 __global__ void __launch_bounds__(256) spawn_kernel(DevState* S, Ctx c, agb_spawn p) {
     pdl_wait();

@@ -48,9 +48,27 @@ std::vector<agb_param_override> overrides(const agb_world* w) {
 
 const int kStoredFields[3] = {AGB_FIELD_TEMPERATURE, AGB_FIELD_CO2, AGB_FIELD_N2};
 
-int64_t body_bytes(const agb_world* w, int32_t count, size_t n_overrides) {
+// The predator store's 20 arrays (collect_tau_spans, snapshot.cu:59-67).
+const size_t kTauElem[20] = {8, 4, 8, 8, 8, 8, 8, 8, 4, 4, 4, 8, 8, 4, 4, 4, 8, 4, 4, 4};
+
+void tau_arrays(const TauSoA& t, void* p[20]) {
+    void* q[20] = {t.id, t.flags, t.x, t.y, t.z, t.vx, t.vy, t.vz, t.dir_x, t.dir_y, t.dir_z, t.biomass,
+                   t.prey_biomass, t.digest_timer, t.tolerance, t.generation, t.rng_state, t.density_ema,
+                   t.run_timer, t.target};
+    std::memcpy(p, q, sizeof(q));
+}
+
+agb_status read_tau_state(agb_world* w, TauState& ts, cudaStream_t s) {
+    if (cudaMemcpyAsync(&ts, w->tS, sizeof(TauState), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return AGB_CUDA_ERROR;
+    return AGB_OK;
+}
+
+int64_t body_bytes(const agb_world* w, int32_t count, int32_t tau_count, size_t n_overrides) {
     int64_t b = (int64_t)(n_overrides * sizeof(agb_param_override));
     for (size_t e : kElem) b += (int64_t)e * count;
+    for (size_t e : kTauElem) b += (int64_t)e * tau_count;
     for (int f : kStoredFields)
         if (w->c.g[f].enabled) b += 4 * w->c.g[f].count;
     return b;
@@ -72,7 +90,8 @@ agb_status read_dev_state(agb_world* w, DevState& st, cudaStream_t s) {
 }
 
 // Body into dst (which holds body_bytes); returns the overrides written.
-agb_status write_body(agb_world* w, const DevState& st, char* dst, cudaStream_t s, int32_t* n_over) {
+agb_status write_body(agb_world* w, const DevState& st, const TauState& ts, char* dst, cudaStream_t s,
+                      int32_t* n_over) {
     const std::vector<agb_param_override> ov = overrides(w);
     char* p = dst;
     if (!ov.empty()) {
@@ -86,6 +105,14 @@ agb_status write_body(agb_world* w, const DevState& st, char* dst, cudaStream_t 
         if (n && cudaMemcpyAsync(p, arr[k], kElem[k] * n, cudaMemcpyDeviceToHost, s) != cudaSuccess)
             return AGB_CUDA_ERROR;
         p += kElem[k] * n;
+    }
+    void* tarr[20];
+    tau_arrays(ts.cur, tarr);
+    const size_t nt = (size_t)ts.count;
+    for (int k = 0; k < 20; ++k) {
+        if (nt && cudaMemcpyAsync(p, tarr[k], kTauElem[k] * nt, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+            return AGB_CUDA_ERROR;
+        p += kTauElem[k] * nt;
     }
     for (int f : kStoredFields) {
         const GridDev& g = w->c.g[f];
@@ -117,10 +144,11 @@ agb_status agb_world_state_hash(agb_world* w, uint64_t* hash, agb_stream stream)
     if (!w || !hash) return AGB_INVALID_ARGUMENT;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     DevState st;
-    if (read_dev_state(w, st, s) != AGB_OK) return AGB_CUDA_ERROR;
-    std::vector<char> body((size_t)body_bytes(w, st.count, overrides(w).size()));
+    TauState ts;
+    if (read_dev_state(w, st, s) != AGB_OK || read_tau_state(w, ts, s) != AGB_OK) return AGB_CUDA_ERROR;
+    std::vector<char> body((size_t)body_bytes(w, st.count, ts.count, overrides(w).size()));
     int32_t n_over = 0;
-    const agb_status rc = write_body(w, st, body.data(), s, &n_over);
+    const agb_status rc = write_body(w, st, ts, body.data(), s, &n_over);
     if (rc != AGB_OK) return rc;
     *hash = agb_fnv1a64(body.data(), body.size(), AGB_FNV1A64_OFFSET);
     return AGB_OK;
@@ -131,14 +159,15 @@ agb_status agb_world_snapshot_save(agb_world* w, const char* scenario_id, void* 
     if (!w || !size) return AGB_INVALID_ARGUMENT;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     DevState st;
-    if (read_dev_state(w, st, s) != AGB_OK) return AGB_CUDA_ERROR;
-    const int64_t body = body_bytes(w, st.count, overrides(w).size());
+    TauState ts;
+    if (read_dev_state(w, st, s) != AGB_OK || read_tau_state(w, ts, s) != AGB_OK) return AGB_CUDA_ERROR;
+    const int64_t body = body_bytes(w, st.count, ts.count, overrides(w).size());
     *size = (int64_t)sizeof(agb_snapshot_header) + body;
     if (!buf) return AGB_OK;                            // size query
     if (cap < *size) return AGB_CAPACITY_EXCEEDED;
     char* out = static_cast<char*>(buf);
     int32_t n_over = 0;
-    const agb_status rc = write_body(w, st, out + sizeof(agb_snapshot_header), s, &n_over);
+    const agb_status rc = write_body(w, st, ts, out + sizeof(agb_snapshot_header), s, &n_over);
     if (rc != AGB_OK) return rc;
     agb_snapshot_header h;
     std::memset(&h, 0, sizeof(h));
@@ -149,7 +178,8 @@ agb_status agb_world_snapshot_save(agb_world* w, const char* scenario_id, void* 
     h.sim_time_s = w->sim_time;
     h.cell_count = st.count;
     h.cell_capacity = w->c.capacity;
-    h.taumoeba_capacity = AGB_DEFAULT_TAUMOEBA;   // what a reference world reports: its default, empty store
+    h.taumoeba_count = ts.count;
+    h.taumoeba_capacity = w->tau_cap;
     h.n_temp = w->c.g[AGB_FIELD_TEMPERATURE].enabled ? w->c.g[AGB_FIELD_TEMPERATURE].nx : 0;
     h.n_co2 = w->c.g[AGB_FIELD_CO2].enabled ? w->c.g[AGB_FIELD_CO2].nx : 0;
     h.n_n2 = w->c.g[AGB_FIELD_N2].enabled ? w->c.g[AGB_FIELD_N2].nx : 0;
@@ -179,14 +209,15 @@ agb_status agb_world_snapshot_load(const agb_world_desc* base, const void* data,
     const char* body = static_cast<const char*>(data) + sizeof(h);
     const uint64_t body_len = (uint64_t)(n - (int64_t)sizeof(h));
     if (agb_fnv1a64(body, body_len, AGB_FNV1A64_OFFSET) != h.state_hash) return AGB_INVALID_ARGUMENT;
-    if (h.taumoeba_count != 0) return AGB_UNSUPPORTED;             // no predator store here
     if (h.cell_count < 0 || h.cell_count > h.cell_capacity || h.override_count < 0) return AGB_INVALID_ARGUMENT;
+    if (h.taumoeba_count < 0 || h.taumoeba_count > h.taumoeba_capacity) return AGB_INVALID_ARGUMENT;
 
     agb_world_desc d = *base;
     d.chamber_w = h.chamber_w;
     d.chamber_h = h.chamber_h;
     d.chamber_d = h.chamber_d;
     d.capacity = h.cell_capacity;
+    d.tau_capacity = h.taumoeba_capacity;
     d.seed = h.seed;
     d.physics_rate = h.physics_rate;
     d.biology_rate = h.biology_rate;
@@ -227,6 +258,26 @@ agb_status agb_world_snapshot_load(const agb_world_desc* base, const void* data,
                  (float*)p[24]};
     rc = agb_world_import_cells(w, &hc, h.cell_count, h.next_cell_id, nullptr);
     if (rc != AGB_OK) { agb_world_destroy(w); return rc; }
+    // Predators: the header carries no next predator id and the reference's
+    // loader leaves it at its initial value (snapshot.cu:218-219); so does this one.
+    const size_t tcnt = (size_t)h.taumoeba_count;
+    if (tcnt > 0) {
+        size_t tneed = 0;
+        for (size_t e : kTauElem) tneed += e * tcnt;
+        if ((size_t)(end - cur) < tneed) { agb_world_destroy(w); return AGB_INVALID_ARGUMENT; }
+        std::vector<char> tau(tneed);
+        std::memcpy(tau.data(), cur, tneed);
+        cur += tneed;
+        void* t[20];
+        char* q = tau.data();
+        for (int k = 0; k < 20; ++k) { t[k] = q; q += kTauElem[k] * tcnt; }
+        agb_taumoeba ht{(uint64_t*)t[0], (uint32_t*)t[1], (double*)t[2], (double*)t[3], (double*)t[4],
+                        (double*)t[5], (double*)t[6], (double*)t[7], (float*)t[8], (float*)t[9], (float*)t[10],
+                        (double*)t[11], (double*)t[12], (float*)t[13], (float*)t[14], (uint32_t*)t[15],
+                        (uint64_t*)t[16], (float*)t[17], (float*)t[18], (int32_t*)t[19]};
+        rc = agb_world_import_taumoeba(w, &ht, h.taumoeba_count, 1, nullptr);
+        if (rc != AGB_OK) { agb_world_destroy(w); return rc; }
+    }
     for (int f : kStoredFields) {
         const GridDev& g = w->c.g[f];
         if (!g.enabled) continue;

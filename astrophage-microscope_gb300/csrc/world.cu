@@ -109,6 +109,57 @@ int32_t substeps_for(const GridDev& g, double D, double dt) {
 }
 bool coeff_ok(const GridDev& g, float c) { return g.nz > 1 ? c <= (float)(1.0 / 6.0) : c <= 0.25f; }
 
+// ou_position_shape (integrator.cuh:80-91) on the host.
+double ou_shape_host(double x) {
+    if (x < 1.0e-2) {
+        const double x3 = x * x * x;
+        return x3 * (2.0 / 3.0 + x * (-0.5 + x * (7.0 / 30.0 + x * (-1.0 / 12.0))));
+    }
+    const double e = std::exp(-x);
+    return 2.0 * x - 3.0 + 4.0 * e - e * e;
+}
+
+// The predator's per-world constants (predation.cu:80-158): the memory weight
+// of tau_should_tumble, tau_drag at the ambient temperature, ou_coefficients
+// of TAU_MASS (integrator.cuh:103-121) and the noise factors of
+// ou_advance_axis, all in the reference's FP64 expressions; the walls.
+void compute_tau_params(agb_world* w) {
+    TauParams& q = w->taup;
+    const TickParams& p = w->tp;
+    q.dt = p.dt;
+    q.dt_bio = p.dt_bio;
+    q.dt_f = (float)q.dt;
+    q.dt_bio_f = (float)q.dt_bio;
+    q.alpha = -std::expm1(-q.dt / AGB_TAXIS_MEMORY_TIME);
+    const double T = w->d.ambient_temp;
+    q.gamma = 6.0 * AGB_PI * (AGB_VF_A * std::exp(AGB_VF_B / (T - AGB_VF_C))) * AGB_TAU_RADIUS;
+    const double beta = q.gamma / AGB_TAU_MASS;
+    const double x = beta * q.dt;
+    q.ome = -std::expm1(-x);
+    q.inv_beta = 1.0 / beta;
+    const double kTm = AGB_K_BOLTZ * T / AGB_TAU_MASS;
+    const double var_vv = kTm * (-std::expm1(-2.0 * x));
+    const double var_rr = kTm * q.inv_beta * q.inv_beta * ou_shape_host(x);
+    q.s_vv = std::sqrt(var_vv > 0.0 ? var_vv : 0.0);
+    q.s_rr = std::sqrt(var_rr > 0.0 ? var_rr : 0.0);
+    const double s_rv = kTm * q.inv_beta * q.ome * q.ome;
+    q.noise_a = q.s_rr > 0.0 ? s_rv / q.s_rr : 0.0;
+    const double b2 = q.s_vv * q.s_vv - q.noise_a * q.noise_a;
+    q.noise_b = std::sqrt(b2 > 0.0 ? b2 : 0.0);
+    const double ext[3] = {w->d.chamber_w, w->d.chamber_h, w->d.chamber_d};
+    for (int a = 0; a < 3; ++a) {
+        q.half[a] = 0.5 * ext[a];
+        q.lo[a] = -q.half[a] + AGB_TAU_RADIUS;
+        q.hi[a] = q.half[a] - AGB_TAU_RADIUS;
+        q.span[a] = 2.0 * q.half[a];
+    }
+    q.boundary_x = w->d.boundary_x;
+    q.boundary_y = w->d.boundary_y;
+    q.noise = w->d.thermal_noise ? 1 : 0;
+    q.disposition = w->d.store_disposition;
+    q.compaction = w->d.tau_compaction_enabled ? 1 : 0;
+}
+
 agb_status compute_tick_params(agb_world* w) {
     TickParams& p = w->tp;
     const Ctx& c = w->c;
@@ -147,6 +198,7 @@ agb_status compute_tick_params(agb_world* w) {
         if (f == AGB_FIELD_CO2) { p.c_substeps = steps; p.c_coeff = coeff; }
         else { p.n_substeps = steps; p.n_coeff = coeff; }
     }
+    compute_tau_params(w);
     return AGB_OK;
 }
 
@@ -254,6 +306,14 @@ void stage_flash_or_taxis(agb_world* w, cudaStream_t s) {
     else if (w->d.taxis_enabled) launch_taxis(w->S, w->c, w->tp, w->blocks, s);
 }
 
+// predation_step (predation.cu:434-484) once predators have been placed: it
+// senses this tick's cell hash and the N2 as diffused this tick.
+void stage_predation(agb_world* w, cudaStream_t s) {
+    if (!w->tau_active) return;
+    refresh_grid_ptrs(w);
+    launch_predation(w->tS, w->S, w->c.h, w->c.g[AGB_FIELD_N2], w->taup, w->claim, w->c.capacity, w->tau_cap, s);
+}
+
 bool compaction_allowed(const agb_world* w) {
     const int32_t P = w->d.compaction_period > 0 ? w->d.compaction_period : 1;
     return w->d.compaction_enabled && ((w->tick + 1) % (uint64_t)P) == 0;
@@ -338,9 +398,14 @@ void tick_once(agb_world* w, cudaStream_t s) {
     cudaStreamWaitEvent(s, w->ev[2], 0);
     const GridDev& co2 = w->c.g[AGB_FIELD_CO2];
     const float inv_gv = co2.enabled ? (float)(1.0 / (co2.dx * co2.dx * co2.dz_eff)) : 0.0f;
+    // With predators the CO2 demand waits for predation (it kills prey before
+    // the lifecycle books demand, step.cu:173-180); otherwise integration
+    // books it.
+    const bool fuse_demand = co2.enabled && !w->tau_active;
     launch_integrate(w->S, c, w->tp, w->fx, w->fy, w->fz, w->blocks, co2,
-                     co2.enabled ? w->life.co2_demand : nullptr, inv_gv, s);
-    stage_lifecycle(w, s, co2.enabled);
+                     fuse_demand ? w->life.co2_demand : nullptr, inv_gv, s);
+    stage_predation(w, s);
+    stage_lifecycle(w, s, fuse_demand);
     stage_clock(w);
 }
 
@@ -361,6 +426,7 @@ void tick_surrogate(agb_world* w, cudaStream_t s) {
     if (w->d.emission_enabled) stage_emission(w, s);
     stage_flash_or_taxis(w, s);
     launch_motion(w->S, w->c, w->tp, w->fx, w->fy, w->fz, w->blocks, w->walk_lanes, s);
+    stage_predation(w, s);
     stage_lifecycle(w, s);
     stage_clock(w);
     if (w->tick % (uint64_t)w->sg_steps == 0) {
@@ -603,6 +669,8 @@ void agb_world_desc_default(agb_world_desc* d) {
     d->division_predicate = AGB_DIVIDE_CO2_QUOTA;
     d->compaction_period = 1;
     d->trap_slot = -1;
+    d->tau_capacity = 0;
+    d->tau_compaction_enabled = 0;
 }
 
 const char* agb_status_str(agb_status s) {
@@ -800,7 +868,23 @@ agb_status agb_world_create(const agb_world_desc* d, agb_world** out) {
     const int64_t co2n = c.g[AGB_FIELD_CO2].enabled ? c.g[AGB_FIELD_CO2].count : 1;
     ok = ok && dalloc(w, &w->life.co2_demand, 8 * (size_t)co2n) == cudaSuccess;
     ok = ok && dalloc(w, &w->flash_accum, 8 * 4) == cudaSuccess;
+    // The predator store (taumoeba_create, predation.cu:306-418) and the per-cell claim words.
+    w->tau_cap = d->tau_capacity > 0 ? d->tau_capacity : AGB_DEFAULT_TAUMOEBA;
+    if (w->tau_cap > AGB_MAX_TAUMOEBA) { agb_world_destroy(w); return AGB_INVALID_ARGUMENT; }
+    for (void*& b : w->tau_blob) ok = ok && dalloc(w, &b, tau_blob_bytes(w->tau_cap)) == cudaSuccess;
+    ok = ok && dalloc(w, &w->tS, sizeof(TauState)) == cudaSuccess;
+    ok = ok && dalloc(w, &w->claim, 8 * (size_t)cap) == cudaSuccess;
     if (!ok) { agb_world_destroy(w); return AGB_OUT_OF_MEMORY; }
+    {
+        TauState ts{};
+        ts.cur = tau_carve(w->tau_blob[0], w->tau_cap);
+        ts.spare = tau_carve(w->tau_blob[1], w->tau_cap);
+        ts.capacity = w->tau_cap;
+        ts.next_id = 1;
+        if (cudaMemcpy(w->tS, &ts, sizeof(ts), cudaMemcpyHostToDevice) != cudaSuccess) {
+            agb_world_destroy(w); return AGB_CUDA_ERROR;
+        }
+    }
     cudaMemset(w->flash_accum, 0, 8 * 4);                 // zeroed once (src/sim/step.cu:58-64)
     if (c.irr_marks) cudaMemset(c.irr_marks, 2, (size_t)w->irr_mark_bytes);   // first sweep: every line
     if (c.irr_stamp_bits) cudaMemset(c.irr_stamp_bits, 0, 4 * (size_t)w->irr_bit_words);
@@ -975,6 +1059,93 @@ agb_status agb_world_export_deposit(agb_world* w, int32_t f, uint64_t* dst, agb_
     if (!w || f < 0 || f >= AGB_FIELD_COUNT || !w->c.g[f].enabled || !dst) return AGB_INVALID_ARGUMENT;
     AGB_CUDA(w, cudaMemcpyAsync(dst, w->gdep[f], 8 * w->c.g[f].count, cudaMemcpyDeviceToHost, s));
     AGB_CUDA(w, cudaStreamSynchronize(s));
+    return AGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// The predator store (taumoeba_spawn and the taumoeba_download_* readers,
+// src/sim/predation.cu:420-574)
+// ---------------------------------------------------------------------------
+namespace {
+agb_status read_tau(agb_world* w, TauState& ts, cudaStream_t s) {
+    AGB_CUDA(w, cudaMemcpyAsync(&ts, w->tS, sizeof(ts), cudaMemcpyDeviceToHost, s));
+    AGB_CUDA(w, cudaStreamSynchronize(s));
+    return AGB_OK;
+}
+// The host arrays of agb_taumoeba with their element sizes, in TauSoA order.
+void tau_host_arrays(const agb_taumoeba* a, void* out[20]) {
+    void* p[20] = {a->id, a->flags, a->x, a->y, a->z, a->vx, a->vy, a->vz, a->dir_x, a->dir_y, a->dir_z,
+                   a->biomass, a->prey_biomass, a->digest_timer, a->tolerance, a->generation, a->rng_state,
+                   a->density_ema, a->run_timer, a->target};
+    for (int k = 0; k < 20; ++k) out[k] = p[k];
+}
+void tau_dev_arrays(const TauSoA& t, void* out[20]) {
+    void* p[20] = {t.id, t.flags, t.x, t.y, t.z, t.vx, t.vy, t.vz, t.dir_x, t.dir_y, t.dir_z, t.biomass,
+                   t.prey_biomass, t.digest_timer, t.tolerance, t.generation, t.rng_state, t.density_ema,
+                   t.run_timer, t.target};
+    for (int k = 0; k < 20; ++k) out[k] = p[k];
+}
+const size_t TAU_WIDTH[20] = {8, 4, 8, 8, 8, 8, 8, 8, 4, 4, 4, 8, 8, 4, 4, 4, 8, 4, 4, 4};
+void set_tau_active(agb_world* w) {
+    if (!w->tau_active) {
+        w->tau_active = true;
+        invalidate_graphs(w);                             // captured ticks lack the predation stage
+    }
+}
+}  // namespace
+
+agb_status agb_world_spawn_taumoeba(agb_world* w, int32_t count, uint64_t seed, agb_stream s) {
+    if (!w || count < 0) return AGB_INVALID_ARGUMENT;
+    if (count == 0) return AGB_OK;
+    TauState ts;
+    agb_status rc = read_tau(w, ts, s);
+    if (rc) return rc;
+    if (ts.count + count > ts.capacity) return fail(w, AGB_CAPACITY_EXCEEDED, "taumoeba spawn exceeds capacity");
+    launch_tau_spawn(w->tS, count, seed, w->taup, s);
+    AGB_CUDA(w, cudaGetLastError());
+    set_tau_active(w);
+    return AGB_OK;
+}
+
+agb_status agb_world_import_taumoeba(agb_world* w, const agb_taumoeba* src, int32_t count, uint64_t next_id,
+                                     agb_stream s) {
+    if (!w || !src || count < 0) return AGB_INVALID_ARGUMENT;
+    if (count > w->tau_cap) return fail(w, AGB_CAPACITY_EXCEEDED, "taumoeba import exceeds capacity");
+    TauState ts;
+    agb_status rc = read_tau(w, ts, s);
+    if (rc) return rc;
+    void* h[20];
+    void* d[20];
+    tau_host_arrays(src, h);
+    tau_dev_arrays(ts.cur, d);
+    for (int k = 0; k < 20; ++k) {
+        if (!h[k]) return AGB_INVALID_ARGUMENT;
+        if (count > 0) AGB_CUDA(w, cudaMemcpyAsync(d[k], h[k], TAU_WIDTH[k] * (size_t)count, cudaMemcpyHostToDevice, s));
+    }
+    ts.count = count;
+    ts.next_id = next_id;
+    AGB_CUDA(w, cudaMemcpyAsync(w->tS, &ts, sizeof(ts), cudaMemcpyHostToDevice, s));
+    AGB_CUDA(w, cudaStreamSynchronize(s));
+    if (count > 0) set_tau_active(w);
+    return AGB_OK;
+}
+
+agb_status agb_world_export_taumoeba(agb_world* w, agb_taumoeba* dst, int32_t max_count, int32_t* count,
+                                     uint64_t* next_id, agb_stream s) {
+    if (!w || !dst || max_count < 0) return AGB_INVALID_ARGUMENT;
+    TauState ts;
+    agb_status rc = read_tau(w, ts, s);
+    if (rc) return rc;
+    const int32_t n = ts.count < max_count ? ts.count : max_count;
+    void* h[20];
+    void* d[20];
+    tau_host_arrays(dst, h);
+    tau_dev_arrays(ts.cur, d);
+    for (int k = 0; k < 20; ++k)
+        if (h[k] && n > 0) AGB_CUDA(w, cudaMemcpyAsync(h[k], d[k], TAU_WIDTH[k] * (size_t)n, cudaMemcpyDeviceToHost, s));
+    AGB_CUDA(w, cudaStreamSynchronize(s));
+    if (count) *count = ts.count;
+    if (next_id) *next_id = ts.next_id;
     return AGB_OK;
 }
 
@@ -1164,6 +1335,7 @@ agb_status agb_world_stage(agb_world* w, int32_t stage, agb_stream s) {
         case AGB_STAGE_FLASH:
             if (w->flash_active) launch_flash(w->S, w->tp.dt, w->flash_power, w->flash_accum, w->blocks, s);
             break;
+        case AGB_STAGE_PREDATION: stage_predation(w, s); break;
         case AGB_STAGE_MOTION: stage_motion(w, s); break;
         case AGB_STAGE_SLOW_FIELDS: stage_slow_fields(w, s); break;
         case AGB_STAGE_LIFECYCLE: stage_lifecycle(w, s); break;
@@ -1194,6 +1366,7 @@ agb_status agb_world_stats(agb_world* w, agb_stats* out, agb_stream s) {
     if (!w || !out) return AGB_INVALID_ARGUMENT;
     refresh_grid_ptrs(w);
     launch_stats(w->S, w->c, w->acc, w->blocks, s);
+    if (w->tau_active) launch_tau_stats(w->tS, w->tau_cap, w->acc, s);
     AGB_CUDA(w, cudaGetLastError());
     AGB_CUDA(w, cudaMemcpyAsync(w->acc_host, w->acc, sizeof(w->acc_host), cudaMemcpyDeviceToHost, s));
     DevState st;
@@ -1232,6 +1405,8 @@ agb_status agb_world_stats(agb_world* w, agb_stats* out, agb_stream s) {
     AGB_CUDA(w, cudaMemcpyAsync(&w->S->divisions_this_window, &zero, sizeof(zero), cudaMemcpyHostToDevice, s));
     AGB_CUDA(w, cudaStreamSynchronize(s));
     r.boil_events = r.max_temp_medium_k >= AGB_WATER_BOILING_POINT ? 1 : 0;
+    r.n_taumoeba = (int32_t)a[11];
+    r.mean_tau_tolerance = a[11] > 0u ? fx(a[6], AGB_DEPOSIT_SCALE_STATS) / (double)a[11] : 0.0;
     *out = r;
     return AGB_OK;
 }

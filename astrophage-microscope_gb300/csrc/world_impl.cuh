@@ -50,6 +50,15 @@ struct agb_world {
     int32_t blocks = 1;
     int walk_lanes = 1;                  // threads sharing one cell's neighbour walk (1, 2, 4, 8)
     bool fuse_cells = false;             // feeding, taxis and forces in one kernel with one walk
+    // The predator store (k_tau.cu): device state, two blobs (compaction
+    // target), per-cell claim words, per-world constants; tau_active once
+    // predators have been placed (the tick then runs the predation stage).
+    TauState* tS = nullptr;
+    void* tau_blob[2] = {nullptr, nullptr};
+    int32_t tau_cap = 0;
+    unsigned long long* claim = nullptr;
+    TauParams taup{};
+    bool tau_active = false;
     bool flash_active = false;           // spin-drive flash armed: the flash stage replaces taxis
     double flash_power = AGB_PETROVA_FLASH_POWER;
     unsigned long long* flash_accum = nullptr;   // imp_x, imp_y, imp_z, energy (fixed point)

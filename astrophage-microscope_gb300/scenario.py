@@ -12,14 +12,12 @@ documented defaults; scope, tools, param_overrides, density_model and
 thermal_bc are parsed and not applied, as there.
 
 The world is duck-typed: anything with the agb.World operations used below
-(spawn with a seed, import_field, set_light, set_flash, flash_audit,
-apply_brush, step, stats, count, export_cells) can be driven, so the same
-scenario runs on the engine and, in the tests, on the CPU oracle.
-
-Not supported, because the engine does not build predation
-(src/sim/predation.cu): Taumoeba populations and their metrics. A scenario
-that needs them raises ScenarioUnsupported from instantiate(); parse()
-accepts it.
+(spawn with a seed, spawn_taumoeba, import_field, set_light, set_flash,
+flash_audit, apply_brush, step, stats, count, export_cells,
+export_taumoeba) can be driven, so the same scenario runs on the engine and,
+in the tests, on the CPU oracle. Every stage a scenario file can name is
+built; ScenarioUnsupported remains for callers that check a scenario against
+a world lacking one (a world without an N2 grid cannot take N2 stimuli).
 """
 import json
 import math
@@ -40,7 +38,7 @@ class ScenarioError(Exception):
 
 
 class ScenarioUnsupported(Exception):
-    """The scenario needs a stage the engine does not build (predation)."""
+    """The scenario needs something the world it is given cannot do."""
 
 
 # contracts/scenario_v3.h enums (values as there).
@@ -59,7 +57,6 @@ METRICS = ["awake_fraction", "medium_temp_mean", "medium_temp_max", "boil_event_
            "population_dead", "mean_charge", "total_energy_j", "mean_tau_tolerance", "max_tau_tolerance",
            "charge_depth_correlation", "charge_height_correlation", "rise_velocity_empty",
            "fall_velocity_full", "doubling_time_s", "impulse_per_cycle"]
-TAU_METRICS = {"mean_tau_tolerance", "max_tau_tolerance"}
 MAX_LIGHT_SOURCES, MAX_POPULATIONS, MAX_ACCEPT_CHECKS, MAX_STIMULI, MAX_OVERRIDES = 8, 8, 16, 16, 32
 
 TOOLS = {"heat": 1 << 0, "chill": 1 << 1, "illuminate": 1 << 2, "inject_co2": 1 << 3, "inject_n2": 1 << 4,
@@ -333,20 +330,24 @@ def clock_rates(preset, physics=1.0, biology=1.0):
     return physics, biology
 
 
-def unsupported(s):
-    """Why the engine cannot run `s`, or None."""
-    if any(p.kind == TAUMOEBA and p.count > 0 for p in s.populations):
-        return "Taumoeba populations (predation) are not built"
-    if any(c.metric in TAU_METRICS for c in s.accept):
-        return "Taumoeba metrics (predation) are not built"
+def unsupported(s, grids=None):
+    """Why `s` cannot run on a world with these grids, or None."""
+    if grids is not None and _n2_grid_missing(grids) and (
+            s.n2_init != 0.0 or any(d.kind in (INJECT_N2, SET_N2) for d in s.drive)):
+        return "the scenario drives N2 and the world has no N2 grid"
     return None
+
+
+def _n2_grid_missing(grids):
+    g = grids.get(agb.FIELD_N2)
+    return g is not None and g.nx <= 0
 
 
 def world_desc(s, grids=None):
     """scenario_instantiate's WorldDesc (src/sim/scenario.cpp:341-357) as an
     agb.WorldDesc. `grids` optionally replaces the default field grids
     (agb.GridDesc per field), e.g. to run a scenario at smaller resolution."""
-    cap, _tau = capacities(s)
+    cap, tau_cap = capacities(s)   # the predator store is sized too (scenario.cpp:344)
     d = agb.default_desc(capacity=cap, seed=s.seed, co2_init=s.co2_init)
     d.chamber_w, d.chamber_h, d.chamber_d = s.chamber_w, s.chamber_h, s.chamber_d
     d.boundary_x, d.boundary_y = s.boundary_x, s.boundary_y
@@ -355,6 +356,8 @@ def world_desc(s, grids=None):
     d.store_disposition = s.store_disposition
     d.thermal_enabled = 1 if s.thermal_active else 0
     d.compaction_enabled = 1 if s.compaction else 0
+    d.tau_capacity = tau_cap
+    d.tau_compaction_enabled = 1 if s.tau_compaction else 0
     if grids is not None:
         for f, g in grids.items():
             d.grid[f] = g
@@ -404,7 +407,7 @@ def instantiate(s, make_world=None, grids=None):
     fills that differ from creation, one spawn per population with seeds
     seed, seed + 1, ... (populations of count <= 0 take no seed), the light
     and the clock. `make_world(desc)` builds the world (agb.World by default)."""
-    why = unsupported(s)
+    why = unsupported(s, grids)
     if why:
         raise ScenarioUnsupported(why)
     d = world_desc(s, grids)
@@ -417,7 +420,10 @@ def instantiate(s, make_world=None, grids=None):
     for p in s.populations:
         if p.count <= 0:
             continue
-        w.spawn(_spawn_of(p, p.count), seed=seed)
+        if p.kind == TAUMOEBA:
+            w.spawn_taumoeba(p.count, seed)
+        else:
+            w.spawn(_spawn_of(p, p.count), seed=seed)
         seed = (seed + 1) & 0xFFFFFFFFFFFFFFFF
     return Driven(w, s, d)
 
@@ -641,6 +647,12 @@ def metric_measure(metric, fin, agg, dw):
         return agg.fall_velocity_full
     if metric == "doubling_time_s":
         return _doubling_time(agg, dw.biology_rate)
+    if metric == "mean_tau_tolerance":
+        return fin.mean_tau_tolerance
+    if metric == "max_tau_tolerance":
+        tau, _nid = dw.world.export_taumoeba()
+        alive = (tau["flags"] & agb.FLAG_OCCUPIED).astype(bool) & (tau["flags"] & agb.FLAG_ALIVE).astype(bool)
+        return float(np.max(tau["tolerance"][alive].astype(np.float64))) if alive.any() else 0.0
     if metric == "impulse_per_cycle":
         imp, dis = dw.world.flash_audit()
         return imp * agb.C_LIGHT / dis if dis > 0.0 else 0.0
@@ -749,7 +761,7 @@ def run_assert(s, dw, ticks=None, csv_path=None, graph=True, out=None):
 def main(argv=None):
     """`scenario.py --scenario ID|PATH [--scenarios-dir DIR] [--assert] [--ticks N]
     [--csv PATH]`: headless's scenario mode. Exit status 0 on ACCEPT (or a run
-    without --assert), 1 on REJECT, 2 on a bad scenario, 3 when unsupported (predation)."""
+    without --assert), 1 on REJECT, 2 on a bad scenario, 3 when the world cannot run it."""
     import argparse
     ap = argparse.ArgumentParser(description=main.__doc__)
     ap.add_argument("--scenario", required=True)

@@ -122,6 +122,11 @@ typedef struct agb_world_desc {
     int32_t compaction_period;                /* ticks between compaction checks; 1 = reference */
     int32_t trap_slot;                        /* optical trap (World::trap_*); -1 = off */
     double trap_x, trap_y, trap_stiffness;
+    /* The predator store (WorldDesc::tau_capacity, MotionConfig::tau_compaction_enabled,
+     * src/sim/world.cuh:76-82): capacity, 0 = AGB_DEFAULT_TAUMOEBA; stable compaction of
+     * dead predators. */
+    int32_t tau_capacity;
+    int32_t tau_compaction_enabled;
 } agb_world_desc;
 
 /* Host view of the 25 SoA arrays of contracts/cell_store_v1.h:42-75, field for
@@ -201,7 +206,8 @@ enum {
     AGB_STAGE_LIFECYCLE = 6,   /* lifecycle_step, src/sim/lifecycle.cu:208-294 */
     AGB_STAGE_COMPACT = 7,     /* cell_store_compact, src/sim/cell_store.cu:414-456 */
     AGB_STAGE_CLOCK = 8,       /* ++tick; sim_time += dt, src/sim/step.cu:182-183 */
-    AGB_STAGE_FLASH = 9        /* flash_step, src/sim/flash.cu:59-67 (a no-op unless armed) */
+    AGB_STAGE_FLASH = 9,       /* flash_step, src/sim/flash.cu:59-67 (a no-op unless armed) */
+    AGB_STAGE_PREDATION = 10   /* predation_step, src/sim/predation.cu:434-484 */
 };
 
 /* Snapshots (contracts/snapshot_v1.h:17-63): file = header, then the body the
@@ -336,6 +342,34 @@ agb_status agb_world_export_cells(agb_world* w, agb_cells* dst, int32_t max_coun
                                   int32_t* count, uint64_t* next_id, agb_stream s);
 /* Device pointers of the SoA (the reference's CellStore::view); count via agb_world_count. */
 agb_status agb_world_device_cells(agb_world* w, agb_cells* dev);
+
+/* Host view of the predator store's 20 arrays (TaumoebaStore, src/sim/predation.cuh:85-105),
+ * field for field, in the snapshot's order. Any pointer may be NULL on export. */
+typedef struct agb_taumoeba {
+    uint64_t* id;
+    uint32_t* flags;
+    double *x, *y, *z;
+    double *vx, *vy, *vz;
+    float *dir_x, *dir_y, *dir_z;
+    double* biomass;
+    double* prey_biomass;
+    float* digest_timer;
+    float* tolerance;
+    uint32_t* generation;
+    uint64_t* rng_state;
+    float* density_ema;
+    float* run_timer;
+    int32_t* target;
+} agb_taumoeba;
+/* taumoeba_spawn (src/sim/predation.cu:420-432): append `count` predators placed uniformly,
+ * streams seeded from (splitmix64(seed), id). Capacity exceeded is an error. */
+agb_status agb_world_spawn_taumoeba(agb_world* w, int32_t count, uint64_t seed, agb_stream s);
+/* Replace the predator store with `count` predators; next_id is the next predator id. */
+agb_status agb_world_import_taumoeba(agb_world* w, const agb_taumoeba* src, int32_t count, uint64_t next_id,
+                                     agb_stream s);
+/* Copy up to max_count predators out (the taumoeba_download_* readers). Syncs. */
+agb_status agb_world_export_taumoeba(agb_world* w, agb_taumoeba* dst, int32_t max_count, int32_t* count,
+                                     uint64_t* next_id, agb_stream s);
 /* One call per host-driven step: import `count` cells from host arrays, run
  * `ticks` ticks (one graph launch), export into host arrays (at most max_out
  * per array) and synchronise once. With device-accessible host arrays

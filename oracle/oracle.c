@@ -298,6 +298,29 @@ typedef struct {
     float *taxis_memory, *run_timer, *t_local, *irradiance, *co2_local, *n2_local;
 } soa;
 
+/* TaumoebaStore (src/sim/predation.cuh:85-105): the predator's 20 arrays. */
+typedef struct {
+    uint64_t* id;
+    uint32_t* flags;
+    double *x, *y, *z, *vx, *vy, *vz;
+    float *dir_x, *dir_y, *dir_z;
+    double *biomass, *prey_biomass;
+    float *digest_timer, *tolerance;
+    uint32_t* generation;
+    uint64_t* rng_state;
+    float *density_ema, *run_timer;
+    int32_t* target;
+} tau_soa;
+static const size_t TAU_SZ[20] = {8, 4, 8, 8, 8, 8, 8, 8, 4, 4, 4, 8, 8, 4, 4, 4, 8, 4, 4, 4};
+static void tau_ptrs(tau_soa* t, void** p[20]) {
+    void** q[20] = {(void**)&t->id, (void**)&t->flags, (void**)&t->x, (void**)&t->y, (void**)&t->z,
+                    (void**)&t->vx, (void**)&t->vy, (void**)&t->vz, (void**)&t->dir_x, (void**)&t->dir_y,
+                    (void**)&t->dir_z, (void**)&t->biomass, (void**)&t->prey_biomass, (void**)&t->digest_timer,
+                    (void**)&t->tolerance, (void**)&t->generation, (void**)&t->rng_state,
+                    (void**)&t->density_ema, (void**)&t->run_timer, (void**)&t->target};
+    memcpy(p, q, sizeof(q));
+}
+
 struct orc_world {
     agb_world_desc d;
     soa c;
@@ -324,6 +347,11 @@ struct orc_world {
     int flash_active;
     double flash_power;
     uint64_t flash_accum[4];
+    /* the predator store, its next id and the per-cell claim words */
+    tau_soa t;
+    int32_t tau_count, tau_capacity;
+    uint64_t tau_next_id;
+    uint64_t* claim;
 };
 
 static void soa_sizes(size_t sz[25]) {
@@ -366,6 +394,10 @@ void orc_world_destroy(orc_world* w) {
     free(w->tmp_k); free(w->tmp_v); free(w->bstart); free(w->bend);
     free(w->fx); free(w->fy); free(w->fz); free(w->co2_demand);
     free(w->scan_flags); free(w->prefix); free(w->compact_src); free(w->scratch);
+    void** tp[20];
+    tau_ptrs(&w->t, tp);
+    for (int k = 0; k < 20; ++k) free(*tp[k]);
+    free(w->claim);
     free(w);
 }
 
@@ -391,6 +423,20 @@ int orc_world_create(const agb_world_desc* d, orc_world** out) {
     for (int f = 0; f < AGB_FIELD_COUNT; ++f) {
         const int rc = grid_init(&w->g[f], &d->grid[f], d->chamber_w, d->chamber_d);
         if (rc) { orc_world_destroy(w); return rc; }
+    }
+    /* taumoeba_create (predation.cu:306-418) */
+    w->tau_capacity = d->tau_capacity > 0 ? d->tau_capacity : AGB_DEFAULT_TAUMOEBA;
+    if (w->tau_capacity > AGB_MAX_TAUMOEBA) { orc_world_destroy(w); return AGB_INVALID_ARGUMENT; }
+    w->tau_next_id = 1;
+    {
+        void** tp[20];
+        tau_ptrs(&w->t, tp);
+        for (int k = 0; k < 20; ++k) {
+            *tp[k] = calloc((size_t)w->tau_capacity, TAU_SZ[k]);
+            if (!*tp[k]) { orc_world_destroy(w); return AGB_OUT_OF_MEMORY; }
+        }
+        w->claim = (uint64_t*)calloc((size_t)d->capacity, 8);
+        if (!w->claim) { orc_world_destroy(w); return AGB_OUT_OF_MEMORY; }
     }
     const double cell = d->hash_cell_size > 0.0 ? d->hash_cell_size
                                                 : AGB_HASH_CELL_FACTOR * AGB_CELL_DIAMETER;
@@ -1361,6 +1407,263 @@ static void flash_step(orc_world* w, double dt) {
     }
 }
 
+/* ------------------------------------------------------------------------- */
+/* Taumoeba, the predator: src/sim/predation.cu, src/sim/predation.cuh        */
+/* ------------------------------------------------------------------------- */
+static double water_viscosity(double t) { return AGB_VF_A * exp(AGB_VF_B / (t - AGB_VF_C)); }   /* integrator.cuh:29-31 */
+static void gaussian3(pcg32* r, double* x, double* y, double* z) {   /* rng.cuh:111-117 */
+    double a, b, c, d;
+    gaussian_pair(r, &a, &b);
+    gaussian_pair(r, &c, &d);
+    (void)d;
+    *x = a; *y = b; *z = c;
+}
+
+/* spawn_kernel + taumoeba_spawn (predation.cu:33-74, 420-432). */
+int orc_world_spawn_taumoeba(orc_world* w, int32_t count, uint64_t seed) {
+    if (count <= 0) return 0;
+    if (w->tau_count + count > w->tau_capacity) return AGB_CAPACITY_EXCEEDED;
+    tau_soa* t = &w->t;
+    const double a = AGB_TAU_RADIUS;
+    for (int32_t i = 0; i < count; ++i) {
+        const int32_t slot = w->tau_count + i;
+        const uint64_t id = w->tau_next_id + (uint64_t)i;
+        pcg32 r = cell_rng(cell_rng_init(splitmix64(seed), id), id);
+        t->x[slot] = uniform_range(&r, -0.5 * w->d.chamber_w + a, 0.5 * w->d.chamber_w - a);
+        t->y[slot] = uniform_range(&r, -0.5 * w->d.chamber_h + a, 0.5 * w->d.chamber_h - a);
+        t->z[slot] = uniform_range(&r, -0.5 * w->d.chamber_d + a, 0.5 * w->d.chamber_d - a);
+        t->vx[slot] = 0.0; t->vy[slot] = 0.0; t->vz[slot] = 0.0;
+        double dx, dy, dz;
+        gaussian3(&r, &dx, &dy, &dz);
+        const vec3 dir = vnormalize(v3(dx, dy, dz));
+        t->dir_x[slot] = (float)dir.x; t->dir_y[slot] = (float)dir.y; t->dir_z[slot] = (float)dir.z;
+        t->id[slot] = id;
+        t->flags[slot] = AGB_FLAG_OCCUPIED | AGB_FLAG_ALIVE;
+        t->biomass[slot] = AGB_TAU_MASS_DRY;
+        t->prey_biomass[slot] = 0.0;
+        t->digest_timer[slot] = 0.0f;
+        t->tolerance[slot] = (float)AGB_TAU_N2_TOLERANCE_INIT;
+        t->generation[slot] = 0u;
+        t->rng_state[slot] = r.state;
+        t->density_ema[slot] = 0.0f;
+        t->run_timer[slot] = 0.0f;
+        t->target[slot] = -1;
+    }
+    w->tau_count += count;
+    w->tau_next_id += (uint64_t)count;
+    return 0;
+}
+
+/* predation_step (predation.cu:434-484): hunt, resolve, nitrogen, division,
+ * compaction, each pass over the predators in slot order. */
+static void predation_step(orc_world* w, double dt) {
+    const int32_t n = w->tau_count;
+    if (n <= 0) return;
+    tau_soa* t = &w->t;
+    soa* c = &w->c;
+    const double dt_bio = dt * w->biology_rate;
+    memset(w->claim, 0xFF, 8 * (size_t)w->capacity);
+    const double t_amb = w->d.ambient_temp;
+    const double gamma = 6.0 * AGB_PI * water_viscosity(t_amb) * AGB_TAU_RADIUS;   /* tau_drag */
+    const ou_coef oc = ou_coefficients(AGB_TAU_MASS, gamma, t_amb, dt);
+    const double rr = (AGB_TAU_RADIUS + AGB_CELL_RADIUS) * (AGB_TAU_RADIUS + AGB_CELL_RADIUS);
+    for (int32_t i = 0; i < n; ++i) {                      /* hunt_kernel, predation.cu:80-158 */
+        const uint32_t f = t->flags[i];
+        if (!(f & AGB_FLAG_OCCUPIED) || !(f & AGB_FLAG_ALIVE)) continue;
+        vec3 pos = v3(t->x[i], t->y[i], t->z[i]);
+        const int digesting = t->digest_timer[i] > 0.0f;
+        int prey_count = 0;
+        int32_t prey = -1;
+        int32_t gx, gy, gz;
+        hash_coords(w, pos.x, pos.y, pos.z, &gx, &gy, &gz);
+        for (int32_t dz = -1; dz <= 1; ++dz) {             /* ASTRO_FOR_EACH_NEIGHBOUR, hash.cuh:88-111 */
+            const int32_t cz = gz + dz;
+            if (cz < 0 || cz >= w->hnz) continue;
+            for (int32_t dy = -1; dy <= 1; ++dy) {
+                const int32_t cy = gy + dy;
+                if (cy < 0 || cy >= w->hny) continue;
+                for (int32_t dx = -1; dx <= 1; ++dx) {
+                    const int32_t cx = gx + dx;
+                    if (cx < 0 || cx >= w->hnx) continue;
+                    const uint32_t b = hash_index(w, cx, cy, cz);
+                    for (int32_t k = w->bstart[b]; k < w->bend[b]; ++k) {
+                        const int32_t j = (int32_t)w->vals_sorted[k];
+                        const uint32_t cf = c->flags[j];
+                        if (!(cf & AGB_FLAG_OCCUPIED) || !(cf & AGB_FLAG_ALIVE)) continue;
+                        ++prey_count;
+                        const vec3 d = vsub(pos, v3(c->x[j], c->y[j], c->z[j]));
+                        if (prey < 0 && vdot(d, d) < rr) prey = j;
+                    }
+                }
+            }
+        }
+        if (!digesting && prey >= 0) {
+            t->target[i] = prey;
+            if (t->id[i] < w->claim[prey]) w->claim[prey] = t->id[i];
+        } else {
+            t->target[i] = -1;
+        }
+        pcg32 rng = cell_rng(t->rng_state[i], t->id[i]);
+        float ema = t->density_ema[i];
+        float run = t->run_timer[i];
+        vec3 dir = v3(t->dir_x[i], t->dir_y[i], t->dir_z[i]);
+        const double alpha = -expm1(-dt / AGB_TAXIS_MEMORY_TIME);   /* tau_should_tumble, predation.cuh:36-41 */
+        const double delta = (double)(float)prey_count - (double)ema;
+        ema = (float)(ema + alpha * delta);
+        if (!(delta > 0.0 && run < AGB_TAXIS_RUN_MAX)) {
+            double gx3, gy3, gz3;
+            gaussian3(&rng, &gx3, &gy3, &gz3);
+            dir = vnormalize(v3(gx3, gy3, gz3));
+            run = 0.0f;
+        } else {
+            run += (float)dt;
+        }
+        t->density_ema[i] = ema;
+        t->run_timer[i] = run;
+        t->dir_x[i] = (float)dir.x; t->dir_y[i] = (float)dir.y; t->dir_z[i] = (float)dir.z;
+        double vel[3] = {t->vx[i], t->vy[i], t->vz[i]};
+        double z[6];
+        gaussian_pair(&rng, &z[0], &z[1]);                 /* integrate_cell, integrator.cuh:159-169 */
+        gaussian_pair(&rng, &z[2], &z[3]);
+        gaussian_pair(&rng, &z[4], &z[5]);
+        ou_advance_axis(&pos.x, &vel[0], dir.x * AGB_TAU_CRAWL_THRUST, gamma, &oc, dt, w->d.thermal_noise, z[0], z[1]);
+        ou_advance_axis(&pos.y, &vel[1], dir.y * AGB_TAU_CRAWL_THRUST, gamma, &oc, dt, w->d.thermal_noise, z[2], z[3]);
+        ou_advance_axis(&pos.z, &vel[2], dir.z * AGB_TAU_CRAWL_THRUST, gamma, &oc, dt, w->d.thermal_noise, z[4], z[5]);
+        t->rng_state[i] = rng.state;
+        apply_boundary_axis(&pos.x, &vel[0], 0.5 * w->d.chamber_w, AGB_TAU_RADIUS, w->d.boundary_x);
+        apply_boundary_axis(&pos.y, &vel[1], 0.5 * w->d.chamber_h, AGB_TAU_RADIUS, w->d.boundary_y);
+        apply_boundary_axis(&pos.z, &vel[2], 0.5 * w->d.chamber_d, AGB_TAU_RADIUS, AGB_WALL_REFLECTING);
+        t->x[i] = pos.x; t->y[i] = pos.y; t->z[i] = pos.z;
+        t->vx[i] = vel[0]; t->vy[i] = vel[1]; t->vz[i] = vel[2];
+        if (digesting) {
+            float dg = t->digest_timer[i] - (float)dt_bio;
+            if (dg <= 0.0f) {
+                t->biomass[i] += t->prey_biomass[i] * AGB_TAU_BIOMASS_YIELD;
+                t->prey_biomass[i] = 0.0;
+                dg = 0.0f;
+            }
+            t->digest_timer[i] = dg;
+        }
+    }
+    for (int32_t i = 0; i < n; ++i) {                      /* resolve_kernel, predation.cu:160-182 */
+        const int32_t prey = t->target[i];
+        if (prey < 0 || w->claim[prey] != t->id[i]) continue;
+        const uint32_t cf = c->flags[prey];
+        if (!(cf & AGB_FLAG_OCCUPIED) || !(cf & AGB_FLAG_ALIVE)) continue;
+        c->flags[prey] = cf & ~AGB_FLAG_ALIVE;
+        c->death_cause[prey] = AGB_DEATH_PREDATED;
+        c->emit_power[prey] = 0.0f;
+        c->energy[prey] = w->d.store_disposition == AGB_STORE_RETAIN ? c->energy[prey] : 0.0;   /* corpse_energy */
+        t->digest_timer[i] = (float)AGB_TAU_DIGEST_TIME;
+        t->prey_biomass[i] = c->biomass[prey];
+    }
+    const grid* n2 = &w->g[AGB_FIELD_N2];
+    for (int32_t i = 0; i < n; ++i) {                      /* nitrogen_kernel, predation.cu:189-205 */
+        const uint32_t f = t->flags[i];
+        if (!(f & AGB_FLAG_OCCUPIED) || !(f & AGB_FLAG_ALIVE)) continue;
+        pcg32 rng = cell_rng(t->rng_state[i], t->id[i]);
+        const double u = uniform01d(&rng);
+        t->rng_state[i] = rng.state;
+        const double n2_local = n2->enabled ? (double)grid_sample(n2, (float)t->x[i], (float)t->y[i], (float)t->z[i]) : 0.0;
+        const double thr = AGB_TAU_N2_LETHAL_CONC * (1.0 + (double)t->tolerance[i] * AGB_TAU_N2_TOLERANCE_K);
+        const double h = n2_local - thr;
+        const double hazard = h > 0.0 ? h : 0.0;
+        if (u < -expm1(-hazard * AGB_TAU_N2_HAZARD_RATE * dt_bio)) t->flags[i] = f & ~AGB_FLAG_ALIVE;
+    }
+    /* tau_mark_kernel + the prefix sum + tau_divide_kernel (predation.cu:211-284, 458-477) */
+    int32_t births = 0, deads = 0;
+    for (int32_t i = 0; i < n; ++i) {
+        const uint32_t f = t->flags[i];
+        const int occ = (f & AGB_FLAG_OCCUPIED) != 0u, alive = (f & AGB_FLAG_ALIVE) != 0u;
+        if (occ && !alive) ++deads;
+        if (!(occ && alive) || !(t->biomass[i] >= AGB_TAU_DIVIDE_BIOMASS)) continue;
+        const int32_t pre = births++;
+        const int32_t slot = n + pre;
+        if (slot >= w->tau_capacity) continue;
+        const uint64_t did = w->tau_next_id + (uint64_t)pre;
+        const double half = 0.5 * t->biomass[i];
+        t->biomass[i] = half;
+        t->biomass[slot] = half;
+        pcg32 dr = cell_rng(pcg_split(t->rng_state[i], did), did);
+        const double mutation = gaussian(&dr);
+        double tol = (double)t->tolerance[i] + AGB_TAU_MUTATION_SIGMA * mutation;
+        tol = tol < 0.0 ? 0.0 : (tol > 1.0 ? 1.0 : tol);
+        t->tolerance[slot] = (float)tol;
+        t->rng_state[slot] = dr.state;
+        t->generation[slot] = t->generation[i] + 1u;
+        double ax, ay, az;
+        division_axis(did, &ax, &ay, &az);
+        const double a = AGB_TAU_RADIUS;
+        t->x[slot] = t->x[i] + a * ax;  t->x[i] -= a * ax;
+        t->y[slot] = t->y[i] + a * ay;  t->y[i] -= a * ay;
+        t->z[slot] = t->z[i] + a * az;  t->z[i] -= a * az;
+        const double hx = 0.5 * w->d.chamber_w - a, hy = 0.5 * w->d.chamber_h - a, hz = 0.5 * w->d.chamber_d - a;
+        t->x[slot] = clampd(t->x[slot], -hx, hx); t->y[slot] = clampd(t->y[slot], -hy, hy);
+        t->z[slot] = clampd(t->z[slot], -hz, hz);
+        t->x[i] = clampd(t->x[i], -hx, hx); t->y[i] = clampd(t->y[i], -hy, hy); t->z[i] = clampd(t->z[i], -hz, hz);
+        t->id[slot] = did;
+        t->flags[slot] = t->flags[i];
+        t->vx[slot] = t->vx[i]; t->vy[slot] = t->vy[i]; t->vz[slot] = t->vz[i];
+        t->dir_x[slot] = t->dir_x[i]; t->dir_y[slot] = t->dir_y[i]; t->dir_z[slot] = t->dir_z[i];
+        t->prey_biomass[slot] = 0.0;
+        t->digest_timer[slot] = 0.0f;
+        t->density_ema[slot] = 0.0f;
+        t->run_timer[slot] = 0.0f;
+        t->target[slot] = -1;
+    }
+    if (n + births > w->tau_capacity) births = w->tau_capacity - n;
+    if (births > 0) {
+        w->tau_next_id += (uint64_t)births;
+        w->tau_count += births;
+    }
+    if (w->d.tau_compaction_enabled && deads > 0) {         /* taumoeba_store_compact, predation.cu:486-521 */
+        void** tp[20];
+        tau_ptrs(t, tp);
+        int32_t live = 0;
+        for (int32_t i = 0; i < w->tau_count; ++i) {
+            const uint32_t f = t->flags[i];
+            if (!((f & AGB_FLAG_OCCUPIED) && (f & AGB_FLAG_ALIVE))) continue;
+            if (live != i)
+                for (int k = 0; k < 20; ++k) {
+                    unsigned char* arr = (unsigned char*)*tp[k];
+                    memmove(arr + TAU_SZ[k] * (size_t)live, arr + TAU_SZ[k] * (size_t)i, TAU_SZ[k]);
+                }
+            ++live;
+        }
+        w->tau_count = live;
+    }
+}
+
+int orc_world_import_taumoeba(orc_world* w, const agb_taumoeba* src, int32_t count, uint64_t next_id) {
+    if (count < 0 || count > w->tau_capacity) return AGB_CAPACITY_EXCEEDED;
+    void* h[20] = {src->id, src->flags, src->x, src->y, src->z, src->vx, src->vy, src->vz, src->dir_x, src->dir_y,
+                   src->dir_z, src->biomass, src->prey_biomass, src->digest_timer, src->tolerance, src->generation,
+                   src->rng_state, src->density_ema, src->run_timer, src->target};
+    void** tp[20];
+    tau_ptrs(&w->t, tp);
+    for (int k = 0; k < 20; ++k) {
+        if (!h[k]) return AGB_INVALID_ARGUMENT;
+        memcpy(*tp[k], h[k], TAU_SZ[k] * (size_t)count);
+    }
+    w->tau_count = count;
+    w->tau_next_id = next_id;
+    return 0;
+}
+
+int orc_world_export_taumoeba(orc_world* w, agb_taumoeba* dst, int32_t max_count, int32_t* count, uint64_t* next_id) {
+    const int32_t n = w->tau_count < max_count ? w->tau_count : max_count;
+    void* h[20] = {dst->id, dst->flags, dst->x, dst->y, dst->z, dst->vx, dst->vy, dst->vz, dst->dir_x, dst->dir_y,
+                   dst->dir_z, dst->biomass, dst->prey_biomass, dst->digest_timer, dst->tolerance, dst->generation,
+                   dst->rng_state, dst->density_ema, dst->run_timer, dst->target};
+    void** tp[20];
+    tau_ptrs(&w->t, tp);
+    for (int k = 0; k < 20; ++k)
+        if (h[k] && n > 0) memcpy(h[k], *tp[k], TAU_SZ[k] * (size_t)n);
+    if (count) *count = w->tau_count;
+    if (next_id) *next_id = w->tau_next_id;
+    return 0;
+}
+
 int orc_world_set_flash(orc_world* w, int32_t active, double power) {
     w->flash_active = active != 0;
     w->flash_power = power > 0.0 ? power : AGB_PETROVA_FLASH_POWER;
@@ -1390,6 +1693,7 @@ int orc_world_stage(orc_world* w, int32_t stage) {
         case AGB_STAGE_COMPACT: return compact(w);
         case AGB_STAGE_CLOCK: ++w->tick; w->sim_time += dt; return 0;
         case AGB_STAGE_FLASH: flash_step(w, dt); return 0;
+        case AGB_STAGE_PREDATION: predation_step(w, dt); return 0;
     }
     return AGB_INVALID_ARGUMENT;
 }
@@ -1406,6 +1710,7 @@ int orc_world_step(orc_world* w, int32_t ticks) {
         motion_step(w, dt);
         rc = slow_fields(w, dt);
         if (rc) return rc;
+        predation_step(w, dt);                                            /* step.cu:173-176 */
         lifecycle_step(w, dt);
         ++w->tick;
         w->sim_time += dt;
@@ -1454,8 +1759,16 @@ int orc_world_stats(orc_world* w, agb_stats* s) {
         for (int64_t i = 0; i < C->count; ++i) co2 += (uint64_t)to_fixed((double)C->value[i], AGB_STATS_SCALE_FIELD);
     if (N->enabled)
         for (int64_t i = 0; i < N->count; ++i) n2 += (uint64_t)to_fixed((double)N->value[i], AGB_STATS_SCALE_FIELD);
-    const uint64_t acc[12] = {energy, temp_cell, temp_medium, co2, n2, max_temp, 0,
-                              n_alive, n_dead, n_awake, n_dormant, 0};
+    uint64_t tau_tol = 0;
+    uint32_t n_tau = 0;
+    for (int32_t i = 0; i < w->tau_count; ++i) {           /* stats_taumoeba_kernel, :65-73 */
+        const uint32_t f = w->t.flags[i];
+        if (!(f & AGB_FLAG_OCCUPIED) || !(f & AGB_FLAG_ALIVE)) continue;
+        ++n_tau;
+        tau_tol += (uint64_t)to_fixed((double)w->t.tolerance[i], AGB_DEPOSIT_SCALE_STATS);
+    }
+    const uint64_t acc[12] = {energy, temp_cell, temp_medium, co2, n2, max_temp, tau_tol,
+                              n_alive, n_dead, n_awake, n_dormant, n_tau};
     memcpy(w->accum, acc, sizeof(acc));
     memset(s, 0, sizeof(*s));                              /* world_stats, :102-153 */
     s->tick = w->tick;
@@ -1466,8 +1779,8 @@ int orc_world_stats(orc_world* w, agb_stats* s) {
     s->n_dead = (int32_t)n_dead;
     s->n_awake = (int32_t)n_awake;
     s->n_dormant = (int32_t)n_dormant;
-    s->n_taumoeba = 0;
-    s->mean_tau_tolerance = 0.0;
+    s->n_taumoeba = (int32_t)n_tau;
+    s->mean_tau_tolerance = n_tau > 0u ? from_fixed(tau_tol, AGB_DEPOSIT_SCALE_STATS) / n_tau : 0.0;
     s->total_energy_j = from_fixed(energy, AGB_DEPOSIT_SCALE_STATS);
     s->mean_charge = (n_alive + n_dead) > 0u
         ? s->total_energy_j / ((n_alive + n_dead) * AGB_CELL_ENERGY_MAX) : 0.0;
@@ -1503,7 +1816,7 @@ uint64_t orc_fnv1a64(const void* data, uint64_t n, uint64_t h) {
     return h;
 }
 
-/* snapshot_to_bytes: header + [overrides][25 cell arrays][no predators][T, CO2, N2].
+/* snapshot_to_bytes: header + [overrides][25 cell arrays][20 predator arrays][T, CO2, N2].
  * Returns the byte count; writes into out when cap suffices. */
 int64_t orc_world_snapshot(orc_world* w, const char* scenario_id, char* out, int64_t cap) {
     const int stored[3] = {AGB_FIELD_TEMPERATURE, AGB_FIELD_CO2, AGB_FIELD_N2};
@@ -1515,6 +1828,7 @@ int64_t orc_world_snapshot(orc_world* w, const char* scenario_id, char* out, int
     const int has_override = ov_power + ov_quota;
     int64_t body = (int64_t)has_override * (int64_t)sizeof(agb_param_override);
     for (int k = 0; k < 25; ++k) body += (int64_t)sz[k] * w->count;
+    for (int k = 0; k < 20; ++k) body += (int64_t)TAU_SZ[k] * w->tau_count;
     for (int k = 0; k < 3; ++k)
         if (w->g[stored[k]].enabled) body += 4 * (int64_t)w->g[stored[k]].count;
     const int64_t total = (int64_t)sizeof(agb_snapshot_header) + body;
@@ -1534,6 +1848,15 @@ int64_t orc_world_snapshot(orc_world* w, const char* scenario_id, char* out, int
         if (b) memcpy(q, *(void**)p[k], b);
         q += b;
     }
+    {
+        void** tp[20];
+        tau_ptrs(&w->t, tp);
+        for (int k = 0; k < 20; ++k) {
+            const size_t b = TAU_SZ[k] * (size_t)w->tau_count;
+            if (b) memcpy(q, *tp[k], b);
+            q += b;
+        }
+    }
     for (int k = 0; k < 3; ++k) {
         const grid* g = &w->g[stored[k]];
         if (!g->enabled) continue;
@@ -1549,7 +1872,8 @@ int64_t orc_world_snapshot(orc_world* w, const char* scenario_id, char* out, int
     h.sim_time_s = w->sim_time;
     h.cell_count = w->count;
     h.cell_capacity = w->capacity;
-    h.taumoeba_capacity = AGB_DEFAULT_TAUMOEBA;   /* the reference world's default store, empty */
+    h.taumoeba_count = w->tau_count;
+    h.taumoeba_capacity = w->tau_capacity;
     h.n_temp = w->g[AGB_FIELD_TEMPERATURE].enabled ? w->g[AGB_FIELD_TEMPERATURE].nx : 0;
     h.n_co2 = w->g[AGB_FIELD_CO2].enabled ? w->g[AGB_FIELD_CO2].nx : 0;
     h.n_n2 = w->g[AGB_FIELD_N2].enabled ? w->g[AGB_FIELD_N2].nx : 0;

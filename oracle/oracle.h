@@ -34,6 +34,9 @@ int orc_world_spawn(orc_world* w, const agb_spawn* p);
 int orc_world_spawn_seeded(orc_world* w, const agb_spawn* p, uint64_t seed);
 int orc_world_set_light(orc_world* w, const agb_light* light);
 int orc_world_set_flash(orc_world* w, int32_t active, double power);
+int orc_world_spawn_taumoeba(orc_world* w, int32_t count, uint64_t seed);
+int orc_world_import_taumoeba(orc_world* w, const agb_taumoeba* src, int32_t count, uint64_t next_id);
+int orc_world_export_taumoeba(orc_world* w, agb_taumoeba* dst, int32_t max_count, int32_t* count, uint64_t* next_id);
 int orc_world_flash_audit(orc_world* w, double* impulse_ns, double* discharged_j);
 int orc_world_import_cells(orc_world* w, const agb_cells* src, int32_t count, uint64_t next_id);
 int orc_world_export_cells(orc_world* w, agb_cells* dst, int32_t max_count, int32_t* count,

@@ -54,6 +54,8 @@ struct RefParams {
     float light_dir_x, light_dir_y, light_irradiance, ambient_irradiance;
     uint8_t light_enabled;
     double physics_rate, biology_rate, co2_mass_per_division;
+    int32_t tau_capacity;                     // 0 = the reference default
+    uint8_t tau_compaction;
 };
 
 struct RefSpawn {
@@ -77,6 +79,7 @@ void* ref_world_create(const RefParams* p) {
     WorldDesc d{};
     d.chamber = Chamber{p->chamber_w, p->chamber_h, p->chamber_d};
     d.capacity = p->capacity;
+    d.tau_capacity = p->tau_capacity;
     d.seed = p->seed;
     MotionConfig m{};
     m.boundary_x = static_cast<Boundary>(p->boundary_x);
@@ -92,6 +95,7 @@ void* ref_world_create(const RefParams* p) {
     m.ambient_temp = p->ambient_temp;
     m.store_disposition = static_cast<contract::StoreDisposition>(p->store_disposition);
     m.compaction_enabled = p->compaction_enabled;
+    m.tau_compaction_enabled = p->tau_compaction != 0;
     d.motion = m;
     d.co2_init = p->co2_init;
     if (world_create(*w, d)) { delete w; return nullptr; }
@@ -184,6 +188,35 @@ int ref_field_deposit(void* h, int fid, uint64_t* host) {
     fields::Grid2D* g = field(static_cast<World*>(h), fid);
     if (!g) return 1;
     std::memcpy(host, g->deposit, sizeof(uint64_t) * static_cast<size_t>(g->n) * g->n);
+    return 0;
+}
+
+// taumoeba_spawn (src/sim/predation.cu:420-432).
+int ref_tau_spawn(void* h, int32_t count, uint64_t seed) {
+    World* w = static_cast<World*>(h);
+    return static_cast<int>(taumoeba_spawn(w->taumoeba, count, w->chamber, seed).status);
+}
+int32_t ref_tau_count(void* h) { return static_cast<World*>(h)->taumoeba.count; }
+uint64_t ref_tau_next_id(void* h) { return static_cast<World*>(h)->taumoeba.next_id; }
+void ref_set_tau_compaction(void* h, int on) { static_cast<World*>(h)->motion.tau_compaction_enabled = on != 0; }
+
+// The predator store's arrays in snapshot order (dir 0: out to host[k], 1: in from host[k]).
+int ref_tau_io(void* h, int dir, void** host, int32_t count, uint64_t next_id) {
+    TaumoebaStore& t = static_cast<World*>(h)->taumoeba;
+    void* d[20] = {t.id, t.flags, t.x, t.y, t.z, t.vx, t.vy, t.vz, t.dir_x, t.dir_y, t.dir_z, t.biomass,
+                   t.prey_biomass, t.digest_timer, t.tolerance, t.generation, t.rng_state, t.density_ema,
+                   t.run_timer, t.target};
+    const size_t sz[20] = {8, 4, 8, 8, 8, 8, 8, 8, 4, 4, 4, 8, 8, 4, 4, 4, 8, 4, 4, 4};
+    if (dir == 1) {
+        if (count > t.capacity) return 1;
+        t.count = count;
+        t.next_id = next_id;
+    }
+    for (int k = 0; k < 20; ++k) {
+        const size_t b = sz[k] * static_cast<size_t>(dir == 1 ? count : t.count);
+        if (dir == 0) std::memcpy(host[k], d[k], b);
+        else std::memcpy(d[k], host[k], b);
+    }
     return 0;
 }
 

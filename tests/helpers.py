@@ -65,6 +65,9 @@ def oracle_lib():
             "orc_world_spawn_seeded": (I32, [P, C.POINTER(agb.Spawn), U64]),
             "orc_world_set_light": (I32, [P, C.POINTER(agb.Light)]),
             "orc_world_set_flash": (I32, [P, I32, C.c_double]),
+            "orc_world_spawn_taumoeba": (I32, [P, I32, U64]),
+            "orc_world_import_taumoeba": (I32, [P, C.POINTER(agb.Taumoeba), I32, U64]),
+            "orc_world_export_taumoeba": (I32, [P, C.POINTER(agb.Taumoeba), I32, C.POINTER(I32), C.POINTER(U64)]),
             "orc_world_flash_audit": (I32, [P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
             "orc_world_import_cells": (I32, [P, C.POINTER(agb.Cells), I32, U64]),
             "orc_world_export_cells": (I32, [P, C.POINTER(agb.Cells), I32, C.POINTER(I32), C.POINTER(U64)]),
@@ -134,6 +137,22 @@ class OracleWorld:
 
     def set_flash(self, active, power=0.0):
         self._ck(self.lib.orc_world_set_flash(self.h, int(bool(active)), power), "set_flash")
+
+    def spawn_taumoeba(self, count, seed):
+        self._ck(self.lib.orc_world_spawn_taumoeba(self.h, count, seed), "spawn_taumoeba")
+
+    def import_taumoeba(self, tau, next_id):
+        s = tau.struct()
+        self._ck(self.lib.orc_world_import_taumoeba(self.h, C.byref(s), tau.n, next_id), "import_taumoeba")
+
+    def export_taumoeba(self):
+        cnt, nid = C.c_int32(), C.c_uint64()
+        empty = agb.Taumoeba()
+        self.lib.orc_world_export_taumoeba(self.h, C.byref(empty), 0, C.byref(cnt), C.byref(nid))
+        out = agb.TaumoebaArrays(cnt.value)
+        s = out.struct()
+        self.lib.orc_world_export_taumoeba(self.h, C.byref(s), cnt.value, C.byref(cnt), C.byref(nid))
+        return out, nid.value
 
     def flash_audit(self):
         i, e = C.c_double(), C.c_double()
@@ -243,7 +262,7 @@ class RefParams(C.Structure):
                 ("light_dir_x", C.c_float), ("light_dir_y", C.c_float), ("light_irradiance", C.c_float),
                 ("ambient_irradiance", C.c_float), ("light_enabled", C.c_uint8),
                 ("physics_rate", C.c_double), ("biology_rate", C.c_double),
-                ("co2_mass_per_division", C.c_double)]
+                ("co2_mass_per_division", C.c_double), ("tau_capacity", C.c_int32), ("tau_compaction", C.c_uint8)]
 
 
 class RefSpawn(C.Structure):
@@ -281,6 +300,11 @@ def ref_lib():
         lib.ref_state_hash.restype = C.c_uint64
         lib.ref_state_hash.argtypes = [C.c_void_p]
         lib.ref_set_flash.argtypes = [C.c_void_p, C.c_int, C.c_double]
+        lib.ref_tau_spawn.argtypes = [C.c_void_p, C.c_int32, C.c_uint64]
+        lib.ref_tau_count.argtypes = [C.c_void_p]
+        lib.ref_tau_next_id.argtypes = [C.c_void_p]
+        lib.ref_tau_next_id.restype = C.c_uint64
+        lib.ref_tau_io.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p), C.c_int32, C.c_uint64]
         lib.ref_flash_audit.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         lib.ref_scenario_run.restype = C.c_void_p
         lib.ref_scenario_run.argtypes = [C.c_char_p, C.c_int64, C.c_void_p, C.POINTER(C.c_int32)]
@@ -309,10 +333,25 @@ class RefWorld:
                       desc.store_disposition, desc.compaction_enabled, desc.ambient_temp,
                       g[1].init, g[0].nx, g[1].nx, g[2].nx, g[3].nx, g[0].bc[0], g[1].bc[0],
                       L.dir_x, L.dir_y, L.irradiance, L.ambient, L.enabled,
-                      desc.physics_rate, desc.biology_rate, desc.co2_mass_per_division)
+                      desc.physics_rate, desc.biology_rate, desc.co2_mass_per_division, desc.tau_capacity,
+                      desc.tau_compaction_enabled)
         self.h = C.c_void_p(lib.ref_world_create(C.byref(p)))
         if not self.h:
             raise RuntimeError("ref_world_create failed")
+
+    def spawn_taumoeba(self, count, seed):
+        assert self.lib.ref_tau_spawn(self.h, count, seed) == 0
+
+    def export_taumoeba(self):
+        n = self.lib.ref_tau_count(self.h)
+        out = agb.TaumoebaArrays(n)
+        ptrs = (C.c_void_p * 20)(*[out.a[name].ctypes.data for name, _t in agb.TAU_FIELDS])
+        assert self.lib.ref_tau_io(self.h, 0, ptrs, n, 0) == 0
+        return out, int(self.lib.ref_tau_next_id(self.h))
+
+    def import_taumoeba(self, tau, next_id):
+        ptrs = (C.c_void_p * 20)(*[tau.a[name].ctypes.data for name, _t in agb.TAU_FIELDS])
+        assert self.lib.ref_tau_io(self.h, 1, ptrs, tau.n, next_id) == 0
 
     @classmethod
     def from_scenario(cls, text, ticks, desc):

@@ -19,7 +19,7 @@ S = H.load_scenario()
 pytestmark = pytest.mark.gpu
 
 SUPPORTED = ["first-light", "three-percent-line", "bloom", "komorov", "shadow-garden", "spin-drive-face",
-             "demo-herd", "sandbox"]
+             "taumoeba", "demo-herd", "sandbox"]
 HAVE = {os.path.basename(p)[:-5] for p in glob.glob(os.path.join(TS.SCEN_DIR, "*.json"))}
 MEASURE_RTOL = 1e-4        # correlations and fits over FP32-computed positions
 
@@ -81,16 +81,15 @@ def test_measured_accept_values_agree():
         assert abs(vg - vo) <= MEASURE_RTOL * abs(vo) + 1e-6, (m, vg, vo)
 
 
-def test_unsupported_scenarios_refuse():
-    for sid in ("taumoeba",):
-        if sid not in HAVE:
-            continue
-        with pytest.raises(S.ScenarioUnsupported):
-            S.instantiate(S.parse(TS.text_of(sid)))
+def test_scenario_needing_a_missing_grid_refuses():
+    if "taumoeba" not in HAVE:
+        pytest.skip("reference scenario files not present")
+    with pytest.raises(S.ScenarioUnsupported):
+        S.instantiate(S.parse(TS.text_of("taumoeba")), grids={agb.FIELD_N2: agb.GridDesc()})
 
 
 @pytest.mark.parametrize("sid", ["shadow-garden", "komorov", "bloom", "three-percent-line", "first-light",
-                                 "spin-drive-face"])
+                                 "spin-drive-face", "taumoeba"])
 def test_reference_scenario_accepts(sid):
     """`--scenario ID --assert` at the scenario's own horizon (300 to 60,000
     ticks): the reference's acceptance gate, run on the engine, accepts."""
@@ -103,19 +102,23 @@ def test_reference_scenario_accepts(sid):
 
 
 def test_headless_entry_point():
-    """scenario.py's command line: ACCEPT exits 0, an unsupported scenario 3."""
+    """scenario.py's command line: ACCEPT exits 0, a file that does not parse 2."""
     import subprocess
     import sys
-    if "komorov" not in HAVE or "taumoeba" not in HAVE:
+    import tempfile
+    if "komorov" not in HAVE:
         pytest.skip("reference scenario files not present")
     script = os.path.join(H.PKG, "scenario.py")
     r = subprocess.run([sys.executable, script, "--scenario", "komorov", "--scenarios-dir", TS.SCEN_DIR, "--assert"],
                        capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "scenario komorov: ACCEPT" in r.stdout
-    r = subprocess.run([sys.executable, script, "--scenario", os.path.join(TS.SCEN_DIR, "taumoeba.json"), "--assert"],
+    with tempfile.NamedTemporaryFile("w", suffix=".json", delete=False) as fh:
+        fh.write('{"objective": {"accept": [{"metric": "no_such_metric"}]}}')
+    r = subprocess.run([sys.executable, script, "--scenario", fh.name, "--assert"],
                        capture_output=True, text=True, timeout=600)
-    assert r.returncode == 3 and "unsupported" in r.stdout
+    os.unlink(fh.name)
+    assert r.returncode == 2 and "unknown accept metric" in r.stdout
 
 
 @pytest.mark.parametrize("graph", [False, True])

@@ -92,9 +92,10 @@ def test_reference_scenarios_parse():
         s = S.load(path)
         ids[s.id] = s
         assert s.populations, s.id
-    assert S.unsupported(ids["taumoeba"])
-    supported = [k for k, s in ids.items() if S.unsupported(s) is None]
-    assert len(supported) == len(ids) - 1
+    assert all(S.unsupported(s) is None for s in ids.values())
+    assert S.capacities(ids["taumoeba"]) == (52096, 4352)
+    no_n2 = {agb.FIELD_N2: agb.GridDesc()}
+    assert S.unsupported(ids["taumoeba"], no_n2) and S.unsupported(ids["bloom"], no_n2) is None
 
 
 def test_parse_defaults_comments_and_errors():
@@ -144,7 +145,8 @@ def test_accept_eval_and_fits():
 
 @needs_ref
 @pytest.mark.parametrize("sid,ticks", [("first-light", 40), ("three-percent-line", 12), ("bloom", 40),
-                                       ("komorov", 40), ("shadow-garden", 25), ("spin-drive-face", 60)])
+                                       ("komorov", 40), ("shadow-garden", 25), ("spin-drive-face", 60),
+                                       ("taumoeba", 12)])
 def test_spine_matches_reference_scenario_code(sid, ticks):
     text = text_of(sid)
     s = S.parse(text)
