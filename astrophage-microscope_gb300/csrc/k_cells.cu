@@ -1037,7 +1037,7 @@ __global__ void __launch_bounds__(256) cell_step_kernel(DevState* S, Ctx c, Tick
 // Batched launches of the per-cell stages (agb_batch): one grid over many
 // chambers, each block running the per-world body for its chamber.
 // ---------------------------------------------------------------------------
-AGB_BATCHED(thermal_batch, 256, thermal_kernel_body(a.S, a.c, a.p, blk))
+AGB_BATCHED_MB(thermal_batch, 256, 4, thermal_kernel_body(a.S, a.c, a.p, blk))
 AGB_BATCHED(clear_stamps_batch, 256, clear_stamps_kernel_body(a.S, a.c, a.stamp_idx, blk))
 AGB_BATCHED(stamp_batch, 256, stamp_kernel_body(a.S, a.c, a.stamp_idx, blk))
 AGB_BATCHED(occlusion_factor_batch, 256, occlusion_factor_kernel_body(a.S, a.c, a.stamp_idx, a.factor, blk))
@@ -1045,7 +1045,7 @@ AGB_BATCHED(sweep_rows_batch, 256, sweep_rows_kernel_body(a.c, a.factor, blk))
 AGB_BATCHED(sweep_lines_batch, 128, sweep_kernel_body(a.c, a.factor, blk))
 AGB_BATCHED_MB(cell_step_batch, 256, 3,
             cell_step_kernel_body<1>(a.S, a.c, a.p, a.arg & 1, (a.arg >> 1) & 1, a.fx, a.fy, a.fz, blk))
-AGB_BATCHED_MB(integrate_batch, 256, 3,
+AGB_BATCHED_MB(integrate_batch, 256, 4,
             integrate_kernel_body(a.S, a.c, a.p, a.fx, a.fy, a.fz, a.g, a.demand, a.inv_gv, blk))
 
 }  // namespace

@@ -610,7 +610,7 @@ void launch_compact_kernels(DevState* S, const LifeBuffers& b, int32_t capacity,
     launch_k(swap_kernel, 1, 1, 0, s, S);
 }
 
-AGB_BATCHED(uptake_mark_batch, 256,
+AGB_BATCHED_MB(uptake_mark_batch, 256, 4,
             uptake_mark_kernel_body(a.S, a.c, a.p, a.demand, a.inv_gv, a.life.flags, blk))
 AGB_BATCHED_MB(divide_batch, 256, 3,
             divide_kernel_body(a.S, a.c, a.life.flags, a.life.prefix, a.arg, a.demand, blk))
