@@ -612,7 +612,7 @@ void launch_compact_kernels(DevState* S, const LifeBuffers& b, int32_t capacity,
 
 AGB_BATCHED_MB(uptake_mark_batch, 256, 4,
             uptake_mark_kernel_body(a.S, a.c, a.p, a.demand, a.inv_gv, a.life.flags, blk))
-AGB_BATCHED_MB(divide_batch, 256, 3,
+AGB_BATCHED_MB(divide_batch, 256, 4,
             divide_kernel_body(a.S, a.c, a.life.flags, a.life.prefix, a.arg, a.demand, blk))
 AGB_BATCHED(keep_batch, 256, keep_kernel_body(a.S, a.life.flags, blk))
 AGB_BATCHED(scatter_src_batch, 256, scatter_src_kernel_body(a.S, a.life.flags, a.life.prefix, a.life.src, blk))
