@@ -415,6 +415,54 @@ __device__ __forceinline__ void sweep_rows_kernel_body(const Ctx& c, const doubl
     }
 }
 
+// The same sweep with one warp per row, 32 consecutive voxels per step; the
+// FP64 recurrence walks the row's stamps in sweep order, broadcasting each
+// factor. The warp issues the FP64 work once per stamp of its row, so this
+// form wins only where rows are too few to give the 32-row tiles a wave
+// (a single world's grid); batches take the tiles.
+__device__ __forceinline__ void sweep_row_warps_kernel_body(const Ctx& c, const double* __restrict__ factor,
+                                                            Blk blk) {
+    const GridDev I = c.g[AGB_FIELD_IRRADIANCE];
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blk.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)blk.n * blockDim.x) >> 5;
+    const int32_t len = I.nx;
+    const int64_t lines = I.count / len;
+    for (int64_t line = warp; line < lines; line += nwarps) {
+        const uint8_t mark = c.irr_marks ? c.irr_marks[line] : 1;    // one byte, broadcast to the warp
+        if (mark == 0) continue;                                    // values already unshadowed
+        __syncwarp();
+        if (c.irr_marks && lane == 0) c.irr_marks[line] = mark == 1 ? 2 : 0;
+        const int64_t base = line * len;
+        double t = 1.0;
+        float cur = fa(d2f(c.source_d * t), c.ambient_irr);
+        for (int32_t s0 = 0; s0 < len; s0 += 32) {
+            const int32_t s = s0 + lane;
+            const bool in = s < len;
+            const int64_t idx = base + (c.light_sign > 0 ? s : (len - 1 - s));
+            const bool raw = in && stamped(c, I, idx);
+            unsigned mask = __ballot_sync(0xFFFFFFFFu, raw);
+            float mine = cur;
+            if (mask) {
+                const double f = raw ? __ldg(&factor[idx]) : 1.0;
+                while (mask) {
+                    const int b = __ffs(mask) - 1;
+                    mask &= mask - 1u;
+                    t *= __shfl_sync(0xFFFFFFFFu, f, b);
+                    cur = fa(d2f(c.source_d * t), c.ambient_irr);
+                    if (lane > b) mine = cur;
+                }
+            }
+            if (in) I.value[idx] = mine;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) sweep_row_warps_kernel(Ctx c, const double* __restrict__ factor) {
+    pdl_wait();
+    sweep_row_warps_kernel_body(c, factor, grid_blk());
+}
+
 __global__ void __launch_bounds__(256) sweep_rows_kernel(Ctx c, const double* __restrict__ factor) {
     pdl_wait();
     sweep_rows_kernel_body(c, factor, grid_blk());
@@ -1093,6 +1141,17 @@ void launch_taxis(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks
 void launch_thermal(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, cudaStream_t s) {
     launch_k(thermal_kernel, blocks, 256, 0, s, S, c, p);
 }
+static int sm_count_of_device() {
+    static int sms = 0;
+    if (sms == 0) {
+        int d = 0;
+        cudaGetDevice(&d);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d);
+        if (sms <= 0) sms = 1;
+    }
+    return sms;
+}
+
 void launch_emission_prep(DevState* S, const Ctx& c, const TickParams& p, int32_t* stamp_idx, double* factor,
                           bool stamp, int32_t blocks, cudaStream_t s) {
     (void)p;
@@ -1105,7 +1164,14 @@ void launch_emission_prep(DevState* S, const Ctx& c, const TickParams& p, int32_
     const int32_t len = c.light_axis == 0 ? I.nx : (c.light_axis == 1 ? I.ny : I.nz);
     const int64_t lines = I.count / len;
     if (c.light_axis == 0) {
-        launch_k(sweep_rows_kernel, (unsigned)sweep_rows_blocks(lines), 32 * SWEEP_ROW_WARPS, 0, s, c, factor);
+        // Tiles of 32 rows need rows for several waves; a single world's grid
+        // rarely has them (a 128^3 grid has 16,384 rows, 64 tile blocks).
+        if (lines >= 32 * 4 * SWEEP_ROW_WARPS * (int64_t)sm_count_of_device()) {
+            launch_k(sweep_rows_kernel, (unsigned)sweep_rows_blocks(lines), 32 * SWEEP_ROW_WARPS, 0, s, c, factor);
+        } else {
+            const int64_t blocks = (lines * 32 + 255) / 256;
+            launch_k(sweep_row_warps_kernel, (unsigned)(blocks < 65535 ? blocks : 65535), 256, 0, s, c, factor);
+        }
     } else {
         launch_k(sweep_kernel, (unsigned)((lines + 127) / 128), 128, 0, s, c, factor);
     }
