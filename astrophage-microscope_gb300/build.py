@@ -9,6 +9,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libagb.so")
+HEADLESS = os.path.join(HERE, "headless")       # the command-line scenario runner over the C ABI
 SOURCES = ["k_grid.cu", "k_hash.cu", "k_cells.cu", "k_life.cu", "k_tau.cu", "world.cu", "batch.cu", "snapshot.cu", "conv_tc.cu", "nn_ops.cu", "nn_abi.cu", "surrogate.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Host code that restates the reference's FP64 expressions (per-world constants)
@@ -46,6 +47,12 @@ def build(verbose=False, extra=()):
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
+    inc = os.path.join(os.path.dirname(HERE), "include")
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-ffp-contract=off", "-I" + inc, os.path.join(CSRC, "headless.cpp"),
+           "-o", HEADLESS, "-L" + HERE, "-lagb", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("headless build failed:\n" + r.stdout + r.stderr)
     return LIB
 
 

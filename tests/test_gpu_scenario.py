@@ -169,3 +169,43 @@ def test_flash_armed_batch_chamber_equals_standalone():
     for i in (0, 2, 3):
         d, s = TB.chambers()
         TB.assert_same(b.chambers[i], TB.standalone(d[i], s[i], 3, walk=b.chambers[i].walk()), "chamber %d" % i)
+
+
+HEADLESS = os.path.join(H.PKG, "headless")
+CHECKED = ["first-light", "three-percent-line", "bloom", "komorov", "shadow-garden", "spin-drive-face", "taumoeba"]
+
+
+def _check_lines(text):
+    return [ln.strip() for ln in text.splitlines() if ln.strip().startswith("[")]
+
+
+@pytest.mark.parametrize("sid", CHECKED)
+def test_native_runner_equals_python_spine(sid):
+    """The native runner (headless.cpp over the C ABI) and the Python spine
+    drive the engine through the same calls: the same measured values, printed
+    the same way, over the first 300 ticks."""
+    import io
+    import subprocess
+    if sid not in HAVE:
+        pytest.skip("reference scenario files not present")
+    s = S.parse(TS.text_of(sid))
+    out = io.StringIO()
+    S.run_assert(s, S.instantiate(s), ticks=300, out=out)
+    r = subprocess.run([HEADLESS, "--scenario", sid, "--scenarios-dir", TS.SCEN_DIR, "--assert", "--ticks", "300"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode in (0, 1), r.stdout + r.stderr
+    assert _check_lines(r.stdout) == _check_lines(out.getvalue())
+
+
+def test_native_runner_accepts_and_is_deterministic():
+    import subprocess
+    if "komorov" in HAVE:
+        r = subprocess.run([HEADLESS, "--scenario", "komorov", "--scenarios-dir", TS.SCEN_DIR, "--assert"],
+                           capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0 and "scenario komorov: ACCEPT" in r.stdout, r.stdout + r.stderr
+    r = subprocess.run([HEADLESS, "--assert-deterministic", "--ticks", "200", "--cells", "3000"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and "MATCH" in r.stdout, r.stdout + r.stderr
+    r = subprocess.run([HEADLESS, "--scenario", "/no/such/file.json", "--assert"], capture_output=True, text=True,
+                       timeout=60)
+    assert r.returncode == 2
