@@ -18,6 +18,7 @@ C oracle (a restatement of the reference's kernel bodies, pinned to the
 reference's own outputs) over the same world with all host threads.
 """
 import argparse
+import datetime
 import json
 import os
 import statistics
@@ -325,8 +326,14 @@ def voxel_steps_per_tick(desc):
 # Instrumentation
 # ---------------------------------------------------------------------------
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
-    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+    """nvidia-smi clocks and throttle reasons sampled during the timed region.
+
+    The sampler is started and its first row awaited before the timed region
+    opens (nvidia-smi takes a while to start); rows are stamped, and those
+    inside [mark_start, mark_end] (widened by one sampling period) are the
+    ones reported."""
+    PERIOD_MS = 50
+    Q = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
@@ -336,12 +343,23 @@ class ClockSampler:
         self.out = tempfile.TemporaryFile(mode="w+")
 
     def start(self):
+        self.t0 = self.t1 = None
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", str(self.PERIOD_MS)],
                                          stdout=self.out, stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+            return
+        deadline = time.time() + 5.0
+        while time.time() < deadline and self.proc.poll() is None and os.fstat(self.out.fileno()).st_size == 0:
+            time.sleep(0.01)
+
+    def mark_start(self):
+        self.t0 = datetime.datetime.now()
+
+    def mark_end(self):
+        self.t1 = datetime.datetime.now()
 
     def stop(self):
         if self.proc is None:
@@ -353,6 +371,19 @@ class ClockSampler:
             self.proc.kill()
         self.out.seek(0)
         rows = [r.split(",") for r in self.out.read().strip().splitlines() if r.strip()]
+        if self.t0 is not None and self.t1 is not None:
+            slack = datetime.timedelta(milliseconds=self.PERIOD_MS)
+            inside = []
+            for r in rows:
+                try:
+                    t = datetime.datetime.strptime(r[0].strip(), "%Y/%m/%d %H:%M:%S.%f")
+                except ValueError:
+                    continue
+                if self.t0 - slack <= t <= self.t1 + slack:
+                    inside.append(r)
+            if inside:
+                rows = inside
+        rows = [r[1:] for r in rows]
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for r in rows:
@@ -623,12 +654,14 @@ def main():
             dist.barrier()
         torch.cuda.synchronize()
         sampler.start()
+        sampler.mark_start()
         for k in range(args.steps):
             l2_flush.zero_()                           # L2 flush, outside the timed interval
             starts[k].record(stream)
             world.step(1, graph=True, stream=sh)
             ends[k].record(stream)
         torch.cuda.synchronize()
+        sampler.mark_end()
         clocks = sampler.stop()
         if dist is not None:
             dist.barrier()
