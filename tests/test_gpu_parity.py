@@ -255,6 +255,13 @@ def test_diffusion_3d_partial_tiles_bit_exact(nx, ny, nz):
     check_3d_diffusion(nx, ny, nz)
 
 
+def test_diffusion_large_field_early_launch_bit_exact():
+    """A 256^3 field (2^24 voxels): each pass lets the next one launch as soon
+    as it has passed its own dependency wait, so back-to-back passes overlap
+    on the SMs; the field after six passes is still the oracle's, bit for bit."""
+    check_3d_diffusion(256, 256, 256)
+
+
 @pytest.mark.parametrize("tile", ["32,1,3", "32,2,1", "32,4,5", "16,1,7", "16,2,2", "32,2,64"])
 @pytest.mark.parametrize("nx,ny,nz", [(136, 40, 11), (64, 64, 64)])
 def test_diffusion_every_tiling_bit_exact(tile, nx, ny, nz, monkeypatch):
