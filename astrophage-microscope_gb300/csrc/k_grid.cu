@@ -176,6 +176,14 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
     atomicCAS(err, 0u, 4u);    // ERR_TMA_TIMEOUT
     return false;
 }
+// Orders this thread's earlier generic-proxy accesses of shared memory before
+// later async-proxy (TMA) accesses. Every thread that read a ring slot runs it
+// before the barrier after which the slot is refilled: a barrier alone orders
+// the generic proxy only, and a shared load still in flight when the barrier
+// completes (its value not yet consumed) could otherwise return the refill.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
 __device__ __forceinline__ void tma_load_plane(float* dst, const CUtensorMap* map, uint64_t* bar, int x, int y,
                                                int z) {
     asm volatile(
@@ -245,6 +253,7 @@ __device__ __forceinline__ void ftcs3d_tma_body(const CUtensorMap* src_map, floa
             below[r] = (k0 > 0) ? *reinterpret_cast<const float4*>(buf(0) + s) : ghost4(f, AGB_FACE_ZMIN, cur[r]);
         }
         ok = wait(2);                                   // nplanes >= 3
+        fence_proxy_async_smem();                       // plane 0's slot is refilled next
         ok = __syncthreads_and(ok);                     // also: everyone is done with plane 0
         if (ok) {
             waited = 3;
@@ -285,6 +294,7 @@ __device__ __forceinline__ void ftcs3d_tma_body(const CUtensorMap* src_map, floa
             // Plane q + 2 is the next step's "above"; the barrier also marks
             // plane q as free, so its slot takes plane q + NBUF.
             ok = wait(q + 2);
+            fence_proxy_async_smem();                   // plane q's slot is refilled next
             ok = __syncthreads_and(ok);
             if (ok) {
                 waited = q + 3;
@@ -410,8 +420,8 @@ struct TmaInstance {
         const dim3 grid((nx + T::TXW - 1) / T::TXW, (ny + T::TYH - 1) / T::TYH, zchunks * nch);
         launch_k(ftcs3d_tma_batch<LX, RPT>, grid, 256, T::SMEM, s, tab, nx, ny, nz, zc, zchunks);
     }
-    static void launch(const GridDev& g, int zc, const CUtensorMap* map, float* dst, float coeff, const Faces& f,
-                       uint32_t* err, cudaStream_t s) {
+    static cudaError_t launch(const GridDev& g, int zc, const CUtensorMap* map, float* dst, float coeff,
+                              const Faces& f, uint32_t* err, cudaStream_t s) {
         using T = TmaTile<LX, RPT>;
         (void)slots_per_sm();                           // sets the shared-memory attribute once
         const dim3 grid((g.nx + T::TXW - 1) / T::TXW, (g.ny + T::TYH - 1) / T::TYH, (g.nz + zc - 1) / zc);
@@ -420,8 +430,8 @@ struct TmaInstance {
         // us: its one short wave then lands unevenly over the SMs), so small
         // fields trigger at exit.
         const int32_t early = (int64_t)g.nx * g.ny * g.nz >= (int64_t)1 << 24;
-        launch_k(ftcs3d_tma_kernel<LX, RPT>, grid, 256, T::SMEM, s, *map, dst, g.nx, g.ny, g.nz, zc, coeff, f, err,
-                 early);
+        return launch_k(ftcs3d_tma_kernel<LX, RPT>, grid, 256, T::SMEM, s, *map, dst, g.nx, g.ny, g.nz, zc, coeff,
+                        f, err, early);
     }
 };
 
@@ -486,33 +496,34 @@ FtcsPlan ftcs_plan(int32_t nx, int32_t ny, int32_t nz) {
     return ftcs_plan_with(nx, ny, nz, lx, rpt, zc);
 }
 
-void launch_ftcs(const GridDev& g, const float* src, float* dst, float coeff, const int32_t* bc,
-                 const float* face, float robin, const CUtensorMap* src_map, const FtcsPlan* plan, uint32_t* err,
-                 cudaStream_t s) {
+cudaError_t launch_ftcs(const GridDev& g, const float* src, float* dst, float coeff, const int32_t* bc,
+                        const float* face, float robin, const CUtensorMap* src_map, const FtcsPlan* plan,
+                        uint32_t* err, cudaStream_t s) {
     Faces f;
     for (int k = 0; k < 6; ++k) { f.bc[k] = bc[k]; f.val[k] = face[k]; }
     f.robin = robin;
     if (g.nz > 1 && src_map != nullptr && plan != nullptr) {
         const FtcsPlan p = *plan;
         if (p.lx == 32) {
-            if (p.rpt == 1) TmaInstance<32, 1>::launch(g, p.zc, src_map, dst, coeff, f, err, s);
-            else if (p.rpt == 2) TmaInstance<32, 2>::launch(g, p.zc, src_map, dst, coeff, f, err, s);
-            else TmaInstance<32, 4>::launch(g, p.zc, src_map, dst, coeff, f, err, s);
-        } else {
-            if (p.rpt == 1) TmaInstance<16, 1>::launch(g, p.zc, src_map, dst, coeff, f, err, s);
-            else TmaInstance<16, 2>::launch(g, p.zc, src_map, dst, coeff, f, err, s);
+            if (p.rpt == 1) return TmaInstance<32, 1>::launch(g, p.zc, src_map, dst, coeff, f, err, s);
+            if (p.rpt == 2) return TmaInstance<32, 2>::launch(g, p.zc, src_map, dst, coeff, f, err, s);
+            return TmaInstance<32, 4>::launch(g, p.zc, src_map, dst, coeff, f, err, s);
         }
-        return;
+        if (p.rpt == 1) return TmaInstance<16, 1>::launch(g, p.zc, src_map, dst, coeff, f, err, s);
+        return TmaInstance<16, 2>::launch(g, p.zc, src_map, dst, coeff, f, err, s);
     }
+    const dim3 block(32, 8);
     if (g.nz == 1) {
-        const dim3 block(32, 8);
         const dim3 grid((g.nx + 31) / 32, (g.ny + 7) / 8);
-        launch_k(ftcs2d_kernel, grid, block, 0, s, src, dst, g.nx, g.ny, coeff, f);
-    } else {
-        const dim3 block(32, 8);
-        const dim3 grid((g.nx + 31) / 32, (g.ny + 7) / 8, (g.nz + ZCHUNK - 1) / ZCHUNK);
-        launch_k(ftcs3d_kernel, grid, block, 0, s, src, dst, g.nx, g.ny, g.nz, coeff, f);
+        return launch_k(ftcs2d_kernel, grid, block, 0, s, src, dst, g.nx, g.ny, coeff, f);
     }
+    const dim3 grid((g.nx + 31) / 32, (g.ny + 7) / 8, (g.nz + ZCHUNK - 1) / ZCHUNK);
+    return launch_k(ftcs3d_kernel, grid, block, 0, s, src, dst, g.nx, g.ny, g.nz, coeff, f);
+}
+
+bool ftcs_plain_fits(int32_t nx, int32_t ny, int32_t nz) {
+    if (nx < 1 || ny < 1 || nz < 1) return false;
+    return (ny + 7) / 8 <= 65535 && (nz == 1 || (nz + ZCHUNK - 1) / ZCHUNK <= 65535);
 }
 
 void launch_ftcs_batch(const FtcsChamber* tab, int32_t nch, int32_t nx, int32_t ny, int32_t nz,

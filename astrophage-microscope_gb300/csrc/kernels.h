@@ -30,9 +30,14 @@ FtcsPlan ftcs_plan_copies(int32_t nx, int32_t ny, int32_t nz, int32_t lx, int32_
                           int32_t copies);
 // One explicit FTCS pass src -> dst (src/fields/diffuse.cu:19-44; 7-point when nz > 1).
 // 3-D grids with a tensor map (and the tiling it was made for) use the TMA-staged kernel.
-void launch_ftcs(const GridDev& g, const float* src, float* dst, float coeff, const int32_t* bc,
-                 const float* face, float robin, const CUtensorMap* src_map, const FtcsPlan* plan, uint32_t* err,
-                 cudaStream_t s);
+// Returns the launch's status.
+cudaError_t launch_ftcs(const GridDev& g, const float* src, float* dst, float coeff, const int32_t* bc,
+                        const float* face, float robin, const CUtensorMap* src_map, const FtcsPlan* plan,
+                        uint32_t* err, cudaStream_t s);
+// Whether the plain FTCS kernels (the path without a tensor map) can be
+// launched on this grid: their launch grids have at most 65535 blocks along y
+// (8 rows each) and along z (8 planes each).
+bool ftcs_plain_fits(int32_t nx, int32_t ny, int32_t nz);
 bool make_plane_map(CUtensorMap* map, float* base, int32_t nx, int32_t ny, int32_t nz, const FtcsPlan& plan);
 // One chamber's FTCS pass in a batched launch (agb_batch). The chambers of a
 // launch share grid dimensions and tiling; each has its own tensor map (over
