@@ -334,6 +334,9 @@ struct orc_world {
     uint32_t *keys, *vals, *keys_sorted, *vals_sorted, *tmp_k, *tmp_v;
     int32_t *bstart, *bend;
     double *fx, *fy, *fz;
+    /* Checker-only: per cell, the summed magnitudes of the terms behind the
+     * last motion stage's force, velocity and displacement (see motion_step). */
+    double *fscale, *vscale, *pscale;
     uint64_t* co2_demand;
     int32_t *scan_flags, *prefix, *compact_src;
     void* scratch;
@@ -393,6 +396,7 @@ void orc_world_destroy(orc_world* w) {
     free(w->keys); free(w->vals); free(w->keys_sorted); free(w->vals_sorted);
     free(w->tmp_k); free(w->tmp_v); free(w->bstart); free(w->bend);
     free(w->fx); free(w->fy); free(w->fz); free(w->co2_demand);
+    free(w->fscale); free(w->vscale); free(w->pscale);
     free(w->scan_flags); free(w->prefix); free(w->compact_src); free(w->scratch);
     void** tp[20];
     tau_ptrs(&w->t, tp);
@@ -462,11 +466,13 @@ int orc_world_create(const agb_world_desc* d, orc_world** out) {
     w->bstart = (int32_t*)calloc((size_t)w->hbuckets, 4);
     w->bend = (int32_t*)calloc((size_t)w->hbuckets, 4);
     w->fx = (double*)calloc(n, 8); w->fy = (double*)calloc(n, 8); w->fz = (double*)calloc(n, 8);
+    w->fscale = (double*)calloc(n, 8); w->vscale = (double*)calloc(n, 8); w->pscale = (double*)calloc(n, 8);
     w->co2_demand = (uint64_t*)calloc(w->g[AGB_FIELD_CO2].enabled ? (size_t)w->g[AGB_FIELD_CO2].count : 1, 8);
     w->scan_flags = (int32_t*)calloc(n, 4); w->prefix = (int32_t*)calloc(n, 4);
     w->compact_src = (int32_t*)calloc(n, 4); w->scratch = calloc(n, 8);
     if (!w->keys || !w->vals || !w->keys_sorted || !w->vals_sorted || !w->tmp_k || !w->tmp_v ||
         !w->bstart || !w->bend || !w->fx || !w->fy || !w->fz || !w->co2_demand ||
+        !w->fscale || !w->vscale || !w->pscale ||
         !w->scan_flags || !w->prefix || !w->compact_src || !w->scratch) {
         orc_world_destroy(w);
         return AGB_OUT_OF_MEMORY;
@@ -1034,7 +1040,7 @@ static void motion_step(orc_world* w, double dt) {        /* motion_step, integr
 #endif
     for (int32_t i = 0; i < n; ++i) {                      /* forces_kernel, :40-76 */
         const uint32_t flags = v->flags[i];
-        if (!(flags & AGB_FLAG_OCCUPIED)) { w->fx[i] = w->fy[i] = w->fz[i] = 0.0; continue; }
+        if (!(flags & AGB_FLAG_OCCUPIED)) { w->fx[i] = w->fy[i] = w->fz[i] = w->fscale[i] = 0.0; continue; }
         const double mass = cell_mass(v->biomass[i], v->energy[i]);
         const int alive = (flags & AGB_FLAG_ALIVE) != 0u;
         const double emit = alive ? (double)v->emit_power[i] : 0.0;
@@ -1042,6 +1048,9 @@ static void motion_step(orc_world* w, double dt) {        /* motion_step, integr
         const double wgt = -(mass - AGB_WATER_DENSITY * AGB_CELL_VOLUME) * AGB_G_ACCEL;
         if (w->d.gravity_axis == AGB_GRAVITY_Y) F.y += wgt; else F.z += wgt;
         const double thrust = emit / AGB_C_LIGHT;
+        /* checker: summed term magnitudes; the buoyant weight is the difference
+         * of the cell's weight and that of the water it displaces */
+        double fs = (mass + AGB_WATER_DENSITY * AGB_CELL_VOLUME) * AGB_G_ACCEL + fabs(thrust);
         if (thrust != 0.0) {
             F.x -= (double)v->dir_x[i] * thrust;
             F.y -= (double)v->dir_y[i] * thrust;
@@ -1061,14 +1070,17 @@ static void motion_step(orc_world* w, double dt) {        /* motion_step, integr
                 const double overlap = two_a - r;
                 const double s = kc * overlap / r;
                 F.x += d.x * s; F.y += d.y * s; F.z += d.z * s;
+                fs += kc * two_a;                          /* a contact's force at full overlap */
             }
         }
         if (i == w->d.trap_slot) {                          /* trap_force, :195-197 */
             F.x += kt * (w->d.trap_x - v->x[i]);
             F.y += kt * (w->d.trap_y - v->y[i]);
             F.z += 0.0;
+            fs += fabs(kt * (w->d.trap_x - v->x[i])) + fabs(kt * (w->d.trap_y - v->y[i]));
         }
         w->fx[i] = F.x; w->fy[i] = F.y; w->fz[i] = F.z;
+        w->fscale[i] = fs;
     }
     const double a = AGB_CELL_RADIUS;
     const double hw = 0.5 * w->d.chamber_w, hh = 0.5 * w->d.chamber_h, hd = 0.5 * w->d.chamber_d;
@@ -1095,6 +1107,30 @@ static void motion_step(orc_world* w, double dt) {        /* motion_step, integr
         ou_advance_axis(&px, &ux, w->fx[i], gamma, &c, dt, w->d.thermal_noise, z1, z2);
         ou_advance_axis(&py, &uy, w->fy[i], gamma, &c, dt, w->d.thermal_noise, z3, z4);
         ou_advance_axis(&pz, &uz, w->fz[i], gamma, &c, dt, w->d.thermal_noise, z5, z6);
+        {   /* checker: the largest summed term magnitude of any axis's velocity and
+             * displacement, the force term taken at its own term scale */
+            const double vt = w->fscale[i] / gamma;
+            const double za[3] = {fabs(z1), fabs(z3), fabs(z5)}, zb[3] = {fabs(z2), fabs(z4), fabs(z6)};
+            const double u0[3] = {fabs(v->vx[i]), fabs(v->vy[i]), fabs(v->vz[i])};
+            double ra = 0.0, rb = 0.0;
+            if (w->d.thermal_noise && c.s_rr > 0.0) {
+                ra = c.s_rv / c.s_rr;
+                const double b2 = c.s_vv * c.s_vv - ra * ra;
+                rb = sqrt(b2 > 0.0 ? b2 : 0.0);
+            } else if (w->d.thermal_noise) {
+                rb = c.s_vv;
+            }
+            double vs = 0.0, ps = 0.0;
+            for (int k = 0; k < 3; ++k) {
+                const double sv = u0[k] * c.e1 + vt * c.ome + ra * za[k] + rb * zb[k];
+                const double sp = vt * dt + (u0[k] + vt) * c.ome * c.inv_beta +
+                                  (w->d.thermal_noise ? c.s_rr * za[k] : 0.0);
+                if (sv > vs) vs = sv;
+                if (sp > ps) ps = sp;
+            }
+            w->vscale[i] = vs;
+            w->pscale[i] = ps;
+        }
         v->rng_state[i] = rng.state;
         int kept = apply_boundary_axis(&px, &ux, hw, a, w->d.boundary_x);
         kept = apply_boundary_axis(&py, &uy, hh, a, w->d.boundary_y) && kept;
@@ -1128,6 +1164,19 @@ static void motion_step(orc_world* w, double dt) {        /* motion_step, integr
 int orc_world_export_forces(orc_world* w, double* fx, double* fy, double* fz) {
     const size_t b = sizeof(double) * (size_t)w->count;
     memcpy(fx, w->fx, b); memcpy(fy, w->fy, b); memcpy(fz, w->fz, b);
+    return 0;
+}
+
+/* Checker-only: per cell, from the last motion stage, the sum of the magnitudes
+ * of the terms its force is made of (the cell's weight and the displaced
+ * water's, recoil, trap, and k * 2a for each contact: the force of that
+ * contact at full overlap), and the largest summed
+ * term magnitude of any axis's velocity and displacement update. A value that
+ * is a sum of terms can be held to a relative bound of that sum, not of itself:
+ * contact sums cancel. */
+int orc_world_export_term_scales(orc_world* w, double* force, double* vel, double* disp) {
+    const size_t b = sizeof(double) * (size_t)w->count;
+    memcpy(force, w->fscale, b); memcpy(vel, w->vscale, b); memcpy(disp, w->pscale, b);
     return 0;
 }
 
@@ -1178,6 +1227,12 @@ static int compact(orc_world* w) {                        /* cell_store_compact,
     const int32_t live = run;
     if (live >= cnt) return 0;
     if (live > 0) gather_all(w, live);
+    double* sc[3] = {w->fscale, w->vscale, w->pscale};   /* checker arrays follow their cells */
+    double* tmp = (double*)w->scratch;
+    for (int k = 0; k < 3; ++k) {
+        for (int32_t i = 0; i < live; ++i) tmp[i] = sc[k][w->compact_src[i]];
+        memcpy(sc[k], tmp, sizeof(double) * (size_t)live);
+    }
     w->count = live;
     return 0;
 }
@@ -1271,6 +1326,7 @@ static void lifecycle_step(orc_world* w, double dt) {    /* lifecycle_step, life
                 v->y[i] = clampd(v->y[i], -hy, hy);
                 v->z[i] = clampd(v->z[i], -hz, hz);
                 v->vx[slot] = v->vx[i]; v->vy[slot] = v->vy[i]; v->vz[slot] = v->vz[i];
+                w->fscale[slot] = w->fscale[i]; w->vscale[slot] = w->vscale[i]; w->pscale[slot] = w->pscale[i];
                 v->id[slot] = did;
                 v->flags[slot] = v->flags[i];
                 v->death_cause[slot] = AGB_DEATH_NONE;

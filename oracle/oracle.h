@@ -55,6 +55,7 @@ int orc_world_set_clock(orc_world* w, double physics_rate, double biology_rate);
 int orc_world_export_hash(orc_world* w, int32_t dims[4], uint32_t* keys_sorted, uint32_t* vals_sorted,
                           int32_t* bucket_start, int32_t* bucket_end);
 int orc_world_export_forces(orc_world* w, double* fx, double* fy, double* fz);
+int orc_world_export_term_scales(orc_world* w, double* force, double* vel, double* disp);
 int orc_world_counters(orc_world* w, int64_t out[4]);
 
 /* Known-answer hooks for the RNG (src/core/rng.cuh). */

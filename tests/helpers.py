@@ -41,6 +41,10 @@ def load_scenario():
     return _load("scenario")
 
 
+def load_workloads():
+    return _load("workloads")
+
+
 def build_oracle():
     src = os.path.join(ROOT, "oracle", "oracle.c")
     if (not os.path.exists(ORACLE_SO)) or os.path.getmtime(ORACLE_SO) < os.path.getmtime(src):
@@ -83,6 +87,7 @@ def oracle_lib():
             "orc_world_set_clock": (I32, [P, C.c_double, C.c_double]),
             "orc_world_export_hash": (I32, [P, P, P, P, P, P]),
             "orc_world_export_forces": (I32, [P, P, P, P]),
+            "orc_world_export_term_scales": (I32, [P, P, P, P]),
             "orc_world_counters": (I32, [P, P]),
             "orc_pcg32_seed_draws": (None, [U64, U64, I32, P]),
             "orc_cell_rng_init": (U64, [U64, U64]),
@@ -231,6 +236,14 @@ class OracleWorld:
         f = [np.zeros(max(n, 1), np.float64) for _ in range(3)]
         self.lib.orc_world_export_forces(self.h, f[0].ctypes.data, f[1].ctypes.data, f[2].ctypes.data)
         return [a[:n] for a in f]
+
+    def export_term_scales(self):
+        """Per cell, from the last motion stage: (force, velocity, displacement)
+        summed term magnitudes, the floors of the parity bounds (parity.py)."""
+        n = self.count()
+        s = [np.zeros(max(n, 1), np.float64) for _ in range(3)]
+        self.lib.orc_world_export_term_scales(self.h, s[0].ctypes.data, s[1].ctypes.data, s[2].ctypes.data)
+        return [a[:n] for a in s]
 
     def counters(self):
         out = np.zeros(4, dtype=np.int64)

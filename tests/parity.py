@@ -1,13 +1,38 @@
 """Comparison helpers for engine-vs-oracle parity.
 
 Integer state (ids, flags, death causes, PCG32 states, hash keys, sorted
-order, bucket ranges, slot assignment) must match exactly. Floating-point
-state is compared with the tolerance the engine is built to: the engine
-computes per-cell physics in FP32 and commits it into FP64 state, so one
-step's increments (displacement, velocity, energy and CO2 changes) agree to
-~1e-6 relative; the test bound is RTOL = 1e-5. Positions are compared
-through their per-step displacement, because 1e-5 of a millimetre position
-is larger than a whole Brownian step.
+order, bucket ranges, slot assignment, compaction survivors, the exact-zero
+irradiance set) must match exactly.
+
+Floating-point state is held to RTOL = 1e-5 relative, the bound the engine
+is specified to (FP32 arithmetic committed into the contract's FP64 state).
+A relative bound needs a scale where a value can sit at or near zero, and
+each floor below is the scale that the value's own arithmetic works at:
+
+  x, y, z        1e-5 of the coordinate, floored at one cell radius (a
+                 coordinate has no natural zero; 1e-5 of 5 um is 50 pm).
+                 With the oracle's term scales: also 1e-5 of the largest
+                 summed term of that step's displacement (drift, velocity
+                 relaxation and the Brownian kick), i.e. the displacement
+                 itself must agree to 1e-5 of its own size.
+  vx, vy, vz     1e-5 of the value, floored at 1e-5 of the summed magnitude
+                 of the terms of that step's velocity update (decayed
+                 velocity, force/drag, the two noise terms). A velocity is
+                 the sum of these; near zero they cancel.
+  forces         1e-5 of the value, floored at 1e-5 of the cell's force
+                 scale: (cell mass + displaced water mass) g + |recoil| +
+                 k * 2a per contact (a contact's force at full overlap).
+                 The buoyant weight is a difference of the first two, and
+                 contact sums cancel.
+  irradiance     1e-5 of the value, floored at 1e-5 of the light source's
+                 irradiance (a shading product is formed relative to the
+                 unshaded value, at most the source).
+  fields         1e-5 of the value (irradiance field: floored as above).
+  everything else (energy, CO2 held, biomass, temperatures, samples, age,
+  run-and-tumble state) 1e-5 of the value, no floor.
+
+The term scales come from the oracle (orc_world_export_term_scales): per cell,
+from the motion stage of the tick being compared.
 """
 import numpy as np
 
@@ -15,7 +40,11 @@ from helpers import agb
 
 RTOL = 1e-5
 INT_FIELDS = ("id", "flags", "death_cause", "rng_state")
-DELTA_FIELDS = ("x", "y", "z", "energy", "co2_held")
+POS_FIELDS = ("x", "y", "z")
+VEL_FIELDS = ("vx", "vy", "vz")
+# Displacements agree to far better than a position's 1e-5; the absolute floor
+# covers the FP64 rounding of the committed coordinate (|x| <= a few mm).
+POS_ABS_FLOOR = 1e-18
 
 
 def copy_state(src, dst, fields=True):
@@ -28,30 +57,38 @@ def copy_state(src, dst, fields=True):
     return cells
 
 
-def _close(a, b, rtol, atol):
+def _excess(a, b, tol):
+    """(number of elements beyond tol, worst |a - b| / tol) for float arrays."""
     a = np.asarray(a, np.float64)
     b = np.asarray(b, np.float64)
-    bad = np.abs(a - b) > rtol * np.abs(b) + atol
-    return int(np.count_nonzero(bad)), (float(np.max(np.abs(a - b))) if a.size else 0.0)
+    d = np.abs(a - b)
+    bad = d > tol
+    if not a.size:
+        return 0, 0.0
+    return int(np.count_nonzero(bad)), float(np.max(d / np.maximum(tol, 1e-300)))
 
 
-def _rms(a):
-    a = np.asarray(a, np.float64)
-    return float(np.sqrt(np.mean(a * a))) if a.size else 0.0
+def source_irradiance(desc):
+    L = desc.light
+    return float(L.irradiance) if L.enabled else 0.0
 
 
-def compare_cells(got, want, before=None, rtol=RTOL, where=""):
+def compare_cells(got, want, before=None, rtol=RTOL, where="", scales=None, source=None, velocities=True):
     """Return a list of human-readable mismatches (empty when in parity).
 
-    Per element: |got - want| <= rtol * |want| + atol, with atol = 1e-4 of the
-    population's RMS of that quantity (for positions, energy and CO2: of the
-    step's increment). The absolute floor covers components that happen to sit
-    near zero, where FP32 contact sums (error ~1e-7 of the summed magnitudes)
-    make a purely relative bound meaningless. Positions must also meet the
-    stated 1e-5 relative bound on the position itself."""
+    `scales` is the oracle's (force, velocity, displacement) term scales per
+    slot of `want` (OracleWorld.export_term_scales) when the compared span
+    contains a motion stage; without them velocities must agree to 1e-5 of
+    themselves. `source` is the light source irradiance that floors the
+    irradiance bound (default: 0, a purely relative bound). `velocities=False`
+    leaves velocities out (free-running trajectories, where contact dynamics
+    amplify FP32 rounding chaotically; positions stay compared). `before` is
+    accepted for call compatibility and not used: both sides start from the
+    same state, so |got - want| is the error of the step itself."""
     errs = []
     if got.n != want.n:
         return ["%s: count %d != %d" % (where, got.n, want.n)]
+    src = 0.0 if source is None else float(source)
     for name, t in agb.CELL_FIELDS:
         a, b = got[name], want[name]
         if name in INT_FIELDS:
@@ -60,27 +97,29 @@ def compare_cells(got, want, before=None, rtol=RTOL, where=""):
                 idx = np.nonzero(a != b)[0][:5]
                 errs.append("%s: %s differs in %d slots, e.g. %s" % (where, name, nd, idx.tolist()))
             continue
-        if name in ("x", "y", "z"):
-            # The stated bound, relative to the position (floored at one cell
-            # radius so that cells near the chamber centre are not held to
-            # sub-picometre agreement).
-            bb = np.maximum(np.abs(b.astype(np.float64)), agb.CELL_RADIUS)
-            nb = int(np.count_nonzero(np.abs(a.astype(np.float64) - b) > rtol * bb))
+        bb = np.abs(np.asarray(b, np.float64))
+        if name in POS_FIELDS:
+            nb, worst = _excess(a, b, rtol * np.maximum(bb, agb.CELL_RADIUS))
             if nb:
-                errs.append("%s: %s beyond 1e-5 relative in %d slots" % (where, name, nb))
-        if before is not None and name in DELTA_FIELDS and before.n == want.n:
-            p = before[name].astype(np.float64)
-            da, db = a.astype(np.float64) - p, b.astype(np.float64) - p
-            atol = 1e-4 * _rms(db) + 1e-300
-            if name in ("x", "y", "z"):
-                atol = max(atol, 1e-15)
-            if name == "energy":
-                atol = max(atol, 1e-15 * float(np.max(np.abs(p))))
-            nb, mx = _close(da, db, rtol, atol)
+                errs.append("%s: %s beyond 1e-5 of the coordinate (floor one radius) in %d slots (worst %.3g x)"
+                            % (where, name, nb, worst))
+            if scales is not None:
+                nb, worst = _excess(a, b, rtol * scales[2] + POS_ABS_FLOOR)
+                if nb:
+                    errs.append("%s: %s displacement beyond 1e-5 of its term scale in %d slots (worst %.3g x)"
+                                % (where, name, nb, worst))
+            continue
+        if name in VEL_FIELDS:
+            if not velocities:
+                continue
+            floor = rtol * scales[1] if scales is not None else 0.0
+            nb, worst = _excess(a, b, rtol * bb + floor + 1e-300)
+        elif name == "irradiance":
+            nb, worst = _excess(a, b, rtol * bb + rtol * src + 1e-300)
         else:
-            nb, mx = _close(a, b, rtol, 1e-4 * _rms(b) + 1e-30)
+            nb, worst = _excess(a, b, rtol * bb + 1e-300)
         if nb:
-            errs.append("%s: %s out of tolerance in %d slots (max abs diff %.3g)" % (where, name, nb, mx))
+            errs.append("%s: %s out of tolerance in %d slots (worst %.3g x the bound)" % (where, name, nb, worst))
     zero_a, zero_b = got["irradiance"] == 0.0, want["irradiance"] == 0.0
     nz = int(np.count_nonzero(zero_a != zero_b))
     if nz:
@@ -88,18 +127,23 @@ def compare_cells(got, want, before=None, rtol=RTOL, where=""):
     return errs
 
 
-def compare_forces(fg, fo, where="", rtol=RTOL):
+def compare_forces(fg, fo, where="", rtol=RTOL, scale=None):
+    """Per axis |got - want| <= rtol * |want| + rtol * force scale (the oracle's
+    per-cell summed magnitudes of the force's terms)."""
     errs = []
     for ax in range(3):
         b = np.asarray(fo[ax], np.float64)
-        nb, mx = _close(fg[ax], b, rtol, 1e-4 * _rms(b) + 1e-30)
+        floor = rtol * np.asarray(scale, np.float64) if scale is not None else 0.0
+        nb, worst = _excess(fg[ax], b, rtol * np.abs(b) + floor + 1e-300)
         if nb:
-            errs.append("%s: force axis %d out of tolerance in %d cells (max %.3g)" % (where, ax, nb, mx))
+            errs.append("%s: force axis %d out of tolerance in %d cells (worst %.3g x the bound)"
+                        % (where, ax, nb, worst))
     return errs
 
 
-def compare_fields(got_world, want_world, rtol=1e-6, exact=False, where=""):
+def compare_fields(got_world, want_world, rtol=RTOL, exact=False, where=""):
     errs = []
+    src = source_irradiance(want_world.desc)
     for f in range(4):
         if want_world.desc.grid[f].nx <= 0:
             continue
@@ -109,8 +153,9 @@ def compare_fields(got_world, want_world, rtol=1e-6, exact=False, where=""):
             if nd:
                 errs.append("%s: field %d differs in %d voxels (max %.3g)" % (where, f, nd, float(np.abs(a - b).max())))
         else:
-            scale = float(np.max(np.abs(b))) if b.size else 0.0
-            nb, mx = _close(a, b, rtol, 1e-3 * rtol * scale + 1e-30)
+            floor = rtol * src if f == agb.FIELD_IRR else 0.0
+            nb, worst = _excess(a, b, rtol * np.abs(b.astype(np.float64)) + floor + 1e-300)
             if nb:
-                errs.append("%s: field %d out of tolerance in %d voxels (max %.3g)" % (where, f, nb, mx))
+                errs.append("%s: field %d out of tolerance in %d voxels (worst %.3g x the bound)"
+                            % (where, f, nb, worst))
     return errs

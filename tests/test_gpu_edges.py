@@ -49,12 +49,13 @@ def test_single_cell_tracks_oracle():
     sc = dict(desc=S.slab_desc(cap=4), ticks=5,
               spawn=agb.spawn(1, charge_dist=agb.DIST_CONSTANT, charge_a=0.1, awake=True))
     gpu, orc = seeded(sc)
-    before, _ = orc.export_cells()
     gpu.step(1)
     orc.step(1)
     a, _ = gpu.export_cells()
     b, _ = orc.export_cells()
-    assert not P.compare_cells(a, b, before, where="tick 0")
+    errs = P.compare_cells(a, b, where="tick 0", scales=orc.export_term_scales(),
+                           source=P.source_irradiance(sc["desc"]))
+    assert not errs, "\n".join(errs)
     gpu.step(4, graph=True)
     orc.step(4)
     a, _ = gpu.export_cells()

@@ -57,12 +57,12 @@ def test_walk_shapes_track_oracle(name, lanes, fused):
     stage_by_stage(sc, lanes)
     gpu, orc = seeded(sc)
     assert gpu.walk(lanes, fused) == (lanes, fused)
-    before, _ = orc.export_cells()
     gpu.step(1, graph=True)
     orc.step(1)
     a, _ = gpu.export_cells()
     b, _ = orc.export_cells()
-    errs = P.compare_cells(a, b, before, where="tick 0")
+    errs = P.compare_cells(a, b, where="tick 0", scales=orc.export_term_scales(),
+                           source=P.source_irradiance(sc["desc"]))
     assert not errs, "\n".join(errs[:20])
     gpu.step(sc["ticks"], graph=True)
     orc.step(sc["ticks"])
@@ -73,14 +73,14 @@ def test_walk_shapes_track_oracle(name, lanes, fused):
         assert np.array_equal(a[k], b[k]), k
 
 
-def stage_by_stage(sc, lanes=None, force_rtol=P.RTOL):
+def stage_by_stage(sc, lanes=None):
     gpu, orc = seeded(sc)
     if lanes is not None:
         gpu.walk(lanes=lanes)
     errs = []
+    src = P.source_irradiance(sc["desc"])
     for t in range(sc["ticks"]):
         for stage, sname in S.stages_for(sc["desc"]):
-            before, _ = orc.export_cells()
             P.copy_state(orc, gpu)
             if stage in (agb.STAGE_EMISSION, agb.STAGE_MOTION):
                 # Both walk the hash built at the top of the tick; positions have
@@ -93,10 +93,11 @@ def stage_by_stage(sc, lanes=None, force_rtol=P.RTOL):
             where = "tick %d %s" % (t, sname)
             a, _ = gpu.export_cells()
             b, _ = orc.export_cells()
-            errs += P.compare_cells(a, b, before, where=where)
+            scales = orc.export_term_scales() if stage == agb.STAGE_MOTION else None
+            errs += P.compare_cells(a, b, where=where, scales=scales, source=src)
             errs += P.compare_fields(gpu, orc, where=where)
             if stage == agb.STAGE_MOTION:
-                errs += P.compare_forces(gpu.export_forces(), orc.export_forces(), where, force_rtol)
+                errs += P.compare_forces(gpu.export_forces(), orc.export_forces(), where, scale=scales[0])
     assert not errs, "\n".join(errs[:20])
 
 
@@ -145,10 +146,10 @@ def _bucket_face_pairs(cells, desc):
 
 # Contact forces here come from overlaps down to 1e-4 of a diameter: the
 # FP32 contact path forms (2a - r) with r good to about 1.5 ulp (1.4e-12 m),
-# so at a 1e-9 m overlap their relative error reaches ~1.4e-3 (measured:
-# 1.37e-3; the FP64 settle band starts at overlaps of 1e-5). A contact the
-# walk missed would be off by 100% of that force.
-FACE_FORCE_RTOL = 1e-2
+# so at a 1e-9 m overlap the force's own relative error reaches ~1.4e-3, while
+# its error against the contact's full-overlap force k * 2a (the force scale
+# that floors the bound) stays near 1.4e-7. A contact the walk missed would be
+# off by the whole contact force.
 
 
 @pytest.mark.parametrize("lanes,fused", [(1, False), (2, False), (1, True), (2, True)])
@@ -160,16 +161,16 @@ def test_contacts_across_bucket_faces(lanes, fused):
     d.contact_enabled = 1
     sc = dict(desc=d, ticks=1, mutate=_bucket_face_pairs,              # 318 cells, all placed
               spawn=agb.spawn(318, charge_dist=agb.DIST_UNIFORM, charge_a=0.0, charge_b=0.2, awake=True))
-    stage_by_stage(sc, lanes, FACE_FORCE_RTOL)
+    stage_by_stage(sc, lanes)
     gpu, orc = seeded(sc)
     gpu.walk(lanes, fused)
-    before, _ = orc.export_cells()
     gpu.step(1, graph=True)
     orc.step(1)
     a, _ = gpu.export_cells()
     b, _ = orc.export_cells()
-    errs = P.compare_cells(a, b, before, where="tick")
-    errs += P.compare_forces(gpu.export_forces(), orc.export_forces(), "tick", FACE_FORCE_RTOL)
+    scales = orc.export_term_scales()
+    errs = P.compare_cells(a, b, where="tick", scales=scales, source=P.source_irradiance(d))
+    errs += P.compare_forces(gpu.export_forces(), orc.export_forces(), "tick", scale=scales[0])
     assert not errs, "\n".join(errs[:20])
 
 
@@ -178,12 +179,12 @@ def test_full_ticks_track_oracle(name):
     """Whole ticks without re-synchronisation: integer state must stay equal."""
     sc = S.scenarios()[name]
     gpu, orc = seeded(sc)
-    before, _ = orc.export_cells()
     gpu.step(1)
     orc.step(1)
     a, _ = gpu.export_cells()
     b, _ = orc.export_cells()
-    errs = P.compare_cells(a, b, before, where="tick 0")
+    errs = P.compare_cells(a, b, where="tick 0", scales=orc.export_term_scales(),
+                           source=P.source_irradiance(sc["desc"]))
     errs += P.compare_fields(gpu, orc, where="tick 0")
     assert not errs, "\n".join(errs[:20])
     gpu.step(sc["ticks"])
@@ -206,15 +207,17 @@ def test_against_reference_fixture(name):
     sc = S.scenarios()[name]
     gold = np.load(os.path.join(H.GOLDEN, name + "_tick0.npz"))
     gpu, orc = seeded(sc)
-    before, _ = orc.export_cells()
     gpu.step(1)
+    orc.step(1)                      # equals the fixture bit for bit (test_oracle_golden); gives the term scales
     a, _ = gpu.export_cells()
     ref = agb.CellArrays.from_dict({k[5:]: gold[k] for k in gold.files if k.startswith("cell_")})
-    errs = P.compare_cells(a, ref, before, where="vs reference")
+    errs = P.compare_cells(a, ref, where="vs reference", scales=orc.export_term_scales(),
+                           source=P.source_irradiance(sc["desc"]))
+    src = P.source_irradiance(sc["desc"])
     for f in range(4):
-        g, r = gpu.export_field(f), gold["field_%d" % f]
-        tol = 1e-6 * np.max(np.abs(r)) + 1e-30
-        if np.abs(g - r).max() > tol:
+        g, r = gpu.export_field(f).astype(np.float64), gold["field_%d" % f].astype(np.float64)
+        tol = P.RTOL * np.abs(r) + (P.RTOL * src if f == agb.FIELD_IRR else 0.0) + 1e-300
+        if (np.abs(g - r) > tol).any():
             errs.append("field %d max diff %g" % (f, float(np.abs(g - r).max())))
     assert not errs, "\n".join(errs[:20])
 
