@@ -107,7 +107,7 @@ _CT = {np.uint64: C.c_uint64, np.uint32: C.c_uint32, np.uint8: C.c_uint8, np.int
 
 
 class Cells(C.Structure):
-    _fields_ = [(n, C.POINTER(_CT[t])) for n, t in CELL_FIELDS]
+    _fields_ = [(n, C.POINTER(_CT[t])) for n, t in CELL_FIELDS] + [("count", C.c_int32), ("capacity", C.c_int32)]
 
 
 class Taumoeba(C.Structure):

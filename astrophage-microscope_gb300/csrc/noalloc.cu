@@ -55,6 +55,10 @@ extern "C" agb_status agb_grid_diffuse_noalloc(float* value, int32_t nx, int32_t
         return AGB_INVALID_ARGUMENT;
     const int64_t count = (int64_t)nx * ny * nz;
     if (count > (int64_t)AGB_NOALLOC_MAX_VOXELS) return AGB_CAPACITY_EXCEEDED;
+    // Within the voxel limit, a very tall and thin grid (e.g. 4 x 1,048,576 x 1)
+    // still exceeds the stencil's launch grid (65,535 blocks of 8 rows along y,
+    // and of 8 planes along z): refused before anything is launched or copied.
+    if (!agb::ftcs_plain_fits(nx, ny, nz)) return AGB_UNSUPPORTED;
     // Substeps and coefficient as grid_diffuse computes them (1/6 bound in 3-D).
     const double lim = nz > 1 ? 6.0 : 4.0;
     const int32_t steps = (int32_t)(dt / (dx * dx / (lim * diffusivity))) + 1;
@@ -74,11 +78,14 @@ extern "C" agb_status agb_grid_diffuse_noalloc(float* value, int32_t nx, int32_t
     float* src = value;
     float* dst = scratch;
     for (int32_t k = 0; k < steps; ++k) {
-        agb::launch_ftcs(g, src, dst, coeff, bc, face, robin, nullptr, nullptr, nullptr, s);
+        // A pass that fails to launch ends the call before the final copy, so
+        // the caller's buffer is never overwritten from a half-done sequence.
+        if (agb::launch_ftcs(g, src, dst, coeff, bc, face, robin, nullptr, nullptr, nullptr, s) != cudaSuccess)
+            return AGB_CUDA_ERROR;
         float* t = src; src = dst; dst = t;
     }
     if (src != value &&
         cudaMemcpyAsync(value, src, sizeof(float) * (size_t)count, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
         return AGB_CUDA_ERROR;
-    return cudaGetLastError() == cudaSuccess ? AGB_OK : AGB_CUDA_ERROR;
+    return AGB_OK;
 }

@@ -950,7 +950,7 @@ agb_status agb_world_device_cells(agb_world* w, agb_cells* dev) {
     agb_cells c = {v.id, v.flags, v.death_cause, v.x, v.y, v.z, v.vx, v.vy, v.vz, v.energy,
                    v.temp_cell, v.emit_power, v.dir_x, v.dir_y, v.dir_z, v.biomass, v.co2_held,
                    v.age_s, v.rng_state, v.taxis_memory, v.run_timer, v.t_local, v.irradiance,
-                   v.co2_local, v.n2_local};
+                   v.co2_local, v.n2_local, st.count, w->c.capacity};
     *dev = c;
     return AGB_OK;
 }
@@ -1003,6 +1003,8 @@ agb_status agb_world_export_cells(agb_world* w, agb_cells* dst, int32_t max_coun
         AGB_CUDA(w, cudaStreamSynchronize(s));
         if (count) *count = (int32_t)w->xfer_host[0];
         if (next_id) *next_id = (uint64_t)w->xfer_host[1];
+        dst->count = (int32_t)w->xfer_host[0];
+        dst->capacity = max_count;
         return AGB_OK;
     }
     DevState st;
@@ -1017,6 +1019,8 @@ agb_status agb_world_export_cells(agb_world* w, agb_cells* dst, int32_t max_coun
     AGB_CUDA(w, cudaStreamSynchronize(s));
     if (count) *count = st.count;
     if (next_id) *next_id = st.next_id;
+    dst->count = st.count;
+    dst->capacity = max_count;
     return AGB_OK;
 }
 

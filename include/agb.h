@@ -129,8 +129,13 @@ typedef struct agb_world_desc {
     int32_t tau_compaction_enabled;
 } agb_world_desc;
 
-/* Host view of the 25 SoA arrays of contracts/cell_store_v1.h:42-75, field for
- * field. Any pointer may be NULL in export calls (that array is skipped). */
+/* CellStoreView (contracts/cell_store_v1.h:42-78), member for member and at the
+ * same offsets: the 25 SoA arrays, then count and capacity, so a reference
+ * caller's view can be passed as it is. Any pointer may be NULL in export
+ * calls (that array is skipped). The import calls take the cell count as an
+ * argument and ignore `count` and `capacity` here; the export calls set
+ * `count` to the population and `capacity` to the caller's array length;
+ * agb_world_device_cells sets both from the store. */
 typedef struct agb_cells {
     uint64_t* id;
     uint32_t* flags;
@@ -151,6 +156,8 @@ typedef struct agb_cells {
     float* irradiance;
     float* co2_local;
     float* n2_local;
+    int32_t count;
+    int32_t capacity;
 } agb_cells;
 
 /* src/sim/cell_store.cuh:15-28 SpawnParams. Placements 0-3 and distributions
@@ -437,8 +444,12 @@ agb_status agb_world_diffuse(agb_world* w, int32_t field, double dt, agb_stream 
  * loops that cannot afford cudaMalloc's implicit synchronisation.
  * `value` is nx*ny*nz floats, x fastest; dx is the isotropic spacing; bc and
  * face_value follow agb_grid_desc; the result is left in `value`.
- * Returns AGB_CAPACITY_EXCEEDED for grids larger than AGB_NOALLOC_MAX_VOXELS.
- * The first call on a device resolves the scratch array's device address
+ * Returns AGB_CAPACITY_EXCEEDED for grids larger than AGB_NOALLOC_MAX_VOXELS,
+ * and AGB_UNSUPPORTED for grids within it whose stencil launch would need more
+ * than 65,535 blocks along y or z (ny > 524,280, or nz > 524,280); in both
+ * cases nothing is launched and `value` is untouched. If a stencil pass fails
+ * to launch, the call returns AGB_CUDA_ERROR before its final copy into
+ * `value`. The first call on a device resolves the scratch array's device address
  * (cudaGetSymbolAddress); make that first call before any stream capture.
  * All calls share the scratch array: calls whose work overlaps on the GPU race.
  * Its contents are left over from the previous call and need no clearing. */

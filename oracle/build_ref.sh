@@ -9,9 +9,11 @@
 # (src/sim/scenario.cpp, accept.cpp) are built too, and the scenario files are
 # placed beside the library as test inputs. Test infrastructure only.
 #
-# Usage: sh oracle/build_ref.sh [reference_root]
+# Usage: sh oracle/build_ref.sh reference_root
+#    or: AGB_REFERENCE_DIR=reference_root sh oracle/build_ref.sh
 set -eu
-REF="${1:-${ASTRO_REFERENCE:-/root/reference}}"
+REF="${1:-${AGB_REFERENCE_DIR:-}}"
+[ -n "$REF" ] || { echo "usage: build_ref.sh reference_root (or set AGB_REFERENCE_DIR)" >&2; exit 2; }
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 [ -d "$REF/src/sim" ] || { echo "reference sources not found at $REF" >&2; exit 2; }

@@ -6,7 +6,8 @@ every scenario in tests/scenarios.py through its World API, recording a
 digest of every array after every stage of every tick, the final Stats, and
 for three scenarios the full state after the first tick; and the fields after
 each of a list of brush strokes. Run from the repo
-root: python tests/golden/make_golden.py [reference_root]
+root: python tests/golden/make_golden.py reference_root (or with the reference's
+root in AGB_REFERENCE_DIR).
 """
 import json
 import os
@@ -22,7 +23,9 @@ import scenarios as S  # noqa: E402
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("AGB_REFERENCE_DIR", "")
+    if not ref_root:
+        sys.exit("usage: make_golden.py reference_root (or set AGB_REFERENCE_DIR)")
     subprocess.check_call(["sh", os.path.join(H.ROOT, "oracle", "build_ref.sh"), ref_root])
     full_for = {"slab_uniform", "lifecycle_compaction", "collinear_shadow"}
     for name, sc in S.scenarios().items():

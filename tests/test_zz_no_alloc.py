@@ -12,7 +12,9 @@ on the same field: two calls in a row, each compared after it returns, with
 the tolerance the other diffusion tests use (bit for bit). Runs the same alone
 in a fresh process (the first call resolves the scratch address) or after the
 other tests (the scratch then holds an earlier call's data, which must not
-matter).
+matter). Also checked: grids beyond the scratch or beyond the stencil's launch
+grid are refused without touching the caller's buffer, and calls after the
+first leave the device's free memory unchanged.
 """
 import numpy as np
 import pytest
@@ -78,3 +80,37 @@ def test_noalloc_rejects_grids_beyond_the_scratch():
     assert agb.status_name(rc) == "CapacityExceeded"
     torch.cuda.synchronize()
     assert float(buf.abs().sum().item()) == 0.0, "nothing may be written when the call is rejected"
+
+
+@pytest.mark.parametrize("nx,ny,nz", [(4, 1048576, 1), (2, 2, 1048576)])
+def test_noalloc_rejects_unlaunchable_shapes(nx, ny, nz):
+    """Grids within the voxel limit whose stencil launch would need more than
+    65,535 blocks along y or z are refused up front; the buffer is untouched."""
+    torch = pytest.importorskip("torch")
+    assert nx * ny * nz <= agb.NOALLOC_MAX_VOXELS
+    gen = torch.Generator(device="cuda").manual_seed(5)
+    buf = 280.0 + 40.0 * torch.rand(nx * ny * nz, dtype=torch.float32, device="cuda", generator=gen)
+    before = buf.clone()
+    rc = agb.grid_diffuse_noalloc(buf.data_ptr(), nx, ny, nz, 1e-5, 1e-9, 1e-3, [agb.BC_NEUMANN] * 6, [0.0] * 6)
+    assert agb.status_name(rc) == "Unsupported"
+    torch.cuda.synchronize()
+    assert torch.equal(buf, before), "a refused call must leave the caller's field as it was"
+
+
+def test_noalloc_allocates_nothing():
+    """The property the entry point exists for: once the first call on the
+    device has resolved the scratch array, further calls leave the device's
+    free memory exactly where it was."""
+    torch = pytest.importorskip("torch")
+    n = 96
+    bufs = [torch.full((n, n, n), 300.0, dtype=torch.float32, device="cuda") for _ in range(3)]
+    bufs[0][n // 2, n // 2, n // 2] = 400.0
+    args = (n, n, n, 1e-5, agb.WATER_THERMAL_DIFFUSIVITY, 1e-3, [agb.BC_NEUMANN] * 6, [0.0] * 6)
+    assert agb.grid_diffuse_noalloc(bufs[0].data_ptr(), *args) == agb.OK
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for b in bufs:
+        for _ in range(3):
+            assert agb.grid_diffuse_noalloc(b.data_ptr(), *args) == agb.OK
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
