@@ -342,6 +342,9 @@ def load(path=LIB_PATH):
         "agb_world_flash_audit": (I32, [P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
         "agb_world_step": (I32, [P, I32, P]),
         "agb_world_step_graph": (I32, [P, I32, P]),
+        "agb_world_prepare_graphs": (I32, [P, I32, P]),
+        "agb_world_set_timing": (I32, [P, I32]),
+        "agb_world_section_times": (I32, [P, P]),
         "agb_world_stage": (I32, [P, I32, P]),
         "agb_world_graph_kernels": (I32, [P, C.POINTER(C.c_int64)]),
         "agb_world_set_walk": (I32, [P, I32, I32]),
@@ -404,7 +407,8 @@ def exported_symbols():
             "agb_world_import_field", "agb_world_export_field", "agb_world_export_deposit",
             "agb_world_apply_brush", "agb_world_set_flash", "agb_world_flash_audit",
             "agb_world_spawn_taumoeba", "agb_world_import_taumoeba", "agb_world_export_taumoeba",
-            "agb_world_step", "agb_world_step_graph", "agb_world_graph_kernels", "agb_world_set_walk",
+            "agb_world_step", "agb_world_step_graph", "agb_world_prepare_graphs", "agb_world_set_timing",
+            "agb_world_section_times", "agb_world_graph_kernels", "agb_world_set_walk",
             "agb_world_walk", "agb_world_stage",
             "agb_world_diffuse",
             "agb_world_stats", "agb_world_stats_accum", "agb_world_set_clock",
@@ -569,6 +573,24 @@ class World:
     def step(self, ticks=1, graph=False, stream=None):
         fn = self.lib.agb_world_step_graph if graph else self.lib.agb_world_step
         self._check(fn(self.h, ticks, _st(stream)), "step")
+
+    def prepare_graphs(self, ticks=1, stream=None):
+        """Capture every graph step(ticks, graph=True) will replay, without running
+        them (agb_world_prepare_graphs); the world's state is unchanged."""
+        self._check(self.lib.agb_world_prepare_graphs(self.h, ticks, _st(stream)), "prepare_graphs")
+
+    SECTIONS = ("tick", "thermal", "t_diffuse", "irradiance", "slow_fields", "hash", "cell_pass", "integrate",
+                "lifecycle")
+
+    def set_timing(self, enable):
+        """Section timers around the tick's parts, inside captured graphs too."""
+        self._check(self.lib.agb_world_set_timing(self.h, int(bool(enable))), "set_timing")
+
+    def section_times(self):
+        """{section: milliseconds} of the last tick (sections that have not run: absent)."""
+        out = np.zeros(len(self.SECTIONS), np.float32)
+        self._check(self.lib.agb_world_section_times(self.h, out.ctypes.data), "section_times")
+        return {k: float(v) for k, v in zip(self.SECTIONS, out) if v >= 0.0}
 
     def stage(self, s):
         self._check(self.lib.agb_world_stage(self.h, s, None), "stage %d" % s)

@@ -343,9 +343,16 @@ void stage_clock(agb_world* w) {
 // writes the other ping-pong buffer.
 void tick_surrogate(agb_world* w, cudaStream_t s);
 
+// A section timer mark (start = 0, end = 1) on stream s when timing is on;
+// an external event record, so that stream capture keeps it as a graph node.
+static void mark(agb_world* w, int section, int end, cudaStream_t s) {
+    if (w->timing) cudaEventRecordWithFlags(w->tev[2 * section + end], s, cudaEventRecordExternal);
+}
+
 void tick_once(agb_world* w, cudaStream_t s) {
     if (w->sg) { tick_surrogate(w, s); return; }
     cudaStream_t s1 = w->side[0], s2 = w->side[1], s3 = w->side[2];
+    mark(w, AGB_SECTION_TICK, 0, s);
     cudaEventRecord(w->ev[0], s);
     cudaStreamWaitEvent(s1, w->ev[0], 0);
     cudaStreamWaitEvent(s2, w->ev[0], 0);
@@ -354,6 +361,7 @@ void tick_once(agb_world* w, cudaStream_t s) {
     // has run.
     const bool thermal = w->d.thermal_enabled && w->c.g[AGB_FIELD_TEMPERATURE].enabled;
     const int32_t nsub = thermal ? w->tp.t_substeps : 0;
+    if (nsub > 0) mark(w, AGB_SECTION_THERMAL, 0, s1);
     for (int32_t k = 0; k < nsub; ++k) {
         refresh_grid_ptrs(w);
         launch_thermal(w->S, w->c, w->tp, w->blocks, s1);
@@ -361,26 +369,36 @@ void tick_once(agb_world* w, cudaStream_t s) {
         launch_flush_by_cells(w->S, w->c.g[AGB_FIELD_TEMPERATURE], nullptr, w->blocks, s1);
         ftcs(w, AGB_FIELD_TEMPERATURE, w->tp.t_coeff, s1);
     }
+    if (nsub > 0) mark(w, AGB_SECTION_THERMAL, 1, s1);
     cudaEventRecord(w->ev[3], s1);
     cudaStreamWaitEvent(s3, w->ev[3], 0);
     if (nsub > 0) {
+        mark(w, AGB_SECTION_T_DIFFUSE, 0, s3);
         launch_flush_by_cells(w->S, w->c.g[AGB_FIELD_TEMPERATURE], nullptr, w->blocks, s3);
         ftcs(w, AGB_FIELD_TEMPERATURE, w->tp.t_coeff, s3);
+        mark(w, AGB_SECTION_T_DIFFUSE, 1, s3);
     }
     cudaEventRecord(w->ev[4], s3);
     const bool emit = emission_active(w);
     if (emit) {
         refresh_grid_ptrs(w);
+        mark(w, AGB_SECTION_IRRADIANCE, 0, s1);
         launch_emission_prep(w->S, w->c, w->tp, w->stamp_idx, w->occl_factor, w->c.source > 0.0f, w->blocks, s1);
+        mark(w, AGB_SECTION_IRRADIANCE, 1, s1);
     }
     cudaEventRecord(w->ev[1], s1);
     refresh_grid_ptrs(w);
     const Ctx pre = w->c;                       // CO2/N2 as motion must see them
+    mark(w, AGB_SECTION_SLOW_FIELDS, 0, s2);
     stage_slow_fields(w, s2);
+    mark(w, AGB_SECTION_SLOW_FIELDS, 1, s2);
     cudaEventRecord(w->ev[2], s2);
+    mark(w, AGB_SECTION_HASH, 0, s);
     stage_hash(w, s);
+    mark(w, AGB_SECTION_HASH, 1, s);
     cudaStreamWaitEvent(s, w->ev[1], 0);
     cudaStreamWaitEvent(s, w->ev[4], 0);
+    mark(w, AGB_SECTION_CELL_PASS, 0, s);
     // Feeding, taxis (step.cu:161-162) and forces: one kernel per cell pass,
     // or the three passes in turn. Feeding reads only the irradiance grid.
     Ctx c = w->c;
@@ -395,7 +413,9 @@ void tick_once(agb_world* w, cudaStream_t s) {
         stage_flash_or_taxis(w, s);
         launch_forces(w->S, c, w->tp, w->fx, w->fy, w->fz, w->blocks, w->walk_lanes, s);
     }
+    mark(w, AGB_SECTION_CELL_PASS, 1, s);
     cudaStreamWaitEvent(s, w->ev[2], 0);
+    mark(w, AGB_SECTION_INTEGRATE, 0, s);
     const GridDev& co2 = w->c.g[AGB_FIELD_CO2];
     const float inv_gv = co2.enabled ? (float)(1.0 / (co2.dx * co2.dx * co2.dz_eff)) : 0.0f;
     // With predators the CO2 demand waits for predation (it kills prey before
@@ -404,8 +424,12 @@ void tick_once(agb_world* w, cudaStream_t s) {
     const bool fuse_demand = co2.enabled && !w->tau_active;
     launch_integrate(w->S, c, w->tp, w->fx, w->fy, w->fz, w->blocks, co2,
                      fuse_demand ? w->life.co2_demand : nullptr, inv_gv, s);
+    mark(w, AGB_SECTION_INTEGRATE, 1, s);
+    mark(w, AGB_SECTION_LIFECYCLE, 0, s);
     stage_predation(w, s);
     stage_lifecycle(w, s, fuse_demand);
+    mark(w, AGB_SECTION_LIFECYCLE, 1, s);
+    mark(w, AGB_SECTION_TICK, 1, s);
     stage_clock(w);
 }
 
@@ -699,6 +723,7 @@ void agb_world_destroy(agb_world* w) {
     if (w->own_stream) cudaStreamDestroy(w->own_stream);
     for (cudaStream_t& st : w->side) if (st) cudaStreamDestroy(st);
     for (cudaEvent_t& e : w->ev) if (e) cudaEventDestroy(e);
+    for (cudaEvent_t& e : w->tev) if (e) cudaEventDestroy(e);
     for (void* p : w->allocs) cudaFree(p);
     if (w->xfer_host) cudaFreeHost(w->xfer_host);
     delete w;
@@ -1221,36 +1246,18 @@ agb_status agb_world_step(agb_world* w, int32_t ticks, agb_stream s) {
     return AGB_OK;
 }
 
-agb_status agb_world_step_graph(agb_world* w, int32_t ticks, agb_stream s) {
-    if (!w || ticks <= 0) return AGB_INVALID_ARGUMENT;
-    if (w->sg) return agb_world_step(w, ticks, s);    // the judge reads results on the host: no capture
+// Captures `ticks` ticks from the world's current host-side state into a new
+// cached graph (not launched). Capture runs tick_once, which advances the
+// host-side tick state (buffer parities, tick, clock) as the replay will.
+static agb_status capture_entry(agb_world* w, int32_t ticks, cudaStream_t s, GraphEntry** out) {
     const uint64_t P = w->d.compaction_period > 0 ? (uint64_t)w->d.compaction_period : 1;
-    const uint32_t par = parity_bits(w);
-    const uint64_t phase = w->tick % P;
-    if (s == nullptr && w->own_stream) s = w->own_stream;
-    for (const GraphEntry& g : w->graphs) {
-        if (g.ticks == ticks && g.parity == par && g.tick_phase == phase) {
-            AGB_CUDA(w, cudaGraphLaunch(g.exec, s));
-            w->graph_kernels_total += g.kernels;
-            for (int f = 0; f < AGB_FIELD_COUNT; ++f) w->gcur[f] = (g.parity_after >> f) & 1;
-            refresh_grid_ptrs(w);
-            w->tick += (uint64_t)ticks;
-            w->sim_time += w->tp.dt * ticks;
-            return AGB_OK;
-        }
-    }
-    if (s == nullptr) {
-        // Capture needs a stream other than the legacy default one; a blocking
-        // stream keeps the launch ordered with the caller's default-stream work.
-        if (!w->own_stream) AGB_CUDA(w, cudaStreamCreate(&w->own_stream));
-        s = w->own_stream;
-    }
     cudaGraph_t graph;
+    GraphEntry e{ticks, parity_bits(w), w->tick % P, nullptr, 0, 0};
     AGB_CUDA(w, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     for (int32_t t = 0; t < ticks; ++t) tick_once(w, s);
     const cudaError_t ce = cudaStreamEndCapture(s, &graph);
     if (ce != cudaSuccess) return cuda_fail(w, ce, "cudaStreamEndCapture");
-    GraphEntry e{ticks, par, phase, nullptr, parity_bits(w), 0};
+    e.parity_after = parity_bits(w);
     {
         size_t nn = 0;
         cudaGraphGetNodes(graph, nullptr, &nn);
@@ -1265,9 +1272,113 @@ agb_status agb_world_step_graph(agb_world* w, int32_t ticks, agb_stream s) {
     cudaGraphDestroy(graph);
     if (ie != cudaSuccess) return cuda_fail(w, ie, "cudaGraphInstantiate");
     w->graphs.push_back(e);
-    w->graph_kernels_total += e.kernels;
+    *out = &w->graphs.back();
+    return AGB_OK;
+}
+
+static GraphEntry* find_entry(agb_world* w, int32_t ticks) {
+    const uint64_t P = w->d.compaction_period > 0 ? (uint64_t)w->d.compaction_period : 1;
+    const uint32_t par = parity_bits(w);
+    const uint64_t phase = w->tick % P;
+    for (GraphEntry& g : w->graphs)
+        if (g.ticks == ticks && g.parity == par && g.tick_phase == phase) return &g;
+    return nullptr;
+}
+
+// The host-side effect of replaying a cached graph: buffer parities, tick, clock.
+static void advance_as_replay(agb_world* w, const GraphEntry& g) {
+    for (int f = 0; f < AGB_FIELD_COUNT; ++f) w->gcur[f] = (g.parity_after >> f) & 1;
+    refresh_grid_ptrs(w);
+    w->tick += (uint64_t)g.ticks;
+    w->sim_time += w->tp.dt * g.ticks;
+}
+
+agb_status agb_world_step_graph(agb_world* w, int32_t ticks, agb_stream s) {
+    if (!w || ticks <= 0) return AGB_INVALID_ARGUMENT;
+    if (w->sg) return agb_world_step(w, ticks, s);    // the judge reads results on the host: no capture
+    if (s == nullptr && w->own_stream) s = w->own_stream;
+    if (GraphEntry* g = find_entry(w, ticks)) {
+        AGB_CUDA(w, cudaGraphLaunch(g->exec, s));
+        w->graph_kernels_total += g->kernels;
+        advance_as_replay(w, *g);
+        return AGB_OK;
+    }
+    if (s == nullptr) {
+        // Capture needs a stream other than the legacy default one; a blocking
+        // stream keeps the launch ordered with the caller's default-stream work.
+        if (!w->own_stream) AGB_CUDA(w, cudaStreamCreate(&w->own_stream));
+        s = w->own_stream;
+    }
+    GraphEntry* g = nullptr;
+    const agb_status rc = capture_entry(w, ticks, s, &g);
+    if (rc != AGB_OK) return rc;
+    w->graph_kernels_total += g->kernels;
     // Capture advanced the host-side tick state; the graph has not run yet.
-    AGB_CUDA(w, cudaGraphLaunch(e.exec, s));
+    AGB_CUDA(w, cudaGraphLaunch(g->exec, s));
+    return AGB_OK;
+}
+
+agb_status agb_world_prepare_graphs(agb_world* w, int32_t ticks, agb_stream stream) {
+    if (!w || ticks <= 0) return AGB_INVALID_ARGUMENT;
+    if (w->sg) return AGB_OK;                           // surrogate-driven worlds step eagerly
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (s == nullptr) {
+        if (!w->own_stream) AGB_CUDA(w, cudaStreamCreate(&w->own_stream));
+        s = w->own_stream;
+    }
+    int saved_gcur[AGB_FIELD_COUNT];
+    for (int f = 0; f < AGB_FIELD_COUNT; ++f) saved_gcur[f] = w->gcur[f];
+    const uint64_t saved_tick = w->tick;
+    const double saved_time = w->sim_time;
+    // Walk the (buffer parities, tick phase) states that stepping by `ticks`
+    // visits from here until one repeats; capture each state's graph once.
+    const uint64_t P = w->d.compaction_period > 0 ? (uint64_t)w->d.compaction_period : 1;
+    const uint64_t limit = 4 * P * (uint64_t)(1u << AGB_FIELD_COUNT) + 8;
+    std::vector<std::pair<uint32_t, uint64_t>> seen;
+    agb_status rc = AGB_OK;
+    for (uint64_t it = 0; it < limit && rc == AGB_OK; ++it) {
+        const std::pair<uint32_t, uint64_t> key{parity_bits(w), w->tick % P};
+        bool repeat = false;
+        for (const auto& k : seen) repeat = repeat || (k == key);
+        if (repeat) break;
+        seen.push_back(key);
+        if (GraphEntry* g = find_entry(w, ticks)) {
+            advance_as_replay(w, *g);
+        } else {
+            GraphEntry* ng = nullptr;
+            rc = capture_entry(w, ticks, s, &ng);
+        }
+    }
+    for (int f = 0; f < AGB_FIELD_COUNT; ++f) w->gcur[f] = saved_gcur[f];
+    refresh_grid_ptrs(w);
+    w->tick = saved_tick;
+    w->sim_time = saved_time;
+    return rc;
+}
+
+agb_status agb_world_set_timing(agb_world* w, int32_t enable) {
+    if (!w) return AGB_INVALID_ARGUMENT;
+    const bool on = enable != 0;
+    if (on && !w->tev[0])
+        for (cudaEvent_t& e : w->tev) AGB_CUDA(w, cudaEventCreate(&e));
+    if (on != w->timing) {
+        w->timing = on;
+        invalidate_graphs(w);
+    }
+    return AGB_OK;
+}
+
+agb_status agb_world_section_times(agb_world* w, float ms[AGB_TICK_SECTIONS]) {
+    if (!w || !ms) return AGB_INVALID_ARGUMENT;
+    for (int k = 0; k < AGB_TICK_SECTIONS; ++k) ms[k] = -1.0f;
+    if (!w->timing) return AGB_OK;
+    AGB_CUDA(w, cudaEventSynchronize(w->tev[2 * AGB_SECTION_TICK + 1]));
+    for (int k = 0; k < AGB_TICK_SECTIONS; ++k) {
+        float t = -1.0f;
+        if (cudaEventElapsedTime(&t, w->tev[2 * k], w->tev[2 * k + 1]) != cudaSuccess) t = -1.0f;
+        ms[k] = t;
+    }
+    (void)cudaGetLastError();     // a section that has not run leaves an unrecorded event: not an error here
     return AGB_OK;
 }
 

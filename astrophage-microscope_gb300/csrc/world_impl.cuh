@@ -45,6 +45,10 @@ struct agb_world {
     double* occl_factor = nullptr;       // per irradiance voxel: transmittance of stamped voxels
     cudaStream_t side[3] = {nullptr, nullptr, nullptr};   // concurrent branches of a tick
     cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    // Section timers (agb_world_set_timing): a start and an end event per
+    // section of the tick, recorded into the captured graph as event nodes.
+    bool timing = false;
+    cudaEvent_t tev[2 * AGB_TICK_SECTIONS] = {};
     float *fx = nullptr, *fy = nullptr, *fz = nullptr;
     unsigned long long* acc = nullptr;
     int32_t blocks = 1;

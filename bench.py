@@ -1,15 +1,22 @@
 #!/usr/bin/env python3
 """Throughput of the per-tick physics step on GB300 (cell-steps/s, voxel-steps/s).
 
-Default workload (the plain step at README scale): a 4 mm cubic chamber with
-25,000 cells uniform in a 550 um-wide slab, lognormal charge (median 3 %,
-sigma_ln 0.5, clipped at 0.2), 128^3 temperature and CO2 grids, light along +x,
-division at a stored-energy threshold with compaction every 10 ticks, dt = 1 ms.
-Inputs are synthetic and seeded (the engine's own PCG32 spawn).
+Headline workload (the plain step at README scale, slab25k): a 4 mm cubic
+chamber with 25,000 cells uniform in a 550 um-wide slab, lognormal charge
+(median 3 %, sigma_ln 0.5, clipped at 0.2), 128^3 temperature and CO2 grids,
+light along +x, division at a stored-energy threshold with compaction every 10
+ticks, dt = 1 ms. Inputs are synthetic and seeded (the engine's own PCG32
+spawn); the workloads live in astrophage-microscope_gb300/workloads.py.
 
-One bench step is one tick of the whole world, replayed as a CUDA graph. The
-L2 cache is flushed (a 256 MB write) between timed steps, outside the timed
-intervals, which are CUDA events on the stream the tick runs on.
+One bench step is one tick of the whole world, replayed as a CUDA graph; every
+tick phase's graph is captured during setup, before warm-up. The L2 cache is
+flushed (a 256 MB write) between timed steps, outside the timed intervals,
+which are CUDA events on the stream the tick runs on. Beside the headline the
+line carries: per-step statistics, the duration of each section of the tick
+(in-graph timing events) and the roofline of the longest one, one FTCS pass's
+roofline, the end-to-end loop through the C ABI with pinned host buffers, the
+CPU baseline, the 1M-cell cluster workload (`scaled`, the HBM-graded
+configuration), the 64-chamber batch and the learned surrogate.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -41,100 +48,13 @@ EMAX = agb.CELL_ENERGY_MAX
 
 
 # ---------------------------------------------------------------------------
-# Workloads
+# Workloads (shared with the parity tests)
 # ---------------------------------------------------------------------------
-def _grid3(n, D, init, scale, bc, face=None):
-    return agb.grid(n, n, D, init, scale, bc, face_value=face)
-
-
-def workload(name, seed=1):
-    """(desc, spawn, description) for the plain-step configurations."""
-    if name == "slab25k":
-        d = agb.default_desc(capacity=50000, seed=seed, co2_init=1.0)
-        d.chamber_w = d.chamber_h = d.chamber_d = 4.0e-3
-        d.grid[agb.FIELD_T] = _grid3(128, agb.WATER_THERMAL_DIFFUSIVITY, agb.AMBIENT_TEMP_DEFAULT, 1e9, agb.BC_ROBIN)
-        d.grid[agb.FIELD_CO2] = _grid3(128, agb.CO2_DIFFUSIVITY_WATER, 1.0, 1e15, agb.BC_NEUMANN)
-        d.grid[agb.FIELD_N2] = agb.GridDesc()
-        d.grid[agb.FIELD_IRR] = _grid3(128, agb.IRRADIANCE_NOMINAL_DIFFUSIVITY, 0.0, 1e18, agb.BC_NEUMANN)
-        d.taxis_enabled = 0
-        d.light = agb.Light(1.0, 0.0, 0.0, 1.0e4, 0.0, 1)
-        d.division_predicate = agb.DIVIDE_ENERGY
-        d.division_energy = 0.16 * EMAX
-        d.compaction_enabled = 1
-        d.compaction_period = 10
-        d.biology_rate = 1.0e5
-        sp = agb.spawn(25000, placement=agb.PLACE_SLAB_X, place_radius=275e-6, charge_dist=agb.DIST_LOGNORMAL,
-                       charge_a=0.03, charge_b=0.5, charge_max=0.2, awake=True)
-        return d, sp, dict(cells=25000, grid=128, chamber_mm=4.0, light="+x", division="energy>=0.16*Emax",
-                           compaction_period=10, hash_cell_um=22.0)
-    if name == "cube2k":
-        d = agb.default_desc(capacity=4000, seed=seed, co2_init=1.0)
-        d.chamber_w = d.chamber_h = d.chamber_d = 400e-6
-        face = [373.15, 293.15, 293.15, 293.15, 293.15, 293.15]
-        bc = [agb.BC_DIRICHLET] + [agb.BC_NEUMANN] * 5
-        d.grid[agb.FIELD_T] = _grid3(64, agb.WATER_THERMAL_DIFFUSIVITY, agb.AMBIENT_TEMP_DEFAULT, 1e9, bc, face)
-        d.grid[agb.FIELD_CO2] = _grid3(64, agb.CO2_DIFFUSIVITY_WATER, 1.0, 1e15, agb.BC_NEUMANN)
-        d.grid[agb.FIELD_N2] = agb.GridDesc()
-        d.grid[agb.FIELD_IRR] = _grid3(64, agb.IRRADIANCE_NOMINAL_DIFFUSIVITY, 0.0, 1e18, agb.BC_NEUMANN)
-        d.taxis_enabled = 0
-        d.hash_cell_size = 10e-6
-        d.light = agb.Light(0.0, 0.0, 1.0, 1.0e4, 0.0, 1)
-        sp = agb.spawn(2000, charge_dist=agb.DIST_UNIFORM, charge_a=0.0, charge_b=0.2, awake=True)
-        return d, sp, dict(cells=2000, grid=64, chamber_mm=0.4, light="+z", hash_cell_um=10.0)
-    if name == "clusters1m":
-        d = agb.default_desc(capacity=2000000, seed=seed, co2_init=1.5)
-        d.chamber_w = d.chamber_h = d.chamber_d = 4.0e-3
-        d.grid[agb.FIELD_T] = _grid3(256, agb.WATER_THERMAL_DIFFUSIVITY, agb.AMBIENT_TEMP_DEFAULT, 1e9, agb.BC_ROBIN)
-        d.grid[agb.FIELD_CO2] = _grid3(256, agb.CO2_DIFFUSIVITY_WATER, 1.5, 1e15, agb.BC_NEUMANN)
-        d.grid[agb.FIELD_N2] = agb.GridDesc()
-        d.grid[agb.FIELD_IRR] = _grid3(256, agb.IRRADIANCE_NOMINAL_DIFFUSIVITY, 0.0, 1e18, agb.BC_NEUMANN)
-        d.taxis_enabled = 0
-        d.light = agb.Light(0.0, 0.0, 1.0, 1.0e4, 0.0, 1)
-        d.compaction_enabled = 1
-        d.biology_rate = 1.38e5
-        d.hash_cell_size = 10e-6
-        # Dormant: awake cells packed ~60 to a 15.6 um voxel overdrive the lumped
-        # thermostat exchange past the lethal temperature within a few ticks.
-        sp = agb.spawn(1000000, placement=agb.PLACE_CLUSTERS, place_radius=40e-6, clusters=64,
-                       cluster_extent=3e-3, charge_dist=agb.DIST_UNIFORM, charge_a=0.0, charge_b=0.2, awake=False)
-        return d, sp, dict(cells=1000000, grid=256, chamber_mm=4.0, light="+z", clusters=64, hash_cell_um=10.0,
-                           awake=False)
-    raise SystemExit("unknown workload " + name)
-
-
-def batch_workload(n=64, seed=1):
-    """The batched ensemble: n independent 4 mm chambers with seeds seed..seed+n-1,
-    cell counts log-uniform in [1e3, 2e5], temperature/CO2/irradiance grid edge
-    drawn from {64, 96, 128, 192}, charge uniform in [0, q] with q swept
-    linearly up to 0.20 over the chambers. Otherwise the slab25k recipe: light
-    +x at 1e4 W/m^2, division at 0.16 Emax, compaction every 10 ticks, awake
-    cells placed uniformly. Draws come from a numpy generator seeded with seed."""
-    rng = np.random.default_rng(seed)
-    counts = np.rint(np.exp(rng.uniform(np.log(1.0e3), np.log(2.0e5), n))).astype(int)
-    edges = rng.choice([64, 96, 128, 192], n)
-    descs, spawns = [], []
-    for i in range(n):
-        d = agb.default_desc(capacity=int(2 * counts[i]), seed=seed + i, co2_init=1.0)
-        d.chamber_w = d.chamber_h = d.chamber_d = 4.0e-3
-        e = int(edges[i])
-        d.grid[agb.FIELD_T] = _grid3(e, agb.WATER_THERMAL_DIFFUSIVITY, agb.AMBIENT_TEMP_DEFAULT, 1e9, agb.BC_ROBIN)
-        d.grid[agb.FIELD_CO2] = _grid3(e, agb.CO2_DIFFUSIVITY_WATER, 1.0, 1e15, agb.BC_NEUMANN)
-        d.grid[agb.FIELD_N2] = agb.GridDesc()
-        d.grid[agb.FIELD_IRR] = _grid3(e, agb.IRRADIANCE_NOMINAL_DIFFUSIVITY, 0.0, 1e18, agb.BC_NEUMANN)
-        d.taxis_enabled = 0
-        d.light = agb.Light(1.0, 0.0, 0.0, 1.0e4, 0.0, 1)
-        d.division_predicate = agb.DIVIDE_ENERGY
-        d.division_energy = 0.16 * EMAX
-        d.compaction_enabled = 1
-        d.compaction_period = 10
-        d.biology_rate = 1.0e5
-        q = 0.20 * (i + 1) / n
-        descs.append(d)
-        spawns.append(agb.spawn(int(counts[i]), charge_dist=agb.DIST_UNIFORM, charge_a=0.0, charge_b=q,
-                                awake=True))
-    info = dict(chambers=n, cells=int(counts.sum()), cells_min=int(counts.min()), cells_max=int(counts.max()),
-                grid_edges={str(k): int((edges == k).sum()) for k in (64, 96, 128, 192)}, chamber_mm=4.0)
-    return descs, spawns, info
+W = H.load_workloads()
+workload = W.workload
+batch_workload = W.batch_workload
+substeps = W.substeps
+voxel_steps_per_tick = W.voxel_steps_per_tick
 
 
 def run_batch(args, stream, l2_flush, dist=None, rank=0, ws=1):
@@ -302,26 +222,6 @@ def step_roofline(cell_steps_per_s, voxel_steps_per_s, peak):
             "formula": "(cell_steps/s * 200 B + voxel_steps/s * 8 B) / peak"}
 
 
-def substeps(desc, f):
-    """FTCS passes per tick of field f (src/fields/grid.cuh:51-53; 1/6 bound in 3-D)."""
-    g = desc.grid[f]
-    if g.nx <= 0:
-        return 0
-    dx = desc.chamber_w / g.nx
-    lim = 6.0 if g.nz > 1 else 4.0
-    return int(agb.DT_PHYSICS * desc.physics_rate / (dx * dx / (lim * g.diffusivity))) + 1
-
-
-def voxel_steps_per_tick(desc):
-    """FTCS voxel-steps of one tick: substeps x voxels for T, CO2 and N2."""
-    total = 0
-    for f in (agb.FIELD_T, agb.FIELD_CO2, agb.FIELD_N2):
-        g = desc.grid[f]
-        if g.nx > 0:
-            total += substeps(desc, f) * g.nx * g.ny * g.nz
-    return total
-
-
 # ---------------------------------------------------------------------------
 # Instrumentation
 # ---------------------------------------------------------------------------
@@ -410,19 +310,6 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic(key):
-    """DRAM bytes per launch from the committed ncu summary, if present."""
-    p = os.path.join(ROOT, "profiles", "traffic.txt")
-    if not os.path.exists(p):
-        return None
-    with open(p) as fh:
-        for line in fh:
-            parts = line.split()
-            if len(parts) >= 2 and parts[0] == key:
-                return float(parts[1])
-    return None
-
-
 # ---------------------------------------------------------------------------
 # Distributed plumbing (one process per GPU; replicas of independent chambers)
 # ---------------------------------------------------------------------------
@@ -487,8 +374,15 @@ def cpu_oracle_rate(desc, sp, seconds, threads, state=None):
     return cell_ticks / el, ticks, el
 
 
+def config_for(args, info, ws):
+    """The workload description both arms print (identical keys and values)."""
+    return dict({"workload": args.workload, "step": "one tick of the whole chamber",
+                 "l2": "flushed between timed steps (256 MB write, untimed)",
+                 "parallelism": "replicas (independent chambers per GPU)" if ws > 1 else "single GPU"}, **info)
+
+
 def run_reference(args, wl):
-    rank, ws, _, dist = (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), 0, None)
+    rank, ws = int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
     if rank != 0:
         return 0
     desc, sp, info = wl
@@ -506,8 +400,8 @@ def run_reference(args, wl):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded PCG32 spawn)",
-            "config": dict({"workload": args.workload}, **info),
+            "data": "synthetic (seeded PCG32 spawn of the workload's distributions)",
+            "config": config_for(args, info, ws),
             "voxel_steps_per_s": vox,
             "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": threads, "kind": "port",
                              "sample": "%d ticks of the full workload (C oracle of the reference algorithm, "
@@ -580,15 +474,258 @@ def profile_surrogate(calls):
     return 0
 
 
+# Algorithmic bytes per tick of each section of the tick (the data the section
+# must move at least once; neighbour candidates, halo planes and re-reads are
+# not counted). n = cells, v(f) = voxels of field f, p(f) = its passes.
+#   hash        per cell: position 24 + flags 4 + key/slot written 8, each radix
+#               pass 16 (key and slot read and written), ranges and snapshot
+#               (sorted key/slot 8, position gather 24, snapshot 16, range 8)
+#   cell_pass   per cell: position 24, flags 4, energy 8, biomass 8, emission
+#               state 16, own snapshot record 16, trilinear samples of the
+#               temperature, CO2 and irradiance fields 3 x 32 read; forces 12,
+#               samples 12, irradiance 4, energy 8 written
+#   integrate   per cell: position 24, velocity 24, force 12, energy 8,
+#               biomass 8, t_local 4, rng 8, id 8, flags 4, co2_local 4 read;
+#               position 24, velocity 24, rng 8, flags 4, age 4, CO2 demand 8
+#               written
+#   lifecycle   per cell: flags 4, co2_local 4, co2_held 8, energy 8, t_local 4
+#               read, co2_held 8 and flags 4 written (+ moved cells, not counted)
+#   thermal     per cell and substep: position 24, flags 4, energy 8, a voxel
+#               4 read; energy 8, temp_cell 4, deposit 8 written
+#   t_diffuse   8 B per temperature voxel (the last pass) + 8 B per cell (flush)
+#   slow_fields 8 B per CO2/N2 voxel and pass
+#   irradiance  per cell 36 B (position, flags, stamp) + 4 B per irradiance voxel
+SECTION_BYTES = {
+    "hash": lambda n, d, p: n * (92.0 + 16.0 * p),
+    "cell_pass": lambda n, d, p: n * (200.0 + 36.0),
+    "integrate": lambda n, d, p: n * (176.0),
+    "lifecycle": lambda n, d, p: n * 40.0,
+    "thermal": lambda n, d, p: n * 60.0 * max(substeps(d, agb.FIELD_T), 1),
+    "t_diffuse": lambda n, d, p: 8.0 * _vox(d, agb.FIELD_T) + 8.0 * n,
+    "slow_fields": lambda n, d, p: 8.0 * (_vox(d, agb.FIELD_CO2) * substeps(d, agb.FIELD_CO2) +
+                                          _vox(d, agb.FIELD_N2) * substeps(d, agb.FIELD_N2)),
+    "irradiance": lambda n, d, p: 36.0 * n + 4.0 * _vox(d, agb.FIELD_IRR),
+}
+
+
+def _vox(desc, f):
+    g = desc.grid[f]
+    return g.nx * g.ny * g.nz if g.nx > 0 else 0
+
+
+def radix_passes(buckets):
+    """Digit passes of the hash sort: 8-bit digits, 9-bit where that saves a
+    pass (17-18 and 25-27-bit keys)."""
+    bits = max(1, int(buckets).bit_length())
+    return -(-bits // 9) if bits in (17, 18, 25, 26, 27) else -(-bits // 8)
+
+
+def step_stats(ms):
+    ms = sorted(ms)
+    return {"mean": sum(ms) / len(ms), "median": statistics.median(ms), "min": ms[0], "max": ms[-1]}
+
+
+def time_sections(world, stream, l2_flush, ticks):
+    """Mean duration of each section of the tick over `ticks` graph replays with
+    the in-graph section timers on (each replay after an L2 flush)."""
+    import torch
+    sh = stream.cuda_stream
+    world.set_timing(True)
+    world.prepare_graphs(1, stream=sh)
+    acc = {}
+    with torch.cuda.stream(stream):
+        for _ in range(ticks):
+            l2_flush.zero_()
+            world.step(1, graph=True, stream=sh)
+            for k, v in world.section_times().items():
+                acc.setdefault(k, []).append(v)
+    world.set_timing(False)
+    return {k: 1e3 * sum(v) / len(v) for k, v in acc.items()}       # microseconds
+
+
+def dominant_roofline(sections_us, desc, cells, passes, peak, peak_kind):
+    """The roofline of the section that takes longest inside the tick."""
+    cand = {k: v for k, v in sections_us.items() if k in SECTION_BYTES}
+    k = max(cand, key=cand.get)
+    algo = SECTION_BYTES[k](cells, desc, passes)
+    t = cand[k] * 1e-6
+    achieved = algo / t / 1e9
+    return {"bound": "hbm", "kernel": k, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind, "algorithmic_bytes_per_launch": algo,
+            "launch_us": cand[k], "traffic": None,
+            "timing": "mean over timed graph replays of the section's in-graph timing events (L2 flushed "
+                      "before each tick); DRAM traffic is in the committed ncu summaries, not measured here"}
+
+
+def ftcs_pass_roofline(world, desc, stream, l2_flush, peak, peak_kind, reps=20, replays=5):
+    """One FTCS pass over the temperature field: the passes of `reps` diffusion
+    calls captured in one CUDA graph, each replay after an L2 flush, timed with
+    events on the replay stream."""
+    import torch
+    sh = stream.cuda_stream
+    gT = desc.grid[agb.FIELD_T]
+    vox = gT.nx * gT.ny * gT.nz
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(stream):
+        world.diffuse(agb.FIELD_T, agb.DT_PHYSICS, stream=sh)
+        torch.cuda.synchronize()
+    with torch.cuda.graph(g, stream=stream):
+        for _ in range(reps):
+            world.diffuse(agb.FIELD_T, agb.DT_PHYSICS, stream=torch.cuda.current_stream().cuda_stream)
+    tot = 0.0
+    with torch.cuda.stream(stream):
+        for _ in range(replays):
+            l2_flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            g.replay()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1)
+    per_pass = tot / 1e3 / (replays * reps * substeps(desc, agb.FIELD_T))
+    algo = 8.0 * vox
+    ach = algo / per_pass / 1e9
+    return {"kernel": "ftcs3d (temperature, %d^3)" % gT.nx, "achieved": ach, "peak": peak, "unit": "GB/s",
+            "frac": ach / peak, "peak_source": peak_kind, "algorithmic_bytes_per_launch": algo,
+            "launch_us": per_pass * 1e6,
+            "timing": "mean pass of %d graph-captured back-to-back passes after an L2 flush; field %.0f MB (%s L2)"
+                      % (reps * substeps(desc, agb.FIELD_T), 4.0 * vox / 1e6,
+                         "inside" if 8.0 * vox < 100e6 else "larger than")}
+
+
+def run_plain(name, args, stream, l2_flush, dist, rank, ws, local, warmup, steps, e2e=False, cpu=False):
+    """One plain-step leg: setup (spawn, every graph phase captured), `warmup`
+    untimed ticks, `steps` timed ticks (one graph replay each, L2 flushed
+    between them, outside the timed intervals), then section timers, the FTCS
+    pass, and optionally the end-to-end loop and the CPU baseline."""
+    import torch
+    desc, sp, info = workload(name, seed=1 + rank)
+    world = agb.World(desc)
+    world.spawn(sp)
+    sh = stream.cuda_stream
+    state0 = None
+    if cpu:
+        cells0, nid0 = world.export_cells()
+        state0 = (cells0, nid0, {f: world.export_field(f) for f in range(4) if desc.grid[f].nx > 0})
+    world.prepare_graphs(1, stream=sh)             # setup: no capture inside warm-up or timing
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            world.step(1, graph=True, stream=sh)
+        torch.cuda.synchronize()
+        n_start = world.count(stream=sh)
+        kernels_before = world.graph_kernels()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        sampler = ClockSampler(local)
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+        sampler.start()
+        sampler.mark_start()
+        for k in range(steps):
+            l2_flush.zero_()                           # L2 flush, outside the timed interval
+            starts[k].record(stream)
+            world.step(1, graph=True, stream=sh)
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+        sampler.mark_end()
+        clocks = sampler.stop()
+        if dist is not None:
+            dist.barrier()
+        n_end = world.count(stream=sh)
+        launches = world.graph_kernels() - kernels_before
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    total_s = allreduce_max(dist, sum(step_ms) / 1e3)
+    cell_steps = allreduce_sum(dist, 0.5 * (n_start + n_end) * steps)
+    vox_steps = allreduce_sum(dist, float(voxel_steps_per_tick(desc)) * steps)
+    peak, peak_kind = measured_peaks()
+    out = {"workload": name, "config": config_for(argparse.Namespace(workload=name), info, ws),
+           "cell_steps_per_s": cell_steps / total_s, "voxel_steps_per_s": vox_steps / total_s,
+           "ms_per_step": total_s * 1e3 / steps, "step_ms": step_stats(step_ms),
+           "cells_start_end": [n_start, n_end], "gpu_launches": launches, "clocks": clocks,
+           "roofline_step": step_roofline(cell_steps / total_s, vox_steps / total_s, peak)}
+    cell = desc.hash_cell_size
+    buckets = 1
+    for extent in (desc.chamber_w, desc.chamber_h, desc.chamber_d):
+        buckets *= int(np.ceil(extent / cell - 1e-9))
+    passes = radix_passes(buckets)
+    sections = time_sections(world, stream, l2_flush, max(10, min(steps, 40)))
+    out["sections_us"] = sections
+    out["roofline"] = dominant_roofline(sections, desc, 0.5 * (n_start + n_end), passes, peak, peak_kind)
+    out["ftcs_pass"] = ftcs_pass_roofline(world, desc, stream, l2_flush, peak, peak_kind)
+    if e2e:
+        out["e2e"] = e2e_leg(world, desc, args, stream)
+    world.close()
+    if cpu:
+        threads = os.cpu_count() or 1
+        rate, ticks, el = cpu_oracle_rate(desc, sp, args.cpu_seconds, threads, state0)
+        out["cpu_baseline"] = {"value": rate, "unit": "cell-steps/s", "cores": threads, "kind": "port",
+                               "sample": "%d ticks (%.1f s) of the same workload from the same initial state, C "
+                                         "oracle (FP64, OpenMP over cells and voxels)" % (ticks, el)}
+    return out
+
+
+def e2e_leg(world, desc, args, stream):
+    """End to end through the C ABI with host buffers: pinned state in, one
+    tick, state out, every step; the faster of the one-call and the
+    separate-calls loop is the value, both are reported."""
+    import torch
+    sh = stream.cuda_stream
+    n = world.count()
+    pinned = agb.CellArrays(n)
+    for name, t in agb.CELL_FIELDS:
+        pinned.a[name] = torch.empty(max(n, 1), dtype=getattr(torch, np.dtype(t).name), pin_memory=True).numpy()
+    cells, nid = world.export_cells()
+    for name, _t in agb.CELL_FIELDS:
+        pinned.a[name][:n] = cells[name]
+    bytes_state = sum(np.dtype(t).itemsize for _n, t in agb.CELL_FIELDS) * n
+    e2e_steps = max(30, args.steps)
+    warm = max(args.warmup, 3)
+
+    def fused(k, pinned, nid):
+        for _ in range(k):
+            pinned, nid = world.step_host(pinned, nid, 1, stream=sh)
+        return pinned, nid
+
+    def separate(k, pinned, nid):
+        for _ in range(k):
+            world.import_cells(pinned, nid, stream=sh)
+            world.step(1, graph=True, stream=sh)
+            pinned, nid = world.export_cells(stream=sh, into=pinned)
+        return pinned, nid
+
+    world.prepare_graphs(1, stream=sh)
+    pinned, nid = fused(warm, pinned, nid)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    pinned, nid = fused(e2e_steps, pinned, nid)
+    torch.cuda.synchronize()
+    el_fused = time.perf_counter() - t0
+    pinned, nid = separate(warm, pinned, nid)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    pinned, nid = separate(e2e_steps, pinned, nid)
+    torch.cuda.synchronize()
+    el_sep = time.perf_counter() - t0
+    return {"value": n * e2e_steps / min(el_fused, el_sep), "unit": "cell-steps/s",
+            "h2d_bytes_per_step": bytes_state, "d2h_bytes_per_step": bytes_state,
+            "fused_call": n * e2e_steps / el_fused, "separate_calls": n * e2e_steps / el_sep,
+            "path": "pinned host SoA in, one graph tick, pinned host SoA out, every step: agb_world_step_host "
+                    "(one call) and agb_world_import_cells + agb_world_step_graph + agb_world_export_cells"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--workload", default="slab25k", choices=["slab25k", "cube2k", "clusters1m"])
+    ap.add_argument("--workload", default="slab25k", choices=list(W.PLAIN))
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--scaled", default="clusters1m", choices=list(W.PLAIN) + ["none"],
+                    help="second plain-step leg reported beside the headline (the HBM-graded configuration)")
+    ap.add_argument("--scaled-steps", type=int, default=20)
     ap.add_argument("--batch-steps", type=int, default=30,
                     help="timed steps of the batched ensemble reported beside the plain step (0: skip)")
     ap.add_argument("--batch-chambers", type=int, default=64)
@@ -627,173 +764,47 @@ def main():
     import torch
     rank, ws, local, dist = dist_init()
     torch.cuda.set_device(local)
-    desc, sp, info = workload(args.workload, seed=1 + rank)
-    lib = agb.load()
-    world = agb.World(desc, lib)
-    world.spawn(sp)
+    agb.load()
     stream = torch.cuda.Stream()
-    sh = stream.cuda_stream
     l2_flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
-    # Initial state for the CPU baseline (before any tick).
-    state0 = None
-    if rank == 0 and not args.no_cpu:
-        cells0, nid0 = world.export_cells()
-        state0 = (cells0, nid0, {f: world.export_field(f) for f in range(4) if desc.grid[f].nx > 0})
+    head = run_plain(args.workload, args, stream, l2_flush, dist, rank, ws, local, args.warmup, args.steps,
+                     e2e=(rank == 0), cpu=(rank == 0 and not args.no_cpu))
 
-    with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
-            world.step(1, graph=True, stream=sh)
-        torch.cuda.synchronize()
-        n_start = world.count(stream=sh)
-        kernels_before = world.graph_kernels()
-        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-        sampler = ClockSampler(local)
-        if dist is not None:
-            dist.barrier()
-        torch.cuda.synchronize()
-        sampler.start()
-        sampler.mark_start()
-        for k in range(args.steps):
-            l2_flush.zero_()                           # L2 flush, outside the timed interval
-            starts[k].record(stream)
-            world.step(1, graph=True, stream=sh)
-            ends[k].record(stream)
-        torch.cuda.synchronize()
-        sampler.mark_end()
-        clocks = sampler.stop()
-        if dist is not None:
-            dist.barrier()
-        n_end = world.count(stream=sh)
-        launches = world.graph_kernels() - kernels_before
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_s = allreduce_max(dist, sum(step_ms) / 1e3)
-    cells_mean = 0.5 * (n_start + n_end)
-    cell_steps = allreduce_sum(dist, cells_mean * args.steps)
-    vox_steps = allreduce_sum(dist, float(voxel_steps_per_tick(desc)) * args.steps)
-    value = cell_steps / total_s
-
-    # Dominant-kernel roofline: the 3-D FTCS pass on the temperature grid. The
-    # passes of `reps` diffusion calls are captured in one CUDA graph (so host
-    # launch cost is not counted) and each replay, after an L2 flush, is timed
-    # with events on the stream it runs on.
-    peak, peak_kind = measured_peaks()
-    gT = desc.grid[agb.FIELD_T]
-    vox_T = gT.nx * gT.ny * gT.nz
-    reps, replays = 20, 5
-    ftcs_graph = torch.cuda.CUDAGraph()
-    with torch.cuda.stream(stream):
-        world.diffuse(agb.FIELD_T, agb.DT_PHYSICS, stream=sh)
-        torch.cuda.synchronize()
-    with torch.cuda.graph(ftcs_graph, stream=stream):
-        for _ in range(reps):
-            world.diffuse(agb.FIELD_T, agb.DT_PHYSICS, stream=torch.cuda.current_stream().cuda_stream)
-    ftcs_ms = 0.0
-    with torch.cuda.stream(stream):
-        for _ in range(replays):
-            l2_flush.zero_()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            ftcs_graph.replay()
-            e1.record(stream)
-            torch.cuda.synchronize()
-            ftcs_ms += e0.elapsed_time(e1)
-    ftcs_s = ftcs_ms / 1e3 / (replays * reps * substeps(desc, agb.FIELD_T))   # per pass
-    algo_bytes = 8.0 * vox_T
-    achieved = algo_bytes / ftcs_s / 1e9
-    traffic = profile_traffic("ftcs3d_%d" % gT.nx)
-
-    # End to end through the C ABI with host buffers: pinned state in, one tick,
-    # state out, every step.
-    e2e = None
-    if rank == 0:
-        n = world.count()
-        pinned = agb.CellArrays(n)
-        for name, t in agb.CELL_FIELDS:
-            pinned.a[name] = torch.empty(max(n, 1), dtype=getattr(torch, np.dtype(t).name),
-                                         pin_memory=True).numpy()
-        cells, nid = world.export_cells()
-        for name, _t in agb.CELL_FIELDS:
-            pinned.a[name][:n] = cells[name]
-        bytes_state = sum(np.dtype(t).itemsize for _n, t in agb.CELL_FIELDS) * n
-        e2e_steps = max(30, args.steps)
-        # Untimed warm-up of each loop over a whole compaction period, so that
-        # every tick phase has its graph captured before timing starts.
-        e2e_warm = max(args.warmup, desc.compaction_period if desc.compaction_period > 0 else 1)
-
-        def fused(k, pinned, nid):
-            for _ in range(k):
-                pinned, nid = world.step_host(pinned, nid, 1, stream=sh)
-            return pinned, nid
-
-        def separate(k, pinned, nid):
-            for _ in range(k):
-                world.import_cells(pinned, nid, stream=sh)
-                world.step(1, graph=True, stream=sh)
-                pinned, nid = world.export_cells(stream=sh, into=pinned)
-            return pinned, nid
-
-        pinned, nid = fused(e2e_warm, pinned, nid)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        pinned, nid = fused(e2e_steps, pinned, nid)
-        torch.cuda.synchronize()
-        el_fused = time.perf_counter() - t0
-        pinned, nid = separate(e2e_warm, pinned, nid)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        pinned, nid = separate(e2e_steps, pinned, nid)
-        torch.cuda.synchronize()
-        el_sep = time.perf_counter() - t0
-        e2e = {"value": n * e2e_steps / min(el_fused, el_sep), "unit": "cell-steps/s",
-               "h2d_bytes_per_step": bytes_state, "d2h_bytes_per_step": bytes_state,
-               "fused_call": n * e2e_steps / el_fused, "separate_calls": n * e2e_steps / el_sep,
-               "path": "pinned host SoA in, one graph tick, pinned host SoA out, every step: agb_world_step_host "
-                       "(one call) and agb_world_import_cells + agb_world_step_graph + agb_world_export_cells"}
+    scaled = None
+    if args.scaled != "none" and args.scaled != args.workload:
+        scaled = run_plain(args.scaled, args, stream, l2_flush, dist, rank, ws, local, 3, args.scaled_steps)
+        scaled.pop("config", None)
 
     batched = None
     if args.batch_steps > 0:
-        world.close()
         batched = run_batch(args, stream, l2_flush, dist, rank, ws)
 
     surrogate = None
     if rank == 0 and args.surrogate_windows > 0:
         surrogate = run_surrogate(args, stream)
-        surrogate["vs_plain_voxel_steps"] = surrogate["world"]["voxel_steps_per_s"] / (vox_steps / total_s)
-
-    cpu = None
-    if rank == 0 and not args.no_cpu:
-        threads = os.cpu_count() or 1
-        rate, ticks, el = cpu_oracle_rate(desc, sp, args.cpu_seconds, threads, state0)
-        cpu = {"value": rate, "unit": "cell-steps/s", "cores": threads, "kind": "port",
-               "sample": "%d ticks (%.1f s) of the same workload from the same initial state, C oracle "
-                         "(FP64, OpenMP over cells and voxels)" % (ticks, el)}
+        surrogate["vs_plain_voxel_steps"] = surrogate["world"]["voxel_steps_per_s"] / head["voxel_steps_per_s"]
 
     if rank == 0:
         line = {
-            "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 compute, f64 state",
+            "metric": METRIC, "value": head["cell_steps_per_s"], "unit": "cell-steps/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms_per_step"],
+            "ms_per_step_median": head["step_ms"]["median"], "ms_per_step_min": head["step_ms"]["min"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 compute, f64 state",
             "data": "synthetic (seeded PCG32 spawn of the workload's distributions)",
-            "config": dict({"workload": args.workload, "step": "one tick of the whole chamber",
-                            "l2": "flushed between timed steps (256 MB write, untimed)",
-                            "parallelism": "replicas (independent chambers per GPU)" if ws > 1 else "single GPU"},
-                           **info),
-            "voxel_steps_per_s": vox_steps / total_s,
-            "cells_start_end": [n_start, n_end],
-            "roofline_step": step_roofline(value, vox_steps / total_s, peak),
-            "roofline": {"bound": "hbm", "kernel": "ftcs3d (temperature, %d^3)" % gT.nx,
-                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "peak_source": peak_kind, "algorithmic_bytes_per_launch": algo_bytes,
-                         "launch_us": ftcs_s * 1e6, "traffic": traffic,
-                         "timing": "mean pass of %d graph-captured back-to-back passes after an L2 flush; "
-                                   "field %.0f MB (%s L2)" % (reps * substeps(desc, agb.FIELD_T), 4.0 * vox_T / 1e6,
-                                                              "inside" if 8.0 * vox_T < 100e6 else "larger than")},
-            "cpu_baseline": cpu,
-            "e2e": e2e,
-            "gpu_launches": launches,
-            "clocks": clocks,
+            "config": head["config"],
+            "voxel_steps_per_s": head["voxel_steps_per_s"],
+            "cells_start_end": head["cells_start_end"],
+            "roofline": head["roofline"],
+            "roofline_step": head["roofline_step"],
+            "sections_us": head["sections_us"],
+            "ftcs_pass": head["ftcs_pass"],
+            "cpu_baseline": head.get("cpu_baseline"),
+            "e2e": head.get("e2e"),
+            "gpu_launches": head["gpu_launches"],
+            "clocks": head["clocks"],
+            "setup": "every tick phase's graph captured before warm-up (agb_world_prepare_graphs)",
+            "scaled": scaled,
             "batched": batched,
             "surrogate": surrogate,
         }

@@ -415,6 +415,36 @@ agb_status agb_world_step(agb_world* w, int32_t ticks, agb_stream s);
 /* Capture `ticks` ticks once as a CUDA graph and replay it on later calls with
  * the same tick count: one launch per call. */
 agb_status agb_world_step_graph(agb_world* w, int32_t ticks, agb_stream s);
+/* Captures, without running them, the graphs agb_world_step_graph(w, ticks, .)
+ * will replay from the world's current state on: one per (field buffer
+ * parities, tick % compaction_period) state that stepping by `ticks` visits,
+ * until the states repeat. Afterwards no step of that size captures or
+ * instantiates anything (no host-side latency spike in a serving loop or a
+ * timed region). The world's state is unchanged. No counterpart in the
+ * reference (its world_step has no graphs). */
+agb_status agb_world_prepare_graphs(agb_world* w, int32_t ticks, agb_stream s);
+/* Section timers: with timing on, every tick (eager or captured into a graph)
+ * records a pair of timing events around each section below, so the times of
+ * the kernels inside a replayed graph can be read without a profiler. The
+ * event nodes end the programmatic (early) launch of the kernel after them, so
+ * timed ticks run slightly slower; off by default. Switching invalidates the
+ * world's captured graphs. agb_world_section_times waits for the last tick and
+ * returns each section's duration in milliseconds (-1 for a section that has
+ * not run). No counterpart in the reference. */
+enum {
+    AGB_SECTION_TICK = 0,        /* the whole tick, first launch to last */
+    AGB_SECTION_THERMAL = 1,     /* thermal substeps (all but the last pass's flush and FTCS) */
+    AGB_SECTION_T_DIFFUSE = 2,   /* last temperature flush + FTCS pass */
+    AGB_SECTION_IRRADIANCE = 3,  /* stamps, occlusion factors, sweep */
+    AGB_SECTION_SLOW_FIELDS = 4, /* CO2 / N2 FTCS passes */
+    AGB_SECTION_HASH = 5,        /* keys, radix sort, bucket ranges */
+    AGB_SECTION_CELL_PASS = 6,   /* feeding, taxis and forces (fused or separate) */
+    AGB_SECTION_INTEGRATE = 7,   /* OU integration (+ CO2 demand) */
+    AGB_SECTION_LIFECYCLE = 8,   /* predation, uptake, death, division, compaction */
+    AGB_TICK_SECTIONS = 9
+};
+agb_status agb_world_set_timing(agb_world* w, int32_t enable);
+agb_status agb_world_section_times(agb_world* w, float ms[AGB_TICK_SECTIONS]);
 /* Kernel launches performed by graph replays since the world was created
  * (the sum of each replayed graph's kernel nodes), for launch accounting. */
 agb_status agb_world_graph_kernels(agb_world* w, int64_t* kernels);
