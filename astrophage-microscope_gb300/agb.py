@@ -371,6 +371,7 @@ def load(path=LIB_PATH):
         "agb_surrogate_create": (I32, [C.POINTER(SurrogateDesc), C.POINTER(P)]),
         "agb_surrogate_destroy": (None, [P]),
         "agb_surrogate_train": (I32, [P, I32, P, P]),
+        "agb_surrogate_train_on": (I32, [P, P, P, P, P, P, P]),
         "agb_surrogate_advance": (I32, [P, P, P, P, P, I32, C.POINTER(SurrogateReport), P]),
         "agb_surrogate_reference": (I32, [P, P, P, P, P, P]),
         "agb_surrogate_window": (I32, [P, C.c_uint64, P, P, P, P, P]),
@@ -417,6 +418,7 @@ def exported_symbols():
             "agb_fnv1a64", "agb_world_state_hash", "agb_world_snapshot_save", "agb_world_snapshot_load",
             "agb_nn_conv3", "agb_nn_wgrad_scratch_bytes", "agb_nn_wgrad", "agb_nn_flip_weights",
             "agb_surrogate_desc_default", "agb_surrogate_create", "agb_surrogate_destroy", "agb_surrogate_train",
+            "agb_surrogate_train_on",
             "agb_surrogate_advance", "agb_surrogate_reference", "agb_surrogate_window", "agb_surrogate_gradients",
             "agb_surrogate_params", "agb_surrogate_set_params", "agb_surrogate_get_report",
             "agb_surrogate_error_word", "agb_world_attach_surrogate",
@@ -780,6 +782,13 @@ class Surrogate:
         losses = np.zeros(max(windows, 1), np.float32)
         self._ck(self.lib.agb_surrogate_train(self.h, windows, losses.ctypes.data, _st(stream)), "train")
         return losses[:windows]
+
+    def train_on(self, T, Cf, qT, qC, stream=None):
+        """One training step on a caller-supplied window (device pointers); returns its loss."""
+        loss = C.c_float()
+        self._ck(self.lib.agb_surrogate_train_on(self.h, self._p(T), self._p(Cf), self._p(qT), self._p(qC),
+                                                 C.byref(loss), _st(stream)), "train_on")
+        return loss.value
 
     def advance(self, T, Cf, qT, qC, judge=0, stream=None):
         rep = SurrogateReport()

@@ -629,6 +629,29 @@ agb_status agb_surrogate_train(agb_surrogate* s, int32_t windows, float* losses,
     return e ? AGB_DEVICE_TIMEOUT : AGB_OK;
 }
 
+agb_status agb_surrogate_train_on(agb_surrogate* s, const float* T0, const float* C0, const float* qT,
+                                  const float* qC, float* loss, agb_stream stream) {
+    if (!s || !T0 || !C0) return AGB_INVALID_ARGUMENT;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const size_t b = 4 * (size_t)s->m[0];
+    cudaMemcpyAsync(s->fT, T0, b, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(s->fC, C0, b, cudaMemcpyDeviceToDevice, st);
+    if (qT) cudaMemcpyAsync(s->fqT, qT, b, cudaMemcpyDeviceToDevice, st);
+    else cudaMemsetAsync(s->fqT, 0, b, st);
+    if (qC) cudaMemcpyAsync(s->fqC, qC, b, cudaMemcpyDeviceToDevice, st);
+    else cudaMemsetAsync(s->fqC, 0, b, st);
+    cudaMemcpyAsync(s->gT, T0, b, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(s->gC, C0, b, cudaMemcpyDeviceToDevice, st);
+    ftcs_window(s, s->gT, s->gC, s->fqT, s->fqC, st);
+    if (!grad_pass(s, s->fT, s->fC, s->fqT, s->fqC, s->gT, s->gC, st) || !step_adam(s, st)) return AGB_CUDA_ERROR;
+    if (loss) {
+        cudaMemcpyAsync(loss, s->loss_dev, 4, cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st) != cudaSuccess) return AGB_CUDA_ERROR;
+        s->rep.last_loss = *loss;
+    }
+    return cudaGetLastError() == cudaSuccess ? AGB_OK : AGB_CUDA_ERROR;
+}
+
 agb_status agb_surrogate_gradients(agb_surrogate* s, const float* T0, const float* C0, const float* qT,
                                    const float* qC, const float* T1, const float* C1, float* grads, int64_t cap,
                                    float* loss, agb_stream stream) {

@@ -114,40 +114,28 @@ def run_batch(args, stream, l2_flush, dist=None, rank=0, ws=1):
     return out
 
 
-def surrogate_for(desc, seed=1):
-    """A surrogate descriptor matching a world's 3-D temperature and CO2 grids
-    (one FTCS pass per tick), trained on windows with heat sources and
-    temperature excursions of the size the 25,000-cell run produces."""
-    gT, gC = desc.grid[agb.FIELD_T], desc.grid[agb.FIELD_CO2]
-    sd = agb.surrogate_desc(nx=gT.nx, ny=gT.ny, nz=gT.nz, extent=desc.chamber_w, dt=agb.DT_PHYSICS * desc.physics_rate,
-                            seed=seed)
-    sd.diffusivity[0], sd.diffusivity[1] = gT.diffusivity, gC.diffusivity
-    sd.init[0], sd.init[1] = gT.init, gC.init
-    for k in range(6):
-        sd.bc[0][k], sd.face[0][k] = gT.bc[k], gT.face_value[k]
-        sd.bc[1][k], sd.face[1][k] = gC.bc[k], gC.face_value[k]
-    sd.train_temperature_amplitude = 20.0
-    sd.train_heat_per_step = 2.0
-    sd.train_source_density = 0.01
-    sd.train_uptake_per_step = 1.0e-5
-    return sd
-
-
 def run_surrogate(args, stream):
-    """The learned field surrogate on the 25,000-cell setup: train it on the
-    GPU, time one network window against the FTCS window it replaces, then
-    drive the world's temperature and CO2 grids with it (FTCS judge every 8th
-    window, fallback past 0.01 K or 1e-6 energy drift)."""
+    """The learned field surrogate on the 25,000-cell setup: train it on the GPU
+    on windows cut from runs of the plain-step workloads (fields and the cells'
+    rasterised heat and uptake sources, on the 128^3 grid), measure it on
+    held-out windows against the plain FTCS window and against persistence,
+    time a network window against the FTCS window it replaces, repeat for
+    longer windows (the error-vs-cost curve), then drive the world's
+    temperature and CO2 grids with it (FTCS judge every 8th window, fallback
+    past 0.01 K or 1e-6 energy drift)."""
     import torch
+    SD = H.load_surrogate_data()
     desc, sp, _info = workload("slab25k", seed=1)
-    sd = surrogate_for(desc)
-    sg = agb.Surrogate(sd)
     sh = stream.cuda_stream
-    t0 = time.perf_counter()
-    losses = sg.train(args.surrogate_windows, stream=sh)
-    train_s = time.perf_counter() - t0
-    shape = (sd.nz, sd.ny, sd.nx)
-    T, Cf, qT, qC = [torch.zeros(shape, dtype=torch.float32, device="cuda") for _ in range(4)]
+    held = list(SD.world_windows(SD.surrogate_desc_for(desc), 9, seed=900, every=7))
+
+    def trained(steps, windows):
+        sd = SD.surrogate_desc_for(desc, steps=steps)
+        sg = agb.Surrogate(sd)
+        t0 = time.perf_counter()
+        losses = [sg.train_on(*[x.data_ptr() for x in win], stream=sh)
+                  for win in SD.world_windows(sd, windows, seed=100)]
+        return sd, sg, np.array(losses, np.float32), time.perf_counter() - t0
 
     def timed(fn, reps=10):
         with torch.cuda.stream(stream):
@@ -161,18 +149,31 @@ def run_surrogate(args, stream):
             torch.cuda.synchronize()
         return e0.elapsed_time(e1) / reps
 
-    sg.window(10 ** 7, T.data_ptr(), Cf.data_ptr(), qT.data_ptr(), qC.data_ptr(), stream=sh)
-    net_ms = timed(lambda: sg.advance(T.data_ptr(), Cf.data_ptr(), qT.data_ptr(), qC.data_ptr(), judge=-1, stream=sh))
-    ftcs_ms = timed(lambda: sg.reference(T.data_ptr(), Cf.data_ptr(), qT.data_ptr(), qC.data_ptr(), stream=sh))
-    # Held-out accuracy against the FTCS window, and the do-nothing baseline.
-    errs, pers = [], []
+    def costs(sg, sd):
+        T, Cf, qT, qC = [x.clone() for x in held[0]]
+        net = timed(lambda: sg.advance(T.data_ptr(), Cf.data_ptr(), qT.data_ptr(), qC.data_ptr(), judge=-1,
+                                       stream=sh))
+        ftcs = timed(lambda: sg.reference(T.data_ptr(), Cf.data_ptr(), qT.data_ptr(), qC.data_ptr(), stream=sh))
+        return net, ftcs
+
+    sd, sg, losses, train_s = trained(16, args.surrogate_windows)
+    net_ms, ftcs_ms = costs(sg, sd)
+    ev_world = SD.evaluate(sg, held)
+    shape = (sd.nz, sd.ny, sd.nx)
+    synth = []
     for idx in range(3):
-        sg.window(10 ** 8 + idx, T.data_ptr(), Cf.data_ptr(), qT.data_ptr(), qC.data_ptr(), stream=sh)
-        rT, rC = T.clone(), Cf.clone()
-        sg.reference(rT.data_ptr(), rC.data_ptr(), qT.data_ptr(), qC.data_ptr(), stream=sh)
-        pers.append(float((rT - T).abs().max()))
-        sg.advance(T.data_ptr(), Cf.data_ptr(), qT.data_ptr(), qC.data_ptr(), judge=-1, stream=sh)
-        errs.append(float((T - rT).abs().max()))
+        f = [torch.zeros(shape, dtype=torch.float32, device="cuda") for _ in range(4)]
+        sg.window(10 ** 8 + idx, *[x.data_ptr() for x in f], stream=sh)
+        synth.append(f)
+    ev_synth = SD.evaluate(sg, synth)
+    curve = [{"steps": 16, "network_ms": net_ms, "ftcs_ms": ftcs_ms, "speedup_vs_ftcs": ftcs_ms / net_ms,
+              "train_windows": args.surrogate_windows, **ev_world}]
+    for steps in args.surrogate_curve:
+        sd2, sg2, _l2, _t2 = trained(steps, args.surrogate_curve_windows)
+        n2, f2 = costs(sg2, sd2)
+        curve.append({"steps": steps, "network_ms": n2, "ftcs_ms": f2, "speedup_vs_ftcs": f2 / n2,
+                      "train_windows": args.surrogate_curve_windows, **SD.evaluate(sg2, held)})
+        sg2.close()
     # The world, driven by the surrogate.
     w = agb.World(desc)
     w.spawn(sp)
@@ -194,9 +195,14 @@ def run_surrogate(args, stream):
     r1 = sg.report()
     vox = 2 * sd.nx * sd.ny * sd.nz
     out = {"train_windows": args.surrogate_windows, "train_s": train_s,
+           "training_data": "windows cut every tick from seeded runs of cube2k (64^3, resampled), slab25k "
+                            "(128^3) and clusters20k (64^3, resampled): T, CO2 and the cells' rasterised heat "
+                            "and uptake sources",
            "loss_first_last": [float(losses[:20].mean()), float(losses[-20:].mean())] if len(losses) >= 20 else None,
            "network_ms_per_window": net_ms, "ftcs_ms_per_window": ftcs_ms,
-           "held_out_max_err_K": max(errs), "persistence_max_err_K": max(pers),
+           "held_out_world": ev_world, "held_out_synthetic": ev_synth,
+           "held_out_max_err_K": ev_world["net_max_K"], "persistence_max_err_K": ev_world["persistence_max_K"],
+           "error_vs_cost": curve,
            "world": {"workload": "slab25k", "ticks": ticks, "ms_per_step": el * 1e3 / ticks,
                      "cell_steps_per_s": 0.5 * (n0 + n1) * ticks / el, "voxel_steps_per_s": vox * ticks / el,
                      "windows": int(r1.calls - r0.calls), "judged": int(r1.judged - r0.judged),
@@ -737,6 +743,9 @@ def main():
     ap.add_argument("--surrogate-windows", type=int, default=1500,
                     help="training windows of the learned field surrogate (0: skip the surrogate leg)")
     ap.add_argument("--surrogate-windows-run", type=int, default=16)
+    ap.add_argument("--surrogate-curve", type=int, nargs="*", default=[32, 64],
+                    help="window lengths (FTCS steps) of the error-vs-cost curve beside the 16-step network")
+    ap.add_argument("--surrogate-curve-windows", type=int, default=600)
     ap.add_argument("--profile-batch", type=int, default=0,
                     help="only run N steps of the batched ensemble inside an NVTX range (small case for ncu)")
     ap.add_argument("--profile-stencil", type=int, default=0,

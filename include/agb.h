@@ -559,6 +559,13 @@ void agb_surrogate_desc_default(agb_surrogate_desc* d);
 agb_status agb_surrogate_create(const agb_surrogate_desc* d, agb_surrogate** out);
 void agb_surrogate_destroy(agb_surrogate* s);
 agb_status agb_surrogate_train(agb_surrogate* s, int32_t windows, float* losses, agb_stream st);
+/* One training step on a window the caller supplies (device arrays on the
+ * surrogate's grid: temperature, CO2 and the per-step sources, NULL sources
+ * = none), e.g. fields and rasterised cell sources taken from world runs; its
+ * target is the plain FTCS window from those fields. *loss (optional, host)
+ * receives the step's loss (the call then waits for it). */
+agb_status agb_surrogate_train_on(agb_surrogate* s, const float* T0, const float* C0, const float* qT,
+                                  const float* qC, float* loss, agb_stream st);
 agb_status agb_surrogate_advance(agb_surrogate* s, float* T, float* C, const float* qT, const float* qC,
                                  int32_t judge, agb_surrogate_report* rep, agb_stream st);
 agb_status agb_surrogate_reference(agb_surrogate* s, float* T, float* C, const float* qT, const float* qC,

@@ -45,6 +45,11 @@ def load_workloads():
     return _load("workloads")
 
 
+def load_surrogate_data():
+    load_workloads()
+    return _load("surrogate_data")
+
+
 def build_oracle():
     src = os.path.join(ROOT, "oracle", "oracle.c")
     if (not os.path.exists(ORACLE_SO)) or os.path.getmtime(ORACLE_SO) < os.path.getmtime(src):

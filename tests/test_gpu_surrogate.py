@@ -69,34 +69,60 @@ def test_gradients_match_cpu_oracle():
         assert rel < 2e-2 and cos > 0.999, "layer %d: rel %.3g cos %.6f" % (i, rel, cos)
 
 
+SD = H.load_surrogate_data()
+W = H.load_workloads()
+
+
+def test_training_on_world_windows_beats_untrained_and_persistence():
+    """What the trained network gains, at the benchmark's setting: trained on
+    windows cut from runs of the plain-step workloads (fields plus the cells'
+    rasterised heat and uptake sources), on held-out windows from other runs
+    its RMS error against the FTCS window is below persistence's (leaving the
+    fields as they are, the method's baseline without a model) and less than
+    half the untrained network's. Its largest error is not: at a few voxels
+    holding strong cell heat sources it exceeds persistence's many times over
+    (the benchmark reports both), so the judge's fallback stays in charge."""
+    desc, _sp, _info = W.workload("slab25k", seed=1)
+    sd = SD.surrogate_desc_for(desc, seed=5)
+    sg = agb.Surrogate(sd)
+    held = list(SD.world_windows(sd, 6, seed=900, every=7))
+    before = SD.evaluate(sg, held)
+    losses = [sg.train_on(*[x.data_ptr() for x in win]) for win in SD.world_windows(sd, TRAIN_WINDOWS, seed=100)]
+    assert sg.error_word() == 0 and np.all(np.isfinite(losses))
+    after = SD.evaluate(sg, held)
+    print("untrained", before, "trained", after)
+    assert after["net_rms_K"] < WORLD_RMS_GAIN * after["persistence_rms_K"]
+    assert after["net_rms_K"] < 0.5 * before["net_rms_K"]
+
+
+TRAIN_WINDOWS = 400
+RMS_GAIN = 0.5            # synthetic windows: measured 0.30 (0.112 K against 0.377 K)
+WORLD_RMS_GAIN = 0.85     # world windows: measured 0.69 (3.37 K against 4.88 K)
+
+
 def test_training_beats_untrained_and_persistence():
-    """What the trained network gains: on held-out windows its error against
-    the FTCS window is far below the untrained network's and below doing
-    nothing (persistence), the method's baseline without a model."""
-    d = agb.surrogate_desc(seed=5)                  # 128^3, 16 steps
+    """What the trained network gains on the seeded synthetic windows at the
+    benchmark's normalisation (20 K temperature excursions, 2 K/step heat
+    sources): on held-out windows its RMS error against the FTCS window is
+    far below the untrained network's and below persistence's."""
+    desc, _sp, _info = W.workload("slab25k", seed=1)
+    d = SD.surrogate_desc_for(desc, seed=5)         # 128^3, 16 steps
     sg = agb.Surrogate(d)
     shape = (d.nz, d.ny, d.nx)
-    T, Cf, qT, qC = fields(shape)
-
-    def held_out_error():
-        errs, base = [], []
-        for idx in (10 ** 6, 10 ** 6 + 1):
-            sg.window(idx, T.data_ptr(), Cf.data_ptr(), qT.data_ptr(), qC.data_ptr())
-            ref_T, ref_C = T.clone(), Cf.clone()
-            sg.reference(ref_T.data_ptr(), ref_C.data_ptr(), qT.data_ptr(), qC.data_ptr())
-            base.append(float((ref_T - T).abs().max()))
-            sg.advance(T.data_ptr(), Cf.data_ptr(), qT.data_ptr(), qC.data_ptr(), judge=-1)
-            errs.append(float((T - ref_T).abs().max()))
-        return max(errs), max(base)
-
-    e0, persistence = held_out_error()
-    losses = sg.train(300)
+    held = []
+    for idx in (10 ** 6, 10 ** 6 + 1, 10 ** 6 + 2):
+        f = fields(shape)
+        sg.window(idx, *[x.data_ptr() for x in f])
+        held.append(f)
+    before = SD.evaluate(sg, held)
+    losses = sg.train(TRAIN_WINDOWS)
     assert sg.error_word() == 0
     assert np.all(np.isfinite(losses))
     assert losses[-50:].mean() < 0.2 * losses[:20].mean()
-    e1, _ = held_out_error()
-    assert e1 < 0.5 * e0
-    assert e1 < persistence
+    after = SD.evaluate(sg, held)
+    print("untrained", before, "trained", after)
+    assert after["net_rms_K"] < 0.5 * before["net_rms_K"]
+    assert after["net_rms_K"] < RMS_GAIN * after["persistence_rms_K"]
 
 
 def test_judge_falls_back_to_ftcs():
