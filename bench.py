@@ -446,7 +446,7 @@ def profile_stencil(n, passes=6):
     d = agb.default_desc(capacity=16, seed=1)
     d.taxis_enabled = 0
     d.chamber_w = d.chamber_h = d.chamber_d = 4.0e-3
-    d.grid[agb.FIELD_T] = _grid3(n, agb.WATER_THERMAL_DIFFUSIVITY, agb.AMBIENT_TEMP_DEFAULT, 1e9, agb.BC_ROBIN)
+    d.grid[agb.FIELD_T] = W.grid3(n, agb.WATER_THERMAL_DIFFUSIVITY, agb.AMBIENT_TEMP_DEFAULT, 1e9, agb.BC_ROBIN)
     for f in (agb.FIELD_CO2, agb.FIELD_N2, agb.FIELD_IRR):
         d.grid[f] = agb.GridDesc()
     w = agb.World(d)
