@@ -325,6 +325,10 @@ def load(path=LIB_PATH):
         "agb_world_destroy": (None, [P]),
         "agb_world_spawn": (I32, [P, C.POINTER(Spawn), P]),
         "agb_world_spawn_seeded": (I32, [P, C.POINTER(Spawn), U64, P]),
+        "agb_world_set_charge": (I32, [P, C.c_double, P]),
+        "agb_world_set_boundary": (I32, [P, I32, C.POINTER(I32), C.POINTER(C.c_double)]),
+        "agb_world_set_rates": (I32, [P, C.c_double, C.c_double]),
+        "agb_world_set_overrides": (I32, [P, C.c_double, C.c_double]),
         "agb_world_import_cells": (I32, [P, C.POINTER(Cells), I32, U64, P]),
         "agb_world_export_cells": (I32, [P, C.POINTER(Cells), I32, C.POINTER(I32), C.POINTER(U64), P]),
         "agb_world_device_cells": (I32, [P, C.POINTER(Cells)]),
@@ -403,7 +407,9 @@ def load(path=LIB_PATH):
 def exported_symbols():
     """Names declared in include/agb.h, for the symbol-export test."""
     return ["agb_world_desc_default", "agb_status_str", "agb_last_error", "agb_device_info",
-            "agb_world_create", "agb_world_destroy", "agb_world_spawn", "agb_world_spawn_seeded", "agb_world_import_cells",
+            "agb_world_create", "agb_world_destroy", "agb_world_spawn", "agb_world_spawn_seeded", "agb_world_set_charge",
+            "agb_world_set_boundary", "agb_world_set_rates", "agb_world_set_overrides",
+            "agb_world_import_cells",
             "agb_world_export_cells", "agb_world_device_cells", "agb_world_step_host", "agb_world_count",
             "agb_world_import_field", "agb_world_export_field", "agb_world_export_deposit",
             "agb_world_apply_brush", "agb_world_set_flash", "agb_world_flash_audit",
@@ -472,6 +478,25 @@ class World:
             self._check(self.lib.agb_world_spawn(self.h, C.byref(p), _st(stream)), "spawn")
         else:
             self._check(self.lib.agb_world_spawn_seeded(self.h, C.byref(p), seed, _st(stream)), "spawn")
+
+    def set_charge(self, charge, stream=None):
+        """cell_store_set_charge: every occupied slot's store to charge * CELL_ENERGY_MAX."""
+        self._check(self.lib.agb_world_set_charge(self.h, float(charge), _st(stream)), "set_charge")
+
+    def set_boundary(self, field, bc, face_value):
+        """A field's six face kinds (BC_*) and face values, between ticks."""
+        b = (C.c_int32 * 6)(*[int(v) for v in bc])
+        f = (C.c_double * 6)(*[float(v) for v in face_value])
+        self._check(self.lib.agb_world_set_boundary(self.h, field, b, f), "set_boundary")
+
+    def set_rates(self, physics_rate, biology_rate):
+        """The clock rates as assigned to the World directly (unclamped)."""
+        self._check(self.lib.agb_world_set_rates(self.h, float(physics_rate), float(biology_rate)), "set_rates")
+
+    def set_overrides(self, co2_mass_per_division, max_emit_power):
+        """World::co2_mass_per_division and World::petrova_max_power, between ticks."""
+        self._check(self.lib.agb_world_set_overrides(self.h, float(co2_mass_per_division), float(max_emit_power)),
+                    "set_overrides")
 
     def spawn_taumoeba(self, count, seed, stream=None):
         """taumoeba_spawn: `count` predators, streams from (splitmix64(seed), id)."""

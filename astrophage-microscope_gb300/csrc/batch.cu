@@ -181,7 +181,7 @@ ChamberArgs chamber_args(agb_world* w) {
     a.nblk = w->blocks;
     const GridDev& co2 = w->c.g[AGB_FIELD_CO2];
     a.demand = co2.enabled ? w->life.co2_demand : nullptr;
-    a.inv_gv = co2.enabled ? (float)(1.0 / (co2.dx * co2.dx * co2.dz_eff)) : 0.0f;
+    a.gv = co2.enabled ? co2.dx * co2.dx * co2.dz_eff : 0.0;
     bool per4 = true;
     hash_sort_shape(w->c.h, w->c.capacity, a.passes, a.max_tiles, per4, a.radix_bits);
     return a;

@@ -33,7 +33,7 @@ struct ChamberArgs {
     unsigned long long* demand;   // CO2 rationing words (null: no CO2 grid)
     LifeBuffers life;
     uint32_t *kalt, *valt, *hist; // hash sort scratch
-    float inv_gv;
+    double gv;
     int32_t nblk;                 // the chamber's blocks in this launch
     int32_t arg;                  // stage switch (cell step: feed | taxis << 1; divide: compaction allowed)
     int32_t passes, max_tiles;    // hash sort: digit passes, tiles per pass
@@ -88,19 +88,29 @@ inline int32_t sweep_rows_blocks(int64_t lines) {
 void hash_sort_shape(const HashDev& h, int32_t capacity, int32_t& passes, int32_t& max_tiles, bool& per4,
                      int32_t& radix_bits);
 
-// co2_uptake_rate (src/sim/lifecycle.cuh:24-28) in FP32.
-__device__ __forceinline__ float co2_uptake_rate_f(float c) {
-    if (c <= 0.0f) return 0.0f;
-    return (float)AGB_LIFE_CO2_UPTAKE_MAX * c / (c + (float)AGB_LIFE_CO2_HALF_SATURATION);
+// co2_uptake_rate (src/sim/lifecycle.cuh:24-28): FP64 in the reference's
+// operation order. The rationing below compares a voxel's booked demand with
+// its contents, and only the reference's precision keeps the total taken
+// within what the voxel holds (in FP32 the relative error of ~1e-7 let a
+// drained voxel go slightly negative).
+__device__ __forceinline__ double co2_uptake_rate_d(double c) {
+    if (c <= 0.0) return 0.0;
+    return __ddiv_rn(__dmul_rn(AGB_LIFE_CO2_UPTAKE_MAX, c), __dadd_rn(c, AGB_LIFE_CO2_HALF_SATURATION));
 }
 
-// One live cell's CO2 demand at (x, y, z) into the voxel's rationing word
-// (demand_kernel body, src/sim/lifecycle.cu:41-57).
+// fixed_atomic.cuh to_fixed: llround(value * scale).
+__device__ __forceinline__ long long to_fixed_d(double v, double scale) {
+    return llround(__dmul_rn(v, scale));
+}
+
+// One live cell's CO2 demand at (x, y, z) into the voxel's rationing word, as
+// a concentration (demand_kernel body, src/sim/lifecycle.cu:41-57); gv is the
+// voxel volume.
 __device__ __forceinline__ void co2_demand_cell(const GridDev& C2, const TickParams& p, float x, float y, float z,
-                                                unsigned long long* demand, float inv_gv) {
+                                                unsigned long long* demand, double gv) {
     const int64_t idx = grid_nearest(C2, x, y, z);
-    const float want = co2_uptake_rate_f(C2.value[idx]) * p.dt_bio_f;
-    if (want > 0.0f) deposit_fixed(&demand[idx], to_fixed_f(want * inv_gv, C2.scale_f));
+    const double want = __dmul_rn(co2_uptake_rate_d((double)C2.value[idx]), p.dt_bio);
+    if (want > 0.0) deposit_fixed(&demand[idx], to_fixed_d(__ddiv_rn(want, gv), C2.scale));
 }
 
 void launch_thermal(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, cudaStream_t s);
@@ -128,7 +138,7 @@ void launch_forces(DevState* S, const Ctx& c, const TickParams& p, float* fx, fl
                    int32_t blocks, int lanes, cudaStream_t s);
 void launch_integrate(DevState* S, const Ctx& c, const TickParams& p, const float* fx, const float* fy,
                       const float* fz, int32_t blocks, const GridDev& co2, unsigned long long* demand,
-                      float inv_gv, cudaStream_t s);
+                      double gv, cudaStream_t s);
 // Feeding (when `feed`), taxis (when `taxis`) and forces in one per-cell pass
 // with one neighbour walk: the same cell values as launch_feed, launch_taxis
 // and launch_forces in turn, with two kernels fewer on the tick's critical
@@ -147,6 +157,8 @@ void launch_compact(DevState* S, const Ctx& c, const LifeBuffers& b, int32_t blo
 void launch_stats(DevState* S, const Ctx& c, unsigned long long* acc, int32_t blocks, cudaStream_t s);
 // spawn_kernel (src/sim/cell_store.cu:42-130) for `count` new cells.
 void launch_spawn(DevState* S, const Ctx& c, const agb_spawn& p, int32_t blocks, cudaStream_t s);
+// Every occupied slot's energy set to `energy` (cell_store.cu:281-297).
+void launch_set_charge(DevState* S, double energy, int32_t blocks, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // Taumoeba, the predator (src/sim/predation.cuh:82-118, k_tau.cu)

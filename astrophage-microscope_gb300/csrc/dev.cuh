@@ -111,7 +111,8 @@ struct GridDev {
     float hx, hy, hz;    // half extents as the reference computes them (0.5f * n * dx)
     double dx, dz_eff;
     double scale;
-    float inv_scale_f;
+    float inv_scale_f;   // (float)(1 / scale)
+    float inv_scale_lo;  // (float)(1 / scale - inv_scale_f): with inv_scale_f, 1 / scale to ~2^-48
     float scale_f;       // (float)scale
 };
 
@@ -222,6 +223,42 @@ __device__ __forceinline__ long long f_to_ll(float v) {
         r = q + ((rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull);
     }
     return (u >> 31) ? -(long long)r : (long long)r;
+}
+
+// A fixed-point deposit as the flush folds it into a float field:
+// (float)((double)raw / scale), from_fixed (fixed_atomic.cuh:31-33) rounded to
+// float as flush_kernel does (diffuse.cu:51-60), bit for bit, on the FP32 pipe.
+// The quotient is formed as a double-float product of raw (split into two
+// floats exactly: hi + remainder) and the scale's reciprocal (inv_hi + inv_lo,
+// ~2^-48 relative), to within 2^-44.5 of |raw / scale|, and rounded to float;
+// the exact two-sum residual of that rounding shows how far the value lies from
+// a rounding midpoint. Only when it lies within the error bound (4 calls in
+// 10^6 on random deposits) does the FP64 division decide, out of line. Checked
+// on the CPU against the double division on 6.5e7 deposits, random and placed
+// next to rounding midpoints, at the three deposit scales: no difference. A plain FP32
+// raw * (1 / scale) is off in the last bit often enough that a field drained
+// by rationing ended at -4e-9 instead of 0.
+static __device__ __noinline__ float fixed_to_f_div(long long raw, double scale) {
+    return (float)__ddiv_rn((double)raw, scale);
+}
+__device__ __forceinline__ float fixed_to_f(long long raw, float inv_hi, float inv_lo, double scale) {
+    const float r_hi = ll_to_f(raw);
+    const float r_lo = ll_to_f(raw - f_to_ll(r_hi));                     // remainder exact in int64
+    const float p = __fmul_rn(r_hi, inv_hi);
+    const float e = __fmaf_rn(r_hi, inv_hi, -p);                         // p's rounding error, exact
+    const float c = __fadd_rn(e, __fmaf_rn(r_hi, inv_lo, __fmul_rn(r_lo, inv_hi)));
+    const float f = __fadd_rn(p, c);
+    const float bb = __fsub_rn(f, p);
+    const float t = __fadd_rn(__fsub_rn(p, __fsub_rn(f, bb)), __fsub_rn(c, bb));   // (p + c) - f, exact
+    // The midpoints next to f lie half an ulp away (a quarter below an exact
+    // power of two, whose lower neighbour is closer); f stands when |t| plus
+    // the bound on the product's error and on the reference's own rounding to
+    // double stays short of that.
+    const float af = fabsf(f);
+    const uint32_t ab = __float_as_uint(af);
+    const float lim = __uint_as_float(ab & 0x7F800000u) * ((ab & 0x7FFFFFu) ? 0x1p-24f : 0x1p-25f);
+    if (fabsf(t) + af * 0x1p-43f < lim) return f;
+    return fixed_to_f_div(raw, scale);
 }
 
 // FP64 draws as the reference takes them (rng.cuh:86-101), for the seeded

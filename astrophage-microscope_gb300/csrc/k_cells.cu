@@ -563,7 +563,9 @@ __device__ __forceinline__ void feed_cell(DevState* S, const SoA& v, const Ctx& 
     const HashDev h = c.h;
     const double px = v.x[i], py = v.y[i], pz = v.z[i];
     float directional = feed_directional(c, px, py, pz);
-    if (c.occlusion_exact) {
+    // A cell in exact darkness stays dark whatever shades it: skip the walk
+    // (directional * open is 0 for any open in [0, 1]).
+    if (c.occlusion_exact && directional > 0.0f) {
         const float4 me = h.rec[ks];
         int32_t gx, gy, gz;
         unpack_bucket(me.w, gx, gy, gz);
@@ -784,7 +786,7 @@ __device__ __forceinline__ void integrate_kernel_body(DevState* S, const Ctx& c,
                                                       const float* __restrict__ fx_in,
                                                       const float* __restrict__ fy_in,
                                                       const float* __restrict__ fz_in, const GridDev& co2,
-                                                      unsigned long long* demand, float inv_gv, Blk blk) {
+                                                      unsigned long long* demand, double gv, Blk blk) {
     const SoA v = S->cur;
     const int32_t n = S->count;
     AGB_FOR_CELLS_B(i, blk, n) {
@@ -854,7 +856,7 @@ __device__ __forceinline__ void integrate_kernel_body(DevState* S, const Ctx& c,
         v.x[i] = px; v.y[i] = py; v.z[i] = pz;
         v.vx[i] = f2d(ux); v.vy[i] = f2d(uy); v.vz[i] = f2d(uz);
         v.age_s[i] = v.age_s[i] + p.dtf;
-        if (demand && (nf & AGB_FLAG_ALIVE)) co2_demand_cell(co2, p, d2f(px), d2f(py), d2f(pz), demand, inv_gv);
+        if (demand && (nf & AGB_FLAG_ALIVE)) co2_demand_cell(co2, p, d2f(px), d2f(py), d2f(pz), demand, gv);
     }
 }
 
@@ -862,9 +864,9 @@ __global__ void __launch_bounds__(256) integrate_kernel(DevState* S, Ctx c, Tick
                                                         const float* __restrict__ fx_in,
                                                         const float* __restrict__ fy_in,
                                                         const float* __restrict__ fz_in, GridDev co2,
-                                                        unsigned long long* demand, float inv_gv) {
+                                                        unsigned long long* demand, double gv) {
     pdl_wait();
-    integrate_kernel_body(S, c, p, fx_in, fy_in, fz_in, co2, demand, inv_gv, grid_blk());
+    integrate_kernel_body(S, c, p, fx_in, fy_in, fz_in, co2, demand, gv, grid_blk());
 }
 
 // ---------------------------------------------------------------------------
@@ -1030,8 +1032,11 @@ __device__ __forceinline__ void cell_step_kernel_body(DevState* S, const Ctx& c,
         }
         const uint32_t f = v.flags[i];
         const bool fd = feed && (f & AGB_FLAG_OCCUPIED) && (f & AGB_FLAG_ALIVE);
-        const bool shade = fd && c.occlusion_exact;
         const double px = v.x[i], py = v.y[i], pz = v.z[i];
+        float directional = fd ? feed_directional(c, px, py, pz) : 0.0f;
+        // A cell in exact darkness needs no shading test (directional * open
+        // is 0 for any open in [0, 1]); its contacts are still walked.
+        const bool shade = fd && c.occlusion_exact && directional > 0.0f;
         float open = 1.0f, Cx = 0.0f, Cy = 0.0f, Cz = 0.0f;
         int32_t rs = 0, rc = 0;
         if (shade || contact) {
@@ -1064,7 +1069,6 @@ __device__ __forceinline__ void cell_step_kernel_body(DevState* S, const Ctx& c,
         if (rs) atomicAdd(&S->n_shadow_refine, rs);
         if (rc) atomicAdd(&S->n_contact_refine, rc);
         if (fd) {
-            float directional = feed_directional(c, px, py, pz);
             if (shade) directional *= open;
             feed_finish(v, c, p, i, directional);
         }
@@ -1094,7 +1098,7 @@ AGB_BATCHED(sweep_lines_batch, 128, sweep_kernel_body(a.c, a.factor, blk))
 AGB_BATCHED_MB(cell_step_batch, 256, 4,
             cell_step_kernel_body<1>(a.S, a.c, a.p, a.arg & 1, (a.arg >> 1) & 1, a.fx, a.fy, a.fz, blk))
 AGB_BATCHED_MB(integrate_batch, 256, 4,
-            integrate_kernel_body(a.S, a.c, a.p, a.fx, a.fy, a.fz, a.g, a.demand, a.inv_gv, blk))
+            integrate_kernel_body(a.S, a.c, a.p, a.fx, a.fy, a.fz, a.g, a.demand, a.gv, blk))
 
 }  // namespace
 
@@ -1219,8 +1223,8 @@ void launch_forces(DevState* S, const Ctx& c, const TickParams& p, float* fx, fl
 }
 void launch_integrate(DevState* S, const Ctx& c, const TickParams& p, const float* fx, const float* fy,
                       const float* fz, int32_t blocks, const GridDev& co2, unsigned long long* demand,
-                      float inv_gv, cudaStream_t s) {
-    launch_k(integrate_kernel, blocks, 256, 0, s, S, c, p, fx, fy, fz, co2, demand, inv_gv);
+                      double gv, cudaStream_t s) {
+    launch_k(integrate_kernel, blocks, 256, 0, s, S, c, p, fx, fy, fz, co2, demand, gv);
 }
 void launch_motion(DevState* S, const Ctx& c, const TickParams& p, float* fx, float* fy, float* fz,
                    int32_t blocks, int lanes, cudaStream_t s) {

@@ -350,11 +350,8 @@ __device__ __forceinline__ void flush_by_cells_kernel_body(DevState* S, const Gr
         if (!(v.flags[i] & AGB_FLAG_OCCUPIED)) continue;
         const int64_t idx = grid_nearest(g, (float)v.x[i], (float)v.y[i], (float)v.z[i]);
         const unsigned long long raw = atomicExch(&g.deposit[idx], 0ull);
-        if (raw != 0ull) {
-            // (float)(raw / scale): FP32 scaling; identical to the reference's
-            // double division except in the last bit of a ~1e-2 increment.
-            g.value[idx] = fa(g.value[idx], ll_to_f((long long)raw) * g.inv_scale_f);
-        }
+        if (raw != 0ull)
+            g.value[idx] = fa(g.value[idx], fixed_to_f((long long)raw, g.inv_scale_f, g.inv_scale_lo, g.scale));
         if (demand) demand[idx] = 0ull;
     }
 }
@@ -475,7 +472,10 @@ FtcsPlan ftcs_plan_copies(int32_t nx, int32_t ny, int32_t nz, int32_t lx, int32_
         const int64_t tx = 4 * p.lx, ty = (256 / p.lx) * p.rpt;
         const int64_t tiles = ((nx + tx - 1) / tx) * ((ny + ty - 1) / ty);
         const int64_t slots = (int64_t)sm_count() * per_sm;
-        int64_t zc = (tiles * nz * copies + slots - 1) / slots;
+        // As many z chunks as one wave holds (rounding the chunk count up
+        // instead would leave a few CTAs to run alone after the wave).
+        const int64_t per_wave = slots / (tiles * copies);
+        int64_t zc = per_wave >= 1 ? (nz + per_wave - 1) / per_wave : (tiles * nz * copies + slots - 1) / slots;
         zc = zc < 2 ? 2 : (zc > 32 ? 32 : zc);
         const int64_t chunks = (nz + zc - 1) / zc;
         p.zc = (int32_t)((nz + chunks - 1) / chunks);

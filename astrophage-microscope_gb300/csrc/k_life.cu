@@ -27,7 +27,7 @@ constexpr int STILE = ST * SITEMS;
 // integration (integrate_kernel), which has the moved cell at hand; the
 // per-stage lifecycle runs it here.
 __global__ void __launch_bounds__(256) demand_kernel(DevState* S, Ctx c, TickParams p,
-                                                     unsigned long long* demand, float inv_gv) {
+                                                     unsigned long long* demand, double gv) {
     pdl_wait();
     const SoA v = S->cur;
     const int32_t n = S->count;
@@ -35,7 +35,7 @@ __global__ void __launch_bounds__(256) demand_kernel(DevState* S, Ctx c, TickPar
     AGB_FOR_CELLS(i, n) {
         const uint32_t f = v.flags[i];
         if (!(f & AGB_FLAG_OCCUPIED) || !(f & AGB_FLAG_ALIVE)) continue;
-        co2_demand_cell(C2, p, d2f(v.x[i]), d2f(v.y[i]), d2f(v.z[i]), demand, inv_gv);
+        co2_demand_cell(C2, p, d2f(v.x[i]), d2f(v.y[i]), d2f(v.z[i]), demand, gv);
     }
 }
 
@@ -51,7 +51,7 @@ __device__ __forceinline__ bool ready_to_divide(const Ctx& c, const SoA& v, int3
 // word, which nothing here reads; the CO2 flush that must follow every
 // deposit (lifecycle.cu:235) runs in the divide pass.
 __device__ __forceinline__ void uptake_mark_kernel_body(DevState* S, const Ctx& c, const TickParams& p,
-                                                        const unsigned long long* __restrict__ demand, float inv_gv,
+                                                        const unsigned long long* __restrict__ demand, double gv,
                                                         int32_t* divflag, Blk blk) {
     const SoA v = S->cur;
     const int32_t n = S->count;
@@ -60,16 +60,17 @@ __device__ __forceinline__ void uptake_mark_kernel_body(DevState* S, const Ctx& 
     AGB_FOR_CELLS_B(i, blk, n) {
         uint32_t f = v.flags[i];
         if (demand && (f & AGB_FLAG_OCCUPIED) && (f & AGB_FLAG_ALIVE)) {
+            // uptake_kernel (lifecycle.cu:62-86) in FP64, the reference's order.
             const int64_t idx = grid_nearest(C2, d2f(v.x[i]), d2f(v.y[i]), d2f(v.z[i]));
-            const float available = C2.value[idx];
-            const float want = co2_uptake_rate_f(available) * p.dt_bio_f;
-            if (want > 0.0f) {
-                const float asked = ll_to_f((long long)demand[idx]) * C2.inv_scale_f;   // from_fixed
-                float taken = want;
-                if (asked > available && asked > 0.0f) taken = want * (available / asked);
-                if (taken > 0.0f) {
-                    v.co2_held[i] = v.co2_held[i] + f2d(taken);
-                    deposit_fixed(&C2.deposit[idx], to_fixed_f(-taken * inv_gv, C2.scale_f));
+            const double available = (double)C2.value[idx];
+            const double want = __dmul_rn(co2_uptake_rate_d(available), p.dt_bio);
+            if (want > 0.0) {
+                const double asked = __ddiv_rn((double)(long long)demand[idx], C2.scale);   // from_fixed
+                double taken = want;
+                if (asked > available && asked > 0.0) taken = __dmul_rn(want, __ddiv_rn(available, asked));
+                if (taken > 0.0) {
+                    v.co2_held[i] = __dadd_rn(v.co2_held[i], taken);
+                    deposit_fixed(&C2.deposit[idx], to_fixed_d(__ddiv_rn(-taken, gv), C2.scale));
                 }
             }
         }
@@ -99,9 +100,9 @@ __device__ __forceinline__ void uptake_mark_kernel_body(DevState* S, const Ctx& 
 
 __global__ void __launch_bounds__(256) uptake_mark_kernel(DevState* S, Ctx c, TickParams p,
                                                           const unsigned long long* __restrict__ demand,
-                                                          float inv_gv, int32_t* divflag) {
+                                                          double gv, int32_t* divflag) {
     pdl_wait();
-    uptake_mark_kernel_body(S, c, p, demand, inv_gv, divflag, grid_blk());
+    uptake_mark_kernel_body(S, c, p, demand, gv, divflag, grid_blk());
 }
 
 // ---------------------------------------------------------------------------
@@ -287,7 +288,7 @@ __device__ __forceinline__ void divide_kernel_body(DevState* S, const Ctx& c, co
         if (demand && (v.flags[i] & AGB_FLAG_OCCUPIED)) {
             const int64_t idx = grid_nearest(C2, (float)v.x[i], (float)v.y[i], (float)v.z[i]);
             const unsigned long long raw = atomicExch(&C2.deposit[idx], 0ull);
-            if (raw != 0ull) C2.value[idx] = fa(C2.value[idx], ll_to_f((long long)raw) * C2.inv_scale_f);
+            if (raw != 0ull) C2.value[idx] = fa(C2.value[idx], fixed_to_f((long long)raw, C2.inv_scale_f, C2.inv_scale_lo, C2.scale));
             demand[idx] = 0ull;
         }
         if (births_now <= 0 || !divflag[i]) continue;
@@ -611,7 +612,7 @@ void launch_compact_kernels(DevState* S, const LifeBuffers& b, int32_t capacity,
 }
 
 AGB_BATCHED_MB(uptake_mark_batch, 256, 4,
-            uptake_mark_kernel_body(a.S, a.c, a.p, a.demand, a.inv_gv, a.life.flags, blk))
+            uptake_mark_kernel_body(a.S, a.c, a.p, a.demand, a.gv, a.life.flags, blk))
 AGB_BATCHED_MB(divide_batch, 256, 4,
             divide_kernel_body(a.S, a.c, a.life.flags, a.life.prefix, a.arg, a.demand, blk))
 AGB_BATCHED(keep_batch, 256, keep_kernel_body(a.S, a.life.flags, blk))
@@ -652,9 +653,9 @@ void launch_lifecycle(DevState* S, const Ctx& c, const TickParams& p, const Life
                       bool compaction_allowed, int32_t blocks, cudaStream_t s, bool demand_done) {
     const GridDev& C2 = c.g[AGB_FIELD_CO2];
     unsigned long long* dem = C2.enabled ? b.co2_demand : nullptr;
-    const float inv_gv = C2.enabled ? (float)(1.0 / (C2.dx * C2.dx * C2.dz_eff)) : 0.0f;
-    if (C2.enabled && !demand_done) launch_k(demand_kernel, blocks, 256, 0, s, S, c, p, dem, inv_gv);
-    launch_k(uptake_mark_kernel, blocks, 256, 0, s, S, c, p, dem, inv_gv, b.flags);
+    const double gv = C2.enabled ? C2.dx * C2.dx * C2.dz_eff : 0.0;
+    if (C2.enabled && !demand_done) launch_k(demand_kernel, blocks, 256, 0, s, S, c, p, dem, gv);
+    launch_k(uptake_mark_kernel, blocks, 256, 0, s, S, c, p, dem, gv, b.flags);
     launch_scan(S, b, c.capacity, 0, s);
     launch_k(divide_kernel, blocks, 256, 0, s, S, c, b.flags, b.prefix, compaction_allowed ? 1 : 0, dem);
     // Compaction cannot run on this tick unless the host-side period allows it.
@@ -681,6 +682,20 @@ void launch_stats(DevState* S, const Ctx& c, unsigned long long* acc, int32_t bl
 void launch_spawn(DevState* S, const Ctx& c, const agb_spawn& p, int32_t blocks, cudaStream_t s) {
     launch_k(spawn_kernel, blocks, 256, 0, s, S, c, p);
     launch_k(spawn_finalize_kernel, 1, 1, 0, s, S, p.count);
+}
+
+// Every occupied slot's store set to one energy (set_charge_kernel,
+// cell_store.cu:281-297).
+__global__ void __launch_bounds__(256) set_charge_kernel(DevState* S, double energy) {
+    pdl_wait();
+    const SoA v = S->cur;
+    AGB_FOR_CELLS(i, S->count) {
+        if (v.flags[i] & AGB_FLAG_OCCUPIED) v.energy[i] = energy;
+    }
+}
+
+void launch_set_charge(DevState* S, double energy, int32_t blocks, cudaStream_t s) {
+    launch_k(set_charge_kernel, blocks, 256, 0, s, S, energy);
 }
 
 }  // namespace agb

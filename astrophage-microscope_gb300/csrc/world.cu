@@ -417,13 +417,13 @@ void tick_once(agb_world* w, cudaStream_t s) {
     cudaStreamWaitEvent(s, w->ev[2], 0);
     mark(w, AGB_SECTION_INTEGRATE, 0, s);
     const GridDev& co2 = w->c.g[AGB_FIELD_CO2];
-    const float inv_gv = co2.enabled ? (float)(1.0 / (co2.dx * co2.dx * co2.dz_eff)) : 0.0f;
+    const double gv = co2.enabled ? co2.dx * co2.dx * co2.dz_eff : 0.0;
     // With predators the CO2 demand waits for predation (it kills prey before
     // the lifecycle books demand, step.cu:173-180); otherwise integration
     // books it.
     const bool fuse_demand = co2.enabled && !w->tau_active;
     launch_integrate(w->S, c, w->tp, w->fx, w->fy, w->fz, w->blocks, co2,
-                     fuse_demand ? w->life.co2_demand : nullptr, inv_gv, s);
+                     fuse_demand ? w->life.co2_demand : nullptr, gv, s);
     mark(w, AGB_SECTION_INTEGRATE, 1, s);
     mark(w, AGB_SECTION_LIFECYCLE, 0, s);
     stage_predation(w, s);
@@ -810,6 +810,7 @@ agb_status agb_world_create(const agb_world_desc* d, agb_world** out) {
         g.hz = 0.5f * gd.nz * g.dzf;
         g.scale = gd.deposit_scale;
         g.inv_scale_f = (float)(1.0 / gd.deposit_scale);
+        g.inv_scale_lo = (float)(1.0 / gd.deposit_scale - (double)g.inv_scale_f);
         g.scale_f = (float)g.scale;
         for (int k = 0; k < 6; ++k) { w->gbc[f][k] = gd.bc[k]; w->gface[f][k] = (float)gd.face_value[k]; }
         w->grobin[f] = (float)(g.dx * AGB_AIR_CONVECTION_H / AGB_WATER_CONDUCTIVITY);
@@ -957,6 +958,16 @@ agb_status agb_world_spawn_seeded(agb_world* w, const agb_spawn* p, uint64_t see
 agb_status agb_world_spawn(agb_world* w, const agb_spawn* p, agb_stream s) {
     if (!w) return AGB_INVALID_ARGUMENT;
     return agb_world_spawn_seeded(w, p, w->c.seed, s);
+}
+
+agb_status agb_world_set_charge(agb_world* w, double charge, agb_stream s) {
+    if (!w) return AGB_INVALID_ARGUMENT;
+    // clamp01: NaN falls through both tests, as it does in the reference.
+    const double q = charge < 0.0 ? 0.0 : (charge > 1.0 ? 1.0 : charge);
+    if (s == nullptr && w->own_stream) s = w->own_stream;
+    launch_set_charge(w->S, q * AGB_CELL_ENERGY_MAX, w->blocks, s);
+    AGB_CUDA(w, cudaGetLastError());
+    return AGB_OK;
 }
 
 agb_status agb_world_count(agb_world* w, int32_t* count, agb_stream s) {
@@ -1540,6 +1551,27 @@ agb_status agb_world_set_clock(agb_world* w, double p, double b) {   // world_se
     return compute_tick_params(w);
 }
 
+agb_status agb_world_set_rates(agb_world* w, double p, double b) {
+    if (!w) return AGB_INVALID_ARGUMENT;
+    if (!(std::isfinite(p) && p > 0.0 && std::isfinite(b) && b > 0.0))
+        return fail(w, AGB_INVALID_ARGUMENT, "clock rates must be finite and positive");
+    w->physics_rate = p;
+    w->biology_rate = b;
+    invalidate_graphs(w);
+    return compute_tick_params(w);
+}
+
+agb_status agb_world_set_overrides(agb_world* w, double co2_mass_per_division, double max_emit_power) {
+    if (!w) return AGB_INVALID_ARGUMENT;
+    if (!std::isfinite(co2_mass_per_division) || !std::isfinite(max_emit_power))
+        return fail(w, AGB_INVALID_ARGUMENT, "overrides must be finite");
+    w->d.co2_mass_per_division = co2_mass_per_division;
+    w->d.max_emit_power = max_emit_power;
+    w->c.co2_quota = co2_mass_per_division;
+    invalidate_graphs(w);
+    return compute_tick_params(w);
+}
+
 agb_status agb_world_set_light(agb_world* w, const agb_light* light) {
     if (!w || !light) return AGB_INVALID_ARGUMENT;
     w->d.light = *light;
@@ -1550,6 +1582,23 @@ agb_status agb_world_set_light(agb_world* w, const agb_light* light) {
     AGB_CUDA(w, cudaDeviceSynchronize());
     irr_all_lines(w, nullptr);
     AGB_CUDA(w, cudaDeviceSynchronize());
+    return AGB_OK;
+}
+
+agb_status agb_world_set_boundary(agb_world* w, int32_t field, const int32_t bc[6], const double face_value[6]) {
+    if (!w || !bc || !face_value || field < 0 || field >= AGB_FIELD_COUNT) return AGB_INVALID_ARGUMENT;
+    if (!w->c.g[field].enabled) return fail(w, AGB_INVALID_ARGUMENT, "boundary of a field the world does not have");
+    for (int k = 0; k < 6; ++k) {
+        if (bc[k] < AGB_BC_DIRICHLET || bc[k] > AGB_BC_ROBIN) return fail(w, AGB_INVALID_ARGUMENT, "boundary kind");
+        if (!std::isfinite(face_value[k])) return fail(w, AGB_INVALID_ARGUMENT, "face value must be finite");
+    }
+    for (int k = 0; k < 6; ++k) {
+        w->d.grid[field].bc[k] = bc[k];
+        w->d.grid[field].face_value[k] = face_value[k];
+        w->gbc[field][k] = bc[k];
+        w->gface[field][k] = (float)face_value[k];
+    }
+    invalidate_graphs(w);                              // captured passes baked the old faces
     return AGB_OK;
 }
 

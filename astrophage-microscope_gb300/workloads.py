@@ -17,6 +17,12 @@ the CPU oracle. Used by bench.py (timing) and the 3-D parity tests.
   clusters20k the 1M-cell workload scaled to 20,000 cells and 64^3 grids for
               the oracle: 8 clusters of sigma 20 um, which keeps the cluster
               cores as dense as the 1M-cell workload's.
+  ref200k     the reference's own throughput test (tests/physics/test_perf.cu
+              T28): its default world (4 mm x 4 mm x 60 um, depth-averaged
+              512^2 temperature / 256^2 CO2 / 128^2 N2 / 512^2 irradiance
+              grids), 200,000 dormant cells uniform at charge 0.02, seed
+              20260802; the configuration the reference's published hash
+              rebuild (0.110 ms) and tick rate (281 ticks/s) are quoted at.
   batch       n 4 mm chambers, cells log-uniform in [1e3, 2e5], grid edges
               from {64, 96, 128, 192}, charge swept to 20 %.
 """
@@ -25,7 +31,7 @@ import numpy as np
 import agb
 
 EMAX = agb.CELL_ENERGY_MAX
-PLAIN = ("slab25k", "cube2k", "clusters1m", "clusters20k")
+PLAIN = ("slab25k", "cube2k", "clusters1m", "clusters20k", "ref200k")
 
 
 def grid3(n, D, init, scale, bc, face=None):
@@ -91,6 +97,11 @@ def workload(name, seed=1):
         return _clusters(1000000, 256, 64, 40e-6, seed, 2000000)
     if name == "clusters20k":
         return _clusters(20000, 64, 8, 20e-6, seed, 40000)
+    if name == "ref200k":
+        d = agb.default_desc(capacity=200000, seed=20260802 + seed - 1)
+        sp = agb.spawn(200000, charge_dist=agb.DIST_CONSTANT, charge_a=0.02, awake=False)
+        return d, sp, dict(cells=200000, grid="512^2 T, 256^2 CO2, 128^2 N2, 512^2 irradiance (depth-averaged)",
+                           chamber_mm="4 x 4 x 0.06", light="off", hash_cell_um=22.0)
     raise ValueError("unknown workload " + name)
 
 

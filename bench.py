@@ -732,6 +732,8 @@ def main():
     ap.add_argument("--scaled", default="clusters1m", choices=list(W.PLAIN) + ["none"],
                     help="second plain-step leg reported beside the headline (the HBM-graded configuration)")
     ap.add_argument("--scaled-steps", type=int, default=20)
+    ap.add_argument("--ref200k-steps", type=int, default=50,
+                    help="timed ticks of the reference's own 200,000-cell throughput configuration (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=30,
                     help="timed steps of the batched ensemble reported beside the plain step (0: skip)")
     ap.add_argument("--batch-chambers", type=int, default=64)
@@ -785,6 +787,17 @@ def main():
         scaled = run_plain(args.scaled, args, stream, l2_flush, dist, rank, ws, local, 3, args.scaled_steps)
         scaled.pop("config", None)
 
+    ref200k = None
+    if args.ref200k_steps > 0:
+        # The configuration the reference publishes its hash rebuild and tick
+        # rate at (RTX 4070 Ti SUPER): measured here the same way as the headline.
+        ref200k = run_plain("ref200k", args, stream, l2_flush, dist, rank, ws, local, 3, args.ref200k_steps)
+        ref200k.pop("config", None)
+        ref200k["published"] = {"hash_rebuild_ms": 0.110, "ticks_per_s": 281, "hardware": "RTX 4070 Ti SUPER",
+                                "source": "reference README.md:110-112"}
+        ref200k["hash_rebuild_ms"] = ref200k["sections_us"].get("hash", 0.0) / 1e3
+        ref200k["ticks_per_s"] = 1e3 / ref200k["ms_per_step"]
+
     batched = None
     if args.batch_steps > 0:
         batched = run_batch(args, stream, l2_flush, dist, rank, ws)
@@ -814,6 +827,7 @@ def main():
             "clocks": head["clocks"],
             "setup": "every tick phase's graph captured before warm-up (agb_world_prepare_graphs)",
             "scaled": scaled,
+            "ref200k": ref200k,
             "batched": batched,
             "surrogate": surrogate,
         }

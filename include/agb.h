@@ -340,6 +340,10 @@ agb_status agb_world_spawn(agb_world* w, const agb_spawn* p, agb_stream s);
  * seed + i and a top-up with seed + tick (src/sim/scenario.cpp:368-385, 436-452). */
 agb_status agb_world_spawn_seeded(agb_world* w, const agb_spawn* p, uint64_t seed, agb_stream s);
 
+/* cell_store_set_charge (src/sim/cell_store.cuh:78): every occupied slot's
+ * stored energy set to clamp(charge, 0, 1) * CELL_ENERGY_MAX. */
+agb_status agb_world_set_charge(agb_world* w, double charge, agb_stream s);
+
 /* Replace the whole population with `count` cells in contract layout; next_id
  * is the id the next daughter gets (CellStore::next_id). */
 agb_status agb_world_import_cells(agb_world* w, const agb_cells* src, int32_t count,
@@ -498,6 +502,18 @@ agb_status agb_world_stats_accum(agb_world* w, uint64_t out[12]);
 /* world_set_clock with explicit rates (src/sim/step.cu:196-205, clamped). */
 agb_status agb_world_set_clock(agb_world* w, double physics_rate, double biology_rate);
 agb_status agb_world_set_light(agb_world* w, const agb_light* light);
+/* The rates as a caller assigns World::physics_rate / biology_rate directly
+ * (src/sim/step.cu:133 reads them unclamped): finite and positive. */
+agb_status agb_world_set_rates(agb_world* w, double physics_rate, double biology_rate);
+/* The live overrides World::co2_mass_per_division and World::petrova_max_power
+ * (src/sim/world.cuh:171-173), assigned between ticks. */
+agb_status agb_world_set_overrides(agb_world* w, double co2_mass_per_division, double max_emit_power);
+
+
+/* A field's boundary between ticks (the caller assigning Grid2D::bc,
+ * src/fields/grid.cuh:84, as tests/physics/test_thermal.cu does): per face kind
+ * (AGB_BC_*) and Dirichlet value / Robin reference, AGB_FACE_* order. */
+agb_status agb_world_set_boundary(agb_world* w, int32_t field, const int32_t bc[6], const double face_value[6]);
 
 /* Hash state after the last hash stage: dims = {nx, ny, nz, bucket_count};
  * keys/vals in sorted order (count entries); bucket_start/end dense
