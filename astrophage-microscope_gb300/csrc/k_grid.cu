@@ -450,8 +450,9 @@ int sm_count() {
 // grids under 8 M voxels take one row per thread (more CTAs), larger ones two.
 // The z chunk is the smallest that fits the whole grid in one wave of resident
 // CTAs (fewer planes per CTA re-read more halo planes), at least 2 planes.
-// On a GB300 this measured 24.7 us per pass on 256^3 (5.4 TB/s) and 8.2 us on
-// 128^3, within 5 % of the best tiling of each. AGB_FTCS_TILE="lx,rpt,zc"
+// On a GB300 a pass on 256^3 takes 23.3 us inside a graph of passes (5.8 TB/s,
+// 704 CTAs of 12 planes) and 8.2 us on 128^3, within 5 % of the best tiling
+// of each. AGB_FTCS_TILE="lx,rpt,zc"
 // overrides the choice (a tuning knob; results are the same for every tiling).
 FtcsPlan ftcs_plan_with(int32_t nx, int32_t ny, int32_t nz, int32_t lx, int32_t rpt, int32_t zc_in) {
     return ftcs_plan_copies(nx, ny, nz, lx, rpt, zc_in, 1);

@@ -1,8 +1,9 @@
 """The host <-> device cell transfer kernels (agb_world_import_cells /
-agb_world_export_cells when the GPU addresses the host arrays directly): the
-25 contract arrays move as 16-byte chunks where both ends are 16-byte aligned,
-element by element otherwise and in each array's last partial chunk. Every
-combination moves the same bytes."""
+agb_world_export_cells when the GPU addresses the host arrays directly): one
+thread per cell moves its 25 contract elements. Host arrays need only be
+aligned to their element size; populations of any size, including empty and
+one cell, and arrays one element past a 16-byte boundary move the same bytes
+as aligned ones."""
 import numpy as np
 import pytest
 
@@ -12,10 +13,10 @@ agb = H.agb
 pytestmark = pytest.mark.gpu
 
 
-def world(n, seed=5):
+def world(n, seed=5, spawn=True):
     d = agb.default_desc(capacity=max(n, 1) + 64, seed=seed)
     w = agb.World(d)
-    if n:
+    if n and spawn:
         w.spawn(agb.spawn(n, charge_dist=agb.DIST_UNIFORM, charge_a=0.1, charge_b=0.9, awake=True))
         w.step(1)                     # every array non-trivial (velocities, temperatures, timers)
     return w
@@ -52,7 +53,7 @@ def test_export_import_aligned_and_misaligned_move_the_same_bytes(n):
     assert nid2 == nid
     same(got, ref)
     # Import from the misaligned arrays into a fresh world; export aligned.
-    w2 = world(0)
+    w2 = world(n, spawn=False)
     w2.import_cells(got, nid)
     back, nid3 = w2.export_cells()
     assert nid3 == nid and w2.count() == n
