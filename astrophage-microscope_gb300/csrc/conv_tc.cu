@@ -271,6 +271,267 @@ __global__ void __launch_bounds__(128) conv3_kernel(const __grid_constant__ CUte
     if (warp == 2) tmem_free(tmem, C::TCOLS);
 }
 
+// ---------------------------------------------------------------------------
+// Forward convolution over rows of 128 voxels: persistent, with row reuse.
+//
+// A tile is 128 x-consecutive voxels of one row (W a multiple of 128). Its
+// 27 taps read nine input rows -- (dz, dy) in {-1, 0, 1}^2, each 130 voxels
+// wide with the x halo. A slice is the three rows (dz = -1, 0, 1) of one y;
+// tile y reads slices y - 1, y, y + 1. Tiles are ordered y fastest and dealt
+// to the CTAs in groups of RG consecutive tiles, round robin, so the CTAs
+// work on neighbouring rows at any moment (each input row is fetched from
+// DRAM about once and its other reads hit L2), and inside a group
+// consecutive tiles share two of their three slices: a ring of slices in
+// shared memory is loaded once each, and a group of RG tiles costs RG + 2
+// slices instead of 3 RG. A row is copied
+// one 8-channel chunk per copy, so it lands as 130 consecutive 16-byte rows:
+// the K-major layout without swizzle (core matrices of 8 rows x 16 bytes,
+// 8-row groups 128 bytes apart, channel chunks one padded row block apart),
+// and the three x taps of a row start 0, 16 and 32 bytes into it. All 27
+// taps' weights stay in shared memory for the CTA's life. Roles: one TMA
+// producer thread, one MMA thread issuing the tile's 27 x (cin / 16)
+// tcgen05.mma into one of four tensor-memory accumulators, and four epilogue
+// warps draining the others (bias, ReLU, mask, conversion, store; an
+// accumulator is handed back as soon as it is read, before the stores), so
+// the epilogues of earlier tiles overlap the MMAs of later ones.
+//
+// Shared memory past the slices and the weights keeps spare room, so that
+// every descriptor's reach stays inside the allocation whichever way its two
+// strides are read.
+// ---------------------------------------------------------------------------
+constexpr int RCH = 2176;               // one 8-channel chunk of a 130-voxel row (2,080 B), padded to 128 B
+constexpr uint32_t RCH_TX = 2080;       // bytes one such copy delivers
+
+template <int COUT, int CIN>
+struct RowCfg {
+    static constexpr int Q = CIN / 8;                       // 16-byte channel chunks
+    static constexpr int RB = Q * RCH;                      // one input row
+    static constexpr int SL = 3 * RB;                       // one slice: the rows dz = -1, 0, 1 of one y
+    static constexpr int NSL = CIN == 16 ? 12 : 6;          // slices in the ring
+    static constexpr int WB = 27 * Q * COUT * 16;           // every tap's weights
+    static constexpr int NACC = 4;                          // tensor-memory accumulators
+    static constexpr uint32_t TCOLS = NACC * COUT <= 32 ? 32 : (NACC * COUT <= 64 ? 64 : (NACC * COUT <= 128 ? 128 : 256));
+    // Farthest byte an A descriptor could address with its two strides
+    // exchanged (16 row groups one chunk apart); B's exchanged reach past the
+    // weights is under 8 KB.
+    static constexpr int REACH = (NSL - 1) * SL + 2 * RB + (Q - 2) * RCH + 48 + 16 * RCH + 256;
+    static constexpr int SPARE = REACH - (NSL * SL + WB) > 8192 ? REACH - (NSL * SL + WB) : 8192;
+    static constexpr int SMEM = 1024 + NSL * SL + WB + SPARE + 768;
+    static constexpr uint32_t TX = 3 * Q * RCH_TX;          // bytes a slice's copies deliver
+};
+
+// K-major operand without swizzle: 8-row groups `sbo` bytes apart, 16-byte
+// K chunks `lbo` bytes apart.
+__device__ __forceinline__ uint64_t sdesc_plain(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+__device__ __forceinline__ void bar_arrive(uint64_t* b) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(saddr(b)) : "memory");
+}
+
+// Tiles y fastest: tile t is (x0, y, z) = ((t / H) % xt * 128, t % H, t / (H * xt)).
+// CTA b's i-th tile is t = (b + (i / RG) * gridDim.x) * RG + i % RG.
+constexpr int RG = 4;
+struct RowTile {
+    int x0, y, z;
+};
+// Tile counts stay below 2^31 (the launcher checks), so the tile arithmetic is 32-bit.
+__device__ __forceinline__ RowTile row_tile(int t, int H, int xt) {
+    const int r = t / H;
+    return RowTile{(r % xt) * BM, t % H, r / xt};
+}
+__device__ __forceinline__ int row_tile_index(int i) {
+    return ((int)blockIdx.x + (i / RG) * (int)gridDim.x) * RG + i % RG;
+}
+// Whether the CTA's i-th tile t starts a run (its y - 1 and y slices are not
+// the previous tile's).
+__device__ __forceinline__ bool run_start(int i, int t, int H) {
+    return i % RG == 0 || t % H == 0;
+}
+// Tiles of this CTA: whole groups, less the missing tail of the last group.
+__device__ __forceinline__ int row_tiles_of_cta(int ntiles) {
+    const int groups = (ntiles + RG - 1) / RG;
+    if ((int)blockIdx.x >= groups) return 0;
+    const int mine = (groups - 1 - (int)blockIdx.x) / (int)gridDim.x + 1;
+    int n = mine * RG;
+    if ((int)blockIdx.x + (mine - 1) * (int)gridDim.x == groups - 1) n -= groups * RG - ntiles;
+    return n;
+}
+
+template <int COUT, int CIN>
+__global__ void __launch_bounds__(192, 1) conv3_rows_kernel(const __grid_constant__ CUtensorMap xmap,
+                                                            const __nv_bfloat16* __restrict__ wgt, Conv3Args p) {
+    using C = RowCfg<COUT, CIN>;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = align1024(smem_raw);
+    uint8_t* wsm = smem + C::NSL * C::SL;
+    uint64_t* sfull = reinterpret_cast<uint64_t*>(wsm + C::WB + C::SPARE);
+    uint64_t* sempty = sfull + C::NSL;
+    uint64_t* accf = sempty + C::NSL;
+    uint64_t* acce = accf + C::NACC;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(acce + C::NACC);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
+    float* bias_sm = reinterpret_cast<float*>(tslot + 4);           // COUT floats
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int xt = p.W / BM;
+    const int ntiles = p.D * p.H * xt;
+    const int my = row_tiles_of_cta(ntiles);
+
+    // Every tap's weights, [tap][chunk][cout][8 channels], written by all
+    // threads; the proxy fence makes them visible to the tensor core.
+    for (int c = threadIdx.x; c < 27 * C::Q * COUT; c += blockDim.x) {
+        const int q = c % C::Q, co = (c / C::Q) % COUT, tap = c / (C::Q * COUT);
+        const uint4 v = *reinterpret_cast<const uint4*>(wgt + ((size_t)(tap * COUT + co) * CIN + q * 8));
+        *reinterpret_cast<uint4*>(wsm + ((size_t)(tap * C::Q + q) * COUT + co) * 16) = v;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    for (int c = threadIdx.x; c < COUT; c += blockDim.x) bias_sm[c] = p.bias ? p.bias[c] : 0.0f;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < C::NSL; ++s) { bar_init(&sfull[s], 1); bar_init(&sempty[s], 1); }
+        for (int a = 0; a < C::NACC; ++a) { bar_init(&accf[a], 1); bar_init(&acce[a], 4); }
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) tmem_alloc(tslot, C::TCOLS);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+
+    int loaded = 0, committed = 0;
+    if (warp == 0) {
+        if (lane == 0) {                                 // TMA producer: slices in order
+            bool ok = true;
+            for (int i = 0; i < my && ok; ++i) {
+                const int t = row_tile_index(i);
+                const RowTile c = row_tile(t, p.H, xt);
+                const int first = run_start(i, t, p.H) ? -1 : 1;     // y offsets of the new slices
+                for (int d = first; d <= 1; ++d) {
+                    const int k = loaded, slot = k % C::NSL;
+                    if (k >= C::NSL && !bar_wait(&sempty[slot], (uint32_t)((k / C::NSL - 1) & 1), abort_flag, p.err, 11)) {
+                        ok = false;
+                        break;
+                    }
+                    uint8_t* sl = smem + slot * C::SL;
+                    bar_expect(&sfull[slot], C::TX);
+                    for (int dz = 0; dz < 3; ++dz)
+#pragma unroll
+                        for (int q = 0; q < C::Q; ++q)
+                            tma4(sl + dz * C::RB + q * RCH, &xmap, &sfull[slot], q * 8, c.x0 - 1, c.y + d, c.z + dz - 1);
+                    loaded = k + 1;
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {                                 // MMA issuer
+            constexpr uint32_t idesc = idesc_bf16(COUT);
+            // Descriptors are built once; a tap adds its constant offset (in
+            // 16-byte units) to the start-address field, which stays below
+            // 2^14 for any shared-memory address, so the sum never carries.
+            const uint64_t bbase = sdesc_plain(saddr(wsm), COUT * 16, 128);
+            int hi = -1;                                 // slice index of the tile's y + 1 row
+            for (int i = 0; i < my; ++i) {
+                const int t = row_tile_index(i);
+                hi += run_start(i, t, p.H) ? 3 : 1;
+                const int a = i % C::NACC;
+                bool ok = true;
+                for (int k = hi - 2; k <= hi && ok; ++k)
+                    ok = bar_wait(&sfull[k % C::NSL], (uint32_t)((k / C::NSL) & 1), abort_flag, p.err, 12);
+                if (!ok) break;
+                if (i >= C::NACC && !bar_wait(&acce[a], (uint32_t)((i / C::NACC - 1) & 1), abort_flag, p.err, 13)) break;
+                tc_fence_after();
+                const uint32_t d = tmem + (uint32_t)(a * COUT);
+                uint64_t abase[3];                       // slices hi - 2, hi - 1, hi (dy = -1, 0, 1)
+#pragma unroll
+                for (int q = 0; q < 3; ++q)
+                    abase[q] = sdesc_plain(saddr(smem + ((hi - 2 + q) % C::NSL) * C::SL), RCH, 128);
+#pragma unroll
+                for (int tap = 0; tap < 27; ++tap) {
+                    // tap = (dz+1)*9 + (dy+1)*3 + (dx+1): slice dy+1, row dz+1, x shift dx+1 rows
+#pragma unroll
+                    for (int j = 0; j < C::Q / 2; ++j) {
+                        const uint64_t ad = abase[(tap / 3) % 3] +
+                                            (uint64_t)(((tap / 9) * C::RB + 2 * j * RCH + (tap % 3) * 16) >> 4);
+                        const uint64_t bd = bbase + (uint64_t)(((tap * C::Q + 2 * j) * COUT * 16) >> 4);
+                        mma_bf16(d, ad, bd, idesc, (tap | j) != 0);
+                    }
+                }
+                // Slices the next tile does not read are free once these MMAs are done.
+                const int next_lo = i + 1 < my ? hi + (run_start(i + 1, row_tile_index(i + 1), p.H) ? 3 : 1) - 2 : hi + 1;
+                for (int k = hi - 2; k < next_lo && k <= hi; ++k) mma_commit(&sempty[k % C::NSL]);
+                mma_commit(&accf[a]);
+                committed = i + 1;
+            }
+        }
+    } else {                                             // epilogue: warps 2-5, TMEM lanes of sub-partition warp % 4
+        const int sub = warp & 3;
+        for (int i = 0; i < my; ++i) {
+            const int a = i % C::NACC;
+            const bool ok = bar_wait(&accf[a], (uint32_t)((i / C::NACC) & 1), abort_flag, p.err, 14);
+            if (!__all_sync(0xFFFFFFFFu, ok)) break;
+            tc_fence_after();
+            const RowTile c = row_tile(row_tile_index(i), p.H, xt);
+            const int64_t m = ((int64_t)c.z * p.H + c.y) * p.W + c.x0 + sub * 32 + lane;
+#pragma unroll
+            for (int c0 = 0; c0 < COUT; c0 += 16) {
+                float v[16];
+                tmem_ld16(tmem + ((uint32_t)(sub * 32) << 16) + (uint32_t)(a * COUT + c0), v);
+#pragma unroll
+                for (int k = 0; k < 16; ++k) v[k] += bias_sm[c0 + k];
+                if (p.act == 1) {
+#pragma unroll
+                    for (int k = 0; k < 16; ++k) v[k] = fmaxf(v[k], 0.0f);
+                }
+                if (p.mask) {
+                    const uint4* mk = reinterpret_cast<const uint4*>(p.mask + m * COUT + c0);
+                    const uint4 u0 = __ldg(mk), u1 = __ldg(mk + 1);
+                    const uint32_t w[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        const __nv_bfloat162 h = *reinterpret_cast<const __nv_bfloat162*>(&w[k]);
+                        if (!(__bfloat162float(h.x) > 0.0f)) v[2 * k] = 0.0f;
+                        if (!(__bfloat162float(h.y) > 0.0f)) v[2 * k + 1] = 0.0f;
+                    }
+                }
+                if (c0 + 16 >= COUT) {
+                    // The accumulator is read out: hand it back before the stores.
+                    tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) bar_arrive(&acce[a]);
+                }
+                if (p.out_f32) {
+                    float4* o = reinterpret_cast<float4*>(static_cast<float*>(p.out) + m * COUT + c0);
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) o[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+                } else {
+                    uint32_t w[8];
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
+                        w[k] = *reinterpret_cast<const uint32_t*>(&h);
+                    }
+                    uint4* o = reinterpret_cast<uint4*>(static_cast<__nv_bfloat16*>(p.out) + m * COUT + c0);
+                    o[0] = make_uint4(w[0], w[1], w[2], w[3]);
+                    o[1] = make_uint4(w[4], w[5], w[6], w[7]);
+                }
+            }
+        }
+    }
+    // On an abort, wait (bounded) for this CTA's own copies and MMAs in flight
+    // before its shared and tensor memory go away.
+    if (*abort_flag) {
+        if (warp == 0 && lane == 0)
+            for (int k = loaded - C::NSL > 0 ? loaded - C::NSL : 0; k < loaded; ++k)
+                bar_drain(&sfull[k % C::NSL], (uint32_t)((k / C::NSL) & 1));
+        if (warp == 1 && lane == 0 && committed > 0)
+            bar_drain(&accf[(committed - 1) % C::NACC], (uint32_t)(((committed - 1) / C::NACC) & 1));
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) tmem_free(tmem, C::TCOLS);
+}
+
 template <int CIN, int KV>
 struct WgradCfg {
     static constexpr int ROWB = KV * 2;
@@ -395,6 +656,7 @@ CUtensorMapSwizzle swizzle_for(int rowb) {
     return rowb == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : (rowb == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B);
 }
 
+// rowb 0: no swizzle (the row kernel's copies); otherwise the swizzle matching a rowb-byte row.
 bool map_bf16(CUtensorMap* m, const void* base, int rank, const uint64_t* dims, const uint32_t* box, int rowb) {
     Encode enc = encoder();
     if (!enc) return false;
@@ -409,7 +671,8 @@ bool map_bf16(CUtensorMap* m, const void* base, int rank, const uint64_t* dims, 
         stride *= dims[i];
     }
     return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, (cuuint32_t)rank, const_cast<void*>(base), d, st, b, es,
-               CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle_for(rowb), CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, rowb == 0 ? CU_TENSOR_MAP_SWIZZLE_NONE : swizzle_for(rowb),
+               CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
@@ -430,6 +693,39 @@ cudaError_t launch_conv(const Conv3Args& a, const void* x, const void* w, cudaSt
     }
     const int64_t m = (int64_t)a.D * a.H * a.W;
     conv3_kernel<COUT, KC><<<(unsigned)(m / BM), 128, C::SMEM, s>>>(xm, wm, a);
+    return cudaGetLastError();
+}
+
+int sm_count() {
+    static int n = 0;
+    if (n == 0) {
+        int d = 0;
+        cudaGetDevice(&d);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, d);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+template <int COUT, int CIN>
+cudaError_t launch_conv_rows(const Conv3Args& a, const void* x, const void* w, cudaStream_t s) {
+    using C = RowCfg<COUT, CIN>;
+    static_assert(C::SMEM <= 232448, "row kernel shared memory");
+    CUtensorMap xm;
+    const uint64_t xd[4] = {(uint64_t)a.cin, (uint64_t)a.W, (uint64_t)a.H, (uint64_t)a.D};
+    const uint32_t xb[4] = {8u, (uint32_t)(BM + 2), 1u, 1u};
+    if (!map_bf16(&xm, x, 4, xd, xb, 0)) return cudaErrorInvalidValue;
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(conv3_rows_kernel<COUT, CIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
+        attr = true;
+    }
+    const int64_t tiles = (int64_t)a.D * a.H * (a.W / BM);
+    if (tiles >= (1LL << 31) - RG) return cudaErrorInvalidValue;
+    const int sms = sm_count();
+    const int64_t groups = (tiles + RG - 1) / RG;
+    const unsigned grid = (unsigned)(groups < sms ? groups : sms);    // one CTA per SM
+    conv3_rows_kernel<COUT, CIN><<<grid, 192, C::SMEM, s>>>(xm, static_cast<const __nv_bfloat16*>(w), a);
     return cudaGetLastError();
 }
 
@@ -463,6 +759,14 @@ bool conv3_supported(int D, int H, int W, int cin, int cout) {
 
 cudaError_t conv3(const Conv3Args& a, const void* x, const void* w, cudaStream_t s) {
     if (!conv3_supported(a.D, a.H, a.W, a.cin, a.cout)) return cudaErrorInvalidValue;
+    // Rows of 128 voxels with 16 or 32 input channels: the persistent row kernel.
+    if (a.W % BM == 0) {
+#define AGB_ROW_CASE(CO, CI) \
+        if (a.cout == CO && a.cin == CI) return launch_conv_rows<CO, CI>(a, x, w, s);
+        AGB_ROW_CASE(16, 16) AGB_ROW_CASE(32, 16) AGB_ROW_CASE(64, 16)
+        AGB_ROW_CASE(16, 32) AGB_ROW_CASE(32, 32)
+#undef AGB_ROW_CASE
+    }
     const int kc = a.cin >= 64 ? 64 : a.cin;
 #define AGB_CONV_CASE(CO, K) \
     if (a.cout == CO && kc == K) return launch_conv<CO, K>(a, x, w, s);

@@ -97,22 +97,53 @@ __global__ void flip_kernel(const __nv_bfloat16* __restrict__ w, __nv_bfloat16* 
 }
 
 // Fine dims D, H, W (even); y is [D/2][H/2][W/2][c].
+// Eight channels (16 bytes) per thread; per channel the same FP32 sum in the
+// same order as one channel per thread would form it.
+struct Bf8 {
+    float v[8];
+};
+__device__ __forceinline__ Bf8 load8(const __nv_bfloat16* p) {
+    const uint4 u = *reinterpret_cast<const uint4*>(p);
+    const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+    Bf8 r;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w[k]));
+        r.v[2 * k] = f.x;
+        r.v[2 * k + 1] = f.y;
+    }
+    return r;
+}
+__device__ __forceinline__ void store8(__nv_bfloat16* p, const Bf8& r) {
+    uint32_t w[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const __nv_bfloat162 h = __floats2bfloat162_rn(r.v[2 * k], r.v[2 * k + 1]);
+        w[k] = *reinterpret_cast<const uint32_t*>(&h);
+    }
+    *reinterpret_cast<uint4*>(p) = make_uint4(w[0], w[1], w[2], w[3]);
+}
+
 __global__ void avgpool_kernel(const __nv_bfloat16* __restrict__ x, __nv_bfloat16* __restrict__ y, int D, int H, int W,
                                int c) {
-    const int d2 = D / 2, h2 = H / 2, w2 = W / 2;
-    const int64_t total = (int64_t)d2 * h2 * w2 * c;
+    const int d2 = D / 2, h2 = H / 2, w2 = W / 2, cq = c / 8;
+    const int64_t total = (int64_t)d2 * h2 * w2 * cq;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int ch = (int)(i % c);
-        int64_t v = i / c;
-        const int X = (int)(v % w2); v /= w2;
-        const int Y = (int)(v % h2);
-        const int Z = (int)(v / h2);
-        float s = 0.0f;
+        const int q = (int)(i % cq);
+        const int v = (int)(i / cq);                 // coarse voxel (< 2^31)
+        const int X = v % w2, Y = (v / w2) % h2, Z = v / (w2 * h2);
+        Bf8 s;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) s.v[j] = 0.0f;
         for (int k = 0; k < 8; ++k) {
             const int z = 2 * Z + (k >> 2), yy = 2 * Y + ((k >> 1) & 1), xx = 2 * X + (k & 1);
-            s += bf(x[(((int64_t)z * H + yy) * W + xx) * c + ch]);
+            const Bf8 a = load8(x + (((int64_t)z * H + yy) * W + xx) * c + q * 8);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) s.v[j] += a.v[j];
         }
-        y[i] = tobf(0.125f * s);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) s.v[j] = 0.125f * s.v[j];
+        store8(y + (int64_t)v * c + q * 8, s);
     }
 }
 
@@ -138,17 +169,19 @@ __global__ void avgpool_bwd_kernel(const __nv_bfloat16* __restrict__ dy, const _
 // y (fine) = coarse(parent) + skip.
 __global__ void upsample_add_kernel(const __nv_bfloat16* __restrict__ coarse, const __nv_bfloat16* __restrict__ skip,
                                     __nv_bfloat16* __restrict__ y, int D, int H, int W, int c) {
-    const int64_t total = (int64_t)D * H * W * c;
-    const int h2 = H / 2, w2 = W / 2;
+    const int cq = c / 8, h2 = H / 2, w2 = W / 2;
+    const int64_t total = (int64_t)D * H * W * cq;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int ch = (int)(i % c);
-        int64_t v = i / c;
-        const int xx = (int)(v % W); v /= W;
-        const int yy = (int)(v % H);
-        const int z = (int)(v / H);
-        float s = bf(coarse[(((int64_t)(z / 2) * h2 + yy / 2) * w2 + xx / 2) * c + ch]);
-        if (skip) s += bf(skip[i]);
-        y[i] = tobf(s);
+        const int q = (int)(i % cq);
+        const int v = (int)(i / cq);                 // fine voxel (< 2^31)
+        const int xx = v % W, yy = (v / W) % H, z = v / (W * H);
+        Bf8 s = load8(coarse + (((int64_t)(z / 2) * h2 + yy / 2) * w2 + xx / 2) * c + q * 8);
+        if (skip) {
+            const Bf8 k = load8(skip + (int64_t)v * c + q * 8);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) s.v[j] += k.v[j];
+        }
+        store8(y + (int64_t)v * c + q * 8, s);
     }
 }
 
@@ -198,7 +231,7 @@ void flip_weights(const __nv_bfloat16* w, __nv_bfloat16* wf, int cout, int cin, 
     flip_kernel<<<grid_for(27LL * cout * cin), 256, 0, s>>>(w, wf, cout, cin);
 }
 void avgpool2(const __nv_bfloat16* x, __nv_bfloat16* y, int D, int H, int W, int c, cudaStream_t s) {
-    avgpool_kernel<<<grid_for((int64_t)D * H * W * c / 8), 256, 0, s>>>(x, y, D, H, W, c);
+    avgpool_kernel<<<grid_for((int64_t)D * H * W * c / 64), 256, 0, s>>>(x, y, D, H, W, c);
 }
 void avgpool2_backward_add(const __nv_bfloat16* dy, const __nv_bfloat16* dskip, const __nv_bfloat16* act,
                            __nv_bfloat16* dx, int D, int H, int W, int c, cudaStream_t s) {
@@ -206,7 +239,7 @@ void avgpool2_backward_add(const __nv_bfloat16* dy, const __nv_bfloat16* dskip, 
 }
 void upsample2_add(const __nv_bfloat16* coarse, const __nv_bfloat16* skip, __nv_bfloat16* y, int D, int H, int W,
                    int c, cudaStream_t s) {
-    upsample_add_kernel<<<grid_for((int64_t)D * H * W * c), 256, 0, s>>>(coarse, skip, y, D, H, W, c);
+    upsample_add_kernel<<<grid_for((int64_t)D * H * W * c / 8), 256, 0, s>>>(coarse, skip, y, D, H, W, c);
 }
 void upsample2_backward(const __nv_bfloat16* dy, const __nv_bfloat16* act, __nv_bfloat16* dcoarse, int D, int H,
                         int W, int c, cudaStream_t s) {

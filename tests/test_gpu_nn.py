@@ -33,7 +33,11 @@ def rand(shape, seed, scale=1.0):
 
 
 CASES = [(4, 4, 32, 16, 32), (2, 4, 64, 32, 64), (4, 8, 32, 64, 128), (2, 2, 128, 128, 64),
-         (2, 2, 64, 32, 16), (2, 4, 64, 64, 32), (2, 1, 128, 16, 16), (2, 2, 128, 256, 32)]
+         (2, 2, 64, 32, 16), (2, 4, 64, 64, 32), (2, 1, 128, 16, 16), (2, 2, 128, 256, 32),
+         # the persistent row kernel (rows of 128 voxels, 16 or 32 input channels): a few tiles per
+         # CTA; several tiles per CTA (stage and accumulator rings wrap); two tiles per row
+         (3, 5, 128, 16, 32), (2, 3, 128, 32, 16), (3, 3, 128, 32, 32), (2, 3, 128, 16, 64),
+         (16, 48, 128, 16, 32), (12, 40, 128, 32, 16), (3, 4, 256, 16, 32)]
 
 
 @pytest.mark.parametrize("D,Hh,W,cin,cout", CASES)
