@@ -29,8 +29,8 @@ static_assert(sizeof(agb_param_override) == 56, "override record is 56 bytes");
 constexpr size_t kElem[25] = {8, 4, 1, 8, 8, 8, 8, 8, 8, 8, 4, 4, 4, 4, 4, 8, 8, 4, 8, 4, 4, 4, 4, 4, 4};
 
 // The overrides this engine carries, in the reference's order
-// (src/sim/snapshot.cu:75-80): the emission cap and the division quota; the
-// flash power has no counterpart here (no flash stage) and is read and ignored.
+// (OVERRIDE_FIELDS, src/sim/snapshot.cu:79-83): the emission cap, the flash
+// power and the division quota, each when it differs from canon.
 std::vector<agb_param_override> overrides(const agb_world* w) {
     std::vector<agb_param_override> out;
     auto add = [&](const char* key, double value) {
@@ -42,6 +42,7 @@ std::vector<agb_param_override> overrides(const agb_world* w) {
     };
     const double pmax = w->d.max_emit_power > 0.0 ? w->d.max_emit_power : AGB_PETROVA_MAX_POWER;
     if (pmax != AGB_PETROVA_MAX_POWER) add("PETROVA_MAX_POWER", pmax);
+    if (w->flash_power != AGB_PETROVA_FLASH_POWER) add("PETROVA_FLASH_POWER", w->flash_power);
     if (w->d.co2_mass_per_division != AGB_CO2_MASS_PER_DIVISION) add("CO2_MASS_PER_DIVISION", w->d.co2_mass_per_division);
     return out;
 }
@@ -227,6 +228,7 @@ agb_status agb_world_snapshot_load(const agb_world_desc* base, const void* data,
             return AGB_INVALID_ARGUMENT;                           // field resolution mismatch
     const char* cur = body;
     const char* end = body + body_len;
+    double flash_power = AGB_PETROVA_FLASH_POWER;
     for (int32_t i = 0; i < h.override_count; ++i) {               // overrides come first
         if (cur + sizeof(agb_param_override) > end) return AGB_INVALID_ARGUMENT;
         agb_param_override ov;
@@ -234,10 +236,12 @@ agb_status agb_world_snapshot_load(const agb_world_desc* base, const void* data,
         cur += sizeof(ov);
         if (std::strncmp(ov.key, "CO2_MASS_PER_DIVISION", sizeof(ov.key)) == 0) d.co2_mass_per_division = ov.value;
         if (std::strncmp(ov.key, "PETROVA_MAX_POWER", sizeof(ov.key)) == 0) d.max_emit_power = ov.value;
+        if (std::strncmp(ov.key, "PETROVA_FLASH_POWER", sizeof(ov.key)) == 0) flash_power = ov.value;
     }
     agb_world* w = nullptr;
     agb_status rc = agb_world_create(&d, &w);
     if (rc != AGB_OK) return rc;
+    w->flash_power = flash_power;                                   // the flash stays disarmed
     // Cells: the arrays are laid end to end; import takes one pointer per array.
     const size_t cnt = (size_t)h.cell_count;
     size_t need = 0;

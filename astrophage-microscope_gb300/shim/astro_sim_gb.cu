@@ -12,6 +12,9 @@
 //                               (src/sim/cell_store.cuh:73-106)
 //   grid_fill / grid_download / grid_brush, for a world's own fields
 //                               (src/fields/grid.cuh:91-103)
+//   taumoeba_spawn / taumoeba_download_*   (src/sim/predation.cuh:133-141)
+//   snapshot_to_bytes / snapshot_from_bytes / snapshot_save / snapshot_load /
+//   snapshot_state_hash         (src/sim/snapshot.h:20-37)
 //
 // The engine's world lives behind the reference's World object, and the World's
 // public members that callers read or set between ticks are kept in step:
@@ -30,24 +33,33 @@
 //     diffusivity, ambient, deposit scale, Robin coefficient, substeps, bc);
 //     their device pointers stay null, because the engine ping-pongs its field
 //     buffers inside the tick: read and write them with grid_download/grid_fill.
+//   * the predator store mirrors its count, capacity and next id; its device
+//     pointers stay null (read predators with taumoeba_download_*).
 // Not provided: the stage functions (motion_step, thermal_step, ...) and the
 // lower-level stores (hash_*, grid_create/diffuse, cell_store_create/destroy/
-// compact/sample, taumoeba_*, snapshot_*, scenario_*): the engine runs the whole
-// tick as one captured graph and owns its stores.
+// compact/sample, taumoeba_create/destroy/compact): the engine runs the whole
+// tick as one captured graph and owns its stores. The reference's own
+// scenario loader and acceptance code (src/sim/scenario.cpp, accept.cpp) and
+// tools/headless.cpp compile against these unchanged.
+#include <cstdio>
 #include <cstring>
 #include <map>
 #include <mutex>
 #include <vector>
 
 #include "agb.h"
+#include "contracts/snapshot_v1.h"
 #include "core/canon_generated.h"
 #include "sim/cell_store.cuh"
+#include "sim/predation.cuh"
+#include "sim/snapshot.h"
 #include "sim/world.cuh"
 
 namespace {
 
 struct Binding {
     agb_world* h = nullptr;
+    int32_t tau_capacity = 0;
     double physics = 1.0, biology = 1.0;   // last rates pushed
     agb_light light{};                     // last light pushed
     bool flash = false;
@@ -66,6 +78,7 @@ std::mutex g_mu;
 std::map<const void*, Binding*> g_by_world;    // World* -> binding
 std::map<const void*, Binding*> g_by_cells;    // &World::cells -> binding
 std::map<const void*, GridKey> g_by_grid;      // &World::fields.<field> -> binding, field
+std::map<const void*, Binding*> g_by_tau;       // &World::taumoeba -> binding
 
 astro::fields::Grid2D* world_grid(astro::sim::World& w, int32_t f) {
     switch (f) {
@@ -123,6 +136,17 @@ void pull_cells(astro::sim::World& w, agb_world* h) {
     w.cells.capacity = v.capacity;
 }
 
+// The predator store's count, capacity and next id (predation.cuh:85-106).
+void pull_tau(astro::sim::World& w, agb_world* h, int32_t capacity) {
+    agb_taumoeba none{};
+    int32_t n = 0;
+    uint64_t nid = 1;
+    if (agb_world_export_taumoeba(h, &none, 0, &n, &nid, nullptr) != AGB_OK) return;
+    w.taumoeba.count = n;
+    w.taumoeba.capacity = capacity;
+    w.taumoeba.next_id = nid;
+}
+
 // The lifecycle counters the reference keeps on the World (world.cuh:110-120).
 void pull_counters(astro::sim::World& w, agb_world* h) {
     int64_t c[4] = {};
@@ -176,7 +200,10 @@ void push_knobs(astro::sim::World& w, Binding* b) {
 
 namespace astro::sim {
 
-Error world_create(World& w, const WorldDesc& d) {
+namespace {
+
+// world_create's descriptor (step.cu:9-78) in the engine's terms.
+agb_world_desc engine_desc(const WorldDesc& d) {
     agb_world_desc a;
     agb_world_desc_default(&a);
     a.chamber_w = d.chamber.w;
@@ -208,10 +235,13 @@ Error world_create(World& w, const WorldDesc& d) {
         a.grid[AGB_FIELD_TEMPERATURE].face_value[k] = m.ambient_temp;
         a.grid[AGB_FIELD_CO2].face_value[k] = d.co2_init;
     }
-    agb_world* h = nullptr;
-    const agb_status rc = agb_world_create(&a, &h);
-    if (rc != AGB_OK) return status_error(rc, "agb_world_create");
+    return a;
+}
+
+// Ties the engine world h to w and mirrors its state into w's members.
+void bind(World& w, const WorldDesc& d, const agb_world_desc& a, agb_world* h) {
     Binding* b = new Binding();
+    b->tau_capacity = a.tau_capacity > 0 ? a.tau_capacity : canon::DEFAULT_TAUMOEBA;
     b->h = h;
     b->quota = a.co2_mass_per_division;
     b->max_power = a.max_emit_power;
@@ -224,6 +254,7 @@ Error world_create(World& w, const WorldDesc& d) {
         std::lock_guard<std::mutex> lock(g_mu);
         g_by_world[&w] = b;
         g_by_cells[&w.cells] = b;
+        g_by_tau[&w.taumoeba] = b;
         for (int32_t f = 0; f < AGB_FIELD_COUNT; ++f) g_by_grid[world_grid(w, f)] = GridKey{b, f};
     }
     w.chamber = d.chamber;
@@ -235,6 +266,17 @@ Error world_create(World& w, const WorldDesc& d) {
     w.biology_rate = 1.0;
     w.cells.next_id = 1;
     pull_cells(w, h);
+    pull_tau(w, h, b->tau_capacity);
+}
+
+}  // namespace
+
+Error world_create(World& w, const WorldDesc& d) {
+    const agb_world_desc a = engine_desc(d);
+    agb_world* h = nullptr;
+    const agb_status rc = agb_world_create(&a, &h);
+    if (rc != AGB_OK) return status_error(rc, "agb_world_create");
+    bind(w, d, a, h);
     return ok();
 }
 
@@ -247,6 +289,7 @@ void world_destroy(World& w) {
             b = it->second;
             g_by_world.erase(it);
             g_by_cells.erase(&w.cells);
+            g_by_tau.erase(&w.taumoeba);
             for (int32_t f = 0; f < AGB_FIELD_COUNT; ++f) g_by_grid.erase(world_grid(w, f));
         }
     }
@@ -264,6 +307,7 @@ void world_step(World& w) {
     agb_world_step_graph(b->h, 1, nullptr);
     pull_cells(w, b->h);
     pull_counters(w, b->h);
+    pull_tau(w, b->h, b->tau_capacity);
     ++w.tick;                                          // the clock as step.cu advances it
     w.sim_time_s += canon::DT_PHYSICS * w.physics_rate;
 }
@@ -385,6 +429,139 @@ Error cell_store_download_energy(const CellStore& s, double* energy, int32_t max
     const double* src[1] = {s.view.energy};
     double* dst[1] = {energy};
     return copy_columns(src, dst, 1, s.count, max_count, "download energy");
+}
+
+namespace {
+
+// One predator array, copied out through the engine (taumoeba_download_*).
+template <class T>
+Error tau_column(const TaumoebaStore& s, T* out, int32_t max_count, T* agb_taumoeba::* col, const char* what) {
+    Binding* b = binding_of(&s, g_by_tau);
+    if (!b) return fail(Status::InvalidArgument, "predator store not created by the engine");
+    const int32_t n = s.count < max_count ? s.count : max_count;
+    if (n <= 0) return ok();
+    agb_taumoeba dst{};
+    dst.*col = out;
+    int32_t cnt = 0;
+    uint64_t nid = 0;
+    return status_error(agb_world_export_taumoeba(b->h, &dst, n, &cnt, &nid, nullptr), what);
+}
+
+}  // namespace
+
+Error taumoeba_spawn(TaumoebaStore& s, int32_t count, const Chamber& c, uint64_t seed) {
+    (void)c;                                           // the engine's world carries the chamber
+    Binding* b = binding_of(&s, g_by_tau);
+    if (!b) return fail(Status::InvalidArgument, "predator store not created by the engine");
+    if (count <= 0) return ok();
+    const agb_status rc = agb_world_spawn_taumoeba(b->h, count, seed, nullptr);
+    if (rc != AGB_OK) return status_error(rc, "agb_world_spawn_taumoeba");
+    agb_taumoeba none{};
+    int32_t n = 0;
+    uint64_t nid = 1;
+    if (agb_world_export_taumoeba(b->h, &none, 0, &n, &nid, nullptr) == AGB_OK) {
+        s.count = n;
+        s.next_id = nid;
+    }
+    return ok();
+}
+
+Error taumoeba_download_positions(const TaumoebaStore& s, double* x, double* y, double* z, int32_t max_count) {
+    if (Error e = tau_column(s, x, max_count, &agb_taumoeba::x, "taumoeba positions")) return e;
+    if (Error e = tau_column(s, y, max_count, &agb_taumoeba::y, "taumoeba positions")) return e;
+    return tau_column(s, z, max_count, &agb_taumoeba::z, "taumoeba positions");
+}
+Error taumoeba_download_biomass(const TaumoebaStore& s, double* biomass, int32_t max_count) {
+    return tau_column(s, biomass, max_count, &agb_taumoeba::biomass, "taumoeba biomass");
+}
+Error taumoeba_download_tolerance(const TaumoebaStore& s, float* tolerance, int32_t max_count) {
+    return tau_column(s, tolerance, max_count, &agb_taumoeba::tolerance, "taumoeba tolerance");
+}
+Error taumoeba_download_generation(const TaumoebaStore& s, uint32_t* generation, int32_t max_count) {
+    return tau_column(s, generation, max_count, &agb_taumoeba::generation, "taumoeba generation");
+}
+Error taumoeba_download_flags(const TaumoebaStore& s, uint32_t* flags, int32_t max_count) {
+    return tau_column(s, flags, max_count, &agb_taumoeba::flags, "taumoeba flags");
+}
+
+// Snapshots (snapshot.cu:134-262): the engine writes and reads the same file
+// layout; the World's knobs go to the engine first so the bytes carry them.
+Error snapshot_to_bytes(const World& w, const char* scenario_id, std::vector<char>& out) {
+    Binding* b = binding_of(&w, g_by_world);
+    if (!b) return fail(Status::InvalidArgument, "world not created by the engine");
+    push_knobs(const_cast<World&>(w), b);
+    int64_t size = 0;
+    agb_status rc = agb_world_snapshot_save(b->h, scenario_id, nullptr, 0, &size, nullptr);
+    if (rc != AGB_OK) return status_error(rc, "agb_world_snapshot_save");
+    out.resize((size_t)size);
+    rc = agb_world_snapshot_save(b->h, scenario_id, out.data(), size, &size, nullptr);
+    return status_error(rc, "agb_world_snapshot_save");
+}
+
+Error snapshot_from_bytes(const char* data, size_t n, World& w) {
+    if (n < sizeof(contract::SnapshotHeader)) return fail(Status::FileIoError, "snapshot: too small");
+    contract::SnapshotHeader hd{};
+    std::memcpy(&hd, data, sizeof(hd));
+    // The world is created from the header's chamber, capacities and seed with
+    // the default motion configuration, as the reference does.
+    WorldDesc d;
+    d.chamber = Chamber{hd.chamber_w, hd.chamber_h, hd.chamber_d};
+    d.capacity = hd.cell_capacity;
+    d.tau_capacity = hd.taumoeba_capacity;
+    d.seed = hd.seed;
+    if (binding_of(&w, g_by_world)) world_destroy(w);
+    const agb_world_desc a = engine_desc(d);
+    agb_world* h = nullptr;
+    const agb_status rc = agb_world_snapshot_load(&a, data, (int64_t)n, &h);
+    if (rc != AGB_OK) return status_error(rc, "agb_world_snapshot_load");
+    bind(w, d, a, h);
+    Binding* b = binding_of(&w, g_by_world);
+    // Overrides come first in the body (OVERRIDE_FIELDS, snapshot.cu:79-83).
+    const char* cur = data + sizeof(hd);
+    for (int32_t i = 0; i < hd.override_count && cur + sizeof(contract::ParamOverride) <= data + n; ++i) {
+        contract::ParamOverride ov{};
+        std::memcpy(&ov, cur, sizeof(ov));
+        cur += sizeof(ov);
+        if (std::strncmp(ov.key, "PETROVA_MAX_POWER", sizeof(ov.key)) == 0) w.petrova_max_power = b->max_power = ov.value;
+        if (std::strncmp(ov.key, "PETROVA_FLASH_POWER", sizeof(ov.key)) == 0) w.petrova_flash_power = b->flash_power = ov.value;
+        if (std::strncmp(ov.key, "CO2_MASS_PER_DIVISION", sizeof(ov.key)) == 0) w.co2_mass_per_division = b->quota = ov.value;
+    }
+    w.seed = hd.seed;
+    w.tick = hd.tick;
+    w.sim_time_s = hd.sim_time_s;
+    w.physics_rate = b->physics = hd.physics_rate;
+    w.biology_rate = b->biology = hd.biology_rate;
+    w.non_canon_run = hd.non_canon_run != 0;
+    w.cells.next_id = hd.next_cell_id;
+    return ok();
+}
+
+Error snapshot_save(const World& w, const char* path, const char* scenario_id) {
+    std::vector<char> bytes;
+    if (Error e = snapshot_to_bytes(w, scenario_id, bytes)) return e;
+    std::FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(Status::FileIoError, "snapshot: cannot open file for write");
+    const bool wrote = std::fwrite(bytes.data(), 1, bytes.size(), f) == bytes.size();
+    std::fclose(f);
+    return wrote ? ok() : fail(Status::FileIoError, "snapshot: write failed");
+}
+
+Error snapshot_load(const char* path, World& w) {
+    std::FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(Status::FileIoError, "snapshot: cannot open file for read");
+    std::vector<char> all;
+    char buf[65536];
+    size_t r = 0;
+    while ((r = std::fread(buf, 1, sizeof(buf), f)) > 0) all.insert(all.end(), buf, buf + r);
+    std::fclose(f);
+    return snapshot_from_bytes(all.data(), all.size(), w);
+}
+
+Error snapshot_state_hash(const World& w, uint64_t& hash_out) {
+    Binding* b = binding_of(&w, g_by_world);
+    if (!b) return fail(Status::InvalidArgument, "world not created by the engine");
+    push_knobs(const_cast<World&>(w), b);
+    return status_error(agb_world_state_hash(b->h, &hash_out, nullptr), "agb_world_state_hash");
 }
 
 }  // namespace astro::sim

@@ -7,10 +7,13 @@
 # The shim is compiled against the reference's headers, read in place: it needs
 # a reference checkout, and the engine (libagb.so, built by build.py) beside it.
 #
-# Usage: sh build_shim.sh REFERENCE_ROOT [OUT_DIR [PROGRAM.cu ...]]
+# Usage: sh build_shim.sh REFERENCE_ROOT [OUT_DIR [PROGRAM ...]]
 #    or: AGB_REFERENCE_DIR=REFERENCE_ROOT sh build_shim.sh
 # Writes OUT_DIR/libastro_sim_gb.so (OUT_DIR defaults to this folder) and one
-# executable per PROGRAM.cu, named after it, in OUT_DIR.
+# executable per PROGRAM, named after its first source, in OUT_DIR. A PROGRAM
+# is one source file or several joined by colons (main.cpp:more.cpp), e.g. the
+# reference's headless runner with its scenario loader and acceptance code:
+#   REF/tools/headless.cpp:REF/src/sim/scenario.cpp:REF/src/sim/accept.cpp
 set -eu
 REF="${1:-${AGB_REFERENCE_DIR:-}}"
 [ -n "$REF" ] || { echo "usage: build_shim.sh REFERENCE_ROOT [OUT_DIR [PROGRAM.cu ...]]" >&2; exit 2; }
@@ -29,8 +32,10 @@ $NVCC $ARCH $FLAGS -shared "$HERE/astro_sim_gb.cu" -o "$OUT/libastro_sim_gb.so" 
     -L"$PKG" -lagb -Xlinker -rpath -Xlinker "$PKG"
 pids=""
 for prog in "$@"; do
-    name="$(basename "$prog" .cu)"
-    $NVCC $ARCH $FLAGS "$prog" -o "$OUT/$name" -L"$OUT" -lastro_sim_gb -L"$PKG" -lagb \
+    srcs="$(echo "$prog" | tr ':' ' ')"
+    first="${prog%%:*}"
+    name="$(basename "$(basename "$first" .cu)" .cpp)"
+    $NVCC $ARCH $FLAGS $srcs -o "$OUT/$name" -L"$OUT" -lastro_sim_gb -L"$PKG" -lagb \
         -Xlinker -rpath -Xlinker "$OUT" -Xlinker -rpath -Xlinker "$PKG" &
     pids="$pids $!"
 done

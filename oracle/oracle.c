@@ -1879,9 +1879,12 @@ int64_t orc_world_snapshot(orc_world* w, const char* scenario_id, char* out, int
     size_t sz[25]; void* p[25];
     soa_sizes(sz); soa_ptrs(&w->c, p);
     const double pmax = w->d.max_emit_power > 0.0 ? w->d.max_emit_power : AGB_PETROVA_MAX_POWER;
-    const int ov_power = pmax != AGB_PETROVA_MAX_POWER;                    /* snapshot.cu:75-80 order */
-    const int ov_quota = w->d.co2_mass_per_division != AGB_CO2_MASS_PER_DIVISION;
-    const int has_override = ov_power + ov_quota;
+    /* OVERRIDE_FIELDS order, snapshot.cu:79-83: emission cap, flash power, division quota. */
+    const char* const keys[3] = {"PETROVA_MAX_POWER", "PETROVA_FLASH_POWER", "CO2_MASS_PER_DIVISION"};
+    const double vals[3] = {pmax, w->flash_power, w->d.co2_mass_per_division};
+    const int on[3] = {pmax != AGB_PETROVA_MAX_POWER, w->flash_power != AGB_PETROVA_FLASH_POWER,
+                       w->d.co2_mass_per_division != AGB_CO2_MASS_PER_DIVISION};
+    const int has_override = on[0] + on[1] + on[2];
     int64_t body = (int64_t)has_override * (int64_t)sizeof(agb_param_override);
     for (int k = 0; k < 25; ++k) body += (int64_t)sz[k] * w->count;
     for (int k = 0; k < 20; ++k) body += (int64_t)TAU_SZ[k] * w->tau_count;
@@ -1890,12 +1893,12 @@ int64_t orc_world_snapshot(orc_world* w, const char* scenario_id, char* out, int
     const int64_t total = (int64_t)sizeof(agb_snapshot_header) + body;
     if (!out || cap < total) return total;
     char* q = out + sizeof(agb_snapshot_header);
-    for (int o = 0; o < 2; ++o) {
-        if (!(o == 0 ? ov_power : ov_quota)) continue;
+    for (int o = 0; o < 3; ++o) {
+        if (!on[o]) continue;
         agb_param_override ov;
         memset(&ov, 0, sizeof(ov));
-        strncpy(ov.key, o == 0 ? "PETROVA_MAX_POWER" : "CO2_MASS_PER_DIVISION", sizeof(ov.key) - 1);
-        ov.value = o == 0 ? pmax : w->d.co2_mass_per_division;
+        strncpy(ov.key, keys[o], sizeof(ov.key) - 1);
+        ov.value = vals[o];
         memcpy(q, &ov, sizeof(ov));
         q += sizeof(ov);
     }
