@@ -134,6 +134,10 @@ void pull_cells(astro::sim::World& w, agb_world* h) {
     std::memcpy(&w.cells.view, &v, sizeof(v));
     w.cells.count = v.count;
     w.cells.capacity = v.capacity;
+    agb_cells none{};                                  // no arrays: count and next id only
+    int32_t cnt = 0;
+    uint64_t nid = 0;
+    if (agb_world_export_cells(h, &none, 0, &cnt, &nid, nullptr) == AGB_OK) w.cells.next_id = nid;
 }
 
 // The predator store's count, capacity and next id (predation.cuh:85-106).
