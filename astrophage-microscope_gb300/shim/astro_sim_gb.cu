@@ -246,6 +246,8 @@ agb_world_desc engine_desc(const WorldDesc& d) {
 void bind(World& w, const WorldDesc& d, const agb_world_desc& a, agb_world* h) {
     Binding* b = new Binding();
     b->tau_capacity = a.tau_capacity > 0 ? a.tau_capacity : canon::DEFAULT_TAUMOEBA;
+    b->light = a.light;                                // what the engine starts with
+    b->flash_power = canon::PETROVA_FLASH_POWER;
     b->h = h;
     b->quota = a.co2_mass_per_division;
     b->max_power = a.max_emit_power;
