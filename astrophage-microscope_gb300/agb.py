@@ -123,6 +123,13 @@ class Taumoeba(C.Structure):
                 ("target", C.POINTER(C.c_int32))]
 
 
+class Mirror(C.Structure):
+    """agb_mirror: a world's host-visible state after a tick, read in one go."""
+    _fields_ = [("cells", Cells), ("next_id", C.c_uint64), ("divisions_this_window", C.c_int64),
+                ("deaths_total", C.c_int64), ("dead_slots_prev", C.c_int64), ("error", C.c_uint32),
+                ("tau_count", C.c_int32), ("tau_next_id", C.c_uint64)]
+
+
 class Spawn(C.Structure):
     _fields_ = [("count", C.c_int32), ("placement", C.c_int32), ("charge_dist", C.c_int32),
                 ("awake", C.c_int32), ("place_x", C.c_double), ("place_y", C.c_double),
@@ -329,6 +336,7 @@ def load(path=LIB_PATH):
         "agb_world_set_boundary": (I32, [P, I32, C.POINTER(I32), C.POINTER(C.c_double)]),
         "agb_world_set_rates": (I32, [P, C.c_double, C.c_double]),
         "agb_world_set_overrides": (I32, [P, C.c_double, C.c_double]),
+        "agb_world_mirror": (I32, [P, C.POINTER(Mirror), P]),
         "agb_world_import_cells": (I32, [P, C.POINTER(Cells), I32, U64, P]),
         "agb_world_export_cells": (I32, [P, C.POINTER(Cells), I32, C.POINTER(I32), C.POINTER(U64), P]),
         "agb_world_device_cells": (I32, [P, C.POINTER(Cells)]),
@@ -409,6 +417,7 @@ def exported_symbols():
     return ["agb_world_desc_default", "agb_status_str", "agb_last_error", "agb_device_info",
             "agb_world_create", "agb_world_destroy", "agb_world_spawn", "agb_world_spawn_seeded", "agb_world_set_charge",
             "agb_world_set_boundary", "agb_world_set_rates", "agb_world_set_overrides",
+            "agb_world_mirror",
             "agb_world_import_cells",
             "agb_world_export_cells", "agb_world_device_cells", "agb_world_step_host", "agb_world_count",
             "agb_world_import_field", "agb_world_export_field", "agb_world_export_deposit",
@@ -488,6 +497,16 @@ class World:
         b = (C.c_int32 * 6)(*[int(v) for v in bc])
         f = (C.c_double * 6)(*[float(v) for v in face_value])
         self._check(self.lib.agb_world_set_boundary(self.h, field, b, f), "set_boundary")
+
+    def mirror(self, stream=None):
+        """agb_world_mirror as a dict: count, capacity, next id, counters,
+        predator count and next id, and the cell store's device pointers."""
+        m = Mirror()
+        self._check(self.lib.agb_world_mirror(self.h, C.byref(m), _st(stream)), "mirror")
+        out = {k: getattr(m, k) for k, _t in Mirror._fields_ if k != "cells"}
+        out["count"], out["capacity"] = m.cells.count, m.cells.capacity
+        out["pointers"] = [C.cast(getattr(m.cells, n), C.c_void_p).value for n, _t in CELL_FIELDS]
+        return out
 
     def set_rates(self, physics_rate, biology_rate):
         """The clock rates as assigned to the World directly (unclamped)."""

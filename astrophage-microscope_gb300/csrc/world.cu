@@ -1643,6 +1643,29 @@ agb_status agb_world_export_forces(agb_world* w, float* fx, float* fy, float* fz
     return AGB_OK;
 }
 
+agb_status agb_world_mirror(agb_world* w, agb_mirror* out, agb_stream s) {
+    if (!w || !out) return AGB_INVALID_ARGUMENT;
+    DevState st;
+    TauState ts{};
+    AGB_CUDA(w, cudaMemcpyAsync(&st, w->S, sizeof(DevState), cudaMemcpyDeviceToHost, s));
+    if (w->tS) AGB_CUDA(w, cudaMemcpyAsync(&ts, w->tS, sizeof(TauState), cudaMemcpyDeviceToHost, s));
+    AGB_CUDA(w, cudaStreamSynchronize(s));
+    const SoA& v = st.cur;
+    agb_cells c = {v.id, v.flags, v.death_cause, v.x, v.y, v.z, v.vx, v.vy, v.vz, v.energy,
+                   v.temp_cell, v.emit_power, v.dir_x, v.dir_y, v.dir_z, v.biomass, v.co2_held,
+                   v.age_s, v.rng_state, v.taxis_memory, v.run_timer, v.t_local, v.irradiance,
+                   v.co2_local, v.n2_local, st.count, w->c.capacity};
+    out->cells = c;
+    out->next_id = st.next_id;
+    out->divisions_this_window = st.divisions_this_window;
+    out->deaths_total = st.deaths_total;
+    out->dead_slots_prev = st.dead_slots_prev;
+    out->error = st.error;
+    out->tau_count = w->tS ? ts.count : 0;
+    out->tau_next_id = w->tS ? ts.next_id : 1;
+    return AGB_OK;
+}
+
 agb_status agb_world_counters(agb_world* w, int64_t out[4], agb_stream s) {
     if (!w || !out) return AGB_INVALID_ARGUMENT;
     DevState st;

@@ -23,9 +23,10 @@
 //     irradiance, the flash arming, the live overrides (co2_mass_per_division,
 //     petrova_max_power) and each field's boundary kind (Grid2D::bc) go to the
 //     engine when they changed since the last tick;
-//   * after create, spawn and every tick, the cell store's view (its 25 device
-//     SoA pointers, count and capacity), count and next id, and the death and
-//     division counters come from it, and the tick and the simulated time
+//   * after create, spawn and every tick (one synchronisation), the cell
+//     store's view (its 25 device SoA pointers, count and capacity), count and
+//     next id, and the death and division counters come from it, and the tick
+//     and the simulated time
 //     advance as the reference advances them. The view points into the
 //     engine's device arrays (callers may read and write them between ticks)
 //     and stays valid until the next tick (compaction swaps them);
@@ -151,13 +152,20 @@ void pull_tau(astro::sim::World& w, agb_world* h, int32_t capacity) {
     w.taumoeba.next_id = nid;
 }
 
-// The lifecycle counters the reference keeps on the World (world.cuh:110-120).
-void pull_counters(astro::sim::World& w, agb_world* h) {
-    int64_t c[4] = {};
-    if (agb_world_counters(h, c, nullptr) != AGB_OK) return;
-    w.divisions_this_window = (int32_t)c[0];
-    w.deaths_total = c[1];
-    w.dead_slots_prev = (int32_t)c[2];
+// Everything world_step refreshes, with one synchronisation (agb_world_mirror).
+void pull_all(astro::sim::World& w, Binding* b) {
+    agb_mirror m{};
+    if (agb_world_mirror(b->h, &m, nullptr) != AGB_OK) return;
+    std::memcpy(&w.cells.view, &m.cells, sizeof(m.cells));
+    w.cells.count = m.cells.count;
+    w.cells.capacity = m.cells.capacity;
+    w.cells.next_id = m.next_id;
+    w.divisions_this_window = (int32_t)m.divisions_this_window;
+    w.deaths_total = m.deaths_total;
+    w.dead_slots_prev = (int32_t)m.dead_slots_prev;
+    w.taumoeba.count = m.tau_count;
+    w.taumoeba.capacity = b->tau_capacity;
+    w.taumoeba.next_id = m.tau_next_id;
 }
 
 // The World's knobs that callers set by assignment, pushed when they changed.
@@ -311,9 +319,7 @@ void world_step(World& w) {
     if (!b) return;
     push_knobs(w, b);
     agb_world_step_graph(b->h, 1, nullptr);
-    pull_cells(w, b->h);
-    pull_counters(w, b->h);
-    pull_tau(w, b->h, b->tau_capacity);
+    pull_all(w, b);
     ++w.tick;                                          // the clock as step.cu advances it
     w.sim_time_s += canon::DT_PHYSICS * w.physics_rate;
 }

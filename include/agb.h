@@ -527,6 +527,24 @@ agb_status agb_world_export_forces(agb_world* w, float* fx, float* fy, float* fz
  * device error word}. Syncs. */
 agb_status agb_world_counters(agb_world* w, int64_t out[4], agb_stream s);
 
+/* What a host-side mirror of the world needs after a tick (the reference's
+ * World members that callers read between ticks, src/sim/world.cuh:110-128 and
+ * cell_store.cuh:36-43), read with one synchronisation: the cell store's device
+ * view with count and capacity (as agb_world_device_cells), the next cell id,
+ * the lifecycle counters and error word (as agb_world_counters), and the
+ * predator count and next id. */
+typedef struct agb_mirror {
+    agb_cells cells;
+    uint64_t next_id;
+    int64_t divisions_this_window;
+    int64_t deaths_total;
+    int64_t dead_slots_prev;
+    uint32_t error;
+    int32_t tau_count;
+    uint64_t tau_next_id;
+} agb_mirror;
+agb_status agb_world_mirror(agb_world* w, agb_mirror* out, agb_stream s);
+
 /* fnv1a64 (contracts/snapshot_v1.h:57-61): h = (h ^ byte) * 1099511628211,
  * starting from h (AGB_FNV1A64_OFFSET for a fresh hash). */
 uint64_t agb_fnv1a64(const void* data, uint64_t n, uint64_t h);

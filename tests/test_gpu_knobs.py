@@ -181,3 +181,27 @@ def test_set_overrides_mid_run_reach_replayed_graphs():
     assert not np.array_equal(x["co2_held"], y["co2_held"]) or x.n != y.n   # the halved quota took effect
     for w in (a, b, ctl):
         w.close()
+
+
+def test_mirror_equals_the_separate_reads():
+    """agb_world_mirror (one synchronisation) returns what the separate calls
+    return: count, capacity, next id, counters, predators, device pointers."""
+    # At 3e8 a cell banks ~9e-15 kg of CO2 a tick: divisions from the third tick.
+    d = small_desc(co2_init=CO2_SAT, contact_enabled=0, adhesion_enabled=0, biology_rate=3.0e8, capacity=16000)
+    d.tau_capacity = 64
+    w = populated(d, n=1000)
+    w.spawn_taumoeba(20, 7)
+    for _ in range(8):
+        w.step(1, graph=True)
+        m = w.mirror()
+        cells, nid = w.export_cells()
+        tau, tnid = w.export_taumoeba()
+        c = w.counters()
+        assert m["count"] == w.count() == cells.n
+        assert m["capacity"] == 16000
+        assert m["next_id"] == nid
+        assert (m["divisions_this_window"], m["deaths_total"], m["dead_slots_prev"], m["error"]) == tuple(c)
+        assert m["tau_count"] == tau.n == 20 and m["tau_next_id"] == tnid
+        assert all(p for p in m["pointers"])
+    assert w.count() > 1000                          # divisions happened, so next id moved
+    w.close()
