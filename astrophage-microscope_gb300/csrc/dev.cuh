@@ -98,6 +98,8 @@ struct DevState {
     uint32_t fin_count;      // CTAs of the division pass that have finished (the last one finalises)
     uint32_t scan_tile;      // next tile of the single-pass scan
     uint32_t scan_done;      // CTAs of the single-pass scan that have finished (the last one resets)
+    uint32_t t_deposited;    // 1 when a thermal substep may have left heat in the temperature deposits
+    uint32_t t_flush_fin;    // CTAs of the temperature flush that have finished (the last one clears t_deposited)
 };
 
 // Immutable per-world constants, passed by value.

@@ -138,6 +138,7 @@ __device__ __forceinline__ void thermal_kernel_body(DevState* S, const Ctx& c, c
     const SoA v = S->cur;
     const int32_t n = S->count;
     const GridDev T = c.g[AGB_FIELD_TEMPERATURE];
+    bool deposited = false;
     AGB_FOR_CELLS_B(i, blk, n) {
         const uint32_t flags = v.flags[i];
         if (!(flags & AGB_FLAG_OCCUPIED)) continue;
@@ -168,12 +169,16 @@ __device__ __forceinline__ void thermal_kernel_body(DevState* S, const Ctx& c, c
         }
         v.energy[i] = En;
         deposit_fixed(&T.deposit[idx], to_fixed_f(amount, T.scale_f));
+        deposited = true;
         if (dkey(En) <= dkey(0.0)) {                     // starved
             v.flags[i] = nf & ~AGB_FLAG_ALIVE;
             v.death_cause[i] = AGB_DEATH_STARVED;
             v.emit_power[i] = 0.0f;
         }
     }
+    // Only awake, living cells exchange heat; when none did, the flush that
+    // follows has nothing to fold in (flush_by_cells_kernel_body skips it).
+    if (__syncthreads_or(deposited) && threadIdx.x == 0) S->t_deposited = 1u;
 }
 
 __global__ void __launch_bounds__(256) thermal_kernel(DevState* S, Ctx c, TickParams p) {

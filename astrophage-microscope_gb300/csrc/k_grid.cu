@@ -342,8 +342,14 @@ __global__ void __launch_bounds__(256) ftcs3d_tma_batch(const FtcsChamber* __res
 // result equals the reference's dense flush over all voxels (a voxel without a
 // depositing cell holds zero). Optionally also zeroes a per-voxel demand
 // accumulator of the same grid (the CO2 rationing buffer).
+// The temperature flush (`gated`) is skipped while no cell has deposited heat
+// since the last one (thermal_kernel_body raises S->t_deposited): with every
+// deposit word zero the dense flush it replaces changes nothing either. All
+// CTAs read the flag before any clears it: each counts itself done after its
+// read, and the last one to finish clears the flag and the count.
 __device__ __forceinline__ void flush_by_cells_kernel_body(DevState* S, const GridDev& g, unsigned long long* demand,
-                                                           Blk blk) {
+                                                           bool gated, Blk blk) {
+    if (gated && *(volatile const uint32_t*)&S->t_deposited == 0u) return;   // block-uniform
     const SoA v = S->cur;
     const int32_t n = S->count;
     AGB_FOR_CELLS_B(i, blk, n) {
@@ -354,14 +360,20 @@ __device__ __forceinline__ void flush_by_cells_kernel_body(DevState* S, const Gr
             g.value[idx] = fa(g.value[idx], fixed_to_f((long long)raw, g.inv_scale_f, g.inv_scale_lo, g.scale));
         if (demand) demand[idx] = 0ull;
     }
+    if (!gated) return;
+    __syncthreads();
+    if (threadIdx.x == 0 && atomicAdd(&S->t_flush_fin, 1u) == (uint32_t)blk.n - 1u) {
+        S->t_deposited = 0u;
+        S->t_flush_fin = 0u;
+    }
 }
 
-__global__ void flush_by_cells_kernel(DevState* S, GridDev g, unsigned long long* demand) {
+__global__ void flush_by_cells_kernel(DevState* S, GridDev g, unsigned long long* demand, int gated) {
     pdl_wait();
-    flush_by_cells_kernel_body(S, g, demand, grid_blk());
+    flush_by_cells_kernel_body(S, g, demand, gated != 0, grid_blk());
 }
 
-AGB_BATCHED(flush_batch, 256, flush_by_cells_kernel_body(a.S, a.g, nullptr, blk))
+AGB_BATCHED(flush_batch, 256, flush_by_cells_kernel_body(a.S, a.g, nullptr, true, blk))
 
 }  // namespace
 
@@ -541,8 +553,8 @@ void launch_ftcs_batch(const FtcsChamber* tab, int32_t nch, int32_t nx, int32_t 
 }
 
 void launch_flush_by_cells(DevState* S, GridDev g, unsigned long long* demand, int32_t grid_blocks,
-                           cudaStream_t s) {
-    launch_k(flush_by_cells_kernel, grid_blocks, 256, 0, s, S, g, demand);
+                           cudaStream_t s, bool temperature) {
+    launch_k(flush_by_cells_kernel, grid_blocks, 256, 0, s, S, g, demand, temperature ? 1 : 0);
 }
 
 }  // namespace agb

@@ -54,8 +54,10 @@ void launch_ftcs_batch(const FtcsChamber* tab, int32_t nch, int32_t nx, int32_t 
                        const FtcsPlan& plan, cudaStream_t s);
 // Fold deposits into the field for the voxels cells sit in (flush_kernel,
 // src/fields/diffuse.cu:51-60, restricted to voxels that can hold a deposit).
+// `temperature`: the temperature grid's flush, skipped on the device when no
+// thermal substep has deposited heat since the previous one.
 void launch_flush_by_cells(DevState* S, GridDev g, unsigned long long* demand_to_clear,
-                           int32_t grid_blocks, cudaStream_t s);
+                           int32_t grid_blocks, cudaStream_t s, bool temperature);
 
 // Spatial hash (k_hash.cu)
 void hash_build(DevState* S, const HashDev& h, int32_t capacity, uint32_t* sort_keys_alt,

@@ -266,7 +266,7 @@ void stage_thermal(agb_world* w, cudaStream_t s) {   // thermal_step, src/sim/th
         refresh_grid_ptrs(w);
         if (w->d.thermal_enabled) {
             launch_thermal(w->S, w->c, w->tp, w->blocks, s);
-            launch_flush_by_cells(w->S, w->c.g[AGB_FIELD_TEMPERATURE], nullptr, w->blocks, s);
+            launch_flush_by_cells(w->S, w->c.g[AGB_FIELD_TEMPERATURE], nullptr, w->blocks, s, true);
         }
         ftcs(w, AGB_FIELD_TEMPERATURE, w->tp.t_coeff, s);
     }
@@ -366,7 +366,7 @@ void tick_once(agb_world* w, cudaStream_t s) {
         refresh_grid_ptrs(w);
         launch_thermal(w->S, w->c, w->tp, w->blocks, s1);
         if (k + 1 == nsub) break;
-        launch_flush_by_cells(w->S, w->c.g[AGB_FIELD_TEMPERATURE], nullptr, w->blocks, s1);
+        launch_flush_by_cells(w->S, w->c.g[AGB_FIELD_TEMPERATURE], nullptr, w->blocks, s1, true);
         ftcs(w, AGB_FIELD_TEMPERATURE, w->tp.t_coeff, s1);
     }
     if (nsub > 0) mark(w, AGB_SECTION_THERMAL, 1, s1);
@@ -374,7 +374,7 @@ void tick_once(agb_world* w, cudaStream_t s) {
     cudaStreamWaitEvent(s3, w->ev[3], 0);
     if (nsub > 0) {
         mark(w, AGB_SECTION_T_DIFFUSE, 0, s3);
-        launch_flush_by_cells(w->S, w->c.g[AGB_FIELD_TEMPERATURE], nullptr, w->blocks, s3);
+        launch_flush_by_cells(w->S, w->c.g[AGB_FIELD_TEMPERATURE], nullptr, w->blocks, s3, true);
         ftcs(w, AGB_FIELD_TEMPERATURE, w->tp.t_coeff, s3);
         mark(w, AGB_SECTION_T_DIFFUSE, 1, s3);
     }
