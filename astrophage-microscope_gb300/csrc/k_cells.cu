@@ -217,8 +217,13 @@ __device__ __forceinline__ int64_t irr_line(const GridDev& I, int axis, int64_t 
     return idx % plane;
 }
 
-// occlusion_stamp_kernel (emission.cu:17-27). Also records each cell's voxel so
-// the next emission stage can clear exactly these voxels.
+// occlusion_stamp_kernel (emission.cu:17-27). The deposit words are zero
+// before it (cleared by the previous emission stage) and every stamp is
+// positive, so exactly one cell per stamped voxel sees zero come back from its
+// add: that cell owns the voxel. Owners alone record the voxel (stamp_idx;
+// other cells record -1), mark its line and set its bit, so the next emission
+// stage clears each voxel once and the occlusion factor of each is computed
+// once, not once per cell (a cluster core holds dozens of cells per voxel).
 __device__ __forceinline__ void stamp_kernel_body(DevState* S, const Ctx& c, int32_t* stamp_idx, Blk blk) {
     const SoA v = S->cur;
     const int32_t n = S->count;
@@ -229,10 +234,12 @@ __device__ __forceinline__ void stamp_kernel_body(DevState* S, const Ctx& c, int
         int32_t rec = -1;
         if (f & AGB_FLAG_OCCUPIED) {
             const int64_t idx = grid_nearest(I, d2f(v.x[i]), d2f(v.y[i]), d2f(v.z[i]));
-            deposit_fixed(&I.deposit[idx], (f & AGB_FLAG_ALIVE) ? c.stamp_alive : c.stamp_dead);
-            rec = (int32_t)idx;
-            if (c.irr_marks) c.irr_marks[irr_line(I, c.light_axis, idx)] = 1;
-            if (c.irr_stamp_bits) atomicOr(&c.irr_stamp_bits[idx >> 5], 1u << (idx & 31));
+            const long long stamp = (f & AGB_FLAG_ALIVE) ? c.stamp_alive : c.stamp_dead;
+            if (atomicAdd(&I.deposit[idx], (unsigned long long)stamp) == 0ull) {
+                rec = (int32_t)idx;
+                if (c.irr_marks) c.irr_marks[irr_line(I, c.light_axis, idx)] = 1;
+                if (c.irr_stamp_bits) atomicOr(&c.irr_stamp_bits[idx >> 5], 1u << (idx & 31));
+            }
         }
         stamp_idx[i] = rec;
     }
@@ -250,11 +257,10 @@ __device__ __noinline__ double occlusion_fp64(unsigned long long dep, double sca
 }
 
 // column_transmittance (emission.cuh:43-47) of every stamped voxel, computed
-// once per cell, before the sweep (FP64 divisions in divergent sweep code
-// would cost a whole warp's FP64 issue time per stamped voxel). Voxels holding
-// one, two or three live cells or one dead cell take the factor from the
-// world's table (the same bits); others divide. Duplicate cells of a voxel
-// write the same value.
+// once per voxel by its owning cell, before the sweep (FP64 divisions in
+// divergent sweep code would cost a whole warp's FP64 issue time per stamped
+// voxel). Voxels holding one, two or three live cells or one dead cell take
+// the factor from the world's table (the same bits); others divide.
 __device__ __forceinline__ void occlusion_factor_kernel_body(DevState* S, const Ctx& c,
                                                              const int32_t* __restrict__ stamp_idx, double* factor,
                                                              Blk blk) {
