@@ -297,7 +297,11 @@ __device__ __forceinline__ bool stamped(const Ctx& c, const GridDev& I, int64_t 
 // sweep_kernel (emission.cu:37-53): one thread per line in sweep order. The
 // FP64 transmittance recurrence runs only at stamped voxels (an empty voxel's
 // factor is exactly 1), and the float output only changes there, so empty
-// voxels cost one load and one store.
+// voxels cost one load and one store. The line is walked in chunks of
+// SWEEP_PF voxels: the next chunk's stamp bits and this chunk's occlusion
+// factors are requested before this chunk's recurrence runs, so a chunk waits
+// on at most one memory round trip rather than one per chunk and one per
+// stamped voxel.
 constexpr int SWEEP_PF = 16;
 
 __device__ __forceinline__ void sweep_kernel_body(const Ctx& c, const double* __restrict__ factor, Blk blk) {
@@ -308,6 +312,8 @@ __device__ __forceinline__ void sweep_kernel_body(const Ctx& c, const double* __
     const int32_t len = axis == 0 ? nx : (axis == 1 ? ny : I.nz);
     const int64_t stride = axis == 0 ? 1 : (axis == 1 ? nx : plane);
     const int64_t lines = I.count / len;
+    // Voxel of step s along a line: first + step * s.
+    const int64_t step = c.light_sign > 0 ? stride : -stride;
     for (int64_t line = blk.x * (int64_t)blockDim.x + threadIdx.x; line < lines;
          line += (int64_t)blk.n * blockDim.x) {
         const uint8_t mark = c.irr_marks ? c.irr_marks[line] : 1;
@@ -317,24 +323,29 @@ __device__ __forceinline__ void sweep_kernel_body(const Ctx& c, const double* __
         if (axis == 0) base = line * nx;
         else if (axis == 1) base = (line % nx) + (line / nx) * plane;
         else base = line;
+        const int64_t first = c.light_sign > 0 ? base : base + stride * (len - 1);
         double t = 1.0;
         float cur = fa(d2f(c.source_d * t), c.ambient_irr);
+        bool next[SWEEP_PF];
+#pragma unroll
+        for (int u = 0; u < SWEEP_PF; ++u) next[u] = u < len && stamped(c, I, first + step * u);
         for (int32_t s0 = 0; s0 < len; s0 += SWEEP_PF) {
             bool raw[SWEEP_PF];
+            double fac[SWEEP_PF];
 #pragma unroll
             for (int u = 0; u < SWEEP_PF; ++u) {
-                const int32_t s = s0 + u;
-                const int32_t step = c.light_sign > 0 ? s : (len - 1 - s);
-                raw[u] = s < len && stamped(c, I, base + stride * step);
+                raw[u] = next[u];
+                const int32_t sn = s0 + SWEEP_PF + u;
+                next[u] = sn < len && stamped(c, I, first + step * sn);
+                fac[u] = raw[u] ? __ldg(&factor[first + step * (s0 + u)]) : 1.0;
             }
 #pragma unroll
             for (int u = 0; u < SWEEP_PF; ++u) {
                 const int32_t s = s0 + u;
                 if (s >= len) break;
-                const int32_t step = c.light_sign > 0 ? s : (len - 1 - s);
-                I.value[base + stride * step] = cur;
+                I.value[first + step * s] = cur;
                 if (raw[u]) {
-                    t *= __ldg(&factor[base + stride * step]);
+                    t *= fac[u];
                     cur = fa(d2f(c.source_d * t), c.ambient_irr);
                 }
             }
