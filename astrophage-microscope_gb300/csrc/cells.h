@@ -13,6 +13,7 @@ struct LifeBuffers {
     int32_t* tile_sums;      // per-tile totals for the two-level scan
     int32_t* src;            // compaction: source slot of each output slot
     unsigned long long* co2_demand;   // per CO2 voxel, fixed point (src/sim/world.cuh:108)
+    double* co2_want;        // per slot: the uptake the demand pass computed (the uptake pass reads it back)
 };
 
 // ---------------------------------------------------------------------------
@@ -105,12 +106,16 @@ __device__ __forceinline__ long long to_fixed_d(double v, double scale) {
 
 // One live cell's CO2 demand at (x, y, z) into the voxel's rationing word, as
 // a concentration (demand_kernel body, src/sim/lifecycle.cu:41-57); gv is the
-// voxel volume.
+// voxel volume. The cell's wanted uptake is kept in want[i]: the uptake pass
+// (uptake_kernel, lifecycle.cu:62-86) evaluates the same expression on the
+// same voxel value, so it reads it back instead of dividing again.
 __device__ __forceinline__ void co2_demand_cell(const GridDev& C2, const TickParams& p, float x, float y, float z,
-                                                unsigned long long* demand, double gv) {
+                                                unsigned long long* demand, double gv, double* want_out,
+                                                int32_t i) {
     const int64_t idx = grid_nearest(C2, x, y, z);
     const double want = __dmul_rn(co2_uptake_rate_d((double)C2.value[idx]), p.dt_bio);
-    if (want > 0.0) deposit_fixed(&demand[idx], to_fixed_d(__ddiv_rn(want, gv), C2.scale));
+    want_out[i] = want;
+    if (want > 0.0) deposit_fixed(&demand[idx], to_fixed_d(div_known(want, gv, C2.vol_inv), C2.scale));
 }
 
 void launch_thermal(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, cudaStream_t s);
@@ -138,7 +143,7 @@ void launch_forces(DevState* S, const Ctx& c, const TickParams& p, float* fx, fl
                    int32_t blocks, int lanes, cudaStream_t s);
 void launch_integrate(DevState* S, const Ctx& c, const TickParams& p, const float* fx, const float* fy,
                       const float* fz, int32_t blocks, const GridDev& co2, unsigned long long* demand,
-                      double gv, cudaStream_t s);
+                      double gv, double* want, cudaStream_t s);
 // Feeding (when `feed`), taxis (when `taxis`) and forces in one per-cell pass
 // with one neighbour walk: the same cell values as launch_feed, launch_taxis
 // and launch_forces in turn, with two kernels fewer on the tick's critical

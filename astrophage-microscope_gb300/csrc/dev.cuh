@@ -116,6 +116,8 @@ struct GridDev {
     float inv_scale_f;   // (float)(1 / scale)
     float inv_scale_lo;  // (float)(1 / scale - inv_scale_f): with inv_scale_f, 1 / scale to ~2^-48
     float scale_f;       // (float)scale
+    double vol_inv;      // 1 / (dx * dx * dz_eff), rounded once (div_known's reciprocal of the voxel volume)
+    double scale_inv;    // 1 / scale, rounded once
 };
 
 struct HashDev {
@@ -480,6 +482,30 @@ __host__ __device__ inline double occlusion_of(long long dep, double scale, doub
     const double area = (double)dep / scale;
     const double tr = 1.0 - area / face;
     return tr > 0.0 ? tr : 0.0;
+}
+
+// a / b rounded to nearest for a divisor known ahead, y = 1 / b rounded to
+// nearest (computed on the host): Markstein's correction step (P. Markstein,
+// "Computation of elementary functions on the IBM RISC System/6000
+// processor", IBM J. Res. Dev. 34(1), 1990): q = a y, r = a - b q by FMA,
+// q1 = q + r y by FMA. q1 is returned only where an exact test shows it is
+// the nearest double to a / b: q1 normal and not a power of two (its
+// neighbours an ulp away on both sides), h = b ulp(q1) / 2 formed exactly (b
+// times a power of two, a normal result), and |RN(a - b q1)| < h, which by the
+// monotonicity of rounding implies |a / b - q1| < ulp(q1) / 2. Anything else
+// (ties, binade edges, zero, extreme exponents, a stale y) takes the IEEE
+// division, so the result is the correctly rounded quotient in every case.
+static __device__ __noinline__ double div_known_ieee(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ double div_known(double a, double b, double y) {
+    const double q = __dmul_rn(a, y);
+    const double q1 = __fma_rn(__fma_rn(-b, q, a), y, q);
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(q1);
+    const int e = (int)((bits >> 52) & 0x7FFu);
+    if (e > 53 && e < 2047 && (bits & 0xFFFFFFFFFFFFFull) != 0ull) {
+        const double h = __dmul_rn(b, __longlong_as_double((long long)(e - 53) << 52));
+        if (h >= 2.2250738585072014e-308 && fabs(__fma_rn(-b, q1, a)) < h) return q1;
+    }
+    return div_known_ieee(a, b);
 }
 
 // Order-preserving map of a double onto uint64: compares of finite doubles

@@ -27,7 +27,7 @@ constexpr int STILE = ST * SITEMS;
 // integration (integrate_kernel), which has the moved cell at hand; the
 // per-stage lifecycle runs it here.
 __global__ void __launch_bounds__(256) demand_kernel(DevState* S, Ctx c, TickParams p,
-                                                     unsigned long long* demand, double gv) {
+                                                     unsigned long long* demand, double gv, double* want) {
     pdl_wait();
     const SoA v = S->cur;
     const int32_t n = S->count;
@@ -35,7 +35,7 @@ __global__ void __launch_bounds__(256) demand_kernel(DevState* S, Ctx c, TickPar
     AGB_FOR_CELLS(i, n) {
         const uint32_t f = v.flags[i];
         if (!(f & AGB_FLAG_OCCUPIED) || !(f & AGB_FLAG_ALIVE)) continue;
-        co2_demand_cell(C2, p, d2f(v.x[i]), d2f(v.y[i]), d2f(v.z[i]), demand, gv);
+        co2_demand_cell(C2, p, d2f(v.x[i]), d2f(v.y[i]), d2f(v.z[i]), demand, gv, want, i);
     }
 }
 
@@ -52,7 +52,8 @@ __device__ __forceinline__ bool ready_to_divide(const Ctx& c, const SoA& v, int3
 // deposit (lifecycle.cu:235) runs in the divide pass.
 __device__ __forceinline__ void uptake_mark_kernel_body(DevState* S, const Ctx& c, const TickParams& p,
                                                         const unsigned long long* __restrict__ demand, double gv,
-                                                        int32_t* divflag, Blk blk) {
+                                                        const double* __restrict__ want_in, int32_t* divflag,
+                                                        Blk blk) {
     const SoA v = S->cur;
     const int32_t n = S->count;
     const GridDev C2 = c.g[AGB_FIELD_CO2];
@@ -63,14 +64,14 @@ __device__ __forceinline__ void uptake_mark_kernel_body(DevState* S, const Ctx& 
             // uptake_kernel (lifecycle.cu:62-86) in FP64, the reference's order.
             const int64_t idx = grid_nearest(C2, d2f(v.x[i]), d2f(v.y[i]), d2f(v.z[i]));
             const double available = (double)C2.value[idx];
-            const double want = __dmul_rn(co2_uptake_rate_d(available), p.dt_bio);
+            const double want = want_in[i];                 // rate(available) * dt, from the demand pass
             if (want > 0.0) {
-                const double asked = __ddiv_rn((double)(long long)demand[idx], C2.scale);   // from_fixed
+                const double asked = div_known((double)(long long)demand[idx], C2.scale, C2.scale_inv);  // from_fixed
                 double taken = want;
                 if (asked > available && asked > 0.0) taken = __dmul_rn(want, __ddiv_rn(available, asked));
                 if (taken > 0.0) {
                     v.co2_held[i] = __dadd_rn(v.co2_held[i], taken);
-                    deposit_fixed(&C2.deposit[idx], to_fixed_d(__ddiv_rn(-taken, gv), C2.scale));
+                    deposit_fixed(&C2.deposit[idx], to_fixed_d(div_known(-taken, gv, C2.vol_inv), C2.scale));
                 }
             }
         }
@@ -100,9 +101,10 @@ __device__ __forceinline__ void uptake_mark_kernel_body(DevState* S, const Ctx& 
 
 __global__ void __launch_bounds__(256) uptake_mark_kernel(DevState* S, Ctx c, TickParams p,
                                                           const unsigned long long* __restrict__ demand,
-                                                          double gv, int32_t* divflag) {
+                                                          double gv, const double* __restrict__ want,
+                                                          int32_t* divflag) {
     pdl_wait();
-    uptake_mark_kernel_body(S, c, p, demand, gv, divflag, grid_blk());
+    uptake_mark_kernel_body(S, c, p, demand, gv, want, divflag, grid_blk());
 }
 
 // ---------------------------------------------------------------------------
@@ -612,7 +614,7 @@ void launch_compact_kernels(DevState* S, const LifeBuffers& b, int32_t capacity,
 }
 
 AGB_BATCHED_MB(uptake_mark_batch, 256, 4,
-            uptake_mark_kernel_body(a.S, a.c, a.p, a.demand, a.gv, a.life.flags, blk))
+            uptake_mark_kernel_body(a.S, a.c, a.p, a.demand, a.gv, a.life.co2_want, a.life.flags, blk))
 AGB_BATCHED_MB(divide_batch, 256, 4,
             divide_kernel_body(a.S, a.c, a.life.flags, a.life.prefix, a.arg, a.demand, blk))
 AGB_BATCHED(keep_batch, 256, keep_kernel_body(a.S, a.life.flags, blk))
@@ -654,8 +656,8 @@ void launch_lifecycle(DevState* S, const Ctx& c, const TickParams& p, const Life
     const GridDev& C2 = c.g[AGB_FIELD_CO2];
     unsigned long long* dem = C2.enabled ? b.co2_demand : nullptr;
     const double gv = C2.enabled ? C2.dx * C2.dx * C2.dz_eff : 0.0;
-    if (C2.enabled && !demand_done) launch_k(demand_kernel, blocks, 256, 0, s, S, c, p, dem, gv);
-    launch_k(uptake_mark_kernel, blocks, 256, 0, s, S, c, p, dem, gv, b.flags);
+    if (C2.enabled && !demand_done) launch_k(demand_kernel, blocks, 256, 0, s, S, c, p, dem, gv, b.co2_want);
+    launch_k(uptake_mark_kernel, blocks, 256, 0, s, S, c, p, dem, gv, (const double*)b.co2_want, b.flags);
     launch_scan(S, b, c.capacity, 0, s);
     launch_k(divide_kernel, blocks, 256, 0, s, S, c, b.flags, b.prefix, compaction_allowed ? 1 : 0, dem);
     // Compaction cannot run on this tick unless the host-side period allows it.

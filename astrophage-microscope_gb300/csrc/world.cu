@@ -423,7 +423,7 @@ void tick_once(agb_world* w, cudaStream_t s) {
     // books it.
     const bool fuse_demand = co2.enabled && !w->tau_active;
     launch_integrate(w->S, c, w->tp, w->fx, w->fy, w->fz, w->blocks, co2,
-                     fuse_demand ? w->life.co2_demand : nullptr, gv, s);
+                     fuse_demand ? w->life.co2_demand : nullptr, gv, w->life.co2_want, s);
     mark(w, AGB_SECTION_INTEGRATE, 1, s);
     mark(w, AGB_SECTION_LIFECYCLE, 0, s);
     stage_predation(w, s);
@@ -812,6 +812,8 @@ agb_status agb_world_create(const agb_world_desc* d, agb_world** out) {
         g.inv_scale_f = (float)(1.0 / gd.deposit_scale);
         g.inv_scale_lo = (float)(1.0 / gd.deposit_scale - (double)g.inv_scale_f);
         g.scale_f = (float)g.scale;
+        g.vol_inv = 1.0 / (g.dx * g.dx * g.dz_eff);
+        g.scale_inv = 1.0 / g.scale;
         for (int k = 0; k < 6; ++k) { w->gbc[f][k] = gd.bc[k]; w->gface[f][k] = (float)gd.face_value[k]; }
         w->grobin[f] = (float)(g.dx * AGB_AIR_CONVECTION_H / AGB_WATER_CONDUCTIVITY);
         for (int b = 0; b < 2; ++b)
@@ -875,7 +877,7 @@ agb_status agb_world_create(const agb_world_desc* d, agb_world** out) {
     const int32_t stiles = (cap + 1023) / 1024;
     ok = ok && dalloc(w, &w->life.flags, 4 * n) == cudaSuccess && dalloc(w, &w->life.prefix, 4 * n) == cudaSuccess &&
          dalloc(w, &w->life.tile_sums, 4 * (size_t)stiles) == cudaSuccess &&
-         dalloc(w, &w->life.src, 4 * n) == cudaSuccess &&
+         dalloc(w, &w->life.src, 4 * n) == cudaSuccess && dalloc(w, &w->life.co2_want, 8 * n) == cudaSuccess &&
          dalloc(w, &w->stamp_idx, 4 * n) == cudaSuccess && dalloc(w, &w->fx, 4 * n) == cudaSuccess &&
          dalloc(w, &w->fy, 4 * n) == cudaSuccess && dalloc(w, &w->fz, 4 * n) == cudaSuccess &&
          dalloc(w, &w->acc, 8 * 12) == cudaSuccess && dalloc(w, &w->S, sizeof(DevState)) == cudaSuccess;
