@@ -940,7 +940,7 @@ __device__ __forceinline__ void taxis_cell(const SoA& v, const TickParams& p, in
     const double irr = (double)v.irradiance[i];
     const double co2 = (double)v.co2_local[i];
     const double energy = v.energy[i];
-    const double charge = __ddiv_rn(energy, AGB_CELL_ENERGY_MAX);
+    const double charge = div_known(energy, AGB_CELL_ENERGY_MAX, 1.0 / AGB_CELL_ENERGY_MAX);
     const bool dark = irr < AGB_TAXIS_DARK_THRESHOLD, co2_here = co2 > 0.0;   // taxis.cuh:56-62
     int state = 0;                                             // 0 idle, 1 feed, 2 breed
     if (!(dark && !co2_here)) {
@@ -972,7 +972,7 @@ __device__ __forceinline__ void taxis_cell(const SoA& v, const TickParams& p, in
     v.dir_z[i] = (float)(-nh.z);
     double pw = 0.0;                                           // taxis_emit_power, taxis.cuh:136-141
     if (energy > 0.0) {
-        const double avail = p.dt > 0.0 ? __ddiv_rn(energy, p.dt) : 0.0;
+        const double avail = p.dt > 0.0 ? div_known(energy, p.dt, p.dt_inv) : 0.0;
         pw = p.max_emit_power < avail ? p.max_emit_power : avail;
     }
     v.emit_power[i] = (float)pw;

@@ -164,6 +164,7 @@ agb_status compute_tick_params(agb_world* w) {
     TickParams& p = w->tp;
     const Ctx& c = w->c;
     p.dt = AGB_DT_PHYSICS * w->physics_rate;
+    p.dt_inv = 1.0 / p.dt;
     p.dtf = (float)p.dt;
     p.k_contact = (float)(AGB_CONTACT_STIFFNESS / w->physics_rate);
     p.k_contact64 = AGB_CONTACT_STIFFNESS / w->physics_rate;

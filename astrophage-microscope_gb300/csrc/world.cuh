@@ -61,6 +61,7 @@ struct Ctx {
 // Per-tick scalars derived from the clock.
 struct TickParams {
     double dt;                  // DT_PHYSICS * physics_rate
+    double dt_inv;              // 1 / dt, rounded once (div_known)
     float dtf;
     float k_contact;            // CONTACT_STIFFNESS / physics_rate
     double k_contact64;
