@@ -298,10 +298,13 @@ __device__ __forceinline__ bool stamped(const Ctx& c, const GridDev& I, int64_t 
 // FP64 transmittance recurrence runs only at stamped voxels (an empty voxel's
 // factor is exactly 1), and the float output only changes there, so empty
 // voxels cost one load and one store. The line is walked in chunks of
-// SWEEP_PF voxels: the next chunk's stamp bits and this chunk's occlusion
-// factors are requested before this chunk's recurrence runs, so a chunk waits
-// on at most one memory round trip rather than one per chunk and one per
-// stamped voxel.
+// SWEEP_PF voxels. The next chunk's stamp-bitmap words are loaded
+// unconditionally (the step clamped to the line, so every address is in
+// bounds) into registers while this chunk is written, and this chunk's
+// occlusion factors are requested before its recurrence runs, so a chunk waits
+// on at most one memory round trip. A bitmap word serves a warp's 32
+// neighbouring lines at once along y and z. (The bitmap exists whenever the
+// irradiance grid does.)
 constexpr int SWEEP_PF = 16;
 
 __device__ __forceinline__ void sweep_kernel_body(const Ctx& c, const double* __restrict__ factor, Blk blk) {
@@ -314,6 +317,7 @@ __device__ __forceinline__ void sweep_kernel_body(const Ctx& c, const double* __
     const int64_t lines = I.count / len;
     // Voxel of step s along a line: first + step * s.
     const int64_t step = c.light_sign > 0 ? stride : -stride;
+    const uint32_t* __restrict__ bits = c.irr_stamp_bits;
     for (int64_t line = blk.x * (int64_t)blockDim.x + threadIdx.x; line < lines;
          line += (int64_t)blk.n * blockDim.x) {
         const uint8_t mark = c.irr_marks ? c.irr_marks[line] : 1;
@@ -326,19 +330,21 @@ __device__ __forceinline__ void sweep_kernel_body(const Ctx& c, const double* __
         const int64_t first = c.light_sign > 0 ? base : base + stride * (len - 1);
         double t = 1.0;
         float cur = fa(d2f(c.source_d * t), c.ambient_irr);
-        bool next[SWEEP_PF];
+        uint32_t next[SWEEP_PF];                           // stamp-bitmap word of each step of the next chunk
 #pragma unroll
-        for (int u = 0; u < SWEEP_PF; ++u) next[u] = u < len && stamped(c, I, first + step * u);
+        for (int u = 0; u < SWEEP_PF; ++u) next[u] = __ldg(&bits[(first + step * (u < len ? u : len - 1)) >> 5]);
         for (int32_t s0 = 0; s0 < len; s0 += SWEEP_PF) {
             bool raw[SWEEP_PF];
-            double fac[SWEEP_PF];
 #pragma unroll
             for (int u = 0; u < SWEEP_PF; ++u) {
-                raw[u] = next[u];
-                const int32_t sn = s0 + SWEEP_PF + u;
-                next[u] = sn < len && stamped(c, I, first + step * sn);
-                fac[u] = raw[u] ? __ldg(&factor[first + step * (s0 + u)]) : 1.0;
+                const int32_t s = s0 + u;
+                raw[u] = s < len && ((next[u] >> ((first + step * s) & 31)) & 1u) != 0u;
+                const int32_t sn = s + SWEEP_PF;
+                next[u] = __ldg(&bits[(first + step * (sn < len ? sn : len - 1)) >> 5]);
             }
+            double fac[SWEEP_PF];
+#pragma unroll
+            for (int u = 0; u < SWEEP_PF; ++u) fac[u] = raw[u] ? __ldg(&factor[first + step * (s0 + u)]) : 1.0;
 #pragma unroll
             for (int u = 0; u < SWEEP_PF; ++u) {
                 const int32_t s = s0 + u;
@@ -353,7 +359,7 @@ __device__ __forceinline__ void sweep_kernel_body(const Ctx& c, const double* __
     }
 }
 
-__global__ void __launch_bounds__(128) sweep_kernel(Ctx c, const double* __restrict__ factor) {
+__global__ void __launch_bounds__(128, 4) sweep_kernel(Ctx c, const double* __restrict__ factor) {
     pdl_wait();
     sweep_kernel_body(c, factor, grid_blk());
 }
@@ -1118,7 +1124,7 @@ AGB_BATCHED(clear_stamps_batch, 256, clear_stamps_kernel_body(a.S, a.c, a.stamp_
 AGB_BATCHED(stamp_batch, 256, stamp_kernel_body(a.S, a.c, a.stamp_idx, blk))
 AGB_BATCHED(occlusion_factor_batch, 256, occlusion_factor_kernel_body(a.S, a.c, a.stamp_idx, a.factor, blk))
 AGB_BATCHED(sweep_rows_batch, 256, sweep_rows_kernel_body(a.c, a.factor, blk))
-AGB_BATCHED(sweep_lines_batch, 128, sweep_kernel_body(a.c, a.factor, blk))
+AGB_BATCHED_MB(sweep_lines_batch, 128, 4, sweep_kernel_body(a.c, a.factor, blk))
 AGB_BATCHED_MB(cell_step_batch, 256, 4,
             cell_step_kernel_body<1>(a.S, a.c, a.p, a.arg & 1, (a.arg >> 1) & 1, a.fx, a.fy, a.fz, blk))
 AGB_BATCHED_MB(integrate_batch, 256, 4,
