@@ -260,6 +260,7 @@ void plan_tick(agb_batch* b, StagedPlan& P) {
         for (size_t i = 0; i < n; ++i) {
             if (k >= nsub[i]) continue;
             ChamberArgs a = chamber_args(W[i]);
+            a.arg = k == 0 ? 1 : 0;                      // the first substep records the cells' voxels
             th.push_back(a);
             a.g = W[i]->c.g[AGB_FIELD_TEMPERATURE];
             const bool last = k + 1 == nsub[i];

@@ -118,7 +118,8 @@ __device__ __forceinline__ void co2_demand_cell(const GridDev& C2, const TickPar
     if (want > 0.0) deposit_fixed(&demand[idx], to_fixed_d(div_known(want, gv, C2.vol_inv), C2.scale));
 }
 
-void launch_thermal(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, cudaStream_t s);
+// `first`: the tick's first thermal substep (it records each cell's voxel in c.t_vox).
+void launch_thermal(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, bool first, cudaStream_t s);
 // flash_step (src/sim/flash.cu:59-67) while the spin-drive flash is armed.
 void launch_flash(DevState* S, double dt, double power, unsigned long long* accum, int32_t blocks, cudaStream_t s);
 // `lanes` (1, 2, 4 or 8) threads share each cell's neighbour walk in the

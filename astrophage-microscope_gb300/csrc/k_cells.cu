@@ -134,7 +134,10 @@ __device__ __forceinline__ void rec_delta(const HashDev& h, const float4& a, int
 // ---------------------------------------------------------------------------
 // Thermal substep (thermal_kernel, src/sim/thermal.cu:19-71)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void thermal_kernel_body(DevState* S, const Ctx& c, const TickParams& p, Blk blk) {
+// `first`: the tick's first substep, which finds each cell's voxel from its
+// position and keeps it in c.t_vox; the later substeps read it back.
+__device__ __forceinline__ void thermal_kernel_body(DevState* S, const Ctx& c, const TickParams& p, bool first,
+                                                    Blk blk) {
     const SoA v = S->cur;
     const int32_t n = S->count;
     const GridDev T = c.g[AGB_FIELD_TEMPERATURE];
@@ -142,7 +145,13 @@ __device__ __forceinline__ void thermal_kernel_body(DevState* S, const Ctx& c, c
     AGB_FOR_CELLS_B(i, blk, n) {
         const uint32_t flags = v.flags[i];
         if (!(flags & AGB_FLAG_OCCUPIED)) continue;
-        const int64_t idx = grid_nearest(T, d2f(v.x[i]), d2f(v.y[i]), d2f(v.z[i]));
+        int64_t idx;
+        if (first || !c.t_vox) {
+            idx = grid_nearest(T, d2f(v.x[i]), d2f(v.y[i]), d2f(v.z[i]));
+            if (c.t_vox) c.t_vox[i] = (int32_t)idx;
+        } else {
+            idx = c.t_vox[i];
+        }
         const float t_grid = T.value[idx];
         bool awake = (flags & AGB_FLAG_AWAKE) != 0u;
         uint32_t nf = flags;
@@ -181,9 +190,9 @@ __device__ __forceinline__ void thermal_kernel_body(DevState* S, const Ctx& c, c
     if (__syncthreads_or(deposited) && threadIdx.x == 0) S->t_deposited = 1u;
 }
 
-__global__ void __launch_bounds__(256) thermal_kernel(DevState* S, Ctx c, TickParams p) {
+__global__ void __launch_bounds__(256) thermal_kernel(DevState* S, Ctx c, TickParams p, int first) {
     pdl_wait();
-    thermal_kernel_body(S, c, p, grid_blk());
+    thermal_kernel_body(S, c, p, first != 0, grid_blk());
 }
 
 // ---------------------------------------------------------------------------
@@ -1119,7 +1128,7 @@ __global__ void __launch_bounds__(256) cell_step_kernel(DevState* S, Ctx c, Tick
 // Batched launches of the per-cell stages (agb_batch): one grid over many
 // chambers, each block running the per-world body for its chamber.
 // ---------------------------------------------------------------------------
-AGB_BATCHED_MB(thermal_batch, 256, 4, thermal_kernel_body(a.S, a.c, a.p, blk))
+AGB_BATCHED_MB(thermal_batch, 256, 4, thermal_kernel_body(a.S, a.c, a.p, a.arg != 0, blk))
 AGB_BATCHED(clear_stamps_batch, 256, clear_stamps_kernel_body(a.S, a.c, a.stamp_idx, blk))
 AGB_BATCHED(stamp_batch, 256, stamp_kernel_body(a.S, a.c, a.stamp_idx, blk))
 AGB_BATCHED(occlusion_factor_batch, 256, occlusion_factor_kernel_body(a.S, a.c, a.stamp_idx, a.factor, blk))
@@ -1172,8 +1181,8 @@ void launch_taxis(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks
     launch_k(taxis_kernel, blocks, 256, 0, s, S, c, p);
 }
 
-void launch_thermal(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, cudaStream_t s) {
-    launch_k(thermal_kernel, blocks, 256, 0, s, S, c, p);
+void launch_thermal(DevState* S, const Ctx& c, const TickParams& p, int32_t blocks, bool first, cudaStream_t s) {
+    launch_k(thermal_kernel, blocks, 256, 0, s, S, c, p, first ? 1 : 0);
 }
 static int sm_count_of_device() {
     static int sms = 0;

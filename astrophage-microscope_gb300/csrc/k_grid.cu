@@ -347,14 +347,15 @@ __global__ void __launch_bounds__(256) ftcs3d_tma_batch(const FtcsChamber* __res
 // deposit word zero the dense flush it replaces changes nothing either. All
 // CTAs read the flag before any clears it: each counts itself done after its
 // read, and the last one to finish clears the flag and the count.
+// `vox`, when set, holds each cell's voxel in g (the thermal substeps' record).
 __device__ __forceinline__ void flush_by_cells_kernel_body(DevState* S, const GridDev& g, unsigned long long* demand,
-                                                           bool gated, Blk blk) {
+                                                           bool gated, const int32_t* vox, Blk blk) {
     if (gated && *(volatile const uint32_t*)&S->t_deposited == 0u) return;   // block-uniform
     const SoA v = S->cur;
     const int32_t n = S->count;
     AGB_FOR_CELLS_B(i, blk, n) {
         if (!(v.flags[i] & AGB_FLAG_OCCUPIED)) continue;
-        const int64_t idx = grid_nearest(g, (float)v.x[i], (float)v.y[i], (float)v.z[i]);
+        const int64_t idx = vox ? (int64_t)vox[i] : grid_nearest(g, (float)v.x[i], (float)v.y[i], (float)v.z[i]);
         const unsigned long long raw = atomicExch(&g.deposit[idx], 0ull);
         if (raw != 0ull)
             g.value[idx] = fa(g.value[idx], fixed_to_f((long long)raw, g.inv_scale_f, g.inv_scale_lo, g.scale));
@@ -368,12 +369,13 @@ __device__ __forceinline__ void flush_by_cells_kernel_body(DevState* S, const Gr
     }
 }
 
-__global__ void flush_by_cells_kernel(DevState* S, GridDev g, unsigned long long* demand, int gated) {
+__global__ void flush_by_cells_kernel(DevState* S, GridDev g, unsigned long long* demand, int gated,
+                                      const int32_t* vox) {
     pdl_wait();
-    flush_by_cells_kernel_body(S, g, demand, gated != 0, grid_blk());
+    flush_by_cells_kernel_body(S, g, demand, gated != 0, vox, grid_blk());
 }
 
-AGB_BATCHED(flush_batch, 256, flush_by_cells_kernel_body(a.S, a.g, nullptr, true, blk))
+AGB_BATCHED(flush_batch, 256, flush_by_cells_kernel_body(a.S, a.g, nullptr, true, a.c.t_vox, blk))
 
 }  // namespace
 
@@ -553,8 +555,8 @@ void launch_ftcs_batch(const FtcsChamber* tab, int32_t nch, int32_t nx, int32_t 
 }
 
 void launch_flush_by_cells(DevState* S, GridDev g, unsigned long long* demand, int32_t grid_blocks,
-                           cudaStream_t s, bool temperature) {
-    launch_k(flush_by_cells_kernel, grid_blocks, 256, 0, s, S, g, demand, temperature ? 1 : 0);
+                           cudaStream_t s, bool temperature, const int32_t* vox) {
+    launch_k(flush_by_cells_kernel, grid_blocks, 256, 0, s, S, g, demand, temperature ? 1 : 0, vox);
 }
 
 }  // namespace agb

@@ -56,8 +56,9 @@ void launch_ftcs_batch(const FtcsChamber* tab, int32_t nch, int32_t nx, int32_t 
 // src/fields/diffuse.cu:51-60, restricted to voxels that can hold a deposit).
 // `temperature`: the temperature grid's flush, skipped on the device when no
 // thermal substep has deposited heat since the previous one.
+// `vox`: each cell's voxel in g when known (the thermal substeps' record), else null.
 void launch_flush_by_cells(DevState* S, GridDev g, unsigned long long* demand_to_clear,
-                           int32_t grid_blocks, cudaStream_t s, bool temperature);
+                           int32_t grid_blocks, cudaStream_t s, bool temperature, const int32_t* vox);
 
 // Spatial hash (k_hash.cu)
 void hash_build(DevState* S, const HashDev& h, int32_t capacity, uint32_t* sort_keys_alt,

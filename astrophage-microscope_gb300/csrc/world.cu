@@ -266,8 +266,8 @@ void stage_thermal(agb_world* w, cudaStream_t s) {   // thermal_step, src/sim/th
     for (int32_t k = 0; k < w->tp.t_substeps; ++k) {
         refresh_grid_ptrs(w);
         if (w->d.thermal_enabled) {
-            launch_thermal(w->S, w->c, w->tp, w->blocks, s);
-            launch_flush_by_cells(w->S, w->c.g[AGB_FIELD_TEMPERATURE], nullptr, w->blocks, s, true);
+            launch_thermal(w->S, w->c, w->tp, w->blocks, k == 0, s);
+            launch_flush_by_cells(w->S, w->c.g[AGB_FIELD_TEMPERATURE], nullptr, w->blocks, s, true, w->c.t_vox);
         }
         ftcs(w, AGB_FIELD_TEMPERATURE, w->tp.t_coeff, s);
     }
@@ -365,9 +365,9 @@ void tick_once(agb_world* w, cudaStream_t s) {
     if (nsub > 0) mark(w, AGB_SECTION_THERMAL, 0, s1);
     for (int32_t k = 0; k < nsub; ++k) {
         refresh_grid_ptrs(w);
-        launch_thermal(w->S, w->c, w->tp, w->blocks, s1);
+        launch_thermal(w->S, w->c, w->tp, w->blocks, k == 0, s1);
         if (k + 1 == nsub) break;
-        launch_flush_by_cells(w->S, w->c.g[AGB_FIELD_TEMPERATURE], nullptr, w->blocks, s1, true);
+        launch_flush_by_cells(w->S, w->c.g[AGB_FIELD_TEMPERATURE], nullptr, w->blocks, s1, true, w->c.t_vox);
         ftcs(w, AGB_FIELD_TEMPERATURE, w->tp.t_coeff, s1);
     }
     if (nsub > 0) mark(w, AGB_SECTION_THERMAL, 1, s1);
@@ -375,7 +375,7 @@ void tick_once(agb_world* w, cudaStream_t s) {
     cudaStreamWaitEvent(s3, w->ev[3], 0);
     if (nsub > 0) {
         mark(w, AGB_SECTION_T_DIFFUSE, 0, s3);
-        launch_flush_by_cells(w->S, w->c.g[AGB_FIELD_TEMPERATURE], nullptr, w->blocks, s3, true);
+        launch_flush_by_cells(w->S, w->c.g[AGB_FIELD_TEMPERATURE], nullptr, w->blocks, s3, true, w->c.t_vox);
         ftcs(w, AGB_FIELD_TEMPERATURE, w->tp.t_coeff, s3);
         mark(w, AGB_SECTION_T_DIFFUSE, 1, s3);
     }
@@ -447,7 +447,7 @@ void tick_surrogate(agb_world* w, cudaStream_t s) {
     refresh_grid_ptrs(w);
     stage_hash(w, s);
     if (w->d.thermal_enabled && w->c.g[AGB_FIELD_TEMPERATURE].enabled)
-        for (int32_t k = 0; k < w->tp.t_substeps; ++k) launch_thermal(w->S, w->c, w->tp, w->blocks, s);
+        for (int32_t k = 0; k < w->tp.t_substeps; ++k) launch_thermal(w->S, w->c, w->tp, w->blocks, k == 0, s);
     if (w->d.emission_enabled) stage_emission(w, s);
     stage_flash_or_taxis(w, s);
     launch_motion(w->S, w->c, w->tp, w->fx, w->fy, w->fz, w->blocks, w->walk_lanes, s);
@@ -892,6 +892,9 @@ agb_status agb_world_create(const agb_world_desc* d, agb_world** out) {
         w->irr_bit_words = (I.count + 31) / 32;
         ok = ok && dalloc(w, &c.irr_stamp_bits, 4 * (size_t)w->irr_bit_words) == cudaSuccess;
     }
+    c.t_vox = nullptr;
+    if (c.g[AGB_FIELD_TEMPERATURE].enabled && c.g[AGB_FIELD_TEMPERATURE].count <= INT32_MAX)
+        ok = ok && dalloc(w, &c.t_vox, 4 * n) == cudaSuccess;
     for (cudaStream_t& st : w->side) ok = ok && cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess;
     for (cudaEvent_t& e : w->ev) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
     const int64_t co2n = c.g[AGB_FIELD_CO2].enabled ? c.g[AGB_FIELD_CO2].count : 1;

@@ -43,6 +43,8 @@ struct Ctx {
     // (mirrors deposit != 0), so the sweep tests bits instead of reading the
     // 8-byte deposit of every voxel.
     uint32_t* irr_stamp_bits;
+    int32_t* t_vox;          // per slot: its temperature voxel, written by a tick's first thermal substep and read
+                             // by the later substeps and flushes (cells do not move in between); null: recompute
     double face_area;
     long long stamp_alive, stamp_dead;   // fixed-point occlusion stamps
     // Occlusion factors of the commonest stamped voxels (one, two or three
