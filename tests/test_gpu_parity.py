@@ -38,6 +38,27 @@ def test_hash_bit_exact(name):
         assert np.array_equal(hg[k], ho[k]), what
 
 
+@pytest.mark.parametrize("capacity,cells", [(300000, 280000), (200000, 150000)])
+def test_hash_bit_exact_large(capacity, cells):
+    """The sort shapes of large worlds with 17-bit bucket keys: above 256k
+    slots three 8-bit passes over 2048-key tiles, below it two 9-bit passes
+    over 1024-key tiles, each with over a hundred tiles in the look-back;
+    keys, sorted order and ranges equal the oracle's, also on a second build
+    (which clears the first one's ranges)."""
+    d = agb.default_desc(capacity=capacity, seed=20260811)
+    orc = H.OracleWorld(d)
+    orc.spawn(agb.spawn(cells, charge_dist=agb.DIST_UNIFORM, charge_a=0.0, charge_b=0.2, awake=False))
+    gpu = agb.World(d)
+    P.copy_state(orc, gpu)
+    for _ in range(2):                           # a second build clears the first one's ranges
+        gpu.stage(agb.STAGE_HASH)
+        orc.stage(agb.STAGE_HASH)
+        hg, ho = gpu.export_hash(), orc.export_hash()
+        for k, what in enumerate(["dims", "keys_sorted", "vals_sorted", "bucket_start", "bucket_end"]):
+            assert np.array_equal(hg[k], ho[k]), what
+    assert gpu.counters()[3] == 0
+
+
 @pytest.mark.parametrize("name", NAMES)
 def test_each_stage_from_identical_state(name):
     """One stage at a time, each from the oracle's state after the previous one."""
