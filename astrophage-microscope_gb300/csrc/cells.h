@@ -14,6 +14,8 @@ struct LifeBuffers {
     int32_t* src;            // compaction: source slot of each output slot
     unsigned long long* co2_demand;   // per CO2 voxel, fixed point (src/sim/world.cuh:108)
     double* co2_want;        // per slot: the uptake the demand pass computed (the uptake pass reads it back)
+    int32_t* co2_vox;        // per slot: its CO2 voxel as the demand pass found it, -1 for a cell that booked no
+                             // demand (the uptake pass and the CO2 flush read it back); null: recompute
 };
 
 // ---------------------------------------------------------------------------
@@ -111,10 +113,11 @@ __device__ __forceinline__ long long to_fixed_d(double v, double scale) {
 // same voxel value, so it reads it back instead of dividing again.
 __device__ __forceinline__ void co2_demand_cell(const GridDev& C2, const TickParams& p, float x, float y, float z,
                                                 unsigned long long* demand, double gv, double* want_out,
-                                                int32_t i) {
+                                                int32_t* vox_out, int32_t i) {
     const int64_t idx = grid_nearest(C2, x, y, z);
     const double want = __dmul_rn(co2_uptake_rate_d((double)C2.value[idx]), p.dt_bio);
     want_out[i] = want;
+    if (vox_out) vox_out[i] = (int32_t)idx;
     if (want > 0.0) deposit_fixed(&demand[idx], to_fixed_d(div_known(want, gv, C2.vol_inv), C2.scale));
 }
 
@@ -144,7 +147,7 @@ void launch_forces(DevState* S, const Ctx& c, const TickParams& p, float* fx, fl
                    int32_t blocks, int lanes, cudaStream_t s);
 void launch_integrate(DevState* S, const Ctx& c, const TickParams& p, const float* fx, const float* fy,
                       const float* fz, int32_t blocks, const GridDev& co2, unsigned long long* demand,
-                      double gv, double* want, cudaStream_t s);
+                      double gv, double* want, int32_t* vox, cudaStream_t s);
 // Feeding (when `feed`), taxis (when `taxis`) and forces in one per-cell pass
 // with one neighbour walk: the same cell values as launch_feed, launch_taxis
 // and launch_forces in turn, with two kernels fewer on the tick's critical

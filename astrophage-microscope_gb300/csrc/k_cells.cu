@@ -824,7 +824,7 @@ __device__ __forceinline__ void integrate_kernel_body(DevState* S, const Ctx& c,
                                                       const float* __restrict__ fy_in,
                                                       const float* __restrict__ fz_in, const GridDev& co2,
                                                       unsigned long long* demand, double gv, double* want,
-                                                      Blk blk) {
+                                                      int32_t* vox, Blk blk) {
     const SoA v = S->cur;
     const int32_t n = S->count;
     AGB_FOR_CELLS_B(i, blk, n) {
@@ -894,8 +894,10 @@ __device__ __forceinline__ void integrate_kernel_body(DevState* S, const Ctx& c,
         v.x[i] = px; v.y[i] = py; v.z[i] = pz;
         v.vx[i] = f2d(ux); v.vy[i] = f2d(uy); v.vz[i] = f2d(uz);
         v.age_s[i] = v.age_s[i] + p.dtf;
-        if (demand && (nf & AGB_FLAG_ALIVE))
-            co2_demand_cell(co2, p, d2f(px), d2f(py), d2f(pz), demand, gv, want, i);
+        if (demand) {
+            if (nf & AGB_FLAG_ALIVE) co2_demand_cell(co2, p, d2f(px), d2f(py), d2f(pz), demand, gv, want, vox, i);
+            else if (vox) vox[i] = -1;
+        }
     }
 }
 
@@ -903,9 +905,10 @@ __global__ void __launch_bounds__(256) integrate_kernel(DevState* S, Ctx c, Tick
                                                         const float* __restrict__ fx_in,
                                                         const float* __restrict__ fy_in,
                                                         const float* __restrict__ fz_in, GridDev co2,
-                                                        unsigned long long* demand, double gv, double* want) {
+                                                        unsigned long long* demand, double gv, double* want,
+                                                        int32_t* vox) {
     pdl_wait();
-    integrate_kernel_body(S, c, p, fx_in, fy_in, fz_in, co2, demand, gv, want, grid_blk());
+    integrate_kernel_body(S, c, p, fx_in, fy_in, fz_in, co2, demand, gv, want, vox, grid_blk());
 }
 
 // ---------------------------------------------------------------------------
@@ -1137,7 +1140,8 @@ AGB_BATCHED_MB(sweep_lines_batch, 128, 4, sweep_kernel_body(a.c, a.factor, blk))
 AGB_BATCHED_MB(cell_step_batch, 256, 4,
             cell_step_kernel_body<1>(a.S, a.c, a.p, a.arg & 1, (a.arg >> 1) & 1, a.fx, a.fy, a.fz, blk))
 AGB_BATCHED_MB(integrate_batch, 256, 4,
-            integrate_kernel_body(a.S, a.c, a.p, a.fx, a.fy, a.fz, a.g, a.demand, a.gv, a.life.co2_want, blk))
+            integrate_kernel_body(a.S, a.c, a.p, a.fx, a.fy, a.fz, a.g, a.demand, a.gv, a.life.co2_want,
+                                  a.life.co2_vox, blk))
 
 }  // namespace
 
@@ -1262,13 +1266,13 @@ void launch_forces(DevState* S, const Ctx& c, const TickParams& p, float* fx, fl
 }
 void launch_integrate(DevState* S, const Ctx& c, const TickParams& p, const float* fx, const float* fy,
                       const float* fz, int32_t blocks, const GridDev& co2, unsigned long long* demand,
-                      double gv, double* want, cudaStream_t s) {
-    launch_k(integrate_kernel, blocks, 256, 0, s, S, c, p, fx, fy, fz, co2, demand, gv, want);
+                      double gv, double* want, int32_t* vox, cudaStream_t s) {
+    launch_k(integrate_kernel, blocks, 256, 0, s, S, c, p, fx, fy, fz, co2, demand, gv, want, vox);
 }
 void launch_motion(DevState* S, const Ctx& c, const TickParams& p, float* fx, float* fy, float* fz,
                    int32_t blocks, int lanes, cudaStream_t s) {
     launch_forces(S, c, p, fx, fy, fz, blocks, lanes, s);
-    launch_integrate(S, c, p, fx, fy, fz, blocks, c.g[AGB_FIELD_CO2], nullptr, 0.0, nullptr, s);
+    launch_integrate(S, c, p, fx, fy, fz, blocks, c.g[AGB_FIELD_CO2], nullptr, 0.0, nullptr, nullptr, s);
 }
 
 }  // namespace agb

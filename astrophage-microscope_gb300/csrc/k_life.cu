@@ -27,15 +27,20 @@ constexpr int STILE = ST * SITEMS;
 // integration (integrate_kernel), which has the moved cell at hand; the
 // per-stage lifecycle runs it here.
 __global__ void __launch_bounds__(256) demand_kernel(DevState* S, Ctx c, TickParams p,
-                                                     unsigned long long* demand, double gv, double* want) {
+                                                     unsigned long long* demand, double gv, double* want,
+                                                     int32_t* vox) {
     pdl_wait();
     const SoA v = S->cur;
     const int32_t n = S->count;
     const GridDev C2 = c.g[AGB_FIELD_CO2];
     AGB_FOR_CELLS(i, n) {
         const uint32_t f = v.flags[i];
-        if (!(f & AGB_FLAG_OCCUPIED) || !(f & AGB_FLAG_ALIVE)) continue;
-        co2_demand_cell(C2, p, d2f(v.x[i]), d2f(v.y[i]), d2f(v.z[i]), demand, gv, want, i);
+        if (!(f & AGB_FLAG_OCCUPIED)) continue;
+        if (!(f & AGB_FLAG_ALIVE)) {
+            if (vox) vox[i] = -1;
+            continue;
+        }
+        co2_demand_cell(C2, p, d2f(v.x[i]), d2f(v.y[i]), d2f(v.z[i]), demand, gv, want, vox, i);
     }
 }
 
@@ -52,7 +57,8 @@ __device__ __forceinline__ bool ready_to_divide(const Ctx& c, const SoA& v, int3
 // deposit (lifecycle.cu:235) runs in the divide pass.
 __device__ __forceinline__ void uptake_mark_kernel_body(DevState* S, const Ctx& c, const TickParams& p,
                                                         const unsigned long long* __restrict__ demand, double gv,
-                                                        const double* __restrict__ want_in, int32_t* divflag,
+                                                        const double* __restrict__ want_in,
+                                                        const int32_t* __restrict__ vox_in, int32_t* divflag,
                                                         Blk blk) {
     const SoA v = S->cur;
     const int32_t n = S->count;
@@ -62,7 +68,7 @@ __device__ __forceinline__ void uptake_mark_kernel_body(DevState* S, const Ctx& 
         uint32_t f = v.flags[i];
         if (demand && (f & AGB_FLAG_OCCUPIED) && (f & AGB_FLAG_ALIVE)) {
             // uptake_kernel (lifecycle.cu:62-86) in FP64, the reference's order.
-            const int64_t idx = grid_nearest(C2, d2f(v.x[i]), d2f(v.y[i]), d2f(v.z[i]));
+            const int64_t idx = vox_in ? (int64_t)vox_in[i] : grid_nearest(C2, d2f(v.x[i]), d2f(v.y[i]), d2f(v.z[i]));
             const double available = (double)C2.value[idx];
             const double want = want_in[i];                 // rate(available) * dt, from the demand pass
             if (want > 0.0) {
@@ -102,9 +108,9 @@ __device__ __forceinline__ void uptake_mark_kernel_body(DevState* S, const Ctx& 
 __global__ void __launch_bounds__(256) uptake_mark_kernel(DevState* S, Ctx c, TickParams p,
                                                           const unsigned long long* __restrict__ demand,
                                                           double gv, const double* __restrict__ want,
-                                                          int32_t* divflag) {
+                                                          const int32_t* __restrict__ vox, int32_t* divflag) {
     pdl_wait();
-    uptake_mark_kernel_body(S, c, p, demand, gv, want, divflag, grid_blk());
+    uptake_mark_kernel_body(S, c, p, demand, gv, want, vox, divflag, grid_blk());
 }
 
 // ---------------------------------------------------------------------------
@@ -280,15 +286,20 @@ __device__ void life_finalize(DevState* S, int32_t capacity, int32_t compaction_
 // before division moves it, and clears the rationing demand there.
 __device__ __forceinline__ void divide_kernel_body(DevState* S, const Ctx& c, const int32_t* __restrict__ divflag,
                                                    const int32_t* __restrict__ prefix, int32_t compaction_allowed,
-                                                   unsigned long long* demand, Blk blk) {
+                                                   unsigned long long* demand, const int32_t* __restrict__ vox,
+                                                   Blk blk) {
     const int32_t births_now = S->births;
     const SoA v = S->cur;
     const int32_t n = S->count;                 // base = old count
     const uint64_t first_id = S->next_id;
     const GridDev C2 = c.g[AGB_FIELD_CO2];
     AGB_FOR_CELLS_B(i, blk, (births_now > 0 || demand) ? n : 0) {
-        if (demand && (v.flags[i] & AGB_FLAG_OCCUPIED)) {
-            const int64_t idx = grid_nearest(C2, (float)v.x[i], (float)v.y[i], (float)v.z[i]);
+        // Only cells that booked demand this tick can have left a deposit or a
+        // demand word, so the cells the demand pass marked -1 have nothing to fold.
+        const int64_t idx = !demand || !(v.flags[i] & AGB_FLAG_OCCUPIED) ? -1
+                            : vox ? (int64_t)vox[i]
+                                  : grid_nearest(C2, (float)v.x[i], (float)v.y[i], (float)v.z[i]);
+        if (idx >= 0) {
             const unsigned long long raw = atomicExch(&C2.deposit[idx], 0ull);
             if (raw != 0ull) C2.value[idx] = fa(C2.value[idx], fixed_to_f((long long)raw, C2.inv_scale_f, C2.inv_scale_lo, C2.scale));
             demand[idx] = 0ull;
@@ -314,9 +325,10 @@ __device__ __forceinline__ void divide_kernel_body(DevState* S, const Ctx& c, co
 
 __global__ void __launch_bounds__(256) divide_kernel(DevState* S, Ctx c, const int32_t* __restrict__ divflag,
                                                      const int32_t* __restrict__ prefix,
-                                                     int32_t compaction_allowed, unsigned long long* demand) {
+                                                     int32_t compaction_allowed, unsigned long long* demand,
+                                                     const int32_t* __restrict__ vox) {
     pdl_wait();
-    divide_kernel_body(S, c, divflag, prefix, compaction_allowed, demand, grid_blk());
+    divide_kernel_body(S, c, divflag, prefix, compaction_allowed, demand, vox, grid_blk());
 }
 
 // The host bookkeeping of lifecycle_step (lifecycle.cu:250-293), on the device.
@@ -614,9 +626,10 @@ void launch_compact_kernels(DevState* S, const LifeBuffers& b, int32_t capacity,
 }
 
 AGB_BATCHED_MB(uptake_mark_batch, 256, 4,
-            uptake_mark_kernel_body(a.S, a.c, a.p, a.demand, a.gv, a.life.co2_want, a.life.flags, blk))
+            uptake_mark_kernel_body(a.S, a.c, a.p, a.demand, a.gv, a.life.co2_want, a.life.co2_vox, a.life.flags,
+                                    blk))
 AGB_BATCHED_MB(divide_batch, 256, 4,
-            divide_kernel_body(a.S, a.c, a.life.flags, a.life.prefix, a.arg, a.demand, blk))
+            divide_kernel_body(a.S, a.c, a.life.flags, a.life.prefix, a.arg, a.demand, a.life.co2_vox, blk))
 AGB_BATCHED(keep_batch, 256, keep_kernel_body(a.S, a.life.flags, blk))
 AGB_BATCHED(scatter_src_batch, 256, scatter_src_kernel_body(a.S, a.life.flags, a.life.prefix, a.life.src, blk))
 AGB_BATCHED(gather_batch, 256, gather_kernel_body(a.S, a.life.src, blk))
@@ -656,10 +669,13 @@ void launch_lifecycle(DevState* S, const Ctx& c, const TickParams& p, const Life
     const GridDev& C2 = c.g[AGB_FIELD_CO2];
     unsigned long long* dem = C2.enabled ? b.co2_demand : nullptr;
     const double gv = C2.enabled ? C2.dx * C2.dx * C2.dz_eff : 0.0;
-    if (C2.enabled && !demand_done) launch_k(demand_kernel, blocks, 256, 0, s, S, c, p, dem, gv, b.co2_want);
-    launch_k(uptake_mark_kernel, blocks, 256, 0, s, S, c, p, dem, gv, (const double*)b.co2_want, b.flags);
+    if (C2.enabled && !demand_done)
+        launch_k(demand_kernel, blocks, 256, 0, s, S, c, p, dem, gv, b.co2_want, b.co2_vox);
+    launch_k(uptake_mark_kernel, blocks, 256, 0, s, S, c, p, dem, gv, (const double*)b.co2_want,
+             (const int32_t*)b.co2_vox, b.flags);
     launch_scan(S, b, c.capacity, 0, s);
-    launch_k(divide_kernel, blocks, 256, 0, s, S, c, b.flags, b.prefix, compaction_allowed ? 1 : 0, dem);
+    launch_k(divide_kernel, blocks, 256, 0, s, S, c, b.flags, b.prefix, compaction_allowed ? 1 : 0, dem,
+             (const int32_t*)b.co2_vox);
     // Compaction cannot run on this tick unless the host-side period allows it.
     if (compaction_allowed) launch_compact_kernels(S, b, c.capacity, blocks, s);
 }

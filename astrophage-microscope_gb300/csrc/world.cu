@@ -424,7 +424,7 @@ void tick_once(agb_world* w, cudaStream_t s) {
     // books it.
     const bool fuse_demand = co2.enabled && !w->tau_active;
     launch_integrate(w->S, c, w->tp, w->fx, w->fy, w->fz, w->blocks, co2,
-                     fuse_demand ? w->life.co2_demand : nullptr, gv, w->life.co2_want, s);
+                     fuse_demand ? w->life.co2_demand : nullptr, gv, w->life.co2_want, w->life.co2_vox, s);
     mark(w, AGB_SECTION_INTEGRATE, 1, s);
     mark(w, AGB_SECTION_LIFECYCLE, 0, s);
     stage_predation(w, s);
@@ -895,6 +895,9 @@ agb_status agb_world_create(const agb_world_desc* d, agb_world** out) {
     c.t_vox = nullptr;
     if (c.g[AGB_FIELD_TEMPERATURE].enabled && c.g[AGB_FIELD_TEMPERATURE].count <= INT32_MAX)
         ok = ok && dalloc(w, &c.t_vox, 4 * n) == cudaSuccess;
+    w->life.co2_vox = nullptr;
+    if (c.g[AGB_FIELD_CO2].enabled && c.g[AGB_FIELD_CO2].count <= INT32_MAX)
+        ok = ok && dalloc(w, &w->life.co2_vox, 4 * n) == cudaSuccess;
     for (cudaStream_t& st : w->side) ok = ok && cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess;
     for (cudaEvent_t& e : w->ev) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
     const int64_t co2n = c.g[AGB_FIELD_CO2].enabled ? c.g[AGB_FIELD_CO2].count : 1;
