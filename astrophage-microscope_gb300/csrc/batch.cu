@@ -339,7 +339,13 @@ void plan_tick(agb_batch* b, StagedPlan& P) {
             maxp = std::max(maxp, a.passes);
         }
         P.stage(0, BStage::HashClear, hc);
-        P.stage(0, BStage::KeyHist, kh);
+        {
+            // Fewer, longer-running blocks for keys and digit counts: each block
+            // folds its shared-memory counts into the chamber's histograms once.
+            std::vector<ChamberArgs> kq = kh;
+            for (ChamberArgs& a : kq) a.nblk = std::max(1, (a.nblk + 3) / 4);
+            P.stage(0, BStage::KeyHist, kq);
+        }
         for (int32_t p = 0; p < maxp; ++p) {
             std::vector<ChamberArgs> r4, r49, r8;
             for (size_t i = 0; i < n; ++i) {
