@@ -178,7 +178,12 @@ ChamberArgs chamber_args(agb_world* w) {
     a.fx = w->fx; a.fy = w->fy; a.fz = w->fz;
     a.life = w->life;
     a.kalt = w->kalt; a.valt = w->valt; a.hist = w->hist;
-    a.nblk = w->blocks;
+    // A quarter of the blocks a world launches on its own: a world sizes its
+    // grid by capacity (twice the cells here), and a batched block first
+    // looks up its chamber and that chamber's arguments in global memory, a
+    // cost that longer grid-stride loops spread over more cells (per step:
+    // 3.50 ms with every block, 3.15 with a quarter, 3.22 with an eighth).
+    a.nblk = std::max(1, (w->blocks + 3) / 4);
     const GridDev& co2 = w->c.g[AGB_FIELD_CO2];
     a.demand = co2.enabled ? w->life.co2_demand : nullptr;
     a.gv = co2.enabled ? co2.dx * co2.dx * co2.dz_eff : 0.0;
@@ -339,13 +344,7 @@ void plan_tick(agb_batch* b, StagedPlan& P) {
             maxp = std::max(maxp, a.passes);
         }
         P.stage(0, BStage::HashClear, hc);
-        {
-            // Fewer, longer-running blocks for keys and digit counts: each block
-            // folds its shared-memory counts into the chamber's histograms once.
-            std::vector<ChamberArgs> kq = kh;
-            for (ChamberArgs& a : kq) a.nblk = std::max(1, (a.nblk + 3) / 4);
-            P.stage(0, BStage::KeyHist, kq);
-        }
+        P.stage(0, BStage::KeyHist, kh);
         for (int32_t p = 0; p < maxp; ++p) {
             std::vector<ChamberArgs> r4, r49, r8;
             for (size_t i = 0; i < n; ++i) {
