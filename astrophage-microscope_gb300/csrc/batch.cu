@@ -150,8 +150,19 @@ struct StagedPlan {
         o.kind = OpKind::Wait; o.stream = stream; o.event = ev;
         ops.push_back(o);
     }
-    // One batched stage over the chambers of `args` (each with its nblk).
-    void stage(int32_t stream, BStage st, const std::vector<ChamberArgs>& args, int32_t arg = 0) {
+    // One batched stage over the chambers of `args` (each with its nblk). The
+    // light per-cell stages (a few loads and stores per cell) take half the
+    // blocks again: 3.11 -> 3.07 ms per batch64 step.
+    void stage(int32_t stream, BStage st, const std::vector<ChamberArgs>& args_in, int32_t arg = 0) {
+        std::vector<ChamberArgs> args = args_in;
+        switch (st) {
+            case BStage::Thermal: case BStage::Flush: case BStage::ClearStamps: case BStage::Stamp:
+            case BStage::Occlusion: case BStage::KeyHist: case BStage::Ranges: case BStage::Keep:
+            case BStage::ScatterSrc: case BStage::Gather:
+                for (ChamberArgs& a : args) a.nblk = std::max(1, (a.nblk + 1) / 2);
+                break;
+            default: break;
+        }
         std::vector<uint32_t> map;
         for (size_t k = 0; k < args.size(); ++k)
             for (int32_t x = 0; x < args[k].nblk; ++x) map.push_back(((uint32_t)k << 16) | (uint32_t)x);
